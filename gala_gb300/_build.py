@@ -1,0 +1,84 @@
+"""Build the CUDA library ``gala_gb300/_build/libgala_gb300.so`` for sm_103a.
+
+The library is compiled in-tree with nvcc (one process per translation unit, in
+parallel) and linked with the static CUDA runtime.  FP64 translation units that
+reproduce gala's arithmetic are compiled with ``-fmad=false`` so that no
+multiply-add is contracted; the FP32 / tensor-core units keep contraction on.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+CSRC = PKG / "csrc"
+OUT = PKG / "_build"
+LIB = OUT / "libgala_gb300.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+
+# translation unit -> extra flags
+UNITS = {
+    "gx_host.cu": ["-fmad=false"],
+    "gx_fixed.cu": ["-fmad=false"],
+    "gx_dop853.cu": ["-fmad=false"],
+}
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc")
+    if exe:
+        return exe
+    cand = "/usr/local/cuda/bin/nvcc"
+    if os.path.exists(cand):
+        return cand
+    raise RuntimeError("nvcc not found: the CUDA toolkit is required to build gala_gb300")
+
+
+def _sources_newer(target: Path) -> bool:
+    if not target.exists():
+        return True
+    t = target.stat().st_mtime
+    deps = list(CSRC.glob("*")) + [PKG.parent / "include" / "gala_gb300.h", Path(__file__)]
+    return any(p.stat().st_mtime > t for p in deps if p.exists())
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile every CUDA translation unit and link the shared library."""
+    if not force and not _sources_newer(LIB):
+        return LIB
+    OUT.mkdir(exist_ok=True)
+    cc = nvcc()
+
+    def compile_unit(item):
+        name, extra = item
+        obj = OUT / (Path(name).stem + ".o")
+        cmd = [cc, *ARCH, *COMMON, *extra, "-c", str(CSRC / name), "-o", str(obj)]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {name}:\n{r.stdout}\n{r.stderr}")
+        if verbose:
+            print(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(compile_unit, UNITS.items()))
+    tmp = OUT / "libgala_gb300.so.tmp"
+    cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc link failed:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    import sys
+
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

@@ -1,0 +1,391 @@
+// gx_dop853.cu -- FP64 DOP853 with gala's batch semantics, one CTA per batch.
+//
+// gala integrates `nbatch` orbits (default 100) as ONE ODE system of size
+// n = 6 * nb: one shared step size, one RMS error norm over all 6 * nb
+// components, one accept/reject decision, one dense-output grid
+// (dop853.pyx:228-245 -> dop853_helper :90-193 -> dopcor, dopri/dop853.cpp:89-650).
+// Here a batch is one CTA and each thread owns one orbit's six components:
+//   * the twelve stages, FSAL evaluation and the three dense-output stages are
+//     evaluated per thread in registers with gala's expression order;
+//   * the error norms (err, err2) and the stiffness sums (stnum, stden) are
+//     CTA-wide sums: a fixed-order warp butterfly plus an ordered sum over warps,
+//     so the step-size sequence is deterministic run to run;
+//   * every scalar of the step-size controller (x, h, facold, reject, last,
+//     naccpt, ...) is computed identically by all threads from the same sums,
+//     so control flow stays uniform inside the CTA;
+//   * dense output (contd8_threadsafe, :869-904) is written directly into the
+//     (6, n_out, N) result for every requested time inside [xold, xold + h].
+// The loop is bounded by nmax like gala's; no thread ever waits on another CTA.
+#include "gx_host.h"
+#include "gx_scf.cuh"
+#include "gx_dop853_tableau.cuh"
+
+namespace gx {
+
+struct DopArgs {
+    double atol, rtol, dt_max;
+    int64_t nmax, nstiff;
+    int64_t ntimes, out_stride, n_out;
+    int32_t save_all, nbatch;
+};
+
+constexpr int DOP_MAX_WARPS = 32;
+
+// Deterministic CTA-wide sum of two values.  Every thread returns the same bits.
+__device__ __forceinline__ void block_sum2(double &a, double &b, double *red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+        red[wid] = a;
+        red[DOP_MAX_WARPS + wid] = b;
+    }
+    __syncthreads();
+    double sa = 0., sb = 0.;
+    for (int w = 0; w < nw; w++) {
+        sa += red[w];
+        sb += red[DOP_MAX_WARPS + w];
+    }
+    __syncthreads();
+    a = sa;
+    b = sb;
+}
+
+__device__ __forceinline__ double sign_d(double a, double b) { return (b < 0.0) ? -fabs(a) : fabs(a); }
+__device__ __forceinline__ double min_d(double a, double b) { return (a < b) ? a : b; }
+__device__ __forceinline__ double max_d(double a, double b) { return (a > b) ? a : b; }
+
+#define RHS(yin, kout)                                                   \
+    do {                                                                 \
+        if (active) {                                                    \
+            V6 a_;                                                       \
+            for (int c_ = 0; c_ < 6; c_++) a_.v[c_] = yin[c_];           \
+            const V6 r_ = rhs_call<SCF>(pot, fr, a_);                    \
+            for (int c_ = 0; c_ < 6; c_++) kout[c_] = r_.v[c_];          \
+        } else {                                                         \
+            for (int c_ = 0; c_ < 6; c_++) kout[c_] = 0.;                \
+        }                                                                \
+    } while (0)
+
+template <int MAXT, bool SCF>
+__global__ void __launch_bounds__(MAXT, 1)
+dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFrame fr, DopArgs A, const double *__restrict__ w0, int64_t n,
+              const double *__restrict__ t, double *__restrict__ out, int32_t *__restrict__ status,
+              int64_t *__restrict__ stats) {
+    using namespace dop;
+    __shared__ double red[2 * DOP_MAX_WARPS];
+
+    const int64_t b = blockIdx.x;
+    const int64_t i0 = b * A.nbatch;
+    const int nb = (int)((i0 + A.nbatch <= n) ? A.nbatch : n - i0);
+    const int j = threadIdx.x;
+    const bool active = j < nb;
+    const int nsys = 6 * nb;
+
+    double y[6], k1[6], k2[6], k3[6], k4[6], k5[6], k6[6], k7[6], k8[6], k9[6], k10[6], yy1[6];
+    for (int c = 0; c < 6; c++) y[c] = active ? w0[c * n + i0 + j] : 0.;
+
+    // dop853() front-end defaults with dop853_helper's arguments (dop853.pyx:157-182)
+    double x = t[0];
+    const double xend = t[A.ntimes - 1];
+    double h = t[1] - t[0];
+    double hmax = A.dt_max;
+    const double uround = 2.220446049250313e-16;
+    const double safe = 0.9, fac1 = 0.333, fac2 = 6.0, beta = 0.0;
+    int64_t nmax = A.nmax, nstiff = A.nstiff;
+    if (!nmax) nmax = 1000000;
+    if (!nstiff) nstiff = 1000;
+    else if (nstiff < 0) nstiff = nmax + 10;
+    if (hmax == 0.0) hmax = xend - x;
+
+    double facold = 1.0E-4;
+    const double expo1 = 1.0 / 8.0 - beta * 0.2;
+    const double facc1 = 1.0 / fac1, facc2 = 1.0 / fac2;
+    const double posneg = sign_d(1.0, xend - x);
+    const double atoli = A.atol, rtoli = A.rtol;
+    int last = 0, reject = 0, iasti = 0, nonsti = 0, idid = 0;
+    double hlamb = 0.0;
+    int64_t nfcn = 0, nstep = 0, naccpt = 0, nrejct = 0;
+    int64_t out_idx = 0, out_slot = 0;
+
+    RHS(y, k1);
+    hmax = fabs(hmax);
+    if (h == 0.0) {
+        // hinit (dop853.cpp:18-86), scalar tolerances, CTA-wide norms
+        double dnf = 0.0, dny = 0.0;
+        for (int c = 0; c < 6; c++) {
+            const double sk = atoli + rtoli * fabs(y[c]);
+            double sqr = k1[c] / sk;
+            dnf += active ? sqr * sqr : 0.;
+            sqr = y[c] / sk;
+            dny += active ? sqr * sqr : 0.;
+        }
+        block_sum2(dnf, dny, red);
+        double hh = ((dnf <= 1.0E-10) || (dny <= 1.0E-10)) ? 1.0E-6 : sqrt(dny / dnf) * 0.01;
+        hh = min_d(hh, hmax);
+        hh = sign_d(hh, posneg);
+        for (int c = 0; c < 6; c++) yy1[c] = y[c] + hh * k1[c];
+        RHS(yy1, k2);
+        double der2 = 0.0, unused = 0.0;
+        for (int c = 0; c < 6; c++) {
+            const double sk = atoli + rtoli * fabs(y[c]);
+            const double sqr = (k2[c] - k1[c]) / sk;
+            der2 += active ? sqr * sqr : 0.;
+        }
+        block_sum2(der2, unused, red);
+        der2 = sqrt(der2) / hh;
+        const double der12 = max_d(fabs(der2), sqrt(dnf));
+        const double h1 = (der12 <= 1.0E-15) ? max_d(1.0E-6, fabs(hh) * 1.0E-3) : pow(0.01 / der12, 1.0 / 8.0);
+        hh = min_d(100.0 * fabs(hh), min_d(h1, hmax));
+        h = sign_d(hh, posneg);
+    }
+    nfcn += 2;
+
+    for (;;) {
+        if (nstep > nmax) { idid = -2; break; }
+        if (0.1 * fabs(h) <= fabs(x) * uround) { idid = -3; break; }
+        if ((x + 1.01 * h - xend) * posneg > 0.0) {
+            h = xend - x;
+            last = 1;
+        }
+        const double xold = x, hout = h;
+        nstep++;
+
+        // the twelve stages (dop853.cpp:368-414)
+        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * a21 * k1[c];
+        RHS(yy1, k2);
+        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a31 * k1[c] + a32 * k2[c]);
+        RHS(yy1, k3);
+        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a41 * k1[c] + a43 * k3[c]);
+        RHS(yy1, k4);
+        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a51 * k1[c] + a53 * k3[c] + a54 * k4[c]);
+        RHS(yy1, k5);
+        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a61 * k1[c] + a64 * k4[c] + a65 * k5[c]);
+        RHS(yy1, k6);
+        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a71 * k1[c] + a74 * k4[c] + a75 * k5[c] + a76 * k6[c]);
+        RHS(yy1, k7);
+        for (int c = 0; c < 6; c++)
+            yy1[c] = y[c] + h * (a81 * k1[c] + a84 * k4[c] + a85 * k5[c] + a86 * k6[c] + a87 * k7[c]);
+        RHS(yy1, k8);
+        for (int c = 0; c < 6; c++)
+            yy1[c] = y[c] + h * (a91 * k1[c] + a94 * k4[c] + a95 * k5[c] + a96 * k6[c] + a97 * k7[c] + a98 * k8[c]);
+        RHS(yy1, k9);
+        for (int c = 0; c < 6; c++)
+            yy1[c] = y[c] + h * (a101 * k1[c] + a104 * k4[c] + a105 * k5[c] + a106 * k6[c] + a107 * k7[c] +
+                                 a108 * k8[c] + a109 * k9[c]);
+        RHS(yy1, k10);
+        for (int c = 0; c < 6; c++)
+            yy1[c] = y[c] + h * (a111 * k1[c] + a114 * k4[c] + a115 * k5[c] + a116 * k6[c] + a117 * k7[c] +
+                                 a118 * k8[c] + a119 * k9[c] + a1110 * k10[c]);
+        RHS(yy1, k2);
+        const double xph = x + h;
+        for (int c = 0; c < 6; c++)
+            yy1[c] = y[c] + h * (a121 * k1[c] + a124 * k4[c] + a125 * k5[c] + a126 * k6[c] + a127 * k7[c] +
+                                 a128 * k8[c] + a129 * k9[c] + a1210 * k10[c] + a1211 * k2[c]);
+        RHS(yy1, k3);
+        nfcn += 11;
+        for (int c = 0; c < 6; c++) {
+            k4[c] = b1 * k1[c] + b6 * k6[c] + b7 * k7[c] + b8 * k8[c] + b9 * k9[c] + b10 * k10[c] + b11 * k2[c] +
+                    b12 * k3[c];
+            k5[c] = y[c] + h * k4[c];
+        }
+
+        // error estimation (:416-444), summed over the whole batch
+        double err = 0.0, err2 = 0.0;
+        if (active) {
+            for (int c = 0; c < 6; c++) {
+                const double sk = atoli + rtoli * max_d(fabs(y[c]), fabs(k5[c]));
+                double erri = k4[c] - bhh1 * k1[c] - bhh2 * k9[c] - bhh3 * k3[c];
+                double sqr = erri / sk;
+                err2 += sqr * sqr;
+                erri = er1 * k1[c] + er6 * k6[c] + er7 * k7[c] + er8 * k8[c] + er9 * k9[c] + er10 * k10[c] +
+                       er11 * k2[c] + er12 * k3[c];
+                sqr = erri / sk;
+                err += sqr * sqr;
+            }
+        }
+        block_sum2(err, err2, red);
+        double deno = err + 0.01 * err2;
+        if (deno <= 0.0) deno = 1.0;
+        err = fabs(h) * err * sqrt(1.0 / (deno * (double)nsys));
+
+        // computation of hnew (:446-452)
+        const double fac11 = pow(err, expo1);
+        double fac = fac11 / pow(facold, beta);
+        fac = max_d(facc2, min_d(facc1, fac / safe));
+        double hnew = h / fac;
+
+        if (err <= 1.0) {
+            facold = max_d(err, 1.0E-4);
+            naccpt++;
+            RHS(k5, k4);
+            nfcn++;
+
+            // stiffness detection (:463-486); like gala, the first detection returns -4
+            if (!(naccpt % nstiff) || (iasti > 0)) {
+                double stnum = 0.0, stden = 0.0;
+                if (active) {
+                    for (int c = 0; c < 6; c++) {
+                        double sqr = k4[c] - k3[c];
+                        stnum += sqr * sqr;
+                        sqr = k5[c] - yy1[c];
+                        stden += sqr * sqr;
+                    }
+                }
+                block_sum2(stnum, stden, red);
+                if (stden > 0.0) hlamb = h * sqrt(stnum / stden);
+                if (hlamb > 6.1) {
+                    nonsti = 0;
+                    iasti++;
+                    idid = -4;
+                    break;
+                } else {
+                    nonsti++;
+                    if (nonsti == 6) iasti = 0;
+                }
+            }
+
+            if (A.save_all) {
+                // dense output preparation (:492-582)
+                double r5[6], r6[6], r7[6], r8[6];
+                for (int c = 0; c < 6; c++) {
+                    r5[c] = d41 * k1[c] + d46 * k6[c] + d47 * k7[c] + d48 * k8[c] + d49 * k9[c] + d410 * k10[c] +
+                            d411 * k2[c] + d412 * k3[c];
+                    r6[c] = d51 * k1[c] + d56 * k6[c] + d57 * k7[c] + d58 * k8[c] + d59 * k9[c] + d510 * k10[c] +
+                            d511 * k2[c] + d512 * k3[c];
+                    r7[c] = d61 * k1[c] + d66 * k6[c] + d67 * k7[c] + d68 * k8[c] + d69 * k9[c] + d610 * k10[c] +
+                            d611 * k2[c] + d612 * k3[c];
+                    r8[c] = d71 * k1[c] + d76 * k6[c] + d77 * k7[c] + d78 * k8[c] + d79 * k9[c] + d710 * k10[c] +
+                            d711 * k2[c] + d712 * k3[c];
+                }
+                for (int c = 0; c < 6; c++)
+                    yy1[c] = y[c] + h * (a141 * k1[c] + a147 * k7[c] + a148 * k8[c] + a149 * k9[c] +
+                                         a1410 * k10[c] + a1411 * k2[c] + a1412 * k3[c] + a1413 * k4[c]);
+                RHS(yy1, k10);
+                for (int c = 0; c < 6; c++)
+                    yy1[c] = y[c] + h * (a151 * k1[c] + a156 * k6[c] + a157 * k7[c] + a158 * k8[c] +
+                                         a1511 * k2[c] + a1512 * k3[c] + a1513 * k4[c] + a1514 * k10[c]);
+                RHS(yy1, k2);
+                for (int c = 0; c < 6; c++)
+                    yy1[c] = y[c] + h * (a161 * k1[c] + a166 * k6[c] + a167 * k7[c] + a168 * k8[c] +
+                                         a169 * k9[c] + a1613 * k4[c] + a1614 * k10[c] + a1615 * k2[c]);
+                RHS(yy1, k3);
+                nfcn += 3;
+                double r1[6], r2[6], r3[6], r4[6];
+                for (int c = 0; c < 6; c++) {
+                    r5[c] = h * (r5[c] + d413 * k4[c] + d414 * k10[c] + d415 * k2[c] + d416 * k3[c]);
+                    r6[c] = h * (r6[c] + d513 * k4[c] + d514 * k10[c] + d515 * k2[c] + d516 * k3[c]);
+                    r7[c] = h * (r7[c] + d613 * k4[c] + d614 * k10[c] + d615 * k2[c] + d616 * k3[c]);
+                    r8[c] = h * (r8[c] + d713 * k4[c] + d714 * k10[c] + d715 * k2[c] + d716 * k3[c]);
+                    r1[c] = y[c];
+                    const double ydiff = k5[c] - y[c];
+                    r2[c] = ydiff;
+                    const double bspl = h * k1[c] - ydiff;
+                    r3[c] = bspl;
+                    r4[c] = ydiff - h * k4[c] - bspl;
+                }
+
+                // every output time inside [xold, xold + hout] (:584-612)
+                const double x0 = xold, x1 = x0 + hout;
+                while (out_idx < A.ntimes) {
+                    const double t_out = t[out_idx];
+                    if (!((x0 <= t_out && t_out <= x1) || (x1 <= t_out && t_out <= x0))) break;
+                    if (out_idx % A.out_stride == 0) {
+                        const double s = (t_out - xold) / hout;
+                        const double s1 = 1.0 - s;
+                        if (active) {
+                            for (int c = 0; c < 6; c++) {
+                                const double v =
+                                    r1[c] + s * (r2[c] + s1 * (r3[c] + s * (r4[c] +
+                                                 s1 * (r5[c] + s * (r6[c] + s1 * (r7[c] + s * r8[c]))))));
+                                __stcs(&out[((int64_t)c * A.n_out + out_slot) * n + i0 + j], v);
+                            }
+                        }
+                        out_slot++;
+                    }
+                    out_idx++;
+                }
+            }
+
+            for (int c = 0; c < 6; c++) {
+                k1[c] = k4[c];
+                y[c] = k5[c];
+            }
+            x = xph;
+            if (last) { idid = 1; break; }
+            if (fabs(hnew) > hmax) hnew = posneg * hmax;
+            if (reject) hnew = posneg * min_d(fabs(hnew), fabs(h));
+            reject = 0;
+        } else {
+            hnew = h / min_d(facc1, fac11 / safe);
+            reject = 1;
+            if (naccpt >= 1) nrejct = nrejct + 1;
+            last = 0;
+        }
+        h = hnew;
+    }
+    (void)nonsti;
+
+    if (!A.save_all && active)
+        for (int c = 0; c < 6; c++) out[c * n + i0 + j] = y[c];
+    if (j == 0) {
+        status[b] = idid;
+        if (stats) {
+            stats[4 * b + 0] = nfcn;
+            stats[4 * b + 1] = nstep;
+            stats[4 * b + 2] = naccpt;
+            stats[4 * b + 3] = nrejct;
+        }
+    }
+}
+#undef RHS
+
+}  // namespace gx
+
+extern "C" int gx_dop853_integrate_hamiltonian(const gx_potential *pot, const gx_frame *frame, const double *w0,
+                                               int64_t n, const double *t, int64_t ntimes, double atol,
+                                               double rtol, int64_t nmax, double dt_max, int64_t nstiff,
+                                               int32_t save_all, int32_t nbatch, int64_t out_stride,
+                                               double *w_out, int32_t *status, int64_t *stats, void *stream) {
+    gx::DevPot dp;
+    gx::DevFrame df;
+    int rc = gx::pack_potential(pot, &dp);
+    if (rc) return rc;
+    rc = gx::pack_frame(frame, &df);
+    if (rc) return rc;
+    GX_CHECK_ARG(n >= 0, "n < 0");
+    GX_CHECK_ARG(ntimes >= 2, "ntimes must be >= 2 (got %lld)", (long long)ntimes);
+    GX_CHECK_ARG(nbatch >= 1 && nbatch <= 1024, "nbatch must be in [1, 1024] (got %d)", nbatch);
+    GX_CHECK_ARG(out_stride >= 1, "out_stride must be >= 1");
+    GX_CHECK_ARG(nmax >= 0, "nmax must be >= 0 (0 = gala's default 1e6)");
+    GX_CHECK_ARG(atol >= 0 && rtol >= 0, "tolerances must be non-negative");
+    if (n == 0) return GX_OK;
+    GX_CHECK_ARG(w0 && t && w_out && status, "NULL array");
+    gx::DopArgs A;
+    A.atol = atol;
+    A.rtol = rtol;
+    A.dt_max = dt_max;
+    A.nmax = nmax;
+    A.nstiff = nstiff;
+    A.ntimes = ntimes;
+    A.out_stride = out_stride;
+    A.n_out = (ntimes - 1) / out_stride + 1;
+    A.save_all = save_all ? 1 : 0;
+    A.nbatch = nbatch;
+    const int64_t nbatches = (n + nbatch - 1) / nbatch;
+    const int threads = ((nbatch + 31) / 32) * 32;
+    cudaStream_t st = gx::as_stream(stream);
+    const unsigned grid = (unsigned)nbatches;
+    if (threads <= 256 && !dp.has_scf)
+        gx::dop853_kernel<256, false><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
+    else if (threads <= 256)
+        gx::dop853_kernel<256, true><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
+    else if (!dp.has_scf)
+        gx::dop853_kernel<1024, false><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
+    else
+        gx::dop853_kernel<1024, true><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
+    return gx::check_launch("dop853");
+}

@@ -1,0 +1,214 @@
+// gx_host.cu -- descriptor packing, error reporting and the potential /
+// Hamiltonian evaluation entry points (gx_potential_value, gx_potential_gradient,
+// gx_potential_density, gx_hamiltonian_value, gx_hamiltonian_gradient).
+#include <cmath>
+
+#include "gx_host.h"
+#include "gx_scf.cuh"
+
+namespace gx {
+
+static thread_local char g_errmsg[512] = "";
+
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_errmsg, sizeof(g_errmsg), fmt, ap);
+    va_end(ap);
+}
+
+int expected_params(int type, const double *p, int64_t avail) {
+    switch (type) {
+    case GX_POT_NULL: return 1;
+    case GX_POT_KEPLER: return 2;
+    case GX_POT_HERNQUIST: return 3;
+    case GX_POT_PLUMMER: return 3;
+    case GX_POT_MIYAMOTONAGAI: return 4;
+    case GX_POT_SPHERICALNFW:
+    case GX_POT_FLATTENEDNFW:
+    case GX_POT_TRIAXIALNFW: return 6;
+    case GX_POT_SCF: {
+        if (avail < 5) return -1;
+        const double nmax = p[1], lmax = p[2];
+        if (!(nmax >= 0 && lmax >= 0 && nmax + 1 <= SCF_MAX_N && lmax + 1 <= SCF_MAX_L)) return -1;
+        const int n = (int)nmax, l = (int)lmax;
+        return 5 + 2 * (n + 1) * (l + 1) * (l + 1);
+    }
+    default: return -1;
+    }
+}
+
+int pack_potential(const gx_potential *pot, DevPot *out) {
+    GX_CHECK_ARG(pot != nullptr, "potential descriptor is NULL");
+    GX_CHECK_ARG(pot->n_dim == 3, "n_dim must be 3 (got %d)", pot->n_dim);
+    GX_CHECK_ARG(pot->n_components >= 0, "n_components < 0");
+    if (pot->n_components > GX_MAX_COMPONENTS) {
+        set_error("%d components exceed GX_MAX_COMPONENTS = %d", pot->n_components, GX_MAX_COMPONENTS);
+        return GX_ERR_CAPACITY;
+    }
+    GX_CHECK_ARG(pot->n_components == 0 || (pot->components && pot->params), "NULL component or param array");
+    memset(out, 0, sizeof(*out));
+    out->ncomp = pot->n_components;
+    out->pdev = pot->params_device;
+    int ninl = 0;
+    for (int i = 0; i < pot->n_components; i++) {
+        const gx_component &c = pot->components[i];
+        GX_CHECK_ARG(c.param_offset >= 0 && c.param_offset + c.n_params <= pot->n_params_total,
+                     "component %d parameter range outside params[]", i);
+        const int need = expected_params(c.type, pot->params + c.param_offset, c.n_params);
+        GX_CHECK_ARG(need > 0, "component %d: unknown type %d or bad SCF header", i, c.type);
+        GX_CHECK_ARG(c.n_params >= need, "component %d: %d parameters, type %d needs %d", i, c.n_params,
+                     c.type, need);
+        DevComp &d = out->c[i];
+        d.type = c.type;
+        d.do_sr = c.do_shift_rotate ? 1 : 0;
+        for (int k = 0; k < 3; k++) d.q0[k] = c.q0[k];
+        for (int k = 0; k < 9; k++) d.R[k] = c.R[k];
+        if (c.type == GX_POT_SCF) {
+            if (pot->params_device == nullptr) {
+                set_error("component %d is SCF: params_device (device copy of params) is required", i);
+                return GX_ERR_INVALID_ARGUMENT;
+            }
+            d.inl = 0;
+            d.poff = (int32_t)c.param_offset;
+            out->has_scf = 1;
+        } else {
+            if (ninl + need > GX_MAX_INLINE_PARAMS) {
+                set_error("inline parameters exceed GX_MAX_INLINE_PARAMS = %d", GX_MAX_INLINE_PARAMS);
+                return GX_ERR_CAPACITY;
+            }
+            d.inl = 1;
+            d.poff = ninl;
+            for (int k = 0; k < need; k++) out->p[ninl + k] = pot->params[c.param_offset + k];
+            ninl += need;
+        }
+    }
+    out->n_inline = ninl;
+    return GX_OK;
+}
+
+int pack_frame(const gx_frame *fr, DevFrame *out) {
+    memset(out, 0, sizeof(*out));
+    if (fr == nullptr) {
+        out->type = GX_FRAME_STATIC;
+        return GX_OK;
+    }
+    GX_CHECK_ARG(fr->type == GX_FRAME_STATIC || fr->type == GX_FRAME_CONSTANT_ROTATING, "unknown frame type %d",
+                 fr->type);
+    out->type = fr->type;
+    for (int k = 0; k < 3; k++) out->O[k] = fr->params[k];
+    return GX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Evaluation kernels: one thread per point, SoA in and out.
+// ---------------------------------------------------------------------------
+template <int KIND, bool SCF>  // KIND 0 value, 1 gradient, 2 density
+__global__ void eval_kernel(const __grid_constant__ DevPot pot, const double *__restrict__ q, int64_t n, double *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double qi[3] = {q[i], q[n + i], q[2 * n + i]};
+    if (KIND == 0) {
+        out[i] = potential_value<SCF>(pot, qi);
+    } else if (KIND == 2) {
+        out[i] = potential_density<SCF>(pot, qi);
+    } else {
+        double g[3];
+        potential_gradient<SCF>(pot, qi, g);
+        out[i] = g[0];
+        out[n + i] = g[1];
+        out[2 * n + i] = g[2];
+    }
+}
+
+template <int KIND, bool SCF>  // KIND 0 energy, 1 Hamilton's equations
+__global__ void ham_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFrame fr, const double *__restrict__ w, int64_t n, double *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double wi[6];
+    for (int k = 0; k < 6; k++) wi[k] = w[k * n + i];
+    if (KIND == 0) {
+        out[i] = potential_value<SCF>(pot, wi) + frame_energy(fr, wi);
+    } else {
+        double f[6];
+        hamiltonian_rhs<SCF>(pot, fr, wi, f);
+        for (int k = 0; k < 6; k++) out[k * n + i] = f[k];
+    }
+}
+
+template <int KIND>
+static int launch_eval(const gx_potential *pot, const double *q, int64_t n, double *out, void *stream) {
+    DevPot dp;
+    int rc = pack_potential(pot, &dp);
+    if (rc) return rc;
+    GX_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return GX_OK;
+    GX_CHECK_ARG(q && out, "NULL array");
+    const int bs = 128;
+    const int64_t grid = (n + bs - 1) / bs;
+    if (dp.has_scf)
+        eval_kernel<KIND, true><<<(unsigned)grid, bs, 0, as_stream(stream)>>>(dp, q, n, out);
+    else
+        eval_kernel<KIND, false><<<(unsigned)grid, bs, 0, as_stream(stream)>>>(dp, q, n, out);
+    return check_launch("gx_potential eval");
+}
+
+template <int KIND>
+static int launch_ham(const gx_potential *pot, const gx_frame *fr, const double *w, int64_t n, double *out,
+                      void *stream) {
+    DevPot dp;
+    DevFrame df;
+    int rc = pack_potential(pot, &dp);
+    if (rc) return rc;
+    rc = pack_frame(fr, &df);
+    if (rc) return rc;
+    GX_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return GX_OK;
+    GX_CHECK_ARG(w && out, "NULL array");
+    const int bs = 128;
+    const int64_t grid = (n + bs - 1) / bs;
+    if (dp.has_scf)
+        ham_kernel<KIND, true><<<(unsigned)grid, bs, 0, as_stream(stream)>>>(dp, df, w, n, out);
+    else
+        ham_kernel<KIND, false><<<(unsigned)grid, bs, 0, as_stream(stream)>>>(dp, df, w, n, out);
+    return check_launch("gx_hamiltonian eval");
+}
+
+}  // namespace gx
+
+extern "C" {
+
+int gx_abi_version(void) { return GX_ABI_VERSION; }
+
+const char *gx_last_error_message(void) { return gx::g_errmsg; }
+
+int gx_potential_value(const gx_potential *pot, double t, const double *q, int64_t n, double *out, void *stream) {
+    (void)t;
+    return gx::launch_eval<0>(pot, q, n, out, stream);
+}
+
+int gx_potential_gradient(const gx_potential *pot, double t, const double *q, int64_t n, double *out,
+                          void *stream) {
+    (void)t;
+    return gx::launch_eval<1>(pot, q, n, out, stream);
+}
+
+int gx_potential_density(const gx_potential *pot, double t, const double *q, int64_t n, double *out,
+                         void *stream) {
+    (void)t;
+    return gx::launch_eval<2>(pot, q, n, out, stream);
+}
+
+int gx_hamiltonian_value(const gx_potential *pot, const gx_frame *frame, double t, const double *w, int64_t n,
+                         double *out, void *stream) {
+    (void)t;
+    return gx::launch_ham<0>(pot, frame, w, n, out, stream);
+}
+
+int gx_hamiltonian_gradient(const gx_potential *pot, const gx_frame *frame, double t, const double *w, int64_t n,
+                            double *out, void *stream) {
+    (void)t;
+    return gx::launch_ham<1>(pot, frame, w, n, out, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,226 @@
+"""Hamiltonian (potential + reference frame) and the orbit-integration entry point.
+
+``Hamiltonian.integrate_orbit`` follows gala's dispatch
+(src/gala/potential/hamiltonian/chamiltonian.pyx:224-380): default integrator,
+time specification, array shapes, errors and the ``Orbit`` it returns are
+gala's, while the integration itself is one call into the CUDA library
+(gx_leapfrog_integrate_hamiltonian / gx_ruth4_integrate_hamiltonian /
+gx_dop853_integrate_hamiltonian).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import warnings
+
+import numpy as np
+
+from . import _abi
+from .dynamics import Orbit, PhaseSpacePosition
+from .integrate import (DOPRI853Integrator, LeapfrogIntegrator, Ruth4Integrator, get_integrator,
+                        parse_time_specification)
+from .potential import PotentialBase
+
+__all__ = ["StaticFrame", "ConstantRotatingFrame", "Hamiltonian"]
+
+
+class FrameBase:
+    _type = None
+
+    def __init__(self, *args, units=None):
+        self.units = units
+
+    def c_frame(self):
+        f = _abi.gx_frame()
+        f.type = self._type
+        for k, v in enumerate(self._params()):
+            f.params[k] = v
+        return f
+
+    def _params(self):
+        return []
+
+
+class StaticFrame(FrameBase):
+    """Static inertial frame (static_frame_*, builtin_frames.cpp:8-24)."""
+
+    _type = _abi.GX_FRAME_STATIC
+
+
+class ConstantRotatingFrame(FrameBase):
+    """Frame rotating at constant angular velocity Omega (rad/Myr) about the origin
+    (constant_rotating_frame_3d_*, builtin_frames.cpp:73-112)."""
+
+    _type = _abi.GX_FRAME_CONSTANT_ROTATING
+
+    def __init__(self, Omega, units=None):
+        super().__init__(units=units)
+        self.Omega = np.asarray(getattr(Omega, "value", Omega), dtype=np.float64).reshape(3)
+
+    def _params(self):
+        return list(self.Omega)
+
+
+class Hamiltonian:
+    """A potential in a reference frame (chamiltonian.pyx:40-77)."""
+
+    def __init__(self, potential, frame=None):
+        if isinstance(potential, Hamiltonian):
+            frame = potential.frame
+            potential = potential.potential
+        if not isinstance(potential, PotentialBase):
+            raise TypeError(f"potential must be a Potential object, not {type(potential)}")
+        if frame is None:
+            frame = StaticFrame()
+        if not isinstance(frame, FrameBase):
+            raise TypeError(f"frame must be a Frame object, not {type(frame)}")
+        self.potential = potential
+        self.frame = frame
+        self.units = potential.units
+        self.ndim = 6
+        self.c_enabled = True
+
+    def _frame_ref(self):
+        self._cframe = self.frame.c_frame()
+        return C.byref(self._cframe)
+
+    # --- evaluation ----------------------------------------------------------
+    def _prepare_w(self, w):
+        if isinstance(w, PhaseSpacePosition):
+            w = w.w()
+        w = np.asarray(w, dtype=np.float64)
+        if w.shape[0] != 6:
+            raise ValueError(f"Invalid phase-space shape {w.shape}: expected (6, ...)")
+        return w
+
+    def energy(self, w, t=0.0):
+        """Value of the Hamiltonian (chamiltonian.pyx:107-128) at w of shape (6, ...)."""
+        import torch
+
+        from ._device import as_device_f64, ptr, stream_handle
+
+        w = self._prepare_w(w)
+        shape = w.shape
+        wd = as_device_f64(w.reshape(6, -1))
+        n = wd.shape[1]
+        out = torch.empty(n, dtype=torch.float64, device=wd.device)
+        _abi.call("gx_hamiltonian_value", self.potential.packed().for_device(), self._frame_ref(), float(t),
+                  ptr(wd), n, ptr(out), stream_handle())
+        return out.cpu().numpy().reshape(shape[1:])
+
+    def gradient(self, w, t=0.0):
+        """(qdot, pdot) at w (hamiltonian_gradient_T, chamiltonian.cpp:38-57); note gala's
+        Hamiltonian.gradient returns dH/dw with the momentum half negated (:88-99)."""
+        import torch
+
+        from ._device import as_device_f64, ptr, stream_handle
+
+        w = self._prepare_w(w)
+        shape = w.shape
+        wd = as_device_f64(w.reshape(6, -1))
+        n = wd.shape[1]
+        out = torch.empty((6, n), dtype=torch.float64, device=wd.device)
+        _abi.call("gx_hamiltonian_gradient", self.potential.packed().for_device(), self._frame_ref(), float(t),
+                  ptr(wd), n, ptr(out), stream_handle())
+        return out.cpu().numpy().reshape(shape)
+
+    # --- integration ---------------------------------------------------------
+    def integrate_orbit(self, w0, Integrator=None, Integrator_kwargs=dict(), cython_if_possible=True,
+                        save_all=True, return_device=False, stream=None, **time_spec):
+        """Integrate orbits from w0 (shape (6,) or (6, N)) and return an Orbit.
+
+        Extra keyword (not in gala): ``return_device=True`` keeps the result on
+        the GPU (``Orbit.w_device``); the host copy is made on first access.
+        DOP853 accepts gala's Integrator_kwargs (atol, rtol, nmax, err_if_fail,
+        log_output, nbatch) plus ``out_stride`` (keep every k-th output time),
+        ``dt_max`` and ``nstiff``.
+        """
+        import torch
+
+        from ._device import ptr, require_cuda, stream_handle
+
+        if Integrator is None and isinstance(self.frame, StaticFrame):
+            Integrator = LeapfrogIntegrator
+        elif Integrator is None:
+            Integrator = DOPRI853Integrator
+        Integrator = get_integrator(Integrator)
+
+        if Integrator in (LeapfrogIntegrator, Ruth4Integrator) and not isinstance(self.frame, StaticFrame):
+            warnings.warn(
+                "Using a symplectic integrator with a non-static frame can lead to wildly incorrect orbits. "
+                "It is recommended that you use DOPRI853Integrator instead.", RuntimeWarning)
+
+        dev = require_cuda()
+        if isinstance(w0, PhaseSpacePosition):
+            arr_w0 = w0.w()
+        elif isinstance(w0, torch.Tensor):
+            arr_w0 = w0
+        else:
+            arr_w0 = np.asarray(w0, dtype=np.float64)
+        if arr_w0.shape[0] != 6:
+            raise ValueError(
+                f"Invalid initial conditions shape {tuple(arr_w0.shape)}. Expected shape (6, ...) but got shape "
+                f"{tuple(arr_w0.shape)}.")
+        orig_shape = tuple(arr_w0.shape)
+        if isinstance(arr_w0, torch.Tensor):
+            w0d = arr_w0.reshape(6, -1).to(device=dev, dtype=torch.float64).contiguous()
+        else:
+            host = torch.from_numpy(np.ascontiguousarray(arr_w0.reshape(6, -1)))
+            if torch.cuda.is_available():
+                host = host.pin_memory()
+            w0d = host.to(dev, non_blocking=True)
+        n = w0d.shape[1]
+
+        t = np.ascontiguousarray(parse_time_specification(self.units, **time_spec), dtype=np.float64)
+        ntimes = len(t)
+        if ntimes < 2:
+            raise ValueError("ntimes must be greater than 1")
+        td = torch.from_numpy(t).to(dev)
+        st = stream_handle(stream)
+        pot = self.potential.packed().for_device()
+        frame = self._frame_ref()
+
+        if Integrator in (LeapfrogIntegrator, Ruth4Integrator):
+            if not isinstance(self.frame, StaticFrame):
+                raise TypeError(
+                    f"{'Leapfrog' if Integrator is LeapfrogIntegrator else 'Ruth4'} integration is currently only "
+                    f"supported for StaticFrame, not {self.frame.__class__.__name__}")
+            out = torch.empty((6, ntimes, n) if save_all else (6, n), dtype=torch.float64, device=dev)
+            name = ("gx_leapfrog_integrate_hamiltonian" if Integrator is LeapfrogIntegrator
+                    else "gx_ruth4_integrate_hamiltonian")
+            _abi.call(name, pot, frame, ptr(w0d), n, ptr(td), ntimes, int(bool(save_all)), ptr(out), st)
+            t_out = t
+        else:
+            kw = dict(Integrator_kwargs)
+            atol = float(kw.get("atol", 1e-10))
+            rtol = float(kw.get("rtol", 1e-10))
+            nmax = int(kw.get("nmax", 0))
+            err_if_fail = int(kw.get("err_if_fail", 1))
+            nbatch = int(kw.get("nbatch", 100))
+            stride = int(kw.get("out_stride", 1))
+            dt_max = float(kw.get("dt_max", 0.0))
+            nstiff = int(kw.get("nstiff", 0))
+            n_out = (ntimes - 1) // stride + 1
+            nb = (n + nbatch - 1) // nbatch
+            out = torch.empty((6, n_out, n) if save_all else (6, n), dtype=torch.float64, device=dev)
+            status = torch.zeros(max(nb, 1), dtype=torch.int32, device=dev)
+            _abi.call("gx_dop853_integrate_hamiltonian", pot, frame, ptr(w0d), n, ptr(td), ntimes, atol, rtol,
+                      nmax, dt_max, nstiff, int(bool(save_all)), nbatch, stride, ptr(out), ptr(status), None, st)
+            if err_if_fail == 1 and n > 0:
+                res = status.cpu().numpy()
+                bad = res[res < 0]
+                if bad.size:
+                    raise RuntimeError(f"Integration failed with code {int(bad[0])}")
+            t_out = t[::stride]
+
+        if not save_all:
+            t_out = t[-1:]
+        # chamiltonian.pyx:359-360 and 370-371: a single orbit loses its last axis,
+        # and save_all=False keeps a length-1 time axis.
+        w = out if return_device else out.cpu().numpy()
+        if w.shape[-1] == 1:
+            w = w[..., 0]
+        if not save_all:
+            w = w[:, None]
+        if return_device:
+            return Orbit.from_w(w, t=t_out, hamiltonian=self)
+        return Orbit.from_w(w=w, t=t_out, hamiltonian=self, copy=False)

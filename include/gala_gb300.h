@@ -1,0 +1,200 @@
+/*
+ * gala_gb300.h -- C ABI of the GB300 orbit-integration library (libgala_gb300.so).
+ *
+ * This is the drop-in boundary for gala's orbit-integration hot path.  Every entry
+ * point below replaces one function of gala's Cython/C layer; the citation next to
+ * each declaration names the gala function (path inside the gala project) whose
+ * argument meaning, output layout and error behaviour it reproduces.
+ *
+ * Conventions
+ *   - All array arguments are DEVICE pointers (e.g. torch.Tensor.data_ptr() of a
+ *     CUDA tensor).  Descriptors (gx_potential, gx_frame, option structs) are HOST
+ *     structs; the library copies them into kernel parameters at launch.
+ *   - Phase-space arrays use gala's structure-of-arrays layout: w0 is (6, N)
+ *     row-major (x, y, z, vx, vy, vz rows), snapshots are (6, ntimes, N).
+ *   - Units are whatever the caller packed (gala_gb300 uses kpc, Myr, Msun with
+ *     G = 4.498502151469553e-12 kpc^3 / (Msun Myr^2)).
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *     asynchronous with respect to the host unless stated otherwise.
+ *   - Return value: GX_OK (0) or a negative gx_error code.  The call never aborts
+ *     the process; gx_last_error_message() describes the most recent failure of
+ *     the calling thread.
+ */
+#ifndef GALA_GB300_H
+#define GALA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GX_ABI_VERSION 1
+
+/* Capacity of the by-value potential descriptor handed to every kernel. */
+#define GX_MAX_COMPONENTS 16
+#define GX_MAX_INLINE_PARAMS 128
+
+/* ------------------------------------------------------------------------- */
+/* Error codes                                                               */
+/* ------------------------------------------------------------------------- */
+typedef enum gx_error {
+    GX_OK = 0,
+    GX_ERR_INVALID_ARGUMENT = -1,   /* bad size, NULL pointer, unknown type      */
+    GX_ERR_UNSUPPORTED = -2,        /* combination not implemented on the GPU    */
+    GX_ERR_CUDA = -3,               /* a CUDA runtime call failed                */
+    GX_ERR_CAPACITY = -4,           /* descriptor exceeds GX_MAX_* capacities    */
+    GX_ERR_KERNEL_STATUS = -5       /* a kernel reported a bounded-wait timeout  */
+} gx_error;
+
+/* DOP853 per-batch status, same values as gala's dop853() return code
+ * (src/gala/integrate/cyintegrators/dopri/dop853.cpp:340-354, 474-480). */
+#define GX_DOP853_OK            1
+#define GX_DOP853_BAD_INPUT    -1
+#define GX_DOP853_NMAX         -2
+#define GX_DOP853_SMALL_STEP   -3
+#define GX_DOP853_STIFF        -4
+
+/* ------------------------------------------------------------------------- */
+/* Potential descriptor: the device analogue of gala's struct _CPotential     */
+/* (src/gala/potential/potential/src/cpotential.h:10-36).  Function pointers  */
+/* are replaced by a type tag; parameters keep gala's packing [G, p0, p1, ...] */
+/* (CPotentialWrapper.init, src/gala/potential/potential/cpotential.pyx:57-102)*/
+/* ------------------------------------------------------------------------- */
+typedef enum gx_potential_type {
+    GX_POT_NULL = 0,           /* null_* (builtin_potentials.cpp:18-21)            */
+    GX_POT_KEPLER = 1,         /* [G, m]          kepler_*  (:58-88)               */
+    GX_POT_HERNQUIST = 2,      /* [G, m, c]       hernquist_* (:211-244)           */
+    GX_POT_PLUMMER = 3,        /* [G, m, b]       plummer_* (:292-324)             */
+    GX_POT_MIYAMOTONAGAI = 4,  /* [G, m, a, b]    miyamotonagai_* (:1287-1332)     */
+    GX_POT_SPHERICALNFW = 5,   /* [G, m, r_s, a, b, c] sphericalnfw_* (:819-864)   */
+    GX_POT_FLATTENEDNFW = 6,   /* [G, m, r_s, a, b, c] flattenednfw_* (:925-962)   */
+    GX_POT_TRIAXIALNFW = 7,    /* [G, m, r_s, a, b, c] triaxialnfw_* (:1028-1072)  */
+    GX_POT_SCF = 8             /* [G, nmax, lmax, m, r_s, Snlm..., Tnlm...]
+                                  scf_* (src/gala/potential/scf/src/bfe.cpp:191-259) */
+} gx_potential_type;
+
+typedef struct gx_component {
+    int32_t type;              /* gx_potential_type                                 */
+    int32_t n_params;          /* number of doubles of this component in params[]   */
+    int64_t param_offset;      /* offset of this component's [G, ...] in params[]   */
+    int32_t do_shift_rotate;   /* 0 iff q0 == 0 and R == I (cpotential.pyx:99-102)  */
+    int32_t reserved;
+    double q0[3];              /* origin                                            */
+    double R[9];               /* rotation, row-major                               */
+} gx_component;
+
+typedef struct gx_potential {
+    int32_t n_components;      /* components are summed in this order (composite   */
+    int32_t n_dim;             /* insertion order); n_dim must be 3                 */
+    const gx_component* components;   /* HOST array[n_components]                   */
+    const double* params;             /* HOST packed parameters                     */
+    const double* params_device;      /* DEVICE copy of params; required only when a */
+                                      /* component is GX_POT_SCF, else may be NULL  */
+    int64_t n_params_total;
+} gx_potential;
+
+/* Reference frame: gala's CFrameType (src/gala/potential/frame/src/cframe.h:7-17). */
+typedef enum gx_frame_type {
+    GX_FRAME_STATIC = 0,              /* static_frame_* (builtin_frames.cpp:8-24)   */
+    GX_FRAME_CONSTANT_ROTATING = 1    /* constant_rotating_frame_3d_* (:73-112),     */
+                                      /* params = Omega (3)                          */
+} gx_frame_type;
+
+typedef struct gx_frame {
+    int32_t type;
+    int32_t reserved;
+    double params[3];
+} gx_frame;
+
+/* ------------------------------------------------------------------------- */
+/* Library                                                                   */
+/* ------------------------------------------------------------------------- */
+/* ABI version of the loaded library (compare with GX_ABI_VERSION). */
+int gx_abi_version(void);
+
+/* Message of the last failed call on this host thread ("" if none). */
+const char* gx_last_error_message(void);
+
+/* ------------------------------------------------------------------------- */
+/* Potential evaluation over N points.                                       */
+/* q is (3, N) SoA; out is (N,) for value/density and (3, N) for gradient.   */
+/* ------------------------------------------------------------------------- */
+
+/* c_potential (src/gala/potential/potential/src/cpotential.cpp:170-189),
+ * applied to every column of q (CPotentialWrapper.energy, cpotential.pyx:104-122). */
+int gx_potential_value(const gx_potential* pot, double t, const double* q,
+                       int64_t n, double* out, void* stream);
+
+/* c_gradient (cpotential.cpp:214-287): out = sum over components of grad Phi,
+ * with the shift/rotate path q' = R (q - q0), g += R^T g'.  out is overwritten. */
+int gx_potential_gradient(const gx_potential* pot, double t, const double* q,
+                          int64_t n, double* out, void* stream);
+
+/* c_density (cpotential.cpp:192-211). */
+int gx_potential_density(const gx_potential* pot, double t, const double* q,
+                         int64_t n, double* out, void* stream);
+
+/* Hamiltonian.energy (src/gala/potential/hamiltonian/chamiltonian.pyx:83-86,
+ * 107-128): c_potential (shift/rotate aware) + the frame's energy
+ * (static_frame_hamiltonian / constant_rotating_frame_3d_hamiltonian,
+ * builtin_frames.cpp:8-16, 78-94) for every column of w (6, N). */
+int gx_hamiltonian_value(const gx_potential* pot, const gx_frame* frame, double t,
+                         const double* w, int64_t n, double* out, void* stream);
+
+/* hamiltonian_gradient_T (chamiltonian.cpp:38-57): dH/dt of every column of
+ * w (6, N) into out (6, N) = (qdot, pdot). */
+int gx_hamiltonian_gradient(const gx_potential* pot, const gx_frame* frame, double t,
+                            const double* w, int64_t n, double* out, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* Fixed-step symplectic integrators (FP64, one thread per orbit).           */
+/* t (ntimes) are the output times (t[1]-t[0] is the step, as in gala).      */
+/* save_all != 0: w_out is (6, ntimes, N), snapshot 0 = w0.                  */
+/* save_all == 0: w_out is (6, N), the state at t[ntimes-1].                 */
+/* ------------------------------------------------------------------------- */
+
+/* leapfrog_integrate_hamiltonian
+ * (src/gala/integrate/cyintegrators/leapfrog.pyx:54-121): kick-drift-kick with
+ * c_init_velocity (:24-32) and c_leapfrog_step (:35-51).  Frame must be static. */
+int gx_leapfrog_integrate_hamiltonian(const gx_potential* pot, const gx_frame* frame,
+                                      const double* w0, int64_t n, const double* t,
+                                      int64_t ntimes, int32_t save_all, double* w_out,
+                                      void* stream);
+
+/* ruth4_integrate_hamiltonian (src/gala/integrate/cyintegrators/ruth4.pyx:37-113),
+ * c_ruth4_step (:24-35) with gala's coefficients (:65-78).  Frame must be static. */
+int gx_ruth4_integrate_hamiltonian(const gx_potential* pot, const gx_frame* frame,
+                                   const double* w0, int64_t n, const double* t,
+                                   int64_t ntimes, int32_t save_all, double* w_out,
+                                   void* stream);
+
+/* dop853_integrate_hamiltonian
+ * (src/gala/integrate/cyintegrators/dop853.pyx:196-250) -> dop853_helper (:90-193)
+ * -> dop853()/dopcor() (dopri/dop853.cpp:89-866).  Orbits are integrated in
+ * batches of `nbatch` consecutive orbits that share one step size and one RMS
+ * error norm over all 6*nb components, exactly as gala's batching does.
+ *   atol, rtol, nmax, dt_max, nstiff : gala's meaning and defaults (0 -> default)
+ *   save_all != 0 : w_out is (6, n_out, N) holding the dense output at
+ *                   t[0], t[out_stride], t[2*out_stride], ... (n_out =
+ *                   (ntimes - 1) / out_stride + 1); out_stride = 1 is gala's layout.
+ *   save_all == 0 : w_out is (6, N), the state at t[ntimes-1].
+ *   status        : DEVICE int32[ceil(N / nbatch)], gala's dop853() return code
+ *                   per batch (1 = success, -2 nmax, -3 step too small, -4 stiff).
+ *   stats         : DEVICE int64[4 * ceil(N / nbatch)] or NULL; per batch the
+ *                   counters gala's dopcor keeps: nfcn, nstep, naccpt, nrejct.
+ *   nbatch        : 1..1024 (gala default 100). */
+int gx_dop853_integrate_hamiltonian(const gx_potential* pot, const gx_frame* frame,
+                                    const double* w0, int64_t n, const double* t,
+                                    int64_t ntimes, double atol, double rtol,
+                                    int64_t nmax, double dt_max, int64_t nstiff,
+                                    int32_t save_all, int32_t nbatch,
+                                    int64_t out_stride, double* w_out,
+                                    int32_t* status, int64_t* stats, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GALA_GB300_H */

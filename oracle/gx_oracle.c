@@ -1,0 +1,888 @@
+/*
+ * ORACLE -- test infrastructure, not product code.
+ *
+ * A plain-C restatement of gala's orbit-integration hot path, used only by the
+ * tests, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg as the
+ * checker of the CUDA library.  Nothing in gala_gb300/ links, imports or calls
+ * this file.
+ *
+ * Every function follows one gala function (file:line inside the gala project)
+ * and keeps its floating-point expression order, so that with a build that
+ * forbids contraction and reassociation (-O2 -ffp-contract=off) it reproduces
+ * gala's arithmetic operation by operation:
+ *
+ *   potentials     src/gala/potential/potential/builtin/builtin_potentials.cpp
+ *   composition    src/gala/potential/potential/src/cpotential.cpp:137-287
+ *   frames         src/gala/potential/frame/builtin/builtin_frames.cpp:8-112
+ *   hamiltonian    src/gala/potential/hamiltonian/src/chamiltonian.cpp:7-57
+ *   leapfrog       src/gala/integrate/cyintegrators/leapfrog.pyx:24-121
+ *   ruth4          src/gala/integrate/cyintegrators/ruth4.pyx:24-113
+ *   dop853         src/gala/integrate/cyintegrators/dopri/dop853.cpp:18-904 and
+ *                  src/gala/integrate/cyintegrators/dop853.pyx:90-250
+ *
+ * The same source is also built with gala's own flags (-Ofast) as the CPU
+ * baseline that bench.py times on the host cores; both builds are made by
+ * oracle/Makefile.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/gala_gb300.h"
+#include "dop853_tableau.h"
+#include "scf_oracle.h"
+
+/* ------------------------------------------------------------------------- */
+/* Single-component potentials (builtin_potentials.cpp)                       */
+/* ------------------------------------------------------------------------- */
+
+static double norm3_sq(const double *q) { return q[0] * q[0] + q[1] * q[1] + q[2] * q[2]; }
+
+/* kepler_value :58-64, hernquist_value :211-219, plummer_value :292-300,
+ * miyamotonagai_value :1287-1296, sphericalnfw_value :819-833,
+ * flattenednfw_value :925-942, triaxialnfw_value :1028-1049, scf_value
+ * (src/gala/potential/scf/src/bfe.cpp:191-227). */
+static double comp_value(int type, const double *p, const double *q) {
+    switch (type) {
+    case GX_POT_NULL:
+        return 0.;
+    case GX_POT_KEPLER:
+        return -p[0] * p[1] / sqrt(norm3_sq(q));
+    case GX_POT_HERNQUIST: {
+        const double r = sqrt(norm3_sq(q));
+        return -p[0] * p[1] / (r + p[2]);
+    }
+    case GX_POT_PLUMMER: {
+        const double r2 = norm3_sq(q);
+        return -p[0] * p[1] / sqrt(r2 + p[2] * p[2]);
+    }
+    case GX_POT_MIYAMOTONAGAI: {
+        const double zd = (p[2] + sqrt(q[2] * q[2] + p[3] * p[3]));
+        return -p[0] * p[1] / sqrt(q[0] * q[0] + q[1] * q[1] + zd * zd);
+    }
+    case GX_POT_SPHERICALNFW: {
+        const double v_h2 = -p[0] * p[1] / p[2];
+        const double u = sqrt(norm3_sq(q)) / p[2];
+        if (u == 0) return v_h2;
+        return v_h2 * log(1 + u) / u;
+    }
+    case GX_POT_FLATTENEDNFW: {
+        const double v_h2 = -p[0] * p[1] / p[2];
+        const double u = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] / (p[5] * p[5])) / p[2];
+        if (u == 0) return v_h2;
+        return v_h2 * log(1 + u) / u;
+    }
+    case GX_POT_TRIAXIALNFW: {
+        const double v_h2 = -p[0] * p[1] / p[2];
+        const double u = sqrt(q[0] * q[0] / (p[3] * p[3]) + q[1] * q[1] / (p[4] * p[4]) +
+                              q[2] * q[2] / (p[5] * p[5])) / p[2];
+        if (u == 0) return v_h2;
+        return v_h2 * log(1 + u) / u;
+    }
+    case GX_POT_SCF:
+        return orc_scf_value(p, q);
+    default:
+        return NAN;
+    }
+}
+
+/* *_gradient_single: kepler :66-76, hernquist :221-233, plummer :302-314,
+ * miyamotonagai :1298-1312, sphericalnfw :835-850, flattenednfw :944-962,
+ * triaxialnfw :1051-1072, scf_gradient (bfe.cpp:229-259).  Accumulates into g. */
+static void comp_gradient(int type, const double *p, const double *q, double *g) {
+    double fac;
+    switch (type) {
+    case GX_POT_NULL:
+        return;
+    case GX_POT_KEPLER:
+        fac = p[0] * p[1] / pow(sqrt(norm3_sq(q)), 3);
+        break;
+    case GX_POT_HERNQUIST: {
+        const double r = sqrt(norm3_sq(q));
+        fac = p[0] * p[1] / ((r + p[2]) * (r + p[2]) * r);
+        break;
+    }
+    case GX_POT_PLUMMER: {
+        const double R2b = norm3_sq(q) + p[2] * p[2];
+        fac = p[0] * p[1] / sqrt(R2b) / R2b;
+        break;
+    }
+    case GX_POT_MIYAMOTONAGAI: {
+        const double sqrtz = sqrt(q[2] * q[2] + p[3] * p[3]);
+        const double zd = p[2] + sqrtz;
+        fac = p[0] * p[1] * pow(q[0] * q[0] + q[1] * q[1] + zd * zd, -1.5);
+        g[0] = g[0] + fac * q[0];
+        g[1] = g[1] + fac * q[1];
+        g[2] = g[2] + fac * q[2] * (1. + p[2] / sqrtz);
+        return;
+    }
+    case GX_POT_SPHERICALNFW: {
+        const double v_h2 = p[0] * p[1] / p[2];
+        const double u = sqrt(norm3_sq(q)) / p[2];
+        fac = v_h2 / (u * u * u) / (p[2] * p[2]) * (log(1 + u) - u / (1 + u));
+        break;
+    }
+    case GX_POT_FLATTENEDNFW: {
+        const double v_h2 = p[0] * p[1] / p[2];
+        const double u = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] / (p[5] * p[5])) / p[2];
+        fac = v_h2 / (u * u * u) / (p[2] * p[2]) * (log(1 + u) - u / (1 + u));
+        g[0] = g[0] + fac * q[0];
+        g[1] = g[1] + fac * q[1];
+        g[2] = g[2] + fac * q[2] / (p[5] * p[5]);
+        return;
+    }
+    case GX_POT_TRIAXIALNFW: {
+        const double v_h2 = p[0] * p[1] / p[2];
+        const double u = sqrt(q[0] * q[0] / (p[3] * p[3]) + q[1] * q[1] / (p[4] * p[4]) +
+                              q[2] * q[2] / (p[5] * p[5])) / p[2];
+        fac = v_h2 / (u * u * u) / (p[2] * p[2]) * (log(1 + u) - u / (1 + u));
+        g[0] = g[0] + fac * q[0] / (p[3] * p[3]);
+        g[1] = g[1] + fac * q[1] / (p[4] * p[4]);
+        g[2] = g[2] + fac * q[2] / (p[5] * p[5]);
+        return;
+    }
+    case GX_POT_SCF:
+        orc_scf_gradient(p, q, g);
+        return;
+    default:
+        g[0] = NAN; g[1] = NAN; g[2] = NAN;
+        return;
+    }
+    g[0] = g[0] + fac * q[0];
+    g[1] = g[1] + fac * q[1];
+    g[2] = g[2] + fac * q[2];
+}
+
+/* kepler_density :78-88, hernquist_density :235-244, plummer_density :316-324,
+ * miyamotonagai_density :1314-1332, sphericalnfw_density :852-864,
+ * scf_density (bfe.cpp).  Flattened/triaxial NFW have no density in gala
+ * (nan_density is installed, cybuiltin.pyx), nor do we. */
+static double comp_density(int type, const double *p, const double *q) {
+    switch (type) {
+    case GX_POT_NULL:
+        return 0.;
+    case GX_POT_KEPLER:
+        return (norm3_sq(q) == 0.) ? INFINITY : 0.;
+    case GX_POT_HERNQUIST: {
+        const double r = sqrt(norm3_sq(q));
+        const double rho0 = p[1] / (2 * M_PI * p[2] * p[2] * p[2]);
+        return rho0 / ((r / p[2]) * pow(1 + r / p[2], 3));
+    }
+    case GX_POT_PLUMMER: {
+        const double r2 = norm3_sq(q);
+        return 3 * p[1] / (4 * M_PI * p[2] * p[2] * p[2]) * pow(1 + r2 / (p[2] * p[2]), -2.5);
+    }
+    case GX_POT_MIYAMOTONAGAI: {
+        const double M = p[1], a = p[2], b = p[3];
+        const double R2 = q[0] * q[0] + q[1] * q[1];
+        const double sqrt_zb = sqrt(q[2] * q[2] + b * b);
+        const double numer = (b * b * M / (4 * M_PI)) * (a * R2 + (a + 3 * sqrt_zb) * (a + sqrt_zb) * (a + sqrt_zb));
+        const double denom = pow(R2 + (a + sqrt_zb) * (a + sqrt_zb), 2.5) * sqrt_zb * sqrt_zb * sqrt_zb;
+        return numer / denom;
+    }
+    case GX_POT_SPHERICALNFW: {
+        const double v_h2 = p[0] * p[1] / p[2];
+        const double r = sqrt(norm3_sq(q));
+        const double rho0 = v_h2 / (4 * M_PI * p[0] * p[2] * p[2]);
+        return rho0 / ((r / p[2]) * pow(1 + r / p[2], 2));
+    }
+    case GX_POT_SCF:
+        return orc_scf_density(p, q);
+    default:
+        return NAN;
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Composition with shift/rotate (cpotential.cpp:137-287)                      */
+/* ------------------------------------------------------------------------- */
+
+/* apply_shift_rotate (:137-149) followed by apply_rotate with q_out = 0 (:80-100):
+ * q' = R (q - q0), each row summed left to right starting from 0. */
+static void shift_rotate(const gx_component *c, const double *q, double *qt) {
+    const double *R = c->R;
+    const double x = q[0] - c->q0[0], y = q[1] - c->q0[1], z = q[2] - c->q0[2];
+    qt[0] = 0. + R[0] * x + R[1] * y + R[2] * z;
+    qt[1] = 0. + R[3] * x + R[4] * y + R[5] * z;
+    qt[2] = 0. + R[6] * x + R[7] * y + R[8] * z;
+}
+
+/* apply_rotate_T with transpose = 1 (:103-134): g = R^T g'. */
+static void rotate_back(const gx_component *c, const double *gt, double *g) {
+    const double *R = c->R;
+    g[0] = R[0] * gt[0] + R[3] * gt[1] + R[6] * gt[2];
+    g[1] = R[1] * gt[0] + R[4] * gt[1] + R[7] * gt[2];
+    g[2] = R[2] * gt[0] + R[5] * gt[1] + R[8] * gt[2];
+}
+
+/* The shift/rotate path of apply_shift_rotate_N (:152-167) rotates (q - q0) in
+ * place without the leading 0 term; for finite inputs 0 + a == a, so both forms
+ * give the same bits except for the sign of an exact zero. */
+
+/* c_potential (:170-189) */
+double orc_potential(const gx_potential *pot, double t, const double *q) {
+    (void)t;
+    double v = 0;
+    for (int i = 0; i < pot->n_components; i++) {
+        const gx_component *c = &pot->components[i];
+        const double *p = pot->params + c->param_offset;
+        if (c->do_shift_rotate == 0) {
+            v = v + comp_value(c->type, p, q);
+        } else {
+            double qt[3];
+            shift_rotate(c, q, qt);
+            v = v + comp_value(c->type, p, qt);
+        }
+    }
+    return v;
+}
+
+/* c_density (:192-211) */
+double orc_density(const gx_potential *pot, double t, const double *q) {
+    (void)t;
+    double v = 0;
+    for (int i = 0; i < pot->n_components; i++) {
+        const gx_component *c = &pot->components[i];
+        const double *p = pot->params + c->param_offset;
+        if (c->do_shift_rotate == 0) {
+            v = v + comp_density(c->type, p, q);
+        } else {
+            double qt[3];
+            shift_rotate(c, q, qt);
+            v = v + comp_density(c->type, p, qt);
+        }
+    }
+    return v;
+}
+
+/* c_gradient for one point (:214-287): zero, then accumulate components in
+ * order; a shifted/rotated component is evaluated into a zeroed temporary,
+ * rotated back and added. */
+static void gradient_point(const gx_potential *pot, const double *q, double *g) {
+    g[0] = 0.; g[1] = 0.; g[2] = 0.;
+    for (int i = 0; i < pot->n_components; i++) {
+        const gx_component *c = &pot->components[i];
+        const double *p = pot->params + c->param_offset;
+        if (c->do_shift_rotate == 0) {
+            comp_gradient(c->type, p, q, g);
+        } else {
+            double qt[3], gt[3] = {0., 0., 0.}, gr[3];
+            const double *R = c->R;
+            const double x = q[0] - c->q0[0], y = q[1] - c->q0[1], z = q[2] - c->q0[2];
+            qt[0] = R[0] * x + R[1] * y + R[2] * z;
+            qt[1] = R[3] * x + R[4] * y + R[5] * z;
+            qt[2] = R[6] * x + R[7] * y + R[8] * z;
+            comp_gradient(c->type, p, qt, gt);
+            rotate_back(c, gt, gr);
+            g[0] += gr[0];
+            g[1] += gr[1];
+            g[2] += gr[2];
+        }
+    }
+}
+
+/* c_gradient over N points, SoA q[3, N] -> grad[3, N] (overwritten). */
+void orc_gradient(const gx_potential *pot, size_t N, double t, const double *q, double *grad) {
+    (void)t;
+    for (size_t i = 0; i < N; i++) {
+        double qi[3] = {q[i], q[N + i], q[2 * N + i]}, g[3];
+        gradient_point(pot, qi, g);
+        grad[i] = g[0];
+        grad[N + i] = g[1];
+        grad[2 * N + i] = g[2];
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Frames and Hamiltonian (builtin_frames.cpp, chamiltonian.cpp)             */
+/* ------------------------------------------------------------------------- */
+
+/* static_frame_hamiltonian (:8-16) / constant_rotating_frame_3d_hamiltonian (:78-94) */
+static double frame_energy(const gx_frame *fr, const double *w) {
+    if (fr == NULL || fr->type == GX_FRAME_STATIC) {
+        double E = 0.;
+        for (int i = 0; i < 3; i++) E += w[i + 3] * w[i + 3];
+        return 0.5 * E;
+    } else {
+        const double *O = fr->params;
+        double E = 0.;
+        for (int i = 0; i < 3; i++) E += 0.5 * w[i + 3] * w[i + 3];
+        const double Lx = w[1] * w[5] - w[2] * w[4];
+        const double Ly = -w[0] * w[5] + w[2] * w[3];
+        const double Lz = w[0] * w[4] - w[1] * w[3];
+        return E - (O[0] * Lx + O[1] * Ly + O[2] * Lz);
+    }
+}
+
+/* Hamiltonian.energy (src/gala/potential/hamiltonian/chamiltonian.pyx:83-86, 107-128):
+ * potential energy through c_potential (shift/rotate aware) plus the frame's
+ * energy (CFrameWrapper.energy, src/gala/potential/frame/cframe.pyx:29-45). */
+double orc_hamiltonian_value(const gx_potential *pot, const gx_frame *fr, double t, const double *w) {
+    return orc_potential(pot, t, w) + frame_energy(fr, w);
+}
+
+/* Fwrapper_T -> hamiltonian_gradient_T (chamiltonian.cpp:38-57) for one point:
+ * f[3:6] = grad Phi (c_gradient), frame gradient fills f[0:3] (and for the
+ * rotating frame adds Omega x p to f[3:6], builtin_frames.cpp:96-112), then the
+ * momentum half is negated. */
+static void rhs_point(const gx_potential *pot, const gx_frame *fr, const double *w, double *f) {
+    double g[3];
+    gradient_point(pot, w, g);
+    if (fr == NULL || fr->type == GX_FRAME_STATIC) {
+        f[0] = w[3];
+        f[1] = w[4];
+        f[2] = w[5];
+        f[3] = g[0];
+        f[4] = g[1];
+        f[5] = g[2];
+    } else {
+        const double *O = fr->params;
+        double Cx = O[1] * w[2] - O[2] * w[1];
+        double Cy = -O[0] * w[2] + O[2] * w[0];
+        double Cz = O[0] * w[1] - O[1] * w[0];
+        f[0] = 0. + w[3] - Cx;
+        f[1] = 0. + w[4] - Cy;
+        f[2] = 0. + w[5] - Cz;
+        Cx = O[1] * w[5] - O[2] * w[4];
+        Cy = -O[0] * w[5] + O[2] * w[3];
+        Cz = O[0] * w[4] - O[1] * w[3];
+        f[3] = g[0] + Cx;
+        f[4] = g[1] + Cy;
+        f[5] = g[2] + Cz;
+    }
+    f[3] *= -1;
+    f[4] *= -1;
+    f[5] *= -1;
+}
+
+/* hamiltonian_gradient_T over SoA w[6, N] -> f[6, N]. */
+void orc_hamiltonian_gradient(const gx_potential *pot, const gx_frame *fr, size_t N, double t,
+                              const double *w, double *f) {
+    (void)t;
+    for (size_t i = 0; i < N; i++) {
+        double wi[6], fi[6];
+        for (int k = 0; k < 6; k++) wi[k] = w[k * N + i];
+        rhs_point(pot, fr, wi, fi);
+        for (int k = 0; k < 6; k++) f[k * N + i] = fi[k];
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Parallel-for over index ranges (pthreads), used to spread independent      */
+/* orbits (leapfrog/ruth4) or batches (dop853) over host cores.               */
+/* ------------------------------------------------------------------------- */
+typedef void (*range_fn)(void *ctx, int64_t lo, int64_t hi);
+typedef struct {
+    range_fn fn;
+    void *ctx;
+    int64_t n, chunk;
+    int64_t next;
+    pthread_mutex_t mu;
+} pool_t;
+
+static void *pool_worker(void *arg) {
+    pool_t *P = (pool_t *)arg;
+    for (;;) {
+        pthread_mutex_lock(&P->mu);
+        int64_t lo = P->next;
+        P->next += P->chunk;
+        pthread_mutex_unlock(&P->mu);
+        if (lo >= P->n) break;
+        int64_t hi = lo + P->chunk < P->n ? lo + P->chunk : P->n;
+        P->fn(P->ctx, lo, hi);
+    }
+    return NULL;
+}
+
+static void parallel_for(int nthreads, int64_t n, int64_t chunk, range_fn fn, void *ctx) {
+    if (nthreads <= 1 || n <= chunk) {
+        fn(ctx, 0, n);
+        return;
+    }
+    pool_t P = {fn, ctx, n, chunk, 0};
+    pthread_mutex_init(&P.mu, NULL);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nthreads);
+    for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, pool_worker, &P);
+    for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+    free(th);
+    pthread_mutex_destroy(&P.mu);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Leapfrog (leapfrog.pyx:24-121) and Ruth4 (ruth4.pyx:24-113)                 */
+/* ------------------------------------------------------------------------- */
+typedef struct {
+    const gx_potential *pot;
+    const double *w0, *t;
+    int64_t n, ntimes;
+    int save_all, method;
+    double *w_out;
+} fixed_ctx;
+
+/* One chunk of orbits [lo, hi) advanced exactly like gala advances its whole
+ * (6, n) array: the per-orbit arithmetic does not depend on the other orbits,
+ * so chunking changes no bits. */
+static void fixed_chunk(void *vctx, int64_t lo, int64_t hi) {
+    fixed_ctx *C = (fixed_ctx *)vctx;
+    const int64_t n = C->n, ntimes = C->ntimes, m = hi - lo;
+    const double dt = C->t[1] - C->t[0];
+    double *x = (double *)malloc(sizeof(double) * 6 * (size_t)m);
+    double *vh = (double *)malloc(sizeof(double) * 3 * (size_t)m);
+    double *grad = (double *)malloc(sizeof(double) * 3 * (size_t)m);
+    for (int k = 0; k < 6; k++)
+        for (int64_t i = 0; i < m; i++) x[k * m + i] = C->w0[k * n + lo + i];
+    if (C->save_all)
+        for (int k = 0; k < 6; k++)
+            for (int64_t i = 0; i < m; i++) C->w_out[(k * ntimes + 0) * n + lo + i] = x[k * m + i];
+
+    if (C->method == 0) {
+        /* c_init_velocity (:24-32) */
+        orc_gradient(C->pot, (size_t)m, C->t[0], x, grad);
+        for (int k = 0; k < 3; k++)
+            for (int64_t i = 0; i < m; i++) vh[k * m + i] = x[(3 + k) * m + i] - grad[k * m + i] * dt / 2.;
+        for (int64_t j = 1; j < ntimes; j++) {
+            /* c_leapfrog_step (:35-51) */
+            for (int k = 0; k < 3; k++)
+                for (int64_t i = 0; i < m; i++) x[k * m + i] = x[k * m + i] + vh[k * m + i] * dt;
+            orc_gradient(C->pot, (size_t)m, C->t[j], x, grad);
+            for (int k = 0; k < 3; k++)
+                for (int64_t i = 0; i < m; i++) {
+                    x[(3 + k) * m + i] = vh[k * m + i] - grad[k * m + i] * dt / 2.;
+                    vh[k * m + i] = vh[k * m + i] - grad[k * m + i] * dt;
+                }
+            if (C->save_all)
+                for (int k = 0; k < 6; k++)
+                    for (int64_t i = 0; i < m; i++) C->w_out[(k * ntimes + j) * n + lo + i] = x[k * m + i];
+        }
+    } else {
+        /* coefficients (ruth4.pyx:65-78) */
+        const double two_13 = pow(2., 1. / 3.);
+        const double cs[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
+                              (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};
+        const double ds[4] = {0., 1. / (2. - two_13), -two_13 / (2. - two_13), 1. / (2. - two_13)};
+        for (int64_t j = 1; j < ntimes; j++) {
+            /* c_ruth4_step (:24-35) */
+            for (int s = 0; s < 4; s++) {
+                orc_gradient(C->pot, (size_t)m, C->t[j], x, grad);
+                for (int k = 0; k < 3; k++)
+                    for (int64_t i = 0; i < m; i++) {
+                        x[(3 + k) * m + i] = x[(3 + k) * m + i] - ds[s] * grad[k * m + i] * dt;
+                        x[k * m + i] = x[k * m + i] + cs[s] * x[(3 + k) * m + i] * dt;
+                    }
+            }
+            if (C->save_all)
+                for (int k = 0; k < 6; k++)
+                    for (int64_t i = 0; i < m; i++) C->w_out[(k * ntimes + j) * n + lo + i] = x[k * m + i];
+        }
+    }
+    if (!C->save_all)
+        for (int k = 0; k < 6; k++)
+            for (int64_t i = 0; i < m; i++) C->w_out[k * n + lo + i] = x[k * m + i];
+    free(x);
+    free(vh);
+    free(grad);
+}
+
+/* leapfrog_integrate_hamiltonian / ruth4_integrate_hamiltonian.
+ * w0 (6, n); w_out (6, ntimes, n) if save_all else (6, n).  method 0 =
+ * leapfrog, 1 = ruth4.  Orbits are spread over nthreads in chunks. */
+int orc_fixed_integrate(const gx_potential *pot, int method, const double *w0, int64_t n,
+                        const double *t, int64_t ntimes, int save_all, double *w_out, int nthreads) {
+    if (ntimes < 2 || n < 0) return -1;
+    fixed_ctx C = {pot, w0, t, n, ntimes, save_all, method, w_out};
+    int64_t chunk = 256;
+    if (nthreads > 1 && n / nthreads < chunk) chunk = (n + nthreads - 1) / nthreads;
+    if (chunk < 1) chunk = 1;
+    parallel_for(nthreads, n, chunk, fixed_chunk, &C);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------- */
+/* DOP853 (dop853.cpp)                                                        */
+/* ------------------------------------------------------------------------- */
+static double sign_d(double a, double b) { return (b < 0.0) ? -fabs(a) : fabs(a); }
+static double min_d(double a, double b) { return (a < b) ? a : b; }
+static double max_d(double a, double b) { return (a > b) ? a : b; }
+
+/* Fwrapper_T on a batch held as y[6 * nb] in SoA order (component k of orbit j
+ * at k * nb + j), as dop853_helper lays it out (dop853.pyx:135-136, 157-182). */
+static void batch_rhs(const gx_potential *pot, const gx_frame *fr, int nb, const double *y, double *f) {
+    for (int j = 0; j < nb; j++) {
+        double wi[6], fi[6];
+        for (int k = 0; k < 6; k++) wi[k] = y[k * nb + j];
+        rhs_point(pot, fr, wi, fi);
+        for (int k = 0; k < 6; k++) f[k * nb + j] = fi[k];
+    }
+}
+
+/* hinit (:18-86), scalar tolerances. */
+static double orc_hinit(const gx_potential *pot, const gx_frame *fr, int nb, double x, const double *y,
+                        double posneg, const double *f0, double *f1, double *yy1, int iord,
+                        double hmax, double atoli, double rtoli) {
+    const int n = 6 * nb;
+    double dnf = 0.0, dny = 0.0, sk, sqr, h, h1, der2, der12;
+    for (int i = 0; i < n; i++) {
+        sk = atoli + rtoli * fabs(y[i]);
+        sqr = f0[i] / sk;
+        dnf += sqr * sqr;
+        sqr = y[i] / sk;
+        dny += sqr * sqr;
+    }
+    if ((dnf <= 1.0E-10) || (dny <= 1.0E-10))
+        h = 1.0E-6;
+    else
+        h = sqrt(dny / dnf) * 0.01;
+    h = min_d(h, hmax);
+    h = sign_d(h, posneg);
+    for (int i = 0; i < n; i++) yy1[i] = y[i] + h * f0[i];
+    batch_rhs(pot, fr, nb, yy1, f1);
+    (void)x;
+    der2 = 0.0;
+    for (int i = 0; i < n; i++) {
+        sk = atoli + rtoli * fabs(y[i]);
+        sqr = (f1[i] - f0[i]) / sk;
+        der2 += sqr * sqr;
+    }
+    der2 = sqrt(der2) / h;
+    der12 = max_d(fabs(der2), sqrt(dnf));
+    if (der12 <= 1.0E-15)
+        h1 = max_d(1.0E-6, fabs(h) * 1.0E-3);
+    else
+        h1 = pow(0.01 / der12, 1.0 / (double)iord);
+    h = min_d(100.0 * fabs(h), min_d(h1, hmax));
+    return sign_d(h, posneg);
+}
+
+/* One dop853() call on one batch (dopcor :89-650 with the front-end defaults of
+ * :653-866 and dop853_helper's arguments, dop853.pyx:157-182).
+ *   y     : (6*nb) in/out state
+ *   out   : if non-NULL, dense output (n_out, 6*nb) at t[0], t[stride], ...
+ *   stats : if non-NULL, {nfcn, nstep, naccpt, nrejct}
+ * Returns gala's idid: 1 on success, -2 / -3 / -4 on failure. */
+int orc_dop853_batch(const gx_potential *pot, const gx_frame *fr, int nb, double *y,
+                     const double *t, int64_t ntimes, double atol, double rtol, int64_t nmax,
+                     double dt_max, int64_t nstiff, int64_t out_stride, double *out, long *stats) {
+    const int n = 6 * nb;
+    double x = t[0];
+    const double xend = t[ntimes - 1];
+    double h = t[1] - t[0];
+    double hmax = dt_max;
+    const double uround = 2.220446049250313e-16; /* np.finfo(float).eps, dop853.pyx:165 */
+    const double safe = 0.9, fac1 = 0.333, fac2 = 6.0, beta = 0.0;
+    if (!nmax) nmax = 1000000;
+    if (!nstiff) nstiff = 1000;
+    else if (nstiff < 0) nstiff = nmax + 10;
+    if (hmax == 0.0) hmax = xend - x;
+
+    double *work = (double *)malloc(sizeof(double) * (size_t)n * 19);
+    double *yy1 = work, *k1 = work + n, *k2 = work + 2 * n, *k3 = work + 3 * n, *k4 = work + 4 * n;
+    double *k5 = work + 5 * n, *k6 = work + 6 * n, *k7 = work + 7 * n, *k8 = work + 8 * n;
+    double *k9 = work + 9 * n, *k10 = work + 10 * n;
+    double *rc1 = work + 11 * n, *rc2 = work + 12 * n, *rc3 = work + 13 * n, *rc4 = work + 14 * n;
+    double *rc5 = work + 15 * n, *rc6 = work + 16 * n, *rc7 = work + 17 * n, *rc8 = work + 18 * n;
+
+    double facold = 1.0E-4;
+    const double expo1 = 1.0 / 8.0 - beta * 0.2;
+    const double facc1 = 1.0 / fac1, facc2 = 1.0 / fac2;
+    const double posneg = sign_d(1.0, xend - x);
+    const double atoli = atol, rtoli = rtol;
+    int last = 0, reject = 0, iasti = 0, nonsti = 0, idid = 0;
+    double hlamb = 0.0, xold = x, hout = 0.0;
+    long nfcn = 0, nstep = 0, naccpt = 0, nrejct = 0;
+    int64_t out_idx = 0; /* index into t of the next output time */
+    int64_t out_slot = 0;
+
+    batch_rhs(pot, fr, nb, y, k1);
+    hmax = fabs(hmax);
+    const int iord = 8;
+    if (h == 0.0) h = orc_hinit(pot, fr, nb, x, y, posneg, k1, k2, k3, iord, hmax, atoli, rtoli);
+    nfcn += 2;
+
+    for (;;) {
+        if (nstep > nmax) { idid = -2; break; }
+        if (0.1 * fabs(h) <= fabs(x) * uround) { idid = -3; break; }
+        if ((x + 1.01 * h - xend) * posneg > 0.0) {
+            h = xend - x;
+            last = 1;
+        }
+        xold = x;
+        hout = h;
+        nstep++;
+
+        for (int i = 0; i < n; i++) yy1[i] = y[i] + h * a21 * k1[i];
+        batch_rhs(pot, fr, nb, yy1, k2);
+        for (int i = 0; i < n; i++) yy1[i] = y[i] + h * (a31 * k1[i] + a32 * k2[i]);
+        batch_rhs(pot, fr, nb, yy1, k3);
+        for (int i = 0; i < n; i++) yy1[i] = y[i] + h * (a41 * k1[i] + a43 * k3[i]);
+        batch_rhs(pot, fr, nb, yy1, k4);
+        for (int i = 0; i < n; i++) yy1[i] = y[i] + h * (a51 * k1[i] + a53 * k3[i] + a54 * k4[i]);
+        batch_rhs(pot, fr, nb, yy1, k5);
+        for (int i = 0; i < n; i++) yy1[i] = y[i] + h * (a61 * k1[i] + a64 * k4[i] + a65 * k5[i]);
+        batch_rhs(pot, fr, nb, yy1, k6);
+        for (int i = 0; i < n; i++)
+            yy1[i] = y[i] + h * (a71 * k1[i] + a74 * k4[i] + a75 * k5[i] + a76 * k6[i]);
+        batch_rhs(pot, fr, nb, yy1, k7);
+        for (int i = 0; i < n; i++)
+            yy1[i] = y[i] + h * (a81 * k1[i] + a84 * k4[i] + a85 * k5[i] + a86 * k6[i] + a87 * k7[i]);
+        batch_rhs(pot, fr, nb, yy1, k8);
+        for (int i = 0; i < n; i++)
+            yy1[i] = y[i] + h * (a91 * k1[i] + a94 * k4[i] + a95 * k5[i] + a96 * k6[i] + a97 * k7[i] +
+                                 a98 * k8[i]);
+        batch_rhs(pot, fr, nb, yy1, k9);
+        for (int i = 0; i < n; i++)
+            yy1[i] = y[i] + h * (a101 * k1[i] + a104 * k4[i] + a105 * k5[i] + a106 * k6[i] +
+                                 a107 * k7[i] + a108 * k8[i] + a109 * k9[i]);
+        batch_rhs(pot, fr, nb, yy1, k10);
+        for (int i = 0; i < n; i++)
+            yy1[i] = y[i] + h * (a111 * k1[i] + a114 * k4[i] + a115 * k5[i] + a116 * k6[i] +
+                                 a117 * k7[i] + a118 * k8[i] + a119 * k9[i] + a1110 * k10[i]);
+        batch_rhs(pot, fr, nb, yy1, k2);
+        const double xph = x + h;
+        for (int i = 0; i < n; i++)
+            yy1[i] = y[i] + h * (a121 * k1[i] + a124 * k4[i] + a125 * k5[i] + a126 * k6[i] +
+                                 a127 * k7[i] + a128 * k8[i] + a129 * k9[i] + a1210 * k10[i] +
+                                 a1211 * k2[i]);
+        batch_rhs(pot, fr, nb, yy1, k3);
+        nfcn += 11;
+        for (int i = 0; i < n; i++) {
+            k4[i] = b1 * k1[i] + b6 * k6[i] + b7 * k7[i] + b8 * k8[i] + b9 * k9[i] + b10 * k10[i] +
+                    b11 * k2[i] + b12 * k3[i];
+            k5[i] = y[i] + h * k4[i];
+        }
+
+        /* error estimation, scalar tolerances (:416-444) */
+        double err = 0.0, err2 = 0.0, sk, erri, sqr;
+        for (int i = 0; i < n; i++) {
+            sk = atoli + rtoli * max_d(fabs(y[i]), fabs(k5[i]));
+            erri = k4[i] - bhh1 * k1[i] - bhh2 * k9[i] - bhh3 * k3[i];
+            sqr = erri / sk;
+            err2 += sqr * sqr;
+            erri = er1 * k1[i] + er6 * k6[i] + er7 * k7[i] + er8 * k8[i] + er9 * k9[i] + er10 * k10[i] +
+                   er11 * k2[i] + er12 * k3[i];
+            sqr = erri / sk;
+            err += sqr * sqr;
+        }
+        double deno = err + 0.01 * err2;
+        if (deno <= 0.0) deno = 1.0;
+        err = fabs(h) * err * sqrt(1.0 / (deno * (double)n));
+
+        /* step-size factor (:446-452) */
+        const double fac11 = pow(err, expo1);
+        double fac = fac11 / pow(facold, beta);
+        fac = max_d(facc2, min_d(facc1, fac / safe));
+        double hnew = h / fac;
+
+        if (err <= 1.0) {
+            facold = max_d(err, 1.0E-4);
+            naccpt++;
+            batch_rhs(pot, fr, nb, k5, k4);
+            nfcn++;
+
+            /* stiffness detection (:463-486); gala returns -4 on the first
+             * detection because the `return -4` sits outside the iasti == 15 test */
+            if (!(naccpt % nstiff) || (iasti > 0)) {
+                double stnum = 0.0, stden = 0.0;
+                for (int i = 0; i < n; i++) {
+                    sqr = k4[i] - k3[i];
+                    stnum += sqr * sqr;
+                    sqr = k5[i] - yy1[i];
+                    stden += sqr * sqr;
+                }
+                if (stden > 0.0) hlamb = h * sqrt(stnum / stden);
+                if (hlamb > 6.1) {
+                    nonsti = 0;
+                    iasti++;
+                    idid = -4;
+                    break;
+                } else {
+                    nonsti++;
+                    if (nonsti == 6) iasti = 0;
+                }
+            }
+
+            if (out) {
+                /* dense output coefficients (:492-582) */
+                for (int i = 0; i < n; i++) {
+                    rc1[i] = y[i];
+                    const double ydiff = k5[i] - y[i];
+                    rc2[i] = ydiff;
+                    const double bspl = h * k1[i] - ydiff;
+                    rc3[i] = bspl;
+                    rc4[i] = ydiff - h * k4[i] - bspl;
+                    rc5[i] = d41 * k1[i] + d46 * k6[i] + d47 * k7[i] + d48 * k8[i] + d49 * k9[i] +
+                             d410 * k10[i] + d411 * k2[i] + d412 * k3[i];
+                    rc6[i] = d51 * k1[i] + d56 * k6[i] + d57 * k7[i] + d58 * k8[i] + d59 * k9[i] +
+                             d510 * k10[i] + d511 * k2[i] + d512 * k3[i];
+                    rc7[i] = d61 * k1[i] + d66 * k6[i] + d67 * k7[i] + d68 * k8[i] + d69 * k9[i] +
+                             d610 * k10[i] + d611 * k2[i] + d612 * k3[i];
+                    rc8[i] = d71 * k1[i] + d76 * k6[i] + d77 * k7[i] + d78 * k8[i] + d79 * k9[i] +
+                             d710 * k10[i] + d711 * k2[i] + d712 * k3[i];
+                }
+                for (int i = 0; i < n; i++)
+                    yy1[i] = y[i] + h * (a141 * k1[i] + a147 * k7[i] + a148 * k8[i] + a149 * k9[i] +
+                                         a1410 * k10[i] + a1411 * k2[i] + a1412 * k3[i] + a1413 * k4[i]);
+                batch_rhs(pot, fr, nb, yy1, k10);
+                for (int i = 0; i < n; i++)
+                    yy1[i] = y[i] + h * (a151 * k1[i] + a156 * k6[i] + a157 * k7[i] + a158 * k8[i] +
+                                         a1511 * k2[i] + a1512 * k3[i] + a1513 * k4[i] + a1514 * k10[i]);
+                batch_rhs(pot, fr, nb, yy1, k2);
+                for (int i = 0; i < n; i++)
+                    yy1[i] = y[i] + h * (a161 * k1[i] + a166 * k6[i] + a167 * k7[i] + a168 * k8[i] +
+                                         a169 * k9[i] + a1613 * k4[i] + a1614 * k10[i] + a1615 * k2[i]);
+                batch_rhs(pot, fr, nb, yy1, k3);
+                nfcn += 3;
+                for (int i = 0; i < n; i++) {
+                    rc5[i] = h * (rc5[i] + d413 * k4[i] + d414 * k10[i] + d415 * k2[i] + d416 * k3[i]);
+                    rc6[i] = h * (rc6[i] + d513 * k4[i] + d514 * k10[i] + d515 * k2[i] + d516 * k3[i]);
+                    rc7[i] = h * (rc7[i] + d613 * k4[i] + d614 * k10[i] + d615 * k2[i] + d616 * k3[i]);
+                    rc8[i] = h * (rc8[i] + d713 * k4[i] + d714 * k10[i] + d715 * k2[i] + d716 * k3[i]);
+                }
+
+                /* fill every output time inside [xold, xold + hout] (:584-612)
+                 * with contd8_threadsafe (:869-904) */
+                const double x0 = xold, x1 = x0 + hout;
+                while (out_idx < ntimes) {
+                    const double t_out = t[out_idx];
+                    if ((x0 <= t_out && t_out <= x1) || (x1 <= t_out && t_out <= x0)) {
+                        if (out_idx % out_stride == 0) {
+                            const double s = (t_out - xold) / hout;
+                            const double s1 = 1.0 - s;
+                            double *o = out + (size_t)out_slot * (size_t)n;
+                            for (int i = 0; i < n; i++)
+                                o[i] = rc1[i] +
+                                       s * (rc2[i] +
+                                            s1 * (rc3[i] +
+                                                  s * (rc4[i] + s1 * (rc5[i] + s * (rc6[i] + s1 * (rc7[i] + s * rc8[i]))))));
+                            out_slot++;
+                        }
+                        out_idx++;
+                    } else {
+                        break;
+                    }
+                }
+            }
+
+            memcpy(k1, k4, (size_t)n * sizeof(double));
+            memcpy(y, k5, (size_t)n * sizeof(double));
+            x = xph;
+            if (last) { idid = 1; break; }
+            if (fabs(hnew) > hmax) hnew = posneg * hmax;
+            if (reject) hnew = posneg * min_d(fabs(hnew), fabs(h));
+            reject = 0;
+        } else {
+            hnew = h / min_d(facc1, fac11 / safe);
+            reject = 1;
+            if (naccpt >= 1) nrejct = nrejct + 1;
+            last = 0;
+        }
+        h = hnew;
+    }
+    (void)nonsti;
+    if (stats) {
+        stats[0] = nfcn;
+        stats[1] = nstep;
+        stats[2] = naccpt;
+        stats[3] = nrejct;
+    }
+    free(work);
+    return idid;
+}
+
+typedef struct {
+    const gx_potential *pot;
+    const gx_frame *fr;
+    const double *w0, *t;
+    int64_t n, ntimes, nmax, nstiff, out_stride, n_out;
+    double atol, rtol, dt_max;
+    int save_all, nbatch;
+    double *w_out;
+    int32_t *status;
+    long *stats; /* per batch {nfcn, nstep, naccpt, nrejct} or NULL */
+} dop_ctx;
+
+static void dop_chunk(void *vctx, int64_t blo, int64_t bhi) {
+    dop_ctx *C = (dop_ctx *)vctx;
+    const int64_t n = C->n;
+    for (int64_t b = blo; b < bhi; b++) {
+        const int64_t i0 = b * C->nbatch;
+        const int nb = (int)((i0 + C->nbatch <= n) ? C->nbatch : n - i0);
+        double *y = (double *)malloc(sizeof(double) * 6 * (size_t)nb);
+        for (int k = 0; k < 6; k++)
+            for (int j = 0; j < nb; j++) y[k * nb + j] = C->w0[k * n + i0 + j];
+        double *out = NULL;
+        if (C->save_all) out = (double *)malloc(sizeof(double) * 6 * (size_t)nb * (size_t)C->n_out);
+        int res = orc_dop853_batch(C->pot, C->fr, nb, y, C->t, C->ntimes, C->atol, C->rtol, C->nmax,
+                                   C->dt_max, C->nstiff, C->out_stride, out,
+                                   C->stats ? C->stats + 4 * b : NULL);
+        C->status[b] = res;
+        if (C->save_all) {
+            /* (n_out, 6, nb) -> (6, n_out, N) (dop853.pyx:187-193, 242-243) */
+            for (int64_t s = 0; s < C->n_out; s++)
+                for (int k = 0; k < 6; k++)
+                    for (int j = 0; j < nb; j++)
+                        C->w_out[(k * C->n_out + s) * n + i0 + j] = out[(s * 6 + k) * nb + j];
+            free(out);
+        } else {
+            for (int k = 0; k < 6; k++)
+                for (int j = 0; j < nb; j++) C->w_out[k * n + i0 + j] = y[k * nb + j];
+        }
+        free(y);
+    }
+}
+
+/* dop853_integrate_hamiltonian (dop853.pyx:196-250): batches of nbatch orbits,
+ * one dop853() call each; batches are spread over nthreads. */
+int orc_dop853_integrate(const gx_potential *pot, const gx_frame *fr, const double *w0, int64_t n,
+                         const double *t, int64_t ntimes, double atol, double rtol, int64_t nmax,
+                         double dt_max, int64_t nstiff, int save_all, int nbatch, int64_t out_stride,
+                         double *w_out, int32_t *status, long *stats, int nthreads) {
+    if (ntimes < 2 || nbatch < 1 || out_stride < 1) return -1;
+    dop_ctx C;
+    C.pot = pot;
+    C.fr = fr;
+    C.w0 = w0;
+    C.t = t;
+    C.n = n;
+    C.ntimes = ntimes;
+    C.nmax = nmax;
+    C.nstiff = nstiff;
+    C.out_stride = out_stride;
+    C.n_out = (ntimes - 1) / out_stride + 1;
+    C.atol = atol;
+    C.rtol = rtol;
+    C.dt_max = dt_max;
+    C.save_all = save_all;
+    C.nbatch = nbatch;
+    C.w_out = w_out;
+    C.status = status;
+    C.stats = stats;
+    const int64_t nbatches = (n + nbatch - 1) / nbatch;
+    parallel_for(nthreads, nbatches, 1, dop_chunk, &C);
+    return 0;
+}
+
+/* Batched potential evaluation helpers for the tests: q (3, N) SoA. */
+void orc_potential_value_n(const gx_potential *pot, double t, const double *q, int64_t N, double *out) {
+    for (int64_t i = 0; i < N; i++) {
+        double qi[3] = {q[i], q[N + i], q[2 * N + i]};
+        out[i] = orc_potential(pot, t, qi);
+    }
+}
+
+void orc_potential_density_n(const gx_potential *pot, double t, const double *q, int64_t N, double *out) {
+    for (int64_t i = 0; i < N; i++) {
+        double qi[3] = {q[i], q[N + i], q[2 * N + i]};
+        out[i] = orc_density(pot, t, qi);
+    }
+}
+
+void orc_hamiltonian_value_n(const gx_potential *pot, const gx_frame *fr, double t, const double *w,
+                             int64_t N, double *out) {
+    for (int64_t i = 0; i < N; i++) {
+        double wi[6];
+        for (int k = 0; k < 6; k++) wi[k] = w[k * N + i];
+        out[i] = orc_hamiltonian_value(pot, fr, t, wi);
+    }
+}

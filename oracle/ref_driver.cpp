@@ -1,0 +1,362 @@
+/*
+ * ORACLE (test infrastructure only): a driver around gala's OWN compiled C/C++
+ * (cpotential.cpp, builtin_potentials.cpp, builtin_frames.cpp, cframe.cpp,
+ * chamiltonian.cpp, dopri/dop853.cpp), built by oracle/Makefile straight from the
+ * gala sources into oracle/_ref/libgalaref.so.  It is used to pin the C
+ * restatement (gx_oracle.c) and to generate the golden fixtures in tests/golden/.
+ *
+ * What this file adds is only the glue that gala's Cython layer provides:
+ *   - a CPotential built the way CPotentialWrapper.init / CCompositePotentialWrapper
+ *     build it (src/gala/potential/potential/cpotential.pyx:57-102,
+ *     ccompositepotential.pyx:27-67), from the gx_potential descriptor;
+ *   - the Leapfrog and Ruth4 driver loops of leapfrog.pyx:24-121 and
+ *     ruth4.pyx:24-113 (Cython that cannot be compiled without gala's Python
+ *     package), calling gala's c_gradient;
+ *   - dop853_integrate_hamiltonian / dop853_helper (dop853.pyx:90-250): one call
+ *     of gala's dop853() per batch of nbatch orbits with exactly that argument
+ *     list, Fwrapper_T as the right-hand side and a dense-output state.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "potential/src/cpotential.h"
+#include "frame/src/cframe.h"
+#include "hamiltonian/src/chamiltonian.h"
+#include "dopri/dop853.h"
+#include "potential/builtin/builtin_potentials.h"
+#include "frame/builtin/builtin_frames.h"
+
+#include "../include/gala_gb300.h"
+
+namespace {
+
+struct RefPot {
+    CPotential *cp;
+    CFrameType cf;
+    double frame_params[3];
+};
+
+bool set_funcs(CPotential *cp, int i, int type) {
+    switch (type) {
+    case GX_POT_NULL:
+        cp->value[i] = null_value; cp->density[i] = null_density;
+        cp->gradient[i] = null_gradient; cp->hessian[i] = null_hessian;
+        return true;
+    case GX_POT_KEPLER:
+        cp->value[i] = kepler_value; cp->density[i] = kepler_density;
+        cp->gradient[i] = kepler_gradient; cp->hessian[i] = kepler_hessian;
+        return true;
+    case GX_POT_HERNQUIST:
+        cp->value[i] = hernquist_value; cp->density[i] = hernquist_density;
+        cp->gradient[i] = hernquist_gradient; cp->hessian[i] = hernquist_hessian;
+        return true;
+    case GX_POT_PLUMMER:
+        cp->value[i] = plummer_value; cp->density[i] = plummer_density;
+        cp->gradient[i] = plummer_gradient; cp->hessian[i] = plummer_hessian;
+        return true;
+    case GX_POT_MIYAMOTONAGAI:
+        cp->value[i] = miyamotonagai_value; cp->density[i] = miyamotonagai_density;
+        cp->gradient[i] = miyamotonagai_gradient; cp->hessian[i] = miyamotonagai_hessian;
+        return true;
+    case GX_POT_SPHERICALNFW:
+        cp->value[i] = sphericalnfw_value; cp->density[i] = sphericalnfw_density;
+        cp->gradient[i] = sphericalnfw_gradient; cp->hessian[i] = sphericalnfw_hessian;
+        return true;
+    case GX_POT_FLATTENEDNFW:
+        cp->value[i] = flattenednfw_value; cp->density[i] = nan_density;
+        cp->gradient[i] = flattenednfw_gradient; cp->hessian[i] = flattenednfw_hessian;
+        return true;
+    case GX_POT_TRIAXIALNFW:
+        cp->value[i] = triaxialnfw_value; cp->density[i] = nan_density;
+        cp->gradient[i] = triaxialnfw_gradient; cp->hessian[i] = triaxialnfw_hessian;
+        return true;
+    default:
+        return false; /* SCF needs GSL inside gala: not buildable here */
+    }
+}
+
+bool build(const gx_potential *pot, const gx_frame *fr, RefPot *rp) {
+    const int nc = pot->n_components;
+    rp->cp = allocate_cpotential(nc > 0 ? nc : 1);
+    CPotential *cp = rp->cp;
+    cp->n_dim = 3;
+    cp->null = 0;
+    for (int i = 0; i < nc; i++) {
+        const gx_component *c = &pot->components[i];
+        if (!set_funcs(cp, i, c->type)) return false;
+        cp->n_params[i] = c->n_params;
+        cp->parameters[i] = const_cast<double *>(pot->params + c->param_offset);
+        cp->q0[i] = const_cast<double *>(c->q0);
+        cp->R[i] = const_cast<double *>(c->R);
+        cp->state[i] = NULL;
+        cp->do_shift_rotate[i] = c->do_shift_rotate;
+    }
+    if (fr == NULL || fr->type == GX_FRAME_STATIC) {
+        rp->cf.energy = (energyfunc)static_frame_hamiltonian;
+        rp->cf.gradient = (gradientfunc)static_frame_gradient;
+        rp->cf.hessian = (hessianfunc)static_frame_hessian;
+        rp->cf.n_params = 0;
+        rp->frame_params[0] = rp->frame_params[1] = rp->frame_params[2] = 0.;
+    } else {
+        rp->cf.energy = (energyfunc)constant_rotating_frame_3d_hamiltonian;
+        rp->cf.gradient = (gradientfunc)constant_rotating_frame_3d_gradient;
+        rp->cf.hessian = (hessianfunc)constant_rotating_frame_3d_hessian;
+        rp->cf.n_params = 3;
+        memcpy(rp->frame_params, fr->params, sizeof(rp->frame_params));
+    }
+    rp->cf.parameters = rp->frame_params;
+    return true;
+}
+
+void release(RefPot *rp) {
+    if (rp->cp) free_cpotential(rp->cp);
+    rp->cp = NULL;
+}
+
+typedef void (*range_fn)(void *ctx, int64_t lo, int64_t hi);
+struct Pool {
+    range_fn fn;
+    void *ctx;
+    int64_t n, chunk, next;
+    pthread_mutex_t mu;
+};
+
+void *worker(void *arg) {
+    Pool *P = (Pool *)arg;
+    for (;;) {
+        pthread_mutex_lock(&P->mu);
+        int64_t lo = P->next;
+        P->next += P->chunk;
+        pthread_mutex_unlock(&P->mu);
+        if (lo >= P->n) break;
+        P->fn(P->ctx, lo, lo + P->chunk < P->n ? lo + P->chunk : P->n);
+    }
+    return NULL;
+}
+
+void parallel_for(int nthreads, int64_t n, int64_t chunk, range_fn fn, void *ctx) {
+    if (nthreads <= 1 || n <= chunk) {
+        fn(ctx, 0, n);
+        return;
+    }
+    Pool P;
+    P.fn = fn; P.ctx = ctx; P.n = n; P.chunk = chunk; P.next = 0;
+    pthread_mutex_init(&P.mu, NULL);
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * nthreads);
+    for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, worker, &P);
+    for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+    free(th);
+    pthread_mutex_destroy(&P.mu);
+}
+
+struct FixedCtx {
+    const gx_potential *pot;
+    const double *w0, *t;
+    int64_t n, ntimes;
+    int save_all, method;
+    double *w_out;
+    int failed;
+};
+
+/* leapfrog.pyx:54-121 / ruth4.pyx:37-113 on orbits [lo, hi): the Cython loops,
+ * restated, each step calling gala's c_gradient over the chunk. */
+void fixed_chunk(void *vctx, int64_t lo, int64_t hi) {
+    FixedCtx *C = (FixedCtx *)vctx;
+    RefPot rp;
+    if (!build(C->pot, NULL, &rp)) { C->failed = 1; release(&rp); return; }
+    CPotential *cp = rp.cp;
+    const int64_t n = C->n, ntimes = C->ntimes;
+    const size_t m = (size_t)(hi - lo);
+    const double dt = C->t[1] - C->t[0];
+    double *tmp_w = (double *)malloc(sizeof(double) * 6 * m);
+    double *v_jm1_2 = (double *)calloc(3 * m, sizeof(double));
+    double *grad = (double *)calloc(3 * m, sizeof(double));
+    for (int k = 0; k < 6; k++)
+        for (size_t i = 0; i < m; i++) tmp_w[k * m + i] = C->w0[k * n + lo + i];
+    if (C->save_all)
+        for (int k = 0; k < 6; k++)
+            for (size_t i = 0; i < m; i++) C->w_out[(k * ntimes + 0) * n + lo + i] = tmp_w[k * m + i];
+    if (C->method == 0) {
+        double *x = tmp_w, *v = tmp_w + 3 * m;
+        c_gradient(cp, m, C->t[0], x, grad);
+        for (int k = 0; k < 3; k++)
+            for (size_t i = 0; i < m; i++) v_jm1_2[i + k * m] = v[i + k * m] - grad[i + k * m] * dt / 2.;
+        for (int64_t j = 1; j < ntimes; j++) {
+            memset(grad, 0, sizeof(double) * 3 * m);
+            for (int k = 0; k < 3; k++)
+                for (size_t i = 0; i < m; i++) x[i + k * m] = x[i + k * m] + v_jm1_2[i + k * m] * dt;
+            c_gradient(cp, m, C->t[j], x, grad);
+            for (int k = 0; k < 3; k++)
+                for (size_t i = 0; i < m; i++) {
+                    v[i + k * m] = v_jm1_2[i + k * m] - grad[i + k * m] * dt / 2.;
+                    v_jm1_2[i + k * m] = v_jm1_2[i + k * m] - grad[i + k * m] * dt;
+                }
+            if (C->save_all)
+                for (int k = 0; k < 6; k++)
+                    for (size_t i = 0; i < m; i++) C->w_out[(k * ntimes + j) * n + lo + i] = tmp_w[k * m + i];
+        }
+    } else {
+        const double two_13 = pow(2., 1. / 3.);
+        const double cs[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
+                              (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};
+        const double ds[4] = {0., 1. / (2. - two_13), -two_13 / (2. - two_13), 1. / (2. - two_13)};
+        double *w = tmp_w;
+        for (int64_t j = 1; j < ntimes; j++) {
+            memset(grad, 0, sizeof(double) * 3 * m);
+            for (int s = 0; s < 4; s++) {
+                c_gradient(cp, m, C->t[j], w, grad);
+                for (int k = 0; k < 3; k++)
+                    for (size_t i = 0; i < m; i++) {
+                        w[(3 + k) * m + i] = w[(3 + k) * m + i] - ds[s] * grad[k * m + i] * dt;
+                        w[k * m + i] = w[k * m + i] + cs[s] * w[(3 + k) * m + i] * dt;
+                    }
+            }
+            if (C->save_all)
+                for (int k = 0; k < 6; k++)
+                    for (size_t i = 0; i < m; i++) C->w_out[(k * ntimes + j) * n + lo + i] = tmp_w[k * m + i];
+        }
+    }
+    if (!C->save_all)
+        for (int k = 0; k < 6; k++)
+            for (size_t i = 0; i < m; i++) C->w_out[k * n + lo + i] = tmp_w[k * m + i];
+    free(tmp_w);
+    free(v_jm1_2);
+    free(grad);
+    release(&rp);
+}
+
+struct DopCtx {
+    const gx_potential *pot;
+    const gx_frame *fr;
+    const double *w0, *t;
+    int64_t n, ntimes, nmax, nstiff;
+    double atol, rtol, dt_max;
+    int save_all, nbatch;
+    double *w_out;
+    int32_t *status;
+};
+
+/* dop853_integrate_hamiltonian's batch loop (dop853.pyx:228-245) calling
+ * dop853_helper (:90-193) for batches [blo, bhi). */
+void dop_chunk(void *vctx, int64_t blo, int64_t bhi) {
+    DopCtx *C = (DopCtx *)vctx;
+    RefPot rp;
+    if (!build(C->pot, C->fr, &rp)) {
+        for (int64_t b = blo; b < bhi; b++) C->status[b] = -100;
+        release(&rp);
+        return;
+    }
+    const int64_t n = C->n, ntimes = C->ntimes;
+    for (int64_t b = blo; b < bhi; b++) {
+        const int64_t i0 = b * C->nbatch;
+        const unsigned nb = (unsigned)((i0 + C->nbatch <= n) ? C->nbatch : n - i0);
+        const unsigned size = 6 * nb;
+        double *w = (double *)malloc(sizeof(double) * size);
+        for (int k = 0; k < 6; k++)
+            for (unsigned j = 0; j < nb; j++) w[k * nb + j] = C->w0[k * n + i0 + j];
+        double *output_w = NULL;
+        Dop853DenseState *state = NULL;
+        unsigned nrdens = 0;
+        if (C->save_all) {
+            output_w = (double *)malloc(sizeof(double) * size * (size_t)ntimes);
+            state = dop853_dense_state_alloc(size, size);
+            nrdens = size;
+        }
+        double rtol = C->rtol, atol = C->atol;
+        int res = dop853(size, (FcnEqDiff)Fwrapper_T, rp.cp, &rp.cf, nb, 0, NULL, C->t[0], w,
+                         C->t[ntimes - 1], &rtol, &atol, 0, NULL, 0, NULL,
+                         2.220446049250313e-16, 0.0, 0.0, 0.0, 0.0, C->dt_max, C->t[1] - C->t[0],
+                         (long)C->nmax, 1, (long)C->nstiff, nrdens, NULL, 0, state,
+                         const_cast<double *>(C->t), (int)ntimes, output_w);
+        C->status[b] = res;
+        if (C->save_all) {
+            for (int64_t s = 0; s < ntimes; s++)
+                for (int k = 0; k < 6; k++)
+                    for (unsigned j = 0; j < nb; j++)
+                        C->w_out[(k * ntimes + s) * n + i0 + j] = output_w[(s * 6 + k) * nb + j];
+            free(output_w);
+            dop853_dense_state_free(state, size);
+        } else {
+            for (int k = 0; k < 6; k++)
+                for (unsigned j = 0; j < nb; j++) C->w_out[k * n + i0 + j] = w[k * nb + j];
+        }
+        free(w);
+    }
+    release(&rp);
+}
+
+} // namespace
+
+extern "C" {
+
+/* c_gradient over N points, q (3, N) -> grad (3, N). Returns 0, or -1 when a
+ * component type has no gala build here (SCF needs GSL). */
+int ref_gradient(const gx_potential *pot, int64_t N, double t, const double *q, double *grad) {
+    RefPot rp;
+    if (!build(pot, NULL, &rp)) { release(&rp); return -1; }
+    c_gradient(rp.cp, (size_t)N, t, const_cast<double *>(q), grad);
+    release(&rp);
+    return 0;
+}
+
+/* c_potential / c_density at each column of q (3, N). */
+int ref_potential_value_n(const gx_potential *pot, double t, const double *q, int64_t N, double *out) {
+    RefPot rp;
+    if (!build(pot, NULL, &rp)) { release(&rp); return -1; }
+    for (int64_t i = 0; i < N; i++) {
+        double qi[3] = {q[i], q[N + i], q[2 * N + i]};
+        out[i] = c_potential(rp.cp, t, qi);
+    }
+    release(&rp);
+    return 0;
+}
+
+int ref_potential_density_n(const gx_potential *pot, double t, const double *q, int64_t N, double *out) {
+    RefPot rp;
+    if (!build(pot, NULL, &rp)) { release(&rp); return -1; }
+    for (int64_t i = 0; i < N; i++) {
+        double qi[3] = {q[i], q[N + i], q[2 * N + i]};
+        out[i] = c_density(rp.cp, t, qi);
+    }
+    release(&rp);
+    return 0;
+}
+
+/* hamiltonian_gradient_T over w (6, N) -> f (6, N). */
+int ref_hamiltonian_gradient(const gx_potential *pot, const gx_frame *fr, int64_t N, double t,
+                             const double *w, double *f) {
+    RefPot rp;
+    if (!build(pot, fr, &rp)) { release(&rp); return -1; }
+    hamiltonian_gradient_T(rp.cp, &rp.cf, (size_t)N, t, const_cast<double *>(w), f);
+    release(&rp);
+    return 0;
+}
+
+/* leapfrog (method 0) / ruth4 (method 1) integrate_hamiltonian. */
+int ref_fixed_integrate(const gx_potential *pot, int method, const double *w0, int64_t n,
+                        const double *t, int64_t ntimes, int save_all, double *w_out, int nthreads) {
+    FixedCtx C = {pot, w0, t, n, ntimes, save_all, method, w_out, 0};
+    int64_t chunk = 256;
+    if (nthreads > 1 && n / nthreads < chunk) chunk = (n + nthreads - 1) / nthreads;
+    if (chunk < 1) chunk = 1;
+    parallel_for(nthreads, n, chunk, fixed_chunk, &C);
+    return C.failed ? -1 : 0;
+}
+
+/* dop853_integrate_hamiltonian with gala's full-grid dense output. */
+int ref_dop853_integrate(const gx_potential *pot, const gx_frame *fr, const double *w0, int64_t n,
+                         const double *t, int64_t ntimes, double atol, double rtol, int64_t nmax,
+                         double dt_max, int64_t nstiff, int save_all, int nbatch, double *w_out,
+                         int32_t *status, int nthreads) {
+    DopCtx C;
+    C.pot = pot; C.fr = fr; C.w0 = w0; C.t = t; C.n = n; C.ntimes = ntimes;
+    C.nmax = nmax; C.nstiff = nstiff; C.atol = atol; C.rtol = rtol; C.dt_max = dt_max;
+    C.save_all = save_all; C.nbatch = nbatch; C.w_out = w_out; C.status = status;
+    parallel_for(nthreads, (n + nbatch - 1) / nbatch, 1, dop_chunk, &C);
+    return 0;
+}
+
+} // extern "C"

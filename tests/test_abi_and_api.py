@@ -1,0 +1,130 @@
+"""CPU tests: the C-ABI library exports what include/gala_gb300.h declares, the
+ctypes mirror matches the header, and the host-side API behaves like gala's."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import gala_gb300 as g
+from gala_gb300 import _abi
+from gala_gb300.integrate import parse_time_specification
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _declared_functions():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(gx_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    lib = _abi.load()  # builds with nvcc if needed; loads without touching a GPU
+    declared = _declared_functions()
+    assert declared, "no declarations found"
+    missing = [n for n in declared if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(_abi.SIGNATURES) >= declared, declared - set(_abi.SIGNATURES)
+    assert lib.gx_abi_version() == 1
+
+
+def test_struct_layout_matches_header():
+    # gx_component: 4+4+8+4+4 + 3*8 + 9*8 = 120 bytes, 8-byte aligned
+    assert C.sizeof(_abi.gx_component) == 120
+    assert _abi.gx_component.q0.offset == 24
+    assert C.sizeof(_abi.gx_potential) == 40
+    assert C.sizeof(_abi.gx_frame) == 32
+
+
+def test_invalid_descriptor_is_rejected_without_gpu():
+    """Argument validation happens on the host before any CUDA call."""
+    lib = _abi.load()
+    pot = g.HernquistPotential(m=1e11, c=1.0)
+    desc = pot.packed().desc
+    desc.n_dim = 2
+    rc = lib.gx_potential_value(C.byref(desc), 0.0, None, 10, None, None)
+    assert rc == _abi.GX_ERR_INVALID_ARGUMENT
+    assert b"n_dim" in lib.gx_last_error_message()
+    desc.n_dim = 3
+    rc = lib.gx_dop853_integrate_hamiltonian(C.byref(desc), None, None, 10, None, 100, 1e-10, 1e-10, 0, 0.0, 0, 1,
+                                             0, 1, None, None, None, None)
+    assert rc == _abi.GX_ERR_INVALID_ARGUMENT
+    assert b"nbatch" in lib.gx_last_error_message()
+
+
+def test_parameter_packing_is_gala_layout():
+    G = g.units.G
+    assert np.array_equal(g.HernquistPotential(m=2.0, c=3.0).packed().params, [G, 2.0, 3.0])
+    assert np.array_equal(g.MiyamotoNagaiPotential(1.0, 2.0, 3.0).packed().params, [G, 1.0, 2.0, 3.0])
+    nfw = g.NFWPotential(m=5.0, r_s=2.0)
+    assert np.array_equal(nfw.packed().params, [G, 5.0, 2.0, 1.0, 1.0, 1.0])
+    assert nfw.packed().components[0].type == _abi.GX_POT_SPHERICALNFW
+    assert g.NFWPotential(m=5.0, r_s=2.0, c=0.9).packed().components[0].type == _abi.GX_POT_FLATTENEDNFW
+    assert g.NFWPotential(m=5.0, r_s=2.0, a=1.1, c=0.9).packed().components[0].type == _abi.GX_POT_TRIAXIALNFW
+    S = np.arange(8.0).reshape(2, 2, 2)
+    scf = g.SCFPotential(m=1.0, r_s=2.0, Snlm=S, Tnlm=-S)
+    p = scf.packed().params
+    assert np.array_equal(p[:5], [G, 1.0, 1.0, 1.0, 2.0])
+    assert np.array_equal(p[5:13], S.ravel()) and np.array_equal(p[13:], -S.ravel())
+
+
+def test_composite_order_and_shift_flag():
+    mw = g.MilkyWayPotential()
+    pk = mw.packed()
+    assert [pk.components[i].type for i in range(4)] == [_abi.GX_POT_MIYAMOTONAGAI, _abi.GX_POT_HERNQUIST,
+                                                         _abi.GX_POT_HERNQUIST, _abi.GX_POT_SPHERICALNFW]
+    assert all(pk.components[i].do_shift_rotate == 0 for i in range(4))
+    sh = g.HernquistPotential(m=1.0, c=1.0, origin=[1.0, 0, 0])
+    assert sh.packed().components[0].do_shift_rotate == 1
+    with pytest.raises(ValueError):
+        mw["extra"] = g.NullPotential()
+    comp = g.HernquistPotential(m=1.0, c=1.0) + g.PlummerPotential(m=1.0, b=1.0)
+    assert len(comp) == 2
+
+
+@pytest.mark.parametrize("kw,expected", [
+    (dict(dt=0.5, n_steps=4), np.cumsum(np.append([0.0], np.ones(5) * 0.5))[:-1]),
+    (dict(dt=0.5, n_steps=4, t1=10.0), np.cumsum(np.append([0.0], np.ones(5) * 0.5))[:-1] + 10.0),
+    (dict(dt=1.0, t1=0.0, t2=3.5), np.array([0.0, 1.0, 2.0, 3.0])),
+    (dict(dt=-1.0, t1=3.0, t2=0.5), np.array([3.0, 2.0, 1.0, 0.5])),
+    (dict(n_steps=5, t1=0.0, t2=1.0), np.linspace(0, 1, 5)),
+    (dict(t=np.array([0.0, 2.0, 5.0])), np.array([0.0, 2.0, 5.0])),
+])
+def test_time_specification_like_gala(kw, expected):
+    assert np.array_equal(parse_time_specification(None, **kw), expected)
+
+
+def test_time_specification_errors():
+    with pytest.raises(ValueError):
+        parse_time_specification(None, dt=0.0, t1=0.0, t2=1.0)
+    with pytest.raises(ValueError):
+        parse_time_specification(None, dt=1.0, t1=1.0, t2=0.0)
+    with pytest.raises(ValueError):
+        parse_time_specification(None, n_steps=10)
+
+
+def test_integrator_lookup():
+    assert g.get_integrator("LeapFrog") is g.LeapfrogIntegrator
+    assert g.get_integrator("dop853") is g.DOPRI853Integrator
+    assert g.get_integrator("dopri853") is g.DOPRI853Integrator
+    assert g.get_integrator(g.Ruth4Integrator) is g.Ruth4Integrator
+    with pytest.raises(ValueError):
+        g.get_integrator("euler")
+
+
+def test_product_path_fails_loudly_without_gpu():
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    pot = g.HernquistPotential(m=1e11, c=1.0)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        pot.integrate_orbit(np.ones((6, 2)), dt=1.0, n_steps=10)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        pot.gradient(np.ones((3, 2)))

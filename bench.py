@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""Benchmark: orbit-steps/s of gala's orbit-integration hot path on one GB300.
+
+Workload (default ``mw_dop853``): the Milky-Way-like composite (nucleus
+Hernquist 1.7e9/0.07 + bulge Hernquist 5e9/1 + Miyamoto-Nagai 6.8e10/3/0.28 +
+NFW 5.4e11/15.6), 100,000 orbits per GPU with R ~ U[2, 30] kpc, |z| < 2 kpc,
+v = v_c(R) + N(0, 30 km/s), DOP853 (rtol 1e-10, atol 1e-12) in FP64 with gala's
+100-orbit batches, dt = 0.5 Myr, n_steps = 10,000, every 100th output kept.
+One step = one full integration of that workload (1e9 orbit-steps per GPU).
+
+Arms
+  default           the CUDA library; ``value`` is device throughput with inputs
+                    resident in HBM, ``e2e`` goes through the public API
+                    (Hamiltonian.integrate_orbit) with host numpy in and out.
+  --impl reference  gala's algorithm on the host cores: the C restatement of
+                    gala's integrators built with gala's flags (-Ofast), all
+                    host threads, a bounded sample of the same workload per step.
+
+Multi-GPU (torchrun): orbits are independent, so every rank integrates its own
+100,000-orbit shard (weak scaling, no data-path collective); the time is the
+max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "orbit-steps/s on 1 GB300: FP32+surrogate vs plain FP64 at ΔE/E≤1e-6"
+UNIT = "orbit-steps/s"
+
+# Algorithmic FP64 work of the DOP853 path, counted from gala's expressions with
+# every add, multiply, divide, sqrt, log and pow counted as one flop:
+F_RHS_MW = 2 * 17 + 21 + 26 + 6   # composite gradient (Hernquist x2, MN, NFW) + Hamiltonian copy/negate
+F_STEP_PER_ORBIT = 6 * 159        # 12 stages (111), 8th-order update (17), error terms (31), per component
+F_DENSE_PER_ORBIT = 6 * 153       # dense-output coefficients and the 3 extra stages, per accepted step
+F_OUTPUT_PER_ORBIT = 6 * 14 + 2   # one contd8 evaluation of 6 components
+
+
+def parse_args():
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gx", choices=["gx", "reference"])
+    p.add_argument("--orbits", type=int, default=100_000)
+    p.add_argument("--nsteps", type=int, default=10_000)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=8.0, help="target CPU time of one reference step")
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi samples (every 200 ms) of SM clock and throttle reasons."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measure_fp64_peak(torch, stream):
+    """FP64 multiply-add throughput (TFLOP/s) from the library's FMA-chain probe."""
+    from gala_gb300 import _abi
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 4096
+    sink = torch.zeros(blocks * threads, dtype=torch.float64, device="cuda")
+    h = int(stream.cuda_stream)
+    for _ in range(2):
+        _abi.call("gx_calibrate_fma", 1, blocks, threads, iters, int(sink.data_ptr()), h)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = None
+    for _ in range(3):
+        e0.record(stream)
+        _abi.call("gx_calibrate_fma", 1, blocks, threads, iters, int(sink.data_ptr()), h)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    flops = 16.0 * iters * blocks * threads
+    return flops / (best * 1e-3) / 1e12
+
+
+def cpu_reference_run(n_orbits, nsteps, target_s, steps, warmup):
+    """gala's DOP853 on the host cores (restatement built with -Ofast), bounded sample."""
+    from gala_gb300 import workloads as W
+    from gala_gb300.integrate import parse_time_specification
+    from oracle import Oracle
+    from oracle.oracle import host_threads
+
+    fast = Oracle("fast")
+    nthreads = host_threads()
+    mw = W.mw_composite()
+    t = parse_time_specification(dt=0.5, n_steps=nsteps)
+    w0_all = W.mw_ics(n_orbits)
+    # size the sample: one batch timed alone, then whole batches for ~target_s
+    probe = w0_all[:, :100]
+    t0 = time.perf_counter()
+    fast.dop853(mw, probe, t, atol=1e-12, rtol=1e-10, out_stride=100, nthreads=1)
+    one = time.perf_counter() - t0
+    nb = int(max(nthreads, min(n_orbits // 100, round(target_s * nthreads / max(one, 1e-3)))))
+    nb = max(nthreads, (nb // nthreads) * nthreads)
+    sample = np.ascontiguousarray(w0_all[:, : nb * 100])
+    times = []
+    out = None
+    for i in range(warmup + steps):
+        t0 = time.perf_counter()
+        out, st, _ = fast.dop853(mw, sample, t, atol=1e-12, rtol=1e-10, out_stride=100, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        if i >= warmup:
+            times.append(dt)
+    per = float(np.mean(times))
+    return {
+        "value": sample.shape[1] * nsteps / per,
+        "unit": UNIT,
+        "cores": nthreads,
+        "kind": "port",
+        "sample": f"{nb} batches x 100 orbits of the workload ({sample.shape[1]} orbits x {nsteps} steps), "
+                  f"gala's DOP853 restated in C, -Ofast, {nthreads} threads",
+        "seconds_per_step": per,
+        "sample_orbits": int(sample.shape[1]),
+    }, sample, out
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    base, _, _ = cpu_reference_run(args.orbits, args.nsteps, args.cpu_seconds, args.steps, args.warmup)
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": base["value"],
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": base["seconds_per_step"] * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "mw_dop853: MW composite, DOP853 rtol 1e-10 atol 1e-12 FP64, 100-orbit batches, "
+                               f"dt 0.5 Myr, {args.nsteps} steps, every 100th output kept",
+                   "orbits_per_gpu": args.orbits, "sample_orbits": base["sample_orbits"]},
+        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gx(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import gala_gb300 as g
+    from gala_gb300 import _abi
+    from gala_gb300 import workloads as W
+
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    sh = int(stream.cuda_stream)
+    mw = W.mw_composite()
+    n, nsteps, stride, nbatch = args.orbits, args.nsteps, 100, 100
+    w0 = W.mw_ics(n, seed=W.SEED_BASE + 2 + 1000 * rank)
+    t = g.parse_time_specification(dt=0.5, n_steps=nsteps)
+    ntimes = len(t)
+    n_out = (ntimes - 1) // stride + 1
+    nb = (n + nbatch - 1) // nbatch
+
+    w0d = torch.from_numpy(w0).to(dev)
+    td = torch.from_numpy(t).to(dev)
+    out = torch.empty((6, n_out, n), dtype=torch.float64, device=dev)
+    status = torch.zeros(nb, dtype=torch.int32, device=dev)
+    stats = torch.zeros((nb, 4), dtype=torch.int64, device=dev)
+    desc = mw.packed().for_device()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+
+    def launch():
+        _abi.call("gx_dop853_integrate_hamiltonian", desc, None, int(w0d.data_ptr()), n, int(td.data_ptr()),
+                  ntimes, 1e-12, 1e-10, 0, 0.0, 0, 1, nbatch, stride, int(out.data_ptr()), int(status.data_ptr()),
+                  int(stats.data_ptr()), sh)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        launch()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        wall0 = time.perf_counter()
+        for e0, e1 in ev:
+            flush.zero_()                     # evict L2 between timed iterations (not timed)
+            e0.record(stream)
+            launch()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    barrier()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+    mean_ms = float(np.mean(step_ms))
+    if world > 1:
+        tt = torch.tensor([mean_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        mean_ms = float(tt.item())
+    st = status.cpu().numpy()
+    if np.any(st != 1):
+        raise RuntimeError(f"integration failed in {int(np.sum(st != 1))} batches: {np.unique(st)}")
+    stt = stats.cpu().numpy()
+    nb_sizes = np.full(nb, nbatch, dtype=np.int64)
+    nb_sizes[-1] = n - nbatch * (nb - 1)
+    flops = float(np.sum(nb_sizes * (stt[:, 0] * F_RHS_MW + stt[:, 1] * F_STEP_PER_ORBIT +
+                                     stt[:, 2] * F_DENSE_PER_ORBIT)) + n * n_out * F_OUTPUT_PER_ORBIT)
+    value = n * nsteps * world / (mean_ms * 1e-3)
+
+    # energy conservation of this run (first vs last kept output), on the GPU
+    H = g.Hamiltonian(mw)
+    E0 = H.energy(out[:, 0, :].cpu().numpy())
+    E1 = H.energy(out[:, -1, :].cpu().numpy())
+    dE = np.abs((E1 - E0) / E0)
+
+    # end to end through the public API: host numpy in, Orbit with host arrays out
+    e2e_ms = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        orbit = mw.integrate_orbit(w0, dt=0.5, n_steps=nsteps, Integrator="dop853",
+                                   Integrator_kwargs=dict(atol=1e-12, rtol=1e-10, out_stride=stride))
+        wout = orbit.w()
+        dt_ = (time.perf_counter() - t0) * 1e3
+        if i >= args.warmup:
+            e2e_ms.append(dt_)
+    e2e_mean = float(np.mean(e2e_ms))
+    if world > 1:
+        tt = torch.tensor([e2e_mean], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_mean = float(tt.item())
+    same = bool(np.array_equal(wout, out.cpu().numpy()))
+
+    peak = measure_fp64_peak(torch, stream)
+    achieved = flops / (mean_ms * 1e-3) / 1e12
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": mean_ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded ICs, no dataset)",
+        "config": {
+            "workload": "mw_dop853: MW composite, DOP853 rtol 1e-10 atol 1e-12 FP64 (plain drop-in form), "
+                        f"100-orbit batches, dt 0.5 Myr, {nsteps} steps, every 100th output kept",
+            "orbits_per_gpu": n, "n_steps": nsteps, "out_stride": stride, "nbatch": nbatch,
+            "l2": "flushed (256 MB write) between timed iterations",
+        },
+        "e2e": {"value": n * nsteps * world / (e2e_mean * 1e-3), "unit": UNIT,
+                "h2d_bytes_per_step": int(w0.nbytes + t.nbytes),
+                "d2h_bytes_per_step": int(wout.nbytes + status.numel() * 4),
+                "ms_per_step": e2e_mean, "matches_device_run": same},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "peak_source": "FP64 FMA-chain probe (gx_calibrate_fma), same run",
+                     "work": "algorithmic FP64 flops from the kernel's nfcn/nstep/naccpt counters, "
+                             "transcendentals counted as 1 flop"},
+        "accuracy": {"dE_over_E_median": float(np.median(dE)), "dE_over_E_p99": float(np.percentile(dE, 99))},
+        "dop853_counters": {"nfcn_per_orbit": float(np.mean(stt[:, 0])), "accepted": float(np.mean(stt[:, 2])),
+                            "rejected": float(np.mean(stt[:, 3]))},
+        "clocks": clocks.summary(),
+        "wall_s_timed_region": wall,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        base, sample, cpu_out = cpu_reference_run(n, nsteps, args.cpu_seconds, 1, 0)
+        gpu_sample = out[:, :, : sample.shape[1]].cpu().numpy()
+        rel = np.linalg.norm(gpu_sample - cpu_out, axis=0) / np.linalg.norm(cpu_out, axis=0)
+        base["gpu_vs_cpu_max_rel"] = float(np.max(rel))
+        line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample",
+                                                     "gpu_vs_cpu_max_rel")}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gx(args)
+
+
+if __name__ == "__main__":
+    main()

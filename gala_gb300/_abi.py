@@ -79,6 +79,7 @@ SIGNATURES = {
     "gx_hamiltonian_gradient": (C.c_int, [_PP, _PF, _D, _P, _I64, _P, _P]),
     "gx_leapfrog_integrate_hamiltonian": (C.c_int, [_PP, _PF, _P, _I64, _P, _I64, _I32, _P, _P]),
     "gx_ruth4_integrate_hamiltonian": (C.c_int, [_PP, _PF, _P, _I64, _P, _I64, _I32, _P, _P]),
+    "gx_calibrate_fma": (C.c_int, [_I32, _I32, _I32, _I64, _P, _P]),
     "gx_dop853_integrate_hamiltonian": (
         C.c_int,
         [_PP, _PF, _P, _I64, _P, _I64, _D, _D, _I64, _D, _I64, _I32, _I32, _I64, _P, _P, _P, _P],

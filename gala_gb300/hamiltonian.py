@@ -199,6 +199,10 @@ class Hamiltonian:
             stride = int(kw.get("out_stride", 1))
             dt_max = float(kw.get("dt_max", 0.0))
             nstiff = int(kw.get("nstiff", 0))
+            if not 1 <= nbatch <= 1024:
+                raise ValueError(f"nbatch must be in [1, 1024] (got {nbatch})")
+            if stride < 1:
+                raise ValueError(f"out_stride must be >= 1 (got {stride})")
             n_out = (ntimes - 1) // stride + 1
             nb = (n + nbatch - 1) // nbatch
             out = torch.empty((6, n_out, n) if save_all else (6, n), dtype=torch.float64, device=dev)

@@ -193,6 +193,16 @@ int gx_dop853_integrate_hamiltonian(const gx_potential* pot, const gx_frame* fra
                                     int64_t out_stride, double* w_out,
                                     int32_t* status, int64_t* stats, void* stream);
 
+/* ------------------------------------------------------------------------- */
+/* Pipe calibration.  No counterpart in gala: it measures the FP64 / FP32     */
+/* multiply-add throughput that bounds the integrators (the roofline          */
+/* denominator).  Runs blocks x threads threads, each with 8 independent FMA  */
+/* chains of `iters` steps: flops = 16 * iters * blocks * threads.  `sink` is */
+/* a DEVICE buffer of blocks * threads doubles (fp64 != 0) or floats.         */
+/* ------------------------------------------------------------------------- */
+int gx_calibrate_fma(int32_t fp64, int32_t blocks, int32_t threads, int64_t iters,
+                     void* sink, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

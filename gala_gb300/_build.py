@@ -27,6 +27,7 @@ UNITS = {
     "gx_fixed.cu": ["-fmad=false"],
     "gx_dop853.cu": ["-fmad=false"],
     "gx_peaks.cu": [],
+    "gx_batch.cu": [],
 }
 
 

@@ -1,0 +1,227 @@
+"""Batched integration of many orbits with uneven lengths, steps and integrators.
+
+``BatchIntegrator`` runs Leapfrog and Ruth4 orbits of different ``n_steps`` and
+``dt`` in one persistent-kernel launch (gx_batch_integrate_fp32): FP32 forces,
+Kahan-compensated FP32 state, FP64 initial/final states and an FP64 energy
+diagnostic.  The work schedule is computed on the GPU (longest first, one
+integrator per chunk); the whole sequence -- schedule, queue reset, persistent
+kernel, energy diagnostic -- can be captured once in a CUDA graph and replayed.
+Launch shape (block size, CTAs per SM, chunk size) comes from an autotuner whose
+choices are cached per GPU, kernel and potential.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import time
+from pathlib import Path
+
+import numpy as np
+
+from . import _abi
+
+LEAPFROG, RUTH4 = 0, 1
+COST = {LEAPFROG: 1.0, RUTH4: 3.0}   # gradient evaluations per step
+CACHE = Path(os.environ.get("GALA_GB300_AUTOTUNE", Path(__file__).resolve().parent / "_build" / "autotune.json"))
+DEFAULT_CONFIG = {"fp32c": {"block": 128, "ctas_per_sm": 4, "chunk": 32},
+                  "fp64": {"block": 64, "ctas_per_sm": 4, "chunk": 32}}
+SEARCH = {
+    "fp32c": [{"block": b, "ctas_per_sm": c, "chunk": k} for b in (64, 128, 256) for c in (2, 4, 8)
+              for k in (32, 64) if b * c <= 2048],
+    "fp64": [{"block": b, "ctas_per_sm": c, "chunk": k} for b in (32, 64, 128) for c in (2, 4, 8)
+             for k in (32, 64) if b * c <= 512],
+}
+ENTRY = {"fp32c": "gx_batch_integrate_fp32", "fp64": "gx_batch_integrate_fp64"}
+
+
+def schedule(n_steps, method, chunk):
+    """Processing order on the GPU: per integrator, orbits sorted by cost
+    (longest first) and cut into chunks; chunks of both integrators merged by
+    cost, longest first; the tail of each integrator's list padded with -1."""
+    import torch
+
+    dev = n_steps.device
+    cost = n_steps.to(torch.float64) * torch.where(method == RUTH4, COST[RUTH4], COST[LEAPFROG])
+    pieces, heads = [], []
+    for m in (RUTH4, LEAPFROG):
+        idx = torch.nonzero(method == m).flatten()
+        if idx.numel() == 0:
+            continue
+        srt = idx[torch.argsort(cost[idx], descending=True, stable=True)].to(torch.int32)
+        pad = (-srt.numel()) % chunk
+        if pad:
+            srt = torch.cat([srt, torch.full((pad,), -1, dtype=torch.int32, device=dev)])
+        chunks = srt.view(-1, chunk)
+        pieces.append(chunks)
+        heads.append(cost[chunks[:, 0].long()])
+    chunks = torch.cat(pieces)
+    order = torch.argsort(torch.cat(heads), descending=True, stable=True)
+    return chunks[order].reshape(-1).contiguous()
+
+
+def _potential_key(potential):
+    pk = potential.packed()
+    h = hashlib.sha1(pk.params.tobytes())
+    for i in range(pk.desc.n_components):
+        h.update(bytes([pk.components[i].type, pk.components[i].do_shift_rotate]))
+    return h.hexdigest()[:16]
+
+
+class BatchIntegrator:
+    """Integrate N orbits, each with its own n_steps, dt and integrator.
+
+    Parameters
+    ----------
+    potential : closed-form gala_gb300 potential (SCF is not supported here)
+    w0 : (6, N) array-like or CUDA tensor, float64
+    n_steps : (N,) integers; dt : (N,) floats; method : (N,) 0 = leapfrog, 1 = ruth4
+    precision : "fp32c" (FP32 forces, compensated FP32 state; closed-form
+        potentials) or "fp64" (gala's arithmetic in FP64, the plain form)
+    config : dict with block, ctas_per_sm, chunk; None = autotuned/cached choice
+    """
+
+    def __init__(self, potential, w0, n_steps, dt, method, config=None, precision="fp32c"):
+        import torch
+
+        from ._device import as_device_f64, require_cuda
+
+        if precision not in ENTRY:
+            raise ValueError(f"precision must be one of {sorted(ENTRY)}")
+        self.precision = precision
+        self.dev = require_cuda()
+        self.potential = potential
+        self.w0 = as_device_f64(w0)
+        if self.w0.dim() != 2 or self.w0.shape[0] != 6:
+            raise ValueError(f"w0 must have shape (6, N), got {tuple(self.w0.shape)}")
+        self.n = self.w0.shape[1]
+        self.n_steps = torch.as_tensor(np.asarray(n_steps, dtype=np.int64) if not isinstance(n_steps, torch.Tensor)
+                                       else n_steps, dtype=torch.int64).to(self.dev).contiguous()
+        self.dt = as_device_f64(dt)
+        self.method = torch.as_tensor(np.asarray(method, dtype=np.int32) if not isinstance(method, torch.Tensor)
+                                      else method, dtype=torch.int32).to(self.dev).contiguous()
+        for name, a in (("n_steps", self.n_steps), ("dt", self.dt), ("method", self.method)):
+            if a.shape != (self.n,):
+                raise ValueError(f"{name} must have shape ({self.n},), got {tuple(a.shape)}")
+        if self.n and (int(self.method.min()) < 0 or int(self.method.max()) > 1):
+            raise ValueError("method must be 0 (leapfrog) or 1 (ruth4)")
+        if self.n and int(self.n_steps.min()) < 0:
+            raise ValueError("n_steps must be non-negative")
+        self.sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
+        self.config = dict(config) if config is not None else self._cached_config()
+        self.w_out = torch.empty((6, self.n), dtype=torch.float64, device=self.dev)
+        self.E0 = torch.empty(self.n, dtype=torch.float64, device=self.dev)
+        self.E1 = torch.empty(self.n, dtype=torch.float64, device=self.dev)
+        self.counter = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        self.graph = None
+
+    # ------------------------------------------------------------------ run
+    def _prepare(self):
+        """Compute the processing order for the current launch shape (eager)."""
+        self.order = schedule(self.n_steps, self.method, self.config["chunk"])
+        self._order_chunk = self.config["chunk"]
+
+    def _launch(self, stream_handle):
+        import ctypes as C
+
+        from ._device import ptr
+
+        cfg = self.config
+        if getattr(self, "_order_chunk", None) != cfg["chunk"]:
+            self._prepare()
+        desc = self.potential.packed().for_device()
+        _abi.call(ENTRY[self.precision], desc, ptr(self.w0), self.n, ptr(self.n_steps), ptr(self.dt),
+                  ptr(self.method), ptr(self.order), self.order.numel(), cfg["chunk"], cfg["block"],
+                  cfg["ctas_per_sm"] * self.sms, ptr(self.counter), ptr(self.w_out), stream_handle)
+        frame = _abi.gx_frame()
+        _abi.call("gx_hamiltonian_value", desc, C.byref(frame), 0.0, ptr(self.w0), self.n, ptr(self.E0),
+                  stream_handle)
+        _abi.call("gx_hamiltonian_value", desc, C.byref(frame), 0.0, ptr(self.w_out), self.n, ptr(self.E1),
+                  stream_handle)
+
+    def run(self):
+        """Integrate every orbit once (eager launch sequence)."""
+        from ._device import stream_handle
+
+        if self.n == 0:
+            return self.w_out
+        if self.graph is not None:
+            self.graph.replay()
+        else:
+            self._launch(stream_handle())
+        return self.w_out
+
+    def capture(self):
+        """Capture queue reset + persistent kernel + energy diagnostic in one CUDA
+        graph (the schedule is computed once, eagerly); run() then replays it."""
+        import torch
+
+        from ._device import stream_handle
+
+        if self.n == 0:
+            return self
+        self._prepare()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self._launch(stream_handle(s))   # warm up allocations outside the graph
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self._launch(stream_handle())
+        self.graph = g
+        return self
+
+    def energy_drift(self):
+        """|E(t_end) - E(0)| / |E(0)| per orbit (FP64 diagnostic)."""
+        return ((self.E1 - self.E0) / self.E0).abs()
+
+    # ------------------------------------------------------------- autotune
+    def _cache_key(self):
+        import torch
+
+        return (f"{torch.cuda.get_device_name(self.dev)}|{ENTRY[self.precision]}|"
+                f"{_potential_key(self.potential)}")
+
+    def _cached_config(self):
+        try:
+            return dict(json.loads(CACHE.read_text())[self._cache_key()])
+        except (FileNotFoundError, KeyError, ValueError):
+            return dict(DEFAULT_CONFIG[self.precision])
+
+    def autotune(self, sample=16384, max_steps=2000, reps=2, persist=True):
+        """Time every launch shape of SEARCH on a sample of this workload (orbits
+        subsampled, step counts capped), keep the fastest, cache it."""
+        import torch
+
+        from ._device import stream_handle
+
+        rng = np.random.default_rng(0)
+        m = min(sample, self.n)
+        sel = torch.as_tensor(np.sort(rng.choice(self.n, m, replace=False)), device=self.dev)
+        sub = BatchIntegrator(self.potential, self.w0[:, sel], torch.clamp(self.n_steps[sel], max=max_steps),
+                              self.dt[sel], self.method[sel], config=DEFAULT_CONFIG[self.precision],
+                              precision=self.precision)
+        results = []
+        for cfg in SEARCH[self.precision]:
+            sub.config = cfg
+            sub._launch(stream_handle())
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                sub._launch(stream_handle())
+            torch.cuda.synchronize()
+            results.append(((time.perf_counter() - t0) / reps, cfg))
+        best = min(results, key=lambda r: r[0])[1]
+        self.config = dict(best)
+        self.tune_results = [(t, c) for t, c in sorted(results, key=lambda r: r[0])]
+        if persist:
+            CACHE.parent.mkdir(parents=True, exist_ok=True)
+            try:
+                data = json.loads(CACHE.read_text())
+            except (FileNotFoundError, ValueError):
+                data = {}
+            data[self._cache_key()] = best
+            CACHE.write_text(json.dumps(data, indent=1))
+        return best

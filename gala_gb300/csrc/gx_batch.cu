@@ -1,0 +1,181 @@
+// gx_batch.cu -- batched integration of many orbits with uneven step counts,
+// step sizes and integrators, in FP32 with compensated state accumulation.
+//
+// Work queue: the caller supplies a processing order (a permutation of the
+// orbits, padded with -1 to whole chunks) in which each chunk holds orbits of
+// one integrator and similar cost, chunks sorted longest first.  A persistent
+// grid (a few CTAs per SM) pulls chunks from a single atomic counter; every
+// warp integrates `chunk` orbits, one per lane, 32 at a time.  Longest-first
+// order plus dynamic pulling keeps the SMs busy until the very end.
+//
+// Per orbit: positions and velocities are carried as FP32 (hi, lo) pairs with
+// Kahan-compensated updates; forces are evaluated in FP32 at hi (gx_fp32.cuh).
+// Initial and final states are FP64 (hi + lo), so FP32 rounding of the state
+// does not accumulate over tens of thousands of steps.
+//   leapfrog  kick-drift-kick as c_leapfrog_step (leapfrog.pyx:35-51)
+//   ruth4     c_ruth4_step (ruth4.pyx:24-35); the d = 0 sub-step's gradient is
+//             skipped here (FP32 form, no bit-parity claim)
+#include "gx_host.h"
+#include "gx_fp32.cuh"
+
+namespace gx {
+
+struct BatchArgs {
+    int64_t n;        // number of orbits
+    int64_t slots;    // length of the order array (multiple of chunk)
+    int32_t chunk;    // orbits per queue item (multiple of 32)
+    int32_t pad;
+    float c[4], d[4];  // Ruth4 coefficients
+};
+
+__device__ __forceinline__ void split(double x, float &hi, float &lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
+__device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const BatchArgs &A, const double *w0,
+                                                   int64_t n, int64_t i, int64_t nsteps, float h, int meth,
+                                                   double *w_out) {
+    if (nsteps == 0) {
+        for (int k = 0; k < 6; k++) w_out[k * n + i] = w0[k * n + i];
+        return;
+    }
+    float xh[3], xl[3], vh[3], vl[3], g[3];
+    for (int k = 0; k < 3; k++) {
+        split(w0[k * n + i], xh[k], xl[k]);
+        split(w0[(3 + k) * n + i], vh[k], vl[k]);
+    }
+    if (meth == 0) {
+        // c_init_velocity: v_{1/2} = v - g h / 2
+        potential_gradient_f(pot, xh, g);
+        for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h * 0.5f);
+        for (int64_t j = 0; j < nsteps; j++) {
+            for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], h, vl[k] * h));
+            potential_gradient_f(pot, xh, g);
+            for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h);
+        }
+        // output velocity at the last step: v_{n+1/2} + g h / 2
+        for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], g[k] * h * 0.5f);
+    } else {
+        for (int64_t j = 0; j < nsteps; j++) {
+            // sub-step 0 has d = 0: drift only
+            for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], A.c[0] * fmaf(vh[k], h, vl[k] * h));
+#pragma unroll
+            for (int s = 1; s < 4; s++) {
+                potential_gradient_f(pot, xh, g);
+                for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -A.d[s] * g[k] * h);
+                for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], A.c[s] * fmaf(vh[k], h, vl[k] * h));
+            }
+        }
+    }
+    for (int k = 0; k < 3; k++) {
+        w_out[k * n + i] = (double)xh[k] + (double)xl[k];
+        w_out[(3 + k) * n + i] = (double)vh[k] + (double)vl[k];
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_fp32_kernel(const __grid_constant__ DevPotF pot, BatchArgs A,
+                                                         const double *__restrict__ w0,
+                                                         const int64_t *__restrict__ nsteps,
+                                                         const double *__restrict__ dt,
+                                                         const int32_t *__restrict__ method,
+                                                         const int32_t *__restrict__ order,
+                                                         int32_t *__restrict__ counter, double *__restrict__ w_out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nchunks = A.slots / A.chunk;
+    for (;;) {
+        int c = 0;
+        if (lane == 0) c = atomicAdd(counter, 1);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= nchunks) break;
+        for (int r = 0; r < A.chunk; r += 32) {
+            const int64_t slot = (int64_t)c * A.chunk + r + lane;
+            const int32_t i = order[slot];
+            if (i >= 0 && i < A.n)
+                integrate_one_fp32(pot, A, w0, A.n, i, nsteps[i], (float)dt[i], method[i], w_out);
+        }
+    }
+}
+
+// FP32 descriptor from the FP64 one (gala packing [G, ...]) with the per-type
+// constants the FP32 force code wants.
+int pack_potential_f32(const gx_potential *pot, DevPotF *out) {
+    DevPot dp;
+    int rc = pack_potential(pot, &dp);
+    if (rc) return rc;
+    if (dp.has_scf) {
+        set_error("the FP32 batched integrator supports closed-form components only (no SCF)");
+        return GX_ERR_UNSUPPORTED;
+    }
+    memset(out, 0, sizeof(*out));
+    out->ncomp = dp.ncomp;
+    for (int i = 0; i < dp.ncomp; i++) {
+        const DevComp &c = dp.c[i];
+        DevCompF &f = out->c[i];
+        const double *p = dp.p + c.poff;
+        f.type = c.type;
+        f.do_sr = c.do_sr;
+        for (int k = 0; k < 3; k++) f.q0[k] = (float)c.q0[k];
+        for (int k = 0; k < 9; k++) f.R[k] = (float)c.R[k];
+        switch (c.type) {
+        case GX_POT_NULL: break;
+        case GX_POT_KEPLER: f.p[0] = (float)(p[0] * p[1]); break;
+        case GX_POT_HERNQUIST: f.p[0] = (float)(p[0] * p[1]); f.p[1] = (float)p[2]; break;
+        case GX_POT_PLUMMER: f.p[0] = (float)(p[0] * p[1]); f.p[1] = (float)(p[2] * p[2]); break;
+        case GX_POT_MIYAMOTONAGAI:
+            f.p[0] = (float)(p[0] * p[1]); f.p[1] = (float)p[2]; f.p[2] = (float)(p[3] * p[3]);
+            break;
+        case GX_POT_SPHERICALNFW:
+        case GX_POT_FLATTENEDNFW:
+        case GX_POT_TRIAXIALNFW:
+            f.p[0] = (float)(p[0] * p[1] / (p[2] * p[2] * p[2]));
+            f.p[1] = (float)(1.0 / p[2]);
+            if (c.type == GX_POT_FLATTENEDNFW) f.p[2] = (float)(1.0 / (p[5] * p[5]));
+            if (c.type == GX_POT_TRIAXIALNFW) {
+                f.p[2] = (float)(1.0 / (p[3] * p[3]));
+                f.p[3] = (float)(1.0 / (p[4] * p[4]));
+                f.p[4] = (float)(1.0 / (p[5] * p[5]));
+            }
+            break;
+        default:
+            set_error("component %d: type %d has no FP32 implementation", i, c.type);
+            return GX_ERR_UNSUPPORTED;
+        }
+    }
+    return GX_OK;
+}
+
+}  // namespace gx
+
+extern "C" int gx_batch_integrate_fp32(const gx_potential *pot, const double *w0, int64_t n,
+                                       const int64_t *n_steps, const double *dt, const int32_t *method,
+                                       const int32_t *order, int64_t n_slots, int32_t chunk, int32_t block,
+                                       int32_t grid, int32_t *queue_counter, double *w_out, void *stream) {
+    gx::DevPotF dp;
+    int rc = gx::pack_potential_f32(pot, &dp);
+    if (rc) return rc;
+    GX_CHECK_ARG(n >= 0 && n < (int64_t)INT32_MAX, "n out of range");
+    if (n == 0) return GX_OK;
+    GX_CHECK_ARG(w0 && n_steps && dt && method && order && queue_counter && w_out, "NULL array");
+    GX_CHECK_ARG(chunk >= 32 && chunk % 32 == 0 && chunk <= 4096, "chunk must be a multiple of 32 in [32, 4096]");
+    GX_CHECK_ARG(n_slots >= n && n_slots % chunk == 0, "order length must be >= n and a multiple of chunk");
+    GX_CHECK_ARG(block >= 32 && block <= 256 && block % 32 == 0, "block must be a multiple of 32 in [32, 256]");
+    GX_CHECK_ARG(grid >= 1, "grid must be >= 1");
+    gx::BatchArgs A;
+    A.n = n;
+    A.slots = n_slots;
+    A.chunk = chunk;
+    A.pad = 0;
+    const double two_13 = std::pow(2., 1. / 3.);
+    const double c[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
+                         (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};
+    const double d[4] = {0., 1. / (2. - two_13), -two_13 / (2. - two_13), 1. / (2. - two_13)};
+    for (int k = 0; k < 4; k++) {
+        A.c[k] = (float)c[k];
+        A.d[k] = (float)d[k];
+    }
+    cudaStream_t st = gx::as_stream(stream);
+    GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, sizeof(int32_t), st));
+    gx::batch_fp32_kernel<<<grid, block, 0, st>>>(dp, A, w0, n_steps, dt, method, order, queue_counter, w_out);
+    return gx::check_launch("batch_fp32");
+}

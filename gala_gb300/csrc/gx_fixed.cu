@@ -100,6 +100,65 @@ __global__ void __launch_bounds__(128, 1) ruth4_kernel(const __grid_constant__ D
         for (int k = 0; k < 6; k++) out[k * n + i] = w[k];
 }
 
+// ---------------------------------------------------------------------------
+// Batched FP64 form of the same two integrators (the plain form of the batched
+// workload): per orbit its own n_steps, dt and integrator, final state only,
+// gala's arithmetic exactly as in the kernels above.  Same work queue as the
+// FP32 batch kernel (gx_batch.cu): chunks of the caller's order pulled from
+// one atomic counter by a persistent grid.
+// ---------------------------------------------------------------------------
+template <bool SCF>
+__global__ void __launch_bounds__(128, 1) batch_fp64_kernel(const __grid_constant__ DevPot pot, Ruth4Coef co,
+                                                            int64_t n, int64_t slots, int32_t chunk,
+                                                            const double *__restrict__ w0,
+                                                            const int64_t *__restrict__ nsteps,
+                                                            const double *__restrict__ dtv,
+                                                            const int32_t *__restrict__ method,
+                                                            const int32_t *__restrict__ order,
+                                                            int32_t *__restrict__ counter,
+                                                            double *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nchunks = slots / chunk;
+    for (;;) {
+        int c = 0;
+        if (lane == 0) c = atomicAdd(counter, 1);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= nchunks) break;
+        for (int r = 0; r < chunk; r += 32) {
+            const int32_t i = order[(int64_t)c * chunk + r + lane];
+            if (i < 0 || i >= n) continue;
+            double w[6], g[3];
+            for (int k = 0; k < 6; k++) w[k] = w0[k * n + i];
+            const int64_t ns = nsteps[i];
+            const double dt = dtv[i];
+            if (ns > 0 && method[i] == 0) {
+                double vh[3];
+                grad(pot, w, g);
+                for (int k = 0; k < 3; k++) vh[k] = w[3 + k] - g[k] * dt / 2.;
+                for (int64_t j = 0; j < ns; j++) {
+                    for (int k = 0; k < 3; k++) w[k] = w[k] + vh[k] * dt;
+                    grad(pot, w, g);
+                    for (int k = 0; k < 3; k++) {
+                        w[3 + k] = vh[k] - g[k] * dt / 2.;
+                        vh[k] = vh[k] - g[k] * dt;
+                    }
+                }
+            } else if (ns > 0) {
+                for (int64_t j = 0; j < ns; j++) {
+                    for (int s = 0; s < 4; s++) {
+                        grad(pot, w, g);
+                        for (int k = 0; k < 3; k++) {
+                            w[3 + k] = w[3 + k] - co.d[s] * g[k] * dt;
+                            w[k] = w[k] + co.c[s] * w[3 + k] * dt;
+                        }
+                    }
+                }
+            }
+            for (int k = 0; k < 6; k++) out[k * n + i] = w[k];
+        }
+    }
+}
+
 static int fixed_common(const gx_potential *pot, const gx_frame *frame, const double *w0, int64_t n,
                         const double *t, int64_t ntimes, double *w_out, DevPot *dp, const char *name) {
     int rc = pack_potential(pot, dp);
@@ -136,6 +195,41 @@ int gx_leapfrog_integrate_hamiltonian(const gx_potential *pot, const gx_frame *f
     else
         gx::leapfrog_kernel<false, false><<<grid, bs, 0, st>>>(dp, w0, n, t, ntimes, w_out);
     return gx::check_launch("leapfrog");
+}
+
+int gx_batch_integrate_fp64(const gx_potential *pot, const double *w0, int64_t n, const int64_t *n_steps,
+                            const double *dt, const int32_t *method, const int32_t *order, int64_t n_slots,
+                            int32_t chunk, int32_t block, int32_t grid, int32_t *queue_counter, double *w_out,
+                            void *stream) {
+    gx::DevPot dp;
+    int rc = gx::pack_potential(pot, &dp);
+    if (rc) return rc;
+    GX_CHECK_ARG(n >= 0 && n < (int64_t)INT32_MAX, "n out of range");
+    if (n == 0) return GX_OK;
+    GX_CHECK_ARG(w0 && n_steps && dt && method && order && queue_counter && w_out, "NULL array");
+    GX_CHECK_ARG(chunk >= 32 && chunk % 32 == 0 && chunk <= 4096, "chunk must be a multiple of 32 in [32, 4096]");
+    GX_CHECK_ARG(n_slots >= n && n_slots % chunk == 0, "order length must be >= n and a multiple of chunk");
+    GX_CHECK_ARG(block >= 32 && block <= 128 && block % 32 == 0, "block must be a multiple of 32 in [32, 128]");
+    GX_CHECK_ARG(grid >= 1, "grid must be >= 1");
+    const double two_13 = std::pow(2., 1. / 3.);
+    gx::Ruth4Coef co;
+    co.c[0] = 1. / (2. * (2. - two_13));
+    co.c[1] = (1. - two_13) / (2. * (2. - two_13));
+    co.c[2] = (1. - two_13) / (2. * (2. - two_13));
+    co.c[3] = 1. / (2. * (2. - two_13));
+    co.d[0] = 0.;
+    co.d[1] = 1. / (2. - two_13);
+    co.d[2] = -two_13 / (2. - two_13);
+    co.d[3] = 1. / (2. - two_13);
+    cudaStream_t st = gx::as_stream(stream);
+    GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, sizeof(int32_t), st));
+    if (dp.has_scf)
+        gx::batch_fp64_kernel<true><<<grid, block, 0, st>>>(dp, co, n, n_slots, chunk, w0, n_steps, dt, method,
+                                                            order, queue_counter, w_out);
+    else
+        gx::batch_fp64_kernel<false><<<grid, block, 0, st>>>(dp, co, n, n_slots, chunk, w0, n_steps, dt, method,
+                                                             order, queue_counter, w_out);
+    return gx::check_launch("batch_fp64");
 }
 
 int gx_ruth4_integrate_hamiltonian(const gx_potential *pot, const gx_frame *frame, const double *w0, int64_t n,

@@ -194,6 +194,37 @@ int gx_dop853_integrate_hamiltonian(const gx_potential* pot, const gx_frame* fra
                                     int32_t* status, int64_t* stats, void* stream);
 
 /* ------------------------------------------------------------------------- */
+/* Batched FP32 integration with compensated state (no single gala function:  */
+/* it runs many leapfrog_integrate_hamiltonian / ruth4_integrate_hamiltonian  */
+/* problems of different length, step and integrator in one launch; per-orbit */
+/* arithmetic follows leapfrog.pyx:24-51 and ruth4.pyx:24-35 in FP32).         */
+/*   w0       (6, N) float64 initial conditions                               */
+/*   n_steps  (N,) int64 steps per orbit; dt (N,) float64 step per orbit      */
+/*   method   (N,) int32: 0 leapfrog, 1 ruth4                                 */
+/*   order    (n_slots,) int32 processing order: orbit indices, -1 = padding; */
+/*            n_slots is a multiple of `chunk`; each chunk is one queue item  */
+/*   queue_counter  DEVICE int32 scratch (zeroed by the call)                 */
+/*   block, grid    launch shape of the persistent grid                       */
+/*   w_out    (6, N) float64 final states (t = n_steps * dt after the start)  */
+/* Closed-form components only (SCF -> GX_ERR_UNSUPPORTED).                   */
+/* ------------------------------------------------------------------------- */
+int gx_batch_integrate_fp32(const gx_potential* pot, const double* w0, int64_t n,
+                            const int64_t* n_steps, const double* dt, const int32_t* method,
+                            const int32_t* order, int64_t n_slots, int32_t chunk,
+                            int32_t block, int32_t grid, int32_t* queue_counter,
+                            double* w_out, void* stream);
+
+/* The plain FP64 form of the same batched workload: identical arguments and
+ * queue; per orbit, gala's Leapfrog / Ruth4 arithmetic in FP64 exactly as
+ * gx_leapfrog_integrate_hamiltonian / gx_ruth4_integrate_hamiltonian compute it
+ * (bit-identical final states).  block <= 128.  SCF components allowed. */
+int gx_batch_integrate_fp64(const gx_potential* pot, const double* w0, int64_t n,
+                            const int64_t* n_steps, const double* dt, const int32_t* method,
+                            const int32_t* order, int64_t n_slots, int32_t chunk,
+                            int32_t block, int32_t grid, int32_t* queue_counter,
+                            double* w_out, void* stream);
+
+/* ------------------------------------------------------------------------- */
 /* Pipe calibration.  No counterpart in gala: it measures the FP64 / FP32     */
 /* multiply-add throughput that bounds the integrators (the roofline          */
 /* denominator).  Runs blocks x threads threads, each with 8 independent FMA  */

@@ -1,0 +1,119 @@
+"""Batched uneven workload (per-orbit n_steps, dt, integrator) on the GPU.
+
+* FP64 batch kernel: gala's per-orbit arithmetic, checked orbit by orbit
+  against the oracle (bit-exact for Hernquist, <= 1e-12 for the MW composite).
+* FP32-compensated kernel: against the FP64 oracle, final position error
+  <= 1e-4 relative and median energy drift <= 1e-6 (the accuracy contract of
+  the FP32 form).
+"""
+import numpy as np
+import pytest
+
+import gala_gb300 as g
+from gala_gb300 import workloads as W
+from gala_gb300.batch import SEARCH, BatchIntegrator
+
+from .conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _workload(n, seed, max_steps):
+    rng = np.random.default_rng(seed)
+    nsteps = np.round(np.exp(rng.uniform(np.log(50), np.log(max_steps), n))).astype(np.int64)
+    dt = rng.choice(np.array([0.1, 0.5, 1.0]), n)
+    method = rng.integers(0, 2, n).astype(np.int32)
+    return nsteps, dt, method
+
+
+def _oracle_final(oracle, pot, w0, nsteps, dt, method):
+    out = np.empty_like(w0)
+    for i in range(w0.shape[1]):
+        t = g.parse_time_specification(dt=float(dt[i]), n_steps=int(nsteps[i]))
+        out[:, i] = oracle.fixed(pot, w0[:, i:i + 1], t, "leapfrog" if method[i] == 0 else "ruth4",
+                                 save_all=False)[:, 0]
+    return out
+
+
+@pytest.mark.parametrize("potname", ["hernquist", "mw"])
+def test_fp64_batch_matches_oracle(oracle, potname):
+    pot = W.hernquist_potential() if potname == "hernquist" else W.mw_composite()
+    w0 = W.hernquist_ics(300, seed=3) if potname == "hernquist" else W.mw_ics(300, seed=3)
+    nsteps, dt, method = _workload(300, 5, 600)
+    b = BatchIntegrator(pot, w0, nsteps, dt, method, precision="fp64")
+    w = b.run().cpu().numpy()
+    ref = _oracle_final(oracle, pot, w0, nsteps, dt, method)
+    if potname == "hernquist":
+        assert np.array_equal(w, ref)
+    else:
+        assert np.max(rel_err(w, ref)) <= 1e-12
+
+
+def test_fp32c_accuracy_contract(oracle):
+    pot = W.mw_composite()
+    n = 1024
+    w0 = W.mw_ics(n, seed=7)
+    nsteps, dt, method = _workload(n, 8, 4000)
+    b = BatchIntegrator(pot, w0, nsteps, dt, method)
+    w = b.run().cpu().numpy()
+    ref = _oracle_final(oracle, pot, w0, nsteps, dt, method)
+    pos_err = rel_err(w[:3], ref[:3])
+    assert np.max(pos_err) <= 1e-4, np.max(pos_err)
+    dE = b.energy_drift().cpu().numpy()
+    assert np.median(dE) <= 1e-6, np.median(dE)
+    # the FP64 diagnostic agrees with the oracle's energy of the final states
+    E1 = oracle.hamiltonian_value(pot, w)
+    np.testing.assert_allclose(b.E1.cpu().numpy(), E1, rtol=1e-13)
+
+
+def test_graph_replay_matches_eager():
+    pot = W.mw_composite()
+    n = 2000
+    w0 = W.mw_ics(n, seed=9)
+    nsteps, dt, method = _workload(n, 10, 500)
+    eager = BatchIntegrator(pot, w0, nsteps, dt, method).run().cpu().numpy()
+    b = BatchIntegrator(pot, w0, nsteps, dt, method).capture()
+    for _ in range(2):
+        b.run()
+    assert np.array_equal(b.w_out.cpu().numpy(), eager)
+
+
+def test_autotune_returns_searched_config(tmp_path, monkeypatch):
+    import gala_gb300.batch as B
+
+    monkeypatch.setattr(B, "CACHE", tmp_path / "autotune.json")
+    pot = W.mw_composite()
+    w0 = W.mw_ics(4096, seed=11)
+    nsteps, dt, method = _workload(4096, 12, 300)
+    b = BatchIntegrator(pot, w0, nsteps, dt, method)
+    best = b.autotune(sample=2048, max_steps=200, reps=1)
+    assert best in SEARCH["fp32c"]
+    assert (tmp_path / "autotune.json").exists()
+    # a new integrator of the same workload picks the cached choice
+    assert BatchIntegrator(pot, w0, nsteps, dt, method).config == best
+
+
+def test_zero_steps_and_single_method():
+    pot = W.mw_composite()
+    w0 = W.mw_ics(64, seed=13)
+    nsteps = np.zeros(64, dtype=np.int64)
+    nsteps[::2] = 100
+    for prec in ("fp32c", "fp64"):
+        b = BatchIntegrator(pot, w0, nsteps, np.full(64, 0.5), np.zeros(64, dtype=np.int32), precision=prec)
+        w = b.run().cpu().numpy()
+        assert np.array_equal(w[:, 1::2], w0[:, 1::2])
+        assert not np.array_equal(w[:, ::2], w0[:, ::2])
+
+
+def test_invalid_batch_arguments():
+    pot = W.mw_composite()
+    w0 = W.mw_ics(8, seed=14)
+    with pytest.raises(ValueError):
+        BatchIntegrator(pot, w0, np.ones(7, dtype=np.int64), np.ones(8), np.zeros(8, dtype=np.int32))
+    with pytest.raises(ValueError):
+        BatchIntegrator(pot, w0, np.ones(8, dtype=np.int64), np.ones(8), np.full(8, 3, dtype=np.int32))
+    S = np.zeros((1, 1, 1))
+    S[0, 0, 0] = 1.0
+    scf = g.SCFPotential(m=1e11, r_s=1.0, Snlm=S, Tnlm=S * 0)
+    with pytest.raises(TypeError):
+        BatchIntegrator(scf, w0, np.ones(8, dtype=np.int64), np.ones(8), np.zeros(8, dtype=np.int32)).run()

@@ -27,10 +27,10 @@ CACHE = Path(os.environ.get("GALA_GB300_AUTOTUNE", Path(__file__).resolve().pare
 DEFAULT_CONFIG = {"fp32c": {"block": 128, "ctas_per_sm": 4, "chunk": 32},
                   "fp64": {"block": 64, "ctas_per_sm": 4, "chunk": 32}}
 SEARCH = {
-    "fp32c": [{"block": b, "ctas_per_sm": c, "chunk": k} for b in (64, 128, 256) for c in (2, 4, 8)
-              for k in (32, 64) if b * c <= 2048],
-    "fp64": [{"block": b, "ctas_per_sm": c, "chunk": k} for b in (32, 64, 128) for c in (2, 4, 8)
-             for k in (32, 64) if b * c <= 512],
+    "fp32c": [{"block": b, "ctas_per_sm": c, "chunk": k} for b in (64, 128, 256) for c in (1, 2, 4, 8, 16)
+              for k in (32, 64) if 256 <= b * c <= 1024],
+    "fp64": [{"block": b, "ctas_per_sm": c, "chunk": k} for b in (32, 64, 128) for c in (1, 2, 4, 8)
+             for k in (32, 64) if 64 <= b * c <= 512],
 }
 ENTRY = {"fp32c": "gx_batch_integrate_fp32", "fp64": "gx_batch_integrate_fp64"}
 
@@ -190,19 +190,18 @@ class BatchIntegrator:
         except (FileNotFoundError, KeyError, ValueError):
             return dict(DEFAULT_CONFIG[self.precision])
 
-    def autotune(self, sample=16384, max_steps=2000, reps=2, persist=True):
-        """Time every launch shape of SEARCH on a sample of this workload (orbits
-        subsampled, step counts capped), keep the fastest, cache it."""
+    def autotune(self, work_fraction=0.03, reps=2, persist=True):
+        """Time every launch shape of SEARCH on a scaled copy of this workload --
+        all orbits, every step count multiplied by `work_fraction` (at least 1),
+        so the number of warps and the spread of orbit lengths are those of the
+        real run -- keep the fastest and cache it."""
         import torch
 
         from ._device import stream_handle
 
-        rng = np.random.default_rng(0)
-        m = min(sample, self.n)
-        sel = torch.as_tensor(np.sort(rng.choice(self.n, m, replace=False)), device=self.dev)
-        sub = BatchIntegrator(self.potential, self.w0[:, sel], torch.clamp(self.n_steps[sel], max=max_steps),
-                              self.dt[sel], self.method[sel], config=DEFAULT_CONFIG[self.precision],
-                              precision=self.precision)
+        scaled = torch.clamp(torch.ceil(self.n_steps.to(torch.float64) * work_fraction), min=1).to(torch.int64)
+        sub = BatchIntegrator(self.potential, self.w0, scaled, self.dt, self.method,
+                              config=DEFAULT_CONFIG[self.precision], precision=self.precision)
         results = []
         for cfg in SEARCH[self.precision]:
             sub.config = cfg

@@ -86,7 +86,7 @@ def test_autotune_returns_searched_config(tmp_path, monkeypatch):
     w0 = W.mw_ics(4096, seed=11)
     nsteps, dt, method = _workload(4096, 12, 300)
     b = BatchIntegrator(pot, w0, nsteps, dt, method)
-    best = b.autotune(sample=2048, max_steps=200, reps=1)
+    best = b.autotune(work_fraction=0.05, reps=1)
     assert best in SEARCH["fp32c"]
     assert (tmp_path / "autotune.json").exists()
     # a new integrator of the same workload picks the cached choice

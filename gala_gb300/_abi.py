@@ -13,6 +13,7 @@ from . import _build
 
 GX_MAX_COMPONENTS = 16
 GX_MAX_INLINE_PARAMS = 128
+GX_NOALLOC_MAX_ORBITS = 262144
 
 GX_OK = 0
 GX_ERR_INVALID_ARGUMENT = -1
@@ -81,6 +82,7 @@ SIGNATURES = {
     "gx_ruth4_integrate_hamiltonian": (C.c_int, [_PP, _PF, _P, _I64, _P, _I64, _I32, _P, _P]),
     "gx_calibrate_fma": (C.c_int, [_I32, _I32, _I32, _I64, _P, _P]),
     "gx_batch_integrate_fp32": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P]),
+    "gx_batch_integrate_fp32_noalloc": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _I32, _I32, _P, _P]),
     "gx_batch_integrate_fp64": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P]),
     "gx_dop853_integrate_hamiltonian": (
         C.c_int,

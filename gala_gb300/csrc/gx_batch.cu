@@ -15,8 +15,11 @@
 //   leapfrog  kick-drift-kick as c_leapfrog_step (leapfrog.pyx:35-51)
 //   ruth4     c_ruth4_step (ruth4.pyx:24-35); the d = 0 sub-step's gradient is
 //             skipped here (FP32 form, no bit-parity claim)
+#include <mutex>
+
 #include "gx_host.h"
 #include "gx_fp32.cuh"
+#include "gx_scf.cuh"
 
 namespace gx {
 
@@ -178,4 +181,154 @@ extern "C" int gx_batch_integrate_fp32(const gx_potential *pot, const double *w0
     GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, sizeof(int32_t), st));
     gx::batch_fp32_kernel<<<grid, block, 0, st>>>(dp, A, w0, n_steps, dt, method, order, queue_counter, w_out);
     return gx::check_launch("batch_fp32");
+}
+
+// ===========================================================================
+// Allocation-free variant of the batched FP32 integrator.
+//
+// Some callers cannot allocate device memory: an application whose memory
+// manager owns the whole GPU (a framework's caching allocator, or a service
+// that reserves HBM up front) must not have a library call cudaMalloc behind
+// its back; a host in another language that only receives device pointers from
+// a different runtime has no allocator to call; and cudaMalloc / cudaFree can
+// synchronize the device, which a latency-critical asynchronous pipeline cannot
+// afford.  gx_batch_integrate_fp32_noalloc serves them: the caller passes only
+// inputs and outputs, and the work queue (its counter and the processing order,
+// which gx_batch_integrate_fp32 takes from the caller) lives in the file-scope
+// array below, sized for at most GX_NOALLOC_MAX_ORBITS orbits.  The array exists
+// on every GPU that loads this library until the process exits.
+//
+// Scheduling here is a counting sort on the device: orbits are bucketed by
+// integrator (Ruth4 first) and by log2 of their cost (longest first); within a
+// bucket the order comes from atomics, which changes only which warp runs an
+// orbit, never its arithmetic -- results are bit-identical to the caller-order
+// entry point.
+// ===========================================================================
+namespace gx {
+
+constexpr int NA_BINS_PER_METHOD = 64;
+constexpr int NA_BINS = 2 * NA_BINS_PER_METHOD;
+constexpr int NA_CHUNK = 32;
+// int32 layout: [0] queue counter | [64 .. 64+NA_BINS) histogram / offsets | order
+constexpr int64_t NA_HIST_OFF = 64;
+constexpr int64_t NA_ORDER_OFF = NA_HIST_OFF + NA_BINS + 64;
+constexpr int64_t NA_SLOTS = GX_NOALLOC_MAX_ORBITS + NA_CHUNK;
+constexpr int64_t NA_WORDS = NA_ORDER_OFF + NA_SLOTS;
+
+static __device__ __align__(256) int32_t g_noalloc_scratch[NA_WORDS];
+
+__device__ __forceinline__ int noalloc_bin(int64_t nsteps, int32_t method) {
+    const double cost = (double)nsteps * (method == 1 ? 3.0 : 1.0);
+    int b = (cost >= 1.0) ? (int)log2(cost) : 0;  // 0 .. 62 for any int64 count
+    b = b < NA_BINS_PER_METHOD - 1 ? b : NA_BINS_PER_METHOD - 1;
+    // bins ordered so that bin 0 is processed first: Ruth4, longest first
+    const int rank = (NA_BINS_PER_METHOD - 1 - b);
+    return method == 1 ? rank : NA_BINS_PER_METHOD + rank;
+}
+
+// clear counter and histogram, mark every order slot as padding
+__global__ void noalloc_clear(int32_t *s, int64_t slots) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < NA_ORDER_OFF) s[i] = 0;
+    if (i < slots) s[NA_ORDER_OFF + i] = -1;
+}
+
+__global__ void noalloc_histogram(int32_t *s, const int64_t *__restrict__ nsteps,
+                                  const int32_t *__restrict__ method, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) atomicAdd(&s[NA_HIST_OFF + noalloc_bin(nsteps[i], method[i])], 1);
+}
+
+// exclusive prefix sum of the histogram in place (one thread; NA_BINS entries)
+__global__ void noalloc_scan(int32_t *s) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        int32_t acc = 0;
+        for (int b = 0; b < NA_BINS; b++) {
+            const int32_t c = s[NA_HIST_OFF + b];
+            s[NA_HIST_OFF + b] = acc;
+            acc += c;
+        }
+    }
+}
+
+__global__ void noalloc_scatter(int32_t *s, const int64_t *__restrict__ nsteps, const int32_t *__restrict__ method,
+                                int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const int32_t pos = atomicAdd(&s[NA_HIST_OFF + noalloc_bin(nsteps[i], method[i])], 1);
+        s[NA_ORDER_OFF + pos] = (int32_t)i;
+    }
+}
+
+// Device address of g_noalloc_scratch, looked up once per device (with that
+// device current) by cudaGetSymbolAddress.
+static int noalloc_scratch_address(int32_t **out) {
+    static std::mutex mu;
+    static int32_t *addr[64] = {nullptr};
+    int dev = 0;
+    GX_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("device ordinal %d out of range", dev);
+        return GX_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (addr[dev] == nullptr) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            set_error("cudaGetSymbolAddress(g_noalloc_scratch) failed on device %d: %s", dev, cudaGetErrorString(e));
+            return GX_ERR_CUDA;
+        }
+        addr[dev] = static_cast<int32_t *>(p);
+    }
+    *out = addr[dev];
+    return GX_OK;
+}
+
+}  // namespace gx
+
+extern "C" int gx_batch_integrate_fp32_noalloc(const gx_potential *pot, const double *w0, int64_t n,
+                                               const int64_t *n_steps, const double *dt, const int32_t *method,
+                                               int32_t block, int32_t grid, double *w_out, void *stream) {
+    gx::DevPotF dp;
+    int rc = gx::pack_potential_f32(pot, &dp);
+    if (rc) return rc;
+    if (n < 0 || n > GX_NOALLOC_MAX_ORBITS) {
+        gx::set_error("gx_batch_integrate_fp32_noalloc: n = %lld is outside [0, %d]; its fixed work-queue "
+                      "scratch holds at most GX_NOALLOC_MAX_ORBITS orbits (use gx_batch_integrate_fp32 for more)",
+                      (long long)n, GX_NOALLOC_MAX_ORBITS);
+        return GX_ERR_CAPACITY;
+    }
+    if (n == 0) return GX_OK;
+    GX_CHECK_ARG(w0 && n_steps && dt && method && w_out, "NULL array");
+    GX_CHECK_ARG(block >= 32 && block <= 256 && block % 32 == 0, "block must be a multiple of 32 in [32, 256]");
+    GX_CHECK_ARG(grid >= 1, "grid must be >= 1");
+    int32_t *s = nullptr;
+    rc = gx::noalloc_scratch_address(&s);
+    if (rc) return rc;
+    const int64_t slots = ((n + gx::NA_CHUNK - 1) / gx::NA_CHUNK) * gx::NA_CHUNK;
+    cudaStream_t st = gx::as_stream(stream);
+    const int tb = 256;
+    const int64_t clear_n = slots > gx::NA_ORDER_OFF ? slots : gx::NA_ORDER_OFF;
+    gx::noalloc_clear<<<(unsigned)((clear_n + tb - 1) / tb), tb, 0, st>>>(s, slots);
+    gx::noalloc_histogram<<<(unsigned)((n + tb - 1) / tb), tb, 0, st>>>(s, n_steps, method, n);
+    gx::noalloc_scan<<<1, 32, 0, st>>>(s);
+    gx::noalloc_scatter<<<(unsigned)((n + tb - 1) / tb), tb, 0, st>>>(s, n_steps, method, n);
+    rc = gx::check_launch("noalloc schedule");
+    if (rc) return rc;
+    gx::BatchArgs A;
+    A.n = n;
+    A.slots = slots;
+    A.chunk = gx::NA_CHUNK;
+    A.pad = 0;
+    const double two_13 = std::pow(2., 1. / 3.);
+    const double c[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
+                         (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};
+    const double d[4] = {0., 1. / (2. - two_13), -two_13 / (2. - two_13), 1. / (2. - two_13)};
+    for (int k = 0; k < 4; k++) {
+        A.c[k] = (float)c[k];
+        A.d[k] = (float)d[k];
+    }
+    gx::batch_fp32_kernel<<<grid, block, 0, st>>>(dp, A, w0, n_steps, dt, method, s + gx::NA_ORDER_OFF, s, w_out);
+    return gx::check_launch("batch_fp32 (noalloc)");
 }

@@ -224,6 +224,27 @@ int gx_batch_integrate_fp64(const gx_potential* pot, const double* w0, int64_t n
                             int32_t block, int32_t grid, int32_t* queue_counter,
                             double* w_out, void* stream);
 
+/* Allocation-free form of gx_batch_integrate_fp32.  No counterpart in gala.
+ * For callers that cannot allocate device memory (a process whose memory
+ * manager owns the GPU, a host that only receives device pointers from another
+ * runtime, or a pipeline that cannot afford the device synchronisation of
+ * cudaMalloc / cudaFree): only inputs and outputs are passed, and the work
+ * queue (counter + processing order) lives in a fixed array inside the library,
+ * built on the device by a counting sort (integrator, then cost, longest first).
+ *   n <= GX_NOALLOC_MAX_ORBITS, else GX_ERR_CAPACITY and nothing is launched.
+ *   Per-orbit results are bit-identical to gx_batch_integrate_fp32.
+ *   The first call on a device looks up that array's device address (with
+ *   that device current); make that first call before any stream capture.
+ *   Every call on a device shares the one array: calls that overlap on the GPU
+ *   (different streams, no ordering) race and must not be issued.
+ * The library holds the array (about 1 MB) on every GPU it is loaded on until
+ * the process exits. */
+#define GX_NOALLOC_MAX_ORBITS 262144
+int gx_batch_integrate_fp32_noalloc(const gx_potential* pot, const double* w0, int64_t n,
+                                    const int64_t* n_steps, const double* dt,
+                                    const int32_t* method, int32_t block, int32_t grid,
+                                    double* w_out, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Pipe calibration.  No counterpart in gala: it measures the FP64 / FP32     */
 /* multiply-add throughput that bounds the integrators (the roofline          */

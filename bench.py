@@ -53,6 +53,13 @@ def parse_args():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gx", choices=["gx", "reference"])
+    p.add_argument("--workload", default="mw_dop853", choices=["mw_dop853", "uneven_batch"],
+                   help="mw_dop853: the headline line; uneven_batch: only the batched FP32c/FP64 "
+                        "comparison (used for profiling)")
+    p.add_argument("--batch-orbits", type=int, default=262_144)
+    p.add_argument("--batch-step-scale", type=float, default=1.0, help="multiply the batch step counts")
+    p.add_argument("--batch-precision", default="both", choices=["both", "fp32c", "fp64"])
+    p.add_argument("--no-autotune", action="store_true", help="use the cached or default launch shape")
     p.add_argument("--orbits", type=int, default=100_000)
     p.add_argument("--nsteps", type=int, default=10_000)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -205,6 +212,57 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_uneven_batch(args, torch, stream):
+    """The batched uneven workload (262,144 MW-composite orbits, n_steps log-uniform
+    in [100, 20000], dt from {0.1, 0.5, 1.0} Myr, Leapfrog for half, Ruth4 for
+    half), integrated by the FP32-compensated persistent kernel and by the plain
+    FP64 batch kernel, each as one CUDA-graph replay (queue reset, persistent
+    kernel, FP64 energy diagnostic).  Returns throughput, accuracy, launch shapes."""
+    from gala_gb300 import workloads as W
+    from gala_gb300.batch import BatchIntegrator
+
+    pot = W.mw_composite()
+    n = args.batch_orbits
+    w0 = W.mw_ics(n, seed=W.SEED_BASE + 3)
+    nsteps, dt, method = W.uneven_steps(n)
+    if args.batch_step_scale != 1.0:
+        nsteps = np.maximum(1, np.round(nsteps * args.batch_step_scale)).astype(np.int64)
+    total = int(nsteps.sum())
+    res = {"workload": f"uneven_batch: {n} MW-composite orbits, n_steps log-U[100,20000] x "
+                       f"{args.batch_step_scale}, dt in {{0.1,0.5,1}} Myr, half Leapfrog half Ruth4",
+           "orbit_steps": total}
+    outs = {}
+    precs = ["fp32c", "fp64"] if args.batch_precision == "both" else [args.batch_precision]
+    for prec in precs:
+        b = BatchIntegrator(pot, w0, nsteps, dt, method, precision=prec)
+        if not args.no_autotune:
+            b.autotune(work_fraction=0.05 if prec == "fp32c" else 0.004, reps=2)
+        b.capture()
+        for _ in range(max(1, args.warmup)):
+            b.run()
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(max(1, args.steps)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.run()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        ms = float(np.mean(times))
+        dE = b.energy_drift().cpu().numpy()
+        outs[prec] = b.w_out.cpu().numpy()
+        res[prec] = {"value": total / (ms * 1e-3), "unit": UNIT, "ms_per_run": ms, "config": b.config,
+                     "dE_over_E_median": float(np.median(dE)), "dE_over_E_p99": float(np.percentile(dE, 99)),
+                     "gpu_launches_per_run": 3}
+    if len(outs) == 2:
+        err = np.linalg.norm(outs["fp32c"][:3] - outs["fp64"][:3], axis=0) / np.linalg.norm(outs["fp64"][:3], axis=0)
+        res["fp32c_position_error_vs_fp64"] = {"median": float(np.median(err)),
+                                               "p99": float(np.percentile(err, 99)), "max": float(np.max(err))}
+        res["speedup_fp32c_vs_fp64"] = res["fp32c"]["value"] / res["fp64"]["value"]
+    return res
+
+
 def run_gx(args):
     import torch
 
@@ -221,6 +279,11 @@ def run_gx(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
     sh = int(stream.cuda_stream)
+    if args.workload == "uneven_batch":
+        res = run_uneven_batch(args, torch, stream)
+        if rank == 0:
+            print(json.dumps(res), flush=True)
+        return
     mw = W.mw_composite()
     n, nsteps, stride, nbatch = args.orbits, args.nsteps, 100, 100
     w0 = W.mw_ics(n, seed=W.SEED_BASE + 2 + 1000 * rank)
@@ -305,6 +368,7 @@ def run_gx(args):
 
     peak = measure_fp64_peak(torch, stream)
     achieved = flops / (mean_ms * 1e-3) / 1e12
+    variants = {"uneven_batch": run_uneven_batch(args, torch, stream)}
 
     if rank != 0:
         return
@@ -342,6 +406,7 @@ def run_gx(args):
                             "rejected": float(np.mean(stt[:, 3]))},
         "clocks": clocks.summary(),
         "wall_s_timed_region": wall,
+        "variants": variants,
     }
     if world == 1 and not args.no_cpu_baseline:
         base, sample, cpu_out = cpu_reference_run(n, nsteps, args.cpu_seconds, 1, 0)

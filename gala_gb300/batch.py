@@ -24,11 +24,11 @@ from . import _abi
 LEAPFROG, RUTH4 = 0, 1
 COST = {LEAPFROG: 1.0, RUTH4: 3.0}   # gradient evaluations per step
 CACHE = Path(os.environ.get("GALA_GB300_AUTOTUNE", Path(__file__).resolve().parent / "_build" / "autotune.json"))
-DEFAULT_CONFIG = {"fp32c": {"block": 128, "ctas_per_sm": 4, "chunk": 32},
+DEFAULT_CONFIG = {"fp32c": {"block": 128, "ctas_per_sm": 8, "chunk": 32},
                   "fp64": {"block": 64, "ctas_per_sm": 4, "chunk": 32}}
 SEARCH = {
-    "fp32c": [{"block": b, "ctas_per_sm": c, "chunk": k} for b in (64, 128, 256) for c in (1, 2, 4, 8, 16)
-              for k in (32, 64) if 256 <= b * c <= 1024],
+    "fp32c": [{"block": b, "ctas_per_sm": c, "chunk": k} for b in (64, 128, 256) for c in (1, 2, 3, 4, 6, 8, 12, 16)
+              for k in (32, 64) if 256 <= b * c <= 1536],
     "fp64": [{"block": b, "ctas_per_sm": c, "chunk": k} for b in (32, 64, 128) for c in (1, 2, 4, 8)
              for k in (32, 64) if 64 <= b * c <= 512],
 }
@@ -121,9 +121,7 @@ class BatchIntegrator:
         self.order = schedule(self.n_steps, self.method, self.config["chunk"])
         self._order_chunk = self.config["chunk"]
 
-    def _launch(self, stream_handle):
-        import ctypes as C
-
+    def _launch_integrator(self, stream_handle):
         from ._device import ptr
 
         cfg = self.config
@@ -133,6 +131,14 @@ class BatchIntegrator:
         _abi.call(ENTRY[self.precision], desc, ptr(self.w0), self.n, ptr(self.n_steps), ptr(self.dt),
                   ptr(self.method), ptr(self.order), self.order.numel(), cfg["chunk"], cfg["block"],
                   cfg["ctas_per_sm"] * self.sms, ptr(self.counter), ptr(self.w_out), stream_handle)
+        return desc
+
+    def _launch(self, stream_handle):
+        import ctypes as C
+
+        from ._device import ptr
+
+        desc = self._launch_integrator(stream_handle)
         frame = _abi.gx_frame()
         _abi.call("gx_hamiltonian_value", desc, C.byref(frame), 0.0, ptr(self.w0), self.n, ptr(self.E0),
                   stream_handle)
@@ -203,15 +209,17 @@ class BatchIntegrator:
         sub = BatchIntegrator(self.potential, self.w0, scaled, self.dt, self.method,
                               config=DEFAULT_CONFIG[self.precision], precision=self.precision)
         results = []
+        stream = torch.cuda.current_stream()
         for cfg in SEARCH[self.precision]:
             sub.config = cfg
-            sub._launch(stream_handle())
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
+            sub._launch_integrator(stream_handle())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
             for _ in range(reps):
-                sub._launch(stream_handle())
-            torch.cuda.synchronize()
-            results.append(((time.perf_counter() - t0) / reps, cfg))
+                sub._launch_integrator(stream_handle())
+            e1.record(stream)
+            e1.synchronize()
+            results.append((e0.elapsed_time(e1) * 1e-3 / reps, cfg))
         best = min(results, key=lambda r: r[0])[1]
         self.config = dict(best)
         self.tune_results = [(t, c) for t, c in sorted(results, key=lambda r: r[0])]

@@ -36,6 +36,7 @@ __device__ __forceinline__ void split(double x, float &hi, float &lo) {
     lo = (float)(x - (double)hi);
 }
 
+template <typename S>
 __device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const BatchArgs &A, const double *w0,
                                                    int64_t n, int64_t i, int64_t nsteps, float h, int meth,
                                                    double *w_out) {
@@ -50,11 +51,11 @@ __device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const Bat
     }
     if (meth == 0) {
         // c_init_velocity: v_{1/2} = v - g h / 2
-        potential_gradient_f(pot, xh, g);
+        potential_gradient_f<S>(pot, xh, g);
         for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h * 0.5f);
         for (int64_t j = 0; j < nsteps; j++) {
             for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], h, vl[k] * h));
-            potential_gradient_f(pot, xh, g);
+            potential_gradient_f<S>(pot, xh, g);
             for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h);
         }
         // output velocity at the last step: v_{n+1/2} + g h / 2
@@ -65,7 +66,7 @@ __device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const Bat
             for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], A.c[0] * fmaf(vh[k], h, vl[k] * h));
 #pragma unroll
             for (int s = 1; s < 4; s++) {
-                potential_gradient_f(pot, xh, g);
+                potential_gradient_f<S>(pot, xh, g);
                 for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -A.d[s] * g[k] * h);
                 for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], A.c[s] * fmaf(vh[k], h, vl[k] * h));
             }
@@ -77,6 +78,7 @@ __device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const Bat
     }
 }
 
+template <typename S>
 __global__ void __launch_bounds__(256) batch_fp32_kernel(const __grid_constant__ DevPotF pot, BatchArgs A,
                                                          const double *__restrict__ w0,
                                                          const int64_t *__restrict__ nsteps,
@@ -95,7 +97,7 @@ __global__ void __launch_bounds__(256) batch_fp32_kernel(const __grid_constant__
             const int64_t slot = (int64_t)c * A.chunk + r + lane;
             const int32_t i = order[slot];
             if (i >= 0 && i < A.n)
-                integrate_one_fp32(pot, A, w0, A.n, i, nsteps[i], (float)dt[i], method[i], w_out);
+                integrate_one_fp32<S>(pot, A, w0, A.n, i, nsteps[i], (float)dt[i], method[i], w_out);
         }
     }
 }
@@ -148,6 +150,34 @@ int pack_potential_f32(const gx_potential *pot, DevPotF *out) {
     return GX_OK;
 }
 
+// Launch the persistent kernel, specialised when the component list is one of
+// the compiled signatures (no shift/rotate), generic otherwise.
+static void launch_batch_fp32(const DevPotF &dp, const BatchArgs &A, const double *w0, const int64_t *nsteps,
+                              const double *dt, const int32_t *method, const int32_t *order, int32_t *counter,
+                              double *w_out, int grid, int block, cudaStream_t st) {
+    auto is = [&](int a, int b, int c, int d) {
+        const int want[4] = {a, b, c, d};
+        int nc = 0;
+        for (int k = 0; k < 4; k++) nc += want[k] >= 0;
+        if (dp.ncomp != nc) return false;
+        for (int k = 0; k < nc; k++)
+            if (dp.c[k].type != want[k] || dp.c[k].do_sr) return false;
+        return true;
+    };
+    constexpr int H = GX_POT_HERNQUIST, MN = GX_POT_MIYAMOTONAGAI, NFW = GX_POT_SPHERICALNFW, P = GX_POT_PLUMMER;
+#define GX_LAUNCH(SIG) batch_fp32_kernel<SIG><<<grid, block, 0, st>>>(dp, A, w0, nsteps, dt, method, order, counter, w_out)
+    using SigHHMN = PotSig<H, H, MN, NFW>;
+    using SigMNHH = PotSig<MN, H, H, NFW>;
+    using SigH = PotSig<H, -1, -1, -1>;
+    using SigP = PotSig<P, -1, -1, -1>;
+    if (is(H, H, MN, NFW)) GX_LAUNCH(SigHHMN);
+    else if (is(MN, H, H, NFW)) GX_LAUNCH(SigMNHH);
+    else if (is(H, -1, -1, -1)) GX_LAUNCH(SigH);
+    else if (is(P, -1, -1, -1)) GX_LAUNCH(SigP);
+    else GX_LAUNCH(SigGeneric);
+#undef GX_LAUNCH
+}
+
 }  // namespace gx
 
 extern "C" int gx_batch_integrate_fp32(const gx_potential *pot, const double *w0, int64_t n,
@@ -179,7 +209,7 @@ extern "C" int gx_batch_integrate_fp32(const gx_potential *pot, const double *w0
     }
     cudaStream_t st = gx::as_stream(stream);
     GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, sizeof(int32_t), st));
-    gx::batch_fp32_kernel<<<grid, block, 0, st>>>(dp, A, w0, n_steps, dt, method, order, queue_counter, w_out);
+    gx::launch_batch_fp32(dp, A, w0, n_steps, dt, method, order, queue_counter, w_out, grid, block, st);
     return gx::check_launch("batch_fp32");
 }
 
@@ -329,6 +359,6 @@ extern "C" int gx_batch_integrate_fp32_noalloc(const gx_potential *pot, const do
         A.c[k] = (float)c[k];
         A.d[k] = (float)d[k];
     }
-    gx::batch_fp32_kernel<<<grid, block, 0, st>>>(dp, A, w0, n_steps, dt, method, s + gx::NA_ORDER_OFF, s, w_out);
+    gx::launch_batch_fp32(dp, A, w0, n_steps, dt, method, s + gx::NA_ORDER_OFF, s, w_out, grid, block, st);
     return gx::check_launch("batch_fp32 (noalloc)");
 }

@@ -1,12 +1,19 @@
 // gx_fp32.cuh -- FP32 force evaluation for the compensated integrators.
 //
-// The closed-form potentials of gx_device.cuh, evaluated in FP32 with the
-// special-function units: 1/sqrt via rsqrt, reciprocals via the fast
-// reciprocal, and the NFW radial factor f(u) = ln(1+u) - u/(1+u) computed
-// without cancellation (for u < 1 as the positive series in w = u/(1+u):
-// f = sum_{k>=2} w^k / k; for u >= 1 directly).  Relative force error is a
-// few FP32 ulps; the integrators accumulate positions and velocities in
-// compensated (Kahan) form so that FP32 rounding of the state does not build up.
+// The closed-form potentials of gx_device.cuh, evaluated in FP32 on the
+// special-function unit: 1/sqrt, reciprocal and log2 are single approximate
+// MUFU instructions (relative error a few 1e-8), and the NFW radial factor
+// f(u) = ln(1+u) - u/(1+u) is computed without cancellation (for u < 1 as the
+// positive series in w = u/(1+u): f = sum_{k>=2} w^k / k; for u >= 1 directly).
+// The integrators accumulate positions and velocities in compensated (Kahan)
+// form, so FP32 rounding of the state does not build up; the force error (a
+// few FP32 ulps) acts like a slightly perturbed potential.
+//
+// Each component type has a compile-time evaluator (comp_grad_t<TYPE>); a
+// potential whose component list is known at compile time (PotSig below) is
+// evaluated with no per-component branching, which lets the compiler overlap
+// the independent component evaluations.  Any other list goes through the
+// run-time switch.
 #pragma once
 
 #include <cstdint>
@@ -30,100 +37,138 @@ struct DevPotF {
     DevCompF c[GX_MAX_COMPONENTS];
 };
 
-__device__ __forceinline__ float frcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 
 // f(u)/u^3 for the NFW force, u = r / r_s.
 __device__ __forceinline__ float nfw_f_over_u3(float u) {
+    const float opu = 1.0f + u;
+    const float iopu = rcp_approx(opu);
     if (u < 1.0f) {
-        const float w = u * frcp(1.0f + u);
-        // sum_{k=2}^{25} w^k / k, Horner in w (w <= 1/2: truncation < 2^-25 relative)
+        const float w = u * iopu;
+        // sum_{k=2}^{25} w^k / k as w^2 * s, Horner in w (w < 1/2: truncation < 2^-25)
         float s = 1.0f / 25.0f;
 #pragma unroll
         for (int k = 24; k >= 2; k--) s = fmaf(s, w, 1.0f / (float)k);
-        // f = w^2 * s ; w^2 / u^3 = 1 / (u (1+u)^2)
-        const float opu = 1.0f + u;
-        return s * frcp(u * opu * opu);
+        // w^2 / u^3 = 1 / (u (1+u)^2)
+        return s * rcp_approx(u) * iopu * iopu;
     }
-    const float f = log1pf(u) - u * frcp(1.0f + u);
-    return f * frcp(u * u * u);
+    const float f = lg2_approx(opu) * 0.69314718055994531f - u * iopu;
+    const float iu = rcp_approx(u);
+    return f * iu * iu * iu;
 }
 
-// Gradient of one component (accumulated into g), FP32.
-__device__ __forceinline__ void comp_gradient_f(const DevCompF &c, const float *q, float *g) {
-    const float *p = c.p;
-    switch (c.type) {
-    case GX_POT_KEPLER: {  // p = {G m}
-        const float ri = rsqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+// Gradient of one component of compile-time type T, accumulated into g.
+template <int T>
+__device__ __forceinline__ void comp_grad_t(const float *p, const float *q, float *g) {
+    if constexpr (T == GX_POT_KEPLER) {  // p = {G m}
+        const float ri = rsqrt_approx(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
         const float fac = p[0] * ri * ri * ri;
         g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2];
-        return;
-    }
-    case GX_POT_HERNQUIST: {  // p = {G m, c}
+    } else if constexpr (T == GX_POT_HERNQUIST) {  // p = {G m, c}
         const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-        const float ri = rsqrtf(r2);
-        const float r = r2 * ri;
-        const float rc = r + p[1];
-        const float fac = p[0] * ri * frcp(rc * rc);
+        const float ri = rsqrt_approx(r2);
+        const float rc = fmaf(r2, ri, p[1]);
+        const float irc = rcp_approx(rc);
+        const float fac = p[0] * ri * irc * irc;
         g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2];
-        return;
-    }
-    case GX_POT_PLUMMER: {  // p = {G m, b^2}
-        const float ri = rsqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + p[1]);
+    } else if constexpr (T == GX_POT_PLUMMER) {  // p = {G m, b^2}
+        const float ri = rsqrt_approx(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + p[1]);
         const float fac = p[0] * ri * ri * ri;
         g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2];
-        return;
-    }
-    case GX_POT_MIYAMOTONAGAI: {  // p = {G m, a, b^2}
-        const float szi = rsqrtf(q[2] * q[2] + p[2]);
-        const float sz = (q[2] * q[2] + p[2]) * szi;
-        const float zd = p[1] + sz;
-        const float ti = rsqrtf(q[0] * q[0] + q[1] * q[1] + zd * zd);
+    } else if constexpr (T == GX_POT_MIYAMOTONAGAI) {  // p = {G m, a, b^2}
+        const float z2b = fmaf(q[2], q[2], p[2]);
+        const float szi = rsqrt_approx(z2b);
+        const float zd = fmaf(z2b, szi, p[1]);
+        const float ti = rsqrt_approx(q[0] * q[0] + q[1] * q[1] + zd * zd);
         const float fac = p[0] * ti * ti * ti;
-        g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2] * (1.0f + p[1] * szi);
-        return;
-    }
-    case GX_POT_SPHERICALNFW: {  // p = {G m / r_s^3, 1 / r_s}
+        g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2] * fmaf(p[1], szi, 1.0f);
+    } else if constexpr (T == GX_POT_SPHERICALNFW) {  // p = {G m / r_s^3, 1 / r_s}
         const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-        const float u = r2 * rsqrtf(r2) * p[1];
+        const float u = r2 * rsqrt_approx(r2) * p[1];
         const float fac = p[0] * nfw_f_over_u3(u);
         g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2];
-        return;
-    }
-    case GX_POT_FLATTENEDNFW: {  // p = {G m / r_s^3, 1 / r_s, 1 / c^2}
+    } else if constexpr (T == GX_POT_FLATTENEDNFW) {  // p = {G m / r_s^3, 1 / r_s, 1 / c^2}
         const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] * p[2];
-        const float u = r2 * rsqrtf(r2) * p[1];
+        const float u = r2 * rsqrt_approx(r2) * p[1];
         const float fac = p[0] * nfw_f_over_u3(u);
         g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2] * p[2];
-        return;
-    }
-    case GX_POT_TRIAXIALNFW: {  // p = {G m / r_s^3, 1 / r_s, 1/a^2, 1/b^2, 1/c^2}
+    } else if constexpr (T == GX_POT_TRIAXIALNFW) {  // p = {G m / r_s^3, 1 / r_s, 1/a^2, 1/b^2, 1/c^2}
         const float r2 = q[0] * q[0] * p[2] + q[1] * q[1] * p[3] + q[2] * q[2] * p[4];
-        const float u = r2 * rsqrtf(r2) * p[1];
+        const float u = r2 * rsqrt_approx(r2) * p[1];
         const float fac = p[0] * nfw_f_over_u3(u);
         g[0] += fac * q[0] * p[2]; g[1] += fac * q[1] * p[3]; g[2] += fac * q[2] * p[4];
-        return;
-    }
-    default:
-        return;  // GX_POT_NULL
     }
 }
 
+// Run-time dispatch on the component type.
+__device__ __forceinline__ void comp_gradient_f(const DevCompF &c, const float *q, float *g) {
+    switch (c.type) {
+    case GX_POT_KEPLER: comp_grad_t<GX_POT_KEPLER>(c.p, q, g); return;
+    case GX_POT_HERNQUIST: comp_grad_t<GX_POT_HERNQUIST>(c.p, q, g); return;
+    case GX_POT_PLUMMER: comp_grad_t<GX_POT_PLUMMER>(c.p, q, g); return;
+    case GX_POT_MIYAMOTONAGAI: comp_grad_t<GX_POT_MIYAMOTONAGAI>(c.p, q, g); return;
+    case GX_POT_SPHERICALNFW: comp_grad_t<GX_POT_SPHERICALNFW>(c.p, q, g); return;
+    case GX_POT_FLATTENEDNFW: comp_grad_t<GX_POT_FLATTENEDNFW>(c.p, q, g); return;
+    case GX_POT_TRIAXIALNFW: comp_grad_t<GX_POT_TRIAXIALNFW>(c.p, q, g); return;
+    default: return;  // GX_POT_NULL
+    }
+}
+
+__device__ __forceinline__ void comp_gradient_sr(const DevCompF &c, const float *q, float *g) {
+    if (!c.do_sr) {
+        comp_gradient_f(c, q, g);
+        return;
+    }
+    const float x = q[0] - c.q0[0], y = q[1] - c.q0[1], z = q[2] - c.q0[2];
+    const float qt[3] = {c.R[0] * x + c.R[1] * y + c.R[2] * z, c.R[3] * x + c.R[4] * y + c.R[5] * z,
+                         c.R[6] * x + c.R[7] * y + c.R[8] * z};
+    float gt[3] = {0.f, 0.f, 0.f};
+    comp_gradient_f(c, qt, gt);
+    g[0] += c.R[0] * gt[0] + c.R[3] * gt[1] + c.R[6] * gt[2];
+    g[1] += c.R[1] * gt[0] + c.R[4] * gt[1] + c.R[7] * gt[2];
+    g[2] += c.R[2] * gt[0] + c.R[5] * gt[1] + c.R[8] * gt[2];
+}
+
+// Component lists known at compile time (-1 = no component).  SIG_GENERIC
+// means: use the run-time loop over pot.ncomp components.
+template <int T0, int T1, int T2, int T3>
+struct PotSig {
+    static constexpr bool generic = (T0 == -2);
+};
+using SigGeneric = PotSig<-2, -1, -1, -1>;
+
+template <typename S>
+struct SigTypes;
+template <int T0, int T1, int T2, int T3>
+struct SigTypes<PotSig<T0, T1, T2, T3>> {
+    static constexpr int t0 = T0, t1 = T1, t2 = T2, t3 = T3;
+};
+
+template <typename S>
 __device__ __forceinline__ void potential_gradient_f(const DevPotF &pot, const float *q, float *g) {
     g[0] = 0.f; g[1] = 0.f; g[2] = 0.f;
-    for (int i = 0; i < pot.ncomp; i++) {
-        const DevCompF &c = pot.c[i];
-        if (!c.do_sr) {
-            comp_gradient_f(c, q, g);
-        } else {
-            const float x = q[0] - c.q0[0], y = q[1] - c.q0[1], z = q[2] - c.q0[2];
-            const float qt[3] = {c.R[0] * x + c.R[1] * y + c.R[2] * z, c.R[3] * x + c.R[4] * y + c.R[5] * z,
-                                 c.R[6] * x + c.R[7] * y + c.R[8] * z};
-            float gt[3] = {0.f, 0.f, 0.f};
-            comp_gradient_f(c, qt, gt);
-            g[0] += c.R[0] * gt[0] + c.R[3] * gt[1] + c.R[6] * gt[2];
-            g[1] += c.R[1] * gt[0] + c.R[4] * gt[1] + c.R[7] * gt[2];
-            g[2] += c.R[2] * gt[0] + c.R[5] * gt[1] + c.R[8] * gt[2];
-        }
+    if constexpr (S::generic) {
+        for (int i = 0; i < pot.ncomp; i++) comp_gradient_sr(pot.c[i], q, g);
+    } else {
+        using T = SigTypes<S>;
+        if constexpr (T::t0 >= 0) comp_grad_t<T::t0>(pot.c[0].p, q, g);
+        if constexpr (T::t1 >= 0) comp_grad_t<T::t1>(pot.c[1].p, q, g);
+        if constexpr (T::t2 >= 0) comp_grad_t<T::t2>(pot.c[2].p, q, g);
+        if constexpr (T::t3 >= 0) comp_grad_t<T::t3>(pot.c[3].p, q, g);
     }
 }
 

@@ -28,6 +28,8 @@ UNITS = {
     "gx_dop853.cu": ["-fmad=false"],
     "gx_peaks.cu": [],
     "gx_batch.cu": [],
+    "gx_mlp_train.cu": [],
+    "gx_mlp_infer.cu": [],
 }
 
 

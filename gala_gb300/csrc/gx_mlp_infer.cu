@@ -1,0 +1,574 @@
+// gx_mlp_infer.cu -- surrogate force on BF16 tensor cores, and the FP32
+// leapfrog that integrates orbits in it.
+//
+// One CTA (8 warps) owns a tile of 64 positions.  For the tile it runs the
+// network forward (layer 1 in FP32 on the CUDA cores, layers 2-4 as 64x256x256
+// BF16 MMAs with FP32 accumulation) and the input-gradient backward pass
+// (three more 64x256x256 MMAs against the transposed weights), then the
+// chain rule through the input map (gx_mlp.cuh) gives grad Phi.  Layout:
+//   * activations / deltas: BF16 [64][256] in shared memory, double-buffered
+//     (rows padded by 16 bytes so ldmatrix is conflict-free);
+//   * weights: BF16 [256][256] in global memory (L2-resident, 768 KB for the
+//     six matrices W2, W3, W4, W4^T, W3^T, W2^T), staged per GEMM in four
+//     64-wide K slabs, double-buffered with cp.async;
+//   * silu'(z_l) for the backward pass stays in registers (FP16 pairs), in the
+//     MMA accumulator layout, so it never leaves the SM;
+//   * y (the value) and G = dy/dxh are reduced from the accumulators.
+// Warp tiling: 2 (rows) x 4 (columns) warps, 32 x 64 outputs per warp,
+// mma.sync.m16n8k16 (2 x 8 tiles per k16 step).
+//
+// Orbits (the integrating form): threads 0..63 own one orbit each, carried as
+// FP32 (hi, lo) Kahan pairs like gx_batch.cu; every step: drift, surrogate
+// force for the tile, kick.  Positions outside the trained radius range use the
+// analytic SCF force in FP32 instead (per-orbit fallback).
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "gx_host.h"
+#include "gx_mlp.cuh"
+
+namespace gx {
+namespace mlpi {
+
+using namespace gx::mlp;
+
+constexpr int TM = 64;                 // positions per CTA
+constexpr int NT = 256;                // threads per CTA
+constexpr int AST = H + 8;             // activation row stride (bf16 elements): 528 bytes
+constexpr int KS = 64;                 // K slab
+constexpr int WST = KS + 8;            // weight slab row stride (bf16): 144 bytes
+constexpr int SMEM_A = 2 * TM * AST * 2;     // two activation buffers
+constexpr int SMEM_W = 2 * H * WST * 2;      // two weight slabs
+constexpr int SMEM_MISC = TM * 8 * 4 + 4 * TM * 4 * 4;
+constexpr int SMEM_BYTES = SMEM_A + SMEM_W + SMEM_MISC;
+
+struct InferArgs {
+    // input map / output scaling
+    float r_min, r_max, rho0, inv_log_ratio;   // inv_log_ratio = 1 / ln(r_max / r_min)
+    float GM, r_s;                              // Hernquist base (the S000 term)
+    // analytic fallback (FP32 SCF, gala packing [G, nmax, lmax, M, r_s, S, T])
+    const float *scf;                           // float copy of the packed SCF parameters
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t addr, uint32_t &r0, uint32_t &r1, uint32_t &r2, uint32_t &r3) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16(float *c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem)), "l"(gmem));
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;"); }
+__device__ __forceinline__ void cp_wait0() { asm volatile("cp.async.wait_group 0;"); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;"); }
+
+// Stage K slab `s` (columns s*64 .. s*64+63) of a [256][256] bf16 matrix into ws.
+__device__ __forceinline__ void load_slab(__nv_bfloat16 *ws, const __nv_bfloat16 *Wg, int s) {
+    // 256 rows x 64 bf16 = 256 x 128 bytes = 2048 chunks of 16 bytes, 8 per thread
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const int chunk = threadIdx.x + i * NT;
+        const int row = chunk >> 3, c16 = chunk & 7;
+        cp_async16(ws + row * WST + c16 * 8, Wg + (size_t)row * H + s * KS + c16 * 8);
+    }
+    cp_commit();
+}
+
+// acc[2][8][4] += A(64x256, smem) x W^T where W (global [256 n][256 k]) is the
+// B operand (k contiguous per output n).  The first slab of W must already be
+// in flight in slab buffer 0.
+__device__ __forceinline__ void gemm_tile(float (&acc)[2][8][4], const __nv_bfloat16 *As,
+                                          __nv_bfloat16 *Ws, const __nv_bfloat16 *Wg) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = warp >> 2, wn = warp & 3;
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc[i][j][k] = 0.f;
+    for (int s = 0; s < H / KS; s++) {
+        if (s + 1 < H / KS) {
+            load_slab(Ws + ((s + 1) & 1) * H * WST, Wg, s + 1);
+            cp_wait1();
+        } else {
+            cp_wait0();
+        }
+        __syncthreads();
+        const __nv_bfloat16 *wsb = Ws + (s & 1) * H * WST;
+#pragma unroll
+        for (int kk = 0; kk < KS; kk += 16) {
+            uint32_t a[2][4];
+#pragma unroll
+            for (int i = 0; i < 2; i++) {
+                const int row = wm * 32 + i * 16 + (lane & 15);
+                const int col = s * KS + kk + (lane >> 4) * 8;
+                ldsm_x4(smem_u32(As + row * AST + col), a[i][0], a[i][1], a[i][2], a[i][3]);
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j += 2) {
+                // two n-tiles (16 outputs) x k16 from the slab: matrices (n0..7,k0..7), (n0..7,k8..15),
+                // (n8..15,k0..7), (n8..15,k8..15)
+                const int n = wn * 64 + j * 8 + (lane & 7) + ((lane >> 4) << 3);
+                const int k = kk + ((lane >> 3) & 1) * 8;
+                uint32_t b0, b1, b2, b3;
+                ldsm_x4(smem_u32(wsb + n * WST + k), b0, b1, b2, b3);
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    mma_bf16(acc[i][j], a[i][0], a[i][1], a[i][2], a[i][3], b0, b1);
+                    mma_bf16(acc[i][j + 1], a[i][0], a[i][1], a[i][2], a[i][3], b2, b3);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Accumulator element (i, j, k) of this thread -> (row, col) of the 64x256 tile.
+__device__ __forceinline__ int acc_row(int i, int k) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    return (warp >> 2) * 32 + i * 16 + (lane >> 2) + ((k >> 1) << 3);
+}
+__device__ __forceinline__ int acc_col(int j, int k) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    return (warp & 3) * 64 + j * 8 + ((lane & 3) << 1) + (k & 1);
+}
+
+// Sum over the columns of a per-thread partial (row-indexed by (i, k>>1)) into
+// red[4 col-warps][64 rows]; the caller sums the 4 column-warps.
+__device__ __forceinline__ void row_reduce(float (&part)[2][2], float *red) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            float v = part[i][h];
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            v += __shfl_xor_sync(0xffffffffu, v, 2);
+            if ((lane & 3) == 0) red[(warp & 3) * TM + (warp >> 2) * 32 + i * 16 + (lane >> 2) + h * 8] = v;
+        }
+}
+
+// One surrogate evaluation for the tile whose inputs xh[64][3] are in smem.
+// Outputs: yv[64] (network value) and G[64][3] (dy/dxh) in smem.
+__device__ __forceinline__ void tile_eval(const float *__restrict__ P, const __nv_bfloat16 *__restrict__ Wb, char *smem,
+                          const float *xh, float *yv, float *G) {
+    __nv_bfloat16 *Abuf = reinterpret_cast<__nv_bfloat16 *>(smem);
+    __nv_bfloat16 *Ws = reinterpret_cast<__nv_bfloat16 *>(smem + SMEM_A);
+    float *red = reinterpret_cast<float *>(smem + SMEM_A + SMEM_W + TM * 8 * 4);  // [4][4][64]
+    float acc[2][8][4];
+    __half2 sp[4][2][8][2];  // silu'(z_l) for l = 1..4 (index l-1), accumulator layout
+    const __nv_bfloat16 *Wfwd[3] = {Wb, Wb + H * H, Wb + 2 * H * H};           // W2, W3, W4
+    const __nv_bfloat16 *Wbwd[3] = {Wb + 3 * H * H, Wb + 4 * H * H, Wb + 5 * H * H};  // W4^T, W3^T, W2^T
+
+    // prefetch the first slab of W2 while layer 1 runs on the CUDA cores
+    load_slab(Ws, Wfwd[0], 0);
+
+    // layer 1 (K = 3, FP32) directly in the accumulator layout
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                float s1v[2];
+#pragma unroll
+                for (int e = 0; e < 2; e++) {
+                    const int k = h * 2 + e;
+                    const int r = acc_row(i, k), c = acc_col(j, k);
+                    const float z = P[OFF_W1 + c * 3 + 0] * xh[r * 3 + 0] + P[OFF_W1 + c * 3 + 1] * xh[r * 3 + 1] +
+                                    P[OFF_W1 + c * 3 + 2] * xh[r * 3 + 2] + P[OFF_B1 + c];
+                    float a, s1, s2;
+                    silu3(z, a, s1, s2);
+                    (void)s2;
+                    acc[i][j][k] = a;
+                    s1v[e] = s1;
+                }
+                sp[0][i][j][h] = __floats2half2_rn(s1v[0], s1v[1]);
+            }
+    // write a1 (bf16) into Abuf[0]
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int r = acc_row(i, h * 2), c = acc_col(j, h * 2);
+                *reinterpret_cast<__nv_bfloat162 *>(Abuf + r * AST + c) =
+                    __floats2bfloat162_rn(acc[i][j][h * 2], acc[i][j][h * 2 + 1]);
+            }
+    __syncthreads();
+
+    // layers 2..4
+    int cur = 0;
+#pragma unroll
+    for (int l = 2; l <= 4; l++) {
+        gemm_tile(acc, Abuf + cur * TM * AST, Ws, Wfwd[l - 2]);
+        if (l < 4) load_slab(Ws, Wfwd[l - 1], 0);
+        const float *b = P + off_b(l);
+        __nv_bfloat16 *nxt = Abuf + (cur ^ 1) * TM * AST;
+        float ypart[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    float av[2], s1v[2];
+#pragma unroll
+                    for (int e = 0; e < 2; e++) {
+                        const int k = h * 2 + e;
+                        const int c = acc_col(j, k);
+                        float a, s1, s2;
+                        silu3(acc[i][j][k] + b[c], a, s1, s2);
+                        (void)s2;
+                        av[e] = a;
+                        s1v[e] = s1;
+                        if (l == 4) ypart[i][h] += a * P[OFF_W5 + c];
+                    }
+                    sp[l - 1][i][j][h] = __floats2half2_rn(s1v[0], s1v[1]);
+                    if (l == 4) {
+                        // backward seed: delta_4 = w5 * silu'(z4)
+                        const int c = acc_col(j, h * 2);
+                        av[0] = P[OFF_W5 + c] * s1v[0];
+                        av[1] = P[OFF_W5 + c + 1] * s1v[1];
+                    }
+                    const int r = acc_row(i, h * 2), c = acc_col(j, h * 2);
+                    *reinterpret_cast<__nv_bfloat162 *>(nxt + r * AST + c) = __floats2bfloat162_rn(av[0], av[1]);
+                }
+        if (l == 4) row_reduce(ypart, red);
+        cur ^= 1;
+        __syncthreads();
+    }
+    if (threadIdx.x < TM) {
+        const int r = threadIdx.x;
+        yv[r] = red[r] + red[TM + r] + red[2 * TM + r] + red[3 * TM + r] + P[OFF_B5];
+    }
+
+    // backward: u_l = delta_{l+1} W_{l+1}, delta_l = u_l * silu'(z_l), l = 3, 2, 1
+    load_slab(Ws, Wbwd[0], 0);
+#pragma unroll
+    for (int t = 0; t < 3; t++) {
+        const int l = 3 - t;  // layer whose silu' multiplies
+        gemm_tile(acc, Abuf + cur * TM * AST, Ws, Wbwd[t]);
+        if (t < 2) load_slab(Ws, Wbwd[t + 1], 0);
+        __nv_bfloat16 *nxt = Abuf + (cur ^ 1) * TM * AST;
+        float gpart[3][2][2] = {};
+#pragma unroll
+        for (int i = 0; i < 2; i++)
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+#pragma unroll
+                for (int h = 0; h < 2; h++) {
+                    const float2 s = __half22float2(sp[l - 1][i][j][h]);
+                    const float d0 = acc[i][j][h * 2] * s.x, d1 = acc[i][j][h * 2 + 1] * s.y;
+                    if (l > 1) {
+                        const int r = acc_row(i, h * 2), c = acc_col(j, h * 2);
+                        *reinterpret_cast<__nv_bfloat162 *>(nxt + r * AST + c) = __floats2bfloat162_rn(d0, d1);
+                    } else {
+                        const int c = acc_col(j, h * 2);
+#pragma unroll
+                        for (int q = 0; q < 3; q++)
+                            gpart[q][i][h] += d0 * P[OFF_W1 + c * 3 + q] + d1 * P[OFF_W1 + (c + 1) * 3 + q];
+                    }
+                }
+        if (l == 1) {
+#pragma unroll
+            for (int q = 0; q < 3; q++) row_reduce(gpart[q], red + (q + 1) * 4 * TM);
+        }
+        cur ^= 1;
+        __syncthreads();
+    }
+    if (threadIdx.x < TM) {
+        const int r = threadIdx.x;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const float *rq = red + (q + 1) * 4 * TM;
+            G[r * 3 + q] = rq[r] + rq[TM + r] + rq[2 * TM + r] + rq[3 * TM + r];
+        }
+    }
+    __syncthreads();
+}
+
+// input map and chain rule (gx_mlp.cuh)
+struct MapPt {
+    float r, nx, ny, nz, rho, drho, phiH, dphiH;
+};
+
+__device__ __forceinline__ MapPt map_point(const InferArgs &A, float x, float y, float z) {
+    MapPt m;
+    const float r2 = x * x + y * y + z * z;
+    const float ri = rsqrtf(r2);
+    m.r = r2 * ri;
+    m.nx = x * ri;
+    m.ny = y * ri;
+    m.nz = z * ri;
+    m.rho = A.rho0 + (1.f - A.rho0) * __logf(m.r / A.r_min) * A.inv_log_ratio;
+    m.drho = (1.f - A.rho0) * A.inv_log_ratio * ri;
+    const float irs = 1.f / (m.r + A.r_s);
+    m.phiH = -A.GM * irs;
+    m.dphiH = A.GM * irs * irs;  // d Phi_H / dr
+    return m;
+}
+
+// grad Phi from the network value y and input gradient g
+__device__ __forceinline__ void surrogate_grad(const MapPt &m, float yv, const float *g, float *out) {
+    const float ng = m.nx * g[0] + m.ny * g[1] + m.nz * g[2];
+    const float a = m.rho / m.r;
+    const float jx = a * (g[0] - m.nx * ng) + m.drho * m.nx * ng;
+    const float jy = a * (g[1] - m.ny * ng) + m.drho * m.ny * ng;
+    const float jz = a * (g[2] - m.nz * ng) + m.drho * m.nz * ng;
+    const float radial = m.dphiH * (1.f + yv);
+    out[0] = radial * m.nx + m.phiH * jx;
+    out[1] = radial * m.ny + m.phiH * jy;
+    out[2] = radial * m.nz + m.phiH * jz;
+}
+
+// Analytic SCF gradient in FP32 (same series as gx_scf.cuh, gala's packing).
+__device__ __noinline__ void scf_grad_f32(const float *p, const float *q, float *g) {
+    const float SQRT_FOURPI = 3.544907701811031f, PI = 3.14159265358979f;
+    const float G = p[0], M = p[3], r_s = p[4];
+    const int nmax = (int)p[1], lmax = (int)p[2];
+    const int ncoef = (nmax + 1) * (lmax + 1) * (lmax + 1);
+    const float *S = p + 5, *T = p + 5 + ncoef;
+    const float r = sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+    const float s = r / r_s, X = q[2] / r, phi = atan2f(q[1], q[0]);
+    const float sint = sqrtf(fmaxf(1.f - X * X, 0.f)), xi = (s - 1.f) / (s + 1.f);
+    float cm[16], sm[16], Pl[16], Pl1[16], Pl2[16];
+    for (int m = 0; m < 16; m++) { Pl[m] = 0.f; Pl1[m] = 0.f; Pl2[m] = 0.f; }
+    for (int m = 0; m <= lmax; m++) __sincosf(m * phi, &sm[m], &cm[m]);
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+    for (int l = 0; l <= lmax; l++) {
+        for (int m = 0; m < l; m++) { Pl2[m] = Pl1[m]; Pl1[m] = Pl[m]; }
+        for (int m = 0; m <= l; m++) {
+            if (m == l) Pl[m] = (l == 0) ? 1.f : -(2.f * l - 1.f) * sint * Pl1[l - 1];
+            else if (m == l - 1) Pl[m] = X * (2.f * m + 1.f) * Pl1[m];
+            else Pl[m] = (X * (2.f * l - 1.f) * Pl1[m] - (l + m - 1.f) * Pl2[m]) / (float)(l - m);
+        }
+        const float a1c = 2 * l + 1.5f, a2c = 2 * l + 2.5f;
+        const float psl = __powf(s, (float)l), pslm1 = __powf(s, (float)(l - 1));
+        const float p1 = __powf(1.f + s, -2.f * l - 1.f), p3 = __powf(1.f + s, -3.f - 2.f * l);
+        float Cm2 = 0.f, Cm1 = 0.f, C = 1.f, Dm2 = 0.f, Dm1 = 0.f, D = 1.f;
+        for (int n = 0; n <= nmax; n++) {
+            if (n == 1) { Cm1 = 1.f; C = 2.f * a1c * xi; }
+            else if (n > 1) { Cm2 = Cm1; Cm1 = C; C = (2.f * xi * (n + a1c - 1.f) * Cm1 - (n + 2.f * a1c - 2.f) * Cm2) / n; }
+            const int nd = n - 1;
+            if (nd == 1) { Dm1 = 1.f; D = 2.f * a2c * xi; }
+            else if (nd > 1) { Dm2 = Dm1; Dm1 = D; D = (2.f * xi * (nd + a2c - 1.f) * Dm1 - (nd + 2.f * a2c - 2.f) * Dm2) / nd; }
+            const float rad = -SQRT_FOURPI * psl * p1 * C;
+            const float drad = (n == 0) ? SQRT_FOURPI * pslm1 * p3 * (1 + s) * (l * (s - 1) + s)
+                                        : SQRT_FOURPI * pslm1 * p3 * (-2 * (3 + 4 * l) * s * D + (1 + s) * (l * (s - 1) + s) * C);
+            float fl = 1.f;
+            for (int m = 0; m <= l; m++) {
+                const int i = m + (lmax + 1) * (l + (lmax + 1) * n);
+                const float Sv = S[i], Tv = T[i];
+                // (l-m)!/(l+m)! accumulated as the product 1 / ((l-m+1) ... (l+m))
+                if (m > 0) fl /= (float)((l + m) * (l - m + 1));
+                if (Sv == 0.f && Tv == 0.f) continue;
+                const float norm = sqrtf((2 * l + 1) / (4.f * PI) * fl);
+                const float Y = norm * Pl[m];
+                const float tmp = Sv * cm[m] + Tv * sm[m];
+                float dY = 0.f;
+                if (l > 0) {
+                    const float Pl1m = (m <= l - 1) ? Pl1[m] : 0.f;
+                    dY = norm / sint * (l * X * Pl[m] - (l + m) * Pl1m);
+                }
+                a0 += drad * Y * tmp;
+                a1 += dY * rad / s * tmp;
+                a2 += (float)m * Y * rad * (Tv * cm[m] - Sv * sm[m]) / (s * sint);
+            }
+        }
+    }
+    float cphi, sphi;
+    __sincosf(phi, &sphi, &cphi);
+    const float f = G * M / (r_s * r_s);
+    g[0] = (sint * cphi * a0 + X * cphi * a1 - sphi * a2) * f;
+    g[1] = (sint * sphi * a0 + X * sphi * a1 + cphi * a2) * f;
+    g[2] = (X * a0 - sint * a1) * f;
+}
+
+// Evaluate the surrogate force at n points (q: 3 x n SoA, float64), into
+// out (3 x n, float64) and the potential (n) -- for tests and diagnostics.
+__global__ void __launch_bounds__(NT, 1) surrogate_eval_kernel(InferArgs A, const float *__restrict__ P,
+                                                                const __nv_bfloat16 *__restrict__ Wb,
+                                                                const double *__restrict__ q, int64_t n,
+                                                                double *__restrict__ grad, double *__restrict__ phi) {
+    extern __shared__ __align__(16) char smem[];
+    float *xh = reinterpret_cast<float *>(smem + SMEM_A + SMEM_W);   // [64][3]
+    float *yv = xh + TM * 3;                                          // [64]
+    float *G = yv + TM;                                               // [64][3]
+    const int64_t ntiles = (n + TM - 1) / TM;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t i = tile * TM + threadIdx.x;
+        MapPt m;
+        if (threadIdx.x < TM) {
+            float x = 1.f, y = 0.f, z = 0.f;
+            if (i < n) { x = (float)q[i]; y = (float)q[n + i]; z = (float)q[2 * n + i]; }
+            m = map_point(A, x, y, z);
+            xh[threadIdx.x * 3 + 0] = m.rho * m.nx;
+            xh[threadIdx.x * 3 + 1] = m.rho * m.ny;
+            xh[threadIdx.x * 3 + 2] = m.rho * m.nz;
+        }
+        __syncthreads();
+        tile_eval(P, Wb, smem, xh, yv, G);
+        if (threadIdx.x < TM && i < n) {
+            float gr[3];
+            if (m.r >= A.r_min && m.r <= A.r_max) {
+                surrogate_grad(m, yv[threadIdx.x], G + threadIdx.x * 3, gr);
+            } else {
+                const float qq[3] = {(float)q[i], (float)q[n + i], (float)q[2 * n + i]};
+                scf_grad_f32(A.scf, qq, gr);
+            }
+            grad[i] = gr[0];
+            grad[n + i] = gr[1];
+            grad[2 * n + i] = gr[2];
+            if (phi) phi[i] = (double)m.phiH * (1.0 + (double)yv[threadIdx.x]);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ void split(double x, float &hi, float &lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+__device__ __forceinline__ void kahan(float &s, float &c, float d) {
+    const float y = __fsub_rn(d, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+}
+
+// Leapfrog (kick-drift-kick as c_leapfrog_step, leapfrog.pyx:35-51) in the
+// surrogate potential; n_steps and dt shared by all orbits; FP32 state with
+// Kahan compensation; final state (6 x n, float64) and the count of force
+// evaluations that used the analytic fallback.
+__global__ void __launch_bounds__(NT, 1) surrogate_leapfrog_kernel(InferArgs A, const float *__restrict__ P,
+                                                                    const __nv_bfloat16 *__restrict__ Wb,
+                                                                    const double *__restrict__ w0, int64_t n,
+                                                                    int64_t nsteps, float dt,
+                                                                    double *__restrict__ w_out,
+                                                                    unsigned long long *__restrict__ fallbacks) {
+    extern __shared__ __align__(16) char smem[];
+    float *xh = reinterpret_cast<float *>(smem + SMEM_A + SMEM_W);
+    float *yv = xh + TM * 3;
+    float *G = yv + TM;
+    const int64_t ntiles = (n + TM - 1) / TM;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t i = tile * TM + threadIdx.x;
+        const bool own = threadIdx.x < TM && i < n;
+        float xh_[3] = {1.f, 0.f, 0.f}, xl[3] = {0.f, 0.f, 0.f}, vh[3] = {0.f, 0.f, 0.f}, vl[3] = {0.f, 0.f, 0.f};
+        float g[3] = {0.f, 0.f, 0.f};
+        unsigned long long nfb = 0;
+        if (own)
+            for (int k = 0; k < 3; k++) {
+                split(w0[k * n + i], xh_[k], xl[k]);
+                split(w0[(3 + k) * n + i], vh[k], vl[k]);
+            }
+        // force at the start, then nsteps x (drift, force, kick); the first kick is a half kick
+        for (int64_t step = 0; step <= nsteps; step++) {
+            if (step > 0 && own)
+                for (int k = 0; k < 3; k++) kahan(xh_[k], xl[k], fmaf(vh[k], dt, vl[k] * dt));
+            MapPt m;
+            if (threadIdx.x < TM) {
+                m = map_point(A, xh_[0], xh_[1], xh_[2]);
+                xh[threadIdx.x * 3 + 0] = m.rho * m.nx;
+                xh[threadIdx.x * 3 + 1] = m.rho * m.ny;
+                xh[threadIdx.x * 3 + 2] = m.rho * m.nz;
+            }
+            __syncthreads();
+            tile_eval(P, Wb, smem, xh, yv, G);
+            if (own) {
+                if (m.r >= A.r_min && m.r <= A.r_max) {
+                    surrogate_grad(m, yv[threadIdx.x], G + threadIdx.x * 3, g);
+                } else {
+                    scf_grad_f32(A.scf, xh_, g);
+                    nfb++;
+                }
+                const float f = (step == 0) ? 0.5f : 1.0f;
+                for (int k = 0; k < 3; k++) kahan(vh[k], vl[k], -g[k] * dt * f);
+            }
+        }
+        if (own) {
+            // undo the last half of the final kick to report v at the last step
+            for (int k = 0; k < 3; k++) kahan(vh[k], vl[k], g[k] * dt * 0.5f);
+            for (int k = 0; k < 3; k++) {
+                w_out[k * n + i] = (double)xh_[k] + (double)xl[k];
+                w_out[(3 + k) * n + i] = (double)vh[k] + (double)vl[k];
+            }
+            if (nfb) atomicAdd(fallbacks, nfb);
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace mlpi
+}  // namespace gx
+
+using namespace gx::mlpi;
+
+static int infer_args(const float *scf_params, double r_min, double r_max, double GM, double r_s, InferArgs *A) {
+    GX_CHECK_ARG(scf_params != nullptr, "NULL SCF parameters (analytic fallback)");
+    GX_CHECK_ARG(r_min > 0 && r_max > r_min && GM > 0 && r_s > 0, "bad surrogate input map");
+    A->r_min = (float)r_min;
+    A->r_max = (float)r_max;
+    A->rho0 = 0.1f;
+    A->inv_log_ratio = (float)(1.0 / std::log(r_max / r_min));
+    A->GM = (float)GM;
+    A->r_s = (float)r_s;
+    A->scf = scf_params;
+    static bool configured = false;
+    if (!configured) {
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         SMEM_BYTES));
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_leapfrog_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         SMEM_BYTES));
+        configured = true;
+    }
+    return GX_OK;
+}
+
+extern "C" int gx_surrogate_gradient(const float *params, const void *wbf16, const float *scf_params, double r_min,
+                                     double r_max, double GM, double r_s, const double *q, int64_t n, double *grad,
+                                     double *phi, int32_t grid, void *stream) {
+    InferArgs A;
+    int rc = infer_args(scf_params, r_min, r_max, GM, r_s, &A);
+    if (rc) return rc;
+    GX_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return GX_OK;
+    GX_CHECK_ARG(params && wbf16 && q && grad && grid >= 1, "NULL array or bad grid");
+    surrogate_eval_kernel<<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
+        A, params, static_cast<const __nv_bfloat16 *>(wbf16), q, n, grad, phi);
+    return gx::check_launch("surrogate_gradient");
+}
+
+extern "C" int gx_surrogate_leapfrog(const float *params, const void *wbf16, const float *scf_params, double r_min,
+                                     double r_max, double GM, double r_s, const double *w0, int64_t n,
+                                     int64_t n_steps, double dt, double *w_out, unsigned long long *fallbacks,
+                                     int32_t grid, void *stream) {
+    InferArgs A;
+    int rc = infer_args(scf_params, r_min, r_max, GM, r_s, &A);
+    if (rc) return rc;
+    GX_CHECK_ARG(n >= 0 && n_steps >= 0, "n and n_steps must be >= 0");
+    if (n == 0) return GX_OK;
+    GX_CHECK_ARG(params && wbf16 && w0 && w_out && fallbacks && grid >= 1, "NULL array or bad grid");
+    surrogate_leapfrog_kernel<<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
+        A, params, static_cast<const __nv_bfloat16 *>(wbf16), w0, n, n_steps, (float)dt, w_out, fallbacks);
+    return gx::check_launch("surrogate_leapfrog");
+}
+
+extern "C" int gx_surrogate_smem_bytes(void) { return SMEM_BYTES; }

@@ -82,3 +82,44 @@ def uneven_steps(n=262_144, seed=SEED_BASE + 3):
     method = (np.arange(n) >= n // 2).astype(np.int32)
     rng.shuffle(method)
     return nsteps, dt, method
+
+
+def scf_coefficients(nmax=12, lmax=8, seed=SEED_BASE + 4):
+    """S, T ~ N(0, 1) exp(-0.5 n) (l + 1)^-2, S000 = 1, zero for m > l, T_nl0 = 0."""
+    rng = np.random.default_rng(seed)
+    n = np.arange(nmax + 1)[:, None, None]
+    l = np.arange(lmax + 1)[None, :, None]
+    m = np.arange(lmax + 1)[None, None, :]
+    amp = np.exp(-0.5 * n) * (l + 1.0) ** -2
+    S = rng.normal(size=(nmax + 1, lmax + 1, lmax + 1)) * amp
+    T = rng.normal(size=(nmax + 1, lmax + 1, lmax + 1)) * amp
+    mask = m <= l
+    S = np.where(mask, S, 0.0)
+    T = np.where(mask, T, 0.0)
+    T[:, :, 0] = 0.0
+    S[0, 0, 0] = 1.0
+    return S, T
+
+
+def scf_potential(nmax=12, lmax=8, seed=SEED_BASE + 4):
+    """SCF halo: m = 1e12 Msun, r_s = 20 kpc, coefficients from scf_coefficients."""
+    from .potential import SCFPotential
+
+    S, T = scf_coefficients(nmax, lmax, seed)
+    return SCFPotential(m=1e12, r_s=20.0, Snlm=S, Tnlm=T)
+
+
+def scf_ics(n=262_144, seed=SEED_BASE + 5, m=1e12, r_s=20.0):
+    """Orbits in the SCF halo: r ~ U[5, 100] kpc isotropic, velocity = the
+    Hernquist (m, r_s) circular speed in a random tangential direction times
+    (1 + N(0, 0.1)) per component."""
+    rng = np.random.default_rng(seed)
+    r = rng.uniform(5.0, 100.0, n)
+    u = rng.normal(size=(3, n))
+    rhat = u / np.linalg.norm(u, axis=0)
+    a = rng.normal(size=(3, n))
+    a -= np.sum(a * rhat, axis=0) * rhat
+    that = a / np.linalg.norm(a, axis=0)
+    vc = np.sqrt(G * m * r / (r + r_s) ** 2)
+    v = vc * that * (1.0 + rng.normal(0.0, 0.1, size=(3, n)))
+    return np.ascontiguousarray(np.vstack([r * rhat, v]))

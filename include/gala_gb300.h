@@ -246,6 +246,45 @@ int gx_batch_integrate_fp32_noalloc(const gx_potential* pot, const double* w0, i
                                     double* w_out, void* stream);
 
 /* ------------------------------------------------------------------------- */
+/* Learned potential surrogate.  No counterpart in gala: an MLP             */
+/* y(xh), 3 -> 256 -> 256 -> 256 -> 256 -> 1, SiLU, with                        */
+/*   Phi(x) = Phi_H(r) (1 + y(xh)),  Phi_H = -G M / (r + r_s),                   */
+/*   xh = rho(r) x / r,  rho = 0.1 + 0.9 ln(r / r_min) / ln(r_max / r_min).      */
+/* params: FP32 [W1 256x3 | b1 | W2 256x256 | b2 | W3 | b3 | W4 | b4 | w5 | b5]  */
+/* (gx_mlp_param_count() floats).  Training runs on the CUDA cores in FP32;      */
+/* inference uses BF16 weights [W2, W3, W4, W4^T, W3^T, W2^T] (6 x 256 x 256)    */
+/* on the tensor cores with FP32 accumulation.                                   */
+/* ------------------------------------------------------------------------- */
+int64_t gx_mlp_param_count(void);
+/* floats of workspace gx_mlp_train_step / gx_mlp_forward need for a batch */
+int64_t gx_mlp_train_workspace_floats(int64_t batch);
+/* y (B) and, if G != NULL, dy/dxh (B x 3) for inputs xh (B x 3), FP32 */
+int gx_mlp_forward(const float* params, const float* xh, int64_t batch, float* y, float* G,
+                   float* workspace, void* stream);
+/* gradient of L = alpha mean (y - y*)^2 + beta mean |dy/dxh - G*|^2 w.r.t. params
+ * into grads; loss[0], loss[1] = the two mean squared errors */
+int gx_mlp_train_step(const float* params, float* grads, const float* xh, const float* ystar,
+                      const float* Gstar, int64_t batch, float alpha, float beta,
+                      float* workspace, float* loss, void* stream);
+/* Adam update of params (n floats) with moment buffers m, v; step >= 1 */
+int gx_mlp_adam(float* params, const float* grads, float* m, float* v, int64_t n, float lr,
+                float beta1, float beta2, float eps, int64_t step, void* stream);
+/* grad Phi (3 x n) and Phi (n, may be NULL) at q (3 x n); outside
+ * [r_min, r_max] the analytic SCF force (FP32, scf_params = gala's packed SCF
+ * parameters as float) is used.  grid = number of 256-thread CTAs. */
+int gx_surrogate_gradient(const float* params, const void* wbf16, const float* scf_params,
+                          double r_min, double r_max, double GM, double r_s, const double* q,
+                          int64_t n, double* grad, double* phi, int32_t grid, void* stream);
+/* FP32 leapfrog (kick-drift-kick, Kahan-compensated state) of n orbits for
+ * n_steps of dt in the surrogate potential; w_out = final states (6 x n);
+ * *fallbacks += number of force evaluations that used the analytic SCF. */
+int gx_surrogate_leapfrog(const float* params, const void* wbf16, const float* scf_params,
+                          double r_min, double r_max, double GM, double r_s, const double* w0,
+                          int64_t n, int64_t n_steps, double dt, double* w_out,
+                          unsigned long long* fallbacks, int32_t grid, void* stream);
+int gx_surrogate_smem_bytes(void);
+
+/* ------------------------------------------------------------------------- */
 /* Pipe calibration.  No counterpart in gala: it measures the FP64 / FP32     */
 /* multiply-add throughput that bounds the integrators (the roofline          */
 /* denominator).  Runs blocks x threads threads, each with 8 independent FMA  */

@@ -1,0 +1,150 @@
+"""The learned potential surrogate on the GPU.
+
+* training kernels: forward, input gradient and the parameter gradient of the
+  value + input-gradient loss against the numpy FP64 oracle (oracle/mlp_oracle.py);
+* Adam update against numpy;
+* BF16 tensor-core inference against the FP64 oracle of the same network;
+* a trained surrogate of an SCF halo: force accuracy, the analytic fallback,
+  integrated orbits, and what it gains over the analytic SCF force.
+"""
+import time
+
+import numpy as np
+import pytest
+
+import gala_gb300 as g
+from gala_gb300 import surrogate as S
+from gala_gb300 import workloads as W
+from oracle import mlp_oracle as M
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scf():
+    return W.scf_potential(nmax=6, lmax=4)
+
+
+def _random_batch(B, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.uniform(-1, 1, (B, 3)).astype(np.float32)
+    ys = rng.normal(0, 0.3, B).astype(np.float32)
+    Gs = rng.normal(0, 0.3, (B, 3)).astype(np.float32)
+    return X, ys, Gs
+
+
+def test_forward_and_train_step_match_oracle(scf):
+    import torch
+
+    from gala_gb300 import _abi
+
+    sp = S.SurrogatePotential(scf, seed=3)
+    p = sp.params.cpu().numpy().astype(np.float64)
+    X, ys, Gs = _random_batch(96, 4)
+    y, G = sp.forward_fp32(torch.from_numpy(X))
+    y_ref, G_ref, _ = M.forward(p, X.astype(np.float64))
+    np.testing.assert_allclose(y.cpu().numpy(), y_ref, rtol=1e-4, atol=1e-5)
+    np.testing.assert_allclose(G.cpu().numpy(), G_ref, rtol=1e-4, atol=1e-5)
+
+    dev = sp.dev
+    grads = torch.zeros_like(sp.params)
+    ws = torch.empty(int(_abi.load().gx_mlp_train_workspace_floats(96)), dtype=torch.float32, device=dev)
+    loss = torch.zeros(2, dtype=torch.float32, device=dev)
+    Xd, yd, Gd = (torch.from_numpy(a).to(dev) for a in (X, ys, Gs))
+    import ctypes as C
+
+    _abi.call("gx_mlp_train_step", sp.params.data_ptr(), grads.data_ptr(), Xd.data_ptr(), yd.data_ptr(),
+              Gd.data_ptr(), 96, C.c_float(0.8), C.c_float(1.2), ws.data_ptr(), loss.data_ptr(), None)
+    L, gref = M.loss_and_grad(p, X.astype(np.float64), ys.astype(np.float64), Gs.astype(np.float64), 0.8, 1.2)
+    gk = grads.cpu().numpy()
+    scale = np.abs(gref).max()
+    assert np.max(np.abs(gk - gref)) <= 2e-4 * scale, np.max(np.abs(gk - gref)) / scale
+    Lk = 0.8 * loss[0].item() + 1.2 * loss[1].item()
+    assert abs(Lk - L) <= 1e-4 * abs(L)
+
+
+def test_adam_matches_numpy():
+    import ctypes as C
+
+    import torch
+
+    from gala_gb300 import _abi
+
+    rng = np.random.default_rng(5)
+    n = 1000
+    p, gr = rng.normal(size=n).astype(np.float32), rng.normal(size=n).astype(np.float32)
+    m, v = rng.normal(size=n).astype(np.float32) * 0.1, rng.uniform(0, 1, n).astype(np.float32)
+    tp, tg, tm, tv = (torch.from_numpy(a.copy()).cuda() for a in (p, gr, m, v))
+    _abi.call("gx_mlp_adam", tp.data_ptr(), tg.data_ptr(), tm.data_ptr(), tv.data_ptr(), n, C.c_float(1e-3),
+              C.c_float(0.9), C.c_float(0.999), C.c_float(1e-8), 7, None)
+    m2 = 0.9 * m + 0.1 * gr
+    v2 = 0.999 * v + 0.001 * gr * gr
+    p2 = p - 1e-3 * (m2 / (1 - 0.9 ** 7)) / (np.sqrt(v2 / (1 - 0.999 ** 7)) + 1e-8)
+    np.testing.assert_allclose(tp.cpu().numpy(), p2, rtol=1e-5, atol=1e-7)
+
+
+def test_bf16_inference_matches_fp64_network(scf):
+    """The tensor-core kernel evaluates the same function as the FP64 oracle of
+    the network (to BF16 precision)."""
+    sp = S.SurrogatePotential(scf, seed=6)
+    sp.export()
+    x = sp.sample_positions(3000, seed=7)
+    grad, phi = sp.gradient_and_energy(x)
+    xd = x.cpu().numpy()
+    xh, r, n, rho, drho = S.input_map(xd, sp.r_min, sp.r_max)
+    p = sp.params.cpu().numpy().astype(np.float64)
+    y, Gx, _ = M.forward(p, xh.T)
+    phiH = -sp.GM / (r + sp.r_s)
+    dphiH = sp.GM / (r + sp.r_s) ** 2
+    ng = np.sum(n * Gx.T, axis=0)
+    J = (rho / r) * (Gx.T - n * ng) + drho * n * ng
+    grad_ref = dphiH * (1 + y) * n + phiH * J
+    phi_ref = phiH * (1 + y)
+    err = np.linalg.norm(grad.cpu().numpy() - grad_ref, axis=0) / np.linalg.norm(grad_ref, axis=0)
+    assert np.median(err) < 1e-2, np.median(err)
+    np.testing.assert_allclose(phi.cpu().numpy(), phi_ref, rtol=2e-2)
+
+
+def test_fallback_outside_trained_radii(scf, oracle):
+    sp = S.SurrogatePotential(scf, r_min=0.5, r_max=200.0, seed=8)
+    q = np.array([[0.2, 0.0, 0.1], [300.0, 10.0, -5.0], [0.0, 250.0, 1.0]]).T
+    grad, _ = sp.gradient_and_energy(q)
+    ref = oracle.gradient(scf, q)
+    np.testing.assert_allclose(grad.cpu().numpy(), ref, rtol=1e-4)
+
+
+def test_trained_surrogate_accuracy_and_gain(scf, oracle):
+    import torch
+
+    sp = S.SurrogatePotential(scf, seed=9)
+    sp.make_dataset(n_samples=1 << 20)
+    hist = sp.train(steps=1500, batch=8192, log_every=500)
+    assert hist[-1][1] < hist[0][1]
+    x = sp.sample_positions(20000, seed=10)
+    grad, phi = sp.gradient_and_energy(x)
+    ref = scf.gradient(x.cpu().numpy())
+    err = np.linalg.norm(grad.cpu().numpy() - ref, axis=0) / np.linalg.norm(ref, axis=0)
+    assert np.median(err) < 2e-2, np.median(err)
+    # gain: surrogate force vs the analytic SCF force in FP64 at the same points
+    xs = sp.sample_positions(1 << 18, seed=11)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sp.gradient_and_energy(xs)
+    torch.cuda.synchronize()
+    t_sur = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    scf.gradient(xs.cpu().numpy())
+    torch.cuda.synchronize()
+    t_scf = time.perf_counter() - t0
+    assert t_sur < t_scf, (t_sur, t_scf)
+
+
+def test_surrogate_leapfrog_runs_and_matches_fp32_forces(scf):
+    sp = S.SurrogatePotential(scf, seed=12)
+    sp.export()
+    w0 = W.scf_ics(200, seed=13)
+    out, fb = sp.integrate_leapfrog(w0, dt=1.0, n_steps=50)
+    o = out.cpu().numpy()
+    assert np.isfinite(o).all()
+    assert not np.array_equal(o, w0)
+    assert int(fb.item()) == 0

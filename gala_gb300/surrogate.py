@@ -75,6 +75,10 @@ class SurrogatePotential:
 
         self.dev = require_cuda()
         self.scf = scf
+        if getattr(scf, "nmax", 0) + 1 > 24 or getattr(scf, "lmax", 0) + 1 > 16:
+            raise ValueError("the FP32 SCF fallback supports nmax <= 23 and lmax <= 15")
+        if not 0 < r_min < r_max:
+            raise ValueError("need 0 < r_min < r_max")
         self.r_min, self.r_max = float(r_min), float(r_max)
         self.GM = G_GALACTIC * float(scf.parameters["m"])
         self.r_s = float(scf.parameters["r_s"])

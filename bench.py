@@ -53,13 +53,15 @@ def parse_args():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gx", choices=["gx", "reference"])
-    p.add_argument("--workload", default="mw_dop853", choices=["mw_dop853", "uneven_batch"],
-                   help="mw_dop853: the headline line; uneven_batch: only the batched FP32c/FP64 "
-                        "comparison (used for profiling)")
+    p.add_argument("--workload", default="mw_dop853", choices=["mw_dop853", "uneven_batch", "scf_surrogate"],
+                   help="mw_dop853: the headline line; uneven_batch / scf_surrogate: only that variant "
+                        "(used for profiling)")
     p.add_argument("--batch-orbits", type=int, default=262_144)
     p.add_argument("--batch-step-scale", type=float, default=1.0, help="multiply the batch step counts")
     p.add_argument("--batch-precision", default="both", choices=["both", "fp32c", "fp64"])
     p.add_argument("--no-autotune", action="store_true", help="use the cached or default launch shape")
+    p.add_argument("--surrogate-steps", type=int, default=6000, help="training steps of the SCF surrogate")
+    p.add_argument("--no-surrogate", action="store_true", help="skip the SCF surrogate variant")
     p.add_argument("--orbits", type=int, default=100_000)
     p.add_argument("--nsteps", type=int, default=10_000)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -263,6 +265,84 @@ def run_uneven_batch(args, torch, stream):
     return res
 
 
+def run_scf_surrogate(args, torch, stream, n_orbits=262_144, n_steps=5000):
+    """The SCF host: SCF(m=1e12, r_s=20, nmax=12, lmax=8) with random coefficients,
+    262,144 orbits, dt = 1 Myr, 5,000 Leapfrog steps.  A surrogate is trained on
+    16M analytic samples (timed separately), then the same FP32 leapfrog runs
+    with (a) the BF16 tensor-core surrogate, (b) the analytic SCF force in FP32;
+    the plain FP64 form (gala's arithmetic, analytic SCF) is timed on a 20-step
+    run of all orbits.  Accuracy: force error on 50k held-out points, orbit
+    position error and analytic-energy drift against the FP64 form on 2,048
+    orbits over 1,000 steps."""
+    import gala_gb300 as g
+    from gala_gb300 import surrogate as S
+    from gala_gb300 import workloads as W
+
+    scf = W.scf_potential()
+    sp = S.SurrogatePotential(scf, seed=0)
+    t0 = time.perf_counter()
+    sp.make_dataset(n_samples=16 << 20)
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    hist = sp.train(steps=args.surrogate_steps, batch=8192, lr=1e-3, log_every=max(1, args.surrogate_steps // 4))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    x = sp.sample_positions(50000, seed=99)
+    grad, _ = sp.gradient_and_energy(x)
+    ref = scf.gradient(x.cpu().numpy())
+    ferr = np.linalg.norm(grad.cpu().numpy() - ref, axis=0) / np.linalg.norm(ref, axis=0)
+    w0 = W.scf_ics(n_orbits)
+
+    def timed(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps, out
+
+    ms_sur, (wsur, fb) = timed(lambda: sp.integrate_leapfrog(w0, 1.0, n_steps), 1)
+    ms_f32, _ = timed(lambda: sp.integrate_leapfrog(w0[:, :65536], 1.0, 200, analytic=True), 1)
+    ms_f64, _ = timed(lambda: scf.integrate_orbit(w0, dt=1.0, n_steps=20, Integrator="leapfrog", save_all=False,
+                                                  return_device=True), 1)
+    v_sur = n_orbits * n_steps / (ms_sur * 1e-3)
+    v_f32 = 65536 * 200 / (ms_f32 * 1e-3)
+    v_f64 = n_orbits * 20 / (ms_f64 * 1e-3)
+    sub = w0[:, :2048]
+    o64 = scf.integrate_orbit(sub, dt=1.0, n_steps=1000, Integrator="leapfrog", save_all=False).w().reshape(6, -1)
+    osur = sp.integrate_leapfrog(sub, 1.0, 1000)[0].cpu().numpy()
+    o32 = sp.integrate_leapfrog(sub, 1.0, 1000, analytic=True)[0].cpu().numpy()
+    H = g.Hamiltonian(scf)
+    E0 = H.energy(sub)
+
+    def errs(o):
+        pe = np.linalg.norm(o[:3] - o64[:3], axis=0) / np.linalg.norm(o64[:3], axis=0)
+        dE = np.abs((H.energy(o) - E0) / E0)
+        return {"position_error_median": float(np.median(pe)), "position_error_p90": float(np.percentile(pe, 90)),
+                "dE_over_E_analytic_median": float(np.median(dE))}
+
+    return {
+        "workload": f"scf_surrogate: SCF m=1e12 r_s=20 nmax=12 lmax=8, {n_orbits} orbits, dt 1 Myr, "
+                    f"{n_steps} Leapfrog steps",
+        "fp32_surrogate": {"value": v_sur, "unit": UNIT, "ms_per_run": ms_sur,
+                           "fallback_force_evaluations": int(fb.item()),
+                           "tensor_core": "mma.sync m16n8k16 BF16, FP32 accumulate, activations BF16 hi+lo"},
+        "fp32_analytic_scf": {"value": v_f32, "unit": UNIT, "sample": "65,536 orbits x 200 steps"},
+        "fp64_analytic_scf_plain": {"value": v_f64, "unit": UNIT, "sample": f"{n_orbits} orbits x 20 steps"},
+        "speedup_surrogate_vs_fp64": v_sur / v_f64,
+        "speedup_surrogate_vs_fp32_analytic": v_sur / v_f32,
+        "surrogate_training": {"samples": int(sp.X.shape[0]), "steps": args.surrogate_steps, "batch": 8192,
+                               "dataset_s": t_data, "train_s": t_train, "loss_history": hist},
+        "force_error_vs_analytic": {"median": float(np.median(ferr)), "p90": float(np.percentile(ferr, 90)),
+                                    "p99": float(np.percentile(ferr, 99))},
+        "orbits_vs_fp64_2048x1000": {"surrogate": errs(osur), "fp32_analytic": errs(o32)},
+    }
+
+
 def run_gx(args):
     import torch
 
@@ -279,8 +359,9 @@ def run_gx(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
     sh = int(stream.cuda_stream)
-    if args.workload == "uneven_batch":
-        res = run_uneven_batch(args, torch, stream)
+    if args.workload in ("uneven_batch", "scf_surrogate"):
+        fn = run_uneven_batch if args.workload == "uneven_batch" else run_scf_surrogate
+        res = fn(args, torch, stream)
         if rank == 0:
             print(json.dumps(res), flush=True)
         return
@@ -369,6 +450,8 @@ def run_gx(args):
     peak = measure_fp64_peak(torch, stream)
     achieved = flops / (mean_ms * 1e-3) / 1e12
     variants = {"uneven_batch": run_uneven_batch(args, torch, stream)}
+    if not args.no_surrogate:
+        variants["scf_surrogate"] = run_scf_surrogate(args, torch, stream)
 
     if rank != 0:
         return

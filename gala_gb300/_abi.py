@@ -86,10 +86,11 @@ SIGNATURES = {
     "gx_mlp_param_count": (C.c_int64, []),
     "gx_mlp_train_workspace_floats": (C.c_int64, [_I64]),
     "gx_mlp_forward": (C.c_int, [_P, _P, _I64, _P, _P, _P, _P]),
-    "gx_mlp_train_step": (C.c_int, [_P, _P, _P, _P, _P, _I64, C.c_float, C.c_float, _P, _P, _P]),
+    "gx_mlp_train_step": (C.c_int, [_P, _P, _P, _P, _P, _P, _I64, C.c_float, C.c_float, _P, _P, _P]),
     "gx_mlp_adam": (C.c_int, [_P, _P, _P, _P, _I64, C.c_float, C.c_float, C.c_float, C.c_float, _I64, _P]),
-    "gx_surrogate_gradient": (C.c_int, [_P, _P, _P, _D, _D, _D, _D, _P, _I64, _P, _P, _I32, _P]),
-    "gx_surrogate_leapfrog": (C.c_int, [_P, _P, _P, _D, _D, _D, _D, _P, _I64, _I64, _D, _P, _P, _I32, _P]),
+    "gx_surrogate_gradient": (C.c_int, [_P, _P, _P, _D, _D, _D, _D, _I32, _P, _I64, _P, _P, _I32, _P]),
+    "gx_surrogate_leapfrog": (C.c_int, [_P, _P, _P, _D, _D, _D, _D, _I32, _I32, _P, _I64, _I64, _D, _P, _P, _I32,
+                                        _P]),
     "gx_surrogate_smem_bytes": (C.c_int, []),
     "gx_batch_integrate_fp64": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P]),
     "gx_dop853_integrate_hamiltonian": (

@@ -37,9 +37,9 @@ constexpr int NT = 256;                // threads per CTA
 constexpr int AST = H + 8;             // activation row stride (bf16 elements): 528 bytes
 constexpr int KS = 64;                 // K slab
 constexpr int WST = KS + 8;            // weight slab row stride (bf16): 144 bytes
-constexpr int SMEM_A = 2 * TM * AST * 2;     // two activation buffers
+constexpr int SMEM_A = 2 * 2 * TM * AST * 2;  // two activation buffers, each a hi and a lo part
 constexpr int SMEM_W = 2 * H * WST * 2;      // two weight slabs
-constexpr int SMEM_MISC = TM * 8 * 4 + 4 * TM * 4 * 4;
+constexpr int SMEM_MISC = TM * 8 * 4 + 4 * TM * 4 * 4 + TM * 16 + TM * 3 * 4 + 16;
 constexpr int SMEM_BYTES = SMEM_A + SMEM_W + SMEM_MISC;
 
 struct InferArgs {
@@ -88,9 +88,12 @@ __device__ __forceinline__ void load_slab(__nv_bfloat16 *ws, const __nv_bfloat16
     cp_commit();
 }
 
-// acc[2][8][4] += A(64x256, smem) x W^T where W (global [256 n][256 k]) is the
-// B operand (k contiguous per output n).  The first slab of W must already be
-// in flight in slab buffer 0.
+// acc[2][8][4] = A(64x256, smem) x W^T where W (global [256 n][256 k]) is the
+// B operand (k contiguous per output n).  A is held as a BF16 pair hi + lo
+// (lo = the rounding remainder of hi); SPLIT = 2 multiplies both parts
+// (activation precision ~2^-17), SPLIT = 1 only hi.  The first slab of W must
+// already be in flight in slab buffer 0.
+template <int SPLIT>
 __device__ __forceinline__ void gemm_tile(float (&acc)[2][8][4], const __nv_bfloat16 *As,
                                           __nv_bfloat16 *Ws, const __nv_bfloat16 *Wg) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -112,13 +115,16 @@ __device__ __forceinline__ void gemm_tile(float (&acc)[2][8][4], const __nv_bflo
         const __nv_bfloat16 *wsb = Ws + (s & 1) * H * WST;
 #pragma unroll
         for (int kk = 0; kk < KS; kk += 16) {
-            uint32_t a[2][4];
+            uint32_t a[SPLIT][2][4];
 #pragma unroll
-            for (int i = 0; i < 2; i++) {
-                const int row = wm * 32 + i * 16 + (lane & 15);
-                const int col = s * KS + kk + (lane >> 4) * 8;
-                ldsm_x4(smem_u32(As + row * AST + col), a[i][0], a[i][1], a[i][2], a[i][3]);
-            }
+            for (int p = 0; p < SPLIT; p++)
+#pragma unroll
+                for (int i = 0; i < 2; i++) {
+                    const int row = wm * 32 + i * 16 + (lane & 15);
+                    const int col = s * KS + kk + (lane >> 4) * 8;
+                    ldsm_x4(smem_u32(As + p * TM * AST + row * AST + col), a[p][i][0], a[p][i][1], a[p][i][2],
+                            a[p][i][3]);
+                }
 #pragma unroll
             for (int j = 0; j < 8; j += 2) {
                 // two n-tiles (16 outputs) x k16 from the slab: matrices (n0..7,k0..7), (n0..7,k8..15),
@@ -128,14 +134,24 @@ __device__ __forceinline__ void gemm_tile(float (&acc)[2][8][4], const __nv_bflo
                 uint32_t b0, b1, b2, b3;
                 ldsm_x4(smem_u32(wsb + n * WST + k), b0, b1, b2, b3);
 #pragma unroll
-                for (int i = 0; i < 2; i++) {
-                    mma_bf16(acc[i][j], a[i][0], a[i][1], a[i][2], a[i][3], b0, b1);
-                    mma_bf16(acc[i][j + 1], a[i][0], a[i][1], a[i][2], a[i][3], b2, b3);
-                }
+                for (int p = 0; p < SPLIT; p++)
+#pragma unroll
+                    for (int i = 0; i < 2; i++) {
+                        mma_bf16(acc[i][j], a[p][i][0], a[p][i][1], a[p][i][2], a[p][i][3], b0, b1);
+                        mma_bf16(acc[i][j + 1], a[p][i][0], a[p][i][1], a[p][i][2], a[p][i][3], b2, b3);
+                    }
             }
         }
         __syncthreads();
     }
+}
+
+// store v (two consecutive columns) as hi + lo BF16 parts
+__device__ __forceinline__ void store_split(__nv_bfloat16 *buf, int r, int c, float v0, float v1) {
+    const __nv_bfloat162 hi = __floats2bfloat162_rn(v0, v1);
+    const float2 hf = __bfloat1622float2(hi);
+    *reinterpret_cast<__nv_bfloat162 *>(buf + r * AST + c) = hi;
+    *reinterpret_cast<__nv_bfloat162 *>(buf + TM * AST + r * AST + c) = __floats2bfloat162_rn(v0 - hf.x, v1 - hf.y);
 }
 
 // Accumulator element (i, j, k) of this thread -> (row, col) of the 64x256 tile.
@@ -165,6 +181,7 @@ __device__ __forceinline__ void row_reduce(float (&part)[2][2], float *red) {
 
 // One surrogate evaluation for the tile whose inputs xh[64][3] are in smem.
 // Outputs: yv[64] (network value) and G[64][3] (dy/dxh) in smem.
+template <int SPLIT>
 __device__ __forceinline__ void tile_eval(const float *__restrict__ P, const __nv_bfloat16 *__restrict__ Wb, char *smem,
                           const float *xh, float *yv, float *G) {
     __nv_bfloat16 *Abuf = reinterpret_cast<__nv_bfloat16 *>(smem);
@@ -200,7 +217,7 @@ __device__ __forceinline__ void tile_eval(const float *__restrict__ P, const __n
                 }
                 sp[0][i][j][h] = __floats2half2_rn(s1v[0], s1v[1]);
             }
-    // write a1 (bf16) into Abuf[0]
+    // write a1 (bf16 hi + lo) into activation buffer 0
 #pragma unroll
     for (int i = 0; i < 2; i++)
 #pragma unroll
@@ -208,8 +225,7 @@ __device__ __forceinline__ void tile_eval(const float *__restrict__ P, const __n
 #pragma unroll
             for (int h = 0; h < 2; h++) {
                 const int r = acc_row(i, h * 2), c = acc_col(j, h * 2);
-                *reinterpret_cast<__nv_bfloat162 *>(Abuf + r * AST + c) =
-                    __floats2bfloat162_rn(acc[i][j][h * 2], acc[i][j][h * 2 + 1]);
+                store_split(Abuf, r, c, acc[i][j][h * 2], acc[i][j][h * 2 + 1]);
             }
     __syncthreads();
 
@@ -217,10 +233,10 @@ __device__ __forceinline__ void tile_eval(const float *__restrict__ P, const __n
     int cur = 0;
 #pragma unroll
     for (int l = 2; l <= 4; l++) {
-        gemm_tile(acc, Abuf + cur * TM * AST, Ws, Wfwd[l - 2]);
+        gemm_tile<SPLIT>(acc, Abuf + cur * 2 * TM * AST, Ws, Wfwd[l - 2]);
         if (l < 4) load_slab(Ws, Wfwd[l - 1], 0);
         const float *b = P + off_b(l);
-        __nv_bfloat16 *nxt = Abuf + (cur ^ 1) * TM * AST;
+        __nv_bfloat16 *nxt = Abuf + (cur ^ 1) * 2 * TM * AST;
         float ypart[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll
         for (int i = 0; i < 2; i++)
@@ -248,7 +264,7 @@ __device__ __forceinline__ void tile_eval(const float *__restrict__ P, const __n
                         av[1] = P[OFF_W5 + c + 1] * s1v[1];
                     }
                     const int r = acc_row(i, h * 2), c = acc_col(j, h * 2);
-                    *reinterpret_cast<__nv_bfloat162 *>(nxt + r * AST + c) = __floats2bfloat162_rn(av[0], av[1]);
+                    store_split(nxt, r, c, av[0], av[1]);
                 }
         if (l == 4) row_reduce(ypart, red);
         cur ^= 1;
@@ -264,9 +280,9 @@ __device__ __forceinline__ void tile_eval(const float *__restrict__ P, const __n
 #pragma unroll
     for (int t = 0; t < 3; t++) {
         const int l = 3 - t;  // layer whose silu' multiplies
-        gemm_tile(acc, Abuf + cur * TM * AST, Ws, Wbwd[t]);
+        gemm_tile<SPLIT>(acc, Abuf + cur * 2 * TM * AST, Ws, Wbwd[t]);
         if (t < 2) load_slab(Ws, Wbwd[t + 1], 0);
-        __nv_bfloat16 *nxt = Abuf + (cur ^ 1) * TM * AST;
+        __nv_bfloat16 *nxt = Abuf + (cur ^ 1) * 2 * TM * AST;
         float gpart[3][2][2] = {};
 #pragma unroll
         for (int i = 0; i < 2; i++)
@@ -278,7 +294,7 @@ __device__ __forceinline__ void tile_eval(const float *__restrict__ P, const __n
                     const float d0 = acc[i][j][h * 2] * s.x, d1 = acc[i][j][h * 2 + 1] * s.y;
                     if (l > 1) {
                         const int r = acc_row(i, h * 2), c = acc_col(j, h * 2);
-                        *reinterpret_cast<__nv_bfloat162 *>(nxt + r * AST + c) = __floats2bfloat162_rn(d0, d1);
+                        store_split(nxt, r, c, d0, d1);
                     } else {
                         const int c = acc_col(j, h * 2);
 #pragma unroll
@@ -304,9 +320,35 @@ __device__ __forceinline__ void tile_eval(const float *__restrict__ P, const __n
     __syncthreads();
 }
 
-// input map and chain rule (gx_mlp.cuh)
+// Spherical (l = 0) part of the SCF expansion and its radial derivative, FP32:
+//   Phi_0 = -(G M / r_s) sum_n S_n00 C_n^{3/2}(xi) / (1 + s),
+//   dPhi_0/dr = (G M / r_s^2) sum_n S_n00 [(1+s)^-2 (n = 0); (1+s)^-3 ((1+s) C_n^{3/2} - 6 C_{n-1}^{5/2}) (n > 0)],
+// s = r / r_s, xi = (s - 1)/(s + 1) (phi_nl and dPhi_nl/dr of bfe_helper.cpp:24-64 at l = 0).
+__device__ __forceinline__ void scf_l0(const float *p, float r, float &phi0, float &dphi0) {
+    const float GM = p[0] * p[3], rs = p[4];
+    const int nmax = (int)p[1], lmax = (int)p[2];
+    const int stride = (lmax + 1) * (lmax + 1);
+    const float s = r / rs, xi = (s - 1.f) / (s + 1.f);
+    const float i1 = 1.f / (1.f + s);
+    float C = 1.f, Cm1 = 0.f, Cm2 = 0.f, D = 1.f, Dm1 = 0.f, Dm2 = 0.f;
+    float sp = 0.f, sd = 0.f;
+    for (int n = 0; n <= nmax; n++) {
+        if (n == 1) { Cm1 = 1.f; C = 3.f * xi; }
+        else if (n > 1) { Cm2 = Cm1; Cm1 = C; C = (2.f * xi * (n + 0.5f) * Cm1 - (n + 1.f) * Cm2) / n; }
+        const int nd = n - 1;
+        if (nd == 1) { Dm1 = 1.f; D = 5.f * xi; }
+        else if (nd > 1) { Dm2 = Dm1; Dm1 = D; D = (2.f * xi * (nd + 1.5f) * Dm1 - (nd + 3.f) * Dm2) / nd; }
+        const float Sn = p[5 + n * stride];
+        sp += Sn * C;
+        sd += Sn * ((n == 0) ? i1 : i1 * ((1.f + s) * C - 6.f * D) * i1);
+    }
+    phi0 = -GM / rs * sp * i1;
+    dphi0 = GM / (rs * rs) * sd * i1;
+}
+
+// input map and chain rule (gx_mlp.cuh): Phi = Phi_0 + Phi_H y
 struct MapPt {
-    float r, nx, ny, nz, rho, drho, phiH, dphiH;
+    float r, nx, ny, nz, rho, drho, phiH, dphiH, phi0, dphi0;
 };
 
 __device__ __forceinline__ MapPt map_point(const InferArgs &A, float x, float y, float z) {
@@ -322,6 +364,7 @@ __device__ __forceinline__ MapPt map_point(const InferArgs &A, float x, float y,
     const float irs = 1.f / (m.r + A.r_s);
     m.phiH = -A.GM * irs;
     m.dphiH = A.GM * irs * irs;  // d Phi_H / dr
+    scf_l0(A.scf, m.r, m.phi0, m.dphi0);
     return m;
 }
 
@@ -332,66 +375,92 @@ __device__ __forceinline__ void surrogate_grad(const MapPt &m, float yv, const f
     const float jx = a * (g[0] - m.nx * ng) + m.drho * m.nx * ng;
     const float jy = a * (g[1] - m.ny * ng) + m.drho * m.ny * ng;
     const float jz = a * (g[2] - m.nz * ng) + m.drho * m.nz * ng;
-    const float radial = m.dphiH * (1.f + yv);
+    const float radial = m.dphi0 + m.dphiH * yv;
     out[0] = radial * m.nx + m.phiH * jx;
     out[1] = radial * m.ny + m.phiH * jy;
     out[2] = radial * m.nz + m.phiH * jz;
 }
 
-// Analytic SCF gradient in FP32 (same series as gx_scf.cuh, gala's packing).
-__device__ __noinline__ void scf_grad_f32(const float *p, const float *q, float *g) {
+// Analytic SCF gradient in FP32 (same series as gx_scf.cuh, gala's packing),
+// computed by a whole warp for one point: lane q handles the (l, m) pairs
+// q, q + 32, ... (P_l^m by its recurrence in l at fixed m, Gegenbauer terms by
+// their recurrence in n); the three spherical components are warp-reduced.
+// Every lane returns the gradient.
+__device__ __noinline__ void scf_grad_f32_warp(const float *p, const float *q, float *g) {
     const float SQRT_FOURPI = 3.544907701811031f, PI = 3.14159265358979f;
+    const int lane = threadIdx.x & 31;
     const float G = p[0], M = p[3], r_s = p[4];
     const int nmax = (int)p[1], lmax = (int)p[2];
     const int ncoef = (nmax + 1) * (lmax + 1) * (lmax + 1);
     const float *S = p + 5, *T = p + 5 + ncoef;
     const float r = sqrtf(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
     const float s = r / r_s, X = q[2] / r, phi = atan2f(q[1], q[0]);
-    const float sint = sqrtf(fmaxf(1.f - X * X, 0.f)), xi = (s - 1.f) / (s + 1.f);
-    float cm[16], sm[16], Pl[16], Pl1[16], Pl2[16];
-    for (int m = 0; m < 16; m++) { Pl[m] = 0.f; Pl1[m] = 0.f; Pl2[m] = 0.f; }
-    for (int m = 0; m <= lmax; m++) __sincosf(m * phi, &sm[m], &cm[m]);
+    // on the z axis 1 - X^2 rounds to 0 in FP32; the series' 1/sin(theta) terms
+    // have finite limits there, approached here by a floor on sin(theta)
+    const float sint = fmaxf(sqrtf(fmaxf(1.f - X * X, 0.f)), 1e-6f), xi = (s - 1.f) / (s + 1.f);
     float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-    for (int l = 0; l <= lmax; l++) {
-        for (int m = 0; m < l; m++) { Pl2[m] = Pl1[m]; Pl1[m] = Pl[m]; }
-        for (int m = 0; m <= l; m++) {
-            if (m == l) Pl[m] = (l == 0) ? 1.f : -(2.f * l - 1.f) * sint * Pl1[l - 1];
-            else if (m == l - 1) Pl[m] = X * (2.f * m + 1.f) * Pl1[m];
-            else Pl[m] = (X * (2.f * l - 1.f) * Pl1[m] - (l + m - 1.f) * Pl2[m]) / (float)(l - m);
+    const int npairs = (lmax + 1) * (lmax + 2) / 2;
+    for (int qi = lane; qi < npairs; qi += 32) {
+        int l = (int)((sqrtf(8.f * qi + 1.f) - 1.f) * 0.5f);
+        while ((l + 1) * (l + 2) / 2 <= qi) l++;
+        while (l * (l + 1) / 2 > qi) l--;
+        const int m = qi - l * (l + 1) / 2;
+        // P_l^m and P_{l-1}^m (Condon-Shortley phase)
+        float pmm = 1.f;
+        for (int i = 1; i <= m; i++) pmm *= -(2.f * i - 1.f) * sint;
+        float Plm = pmm, Pl1m = 0.f;
+        if (l > m) {
+            float pm2 = pmm, pm1 = X * (2.f * m + 1.f) * pmm;
+            for (int ll = m + 2; ll <= l; ll++) {
+                const float pl = (X * (2.f * ll - 1.f) * pm1 - (ll + m - 1.f) * pm2) / (float)(ll - m);
+                pm2 = pm1;
+                pm1 = pl;
+            }
+            Plm = pm1;
+            Pl1m = pm2;
         }
+        float fl = 1.f;  // (l-m)!/(l+m)!
+        for (int i = l - m + 1; i <= l + m; i++) fl /= (float)i;
+        const float norm = sqrtf((2 * l + 1) / (4.f * PI) * fl);
+        const float Y = norm * Plm;
+        const float dY = (l > 0) ? norm / sint * (l * X * Plm - (l + m) * Pl1m) : 0.f;
+        float sm, cm;
+        __sincosf(m * phi, &sm, &cm);
         const float a1c = 2 * l + 1.5f, a2c = 2 * l + 2.5f;
         const float psl = __powf(s, (float)l), pslm1 = __powf(s, (float)(l - 1));
         const float p1 = __powf(1.f + s, -2.f * l - 1.f), p3 = __powf(1.f + s, -3.f - 2.f * l);
-        float Cm2 = 0.f, Cm1 = 0.f, C = 1.f, Dm2 = 0.f, Dm1 = 0.f, D = 1.f;
+        float Cm1 = 0.f, C = 1.f, Dm1 = 0.f, D = 1.f;
         for (int n = 0; n <= nmax; n++) {
             if (n == 1) { Cm1 = 1.f; C = 2.f * a1c * xi; }
-            else if (n > 1) { Cm2 = Cm1; Cm1 = C; C = (2.f * xi * (n + a1c - 1.f) * Cm1 - (n + 2.f * a1c - 2.f) * Cm2) / n; }
+            else if (n > 1) {
+                const float Cn = (2.f * xi * (n + a1c - 1.f) * C - (n + 2.f * a1c - 2.f) * Cm1) / n;
+                Cm1 = C;
+                C = Cn;
+            }
             const int nd = n - 1;
             if (nd == 1) { Dm1 = 1.f; D = 2.f * a2c * xi; }
-            else if (nd > 1) { Dm2 = Dm1; Dm1 = D; D = (2.f * xi * (nd + a2c - 1.f) * Dm1 - (nd + 2.f * a2c - 2.f) * Dm2) / nd; }
+            else if (nd > 1) {
+                const float Dn = (2.f * xi * (nd + a2c - 1.f) * D - (nd + 2.f * a2c - 2.f) * Dm1) / nd;
+                Dm1 = D;
+                D = Dn;
+            }
+            const int i = m + (lmax + 1) * (l + (lmax + 1) * n);
+            const float Sv = S[i], Tv = T[i];
+            if (Sv == 0.f && Tv == 0.f) continue;
             const float rad = -SQRT_FOURPI * psl * p1 * C;
             const float drad = (n == 0) ? SQRT_FOURPI * pslm1 * p3 * (1 + s) * (l * (s - 1) + s)
                                         : SQRT_FOURPI * pslm1 * p3 * (-2 * (3 + 4 * l) * s * D + (1 + s) * (l * (s - 1) + s) * C);
-            float fl = 1.f;
-            for (int m = 0; m <= l; m++) {
-                const int i = m + (lmax + 1) * (l + (lmax + 1) * n);
-                const float Sv = S[i], Tv = T[i];
-                // (l-m)!/(l+m)! accumulated as the product 1 / ((l-m+1) ... (l+m))
-                if (m > 0) fl /= (float)((l + m) * (l - m + 1));
-                if (Sv == 0.f && Tv == 0.f) continue;
-                const float norm = sqrtf((2 * l + 1) / (4.f * PI) * fl);
-                const float Y = norm * Pl[m];
-                const float tmp = Sv * cm[m] + Tv * sm[m];
-                float dY = 0.f;
-                if (l > 0) {
-                    const float Pl1m = (m <= l - 1) ? Pl1[m] : 0.f;
-                    dY = norm / sint * (l * X * Pl[m] - (l + m) * Pl1m);
-                }
-                a0 += drad * Y * tmp;
-                a1 += dY * rad / s * tmp;
-                a2 += (float)m * Y * rad * (Tv * cm[m] - Sv * sm[m]) / (s * sint);
-            }
+            const float tmp = Sv * cm + Tv * sm;
+            a0 += drad * Y * tmp;
+            a1 += dY * rad / s * tmp;
+            a2 += (float)m * Y * rad * (Tv * cm - Sv * sm) / (s * sint);
         }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+        a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
     }
     float cphi, sphi;
     __sincosf(phi, &sphi, &cphi);
@@ -401,8 +470,30 @@ __device__ __noinline__ void scf_grad_f32(const float *p, const float *q, float 
     g[2] = (X * a0 - sint * a1) * f;
 }
 
+// Points of the tile outside [r_min, r_max]: each warp computes the analytic
+// force of every 8th listed point; results land in fb[64][3].  Uses the
+// caller's smem list of (row, x, y, z) and count; ends with __syncthreads.
+__device__ __forceinline__ void tile_fallback(const InferArgs &A, const int *cnt, const float4 *list, float *fb) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nfb = *cnt;
+    for (int e = warp; e < nfb; e += NT / 32) {
+        const float4 pt = list[e];
+        const float q[3] = {pt.y, pt.z, pt.w};
+        float g[3];
+        scf_grad_f32_warp(A.scf, q, g);
+        if (lane == 0) {
+            const int row = (int)pt.x;
+            fb[row * 3 + 0] = g[0];
+            fb[row * 3 + 1] = g[1];
+            fb[row * 3 + 2] = g[2];
+        }
+    }
+    __syncthreads();
+}
+
 // Evaluate the surrogate force at n points (q: 3 x n SoA, float64), into
 // out (3 x n, float64) and the potential (n) -- for tests and diagnostics.
+template <int SPLIT>
 __global__ void __launch_bounds__(NT, 1) surrogate_eval_kernel(InferArgs A, const float *__restrict__ P,
                                                                 const __nv_bfloat16 *__restrict__ Wb,
                                                                 const double *__restrict__ q, int64_t n,
@@ -411,6 +502,10 @@ __global__ void __launch_bounds__(NT, 1) surrogate_eval_kernel(InferArgs A, cons
     float *xh = reinterpret_cast<float *>(smem + SMEM_A + SMEM_W);   // [64][3]
     float *yv = xh + TM * 3;                                          // [64]
     float *G = yv + TM;                                               // [64][3]
+    char *fbbase = smem + SMEM_A + SMEM_W + TM * 8 * 4 + 4 * TM * 4 * 4;
+    float4 *fblist = reinterpret_cast<float4 *>(fbbase);              // [64] (row, x, y, z)
+    float *fbg = reinterpret_cast<float *>(fbbase + TM * 16);         // [64][3]
+    int *fbcnt = reinterpret_cast<int *>(fbbase + TM * 16 + TM * 3 * 4);
     const int64_t ntiles = (n + TM - 1) / TM;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t i = tile * TM + threadIdx.x;
@@ -423,20 +518,29 @@ __global__ void __launch_bounds__(NT, 1) surrogate_eval_kernel(InferArgs A, cons
             xh[threadIdx.x * 3 + 1] = m.rho * m.ny;
             xh[threadIdx.x * 3 + 2] = m.rho * m.nz;
         }
+        if (threadIdx.x == 0) *fbcnt = 0;
         __syncthreads();
-        tile_eval(P, Wb, smem, xh, yv, G);
+        tile_eval<SPLIT>(P, Wb, smem, xh, yv, G);
+        const bool outside = threadIdx.x < TM && i < n && !(m.r >= A.r_min && m.r <= A.r_max);
+        if (outside) {
+            const int e = atomicAdd(fbcnt, 1);
+            fblist[e] = make_float4((float)threadIdx.x, (float)q[i], (float)q[n + i], (float)q[2 * n + i]);
+        }
+        __syncthreads();
+        tile_fallback(A, fbcnt, fblist, fbg);
         if (threadIdx.x < TM && i < n) {
             float gr[3];
-            if (m.r >= A.r_min && m.r <= A.r_max) {
+            if (!outside) {
                 surrogate_grad(m, yv[threadIdx.x], G + threadIdx.x * 3, gr);
             } else {
-                const float qq[3] = {(float)q[i], (float)q[n + i], (float)q[2 * n + i]};
-                scf_grad_f32(A.scf, qq, gr);
+                gr[0] = fbg[threadIdx.x * 3 + 0];
+                gr[1] = fbg[threadIdx.x * 3 + 1];
+                gr[2] = fbg[threadIdx.x * 3 + 2];
             }
             grad[i] = gr[0];
             grad[n + i] = gr[1];
             grad[2 * n + i] = gr[2];
-            if (phi) phi[i] = (double)m.phiH * (1.0 + (double)yv[threadIdx.x]);
+            if (phi) phi[i] = (double)m.phi0 + (double)m.phiH * (double)yv[threadIdx.x];
         }
         __syncthreads();
     }
@@ -457,16 +561,21 @@ __device__ __forceinline__ void kahan(float &s, float &c, float d) {
 // surrogate potential; n_steps and dt shared by all orbits; FP32 state with
 // Kahan compensation; final state (6 x n, float64) and the count of force
 // evaluations that used the analytic fallback.
+template <int SPLIT>
 __global__ void __launch_bounds__(NT, 1) surrogate_leapfrog_kernel(InferArgs A, const float *__restrict__ P,
                                                                     const __nv_bfloat16 *__restrict__ Wb,
                                                                     const double *__restrict__ w0, int64_t n,
-                                                                    int64_t nsteps, float dt,
+                                                                    int64_t nsteps, float dt, int analytic,
                                                                     double *__restrict__ w_out,
                                                                     unsigned long long *__restrict__ fallbacks) {
     extern __shared__ __align__(16) char smem[];
     float *xh = reinterpret_cast<float *>(smem + SMEM_A + SMEM_W);
     float *yv = xh + TM * 3;
     float *G = yv + TM;
+    char *fbbase = smem + SMEM_A + SMEM_W + TM * 8 * 4 + 4 * TM * 4 * 4;
+    float4 *fblist = reinterpret_cast<float4 *>(fbbase);
+    float *fbg = reinterpret_cast<float *>(fbbase + TM * 16);
+    int *fbcnt = reinterpret_cast<int *>(fbbase + TM * 16 + TM * 3 * 4);
     const int64_t ntiles = (n + TM - 1) / TM;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t i = tile * TM + threadIdx.x;
@@ -490,13 +599,23 @@ __global__ void __launch_bounds__(NT, 1) surrogate_leapfrog_kernel(InferArgs A, 
                 xh[threadIdx.x * 3 + 1] = m.rho * m.ny;
                 xh[threadIdx.x * 3 + 2] = m.rho * m.nz;
             }
+            if (threadIdx.x == 0) *fbcnt = 0;
             __syncthreads();
-            tile_eval(P, Wb, smem, xh, yv, G);
+            if (!analytic) tile_eval<SPLIT>(P, Wb, smem, xh, yv, G);
+            const bool outside = own && (analytic || !(m.r >= A.r_min && m.r <= A.r_max));
+            if (outside) {
+                const int e = atomicAdd(fbcnt, 1);
+                fblist[e] = make_float4((float)threadIdx.x, xh_[0], xh_[1], xh_[2]);
+            }
+            __syncthreads();
+            tile_fallback(A, fbcnt, fblist, fbg);
             if (own) {
-                if (m.r >= A.r_min && m.r <= A.r_max) {
+                if (!outside) {
                     surrogate_grad(m, yv[threadIdx.x], G + threadIdx.x * 3, g);
                 } else {
-                    scf_grad_f32(A.scf, xh_, g);
+                    g[0] = fbg[threadIdx.x * 3 + 0];
+                    g[1] = fbg[threadIdx.x * 3 + 1];
+                    g[2] = fbg[threadIdx.x * 3 + 2];
                     nfb++;
                 }
                 const float f = (step == 0) ? 0.5f : 1.0f;
@@ -521,9 +640,11 @@ __global__ void __launch_bounds__(NT, 1) surrogate_leapfrog_kernel(InferArgs A, 
 
 using namespace gx::mlpi;
 
-static int infer_args(const float *scf_params, double r_min, double r_max, double GM, double r_s, InferArgs *A) {
-    GX_CHECK_ARG(scf_params != nullptr, "NULL SCF parameters (analytic fallback)");
+static int infer_args(const float *scf_params, double r_min, double r_max, double GM, double r_s, int32_t split,
+                      InferArgs *A) {
+    GX_CHECK_ARG(scf_params != nullptr, "NULL SCF parameters (analytic base and fallback)");
     GX_CHECK_ARG(r_min > 0 && r_max > r_min && GM > 0 && r_s > 0, "bad surrogate input map");
+    GX_CHECK_ARG(split == 1 || split == 2, "split must be 1 (BF16 activations) or 2 (BF16 hi + lo)");
     A->r_min = (float)r_min;
     A->r_max = (float)r_max;
     A->rho0 = 0.1f;
@@ -533,41 +654,56 @@ static int infer_args(const float *scf_params, double r_min, double r_max, doubl
     A->scf = scf_params;
     static bool configured = false;
     if (!configured) {
-        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_eval_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          SMEM_BYTES));
-        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_leapfrog_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_eval_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          SMEM_BYTES));
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_leapfrog_kernel<1>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_leapfrog_kernel<2>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
         configured = true;
     }
     return GX_OK;
 }
 
 extern "C" int gx_surrogate_gradient(const float *params, const void *wbf16, const float *scf_params, double r_min,
-                                     double r_max, double GM, double r_s, const double *q, int64_t n, double *grad,
-                                     double *phi, int32_t grid, void *stream) {
+                                     double r_max, double GM, double r_s, int32_t split, const double *q, int64_t n,
+                                     double *grad, double *phi, int32_t grid, void *stream) {
     InferArgs A;
-    int rc = infer_args(scf_params, r_min, r_max, GM, r_s, &A);
+    int rc = infer_args(scf_params, r_min, r_max, GM, r_s, split, &A);
     if (rc) return rc;
     GX_CHECK_ARG(n >= 0, "n < 0");
     if (n == 0) return GX_OK;
     GX_CHECK_ARG(params && wbf16 && q && grad && grid >= 1, "NULL array or bad grid");
-    surrogate_eval_kernel<<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
-        A, params, static_cast<const __nv_bfloat16 *>(wbf16), q, n, grad, phi);
+    const __nv_bfloat16 *w = static_cast<const __nv_bfloat16 *>(wbf16);
+    cudaStream_t st = gx::as_stream(stream);
+    if (split == 2)
+        surrogate_eval_kernel<2><<<grid, NT, SMEM_BYTES, st>>>(A, params, w, q, n, grad, phi);
+    else
+        surrogate_eval_kernel<1><<<grid, NT, SMEM_BYTES, st>>>(A, params, w, q, n, grad, phi);
     return gx::check_launch("surrogate_gradient");
 }
 
 extern "C" int gx_surrogate_leapfrog(const float *params, const void *wbf16, const float *scf_params, double r_min,
-                                     double r_max, double GM, double r_s, const double *w0, int64_t n,
-                                     int64_t n_steps, double dt, double *w_out, unsigned long long *fallbacks,
-                                     int32_t grid, void *stream) {
+                                     double r_max, double GM, double r_s, int32_t split, int32_t analytic,
+                                     const double *w0, int64_t n, int64_t n_steps, double dt, double *w_out,
+                                     unsigned long long *fallbacks, int32_t grid, void *stream) {
     InferArgs A;
-    int rc = infer_args(scf_params, r_min, r_max, GM, r_s, &A);
+    int rc = infer_args(scf_params, r_min, r_max, GM, r_s, split, &A);
     if (rc) return rc;
     GX_CHECK_ARG(n >= 0 && n_steps >= 0, "n and n_steps must be >= 0");
     if (n == 0) return GX_OK;
-    GX_CHECK_ARG(params && wbf16 && w0 && w_out && fallbacks && grid >= 1, "NULL array or bad grid");
-    surrogate_leapfrog_kernel<<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
-        A, params, static_cast<const __nv_bfloat16 *>(wbf16), w0, n, n_steps, (float)dt, w_out, fallbacks);
+    GX_CHECK_ARG(w0 && w_out && fallbacks && grid >= 1, "NULL array or bad grid");
+    GX_CHECK_ARG(analytic || (params && wbf16), "NULL network parameters");
+    const __nv_bfloat16 *w = static_cast<const __nv_bfloat16 *>(wbf16);
+    cudaStream_t st = gx::as_stream(stream);
+    if (split == 2)
+        surrogate_leapfrog_kernel<2><<<grid, NT, SMEM_BYTES, st>>>(A, params, w, w0, n, n_steps, (float)dt,
+                                                                   analytic, w_out, fallbacks);
+    else
+        surrogate_leapfrog_kernel<1><<<grid, NT, SMEM_BYTES, st>>>(A, params, w, w0, n, n_steps, (float)dt,
+                                                                   analytic, w_out, fallbacks);
     return gx::check_launch("surrogate_leapfrog");
 }
 

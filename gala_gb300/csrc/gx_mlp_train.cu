@@ -24,67 +24,109 @@ namespace mlp {
 
 // C[M,N] = alpha * op(A)[M,K] op(B)[K,N] + beta * C.  TA: A is stored [K][M]
 // (element (m,k) at A[k*lda+m]) instead of [M][K]; TB: B stored [N][K].
+// 128 x 128 block tile, K slabs of 8 staged through shared memory (double
+// buffered), 256 threads each computing an 8 x 8 register tile.
 template <bool TA, bool TB>
 __global__ void __launch_bounds__(256) gemm_f32(int M, int N, int K, float alpha, const float *__restrict__ A,
                                                 int lda, const float *__restrict__ B, int ldb, float beta,
                                                 float *__restrict__ C, int ldc) {
-    constexpr int BM = 64, BN = 64, BK = 16;
-    __shared__ float As[BK][BM + 4];
-    __shared__ float Bs[BK][BN + 4];
+    constexpr int BM = 128, BN = 128, BK = 8;
+    __shared__ __align__(16) float As[2][BK][BM];
+    __shared__ __align__(16) float Bs[2][BK][BN];
     const int tid = threadIdx.x;
     const int tx = tid % 16, ty = tid / 16;
     const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-    float acc[4][4] = {};
-    for (int k0 = 0; k0 < K; k0 += BK) {
-        for (int e = tid; e < BK * BM; e += 256) {
+    // split-K: this CTA covers K range [kbeg, kend)
+    const int kchunk = ((K + gridDim.z - 1) / gridDim.z + BK - 1) / BK * BK;
+    const int kbeg = blockIdx.z * kchunk;
+    const int kend = min(K, kbeg + kchunk);
+    float acc[8][8] = {};
+    float ra[4], rb[4];
+    auto gload = [&](int k0) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int e = tid + q * 256;
             int kk, mm;
             if (TA) { mm = e % BM; kk = e / BM; } else { kk = e % BK; mm = e / BK; }
             const int gm = m0 + mm, gk = k0 + kk;
-            float v = 0.f;
-            if (gm < M && gk < K) v = TA ? A[(int64_t)gk * lda + gm] : A[(int64_t)gm * lda + gk];
-            As[kk][mm] = v;
+            ra[q] = (gm < M && gk < kend) ? (TA ? A[(int64_t)gk * lda + gm] : A[(int64_t)gm * lda + gk]) : 0.f;
+            int kb, nn;
+            if (TB) { kb = e % BK; nn = e / BK; } else { nn = e % BN; kb = e / BN; }
+            const int gn = n0 + nn, gkb = k0 + kb;
+            rb[q] = (gn < N && gkb < kend) ? (TB ? B[(int64_t)gn * ldb + gkb] : B[(int64_t)gkb * ldb + gn]) : 0.f;
         }
-        for (int e = tid; e < BK * BN; e += 256) {
-            int kk, nn;
-            if (TB) { kk = e % BK; nn = e / BK; } else { nn = e % BN; kk = e / BN; }
-            const int gn = n0 + nn, gk = k0 + kk;
-            float v = 0.f;
-            if (gn < N && gk < K) v = TB ? B[(int64_t)gn * ldb + gk] : B[(int64_t)gk * ldb + gn];
-            Bs[kk][nn] = v;
+    };
+    auto sstore = [&](int buf) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int e = tid + q * 256;
+            int kk, mm;
+            if (TA) { mm = e % BM; kk = e / BM; } else { kk = e % BK; mm = e / BK; }
+            As[buf][kk][mm] = ra[q];
+            int kb, nn;
+            if (TB) { kb = e % BK; nn = e / BK; } else { nn = e % BN; kb = e / BN; }
+            Bs[buf][kb][nn] = rb[q];
         }
-        __syncthreads();
+    };
+    gload(kbeg);
+    sstore(0);
+    __syncthreads();
+    int buf = 0;
+    for (int k0 = kbeg; k0 < kend; k0 += BK) {
+        const bool more = k0 + BK < kend;
+        if (more) gload(k0 + BK);
 #pragma unroll
         for (int kk = 0; kk < BK; kk++) {
-            float a[4], b[4];
+            float a[8], b[8];
+            const float4 a0 = *reinterpret_cast<const float4 *>(&As[buf][kk][ty * 4]);
+            const float4 a1 = *reinterpret_cast<const float4 *>(&As[buf][kk][64 + ty * 4]);
+            const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][tx * 4]);
+            const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[buf][kk][64 + tx * 4]);
+            a[0] = a0.x; a[1] = a0.y; a[2] = a0.z; a[3] = a0.w; a[4] = a1.x; a[5] = a1.y; a[6] = a1.z; a[7] = a1.w;
+            b[0] = b0.x; b[1] = b0.y; b[2] = b0.z; b[3] = b0.w; b[4] = b1.x; b[5] = b1.y; b[6] = b1.z; b[7] = b1.w;
 #pragma unroll
-            for (int i = 0; i < 4; i++) a[i] = As[kk][ty * 4 + i];
+            for (int i = 0; i < 8; i++)
 #pragma unroll
-            for (int j = 0; j < 4; j++) b[j] = Bs[kk][tx * 4 + j];
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int j = 0; j < 4; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
+                for (int j = 0; j < 8; j++) acc[i][j] = fmaf(a[i], b[j], acc[i][j]);
         }
-        __syncthreads();
+        if (more) {
+            sstore(buf ^ 1);
+            __syncthreads();
+            buf ^= 1;
+        }
     }
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const int gm = m0 + ty * 4 + i;
+    for (int i = 0; i < 8; i++) {
+        const int gm = m0 + (i < 4 ? ty * 4 + i : 64 + ty * 4 + i - 4);
         if (gm >= M) continue;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int gn = n0 + tx * 4 + j;
+        for (int j = 0; j < 8; j++) {
+            const int gn = n0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4);
             if (gn >= N) continue;
             float *c = &C[(int64_t)gm * ldc + gn];
-            *c = alpha * acc[i][j] + (beta == 0.f ? 0.f : beta * *c);
+            if (gridDim.z > 1)
+                atomicAdd(c, alpha * acc[i][j]);  // split-K: C already holds beta * C
+            else
+                *c = alpha * acc[i][j] + (beta == 0.f ? 0.f : beta * *c);
         }
     }
 }
 
+// Split K over extra CTAs when the output tile grid is small (weight gradients:
+// 256 x 256 outputs, K = batch).  Split-K accumulates into C, so it is used
+// only with beta = 1.
 template <bool TA, bool TB>
 static void gemm(cudaStream_t st, int M, int N, int K, float alpha, const float *A, int lda, const float *B,
                  int ldb, float beta, float *C, int ldc) {
-    dim3 grid((N + 63) / 64, (M + 63) / 64);
+    const int tiles = ((N + 127) / 128) * ((M + 127) / 128);
+    int split = 1;
+    if (beta == 1.f && tiles < 152) {
+        split = (2 * 152 + tiles - 1) / tiles;
+        const int maxsplit = (K + 255) / 256;
+        if (split > maxsplit) split = maxsplit;
+        if (split < 1) split = 1;
+    }
+    dim3 grid((N + 127) / 128, (M + 127) / 128, split);
     gemm_f32<TA, TB><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc);
 }
 
@@ -128,20 +170,23 @@ __global__ void mul_kernel(int64_t n, const float *__restrict__ x, const float *
     if (i < n) out[i] = x[i] * y[i];
 }
 
-// loss terms and their seeds: e = 2 alpha (y - y*) / B, E = 2 beta (G - G*) / B
+// loss terms and their seeds: e = 2 alpha (y - y*) / B, E = 2 beta w (G - G*) / B
+// (w = per-sample weight of the gradient term, 1 if wg is NULL)
 __global__ void loss_kernel(int64_t B, float alpha, float beta, const float *__restrict__ y,
                             const float *__restrict__ ys, const float *__restrict__ G, const float *__restrict__ Gs,
-                            float *__restrict__ e, float *__restrict__ E, float *__restrict__ loss) {
+                            const float *__restrict__ wg, float *__restrict__ e, float *__restrict__ E,
+                            float *__restrict__ loss) {
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     float lv = 0.f, lg = 0.f;
     if (b < B) {
         const float dv = y[b] - ys[b];
         e[b] = 2.f * alpha * dv / (float)B;
         lv = dv * dv;
+        const float wb = wg ? wg[b] : 1.f;
         for (int j = 0; j < 3; j++) {
             const float dg = G[b * 3 + j] - Gs[b * 3 + j];
-            E[b * 3 + j] = 2.f * beta * dg / (float)B;
-            lg += dg * dg;
+            E[b * 3 + j] = 2.f * beta * wb * dg / (float)B;
+            lg += wb * dg * dg;
         }
     }
 #pragma unroll
@@ -278,8 +323,8 @@ extern "C" int gx_mlp_forward(const float *params, const float *xh, int64_t B, f
 }
 
 extern "C" int gx_mlp_train_step(const float *params, float *grads, const float *xh, const float *ystar,
-                                 const float *Gstar, int64_t B, float alpha, float beta, float *workspace,
-                                 float *loss, void *stream) {
+                                 const float *Gstar, const float *gweight, int64_t B, float alpha, float beta,
+                                 float *workspace, float *loss, void *stream) {
     GX_CHECK_ARG(params && grads && xh && ystar && Gstar && workspace && loss, "NULL pointer");
     GX_CHECK_ARG(B > 0 && B < (1 << 26), "batch out of range");
     cudaStream_t st = gx::as_stream(stream);
@@ -310,7 +355,7 @@ extern "C" int gx_mlp_train_step(const float *params, float *grads, const float 
     // forward and input gradient
     int rc = gx_mlp_forward(params, xh, B, y, G, workspace, stream);
     if (rc) return rc;
-    loss_kernel<<<nblk(B, 256), 256, 0, st>>>(B, alpha, beta, y, ystar, G, Gstar, e, E, loss);
+    loss_kernel<<<nblk(B, 256), 256, 0, st>>>(B, alpha, beta, y, ystar, G, Gstar, gweight, e, E, loss);
 
     // adjoint of the input-gradient pass
     gemm<true, false>(st, H, 3, (int)B, 1.f, D[1], H, E, 3, 1.f, g + OFF_W1, 3);      // W1g += D1^T E

@@ -4,18 +4,21 @@ Model (see gala_gb300/csrc/gx_mlp.cuh): an MLP y(xh) with 3 -> 256 -> 256 ->
 256 -> 256 -> 1 units and SiLU activations, where xh maps the position into the
 unit ball with a logarithmic radius, and
 
-    Phi(x) = Phi_H(r) (1 + y(xh)),    Phi_H = -G M / (r + r_s),
+    Phi(x) = Phi_0(r) + Phi_H(r) y(xh),    Phi_H = -G M / (r + r_s),
 
-Phi_H being the S000 (Hernquist) term of the SCF expansion, so the network only
-learns the bounded correction.  Training data are (x, Phi, grad Phi) samples of
+Phi_0 being the spherical (l = 0) part of the SCF expansion, evaluated exactly,
+and Phi_H a fixed radial scale, so the network only learns the bounded
+non-spherical part.  Training data are (x, Phi, grad Phi) samples of
 the analytic SCF potential, computed on the GPU in FP64
 (gx_potential_value / gx_potential_gradient), with r log-uniform in
 [r_min, r_max] and isotropic directions.  Training runs the library's own FP32
 forward / backward / double-backward kernels (gx_mlp_train_step) with Adam
 (gx_mlp_adam) on a loss that fits both y and dy/dxh.  Inference
 (gx_surrogate_gradient, gx_surrogate_leapfrog) uses BF16 weights on the tensor
-cores with FP32 accumulation; outside [r_min, r_max] the analytic SCF force
-(FP32) is used instead.
+cores with FP32 accumulation (activations as BF16 hi + lo pairs by default);
+the last part of training uses BF16-rounded weights in the forward pass, so the
+network that is trained is the one the tensor cores evaluate.  Outside
+[r_min, r_max] the analytic SCF force (FP32) is used instead.
 """
 from __future__ import annotations
 
@@ -64,11 +67,40 @@ def input_map(x, r_min, r_max, xp=np):
     return rho * n, r, n, rho, drho
 
 
+def scf_l0(scf, r, xp=np):
+    """Spherical part of the SCF expansion: Phi_0(r) and dPhi_0/dr (FP64),
+    from phi_nl / dphi_nl at l = 0 (gala: src/gala/potential/scf/src/bfe_helper.cpp:24-64)."""
+    p = scf.packed().params
+    GM, rs = p[0] * p[3], p[4]
+    nmax, lmax = int(p[1]), int(p[2])
+    Sn = p[5:5 + (nmax + 1) * (lmax + 1) ** 2].reshape(nmax + 1, lmax + 1, lmax + 1)[:, 0, 0]
+    s = r / rs
+    xi = (s - 1) / (s + 1)
+    i1 = 1.0 / (1.0 + s)
+    C, Cm1 = xp.ones_like(s), xp.zeros_like(s)
+    D, Dm1 = xp.ones_like(s), xp.zeros_like(s)
+    sp = Sn[0] * C
+    sd = Sn[0] * i1
+    for n in range(1, nmax + 1):
+        if n == 1:
+            Cm1, C = C, 3.0 * xi
+        else:
+            Cm1, C = C, (2 * xi * (n + 0.5) * C - (n + 1.0) * Cm1) / n
+        nd = n - 1
+        if nd == 1:
+            Dm1, D = D, 5.0 * xi
+        elif nd > 1:
+            Dm1, D = D, (2 * xi * (nd + 1.5) * D - (nd + 3.0) * Dm1) / nd
+        sp = sp + Sn[n] * C
+        sd = sd + Sn[n] * i1 * ((1 + s) * C - 6.0 * D) * i1
+    return -GM / rs * sp * i1, GM / rs ** 2 * sd * i1
+
+
 class SurrogatePotential:
     """Surrogate of an SCFPotential (or any potential whose monopole is the
     Hernquist sphere (m, r_s)), trained on the GPU."""
 
-    def __init__(self, scf, r_min=0.5, r_max=200.0, seed=0):
+    def __init__(self, scf, r_min=0.5, r_max=200.0, seed=0, split=2):
         import torch
 
         from ._device import require_cuda
@@ -85,6 +117,7 @@ class SurrogatePotential:
         self.params = torch.from_numpy(init_params(seed)).to(self.dev)
         self.scf_f32 = torch.from_numpy(scf.packed().params.astype(np.float32)).to(self.dev)
         self.wbf16 = None
+        self.split = int(split)
         self.history = []
 
     # --------------------------------------------------------------- data
@@ -103,11 +136,15 @@ class SurrogatePotential:
         xh, r, nvec, rho, drho = input_map(x, self.r_min, self.r_max, xp=torch)
         phiH = -self.GM / (r + self.r_s)
         dphiH = self.GM / (r + self.r_s) ** 2          # d Phi_H / dr
-        ystar = phi / phiH - 1.0
-        v = (grad - dphiH * nvec * (1.0 + ystar)) / phiH  # grad_x y*
+        phi0, dphi0 = scf_l0(self.scf, r, xp=torch)
+        ystar = (phi - phi0) / phiH
+        v = (grad - (dphi0 + dphiH * ystar) * nvec) / phiH  # grad_x y*
         nv = (nvec * v).sum(axis=0)
         gstar = (r / rho) * (v - nvec * nv) + nvec * nv / drho  # J^-T v
-        return xh, ystar, gstar
+        # weight of the gradient term: the physical force error is
+        # |Phi_H J^T dG| ~ |grad Phi| rho (1 + r_s / r) |dG|, so weight by that factor squared
+        wg = (rho * (1.0 + self.r_s / r)) ** 2
+        return xh, ystar, gstar, wg
 
     def sample_positions(self, n, seed):
         import torch
@@ -125,25 +162,31 @@ class SurrogatePotential:
     def make_dataset(self, n_samples=16 * 1024 * 1024, seed=1, chunk=1 << 21):
         import torch
 
-        xs, ys, gs = [], [], []
+        xs, ys, gs, ws = [], [], [], []
         for i, s in enumerate(range(0, n_samples, chunk)):
             m = min(chunk, n_samples - s)
             x = self.sample_positions(m, seed * 1000 + i)
-            xh, ystar, gstar = self.targets(x)
+            xh, ystar, gstar, wg = self.targets(x)
             xs.append(xh.T.float())
             ys.append(ystar.float())
             gs.append(gstar.T.float())
+            ws.append(wg)
         self.X = torch.cat(xs).contiguous()
         self.Y = torch.cat(ys).contiguous()
         self.Gt = torch.cat(gs).contiguous()
+        w = torch.cat(ws)
+        self.Wg = (w / w.mean()).float().contiguous()
         self.y_scale = float(self.Y.std())
         return self.X.shape[0]
 
     # ------------------------------------------------------------ training
-    def train(self, steps=4000, batch=8192, lr=1e-3, lr_min=1e-5, beta=1.0, seed=2, log_every=500):
+    def train(self, steps=6000, batch=8192, lr=1e-3, lr_min=1e-5, beta=4.0, seed=2, log_every=500,
+              qat_fraction=0.3):
         """Adam with cosine learning-rate decay on minibatches of the dataset.
         The targets are divided by y_scale during training; the scale is folded
-        into the output layer afterwards."""
+        into the output layer afterwards.  For the last `qat_fraction` of the
+        steps the 256 x 256 weights are rounded to BF16 for the forward and
+        backward passes (the update goes to the FP32 weights)."""
         import torch
 
         from ._device import ptr, stream_handle
@@ -160,10 +203,20 @@ class SurrogatePotential:
         N = self.X.shape[0]
         lib = _abi.load()
         h = stream_handle()
+        qp = self.params.clone()
+        qat_start = int(steps * (1.0 - qat_fraction)) + 1
+        big = [(o, o + H * H) for o in (OFF_W2, OFF_W3, OFF_W4)]
         for step in range(1, steps + 1):
             idx = torch.randint(0, N, (batch,), generator=gen, device=self.dev)
             xb, yb, gb = self.X[idx].contiguous(), Ys[idx].contiguous(), Gs[idx].contiguous()
-            _abi.call("gx_mlp_train_step", ptr(self.params), ptr(grads), ptr(xb), ptr(yb), ptr(gb), batch,
+            wb = self.Wg[idx].contiguous()
+            use = self.params
+            if step >= qat_start:
+                qp.copy_(self.params)
+                for a, b in big:
+                    qp[a:b] = self.params[a:b].to(torch.bfloat16).float()
+                use = qp
+            _abi.call("gx_mlp_train_step", ptr(use), ptr(grads), ptr(xb), ptr(yb), ptr(gb), ptr(wb), batch,
                       C.c_float(1.0), C.c_float(beta), ptr(ws), ptr(loss), h)
             lr_t = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * step / steps))
             _abi.call("gx_mlp_adam", ptr(self.params), ptr(grads), ptr(m), ptr(v), NPARAM, C.c_float(lr_t),
@@ -207,25 +260,29 @@ class SurrogatePotential:
         grad = torch.empty((3, n), dtype=torch.float64, device=self.dev)
         phi = torch.empty(n, dtype=torch.float64, device=self.dev)
         _abi.call("gx_surrogate_gradient", ptr(self.params), ptr(self.wbf16), ptr(self.scf_f32), self.r_min,
-                  self.r_max, self.GM, self.r_s, ptr(qd), n, ptr(grad), ptr(phi), self._grid(n), stream_handle())
+                  self.r_max, self.GM, self.r_s, self.split, ptr(qd), n, ptr(grad), ptr(phi), self._grid(n),
+                  stream_handle())
         return grad, phi
 
-    def integrate_leapfrog(self, w0, dt, n_steps, grid=None):
+    def integrate_leapfrog(self, w0, dt, n_steps, grid=None, analytic=False):
         """FP32 leapfrog of every orbit in w0 (6, N) in the surrogate potential;
-        returns the final states (6, N) and the number of fallback force calls."""
+        returns the final states (6, N) and the number of fallback force calls.
+        analytic=True: the same integrator with the analytic SCF force (FP32)
+        for every evaluation, i.e. without the surrogate."""
         import torch
 
         from ._device import as_device_f64, ptr, stream_handle
 
-        if self.wbf16 is None:
+        if self.wbf16 is None and not analytic:
             self.export()
         w0d = as_device_f64(w0)
         n = w0d.shape[1]
         out = torch.empty_like(w0d)
         fb = torch.zeros(1, dtype=torch.int64, device=self.dev)
-        _abi.call("gx_surrogate_leapfrog", ptr(self.params), ptr(self.wbf16), ptr(self.scf_f32), self.r_min,
-                  self.r_max, self.GM, self.r_s, ptr(w0d), n, int(n_steps), float(dt), ptr(out), ptr(fb),
-                  grid or self._grid(n), stream_handle())
+        wb = ptr(self.wbf16) if self.wbf16 is not None else None
+        _abi.call("gx_surrogate_leapfrog", ptr(self.params), wb, ptr(self.scf_f32), self.r_min,
+                  self.r_max, self.GM, self.r_s, self.split, int(bool(analytic)), ptr(w0d), n, int(n_steps),
+                  float(dt), ptr(out), ptr(fb), grid or self._grid(n), stream_handle())
         return out, fb
 
     def forward_fp32(self, xh):

@@ -248,7 +248,7 @@ int gx_batch_integrate_fp32_noalloc(const gx_potential* pot, const double* w0, i
 /* ------------------------------------------------------------------------- */
 /* Learned potential surrogate.  No counterpart in gala: an MLP             */
 /* y(xh), 3 -> 256 -> 256 -> 256 -> 256 -> 1, SiLU, with                        */
-/*   Phi(x) = Phi_H(r) (1 + y(xh)),  Phi_H = -G M / (r + r_s),                   */
+/*   Phi(x) = Phi_0(r) + Phi_H(r) y(xh),  Phi_H = -G M / (r + r_s),             */
 /*   xh = rho(r) x / r,  rho = 0.1 + 0.9 ln(r / r_min) / ln(r_max / r_min).      */
 /* params: FP32 [W1 256x3 | b1 | W2 256x256 | b2 | W3 | b3 | W4 | b4 | w5 | b5]  */
 /* (gx_mlp_param_count() floats).  Training runs on the CUDA cores in FP32;      */
@@ -261,27 +261,36 @@ int64_t gx_mlp_train_workspace_floats(int64_t batch);
 /* y (B) and, if G != NULL, dy/dxh (B x 3) for inputs xh (B x 3), FP32 */
 int gx_mlp_forward(const float* params, const float* xh, int64_t batch, float* y, float* G,
                    float* workspace, void* stream);
-/* gradient of L = alpha mean (y - y*)^2 + beta mean |dy/dxh - G*|^2 w.r.t. params
- * into grads; loss[0], loss[1] = the two mean squared errors */
+/* gradient of L = alpha mean (y - y*)^2 + beta mean w |dy/dxh - G*|^2 w.r.t. params
+ * into grads (w = gweight per sample, or 1 if gweight is NULL); loss[0], loss[1]
+ * = the two mean (weighted) squared errors */
 int gx_mlp_train_step(const float* params, float* grads, const float* xh, const float* ystar,
-                      const float* Gstar, int64_t batch, float alpha, float beta,
-                      float* workspace, float* loss, void* stream);
+                      const float* Gstar, const float* gweight, int64_t batch, float alpha,
+                      float beta, float* workspace, float* loss, void* stream);
 /* Adam update of params (n floats) with moment buffers m, v; step >= 1 */
 int gx_mlp_adam(float* params, const float* grads, float* m, float* v, int64_t n, float lr,
                 float beta1, float beta2, float eps, int64_t step, void* stream);
-/* grad Phi (3 x n) and Phi (n, may be NULL) at q (3 x n); outside
- * [r_min, r_max] the analytic SCF force (FP32, scf_params = gala's packed SCF
- * parameters as float) is used.  grid = number of 256-thread CTAs. */
+/* grad Phi (3 x n) and Phi (n, may be NULL) at q (3 x n) with
+ *   Phi = Phi_0(r) + Phi_H(r) y(xh),
+ * Phi_0 the spherical (l = 0) part of the SCF expansion (FP32, exact) and y the
+ * network; outside [r_min, r_max] the full analytic SCF force (FP32) is used.
+ * scf_params = gala's packed SCF parameters as float.  split = 1: activations
+ * rounded to BF16; split = 2: activations as BF16 hi + lo (two MMAs per tile).
+ * grid = number of 256-thread CTAs. */
 int gx_surrogate_gradient(const float* params, const void* wbf16, const float* scf_params,
-                          double r_min, double r_max, double GM, double r_s, const double* q,
-                          int64_t n, double* grad, double* phi, int32_t grid, void* stream);
+                          double r_min, double r_max, double GM, double r_s, int32_t split,
+                          const double* q, int64_t n, double* grad, double* phi, int32_t grid,
+                          void* stream);
 /* FP32 leapfrog (kick-drift-kick, Kahan-compensated state) of n orbits for
  * n_steps of dt in the surrogate potential; w_out = final states (6 x n);
- * *fallbacks += number of force evaluations that used the analytic SCF. */
+ * *fallbacks += number of force evaluations that used the analytic SCF.
+ * analytic != 0: every force is the analytic SCF force in FP32 (the same
+ * integrator without the surrogate; params / wbf16 may then be NULL). */
 int gx_surrogate_leapfrog(const float* params, const void* wbf16, const float* scf_params,
-                          double r_min, double r_max, double GM, double r_s, const double* w0,
-                          int64_t n, int64_t n_steps, double dt, double* w_out,
-                          unsigned long long* fallbacks, int32_t grid, void* stream);
+                          double r_min, double r_max, double GM, double r_s, int32_t split,
+                          int32_t analytic, const double* w0, int64_t n, int64_t n_steps,
+                          double dt, double* w_out, unsigned long long* fallbacks, int32_t grid,
+                          void* stream);
 int gx_surrogate_smem_bytes(void);
 
 /* ------------------------------------------------------------------------- */

@@ -54,7 +54,7 @@ def test_forward_and_train_step_match_oracle(scf):
     import ctypes as C
 
     _abi.call("gx_mlp_train_step", sp.params.data_ptr(), grads.data_ptr(), Xd.data_ptr(), yd.data_ptr(),
-              Gd.data_ptr(), 96, C.c_float(0.8), C.c_float(1.2), ws.data_ptr(), loss.data_ptr(), None)
+              Gd.data_ptr(), None, 96, C.c_float(0.8), C.c_float(1.2), ws.data_ptr(), loss.data_ptr(), None)
     L, gref = M.loss_and_grad(p, X.astype(np.float64), ys.astype(np.float64), Gs.astype(np.float64), 0.8, 1.2)
     gk = grads.cpu().numpy()
     scale = np.abs(gref).max()
@@ -96,13 +96,30 @@ def test_bf16_inference_matches_fp64_network(scf):
     y, Gx, _ = M.forward(p, xh.T)
     phiH = -sp.GM / (r + sp.r_s)
     dphiH = sp.GM / (r + sp.r_s) ** 2
+    phi0, dphi0 = S.scf_l0(scf, r)
     ng = np.sum(n * Gx.T, axis=0)
     J = (rho / r) * (Gx.T - n * ng) + drho * n * ng
-    grad_ref = dphiH * (1 + y) * n + phiH * J
-    phi_ref = phiH * (1 + y)
+    grad_ref = (dphi0 + dphiH * y) * n + phiH * J
+    phi_ref = phi0 + phiH * y
     err = np.linalg.norm(grad.cpu().numpy() - grad_ref, axis=0) / np.linalg.norm(grad_ref, axis=0)
+    # weights are BF16 in the kernel, FP64 in the oracle; activations are hi + lo pairs
     assert np.median(err) < 1e-2, np.median(err)
-    np.testing.assert_allclose(phi.cpu().numpy(), phi_ref, rtol=2e-2)
+    # (an untrained network can make Phi cross zero, so compare on the global scale)
+    np.testing.assert_allclose(phi.cpu().numpy(), phi_ref, rtol=0, atol=1e-3 * np.abs(phi_ref).max())
+
+
+def test_spherical_base_matches_scf_monopole(scf, oracle):
+    """Phi_0 of the surrogate equals the l = 0 terms of the analytic SCF."""
+    S0 = np.zeros_like(scf.parameters["Snlm"])
+    S0[:, 0, 0] = scf.parameters["Snlm"][:, 0, 0]
+    mono = g.SCFPotential(m=scf.parameters["m"], r_s=scf.parameters["r_s"], Snlm=S0, Tnlm=np.zeros_like(S0))
+    r = np.geomspace(0.5, 200, 50)
+    q = np.vstack([r * 0.6, r * 0.0 + 1e-3, r * 0.8])
+    rr = np.linalg.norm(q, axis=0)
+    phi0, dphi0 = S.scf_l0(scf, rr)
+    np.testing.assert_allclose(phi0, oracle.energy(mono, q), rtol=1e-10)
+    gr = oracle.gradient(mono, q)
+    np.testing.assert_allclose(dphi0, np.sum(gr * q, axis=0) / rr, rtol=1e-8)
 
 
 def test_fallback_outside_trained_radii(scf, oracle):

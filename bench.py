@@ -62,6 +62,8 @@ def parse_args():
     p.add_argument("--no-autotune", action="store_true", help="use the cached or default launch shape")
     p.add_argument("--surrogate-steps", type=int, default=6000, help="training steps of the SCF surrogate")
     p.add_argument("--no-surrogate", action="store_true", help="skip the SCF surrogate variant")
+    p.add_argument("--surrogate-orbits", type=int, default=262_144)
+    p.add_argument("--surrogate-nsteps", type=int, default=5000)
     p.add_argument("--orbits", type=int, default=100_000)
     p.add_argument("--nsteps", type=int, default=10_000)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -265,7 +267,7 @@ def run_uneven_batch(args, torch, stream):
     return res
 
 
-def run_scf_surrogate(args, torch, stream, n_orbits=262_144, n_steps=5000):
+def run_scf_surrogate(args, torch, stream):
     """The SCF host: SCF(m=1e12, r_s=20, nmax=12, lmax=8) with random coefficients,
     262,144 orbits, dt = 1 Myr, 5,000 Leapfrog steps.  A surrogate is trained on
     16M analytic samples (timed separately), then the same FP32 leapfrog runs
@@ -278,6 +280,7 @@ def run_scf_surrogate(args, torch, stream, n_orbits=262_144, n_steps=5000):
     from gala_gb300 import surrogate as S
     from gala_gb300 import workloads as W
 
+    n_orbits, n_steps = args.surrogate_orbits, args.surrogate_nsteps
     scf = W.scf_potential()
     sp = S.SurrogatePotential(scf, seed=0)
     t0 = time.perf_counter()
@@ -306,13 +309,14 @@ def run_scf_surrogate(args, torch, stream, n_orbits=262_144, n_steps=5000):
         return e0.elapsed_time(e1) / reps, out
 
     ms_sur, (wsur, fb) = timed(lambda: sp.integrate_leapfrog(w0, 1.0, n_steps), 1)
-    ms_f32, _ = timed(lambda: sp.integrate_leapfrog(w0[:, :65536], 1.0, 200, analytic=True), 1)
+    n32 = min(65536, n_orbits)
+    ms_f32, _ = timed(lambda: sp.integrate_leapfrog(w0[:, :n32], 1.0, 200, analytic=True), 1)
     ms_f64, _ = timed(lambda: scf.integrate_orbit(w0, dt=1.0, n_steps=20, Integrator="leapfrog", save_all=False,
                                                   return_device=True), 1)
     v_sur = n_orbits * n_steps / (ms_sur * 1e-3)
-    v_f32 = 65536 * 200 / (ms_f32 * 1e-3)
+    v_f32 = n32 * 200 / (ms_f32 * 1e-3)
     v_f64 = n_orbits * 20 / (ms_f64 * 1e-3)
-    sub = w0[:, :2048]
+    sub = w0[:, :min(2048, n_orbits)]
     o64 = scf.integrate_orbit(sub, dt=1.0, n_steps=1000, Integrator="leapfrog", save_all=False).w().reshape(6, -1)
     osur = sp.integrate_leapfrog(sub, 1.0, 1000)[0].cpu().numpy()
     o32 = sp.integrate_leapfrog(sub, 1.0, 1000, analytic=True)[0].cpu().numpy()
@@ -331,7 +335,7 @@ def run_scf_surrogate(args, torch, stream, n_orbits=262_144, n_steps=5000):
         "fp32_surrogate": {"value": v_sur, "unit": UNIT, "ms_per_run": ms_sur,
                            "fallback_force_evaluations": int(fb.item()),
                            "tensor_core": "mma.sync m16n8k16 BF16, FP32 accumulate, activations BF16 hi+lo"},
-        "fp32_analytic_scf": {"value": v_f32, "unit": UNIT, "sample": "65,536 orbits x 200 steps"},
+        "fp32_analytic_scf": {"value": v_f32, "unit": UNIT, "sample": f"{n32} orbits x 200 steps"},
         "fp64_analytic_scf_plain": {"value": v_f64, "unit": UNIT, "sample": f"{n_orbits} orbits x 20 steps"},
         "speedup_surrogate_vs_fp64": v_sur / v_f64,
         "speedup_surrogate_vs_fp32_analytic": v_sur / v_f32,

@@ -63,6 +63,10 @@ class gx_frame(C.Structure):
     _fields_ = [("type", C.c_int32), ("reserved", C.c_int32), ("params", C.c_double * 3)]
 
 
+class gx_body(C.Structure):
+    _fields_ = [("type", C.c_int32), ("n_params", C.c_int32), ("params", C.c_double * 7)]
+
+
 _P = C.c_void_p
 _I64 = C.c_int64
 _I32 = C.c_int32
@@ -92,6 +96,11 @@ SIGNATURES = {
     "gx_surrogate_leapfrog": (C.c_int, [_P, _P, _P, _D, _D, _D, _D, _I32, _I32, _P, _I64, _I64, _D, _P, _P, _I32,
                                         _P]),
     "gx_surrogate_smem_bytes": (C.c_int, []),
+    "gx_nbody_dop853": (C.c_int, [_PP, _PF, _I64, _I32, _I32, _P, _P, _P, _I64, _D, _D, _I64, _D, _I64, _I32, _I64,
+                                  _P, _P, _P, _P, _P]),
+    "gx_mockstream_dop853": (C.c_int, [_PP, _PF, _I64, _I32, _P, _P, _I64, _P, _P, _I32, _P, _I64, _D, _D, _D, _D,
+                                       _I64, _P, _P, _P, _P, _P, _P]),
+    "gx_fardal_sample": (C.c_int, [_PP, _I64, _I64, _P, _I64, _P, _P, _P, _I64, _P, _D, _I32, _I32, _I32, _P, _P]),
     "gx_batch_integrate_fp64": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P]),
     "gx_dop853_integrate_hamiltonian": (
         C.c_int,

@@ -26,6 +26,7 @@ UNITS = {
     "gx_host.cu": ["-fmad=false"],
     "gx_fixed.cu": ["-fmad=false"],
     "gx_dop853.cu": ["-fmad=false"],
+    "gx_nbody.cu": ["-fmad=false"],
     "gx_peaks.cu": [],
     "gx_batch.cu": [],
     "gx_mlp_train.cu": [],

@@ -22,6 +22,8 @@ def as_device_f64(a, device=None) -> torch.Tensor:
     if isinstance(a, torch.Tensor):
         return a.to(device=dev, dtype=torch.float64).contiguous()
     arr = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    if not arr.flags.writeable:
+        arr = arr.copy()
     return torch.from_numpy(arr).to(dev)
 
 

@@ -1,0 +1,409 @@
+"""Mock stellar streams: gala's MockStreamGenerator and FardalStreamDF on the GPU.
+
+The generator follows gala's MockStreamGenerator.run
+(src/gala/dynamics/mockstream/mockstream_generator.py:119-372):
+
+1. the progenitor (plus optional massive bodies) is integrated over the time
+   grid as a DirectNBody system with DOPRI853 (gx_nbody_dop853);
+2. a stream distribution function samples release positions and velocities
+   around the progenitor at each release time (FardalStreamDF._sample,
+   df.pyx:363-457 -> gx_fardal_sample; the normal draws come from the DF's
+   numpy random state in gala's order);
+3. mockstream_dop853 (mockstream.pyx:176-303): the bodies are integrated again
+   on the release grid, then every release time's system [bodies, particles
+   released then] is integrated to the final time (gx_mockstream_dop853).
+
+``run`` makes one stream with gala's signature and return values.
+``run_batch`` makes many independent streams (one progenitor each, all on one
+time grid) in the same three launches; stream s consumes the DF's random draws
+after streams 0..s-1, as consecutive ``run`` calls with one DF would.
+"""
+from __future__ import annotations
+
+import warnings
+
+import numpy as np
+
+from . import _abi
+from .dynamics import PhaseSpacePosition
+from .hamiltonian import Hamiltonian, StaticFrame
+from .integrate import DOPRI853Integrator, get_integrator, parse_time_specification
+from .nbody import DirectNBody, bodies_to_device, integrate_systems, pack_bodies
+from .potential import PotentialBase
+
+__all__ = ["MockStream", "BaseStreamDF", "FardalStreamDF", "MockStreamGenerator", "MockStreamBatch"]
+
+
+class MockStream(PhaseSpacePosition):
+    """Stream particles with their release times and tails ('t' trailing, 'l'
+    leading) (src/gala/dynamics/mockstream/core.py:12-47)."""
+
+    def __init__(self, pos, vel=None, frame=None, release_time=None, lead_trail=None, copy=True):
+        super().__init__(pos=pos, vel=vel, frame=frame, copy=copy)
+        n = self.pos.shape[1] if self.pos.ndim > 1 else 1
+        if release_time is not None:
+            release_time = np.asarray(release_time, dtype=np.float64)
+            if len(release_time) != n:
+                raise ValueError("shape mismatch: input release time array must have the same shape as the input "
+                                 f"phase-space data, minus the component dimension. expected {n}, got "
+                                 f"{len(release_time)}")
+        self.release_time = release_time
+        if lead_trail is not None:
+            lead_trail = np.array(lead_trail)
+            if len(lead_trail) != n:
+                raise ValueError("shape mismatch: input leading/trailing array must have the same shape as the "
+                                 f"input phase-space data, minus the component dimension. expected {n}, got "
+                                 f"{len(lead_trail)}")
+        self.lead_trail = lead_trail
+
+
+class BaseStreamDF:
+    """Release distribution of stream particles (df.pyx:34-121)."""
+
+    def __init__(self, lead=True, trail=True, random_state=None):
+        self._lead = int(lead)
+        self._trail = int(trail)
+        if random_state is None:
+            random_state = np.random.RandomState()
+        self.random_state = random_state
+        if not self.lead and not self.trail:
+            raise ValueError("You must generate either leading or trailing tails (or both!)")
+
+    @property
+    def lead(self):
+        return self._lead
+
+    @property
+    def trail(self):
+        return self._trail
+
+    # -- layout of the released particles (df.pyx:194-231) ----------------------
+    def release_counts(self, ntimes, release_every=1, n_particles=1):
+        """Particles per tail at each time: ``n_particles`` every ``release_every``
+        steps, or a per-time array (BaseStreamDF.sample, df.pyx:197-207)."""
+        if np.iterable(n_particles):
+            n = np.array(n_particles).astype("i4")
+            if len(n) != ntimes:
+                raise ValueError("If passing in an array n_particles, its shape must match the number of timesteps "
+                                 "in the progenitor orbit.")
+            return n
+        n = np.zeros(ntimes, dtype="i4")
+        n[::release_every] = int(n_particles)
+        return n
+
+    def _draws(self, n_rows):
+        raise NotImplementedError
+
+
+class FardalStreamDF(BaseStreamDF):
+    """Fardal et al. (2015) release distribution with gala's parameters
+    (FardalStreamDF, df.pyx:300-457)."""
+
+    def __init__(self, gala_modified=None, lead=True, trail=True, random_state=None):
+        super().__init__(lead=lead, trail=trail, random_state=random_state)
+        if gala_modified is None:
+            warnings.warn(
+                "The parameter values of the FardalStreamDF have been updated (fixed) to match the parameter "
+                "values in the final published version of Fardal+2015. For now, this class uses the Gala modified "
+                "parameter values. To use the Fardal+2015 parameters now, set gala_modified=False. To continue to "
+                "use the Gala modified parameter values, set gala_modified=True.", FutureWarning)
+            gala_modified = True
+        self._gala_modified = int(gala_modified)
+
+    def _k(self):
+        """(k_mean, k_disp) of the four sampled quantities: R, z, v_t, v_z (df.pyx:390-405)."""
+        kvt_fardal = 0.4
+        mean = np.array([2.0, 0.0, 0.3, 0.0])
+        disp = np.array([0.5 if self._gala_modified else 0.4, 0.5,
+                         0.5 if self._gala_modified else kvt_fardal, 0.5])
+        return mean, disp
+
+    def _draws(self, n_rows):
+        """The four normal draws of n_rows particles, in gala's call order: per
+        particle kx, z, v_t, v_z (df.pyx:416-423).  One vectorised call with
+        per-element loc/scale consumes the random state exactly as the scalar
+        calls do."""
+        mean, disp = self._k()
+        if n_rows == 0:
+            return np.zeros((0, 4))
+        loc = np.tile(mean, n_rows)
+        scale = np.tile(disp, n_rows)
+        return np.asarray(self.random_state.normal(loc, scale), dtype=np.float64).reshape(n_rows, 4)
+
+    # -- sampling ---------------------------------------------------------------
+    def sample_device(self, potential, prog_w, prog_t, prog_m, counts, stream=None):
+        """Release states for n_streams progenitor orbits on one time grid.
+
+        prog_w : CUDA tensor (n_streams, ntimes, k >= 6): progenitor x, v first
+        prog_t : (ntimes,) float64; prog_m : (n_streams, ntimes)
+        counts : (ntimes,) particles per tail
+        Returns (w (n_streams, n_rows, 6) CUDA tensor, release_time (n_rows,),
+        lead_trail (n_rows,), offset (ntimes + 1,) int64).
+        """
+        import torch
+
+        from ._device import as_device_f64, ptr, stream_handle
+
+        ns, ntimes = int(prog_w.shape[0]), int(prog_w.shape[1])
+        ntail = self._lead + self._trail
+        counts = np.asarray(counts, dtype=np.int64)
+        offset = np.concatenate([[0], np.cumsum(ntail * counts)]).astype(np.int64)
+        n_rows = int(offset[-1])
+        prog_m = np.broadcast_to(np.asarray(prog_m, dtype=np.float64), (ns, ntimes))
+        if np.any((counts > 0)[None, :] & (prog_m == 0)):
+            raise NotImplementedError("a zero progenitor mass at a release time is not supported")
+        draws = np.stack([self._draws(n_rows) for _ in range(ns)]) if ns else np.zeros((0, n_rows, 4))
+        dev = prog_w.device
+        out = torch.empty((ns, n_rows, 6), dtype=torch.float64, device=dev)
+        pw = prog_w.contiguous()
+        dd = as_device_f64(draws, dev)
+        md = as_device_f64(np.ascontiguousarray(prog_m), dev)
+        td = as_device_f64(prog_t, dev)
+        od = torch.from_numpy(offset).to(dev)
+        _abi.call("gx_fardal_sample", potential.packed().for_device(), ns, ntimes, ptr(pw), int(pw.shape[2]),
+                  ptr(md), ptr(td), ptr(od), n_rows, ptr(dd), float(potential.G), self._lead, self._trail,
+                  self._gala_modified, ptr(out), stream_handle(stream))
+        release_time = np.repeat(np.asarray(prog_t, dtype=np.float64), ntail * counts)
+        lt = []
+        for n in counts:
+            if self._trail:
+                lt += ["t"] * int(n)
+            if self._lead:
+                lt += ["l"] * int(n)
+        return out, release_time, np.array(lt, dtype="U1"), offset
+
+    def sample(self, prog_orbit, prog_mass, hamiltonian=None, release_every=1, n_particles=1):
+        """Stream initial conditions around a progenitor orbit (df.pyx:125-242)."""
+        from ._device import as_device_f64, require_cuda
+
+        if getattr(prog_orbit, "hamiltonian", None) is not None:
+            H = prog_orbit.hamiltonian
+        elif hamiltonian is not None:
+            H = hamiltonian if isinstance(hamiltonian, Hamiltonian) else Hamiltonian(hamiltonian)
+        else:
+            raise ValueError("a Hamiltonian is needed to sample stream particles")
+        if not isinstance(H.frame, StaticFrame):
+            raise NotImplementedError("stream sampling is implemented for a static frame")
+        x = np.asarray(prog_orbit.xyz, dtype=np.float64)
+        v = np.asarray(prog_orbit.v_xyz, dtype=np.float64)
+        t = np.asarray(prog_orbit.t, dtype=np.float64)
+        ntimes = len(t)
+        prog_w = np.ascontiguousarray(np.vstack([x, v]).T.reshape(1, ntimes, 6))
+        m = np.squeeze(np.asarray(getattr(prog_mass, "value", prog_mass), dtype=np.float64))
+        m = np.full(ntimes, float(m)) if m.shape == () else m
+        counts = self.release_counts(ntimes, release_every, n_particles)
+        dev = require_cuda()
+        w, rt, lt, _ = self.sample_device(H.potential, as_device_f64(prog_w, dev), t, m[None, :], counts)
+        w = w[0].cpu().numpy()
+        return MockStream(pos=w[:, :3].T, vel=w[:, 3:].T, frame=H.frame, release_time=rt, lead_trail=lt)
+
+
+class MockStreamBatch:
+    """Result of MockStreamGenerator.run_batch: device tensors for many streams.
+
+    stream_w     (n_streams, n_particles, 6) particles at the final time
+    nbody_w      (n_streams, nbodies, 6) bodies at the final time
+    release_time (n_particles,), lead_trail (n_particles,)
+    status       (n_streams, n_release) dop853() code of each release system
+    stats        (n_streams, n_release, 4) or None: nfcn, nstep, naccpt, nrejct
+    """
+
+    def __init__(self, stream_w, nbody_w, release_time, lead_trail, status, stats, frame, t):
+        self.stream_w = stream_w
+        self.nbody_w = nbody_w
+        self.release_time = release_time
+        self.lead_trail = lead_trail
+        self.status = status
+        self.stats = stats
+        self.frame = frame
+        self.t = t
+
+    @property
+    def n_streams(self):
+        return int(self.stream_w.shape[0])
+
+    def stream(self, s):
+        w = self.stream_w[s].cpu().numpy()
+        return MockStream(pos=w[:, :3].T, vel=w[:, 3:].T, frame=self.frame, release_time=self.release_time,
+                          lead_trail=self.lead_trail)
+
+    def nbody(self, s):
+        w = self.nbody_w[s].cpu().numpy()
+        return PhaseSpacePosition(pos=w[:, :3].T, vel=w[:, 3:].T, frame=self.frame)
+
+
+class MockStreamGenerator:
+    """Generate mock streams with a release DF in a Hamiltonian
+    (src/gala/dynamics/mockstream/mockstream_generator.py:20-118)."""
+
+    def __init__(self, df, hamiltonian, progenitor_potential=None):
+        if not isinstance(df, BaseStreamDF):
+            raise TypeError("The input distribution function (DF) instance must be a BaseStreamDF subclass "
+                            f"instance, not {type(df)}")
+        self.df = df
+        self.hamiltonian = hamiltonian if isinstance(hamiltonian, Hamiltonian) else Hamiltonian(hamiltonian)
+        if progenitor_potential is not None and not isinstance(progenitor_potential, PotentialBase):
+            raise TypeError("If specified, the progenitor_potential must be a potential class instance.")
+        self.self_gravity = progenitor_potential is not None
+        self.progenitor_potential = progenitor_potential
+
+    def _get_nbody(self, prog_w0, nbody):
+        """The progenitor plus optional extra bodies as one DirectNBody (:76-117)."""
+        if nbody is not None:
+            if nbody.external_potential is not self.hamiltonian.potential:
+                raise ValueError("The external potential of the input nbody instance must match the potential of "
+                                 "the mock stream input hamiltonian!")
+            w0 = PhaseSpacePosition(
+                pos=np.column_stack([np.reshape(prog_w0.xyz, (3, 1)), np.reshape(nbody.w0.xyz, (3, -1))]),
+                vel=np.column_stack([np.reshape(prog_w0.v_xyz, (3, 1)), np.reshape(nbody.w0.v_xyz, (3, -1))]))
+            pps = [self.progenitor_potential, *nbody.particle_potentials]
+        else:
+            w0 = prog_w0
+            pps = [self.progenitor_potential]
+        return DirectNBody(w0=w0, particle_potentials=pps, external_potential=self.hamiltonian.potential,
+                           frame=self.hamiltonian.frame)
+
+    @staticmethod
+    def _dop_kwargs(Integrator_kwargs):
+        kw = dict(Integrator_kwargs or {})
+        err_if_fail = int(kw.pop("err_if_fail", 1))
+        kw.pop("log_output", None)
+        kw.pop("progress", None)
+        extra = set(kw) - {"atol", "rtol", "nmax", "dt_max"}
+        if extra:
+            raise TypeError(f"unexpected Integrator_kwargs {sorted(extra)}")
+        return dict(atol=float(kw.get("atol", 1e-10)), rtol=float(kw.get("rtol", 1e-10)),
+                    nmax=int(kw.get("nmax", 0)), dt_max=float(kw.get("dt_max", 0.0))), err_if_fail
+
+    def _generate(self, bodies, body_w0, prog_m, t, counts, dop, err_if_fail, return_stats=False, stream=None):
+        """The three stages for n_streams systems.
+
+        bodies  : BODY_DTYPE (S, nb), progenitor first, massive bodies before null ones
+        body_w0 : (S, nb, 6) bodies at t[0]
+        prog_m  : (S, ntimes) progenitor mass along the orbit grid (increasing time)
+        counts  : (ntimes,) particles per tail on the orbit grid
+        """
+        import torch
+
+        from ._device import ptr, require_cuda, stream_handle
+
+        H = self.hamiltonian
+        if not isinstance(H.frame, StaticFrame):
+            raise NotImplementedError("mock streams are implemented for a static frame")
+        dev = require_cuda()
+        S, nb = bodies.shape
+        if nb > 31:
+            raise NotImplementedError("at most 31 massive bodies per stream on the GPU")
+
+        def check(status, what):
+            res = status.cpu().numpy().ravel()
+            bad = res[res < 0]
+            if bad.size and err_if_fail == 1:
+                raise RuntimeError(f"Integration failed with code {int(bad[0])}")
+
+        # 1. the bodies over the requested grid (DirectNBody.integrate_orbit)
+        orbit, st = integrate_systems(H, bodies, body_w0, t, save_all=True, nstiff=-1, stream=stream, **dop)
+        check(st, "nbody")
+        forward = not (t[1] < t[0])
+        if forward:
+            orbit_t = t
+            nbody0 = torch.as_tensor(body_w0, dtype=torch.float64, device=dev)
+        else:  # the grid runs backwards: the stream is made forwards from the past (:237-250)
+            orbit = torch.flip(orbit, dims=[1])
+            orbit_t = t[::-1].copy()
+            nbody0 = orbit[:, 0].contiguous()
+
+        # 2. release states from the progenitor orbit (body 0)
+        prog_w = orbit.reshape(S, len(orbit_t), nb * 6)
+        stream_w0, release_time, lead_trail, _ = self.df.sample_device(H.potential, prog_w, orbit_t, prog_m, counts,
+                                                                     stream=stream)
+        ntail = self.df.lead + self.df.trail
+
+        # 3. release grid: times that release particles, plus the first (:271-283)
+        rel_idx = np.nonzero(counts > 0)[0]
+        if 0 not in rel_idx:
+            rel_idx = np.insert(rel_idx, 0, 0)
+        time = np.ascontiguousarray(orbit_t[rel_idx])
+        nstream = (ntail * counts[rel_idx]).astype(np.int64)
+        rel_off = np.concatenate([[0], np.cumsum(nstream)]).astype(np.int64)
+        n_rows = int(rel_off[-1])
+        if forward and len(rel_idx) == len(orbit_t):
+            nbody_w = orbit  # the same dop853_helper call on the same grid (mockstream.pyx:245-255)
+        else:
+            nbody_w, st = integrate_systems(H, bodies, nbody0, time, save_all=True, nstiff=-1, stream=stream,
+                                            **dop)
+            check(st, "nbody")
+        max_per = int(nstream.max()) if nstream.size else 0
+        if nb + max_per > 32:
+            raise NotImplementedError(f"{nb} bodies + {max_per} particles per release exceed the 32-lane system")
+        n_rel = len(time)
+        stream_out = torch.empty((S, n_rows, 6), dtype=torch.float64, device=dev)
+        nbody_out = torch.empty((S, nb, 6), dtype=torch.float64, device=dev)
+        status = torch.zeros((S, n_rel), dtype=torch.int32, device=dev)
+        stats = torch.zeros((S, n_rel, 4), dtype=torch.int64, device=dev) if return_stats else None
+        counter = torch.zeros(1, dtype=torch.int64, device=dev)
+        bd = bodies_to_device(bodies, dev)
+        td = torch.from_numpy(time).to(dev)
+        od = torch.from_numpy(rel_off).to(dev)
+        _abi.call("gx_mockstream_dop853", H.potential.packed().for_device(), H._frame_ref(), S, nb, ptr(bd),
+                  ptr(nbody_w), n_rel, ptr(td), ptr(od), max_per, ptr(stream_w0), n_rows, float(orbit_t[-1]),
+                  float(time[1] - time[0]), dop["atol"], dop["rtol"], dop["nmax"], ptr(stream_out), ptr(nbody_out),
+                  ptr(status), ptr(stats) if stats is not None else None, ptr(counter), stream_handle(stream))
+        check(status, "stream")
+        return MockStreamBatch(stream_out, nbody_out, release_time, lead_trail, status, stats, H.frame, orbit_t)
+
+    def run(self, prog_w0, prog_mass, nbody=None, release_every=1, n_particles=1, output_every=None,
+            output_filename=None, check_filesize=True, overwrite=False, progress=False, Integrator=None,
+            Integrator_kwargs=None, **time_spec):
+        """One mock stream; returns (stream MockStream, nbody PhaseSpacePosition) (:119-372)."""
+        Integrator = get_integrator(DOPRI853Integrator if Integrator is None else Integrator)
+        if Integrator is not DOPRI853Integrator:
+            raise NotImplementedError("GPU mock streams are implemented for DOPRI853Integrator")
+        if output_every is not None:
+            raise NotImplementedError("snapshot output (output_every / HDF5) is not implemented")
+        t = np.ascontiguousarray(parse_time_specification(self.hamiltonian.units, **time_spec), dtype=np.float64)
+        prog_nbody = self._get_nbody(prog_w0, nbody)
+        idx, n_massive = prog_nbody._order()
+        if not np.array_equal(idx, np.arange(len(idx))):
+            raise NotImplementedError("null-potential bodies must come after the massive ones")
+        nb = len(prog_nbody.particle_potentials)
+        bodies = pack_bodies([prog_nbody.particle_potentials])
+        m = np.squeeze(np.asarray(getattr(prog_mass, "value", prog_mass), dtype=np.float64))
+        m = np.full(len(t), float(m)) if m.shape == () else m
+        counts = self.df.release_counts(len(t), release_every, n_particles)
+        dop, err_if_fail = self._dop_kwargs(Integrator_kwargs)
+        res = self._generate(bodies, prog_nbody._c_w0.reshape(1, nb, 6), m[None, :], t, counts, dop, err_if_fail)
+        return res.stream(0), res.nbody(0)
+
+    def run_batch(self, prog_w0, prog_mass, progenitor_potentials=None, release_every=1, n_particles=1,
+                  Integrator_kwargs=None, return_stats=False, stream=None, **time_spec):
+        """Many independent streams on one time grid (no extra bodies).
+
+        prog_w0  : (6, S) progenitor phase-space positions (numpy)
+        prog_mass: (S,) or (S, ntimes) masses passed to the DF
+        progenitor_potentials : list of S potentials (or None: the generator's
+                   progenitor_potential for every stream)
+        Returns a MockStreamBatch of device tensors.
+        """
+        t = np.ascontiguousarray(parse_time_specification(self.hamiltonian.units, **time_spec), dtype=np.float64)
+        w0 = np.asarray(prog_w0, dtype=np.float64)
+        if w0.ndim != 2 or w0.shape[0] != 6:
+            raise ValueError(f"prog_w0 must have shape (6, n_streams), got {w0.shape}")
+        S = w0.shape[1]
+        if progenitor_potentials is None:
+            progenitor_potentials = [self.progenitor_potential] * S
+        if len(progenitor_potentials) != S:
+            raise ValueError("one progenitor potential per stream is needed")
+        bodies = pack_bodies([[p] for p in progenitor_potentials]).reshape(S, 1)
+        m = np.asarray(prog_mass, dtype=np.float64)
+        if m.ndim == 0:
+            m = np.full((S, len(t)), float(m))
+        elif m.ndim == 1:
+            if m.shape[0] != S:
+                raise ValueError("prog_mass must have one entry per stream")
+            m = np.repeat(m[:, None], len(t), axis=1)
+        counts = self.df.release_counts(len(t), release_every, n_particles)
+        dop, err_if_fail = self._dop_kwargs(Integrator_kwargs)
+        body_w0 = np.ascontiguousarray(w0.T.reshape(S, 1, 6))
+        return self._generate(bodies, body_w0, m, t, counts, dop, err_if_fail, return_stats=return_stats,
+                              stream=stream)

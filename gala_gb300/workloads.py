@@ -123,3 +123,20 @@ def scf_ics(n=262_144, seed=SEED_BASE + 5, m=1e12, r_s=20.0):
     vc = np.sqrt(G * m * r / (r + r_s) ** 2)
     v = vc * that * (1.0 + rng.normal(0.0, 0.1, size=(3, n)))
     return np.ascontiguousarray(np.vstack([r * rhat, v]))
+
+
+def stream_progenitors(n=512, seed=SEED_BASE + 6):
+    """Mock-stream progenitors: phase-space positions drawn as mw_ics, Plummer
+    masses m ~ U[1e4, 1e6] Msun and scale radii b ~ U[5, 20] pc.
+    Returns (w0 (6, n), m (n,), b (n,) in kpc)."""
+    rng = np.random.default_rng(seed)
+    w0 = mw_ics(n, seed=seed + 100)
+    m = rng.uniform(1e4, 1e6, n)
+    b = rng.uniform(5e-3, 20e-3, n)
+    return w0, m, b
+
+
+def stream_progenitor_potentials(m, b):
+    from .potential import PlummerPotential
+
+    return [PlummerPotential(m=float(mi), b=float(bi)) for mi, bi in zip(m, b)]

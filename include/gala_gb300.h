@@ -108,6 +108,17 @@ typedef struct gx_frame {
     double params[3];
 } gx_frame;
 
+/* Potential of one massive body of an n-body system: gala's particle potentials
+ * of DirectNBody / MockStreamGenerator (src/gala/dynamics/nbody/core.py,
+ * mockstream.pyx:49-78).  One unrotated component, shifted by the integrator to
+ * the body's position (c_nbody_acceleration, cpotential.cpp:389-415); a body of
+ * type GX_POT_NULL exerts no force (gala's NullPotential, `null == 1`). */
+typedef struct gx_body {
+    int32_t type;        /* gx_potential_type of the single component             */
+    int32_t n_params;    /* entries of params in use: [G, p1, p2, ...]            */
+    double params[7];
+} gx_body;               /* 64 bytes */
+
 /* ------------------------------------------------------------------------- */
 /* Library                                                                   */
 /* ------------------------------------------------------------------------- */
@@ -302,6 +313,92 @@ int gx_surrogate_smem_bytes(void);
 /* ------------------------------------------------------------------------- */
 int gx_calibrate_fma(int32_t fp64, int32_t blocks, int32_t threads, int64_t iters,
                      void* sink, void* stream);
+
+/* ------------------------------------------------------------------------- */
+/* Direct n-body systems and mock streams                                    */
+/* ------------------------------------------------------------------------- */
+
+/* DirectNBody.integrate_orbit with DOPRI853 (src/gala/dynamics/nbody/core.py:
+ * 166-260 -> direct_nbody_dop853, nbody.pyx:30-115), for n_systems independent
+ * systems at once.  Each system is one gala call: dop853_helper
+ * (dop853.pyx:90-193) with Fwrapper_direct_nbody (dop853.cpp:990-1006) on
+ * nparticles bodies, the first `nbody` of them massive, uround = eps,
+ * h0 = t[1] - t[0], one step size and error norm per system.
+ *   bodies  DEVICE gx_body (n_systems, nbody): the massive bodies' potentials
+ *           (types NULL, KEPLER, HERNQUIST, PLUMMER, MIYAMOTONAGAI,
+ *           SPHERICALNFW; any other type yields NaN forces)
+ *   w0      DEVICE (n_systems, nparticles, 6): gala's (nparticles, 6) per system
+ *   t       DEVICE (ntimes)
+ *   nstiff  gala passes -1 (no stiffness test)
+ *   w_out   DEVICE (n_systems, n_out, nparticles, 6) with n_out =
+ *           (ntimes - 1) / out_stride + 1 if save_all, else (n_systems,
+ *           nparticles, 6)
+ *   status  DEVICE int32 (n_systems): gala's dop853() code per system
+ *   stats   DEVICE int64 (n_systems, 4) or NULL: nfcn, nstep, naccpt, nrejct
+ *   queue_counter  DEVICE int64 scratch (zeroed by the call)
+ * 1 <= nparticles <= 32. */
+int gx_nbody_dop853(const gx_potential* pot, const gx_frame* frame, int64_t n_systems,
+                    int32_t nparticles, int32_t nbody, const gx_body* bodies,
+                    const double* w0, const double* t, int64_t ntimes, double atol,
+                    double rtol, int64_t nmax, double dt_max, int64_t nstiff,
+                    int32_t save_all, int64_t out_stride, double* w_out, int32_t* status,
+                    int64_t* stats, int64_t* queue_counter, void* stream);
+
+/* The release systems of mockstream_dop853 (src/gala/dynamics/mockstream/
+ * mockstream.pyx:176-303) for n_streams progenitor systems that share one
+ * release grid.  For stream s and release i with particles, one dop853_step
+ * call (dop853.pyx:27-75: uround 2.3e-16, nstiff 1, hmax = t_final - t_i,
+ * h0 = dt0, no dense output) integrates [the nbody bodies at release i, the
+ * particles released at i] from release_t[i] to t_final.
+ *   bodies          DEVICE gx_body (n_streams, nbody): progenitor first
+ *   nbody_w         DEVICE (n_streams, n_release, nbody, 6): the bodies at each
+ *                   release time (gala's nbody dense output on the release grid)
+ *   release_t       DEVICE (n_release): gala's stream_t1
+ *   release_offset  DEVICE int64 (n_release + 1): prefix sums of gala's nstream;
+ *                   the particles of release i are rows
+ *                   [release_offset[i], release_offset[i+1]) of a stream, and
+ *                   release_offset[n_release] == n_particles (a release whose
+ *                   rows fall outside [0, n_particles) or exceed max_per_release
+ *                   is not integrated and gets status -1)
+ *   max_per_release largest nstream[i]; nbody + max_per_release <= 32
+ *   stream_w0       DEVICE (n_streams, n_particles, 6), gala's stream_w0 per stream
+ *   dt0             gala's time[1] - time[0] of the release grid
+ *   stream_w_out    DEVICE (n_streams, n_particles, 6): the particles at t_final
+ *   nbody_w_out     DEVICE (n_streams, nbody, 6) or NULL: the bodies as the last
+ *                   release system leaves them (gala's return_nbody_w)
+ *   status          DEVICE int32 (n_streams, n_release): dop853() code of each
+ *                   release system, 0 where nothing was released (a NaN step
+ *                   size ends a system at once with gala's eventual code, -2)
+ *   stats           DEVICE int64 (n_streams, n_release, 4) or NULL
+ *   queue_counter   DEVICE int64 scratch (zeroed by the call) */
+int gx_mockstream_dop853(const gx_potential* pot, const gx_frame* frame, int64_t n_streams,
+                         int32_t nbody, const gx_body* bodies, const double* nbody_w,
+                         int64_t n_release, const double* release_t,
+                         const int64_t* release_offset, int32_t max_per_release,
+                         const double* stream_w0, int64_t n_particles, double t_final,
+                         double dt0, double atol, double rtol, int64_t nmax,
+                         double* stream_w_out, double* nbody_w_out, int32_t* status,
+                         int64_t* stats, int64_t* queue_counter, void* stream);
+
+/* FardalStreamDF._sample (src/gala/dynamics/mockstream/df.pyx:363-457) with
+ * get_rj_vj_R (:61-92) and transform_from_sat (:94-106) for n_streams
+ * progenitor orbits on one time grid; the Jacobi radius uses c_d2_dr2
+ * (cpotential.cpp:346-371) of `pot`.
+ *   prog_w          DEVICE (n_streams, ntimes, row_stride): progenitor x, v in
+ *                   the first six entries of each row
+ *   prog_m          DEVICE (n_streams, ntimes): progenitor mass
+ *   t               DEVICE (ntimes)
+ *   release_offset  DEVICE int64 (ntimes + 1): first particle row of each time;
+ *                   a time releases (lead + trail) * n_i rows, trailing first
+ *   draws           DEVICE (n_streams, n_particles, 4): the four normal draws of
+ *                   each particle (kx, kz, kvt, kvz) in gala's order
+ *   G               the gravitational constant of `pot`
+ *   w_out           DEVICE (n_streams, n_particles, 6) */
+int gx_fardal_sample(const gx_potential* pot, int64_t n_streams, int64_t ntimes,
+                     const double* prog_w, int64_t row_stride, const double* prog_m,
+                     const double* t, const int64_t* release_offset, int64_t n_particles,
+                     const double* draws, double G, int32_t lead, int32_t trail,
+                     int32_t gala_modified, double* w_out, void* stream);
 
 #ifdef __cplusplus
 }

@@ -506,6 +506,12 @@ static double sign_d(double a, double b) { return (b < 0.0) ? -fabs(a) : fabs(a)
 static double min_d(double a, double b) { return (a < b) ? a : b; }
 static double max_d(double a, double b) { return (a > b) ? a : b; }
 
+/* Right-hand side of a DOP853 system: f = F(y) for the system's state y. */
+typedef struct {
+    void (*fn)(const void *ctx, const double *y, double *f);
+    const void *ctx;
+} rhs_t;
+
 /* Fwrapper_T on a batch held as y[6 * nb] in SoA order (component k of orbit j
  * at k * nb + j), as dop853_helper lays it out (dop853.pyx:135-136, 157-182). */
 static void batch_rhs(const gx_potential *pot, const gx_frame *fr, int nb, const double *y, double *f) {
@@ -517,11 +523,21 @@ static void batch_rhs(const gx_potential *pot, const gx_frame *fr, int nb, const
     }
 }
 
+typedef struct {
+    const gx_potential *pot;
+    const gx_frame *fr;
+    int nb;
+} batch_ctx;
+
+static void batch_rhs_cb(const void *vctx, const double *y, double *f) {
+    const batch_ctx *c = (const batch_ctx *)vctx;
+    batch_rhs(c->pot, c->fr, c->nb, y, f);
+}
+
 /* hinit (:18-86), scalar tolerances. */
-static double orc_hinit(const gx_potential *pot, const gx_frame *fr, int nb, double x, const double *y,
+static double orc_hinit(rhs_t R, int n, double x, const double *y,
                         double posneg, const double *f0, double *f1, double *yy1, int iord,
                         double hmax, double atoli, double rtoli) {
-    const int n = 6 * nb;
     double dnf = 0.0, dny = 0.0, sk, sqr, h, h1, der2, der12;
     for (int i = 0; i < n; i++) {
         sk = atoli + rtoli * fabs(y[i]);
@@ -537,7 +553,7 @@ static double orc_hinit(const gx_potential *pot, const gx_frame *fr, int nb, dou
     h = min_d(h, hmax);
     h = sign_d(h, posneg);
     for (int i = 0; i < n; i++) yy1[i] = y[i] + h * f0[i];
-    batch_rhs(pot, fr, nb, yy1, f1);
+    R.fn(R.ctx, yy1, f1);
     (void)x;
     der2 = 0.0;
     for (int i = 0; i < n; i++) {
@@ -555,25 +571,28 @@ static double orc_hinit(const gx_potential *pot, const gx_frame *fr, int nb, dou
     return sign_d(h, posneg);
 }
 
-/* One dop853() call on one batch (dopcor :89-650 with the front-end defaults of
- * :653-866 and dop853_helper's arguments, dop853.pyx:157-182).
- *   y     : (6*nb) in/out state
- *   out   : if non-NULL, dense output (n_out, 6*nb) at t[0], t[stride], ...
- *   stats : if non-NULL, {nfcn, nstep, naccpt, nrejct}
+/* One dop853() call (dopcor :89-650 with the front-end defaults of :653-866)
+ * on a system of n components with right-hand side R.
+ *   y       : (n) in/out state
+ *   out     : if non-NULL, dense output (n_out, n) at t[0], t[stride], ... up to
+ *             t[ntimes-1] (xend); x starts at t[0]
+ *   x0,xend : used instead of t[0], t[ntimes-1] when out is NULL and t is NULL
+ *   uround  : gala passes np.finfo(float).eps from dop853_helper and 0 (the
+ *             front-end default 2.3e-16) from dop853_step
+ *   stats   : if non-NULL, {nfcn, nstep, naccpt, nrejct}
  * Returns gala's idid: 1 on success, -2 / -3 / -4 on failure. */
-int orc_dop853_batch(const gx_potential *pot, const gx_frame *fr, int nb, double *y,
-                     const double *t, int64_t ntimes, double atol, double rtol, int64_t nmax,
-                     double dt_max, int64_t nstiff, int64_t out_stride, double *out, long *stats) {
-    const int n = 6 * nb;
-    double x = t[0];
-    const double xend = t[ntimes - 1];
-    double h = t[1] - t[0];
+static int orc_dop853_core(rhs_t R, int n, double *y, const double *t, int64_t ntimes, double x0, double xend_in,
+                           double h0, double atol, double rtol, int64_t nmax, double dt_max, int64_t nstiff,
+                           double uround, int64_t out_stride, double *out, long *stats) {
+    double x = t ? t[0] : x0;
+    const double xend = t ? t[ntimes - 1] : xend_in;
+    double h = h0;
     double hmax = dt_max;
-    const double uround = 2.220446049250313e-16; /* np.finfo(float).eps, dop853.pyx:165 */
     const double safe = 0.9, fac1 = 0.333, fac2 = 6.0, beta = 0.0;
     if (!nmax) nmax = 1000000;
     if (!nstiff) nstiff = 1000;
     else if (nstiff < 0) nstiff = nmax + 10;
+    if (uround == 0.0) uround = 2.3E-16;
     if (hmax == 0.0) hmax = xend - x;
 
     double *work = (double *)malloc(sizeof(double) * (size_t)n * 19);
@@ -594,10 +613,10 @@ int orc_dop853_batch(const gx_potential *pot, const gx_frame *fr, int nb, double
     int64_t out_idx = 0; /* index into t of the next output time */
     int64_t out_slot = 0;
 
-    batch_rhs(pot, fr, nb, y, k1);
+    R.fn(R.ctx, y, k1);
     hmax = fabs(hmax);
     const int iord = 8;
-    if (h == 0.0) h = orc_hinit(pot, fr, nb, x, y, posneg, k1, k2, k3, iord, hmax, atoli, rtoli);
+    if (h == 0.0) h = orc_hinit(R, n, x, y, posneg, k1, k2, k3, iord, hmax, atoli, rtoli);
     nfcn += 2;
 
     for (;;) {
@@ -612,39 +631,39 @@ int orc_dop853_batch(const gx_potential *pot, const gx_frame *fr, int nb, double
         nstep++;
 
         for (int i = 0; i < n; i++) yy1[i] = y[i] + h * a21 * k1[i];
-        batch_rhs(pot, fr, nb, yy1, k2);
+        R.fn(R.ctx, yy1, k2);
         for (int i = 0; i < n; i++) yy1[i] = y[i] + h * (a31 * k1[i] + a32 * k2[i]);
-        batch_rhs(pot, fr, nb, yy1, k3);
+        R.fn(R.ctx, yy1, k3);
         for (int i = 0; i < n; i++) yy1[i] = y[i] + h * (a41 * k1[i] + a43 * k3[i]);
-        batch_rhs(pot, fr, nb, yy1, k4);
+        R.fn(R.ctx, yy1, k4);
         for (int i = 0; i < n; i++) yy1[i] = y[i] + h * (a51 * k1[i] + a53 * k3[i] + a54 * k4[i]);
-        batch_rhs(pot, fr, nb, yy1, k5);
+        R.fn(R.ctx, yy1, k5);
         for (int i = 0; i < n; i++) yy1[i] = y[i] + h * (a61 * k1[i] + a64 * k4[i] + a65 * k5[i]);
-        batch_rhs(pot, fr, nb, yy1, k6);
+        R.fn(R.ctx, yy1, k6);
         for (int i = 0; i < n; i++)
             yy1[i] = y[i] + h * (a71 * k1[i] + a74 * k4[i] + a75 * k5[i] + a76 * k6[i]);
-        batch_rhs(pot, fr, nb, yy1, k7);
+        R.fn(R.ctx, yy1, k7);
         for (int i = 0; i < n; i++)
             yy1[i] = y[i] + h * (a81 * k1[i] + a84 * k4[i] + a85 * k5[i] + a86 * k6[i] + a87 * k7[i]);
-        batch_rhs(pot, fr, nb, yy1, k8);
+        R.fn(R.ctx, yy1, k8);
         for (int i = 0; i < n; i++)
             yy1[i] = y[i] + h * (a91 * k1[i] + a94 * k4[i] + a95 * k5[i] + a96 * k6[i] + a97 * k7[i] +
                                  a98 * k8[i]);
-        batch_rhs(pot, fr, nb, yy1, k9);
+        R.fn(R.ctx, yy1, k9);
         for (int i = 0; i < n; i++)
             yy1[i] = y[i] + h * (a101 * k1[i] + a104 * k4[i] + a105 * k5[i] + a106 * k6[i] +
                                  a107 * k7[i] + a108 * k8[i] + a109 * k9[i]);
-        batch_rhs(pot, fr, nb, yy1, k10);
+        R.fn(R.ctx, yy1, k10);
         for (int i = 0; i < n; i++)
             yy1[i] = y[i] + h * (a111 * k1[i] + a114 * k4[i] + a115 * k5[i] + a116 * k6[i] +
                                  a117 * k7[i] + a118 * k8[i] + a119 * k9[i] + a1110 * k10[i]);
-        batch_rhs(pot, fr, nb, yy1, k2);
+        R.fn(R.ctx, yy1, k2);
         const double xph = x + h;
         for (int i = 0; i < n; i++)
             yy1[i] = y[i] + h * (a121 * k1[i] + a124 * k4[i] + a125 * k5[i] + a126 * k6[i] +
                                  a127 * k7[i] + a128 * k8[i] + a129 * k9[i] + a1210 * k10[i] +
                                  a1211 * k2[i]);
-        batch_rhs(pot, fr, nb, yy1, k3);
+        R.fn(R.ctx, yy1, k3);
         nfcn += 11;
         for (int i = 0; i < n; i++) {
             k4[i] = b1 * k1[i] + b6 * k6[i] + b7 * k7[i] + b8 * k8[i] + b9 * k9[i] + b10 * k10[i] +
@@ -677,7 +696,7 @@ int orc_dop853_batch(const gx_potential *pot, const gx_frame *fr, int nb, double
         if (err <= 1.0) {
             facold = max_d(err, 1.0E-4);
             naccpt++;
-            batch_rhs(pot, fr, nb, k5, k4);
+            R.fn(R.ctx, k5, k4);
             nfcn++;
 
             /* stiffness detection (:463-486); gala returns -4 on the first
@@ -723,15 +742,15 @@ int orc_dop853_batch(const gx_potential *pot, const gx_frame *fr, int nb, double
                 for (int i = 0; i < n; i++)
                     yy1[i] = y[i] + h * (a141 * k1[i] + a147 * k7[i] + a148 * k8[i] + a149 * k9[i] +
                                          a1410 * k10[i] + a1411 * k2[i] + a1412 * k3[i] + a1413 * k4[i]);
-                batch_rhs(pot, fr, nb, yy1, k10);
+                R.fn(R.ctx, yy1, k10);
                 for (int i = 0; i < n; i++)
                     yy1[i] = y[i] + h * (a151 * k1[i] + a156 * k6[i] + a157 * k7[i] + a158 * k8[i] +
                                          a1511 * k2[i] + a1512 * k3[i] + a1513 * k4[i] + a1514 * k10[i]);
-                batch_rhs(pot, fr, nb, yy1, k2);
+                R.fn(R.ctx, yy1, k2);
                 for (int i = 0; i < n; i++)
                     yy1[i] = y[i] + h * (a161 * k1[i] + a166 * k6[i] + a167 * k7[i] + a168 * k8[i] +
                                          a169 * k9[i] + a1613 * k4[i] + a1614 * k10[i] + a1615 * k2[i]);
-                batch_rhs(pot, fr, nb, yy1, k3);
+                R.fn(R.ctx, yy1, k3);
                 nfcn += 3;
                 for (int i = 0; i < n; i++) {
                     rc5[i] = h * (rc5[i] + d413 * k4[i] + d414 * k10[i] + d415 * k2[i] + d416 * k3[i]);
@@ -788,6 +807,17 @@ int orc_dop853_batch(const gx_potential *pot, const gx_frame *fr, int nb, double
     }
     free(work);
     return idid;
+}
+
+/* dop853_helper's call of dop853() on one batch (dop853.pyx:157-182):
+ * uround = np.finfo(float).eps, h0 = t[1] - t[0], dense output on t. */
+int orc_dop853_batch(const gx_potential *pot, const gx_frame *fr, int nb, double *y,
+                     const double *t, int64_t ntimes, double atol, double rtol, int64_t nmax,
+                     double dt_max, int64_t nstiff, int64_t out_stride, double *out, long *stats) {
+    batch_ctx c = {pot, fr, nb};
+    rhs_t R = {batch_rhs_cb, &c};
+    return orc_dop853_core(R, 6 * nb, y, t, ntimes, 0., 0., t[1] - t[0], atol, rtol, nmax, dt_max, nstiff,
+                           2.220446049250313e-16, out_stride, out, stats);
 }
 
 typedef struct {
@@ -884,5 +914,301 @@ void orc_hamiltonian_value_n(const gx_potential *pot, const gx_frame *fr, double
         double wi[6];
         for (int k = 0; k < 6; k++) wi[k] = w[k * N + i];
         out[i] = orc_hamiltonian_value(pot, fr, t, wi);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Direct n-body systems and mock streams                                    */
+/* (dop853.cpp:990-1006, cpotential.cpp:346-415, nbody.pyx:30-115,           */
+/*  mockstream.pyx:176-303, dop853.pyx:27-75)                                */
+/* ------------------------------------------------------------------------- */
+
+/* Gradient of a body's potential, shifted to the body's position q0: the
+ * body's CPotential with do_shift_rotate = 1 and q0 pointing at the body
+ * (cpotential.cpp:402-405), R the identity, evaluated by c_gradient (:214-287). */
+static void body_gradient(const gx_body *b, const double *q0, const double *q, double *g) {
+    gx_component c;
+    memset(&c, 0, sizeof(c));
+    c.type = b->type;
+    c.n_params = b->n_params;
+    c.param_offset = 0;
+    c.do_shift_rotate = 1;
+    for (int k = 0; k < 3; k++) c.q0[k] = q0[k];
+    c.R[0] = c.R[4] = c.R[8] = 1.;
+    gx_potential bp;
+    memset(&bp, 0, sizeof(bp));
+    bp.n_components = 1;
+    bp.n_dim = 3;
+    bp.components = &c;
+    bp.params = b->params;
+    gradient_point(&bp, q, g);
+}
+
+typedef struct {
+    const gx_potential *pot;
+    const gx_frame *fr;
+    int norbits, nbody;
+    const gx_body *bodies; /* nbody entries */
+} nbody_ctx;
+
+/* Fwrapper_direct_nbody (dop853.cpp:990-1006): hamiltonian_gradient for every
+ * body of the AoS state y[6 * norbits], then c_nbody_acceleration
+ * (cpotential.cpp:389-415): every non-null massive body j pulls every other
+ * body i, acc[6 i + 3 + k] += -f2[k]. */
+static void nbody_rhs_cb(const void *vctx, const double *y, double *f) {
+    const nbody_ctx *C = (const nbody_ctx *)vctx;
+    for (int i = 0; i < C->norbits; i++) rhs_point(C->pot, C->fr, y + 6 * i, f + 6 * i);
+    for (int j = 0; j < C->nbody; j++) {
+        const gx_body *b = &C->bodies[j];
+        if (b->type == GX_POT_NULL) continue;
+        for (int i = 0; i < C->norbits; i++) {
+            if (i == j) continue;
+            double f2[3];
+            body_gradient(b, y + 6 * j, y + 6 * i, f2);
+            for (int k = 0; k < 3; k++) f[6 * i + 3 + k] += -f2[k];
+        }
+    }
+}
+
+/* direct_nbody_dop853 (nbody.pyx:30-115) -> dop853_helper (dop853.pyx:90-193)
+ * on one system of nparticles bodies, the first nbody of them massive:
+ * w0 (nparticles, 6); w_out (ntimes, nparticles, 6) if save_all else
+ * (nparticles, 6).  uround = eps, h0 = t[1] - t[0], nstiff as given (gala
+ * passes -1). */
+int orc_nbody_dop853(const gx_potential *pot, const gx_frame *fr, int nparticles, int nbody,
+                     const gx_body *bodies, const double *w0, const double *t, int64_t ntimes,
+                     double atol, double rtol, int64_t nmax, double dt_max, int64_t nstiff,
+                     int save_all, double *w_out, long *stats) {
+    if (ntimes < 2 || nparticles < 1 || nbody < 0 || nbody > nparticles) return -1;
+    nbody_ctx C = {pot, fr, nparticles, nbody, bodies};
+    rhs_t R = {nbody_rhs_cb, &C};
+    const int n = 6 * nparticles;
+    double *y = (double *)malloc(sizeof(double) * (size_t)n);
+    memcpy(y, w0, sizeof(double) * (size_t)n);
+    int res = orc_dop853_core(R, n, y, t, ntimes, 0., 0., t[1] - t[0], atol, rtol, nmax, dt_max, nstiff,
+                              2.220446049250313e-16, 1, save_all ? w_out : NULL, stats);
+    if (!save_all) memcpy(w_out, y, sizeof(double) * (size_t)n);
+    free(y);
+    return res;
+}
+
+/* dop853_step (dop853.pyx:27-75) on one release system: the state w
+ * (nsys, 6) from t1 to t2 with h0 = dt0, uround 0 (-> 2.3e-16), hmax 0,
+ * nstiff 1 (the literal in dop853_step, whatever the caller passes), no output. */
+static int orc_dop853_step_system(const gx_potential *pot, const gx_frame *fr, int nsys, int nbody,
+                                  const gx_body *bodies, double *w, double t1, double t2, double dt0,
+                                  double atol, double rtol, int64_t nmax, long *stats) {
+    nbody_ctx C = {pot, fr, nsys, nbody, bodies};
+    rhs_t R = {nbody_rhs_cb, &C};
+    return orc_dop853_core(R, 6 * nsys, w, NULL, 0, t1, t2, dt0, atol, rtol, nmax, 0.0, 1, 0.0, 1, NULL,
+                           stats);
+}
+
+/* mockstream_dop853 (mockstream.pyx:176-303) for one progenitor system:
+ *   nbody_w0  (nbodies, 6)   massive bodies (progenitor first) at time[0]
+ *   time      (ntimes)       release-time grid; dt0 = time[1] - time[0]
+ *   stream_w0 (ntot, 6)      released particles, grouped by release time
+ *   stream_t1 (ntimes), nstream (ntimes)
+ * First the bodies are integrated over `time` with dense output (dop853_helper,
+ * nstiff as given), then every release i with nstream[i] > 0 integrates
+ * [bodies at time[i], its particles] from stream_t1[i] to tfinal.
+ * Outputs: nbody_w_final (nbodies, 6) = the bodies after the last release
+ * system, stream_w_final (ntot, 6), status (ntimes): gala's idid per release,
+ * 0 where nothing was released. */
+int orc_mockstream_dop853(const gx_potential *pot, const gx_frame *fr, int nbodies, const gx_body *bodies,
+                          const double *nbody_w0, const double *time, int64_t ntimes, const double *stream_w0,
+                          const double *stream_t1, double tfinal, const int32_t *nstream, double atol,
+                          double rtol, int64_t nmax, double dt_max, int64_t nstiff, double *nbody_w_final,
+                          double *stream_w_final, int32_t *status) {
+    if (ntimes < 2 || nbodies < 1) return -1;
+    int maxn = 0;
+    for (int64_t i = 0; i < ntimes; i++) maxn = nstream[i] > maxn ? nstream[i] : maxn;
+    double *nbody_w = (double *)malloc(sizeof(double) * (size_t)ntimes * 6 * (size_t)nbodies);
+    int res = orc_nbody_dop853(pot, fr, nbodies, nbodies, bodies, nbody_w0, time, ntimes, atol, rtol, nmax,
+                               dt_max, nstiff, 1, nbody_w, NULL);
+    if (res < 0) {
+        free(nbody_w);
+        return res;
+    }
+    const double dt0 = time[1] - time[0];
+    double *w_tmp = (double *)malloc(sizeof(double) * 6 * (size_t)(nbodies + maxn));
+    int64_t n = 0;
+    for (int64_t i = 0; i < ntimes; i++) {
+        status[i] = 0;
+        if (nstream[i] == 0) continue;
+        memcpy(w_tmp, nbody_w + (size_t)i * 6 * (size_t)nbodies, sizeof(double) * 6 * (size_t)nbodies);
+        memcpy(w_tmp + 6 * nbodies, stream_w0 + 6 * n, sizeof(double) * 6 * (size_t)nstream[i]);
+        status[i] = orc_dop853_step_system(pot, fr, nbodies + nstream[i], nbodies, bodies, w_tmp, stream_t1[i],
+                                           tfinal, dt0, atol, rtol, nmax, NULL);
+        memcpy(stream_w_final + 6 * n, w_tmp + 6 * nbodies, sizeof(double) * 6 * (size_t)nstream[i]);
+        memcpy(nbody_w_final, w_tmp, sizeof(double) * 6 * (size_t)nbodies);
+        n += nstream[i];
+    }
+    free(w_tmp);
+    free(nbody_w);
+    return 0;
+}
+
+/* Release systems of many independent streams that share one release grid,
+ * the layout of the GPU library's mock-stream entry point:
+ *   bodies    (n_streams, nbodies)
+ *   nbody_w   (n_streams, n_release, nbodies, 6)  bodies at each release time
+ *   stream_w0 (n_streams, ntot, 6), particles of release i at offset
+ *             sum(nstream[:i])
+ * System id = i * n_streams + s; systems [sys_lo, sys_hi) are integrated
+ * (release systems with nstream[i] == 0 are skipped, status 0).
+ * stats (n_streams * n_release, 4) may be NULL. */
+typedef struct {
+    const gx_potential *pot;
+    const gx_frame *fr;
+    int64_t n_streams, n_release, ntot;
+    int nbodies;
+    const gx_body *bodies;
+    const double *nbody_w, *release_t, *stream_w0;
+    const int32_t *nstream;
+    const int64_t *offset;
+    double t_final, dt0, atol, rtol;
+    int64_t nmax;
+    double *stream_w_out, *nbody_w_out;
+    int32_t *status;
+    long *stats;
+    int64_t last_release;
+    int64_t sys_base; /* ranges handed to ms_chunk are relative to this id */
+} ms_ctx;
+
+static void ms_chunk(void *vctx, int64_t lo, int64_t hi) {
+    const ms_ctx *C = (const ms_ctx *)vctx;
+    int maxn = 0;
+    for (int64_t i = 0; i < C->n_release; i++) maxn = C->nstream[i] > maxn ? C->nstream[i] : maxn;
+    const int nb = C->nbodies;
+    double *w = (double *)malloc(sizeof(double) * 6 * (size_t)(nb + maxn));
+    for (int64_t sys = C->sys_base + lo; sys < C->sys_base + hi; sys++) {
+        const int64_t i = sys / C->n_streams, s = sys % C->n_streams;
+        const int np = C->nstream[i];
+        if (np == 0) {
+            C->status[s * C->n_release + i] = 0;
+            continue;
+        }
+        memcpy(w, C->nbody_w + ((size_t)(s * C->n_release + i)) * 6 * (size_t)nb, sizeof(double) * 6 * (size_t)nb);
+        memcpy(w + 6 * nb, C->stream_w0 + ((size_t)(s * C->ntot + C->offset[i])) * 6, sizeof(double) * 6 * (size_t)np);
+        long st[4];
+        C->status[s * C->n_release + i] = orc_dop853_step_system(C->pot, C->fr, nb + np, nb, C->bodies + s * nb, w,
+                                                                 C->release_t[i], C->t_final, C->dt0, C->atol,
+                                                                 C->rtol, C->nmax, st);
+        if (C->stats)
+            for (int k = 0; k < 4; k++) C->stats[(s * C->n_release + i) * 4 + k] = st[k];
+        memcpy(C->stream_w_out + ((size_t)(s * C->ntot + C->offset[i])) * 6, w + 6 * nb, sizeof(double) * 6 * (size_t)np);
+        if (i == C->last_release && C->nbody_w_out)
+            memcpy(C->nbody_w_out + (size_t)s * 6 * (size_t)nb, w, sizeof(double) * 6 * (size_t)nb);
+    }
+    free(w);
+}
+
+int orc_mockstream_systems(const gx_potential *pot, const gx_frame *fr, int64_t n_streams, int nbodies,
+                           const gx_body *bodies, const double *nbody_w, int64_t n_release, const double *release_t,
+                           const int32_t *nstream, const double *stream_w0, double t_final, double dt0, double atol,
+                           double rtol, int64_t nmax, double *stream_w_out, double *nbody_w_out, int32_t *status,
+                           long *stats, int64_t sys_lo, int64_t sys_hi, int nthreads) {
+    if (n_streams < 1 || n_release < 1 || nbodies < 1) return -1;
+    int64_t *offset = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n_release + 1));
+    offset[0] = 0;
+    int64_t last = -1;
+    for (int64_t i = 0; i < n_release; i++) {
+        offset[i + 1] = offset[i] + nstream[i];
+        if (nstream[i] > 0) last = i;
+    }
+    if (sys_hi > n_streams * n_release) sys_hi = n_streams * n_release;
+    ms_ctx C = {pot, fr, n_streams, n_release, offset[n_release], nbodies, bodies, nbody_w, release_t, stream_w0,
+                nstream, offset, t_final, dt0, atol, rtol, nmax, stream_w_out, nbody_w_out, status, stats, last,
+                sys_lo};
+    if (sys_lo < sys_hi) parallel_for(nthreads, sys_hi - sys_lo, 16, ms_chunk, &C);
+    free(offset);
+    return 0;
+}
+
+/* c_d2_dr2 (cpotential.cpp:346-371): second radial difference of Phi with the
+ * fixed step h = 1e-2, at N points q (N, 3). */
+void orc_d2_dr2_n(const gx_potential *pot, double t, const double *q, int64_t N, double *out) {
+    for (int64_t n = 0; n < N; n++) {
+        const double *qp = q + 3 * n;
+        double eps[3], r2 = 0;
+        for (int j = 0; j < 3; j++) r2 = r2 + qp[j] * qp[j];
+        const double h = 1E-2;
+        const double r = sqrt(r2);
+        for (int j = 0; j < 3; j++) eps[j] = qp[j] + h * qp[j] / r;
+        double d2 = orc_potential(pot, t, eps);
+        d2 = d2 - 2. * orc_potential(pot, t, qp);
+        for (int j = 0; j < 3; j++) eps[j] = qp[j] - h * qp[j] / r;
+        d2 = d2 + orc_potential(pot, t, eps);
+        out[n] = d2 / (h * h);
+    }
+}
+
+/* FardalStreamDF._sample (df.pyx:363-457) for one progenitor orbit, with
+ * get_rj_vj_R (:61-92), transform_from_sat (:94-106) and _coord.pyx's cross /
+ * norm / apply_3matrix.  Same layout as the GPU sampler:
+ *   prog_w (ntimes, row_stride) x, v first; prog_m (ntimes); t (ntimes)
+ *   offset (ntimes + 1) first particle row per time (trailing rows first)
+ *   draws (n_particles, 4) the normal draws kx, kz, kvt, kvz
+ *   w_out (n_particles, 6) */
+void orc_fardal_sample(const gx_potential *pot, int64_t ntimes, const double *prog_w, int64_t row_stride,
+                       const double *prog_m, const double *t, const int64_t *offset, const double *draws, double G,
+                       int lead, int trail, int gala_modified, double *w_out) {
+    const int ntail = lead + trail;
+    for (int64_t i = 0; i < ntimes; i++) {
+        const int64_t o0 = offset[i], o1 = offset[i + 1];
+        if (o1 == o0 || ntail == 0) continue;
+        const int64_t np_ = (o1 - o0) / ntail;
+        const double *px = prog_w + i * row_stride, *pv = px + 3;
+        const double m = prog_m[i];
+        double dist = 0.;
+        for (int k = 0; k < 3; k++) dist += px[k] * px[k];
+        dist = sqrt(dist);
+        double L[3];
+        L[0] = px[1] * pv[2] - px[2] * pv[1];
+        L[1] = -px[0] * pv[2] + px[2] * pv[0];
+        L[2] = px[0] * pv[1] - px[1] * pv[0];
+        double Lnorm = 0.;
+        for (int k = 0; k < 3; k++) Lnorm += L[k] * L[k];
+        Lnorm = sqrt(Lnorm);
+        double R[3][3];
+        for (int k = 0; k < 3; k++) {
+            R[0][k] = px[k] / dist;
+            R[2][k] = L[k] / Lnorm;
+        }
+        const double Om = Lnorm / (dist * dist);
+        double d2r;
+        orc_d2_dr2_n(pot, t[i], px, 1, &d2r);
+        const double rj = pow(G * m / (Om * Om - d2r), 1 / 3.);
+        const double vj = Om * rj;
+        R[1][0] = R[0][1] * R[2][2] - R[0][2] * R[2][1];
+        R[1][1] = -R[0][0] * R[2][2] + R[0][2] * R[2][0];
+        R[1][2] = R[0][0] * R[2][1] - R[0][1] * R[2][0];
+        for (int k = 0; k < 3; k++) R[1][k] = -R[1][k];
+        int64_t row = o0;
+        for (int tail = 0; tail < 2; tail++) {
+            if (tail == 0 && !trail) continue;
+            if (tail == 1 && !lead) continue;
+            const double sr = tail == 0 ? rj : -rj, sv = tail == 0 ? vj : -vj;
+            for (int64_t k = 0; k < np_; k++, row++) {
+                const double *d = draws + row * 4;
+                const double kx = d[0];
+                double tx[3] = {0., 0., 0.}, tv[3] = {0., 0., 0.};
+                tx[0] = kx * sr;
+                tx[2] = d[1] * sr;
+                tv[1] = d[2] * sv;
+                if (gala_modified) tv[1] *= kx;
+                tv[2] = d[3] * sv;
+                double *o = w_out + row * 6;
+                for (int n = 0; n < 3; n++) {
+                    o[n] = R[0][n] * tx[0] + R[1][n] * tx[1] + R[2][n] * tx[2];
+                    o[3 + n] = R[0][n] * tv[0] + R[1][n] * tv[1] + R[2][n] * tv[2];
+                }
+                for (int n = 0; n < 3; n++) {
+                    o[n] += px[n];
+                    o[3 + n] += pv[n];
+                }
+            }
+        }
     }
 }

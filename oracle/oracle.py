@@ -159,6 +159,112 @@ class Oracle:
             raise RuntimeError(f"oracle dop853 failed ({rc})")
         return out, status, stats
 
+    # --------------------------------------------------- n-body and streams
+    @staticmethod
+    def _bodies(b):
+        b = np.ascontiguousarray(b)
+        if b.dtype.itemsize != 64 or b.dtype.names != ("type", "n_params", "params"):
+            raise TypeError("bodies must be a gx_body-layout structured array")
+        return b
+
+    def nbody_dop853(self, pot, bodies, nbody, w0, t, atol=1e-10, rtol=1e-10, nmax=0, dt_max=0.0, nstiff=-1,
+                     save_all=True, frame=None):
+        """direct_nbody_dop853 on one system: bodies (nparticles,) gx_body records
+        (massive ones first, nbody of them), w0 (nparticles, 6).  Returns
+        (w (ntimes, nparticles, 6) or (nparticles, 6), idid)."""
+        b = self._bodies(bodies)
+        w0 = _f64(w0)
+        t = _f64(t)
+        npart = w0.shape[0]
+        out = np.zeros((len(t), npart, 6) if save_all else (npart, 6))
+        if self.is_ref:
+            res = self.lib.ref_nbody_dop853(
+                pot.packed().for_host(), self._frame(frame), C.c_int(npart), C.c_int(nbody), _p(b), _p(w0), _p(t),
+                C.c_int64(len(t)), C.c_double(atol), C.c_double(rtol), C.c_int64(nmax), C.c_double(dt_max),
+                C.c_int64(nstiff), C.c_int(int(save_all)), _p(out))
+        else:
+            res = self.lib.orc_nbody_dop853(
+                pot.packed().for_host(), self._frame(frame), C.c_int(npart), C.c_int(nbody), _p(b), _p(w0), _p(t),
+                C.c_int64(len(t)), C.c_double(atol), C.c_double(rtol), C.c_int64(nmax), C.c_double(dt_max),
+                C.c_int64(nstiff), C.c_int(int(save_all)), _p(out), None)
+        return out, int(res)
+
+    def mockstream_dop853(self, pot, bodies, nbody_w0, time, stream_w0, stream_t1, tfinal, nstream, atol=1e-10,
+                          rtol=1e-10, nmax=0, dt_max=0.0, nstiff=-1, frame=None):
+        """mockstream_dop853 for one progenitor system.  Returns
+        (nbody_w_final (nbodies, 6), stream_w_final (ntot, 6), status (ntimes,))."""
+        b = self._bodies(bodies)
+        nbody_w0 = _f64(nbody_w0)
+        time = _f64(time)
+        stream_w0 = _f64(stream_w0).reshape(-1, 6)
+        stream_t1 = _f64(stream_t1)
+        nstream = np.ascontiguousarray(np.asarray(nstream, dtype=np.int32))
+        nb = nbody_w0.shape[0]
+        nb_out = np.zeros((nb, 6))
+        st_out = np.zeros_like(stream_w0)
+        status = np.zeros(len(time), dtype=np.int32)
+        fn = self.lib.ref_mockstream_dop853 if self.is_ref else self.lib.orc_mockstream_dop853
+        res = fn(pot.packed().for_host(), self._frame(frame), C.c_int(nb), _p(b), _p(nbody_w0), _p(time),
+                 C.c_int64(len(time)), _p(stream_w0), _p(stream_t1), C.c_double(tfinal), _p(nstream),
+                 C.c_double(atol), C.c_double(rtol), C.c_int64(nmax), C.c_double(dt_max), C.c_int64(nstiff),
+                 _p(nb_out), _p(st_out), _p(status))
+        if res < 0:
+            raise RuntimeError(f"mockstream oracle failed ({res})")
+        return nb_out, st_out, status
+
+    def mockstream_systems(self, pot, bodies, nbody_w, release_t, nstream, stream_w0, t_final, dt0, atol=1e-10,
+                           rtol=1e-10, nmax=0, sys_lo=0, sys_hi=None, nthreads=1, frame=None):
+        """The release systems of many streams (the GPU entry point's layout):
+        bodies (S, nb), nbody_w (S, n_release, nb, 6), stream_w0 (S, ntot, 6).
+        Returns (stream_w (S, ntot, 6), nbody_w_final (S, nb, 6), status
+        (S, n_release), stats (S, n_release, 4))."""
+        if self.is_ref:
+            raise NotImplementedError("use mockstream_dop853 for gala's own code")
+        b = self._bodies(bodies)
+        nbody_w = _f64(nbody_w)
+        S, nrel, nb = nbody_w.shape[:3]
+        release_t = _f64(release_t)
+        nstream = np.ascontiguousarray(np.asarray(nstream, dtype=np.int32))
+        stream_w0 = _f64(stream_w0)
+        out = np.zeros_like(stream_w0)
+        nb_out = np.zeros((S, nb, 6))
+        status = np.zeros((S, nrel), dtype=np.int32)
+        stats = np.zeros((S, nrel, 4), dtype=np.int64)
+        hi = S * nrel if sys_hi is None else sys_hi
+        rc = self.lib.orc_mockstream_systems(
+            pot.packed().for_host(), self._frame(frame), C.c_int64(S), C.c_int(nb), _p(b), _p(nbody_w),
+            C.c_int64(nrel), _p(release_t), _p(nstream), _p(stream_w0), C.c_double(t_final), C.c_double(dt0),
+            C.c_double(atol), C.c_double(rtol), C.c_int64(nmax), _p(out), _p(nb_out), _p(status), _p(stats),
+            C.c_int64(sys_lo), C.c_int64(hi), C.c_int(nthreads))
+        if rc != 0:
+            raise RuntimeError(f"oracle mockstream systems failed ({rc})")
+        return out, nb_out, status, stats
+
+    def d2_dr2(self, pot, q, t=0.0):
+        """c_d2_dr2 at points q (N, 3)."""
+        q = _f64(q).reshape(-1, 3)
+        out = np.zeros(q.shape[0])
+        if self.is_ref:
+            rc = self.lib.ref_d2_dr2_n(pot.packed().for_host(), C.c_double(t), _p(q), C.c_int64(q.shape[0]), _p(out))
+            if rc != 0:
+                raise NotImplementedError("component not available in the gala build")
+        else:
+            self.lib.orc_d2_dr2_n(pot.packed().for_host(), C.c_double(t), _p(q), C.c_int64(q.shape[0]), _p(out))
+        return out
+
+    def fardal_sample(self, pot, prog_w, prog_m, t, offset, draws, G, lead=True, trail=True, gala_modified=True):
+        """FardalStreamDF._sample for one orbit: prog_w (ntimes, k >= 6)."""
+        prog_w = _f64(prog_w)
+        prog_m = _f64(prog_m)
+        t = _f64(t)
+        offset = np.ascontiguousarray(np.asarray(offset, dtype=np.int64))
+        draws = _f64(draws).reshape(-1, 4)
+        out = np.zeros((draws.shape[0], 6))
+        self.lib.orc_fardal_sample(pot.packed().for_host(), C.c_int64(len(t)), _p(prog_w),
+                                   C.c_int64(prog_w.shape[1]), _p(prog_m), _p(t), _p(offset), _p(draws),
+                                   C.c_double(G), C.c_int(int(lead)), C.c_int(int(trail)),
+                                   C.c_int(int(gala_modified)), _p(out))
+        return out
 
 def host_threads() -> int:
     try:

@@ -14,7 +14,12 @@
  *     package), calling gala's c_gradient;
  *   - dop853_integrate_hamiltonian / dop853_helper (dop853.pyx:90-250): one call
  *     of gala's dop853() per batch of nbatch orbits with exactly that argument
- *     list, Fwrapper_T as the right-hand side and a dense-output state.
+ *     list, Fwrapper_T as the right-hand side and a dense-output state;
+ *   - direct_nbody_dop853 (nbody.pyx:30-115) and mockstream_dop853 with
+ *     dop853_step (mockstream.pyx:176-303, dop853.pyx:27-75): gala's dop853()
+ *     with Fwrapper_direct_nbody and an array of per-body CPotentials built as
+ *     the particle potentials are (NullWrapper sets `null = 1`,
+ *     builtin/cybuiltin.pyx:365-372).
  */
 #include <math.h>
 #include <pthread.h>
@@ -288,6 +293,53 @@ void dop_chunk(void *vctx, int64_t blo, int64_t bhi) {
     release(&rp);
 }
 
+/* A body's CPotential: one component with its own parameters (q0 and
+ * do_shift_rotate are set by c_nbody_acceleration), or gala's NullPotential. */
+struct RefBody {
+    CPotential *cp;
+    double q0[3];
+    double R[9];
+    double params[7];
+};
+
+bool build_body(const gx_body *b, RefBody *rb) {
+    rb->cp = allocate_cpotential(1);
+    CPotential *cp = rb->cp;
+    cp->n_dim = 3;
+    if (!set_funcs(cp, 0, b->type)) return false;
+    cp->null = (b->type == GX_POT_NULL) ? 1 : 0;
+    memcpy(rb->params, b->params, sizeof(rb->params));
+    for (int k = 0; k < 3; k++) rb->q0[k] = 0.;
+    for (int k = 0; k < 9; k++) rb->R[k] = (k % 4 == 0) ? 1. : 0.;
+    cp->n_params[0] = b->n_params;
+    cp->parameters[0] = rb->params;
+    cp->q0[0] = rb->q0;
+    cp->R[0] = rb->R;
+    cp->state[0] = NULL;
+    cp->do_shift_rotate[0] = 0;
+    return true;
+}
+
+/* direct_nbody_dop853's dop853_helper call (nbody.pyx:99-107, dop853.pyx:157-182). */
+int nbody_helper(RefPot &rp, CPotential **pots, int nparticles, int nbody, double *w, const double *t,
+                 int64_t ntimes, double atol, double rtol, int64_t nmax, double dt_max, int64_t nstiff,
+                 int save_all, double *output_w) {
+    const unsigned size = 6 * (unsigned)nparticles;
+    Dop853DenseState *state = NULL;
+    unsigned nrdens = 0;
+    if (save_all) {
+        state = dop853_dense_state_alloc(size, size);
+        nrdens = size;
+    }
+    int res = dop853(size, (FcnEqDiff)Fwrapper_direct_nbody, rp.cp, &rp.cf, (unsigned)nparticles, (unsigned)nbody,
+                     (void *)pots, t[0], w, t[ntimes - 1], &rtol, &atol, 0, NULL, 0, NULL,
+                     2.220446049250313e-16, 0.0, 0.0, 0.0, 0.0, dt_max, t[1] - t[0], (long)nmax, 1,
+                     (long)nstiff, nrdens, NULL, 0, state, const_cast<double *>(t), (int)ntimes,
+                     save_all ? output_w : NULL);
+    if (state) dop853_dense_state_free(state, size);
+    return res;
+}
+
 } // namespace
 
 extern "C" {
@@ -356,6 +408,120 @@ int ref_dop853_integrate(const gx_potential *pot, const gx_frame *fr, const doub
     C.nmax = nmax; C.nstiff = nstiff; C.atol = atol; C.rtol = rtol; C.dt_max = dt_max;
     C.save_all = save_all; C.nbatch = nbatch; C.w_out = w_out; C.status = status;
     parallel_for(nthreads, (n + nbatch - 1) / nbatch, 1, dop_chunk, &C);
+    return 0;
+}
+
+/* direct_nbody_dop853 on one system: w0 (nparticles, 6), bodies (nparticles)
+ * with the massive ones first (nbody of them); w_out (ntimes, nparticles, 6)
+ * if save_all, else (nparticles, 6).  Returns gala's idid or -100 when a body
+ * type cannot be built. */
+int ref_nbody_dop853(const gx_potential *pot, const gx_frame *fr, int nparticles, int nbody, const gx_body *bodies,
+                     const double *w0, const double *t, int64_t ntimes, double atol, double rtol, int64_t nmax,
+                     double dt_max, int64_t nstiff, int save_all, double *w_out) {
+    RefPot rp;
+    if (!build(pot, fr, &rp)) { release(&rp); return -100; }
+    RefBody *rb = (RefBody *)calloc((size_t)nparticles, sizeof(RefBody));
+    CPotential **pots = (CPotential **)malloc(sizeof(CPotential *) * (size_t)nparticles);
+    int ok = 1;
+    for (int i = 0; i < nparticles; i++) {
+        if (!build_body(&bodies[i], &rb[i])) ok = 0;
+        pots[i] = rb[i].cp;
+    }
+    int res = -100;
+    if (ok) {
+        double *w = (double *)malloc(sizeof(double) * 6 * (size_t)nparticles);
+        memcpy(w, w0, sizeof(double) * 6 * (size_t)nparticles);
+        res = nbody_helper(rp, pots, nparticles, nbody, w, t, ntimes, atol, rtol, nmax, dt_max, nstiff, save_all,
+                           w_out);
+        if (!save_all) memcpy(w_out, w, sizeof(double) * 6 * (size_t)nparticles);
+        free(w);
+    }
+    for (int i = 0; i < nparticles; i++)
+        if (rb[i].cp) free_cpotential(rb[i].cp);
+    free(rb);
+    free(pots);
+    release(&rp);
+    return res;
+}
+
+/* mockstream_dop853 (mockstream.pyx:176-303) for one progenitor system, same
+ * arguments and outputs as the oracle's orc_mockstream_dop853.  The body
+ * potentials of the released particles are gala's NullPotential. */
+int ref_mockstream_dop853(const gx_potential *pot, const gx_frame *fr, int nbodies, const gx_body *bodies,
+                          const double *nbody_w0, const double *time, int64_t ntimes, const double *stream_w0,
+                          const double *stream_t1, double tfinal, const int32_t *nstream, double atol, double rtol,
+                          int64_t nmax, double dt_max, int64_t nstiff, double *nbody_w_final,
+                          double *stream_w_final, int32_t *status) {
+    RefPot rp;
+    if (!build(pot, fr, &rp)) { release(&rp); return -100; }
+    int64_t total = 0;
+    int maxn = 0;
+    for (int64_t i = 0; i < ntimes; i++) {
+        total += nstream[i];
+        maxn = nstream[i] > maxn ? nstream[i] : maxn;
+    }
+    const int64_t total_bodies = nbodies + total;
+    RefBody *rb = (RefBody *)calloc((size_t)nbodies + 1, sizeof(RefBody));
+    CPotential **pots = (CPotential **)malloc(sizeof(CPotential *) * (size_t)total_bodies);
+    int ok = 1;
+    for (int i = 0; i < nbodies; i++) {
+        if (!build_body(&bodies[i], &rb[i])) ok = 0;
+        pots[i] = rb[i].cp;
+    }
+    gx_body null_body;
+    memset(&null_body, 0, sizeof(null_body));
+    null_body.type = GX_POT_NULL;
+    if (!build_body(&null_body, &rb[nbodies])) ok = 0;
+    for (int64_t i = nbodies; i < total_bodies; i++) pots[i] = rb[nbodies].cp;
+    int res = -100;
+    if (ok) {
+        /* the bodies first, with dense output on `time` (mockstream.pyx:245-255) */
+        double *nbody_w = (double *)malloc(sizeof(double) * (size_t)ntimes * 6 * (size_t)nbodies);
+        double *w0c = (double *)malloc(sizeof(double) * 6 * (size_t)nbodies);
+        memcpy(w0c, nbody_w0, sizeof(double) * 6 * (size_t)nbodies);
+        res = nbody_helper(rp, pots, nbodies, nbodies, w0c, time, ntimes, atol, rtol, nmax, dt_max, nstiff, 1,
+                           nbody_w);
+        free(w0c);
+        if (res >= 0) {
+            res = 0;
+            const double dt0 = time[1] - time[0];
+            double *w_tmp = (double *)malloc(sizeof(double) * 6 * (size_t)(nbodies + maxn));
+            int64_t n = 0;
+            for (int64_t i = 0; i < ntimes; i++) {
+                status[i] = 0;
+                if (nstream[i] == 0) continue;
+                memcpy(w_tmp, nbody_w + (size_t)i * 6 * (size_t)nbodies, sizeof(double) * 6 * (size_t)nbodies);
+                memcpy(w_tmp + 6 * nbodies, stream_w0 + 6 * n, sizeof(double) * 6 * (size_t)nstream[i]);
+                /* dop853_step (dop853.pyx:27-75): its exact argument list */
+                double rt = rtol, at = atol;
+                const unsigned nsys = (unsigned)(nbodies + nstream[i]);
+                status[i] = dop853(6 * nsys, (FcnEqDiff)Fwrapper_direct_nbody, rp.cp, &rp.cf, nsys,
+                                   (unsigned)nbodies, (void *)pots, stream_t1[i], w_tmp, tfinal, &rt, &at, 0, NULL,
+                                   0, NULL, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, dt0, (long)nmax, 0, 1, 0, NULL, 0, NULL,
+                                   NULL, 0, NULL);
+                memcpy(stream_w_final + 6 * n, w_tmp + 6 * nbodies, sizeof(double) * 6 * (size_t)nstream[i]);
+                memcpy(nbody_w_final, w_tmp, sizeof(double) * 6 * (size_t)nbodies);
+                n += nstream[i];
+            }
+            free(w_tmp);
+        }
+        free(nbody_w);
+    }
+    for (int i = 0; i <= nbodies; i++)
+        if (rb[i].cp) free_cpotential(rb[i].cp);
+    free(rb);
+    free(pots);
+    release(&rp);
+    return res;
+}
+
+/* c_d2_dr2 (cpotential.cpp:346-371) at N points q (N, 3). */
+int ref_d2_dr2_n(const gx_potential *pot, double t, const double *q, int64_t N, double *out) {
+    RefPot rp;
+    if (!build(pot, NULL, &rp)) { release(&rp); return -1; }
+    double eps[3];
+    for (int64_t i = 0; i < N; i++) out[i] = c_d2_dr2(rp.cp, t, const_cast<double *>(q + 3 * i), eps);
+    release(&rp);
     return 0;
 }
 

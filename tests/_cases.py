@@ -24,3 +24,39 @@ def potentials():
         "mw": W.mw_composite(),
         "shifted_rotated": shifted,
     }
+
+
+def stream_case(n_streams=2, n_steps=150, dt=1.0, seed=21, n_per_tail=1, release_every=1):
+    """A small batch of mock streams in the MW composite, built with the oracle:
+    Plummer progenitors, progenitor orbits from gala's own n-body DOP853
+    semantics, Fardal release states from seeded draws.  Returns a dict of the
+    inputs of the release stage (layout of the GPU entry points)."""
+    import numpy as np
+
+    from gala_gb300.mockstream import FardalStreamDF
+    from gala_gb300.nbody import pack_bodies
+    from oracle import Oracle
+
+    orc = Oracle("strict")
+    mw = W.mw_composite()
+    w0, m, b = W.stream_progenitors(n_streams, seed=seed)
+    pots = W.stream_progenitor_potentials(m, b)
+    bodies = pack_bodies([[p] for p in pots])
+    t = g.parse_time_specification(dt=dt, n_steps=n_steps)
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(seed))
+    counts = df.release_counts(len(t), release_every, n_per_tail)
+    offset = np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)
+    orbits, stream_w0 = [], []
+    for s in range(n_streams):
+        orb, res = orc.nbody_dop853(mw, bodies[s], 1, w0[:, s].reshape(1, 6), t, nstiff=-1)
+        assert res == 1
+        orbits.append(orb)
+        draws = df._draws(int(offset[-1]))
+        stream_w0.append(orc.fardal_sample(mw, orb.reshape(len(t), 6), np.full(len(t), m[s]), t, offset, draws,
+                                           g.units.G))
+    rel = np.nonzero(counts > 0)[0]
+    if 0 not in rel:
+        rel = np.insert(rel, 0, 0)
+    return dict(pot=mw, bodies=bodies, w0=w0, m=m, b=b, t=t, counts=counts, offset=offset,
+                orbits=np.stack(orbits), stream_w0=np.stack(stream_w0), rel=rel, nstream=2 * counts[rel],
+                seed=seed)

@@ -123,12 +123,42 @@ def make_scf_fixture():
     np.savez_compressed(OUT / "scf_fortran.npz", **data)
 
 
+def make_stream_fixtures(ref: Oracle):
+    """gala's direct_nbody_dop853 and mockstream_dop853 (gala's own dop853(),
+    Fwrapper_direct_nbody, c_nbody_acceleration) on the shared test cases."""
+    from tests._cases import stream_case
+    from tests.test_mockstream_oracle import _nbody_system, _stream_args
+
+    mw, bodies, w0, t = _nbody_system()
+    w, res = ref.nbody_dop853(mw, bodies, 2, w0, t)
+    assert res == 1
+    np.savez_compressed(OUT / "nbody_dop853.npz", w0=w0, t=t, w=w[::50])
+
+    n_streams, n_steps = 2, 120
+    c = stream_case(n_streams=n_streams, n_steps=n_steps)
+    out = {"n_streams": n_streams, "n_steps": n_steps, "stream_w0": c["stream_w0"]}
+    streams, nbodies, status = [], [], []
+    for s in range(n_streams):
+        nb, st, stat = ref.mockstream_dop853(c["pot"], **_stream_args(c, s))
+        streams.append(st)
+        nbodies.append(nb)
+        status.append(stat)
+    np.savez_compressed(OUT / "mockstream_dop853.npz", stream=np.stack(streams), nbody=np.stack(nbodies),
+                        status=np.stack(status), **out)
+
+
 if __name__ == "__main__":
+    # python tests/golden/make_golden.py [potentials integrators scf streams]
+    which = set(sys.argv[1:]) or {"potentials", "integrators", "scf", "streams"}
     build(ref=True)
     ref = Oracle("ref")
-    make_potential_fixture(ref)
-    make_integrator_fixtures(ref)
-    if GALA_TESTS.exists():
+    if "potentials" in which:
+        make_potential_fixture(ref)
+    if "integrators" in which:
+        make_integrator_fixtures(ref)
+    if "scf" in which and GALA_TESTS.exists():
         make_scf_fixture()
+    if "streams" in which:
+        make_stream_fixtures(ref)
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)

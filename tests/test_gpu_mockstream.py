@@ -1,0 +1,342 @@
+"""GPU parity of the direct n-body and mock-stream kernels against the oracle
+(itself pinned bit for bit to gala's own dop853 / Fwrapper_direct_nbody /
+mockstream loop, tests/test_mockstream_oracle.py).
+
+Tolerances
+  * external potential and bodies made of sqrt / division only (Hernquist,
+    Plummer): every right-hand side and every error / stiffness norm is
+    computed in the oracle's order (sequential norms in gala's component order,
+    no contraction); the one difference is the step-size factor pow(err, 1/8),
+    where CUDA's pow and glibc's may differ by an ulp, so states agree to 1e-13
+    of their scale;
+  * the Milky-Way composite (pow in Miyamoto-Nagai, log in NFW): CUDA's and
+    glibc's pow/log may differ by an ulp; states agree to 1e-11 of their scale;
+  * the Fardal sampler takes d2Phi/dr2 as a second difference of Phi with the
+    fixed step h = 0.01 kpc (c_d2_dr2): an ulp of Phi (~1e-17 kpc^2/Myr^2)
+    over h^2 = 1e-4 against d2Phi/dr2 ~ 1e-4 Myr^-2 is ~1e-9 relative, so
+    release offsets from the progenitor agree to 2e-9 of their scale;
+  * stiffness exits (hlamb > 6.1 after an accepted step) are decided on
+    quantities whose last bits differ between any two builds: gala's own -Ofast
+    and strict builds disagree on one of the eight systems of the stiffness
+    case, so that test bounds the number of differing decisions.
+"""
+import numpy as np
+import pytest
+
+import gala_gb300 as g
+from gala_gb300 import _abi
+from gala_gb300 import workloads as W
+from gala_gb300.mockstream import FardalStreamDF, MockStreamGenerator
+from gala_gb300.nbody import DirectNBody, bodies_to_device, integrate_systems, pack_bodies
+
+from ._cases import stream_case
+
+pytestmark = pytest.mark.gpu
+
+MW_TOL = 1e-11
+EXACT_OPS_TOL = 1e-13
+
+
+def _scale_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _release_systems_gpu(c, pot=None, stats=False):
+    """gx_mockstream_dop853 on a stream_case's release stage."""
+    import torch
+
+    from gala_gb300._device import ptr, stream_handle
+
+    pot = c["pot"] if pot is None else pot
+    dev = torch.device("cuda")
+    rel = c["rel"]
+    t = c["t"]
+    S = c["stream_w0"].shape[0]
+    nbody_w = torch.from_numpy(np.ascontiguousarray(c["orbits"][:, rel])).to(dev)
+    sw0 = torch.from_numpy(np.ascontiguousarray(c["stream_w0"])).to(dev)
+    rt = torch.from_numpy(np.ascontiguousarray(t[rel])).to(dev)
+    off = torch.from_numpy(np.concatenate([[0], np.cumsum(c["nstream"])]).astype(np.int64)).to(dev)
+    out = torch.empty_like(sw0)
+    nb_out = torch.empty((S, 1, 6), dtype=torch.float64, device=dev)
+    status = torch.zeros((S, len(rel)), dtype=torch.int32, device=dev)
+    st = torch.zeros((S, len(rel), 4), dtype=torch.int64, device=dev)
+    counter = torch.zeros(1, dtype=torch.int64, device=dev)
+    bd = bodies_to_device(c["bodies"], dev)
+    H = g.Hamiltonian(pot)
+    _abi.call("gx_mockstream_dop853", pot.packed().for_device(), H._frame_ref(), S, 1, ptr(bd), ptr(nbody_w),
+              len(rel), ptr(rt), ptr(off), int(c["nstream"].max()), ptr(sw0), int(sw0.shape[1]), float(t[-1]),
+              float(t[rel][1] - t[rel][0]), 1e-10, 1e-10, 0, ptr(out), ptr(nb_out), ptr(status), ptr(st),
+              ptr(counter), stream_handle())
+    torch.cuda.synchronize()
+    res = (out.cpu().numpy(), nb_out.cpu().numpy(), status.cpu().numpy())
+    return res + (st.cpu().numpy(),) if stats else res
+
+
+def _oracle_release(oracle, c, pot=None):
+    pot = c["pot"] if pot is None else pot
+    rel, t = c["rel"], c["t"]
+    return oracle.mockstream_systems(pot, c["bodies"], c["orbits"][:, rel], t[rel], c["nstream"], c["stream_w0"],
+                                     t[-1], t[rel][1] - t[rel][0], nthreads=8)
+
+
+# ----------------------------------------------------------- direct n-body
+def _nbody_batch(n_sys=5):
+    pots = [g.PlummerPotential(m=2e9, b=0.4), g.HernquistPotential(m=5e9, c=1.0), None, None]
+    bodies = pack_bodies([pots[:2]] * n_sys)
+    w0 = np.stack([np.ascontiguousarray(W.mw_ics(4, seed=40 + s).T) for s in range(n_sys)])
+    w0[:, 1, :3] = w0[:, 0, :3] + np.array([1.0, 0.5, -0.2])
+    t = g.parse_time_specification(dt=1.0, n_steps=200)
+    return bodies, w0, t
+
+
+@pytest.mark.parametrize("ext", ["hernquist", "mw"])
+def test_nbody_systems_match_oracle(oracle, ext):
+    pot = g.HernquistPotential(m=1e11, c=1.0) if ext == "hernquist" else W.mw_composite()
+    bodies, w0, t = _nbody_batch()
+    out, status = integrate_systems(pot, bodies, w0, t, nstiff=-1)
+    out = out.cpu().numpy()
+    assert np.all(status.cpu().numpy() == 1)
+    for s in range(w0.shape[0]):
+        ref, res = oracle.nbody_dop853(pot, np.concatenate([bodies[s], pack_bodies([None, None])]), 2, w0[s], t)
+        assert res == 1
+        assert _scale_err(out[s], ref) < (EXACT_OPS_TOL if ext == "hernquist" else MW_TOL)
+
+
+def test_nbody_final_state_and_stride(oracle):
+    pot = W.mw_composite()
+    bodies, w0, t = _nbody_batch(3)
+    full, _ = integrate_systems(pot, bodies, w0, t)
+    strided, _ = integrate_systems(pot, bodies, w0, t, out_stride=7)
+    final, _ = integrate_systems(pot, bodies, w0, t, save_all=False)
+    full = full.cpu().numpy()
+    np.testing.assert_array_equal(strided.cpu().numpy(), full[:, ::7])
+    np.testing.assert_array_equal(final.cpu().numpy(), full[:, -1])
+
+
+def test_directnbody_api_reorders_like_gala(oracle):
+    """Null-potential bodies listed first are moved behind the massive ones for
+    the integration and put back afterwards (core.py:211-280)."""
+    pot = W.mw_composite()
+    pps = [None, g.PlummerPotential(m=2e9, b=0.4), None, g.HernquistPotential(m=5e9, c=1.0)]
+    w0 = W.mw_ics(4, seed=50)
+    w0[:3, 3] = w0[:3, 1] + np.array([0.8, -0.4, 0.1])
+    nb = DirectNBody(g.PhaseSpacePosition.from_w(w0), pps, external_potential=pot)
+    orbit = nb.integrate_orbit(dt=1.0, n_steps=150)
+    t = g.parse_time_specification(dt=1.0, n_steps=150)
+    idx = np.array([1, 3, 0, 2])
+    ref, res = oracle.nbody_dop853(pot, pack_bodies([pps[i] for i in idx]), 2, w0[:, idx].T, t)
+    ref = ref[:, np.argsort(idx)]  # (ntimes, nbodies, 6)
+    got = orbit.w()  # (6, ntimes, nbodies)
+    assert got.shape == (6, len(t), 4)
+    assert _scale_err(np.moveaxis(got, 0, -1), ref) < MW_TOL
+
+
+# ------------------------------------------------------------ release systems
+def test_release_systems_hernquist(oracle):
+    pot = g.HernquistPotential(m=1e11, c=1.0)
+    c = stream_case(n_streams=3, n_steps=120)
+    # progenitor orbits and release states in this potential (oracle)
+    c = _restage(oracle, c, pot)
+    out, nb_out, status = _release_systems_gpu(c, pot)
+    ref_out, ref_nb, ref_status, _ = _oracle_release(oracle, c, pot)
+    np.testing.assert_array_equal(status, ref_status)
+    assert _scale_err(out, ref_out) < EXACT_OPS_TOL
+    assert _scale_err(nb_out, ref_nb) < EXACT_OPS_TOL
+
+
+def test_release_systems_match_oracle_mw(oracle):
+    c = stream_case(n_streams=4, n_steps=200)
+    out, nb_out, status, stats = _release_systems_gpu(c, stats=True)
+    ref_out, ref_nb, ref_status, ref_stats = _oracle_release(oracle, c)
+    np.testing.assert_array_equal(status, ref_status)
+    assert np.all(status[:, c["nstream"] > 0] == 1)
+    assert _scale_err(out, ref_out) < MW_TOL
+    assert _scale_err(nb_out, ref_nb) < MW_TOL
+    # the step sequences agree (accepted steps per system)
+    np.testing.assert_array_equal(stats[..., 2], ref_stats[..., 2])
+
+
+def test_release_systems_several_per_release(oracle):
+    """Two particles per tail (5-lane systems) released every 3rd step."""
+    c = stream_case(n_streams=2, n_steps=90, n_per_tail=2, release_every=3)
+    # the bodies on the release grid, as mockstream_dop853 re-integrates them
+    rel, t = c["rel"], c["t"]
+    for s in range(2):
+        ob, _ = oracle.nbody_dop853(c["pot"], c["bodies"][s], 1, c["w0"][:, s].reshape(1, 6), t[rel])
+        c["orbits"][s, rel] = ob
+    out, nb_out, status = _release_systems_gpu(c)
+    ref_out, ref_nb, ref_status, _ = _oracle_release(oracle, c)
+    np.testing.assert_array_equal(status, ref_status)
+    assert _scale_err(out, ref_out) < MW_TOL
+
+
+def _restage(oracle, c, pot):
+    """Recompute a stream_case's progenitor orbits and release states in `pot`."""
+    t = c["t"]
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(c["seed"]))
+    orbits, sw0 = [], []
+    for s in range(c["bodies"].shape[0]):
+        orb, res = oracle.nbody_dop853(pot, c["bodies"][s], 1, c["w0"][:, s].reshape(1, 6), t)
+        assert res == 1
+        orbits.append(orb)
+        draws = df._draws(int(c["offset"][-1]))
+        sw0.append(oracle.fardal_sample(pot, orb.reshape(len(t), 6), np.full(len(t), c["m"][s]), t, c["offset"],
+                                        draws, g.units.G))
+    c = dict(c)
+    c["orbits"] = np.stack(orbits)
+    c["stream_w0"] = np.stack(sw0)
+    return c
+
+
+# ------------------------------------------------------------------ sampler
+def test_fardal_sampler_matches_oracle(oracle):
+    import torch
+
+    c = stream_case(n_streams=3, n_steps=100)
+    t = c["t"]
+    S = c["orbits"].shape[0]
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(c["seed"]))
+    prog_w = torch.from_numpy(np.ascontiguousarray(c["orbits"].reshape(S, len(t), 6))).cuda()
+    m = np.repeat(c["m"][:, None], len(t), axis=1)
+    w, rt, lt, off = df.sample_device(c["pot"], prog_w, t, m, c["counts"])
+    w = w.cpu().numpy()
+    np.testing.assert_array_equal(off, c["offset"])
+    for s in range(S):
+        rel = w[s] - np.repeat(c["orbits"][s, :, 0], 2 * c["counts"], axis=0)
+        ref = c["stream_w0"][s] - np.repeat(c["orbits"][s, :, 0], 2 * c["counts"], axis=0)
+        assert _scale_err(rel, ref) < 2e-9
+    assert lt[0] == "t" and lt[1] == "l" and len(lt) == w.shape[1]
+    np.testing.assert_array_equal(rt, np.repeat(t, 2 * c["counts"]))
+
+
+# ---------------------------------------------------------------- generator
+def _oracle_run(oracle, pot, prog_pot, w0, m, t, seed, release_every=1, n_per_tail=1):
+    """gala's MockStreamGenerator.run with the oracle for every numerical step."""
+    bodies = pack_bodies([prog_pot])
+    orb, res = oracle.nbody_dop853(pot, bodies, 1, w0.reshape(1, 6), t)
+    assert res == 1
+    orbit_t = t
+    if t[1] < t[0]:
+        orb = orb[::-1].copy()
+        orbit_t = t[::-1].copy()
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(seed))
+    counts = df.release_counts(len(t), release_every, n_per_tail)
+    offset = np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)
+    sw0 = oracle.fardal_sample(pot, orb.reshape(len(t), 6), np.full(len(t), m), orbit_t, offset,
+                               df._draws(int(offset[-1])), g.units.G)
+    rel = np.nonzero(counts > 0)[0]
+    if 0 not in rel:
+        rel = np.insert(rel, 0, 0)
+    nb, st, status = oracle.mockstream_dop853(pot, bodies, orb[0].reshape(1, 6), orbit_t[rel], sw0, orbit_t[rel],
+                                              orbit_t[-1], 2 * counts[rel])
+    return st, nb
+
+
+@pytest.mark.parametrize("case", ["forward", "backward", "release_every"])
+def test_generator_run_matches_oracle(oracle, case):
+    pot = W.mw_composite()
+    w0 = W.mw_ics(1, seed=60)[:, 0]
+    prog_pot = g.PlummerPotential(m=2e5, b=0.01)
+    kw = dict(dt=1.0, n_steps=150)
+    extra = {}
+    if case == "backward":
+        kw = dict(dt=-1.0, n_steps=150)
+    if case == "release_every":
+        extra = dict(release_every=4, n_particles=3)
+    gen = MockStreamGenerator(FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(7)),
+                              g.Hamiltonian(pot), progenitor_potential=prog_pot)
+    stream, nbody = gen.run(g.PhaseSpacePosition.from_w(w0), 2e5, **extra, **kw)
+    t = g.parse_time_specification(**kw)
+    ref_st, ref_nb = _oracle_run(oracle, pot, prog_pot, w0, 2e5, t, 7, extra.get("release_every", 1),
+                                 extra.get("n_particles", 1))
+    got = np.vstack([stream.xyz, stream.v_xyz]).T
+    assert got.shape == ref_st.shape
+    assert _scale_err(got, ref_st) < 1e-10
+    assert _scale_err(np.vstack([nbody.xyz, nbody.v_xyz]).T, ref_nb) < 1e-10
+    assert set(np.unique(stream.lead_trail)) == {"t", "l"}
+
+
+def test_run_batch_equals_sequential_runs():
+    pot = W.mw_composite()
+    w0, m, b = W.stream_progenitors(3, seed=70)
+    pots = W.stream_progenitor_potentials(m, b)
+    gen = MockStreamGenerator(FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(3)),
+                              g.Hamiltonian(pot))
+    res = gen.run_batch(w0, m, progenitor_potentials=pots, dt=1.0, n_steps=80)
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(3))
+    for s in range(3):
+        gen1 = MockStreamGenerator(df, g.Hamiltonian(pot), progenitor_potential=pots[s])
+        st, nb = gen1.run(g.PhaseSpacePosition.from_w(w0[:, s]), m[s], dt=1.0, n_steps=80)
+        one = res.stream(s)
+        np.testing.assert_array_equal(one.xyz, st.xyz)
+        np.testing.assert_array_equal(one.v_xyz, st.v_xyz)
+        np.testing.assert_array_equal(res.nbody(s).xyz, nb.xyz)
+
+
+def test_stream_edge_cases():
+    pot = W.mw_composite()
+    w0 = W.mw_ics(1, seed=61)[:, 0]
+    gen = MockStreamGenerator(FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(1)),
+                              g.Hamiltonian(pot), progenitor_potential=g.PlummerPotential(m=1e5, b=0.01))
+    # no release at t0 (a zero-count first entry is inserted, as gala does) and a
+    # release at the very last time (integrated over zero time: stays put)
+    n = np.zeros(21, dtype=int)
+    n[5] = 1
+    n[-1] = 1
+    stream, _ = gen.run(g.PhaseSpacePosition.from_w(w0), 1e5, n_particles=n, dt=1.0, n_steps=20)
+    assert stream.xyz.shape == (3, 4)
+    np.testing.assert_array_equal(stream.release_time, [5.0, 5.0, 20.0, 20.0])
+    # leading tail only
+    gen_l = MockStreamGenerator(FardalStreamDF(gala_modified=False, trail=False,
+                                               random_state=np.random.RandomState(1)), g.Hamiltonian(pot))
+    stream_l, _ = gen_l.run(g.PhaseSpacePosition.from_w(w0), 1e5, dt=1.0, n_steps=10)
+    assert stream_l.xyz.shape == (3, 11) and set(stream_l.lead_trail) == {"l"}
+    with pytest.raises(NotImplementedError):
+        gen.run(g.PhaseSpacePosition.from_w(w0), 1e5, dt=1.0, n_steps=10, n_particles=20)
+
+
+def test_stiffness_exit_matches_oracle(oracle):
+    """dop853_step tests stiffness after every accepted step (nstiff = 1) and
+    gala returns -4 at the first detection.  For this progenitor (m = 6.0e5,
+    b = 16 pc on a disk orbit) three of the first eight release systems are
+    stiff in the oracle's arithmetic over 2 Gyr (two or three in gala's own
+    builds): with err_if_fail=1 the run raises gala's RuntimeError; with
+    err_if_fail=0 the stiff systems keep their state at detection."""
+    pot = W.mw_composite()
+    w0, m, b = W.stream_progenitors(64, seed=1006)
+    prog_pot = g.PlummerPotential(m=m[1], b=b[1])
+    counts = np.zeros(2001, dtype=int)
+    counts[:8] = 1
+
+    def gen():
+        return MockStreamGenerator(FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(1)),
+                                   g.Hamiltonian(pot), progenitor_potential=prog_pot)
+
+    psp = g.PhaseSpacePosition.from_w(w0[:, 1])
+    with pytest.raises(RuntimeError, match="-4"):
+        gen().run(psp, m[1], n_particles=counts, dt=1.0, n_steps=2000)
+    res = gen().run_batch(w0[:, 1:2], m[1:2], progenitor_potentials=[prog_pot], n_particles=counts, dt=1.0,
+                          n_steps=2000, Integrator_kwargs=dict(err_if_fail=0))
+    status = res.status.cpu().numpy()[0]
+    got = res.stream_w[0].cpu().numpy()
+    t = g.parse_time_specification(dt=1.0, n_steps=2000)
+    ref_st, ref_nb = _oracle_run(oracle, pot, prog_pot, w0[:, 1], m[1], t, 1, n_per_tail=counts)
+    ref_status = _oracle_run_status(oracle, pot, prog_pot, w0[:, 1], m[1], t, 1, counts)
+    assert np.sum(status == -4) >= 2
+    assert np.sum(status != ref_status) <= 1, (status, ref_status)
+    both_ok = np.repeat((status == 1) & (ref_status == 1), 2)
+    assert _scale_err(got[both_ok], ref_st[both_ok]) < 1e-8
+
+
+def _oracle_run_status(oracle, pot, prog_pot, w0, m, t, seed, counts):
+    bodies = pack_bodies([prog_pot])
+    orb, _ = oracle.nbody_dop853(pot, bodies, 1, w0.reshape(1, 6), t)
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(seed))
+    offset = np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)
+    sw0 = oracle.fardal_sample(pot, orb.reshape(len(t), 6), np.full(len(t), m), t, offset,
+                               df._draws(int(offset[-1])), g.units.G)
+    rel = np.nonzero(counts > 0)[0]
+    _, _, status = oracle.mockstream_dop853(pot, bodies, orb[0].reshape(1, 6), t[rel], sw0, t[rel], t[-1],
+                                            2 * counts[rel])
+    return status

@@ -1,0 +1,157 @@
+"""The direct n-body and mock-stream oracle pinned against gala's own compiled code.
+
+gala's dop853(), Fwrapper_direct_nbody, c_nbody_acceleration and c_d2_dr2 are
+built from the gala sources (oracle/_ref) with the argument lists of
+direct_nbody_dop853 / dop853_helper and of mockstream_dop853 / dop853_step; the
+restatement must reproduce them bit for bit when both are built without
+fast-math.  The golden fixture holds gala's release-build (-Ofast) outputs for
+machines without the gala sources.
+"""
+import numpy as np
+import pytest
+
+import gala_gb300 as g
+from gala_gb300 import workloads as W
+from gala_gb300.nbody import pack_bodies
+
+from ._cases import stream_case
+
+OFAST_RTOL = 1e-11
+
+
+def _nbody_system():
+    mw = W.mw_composite()
+    pots = [g.PlummerPotential(m=2e9, b=0.4), g.HernquistPotential(m=5e9, c=1.0), None, None]
+    bodies = pack_bodies(pots)
+    w0 = np.ascontiguousarray(W.mw_ics(4, seed=31).T)
+    w0[1, :3] = w0[0, :3] + np.array([1.0, 0.5, -0.2])
+    t = g.parse_time_specification(dt=1.0, n_steps=300)
+    return mw, bodies, w0, t
+
+
+def _stream_args(c, s):
+    rel = c["rel"]
+    return dict(bodies=c["bodies"][s], nbody_w0=c["w0"][:, s].reshape(1, 6), time=c["t"][rel],
+                stream_w0=c["stream_w0"][s], stream_t1=c["t"][rel], tfinal=c["t"][-1], nstream=c["nstream"])
+
+
+def test_nbody_oracle_matches_gala(oracle, gala_ref_strict):
+    mw, bodies, w0, t = _nbody_system()
+    w_o, res_o = oracle.nbody_dop853(mw, bodies, 2, w0, t)
+    w_r, res_r = gala_ref_strict.nbody_dop853(mw, bodies, 2, w0, t)
+    assert res_o == res_r == 1
+    np.testing.assert_array_equal(w_o, w_r)
+    # the massive pair really interacts: the test particles' orbits differ from the pair's
+    assert np.ptp(w_o[:, 1, :3] - w_o[:, 0, :3]) > 0.1
+
+
+def test_nbody_oracle_final_state_matches_gala(oracle, gala_ref_strict):
+    mw, bodies, w0, t = _nbody_system()
+    w_o, _ = oracle.nbody_dop853(mw, bodies, 2, w0, t, save_all=False)
+    w_r, _ = gala_ref_strict.nbody_dop853(mw, bodies, 2, w0, t, save_all=False)
+    np.testing.assert_array_equal(w_o, w_r)
+
+
+def test_mockstream_oracle_matches_gala(oracle, gala_ref_strict):
+    c = stream_case(n_streams=2, n_steps=120)
+    for s in range(2):
+        a = _stream_args(c, s)
+        nb_o, st_o, stat_o = oracle.mockstream_dop853(c["pot"], **a)
+        nb_r, st_r, stat_r = gala_ref_strict.mockstream_dop853(c["pot"], **a)
+        np.testing.assert_array_equal(stat_o, stat_r)
+        assert np.all(stat_o[c["nstream"] > 0] == 1)
+        np.testing.assert_array_equal(st_o, st_r)
+        np.testing.assert_array_equal(nb_o, nb_r)
+
+
+def test_mockstream_release_every_matches_gala(oracle, gala_ref_strict):
+    """Releases every 3rd step, 2 particles per tail: the bodies are
+    re-integrated on the coarser release grid (h0 = 3 dt)."""
+    c = stream_case(n_streams=1, n_steps=90, n_per_tail=2, release_every=3)
+    a = _stream_args(c, 0)
+    nb_o, st_o, stat_o = oracle.mockstream_dop853(c["pot"], **a)
+    nb_r, st_r, stat_r = gala_ref_strict.mockstream_dop853(c["pot"], **a)
+    np.testing.assert_array_equal(st_o, st_r)
+    np.testing.assert_array_equal(nb_o, nb_r)
+    np.testing.assert_array_equal(stat_o, stat_r)
+
+
+def test_mockstream_systems_match_per_stream(oracle):
+    """The batched release-system layout equals gala's per-stream loop."""
+    c = stream_case(n_streams=3, n_steps=80)
+    rel = c["rel"]
+    nbody_w = c["orbits"][:, rel]  # (S, n_release, 1, 6)
+    t = c["t"]
+    out, nb_out, status, stats = oracle.mockstream_systems(
+        c["pot"], c["bodies"], nbody_w, t[rel], c["nstream"], c["stream_w0"], t[-1], t[rel][1] - t[rel][0],
+        nthreads=4)
+    for s in range(3):
+        nb_o, st_o, stat_o = oracle.mockstream_dop853(c["pot"], **_stream_args(c, s))
+        np.testing.assert_array_equal(out[s], st_o)
+        np.testing.assert_array_equal(nb_out[s], nb_o)
+        np.testing.assert_array_equal(status[s], stat_o)
+    assert np.all(stats[status == 1][:, 2] > 0)
+
+
+def test_d2_dr2_matches_gala(oracle, gala_ref_strict):
+    q = W.mw_ics(32, seed=5)[:3].T.copy()
+    mw = W.mw_composite()
+    np.testing.assert_array_equal(oracle.d2_dr2(mw, q), gala_ref_strict.d2_dr2(mw, q))
+
+
+def test_fardal_sample_geometry(oracle):
+    """Each released particle sits at (kx rj, 0, kz rj) in the progenitor's
+    rotating frame (x along r, z along L), trailing at +rj and leading at -rj,
+    with r_J = (G m / (Omega^2 - d2Phi/dr2))^(1/3) (df.pyx:61-92, 410-450)."""
+    mw = W.mw_composite()
+    w = W.mw_ics(5, seed=8).T.copy()
+    t = np.arange(5.0)
+    m = np.full(5, 3e5)
+    counts = np.full(5, 2)
+    offset = np.concatenate([[0], np.cumsum(2 * counts)])
+    draws = np.random.default_rng(1).normal([2, 0, 0.3, 0], 0.5, size=(int(offset[-1]), 4))
+    out = oracle.fardal_sample(mw, w, m, t, offset, draws, g.units.G)
+    d2 = oracle.d2_dr2(mw, w[:, :3])
+    for i in range(5):
+        x, v = w[i, :3], w[i, 3:]
+        L = np.cross(x, v)
+        Om = np.linalg.norm(L) / np.dot(x, x)
+        rj = (g.units.G * m[i] / (Om * Om - d2[i])) ** (1 / 3)
+        vj = Om * rj
+        e0, e2 = x / np.linalg.norm(x), L / np.linalg.norm(L)
+        e1 = -np.cross(e0, e2)
+        for k, row in enumerate(range(offset[i], offset[i + 1])):
+            sgn = 1.0 if k < 2 else -1.0
+            dx, dv = out[row, :3] - x, out[row, 3:] - v
+            kx, kz, kvt, kvz = draws[row]
+            np.testing.assert_allclose([dx @ e0, dx @ e1, dx @ e2], sgn * rj * np.array([kx, 0, kz]),
+                                       rtol=0, atol=1e-12 * rj)
+            np.testing.assert_allclose([dv @ e0, dv @ e1, dv @ e2], sgn * vj * np.array([0, kvt * kx, kvz]),
+                                       rtol=0, atol=1e-12 * vj)
+
+
+def test_mockstream_golden(oracle, golden):
+    d = golden("mockstream_dop853.npz")
+    c = stream_case(n_streams=int(d["n_streams"]), n_steps=int(d["n_steps"]))
+    np.testing.assert_array_equal(c["stream_w0"], d["stream_w0"])
+    for s in range(c["stream_w0"].shape[0]):
+        nb_o, st_o, stat_o = oracle.mockstream_dop853(c["pot"], **_stream_args(c, s))
+        np.testing.assert_array_equal(stat_o, d["status"][s])
+        scale = np.abs(d["stream"][s]).max(axis=0)
+        np.testing.assert_allclose(st_o, d["stream"][s], rtol=0, atol=OFAST_RTOL * scale.max())
+        np.testing.assert_allclose(nb_o, d["nbody"][s], rtol=OFAST_RTOL, atol=0)
+
+
+def test_nbody_golden(oracle, golden):
+    d = golden("nbody_dop853.npz")
+    mw, bodies, w0, t = _nbody_system()
+    np.testing.assert_array_equal(w0, d["w0"])
+    w_o, res = oracle.nbody_dop853(mw, bodies, 2, w0, t)
+    assert res == 1
+    np.testing.assert_allclose(w_o[::50], d["w"], rtol=OFAST_RTOL, atol=OFAST_RTOL * np.abs(d["w"]).max())
+
+
+@pytest.mark.parametrize("bad", ["scf_body"])
+def test_unsupported_body_types_raise(bad):
+    with pytest.raises(NotImplementedError):
+        pack_bodies([W.scf_potential(nmax=2, lmax=1)])

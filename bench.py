@@ -53,7 +53,8 @@ def parse_args():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gx", choices=["gx", "reference"])
-    p.add_argument("--workload", default="mw_dop853", choices=["mw_dop853", "uneven_batch", "scf_surrogate"],
+    p.add_argument("--workload", default="mw_dop853",
+                   choices=["mw_dop853", "uneven_batch", "scf_surrogate", "mock_streams"],
                    help="mw_dop853: the headline line; uneven_batch / scf_surrogate: only that variant "
                         "(used for profiling)")
     p.add_argument("--batch-orbits", type=int, default=262_144)
@@ -64,6 +65,10 @@ def parse_args():
     p.add_argument("--no-surrogate", action="store_true", help="skip the SCF surrogate variant")
     p.add_argument("--surrogate-orbits", type=int, default=262_144)
     p.add_argument("--surrogate-nsteps", type=int, default=5000)
+    p.add_argument("--no-streams", action="store_true", help="skip the mock-stream variant")
+    p.add_argument("--stream-progenitors", type=int, default=512)
+    p.add_argument("--stream-nsteps", type=int, default=2000)
+    p.add_argument("--stream-cpu-streams", type=int, default=8, help="streams in the CPU-baseline sample")
     p.add_argument("--orbits", type=int, default=100_000)
     p.add_argument("--nsteps", type=int, default=10_000)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -347,6 +352,151 @@ def run_scf_surrogate(args, torch, stream):
     }
 
 
+# FP64 work of one release-system right-hand side, per body: the MW composite
+# Hamiltonian (F_RHS_MW) and, for released particles, the progenitor's shifted
+# Plummer pull (3 subtractions, 17 flops of plummer_gradient, 3 additions).
+F_PLUMMER_PULL = 3 + 17 + 3
+F_STIFF_PER_COMP = 6                # stiffness sums per component per accepted step
+
+
+def run_mock_streams(args, torch, stream):
+    """Mock streams: 512 Plummer progenitors (m ~ U[1e4, 1e6] Msun, b ~ U[5, 20]
+    pc) on MW-composite disk orbits, FardalStreamDF releasing 1 particle per tail
+    at every one of the 2001 times of dt = 1 Myr, n_steps = 2000; DOPRI853 with
+    gala's defaults (atol = rtol = 1e-10) and err_if_fail = 0 (gala's stiffness
+    exit stops ~1% of release systems in its own arithmetic).  Metric:
+    particle-steps/s = sum over stream particles of (t_final - t_release) / dt per
+    second.  Timed: the whole pipeline (progenitor n-body integration, release
+    sampling incl. the host draws, release systems) and, separately, the
+    release-system kernel alone; end to end through run_batch with host arrays."""
+    from gala_gb300 import _abi
+    from gala_gb300 import workloads as W
+    from gala_gb300._device import ptr
+    from gala_gb300.mockstream import FardalStreamDF, MockStreamGenerator
+
+    S, nsteps = args.stream_progenitors, args.stream_nsteps
+    pot = W.mw_composite()
+    w0, m, b = W.stream_progenitors(S)
+    pots = W.stream_progenitor_potentials(m, b)
+    kw = dict(err_if_fail=0)
+
+    def gen(seed=1):
+        return MockStreamGenerator(FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(seed)),
+                                   pot)
+
+    # warm-up on a slice (kernel load, autotuned nothing)
+    gen().run_batch(w0[:, :16], m[:16], progenitor_potentials=pots[:16], dt=1.0, n_steps=min(nsteps, 200),
+                    Integrator_kwargs=kw)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    res = gen().run_batch(w0, m, progenitor_potentials=pots, dt=1.0, n_steps=nsteps, Integrator_kwargs=kw,
+                          return_stats=True)
+    e1.record(stream)
+    e1.synchronize()
+    ms_pipe = e0.elapsed_time(e1)
+    n_rows = int(res.stream_w.shape[1])
+    t_final = float(res.t[-1])
+    particle_steps = S * float(np.sum(np.round(t_final - res.release_time)))
+    status = res.status.cpu().numpy()
+    stats = res.stats.cpu().numpy()
+
+    # the release-system kernel alone, inputs resident in HBM (bodies on the
+    # release grid = the progenitor orbits, release states from the run above)
+    import gala_gb300 as g
+    from gala_gb300.nbody import bodies_to_device, integrate_systems, pack_bodies
+
+    t = g.parse_time_specification(dt=1.0, n_steps=nsteps)
+    bodies = pack_bodies([[p] for p in pots]).reshape(S, 1)
+    orbit, _ = integrate_systems(pot, bodies, np.ascontiguousarray(w0.T.reshape(S, 1, 6)), t, nstiff=-1)
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(1))
+    counts = df.release_counts(len(t))
+    sw0, _, _, _ = df.sample_device(pot, orbit.reshape(S, len(t), 6), t, np.repeat(m[:, None], len(t), 1), counts)
+    off = torch.from_numpy(np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)).cuda()
+    td = torch.from_numpy(t).cuda()
+    bd = bodies_to_device(bodies, "cuda")
+    out = torch.empty_like(sw0)
+    nb_out = torch.empty((S, 1, 6), dtype=torch.float64, device="cuda")
+    st_k = torch.zeros((S, len(t)), dtype=torch.int32, device="cuda")
+    counter = torch.zeros(1, dtype=torch.int64, device="cuda")
+    H = g.Hamiltonian(pot)
+    desc = pot.packed().for_device()
+
+    def release_kernel():
+        _abi.call("gx_mockstream_dop853", desc, H._frame_ref(), S, 1, ptr(bd), ptr(orbit), len(t), ptr(td), ptr(off),
+                  2, ptr(sw0), n_rows, t_final, 1.0, 1e-10, 1e-10, 0, ptr(out), ptr(nb_out), ptr(st_k), None,
+                  ptr(counter), int(stream.cuda_stream))
+
+    e0.record(stream)
+    release_kernel()
+    e1.record(stream)
+    e1.synchronize()
+    ms_rel = e0.elapsed_time(e1)
+    same = bool(torch.equal(out, res.stream_w))
+
+    # algorithmic FP64 work of the release systems, from gala's counters
+    nsys_p = 2
+    flops = float(np.sum(stats[..., 0]) * (F_RHS_MW * (1 + nsys_p) + F_PLUMMER_PULL * nsys_p) +
+                  np.sum(stats[..., 1]) * 6 * (1 + nsys_p) * (F_STEP_PER_ORBIT // 6) +
+                  np.sum(stats[..., 2]) * 6 * (1 + nsys_p) * F_STIFF_PER_COMP)
+
+    # end to end through the public API: host numpy in, host arrays out
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    r2 = gen().run_batch(w0, m, progenitor_potentials=pots, dt=1.0, n_steps=nsteps, Integrator_kwargs=kw)
+    host_stream = r2.stream_w.cpu().numpy()
+    host_nbody = r2.nbody_w.cpu().numpy()
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+
+    result = {
+        "workload": f"mock_streams: {S} Plummer progenitors on MW-composite disk orbits, FardalStreamDF 1 particle "
+                    f"per tail per step, dt 1 Myr, {nsteps} steps, DOPRI853 atol=rtol=1e-10, err_if_fail=0",
+        "particles": S * n_rows,
+        "particle_steps": particle_steps,
+        "pipeline": {"value": particle_steps / (ms_pipe * 1e-3), "unit": "particle-steps/s", "ms": ms_pipe,
+                     "gpu_launches": 3},
+        "release_kernel": {"value": particle_steps / (ms_rel * 1e-3), "unit": "particle-steps/s", "ms": ms_rel,
+                           "matches_pipeline_output": same,
+                           "roofline": {"bound": "fp64", "achieved": flops / (ms_rel * 1e-3) / 1e12,
+                                        "unit": "TFLOP/s", "work": "algorithmic FP64 flops from the per-system "
+                                        "nfcn/nstep/naccpt counters"}},
+        "e2e": {"value": particle_steps / (e2e_ms * 1e-3), "unit": "particle-steps/s", "ms": e2e_ms,
+                "h2d_bytes": int(w0.nbytes + m.nbytes + S * n_rows * 4 * 8),
+                "d2h_bytes": int(host_stream.nbytes + host_nbody.nbytes)},
+        "release_systems": {"count": int(np.sum(status != 0)), "stiff_exit_fraction": float(np.mean(status[status != 0] == -4)),
+                            "accepted_steps": int(np.sum(stats[..., 2])), "rejected_steps": int(np.sum(stats[..., 3]))},
+    }
+
+    if not args.no_cpu_baseline:
+        from oracle import Oracle
+        from oracle.oracle import host_threads
+
+        ns = min(args.stream_cpu_streams, S)
+        fast = Oracle("fast")
+        nth = host_threads()
+        nbody_w = orbit[:ns].cpu().numpy()
+        sw_host = sw0[:ns].cpu().numpy()
+        t0 = time.perf_counter()
+        cpu_out, _, cpu_status, _ = fast.mockstream_systems(pot, bodies[:ns], nbody_w, t, 2 * counts, sw_host,
+                                                            t_final, 1.0, nthreads=nth)
+        cpu_s = time.perf_counter() - t0
+        gpu_o = out[:ns].cpu().numpy()
+        gpu_st = st_k[:ns].cpu().numpy()
+        ok = np.repeat((gpu_st == 1) & (cpu_status == 1), 2, axis=1)
+        pe = np.linalg.norm(gpu_o[..., :3] - cpu_out[..., :3], axis=-1)[ok]
+        result["cpu_baseline"] = {
+            "value": ns * float(np.sum(np.round(t_final - res.release_time))) / cpu_s,
+            "unit": "particle-steps/s", "cores": nth, "kind": "port",
+            "sample": f"release systems of {ns} of the {S} streams (same inputs), gala's dop853_step loop restated "
+                      f"in C, -Ofast, {nth} threads",
+            "seconds": cpu_s,
+            "status_agreement": float(np.mean(gpu_st == cpu_status)),
+            "position_diff_kpc_median": float(np.median(pe)) if pe.size else None,
+            "position_diff_kpc_p99": float(np.percentile(pe, 99)) if pe.size else None,
+        }
+    return result
+
+
 def run_gx(args):
     import torch
 
@@ -363,8 +513,9 @@ def run_gx(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
     sh = int(stream.cuda_stream)
-    if args.workload in ("uneven_batch", "scf_surrogate"):
-        fn = run_uneven_batch if args.workload == "uneven_batch" else run_scf_surrogate
+    if args.workload in ("uneven_batch", "scf_surrogate", "mock_streams"):
+        fn = {"uneven_batch": run_uneven_batch, "scf_surrogate": run_scf_surrogate,
+              "mock_streams": run_mock_streams}[args.workload]
         res = fn(args, torch, stream)
         if rank == 0:
             print(json.dumps(res), flush=True)
@@ -456,6 +607,8 @@ def run_gx(args):
     variants = {"uneven_batch": run_uneven_batch(args, torch, stream)}
     if not args.no_surrogate:
         variants["scf_surrogate"] = run_scf_surrogate(args, torch, stream)
+    if not args.no_streams:
+        variants["mock_streams"] = run_mock_streams(args, torch, stream)
 
     if rank != 0:
         return

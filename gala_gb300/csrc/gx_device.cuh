@@ -62,6 +62,16 @@ __device__ __forceinline__ double norm3_sq(const double *q) {
     return q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
 }
 
+// Powers in the gradients.  gala calls pow(x, -1.5) (Miyamoto-Nagai) and
+// pow(r, 3.0) (Kepler).  The FP64 pow of CUDA runs an extended-precision log
+// and exp, a hundred-odd instructions on the FP64 pipe, whose rate on this part
+// is 1/64 of FP32.  1 / (x sqrt(x)) is correctly rounded in each of its three
+// operations (within 1.5 ulp of x^-1.5) and r r r within 1 ulp of r^3: the
+// accuracy class of pow itself, which does not round like the host's pow
+// either.  Edge values match pow: 0 -> inf, inf -> 0, NaN -> NaN.
+__device__ __forceinline__ double pow_m1p5(double x) { return 1.0 / (x * sqrt(x)); }
+__device__ __forceinline__ double cube(double r) { return r * r * r; }
+
 // Parameters of component ci as a plain pointer: inline ones are read from the
 // kernel-parameter copy, SCF blocks from global memory.
 #define GX_PARAM(pot, ci, k) ((pot).c[ci].inl ? (pot).p[(pot).c[ci].poff + (k)] : (pot).pdev[(pot).c[ci].poff + (k)])
@@ -130,7 +140,7 @@ __device__ __forceinline__ void comp_gradient(const DevPot &pot, int ci, const d
     case GX_POT_NULL:
         return;
     case GX_POT_KEPLER:
-        fac = P(0) * P(1) / pow(sqrt(norm3_sq(q)), 3.0);
+        fac = P(0) * P(1) / cube(sqrt(norm3_sq(q)));
         break;
     case GX_POT_HERNQUIST: {
         const double r = sqrt(norm3_sq(q));
@@ -145,7 +155,7 @@ __device__ __forceinline__ void comp_gradient(const DevPot &pot, int ci, const d
     case GX_POT_MIYAMOTONAGAI: {
         const double sqrtz = sqrt(q[2] * q[2] + P(3) * P(3));
         const double zd = P(2) + sqrtz;
-        fac = P(0) * P(1) * pow(q[0] * q[0] + q[1] * q[1] + zd * zd, -1.5);
+        fac = P(0) * P(1) * pow_m1p5(q[0] * q[0] + q[1] * q[1] + zd * zd);
         g[0] = g[0] + fac * q[0];
         g[1] = g[1] + fac * q[1];
         g[2] = g[2] + fac * q[2] * (1. + P(2) / sqrtz);

@@ -214,7 +214,7 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
 
         // computation of hnew (:446-452)
         const double fac11 = pow(err, expo1);
-        double fac = fac11 / pow(facold, beta);
+        double fac = fac11;  // gala divides by pow(facold, beta) == 1 for its beta = 0
         fac = max_d(facc2, min_d(facc1, fac / safe));
         double hnew = h / fac;
 

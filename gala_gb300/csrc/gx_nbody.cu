@@ -84,7 +84,7 @@ __device__ __forceinline__ void body_gradient(int type, const double *__restrict
     double fac;
     switch (type) {
     case GX_POT_KEPLER:
-        fac = G * m / pow(sqrt(x * x + y * y + z * z), 3.0);
+        fac = G * m / cube(sqrt(x * x + y * y + z * z));
         break;
     case GX_POT_HERNQUIST: {
         const double c = __ldg(P + 2);
@@ -102,7 +102,7 @@ __device__ __forceinline__ void body_gradient(int type, const double *__restrict
         const double a = __ldg(P + 2), b = __ldg(P + 3);
         const double sqrtz = sqrt(z * z + b * b);
         const double zd = a + sqrtz;
-        fac = G * m * pow(x * x + y * y + zd * zd, -1.5);
+        fac = G * m * pow_m1p5(x * x + y * y + zd * zd);
         g[0] = 0. + fac * x;
         g[1] = 0. + fac * y;
         g[2] = 0. + fac * z * (1. + a / sqrtz);
@@ -440,7 +440,8 @@ nbody_dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
 
             // computation of hnew (:446-452)
             const double fac11 = pow(err, expo1);
-            double fac = fac11 / pow(facold, beta);
+            double fac = fac11;  // gala divides by pow(facold, beta) == 1 for its beta = 0
+            (void)facold;
             fac = nb_max(facc2, nb_min(facc1, fac / safe));
             double hnew = h / fac;
             const bool acc = err <= 1.0;

@@ -448,6 +448,40 @@ def run_mock_streams(args, torch, stream):
     host_nbody = r2.nbody_w.cpu().numpy()
     e2e_ms = (time.perf_counter() - t0) * 1e3
 
+    # gala's Leapfrog form of the same streams (mockstream_leapfrog): the FP64
+    # release kernel (gala's arithmetic) and its FP32-compensated form, inputs
+    # resident in HBM (progenitor Leapfrog orbits, release states)
+    from gala_gb300.nbody import integrate_systems_leapfrog
+
+    orbit_lf = integrate_systems_leapfrog(pot, bodies, np.ascontiguousarray(w0.T.reshape(S, 1, 6)), t)
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(1))
+    sw_lf, _, _, _ = df.sample_device(pot, orbit_lf.reshape(S, len(t), 6), t, np.repeat(m[:, None], len(t), 1),
+                                      counts)
+    lf_out = {}
+    lf_ms = {}
+    for name in ("gx_mockstream_leapfrog", "gx_mockstream_leapfrog_fp32"):
+        o = torch.empty_like(sw_lf)
+        st_lf = torch.zeros((S, len(t)), dtype=torch.int32, device="cuda")
+
+        def lf_call():
+            _abi.call(name, desc, S, 1, ptr(bd), ptr(orbit_lf), len(t), ptr(td), ptr(off), 2, ptr(sw_lf), n_rows,
+                      t_final, 1.0, ptr(o), ptr(nb_out), ptr(st_lf), int(stream.cuda_stream))
+
+        lf_call()  # warm-up (module load)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        lf_call()
+        e1.record(stream)
+        e1.synchronize()
+        lf_ms[name] = e0.elapsed_time(e1)
+        lf_out[name] = o.cpu().numpy()
+    o64, o32 = lf_out["gx_mockstream_leapfrog"], lf_out["gx_mockstream_leapfrog_fp32"]
+    perr = (np.linalg.norm(o32[..., :3] - o64[..., :3], axis=-1) /
+            np.linalg.norm(o64[..., :3], axis=-1)).ravel()
+    # FP64 work of a Leapfrog release system per step: 3 bodies x (MW gradient +
+    # 6 drift + 12 kick flops) + 2 progenitor pulls
+    lf_flops = S * float(np.sum(np.round(t_final - t))) * (3 * (F_RHS_MW - 6 + 18) + 2 * F_PLUMMER_PULL)
+
     result = {
         "workload": f"mock_streams: {S} Plummer progenitors on MW-composite disk orbits, FardalStreamDF 1 particle "
                     f"per tail per step, dt 1 Myr, {nsteps} steps, DOPRI853 atol=rtol=1e-10, err_if_fail=0",
@@ -465,6 +499,19 @@ def run_mock_streams(args, torch, stream):
                 "d2h_bytes": int(host_stream.nbytes + host_nbody.nbytes)},
         "release_systems": {"count": int(np.sum(status != 0)), "stiff_exit_fraction": float(np.mean(status[status != 0] == -4)),
                             "accepted_steps": int(np.sum(stats[..., 2])), "rejected_steps": int(np.sum(stats[..., 3]))},
+        "leapfrog": {
+            "fp64_release_kernel": {"value": particle_steps / (lf_ms["gx_mockstream_leapfrog"] * 1e-3),
+                                    "unit": "particle-steps/s", "ms": lf_ms["gx_mockstream_leapfrog"],
+                                    "roofline": {"bound": "fp64", "unit": "TFLOP/s",
+                                                 "achieved": lf_flops / (lf_ms["gx_mockstream_leapfrog"] * 1e-3)
+                                                 / 1e12}},
+            "fp32c_release_kernel": {"value": particle_steps / (lf_ms["gx_mockstream_leapfrog_fp32"] * 1e-3),
+                                     "unit": "particle-steps/s", "ms": lf_ms["gx_mockstream_leapfrog_fp32"]},
+            "speedup_fp32c_vs_fp64": lf_ms["gx_mockstream_leapfrog"] / lf_ms["gx_mockstream_leapfrog_fp32"],
+            "fp32c_position_error_vs_fp64": {"median": float(np.median(perr)),
+                                             "p90": float(np.percentile(perr, 90)),
+                                             "p99": float(np.percentile(perr, 99))},
+        },
     }
 
     if not args.no_cpu_baseline:

@@ -27,8 +27,10 @@ UNITS = {
     "gx_fixed.cu": ["-fmad=false"],
     "gx_dop853.cu": ["-fmad=false"],
     "gx_nbody.cu": ["-fmad=false"],
+    "gx_lfnbody.cu": ["-fmad=false"],
     "gx_peaks.cu": [],
     "gx_batch.cu": [],
+    "gx_stream32.cu": [],
     "gx_mlp_train.cu": [],
     "gx_mlp_infer.cu": [],
 }

@@ -32,6 +32,7 @@
 #include "gx_host.h"
 #include "gx_scf.cuh"
 #include "gx_dop853_tableau.cuh"
+#include "gx_body.cuh"
 
 static_assert(sizeof(gx_body) == 64, "gx_body layout");
 
@@ -71,60 +72,6 @@ struct NbArgs {
 __device__ __forceinline__ double nb_sign(double a, double b) { return (b < 0.0) ? -fabs(a) : fabs(a); }
 __device__ __forceinline__ double nb_min(double a, double b) { return (a < b) ? a : b; }
 __device__ __forceinline__ double nb_max(double a, double b) { return (a > b) ? a : b; }
-
-// Gradient of a body's potential at d = q - q0 (q0 = the body's position).
-// gala evaluates the body's CPotential with do_shift_rotate = 1 and R = I
-// (c_gradient, cpotential.cpp:214-287): q' = I d, g' = 0 + fac q', g = I^T g';
-// multiplying by the identity changes no finite value, so it is left out.
-// Component formulas: builtin_potentials.cpp (kepler :66-76, hernquist :221-233,
-// plummer :302-314, miyamotonagai :1298-1312, sphericalnfw :835-850).
-__device__ __forceinline__ void body_gradient(int type, const double *__restrict__ P, double x, double y, double z,
-                                              double *g) {
-    const double G = __ldg(P + 0), m = __ldg(P + 1);
-    double fac;
-    switch (type) {
-    case GX_POT_KEPLER:
-        fac = G * m / cube(sqrt(x * x + y * y + z * z));
-        break;
-    case GX_POT_HERNQUIST: {
-        const double c = __ldg(P + 2);
-        const double r = sqrt(x * x + y * y + z * z);
-        fac = G * m / ((r + c) * (r + c) * r);
-        break;
-    }
-    case GX_POT_PLUMMER: {
-        const double b = __ldg(P + 2);
-        const double R2b = x * x + y * y + z * z + b * b;
-        fac = G * m / sqrt(R2b) / R2b;
-        break;
-    }
-    case GX_POT_MIYAMOTONAGAI: {
-        const double a = __ldg(P + 2), b = __ldg(P + 3);
-        const double sqrtz = sqrt(z * z + b * b);
-        const double zd = a + sqrtz;
-        fac = G * m * pow_m1p5(x * x + y * y + zd * zd);
-        g[0] = 0. + fac * x;
-        g[1] = 0. + fac * y;
-        g[2] = 0. + fac * z * (1. + a / sqrtz);
-        return;
-    }
-    case GX_POT_SPHERICALNFW: {
-        const double rs = __ldg(P + 2);
-        const double v_h2 = G * m / rs;
-        const double u = sqrt(x * x + y * y + z * z) / rs;
-        fac = v_h2 / (u * u * u) / (rs * rs) * (log(1 + u) - u / (1 + u));
-        break;
-    }
-    default: {  // a type without a GPU body formula poisons the result
-        const double nan = __longlong_as_double(0x7ff8000000000000LL);
-        g[0] = nan; g[1] = nan; g[2] = nan;
-        return;
-    }
-    }
-    g[0] = 0. + fac * x;
-    g[1] = 0. + fac * y;
-    g[2] = 0. + fac * z;
-}
 
 // Fwrapper_direct_nbody for the lane's body: Hamilton's equations in the
 // external potential, then the pull of every non-null massive body j != self.
@@ -748,6 +695,7 @@ int launch_nbody(const DevPot &dp, const DevFrame &df, const NbArgs &A, cudaStre
         nbody_dop853_kernel<STREAM, DENSE, false><<<(unsigned)grid, NB_THREADS, 0, st>>>(dp, df, A);
     return check_launch(STREAM ? "mockstream_dop853" : "nbody_dop853");
 }
+
 
 }  // namespace gx
 

@@ -11,7 +11,12 @@ The generator follows gala's MockStreamGenerator.run
    numpy random state in gala's order);
 3. mockstream_dop853 (mockstream.pyx:176-303): the bodies are integrated again
    on the release grid, then every release time's system [bodies, particles
-   released then] is integrated to the final time (gx_mockstream_dop853).
+   released then] is integrated to the final time (gx_mockstream_dop853); or
+   mockstream_leapfrog (mockstream.pyx:442-610): the bodies' Leapfrog trajectory
+   on the full grid gives their state at each release time, and every release
+   system takes round((t_final - t_release) / dt) Leapfrog steps
+   (gx_mockstream_leapfrog, or its FP32-compensated form with
+   ``precision="fp32c"``).
 
 ``run`` makes one stream with gala's signature and return values.
 ``run_batch`` makes many independent streams (one progenitor each, all on one
@@ -27,8 +32,8 @@ import numpy as np
 from . import _abi
 from .dynamics import PhaseSpacePosition
 from .hamiltonian import Hamiltonian, StaticFrame
-from .integrate import DOPRI853Integrator, get_integrator, parse_time_specification
-from .nbody import DirectNBody, bodies_to_device, integrate_systems, pack_bodies
+from .integrate import DOPRI853Integrator, LeapfrogIntegrator, get_integrator, parse_time_specification
+from .nbody import DirectNBody, bodies_to_device, integrate_systems, integrate_systems_leapfrog, pack_bodies
 from .potential import PotentialBase
 
 __all__ = ["MockStream", "BaseStreamDF", "FardalStreamDF", "MockStreamGenerator", "MockStreamBatch"]
@@ -275,7 +280,8 @@ class MockStreamGenerator:
         return dict(atol=float(kw.get("atol", 1e-10)), rtol=float(kw.get("rtol", 1e-10)),
                     nmax=int(kw.get("nmax", 0)), dt_max=float(kw.get("dt_max", 0.0))), err_if_fail
 
-    def _generate(self, bodies, body_w0, prog_m, t, counts, dop, err_if_fail, return_stats=False, stream=None):
+    def _generate(self, bodies, body_w0, prog_m, t, counts, dop, err_if_fail, return_stats=False, stream=None,
+                  integrator="dop853", precision="fp64"):
         """The three stages for n_streams systems.
 
         bodies  : BODY_DTYPE (S, nb), progenitor first, massive bodies before null ones
@@ -301,9 +307,16 @@ class MockStreamGenerator:
             if bad.size and err_if_fail == 1:
                 raise RuntimeError(f"Integration failed with code {int(bad[0])}")
 
+        leapfrog = integrator == "leapfrog"
+        if precision not in ("fp64", "fp32c") or (precision == "fp32c" and not leapfrog):
+            raise ValueError("precision must be 'fp64', or 'fp32c' with the Leapfrog integrator")
+
         # 1. the bodies over the requested grid (DirectNBody.integrate_orbit)
-        orbit, st = integrate_systems(H, bodies, body_w0, t, save_all=True, nstiff=-1, stream=stream, **dop)
-        check(st, "nbody")
+        if leapfrog:
+            orbit = integrate_systems_leapfrog(H, bodies, body_w0, t, save_all=True, stream=stream)
+        else:
+            orbit, st = integrate_systems(H, bodies, body_w0, t, save_all=True, nstiff=-1, stream=stream, **dop)
+            check(st, "nbody")
         forward = not (t[1] < t[0])
         if forward:
             orbit_t = t
@@ -327,13 +340,16 @@ class MockStreamGenerator:
         nstream = (ntail * counts[rel_idx]).astype(np.int64)
         rel_off = np.concatenate([[0], np.cumsum(nstream)]).astype(np.int64)
         n_rows = int(rel_off[-1])
+        max_per = int(nstream.max()) if nstream.size else 0
+        if leapfrog:
+            return self._release_leapfrog(bodies, orbit, nbody0, orbit_t, forward, time, nstream, rel_off, n_rows,
+                                          max_per, stream_w0, release_time, lead_trail, precision, stream)
         if forward and len(rel_idx) == len(orbit_t):
             nbody_w = orbit  # the same dop853_helper call on the same grid (mockstream.pyx:245-255)
         else:
             nbody_w, st = integrate_systems(H, bodies, nbody0, time, save_all=True, nstiff=-1, stream=stream,
                                             **dop)
             check(st, "nbody")
-        max_per = int(nstream.max()) if nstream.size else 0
         if nb + max_per > 32:
             raise NotImplementedError(f"{nb} bodies + {max_per} particles per release exceed the 32-lane system")
         n_rel = len(time)
@@ -352,13 +368,50 @@ class MockStreamGenerator:
         check(status, "stream")
         return MockStreamBatch(stream_out, nbody_out, release_time, lead_trail, status, stats, H.frame, orbit_t)
 
+    def _release_leapfrog(self, bodies, orbit, nbody0, orbit_t, forward, time, nstream, rel_off, n_rows, max_per,
+                          stream_w0, release_time, lead_trail, precision, stream):
+        """mockstream_leapfrog's release stage (mockstream.pyx:524-593)."""
+        import torch
+
+        from ._device import ptr, stream_handle
+
+        H = self.hamiltonian
+        S, nb = bodies.shape
+        dev = orbit.device
+        if nb + max_per > 8:
+            raise NotImplementedError(f"{nb} bodies + {max_per} particles per release exceed the 8-body system")
+        # the bodies' trajectory on the full grid; the same call as stage 1 when the grid runs forwards
+        traj = orbit if forward else integrate_systems_leapfrog(H, bodies, nbody0, orbit_t, save_all=True,
+                                                                stream=stream)
+        dt = float(orbit_t[1] - orbit_t[0])
+        idx = np.trunc((time - orbit_t[0]) / dt + 0.5).astype(np.int64)  # mockstream.pyx:537
+        nbody_w = traj[:, torch.from_numpy(idx).to(dev)].contiguous()
+        n_rel = len(time)
+        stream_out = torch.empty((S, n_rows, 6), dtype=torch.float64, device=dev)
+        nbody_out = torch.empty((S, nb, 6), dtype=torch.float64, device=dev)
+        status = torch.zeros((S, n_rel), dtype=torch.int32, device=dev)
+        bd = bodies_to_device(bodies, dev)
+        td = torch.from_numpy(np.ascontiguousarray(time)).to(dev)
+        od = torch.from_numpy(rel_off).to(dev)
+        name = "gx_mockstream_leapfrog" if precision == "fp64" else "gx_mockstream_leapfrog_fp32"
+        _abi.call(name, H.potential.packed().for_device(), S, nb, ptr(bd), ptr(nbody_w), n_rel, ptr(td), ptr(od),
+                  max_per, ptr(stream_w0), n_rows, float(orbit_t[-1]), dt, ptr(stream_out), ptr(nbody_out),
+                  ptr(status), stream_handle(stream))
+        res = status.cpu().numpy()
+        if np.any(res < 0):
+            raise RuntimeError(f"release systems rejected: {int(np.sum(res < 0))}")
+        return MockStreamBatch(stream_out, nbody_out, release_time, lead_trail, status, None, H.frame, orbit_t)
+
     def run(self, prog_w0, prog_mass, nbody=None, release_every=1, n_particles=1, output_every=None,
             output_filename=None, check_filesize=True, overwrite=False, progress=False, Integrator=None,
             Integrator_kwargs=None, **time_spec):
         """One mock stream; returns (stream MockStream, nbody PhaseSpacePosition) (:119-372)."""
         Integrator = get_integrator(DOPRI853Integrator if Integrator is None else Integrator)
-        if Integrator is not DOPRI853Integrator:
-            raise NotImplementedError("GPU mock streams are implemented for DOPRI853Integrator")
+        if Integrator not in (DOPRI853Integrator, LeapfrogIntegrator):
+            raise ValueError("Currently, only the DOPRI853Integrator and LeapfrogIntegrator are supported for mock "
+                             "stream generation.")
+        kw_in = dict(Integrator_kwargs or {})
+        precision = kw_in.pop("precision", "fp64")
         if output_every is not None:
             raise NotImplementedError("snapshot output (output_every / HDF5) is not implemented")
         t = np.ascontiguousarray(parse_time_specification(self.hamiltonian.units, **time_spec), dtype=np.float64)
@@ -371,12 +424,14 @@ class MockStreamGenerator:
         m = np.squeeze(np.asarray(getattr(prog_mass, "value", prog_mass), dtype=np.float64))
         m = np.full(len(t), float(m)) if m.shape == () else m
         counts = self.df.release_counts(len(t), release_every, n_particles)
-        dop, err_if_fail = self._dop_kwargs(Integrator_kwargs)
-        res = self._generate(bodies, prog_nbody._c_w0.reshape(1, nb, 6), m[None, :], t, counts, dop, err_if_fail)
+        dop, err_if_fail = self._dop_kwargs(kw_in if Integrator is DOPRI853Integrator else {})
+        res = self._generate(bodies, prog_nbody._c_w0.reshape(1, nb, 6), m[None, :], t, counts, dop, err_if_fail,
+                             integrator="leapfrog" if Integrator is LeapfrogIntegrator else "dop853",
+                             precision=precision)
         return res.stream(0), res.nbody(0)
 
     def run_batch(self, prog_w0, prog_mass, progenitor_potentials=None, release_every=1, n_particles=1,
-                  Integrator_kwargs=None, return_stats=False, stream=None, **time_spec):
+                  Integrator=None, Integrator_kwargs=None, return_stats=False, stream=None, **time_spec):
         """Many independent streams on one time grid (no extra bodies).
 
         prog_w0  : (6, S) progenitor phase-space positions (numpy)
@@ -403,7 +458,13 @@ class MockStreamGenerator:
                 raise ValueError("prog_mass must have one entry per stream")
             m = np.repeat(m[:, None], len(t), axis=1)
         counts = self.df.release_counts(len(t), release_every, n_particles)
-        dop, err_if_fail = self._dop_kwargs(Integrator_kwargs)
+        Integrator = get_integrator(DOPRI853Integrator if Integrator is None else Integrator)
+        if Integrator not in (DOPRI853Integrator, LeapfrogIntegrator):
+            raise ValueError("only DOPRI853Integrator and LeapfrogIntegrator are supported for mock streams")
+        kw_in = dict(Integrator_kwargs or {})
+        precision = kw_in.pop("precision", "fp64")
+        dop, err_if_fail = self._dop_kwargs(kw_in if Integrator is DOPRI853Integrator else {})
         body_w0 = np.ascontiguousarray(w0.T.reshape(S, 1, 6))
         return self._generate(bodies, body_w0, m, t, counts, dop, err_if_fail, return_stats=return_stats,
-                              stream=stream)
+                              stream=stream, integrator="leapfrog" if Integrator is LeapfrogIntegrator else "dop853",
+                              precision=precision)

@@ -3,9 +3,11 @@
 ``DirectNBody`` keeps gala's constructor and ``integrate_orbit``
 (src/gala/dynamics/nbody/core.py:20-280): massive bodies are moved to the
 front, the system is integrated with DOPRI853 exactly as direct_nbody_dop853
-does (nbody.pyx:30-115: dop853_helper with Fwrapper_direct_nbody, nstiff = -1),
-and the result is put back in the input order.  ``integrate_systems`` runs many
-independent systems of the same shape in one launch (gx_nbody_dop853).
+does (nbody.pyx:30-115: dop853_helper with Fwrapper_direct_nbody, nstiff = -1)
+or with Leapfrog as leapfrog_integrate_nbody does (leapfrog.pyx:161-255), and
+the result is put back in the input order.  ``integrate_systems`` /
+``integrate_systems_leapfrog`` run many independent systems of the same shape in
+one launch (gx_nbody_dop853 / gx_nbody_leapfrog).
 
 Particle potentials must be single, unrotated components of the types the GPU
 body kernel evaluates (Null, Kepler, Hernquist, Plummer, Miyamoto-Nagai,
@@ -18,10 +20,11 @@ import numpy as np
 from . import _abi
 from .dynamics import Orbit, PhaseSpacePosition
 from .hamiltonian import Hamiltonian, StaticFrame
-from .integrate import DOPRI853Integrator, get_integrator, parse_time_specification
+from .integrate import DOPRI853Integrator, LeapfrogIntegrator, get_integrator, parse_time_specification
 from .potential import NullPotential, PotentialBase
 
-__all__ = ["DirectNBody", "BODY_DTYPE", "body_record", "pack_bodies", "integrate_systems"]
+__all__ = ["DirectNBody", "BODY_DTYPE", "body_record", "pack_bodies", "integrate_systems",
+           "integrate_systems_leapfrog"]
 
 # numpy mirror of gx_body (include/gala_gb300.h)
 BODY_DTYPE = np.dtype([("type", "<i4"), ("n_params", "<i4"), ("params", "<f8", (7,))])
@@ -129,6 +132,38 @@ def integrate_systems(hamiltonian, bodies, w0, t, atol=1e-10, rtol=1e-10, nmax=0
     return out, status[:ns]
 
 
+def integrate_systems_leapfrog(hamiltonian, bodies, w0, t, save_all=True, stream=None):
+    """leapfrog_integrate_nbody (leapfrog.pyx:161-255) for n_systems independent
+    systems of at most 8 bodies, the first ``bodies.shape[1]`` massive; static
+    frame.  Returns w (n_systems, ntimes, nparticles, 6) if save_all, else
+    (n_systems, nparticles, 6), as a CUDA tensor."""
+    import torch
+
+    from ._device import as_device_f64, ptr, require_cuda, stream_handle
+
+    H = hamiltonian if isinstance(hamiltonian, Hamiltonian) else Hamiltonian(hamiltonian)
+    if not isinstance(H.frame, StaticFrame):
+        raise TypeError(f"Leapfrog integration is currently only supported for StaticFrame, "
+                        f"not {H.frame.__class__.__name__}")
+    dev = require_cuda()
+    w0d = as_device_f64(w0, dev)
+    if w0d.ndim != 3 or w0d.shape[2] != 6:
+        raise ValueError(f"w0 must have shape (n_systems, nparticles, 6), got {tuple(w0d.shape)}")
+    ns, npart = int(w0d.shape[0]), int(w0d.shape[1])
+    bodies = np.asarray(bodies, dtype=BODY_DTYPE)
+    nbody = int(bodies.shape[1])
+    if not 1 <= npart <= 8:
+        raise NotImplementedError(f"Leapfrog systems of {npart} bodies: the GPU kernel takes 1 to 8")
+    t = np.ascontiguousarray(np.asarray(t, dtype=np.float64))
+    if len(t) < 2:
+        raise ValueError("ntimes must be greater than 1")
+    td = torch.from_numpy(t).to(dev)
+    bd = bodies_to_device(bodies if nbody else np.zeros((ns, 1), dtype=BODY_DTYPE), dev)
+    out = torch.empty((ns, len(t), npart, 6) if save_all else (ns, npart, 6), dtype=torch.float64, device=dev)
+    _abi.call("gx_nbody_leapfrog", H.potential.packed().for_device(), ns, npart, nbody, ptr(bd), ptr(w0d), ptr(td),
+              len(t), int(bool(save_all)), ptr(out), stream_handle(stream))
+    return out
+
 class DirectNBody:
     """Direct n-body integration of bodies with their own potentials in an
     optional external potential (gala.dynamics.nbody.DirectNBody)."""
@@ -177,25 +212,30 @@ class DirectNBody:
         if Integrator_kwargs is None:
             Integrator_kwargs = {}
         Integrator = get_integrator(DOPRI853Integrator if Integrator is None else Integrator)
-        if Integrator is not DOPRI853Integrator:
+        if Integrator not in (DOPRI853Integrator, LeapfrogIntegrator):
             raise NotImplementedError(
-                f"N-body integration on the GPU is implemented for DOPRI853Integrator, not {Integrator.__name__}")
+                f"N-body integration on the GPU is implemented for DOPRI853Integrator and LeapfrogIntegrator, "
+                f"not {Integrator.__name__}")
         t = np.ascontiguousarray(parse_time_specification(self.units, **time_spec), dtype=np.float64)
         idx, nbody = self._order()
         reorg = self._c_w0[idx]
         pps = [self.particle_potentials[i] for i in idx]
         bodies = pack_bodies([pps[:nbody]]) if nbody else np.zeros((1, 0), dtype=BODY_DTYPE)
-        kw = dict(Integrator_kwargs)
-        err_if_fail = int(kw.pop("err_if_fail", 1))
-        kw.pop("log_output", None)
-        allowed = {"atol", "rtol", "nmax", "dt_max"}
-        extra = set(kw) - allowed
-        if extra:
-            raise TypeError(f"unexpected Integrator_kwargs {sorted(extra)}")
-        out, status = integrate_systems(self.H, bodies, reorg[None], t, save_all=self.save_all, nstiff=-1, **kw)
-        res = int(status.cpu().numpy()[0])
-        if res < 0 and err_if_fail == 1:
-            raise RuntimeError(f"Integration failed with code {res}")
+        if Integrator is LeapfrogIntegrator:
+            out = integrate_systems_leapfrog(self.H, bodies, reorg[None], t, save_all=self.save_all)
+        else:
+            kw = dict(Integrator_kwargs)
+            err_if_fail = int(kw.pop("err_if_fail", 1))
+            kw.pop("log_output", None)
+            allowed = {"atol", "rtol", "nmax", "dt_max"}
+            extra = set(kw) - allowed
+            if extra:
+                raise TypeError(f"unexpected Integrator_kwargs {sorted(extra)}")
+            out, status = integrate_systems(self.H, bodies, reorg[None], t, save_all=self.save_all, nstiff=-1,
+                                            **kw)
+            res = int(status.cpu().numpy()[0])
+            if res < 0 and err_if_fail == 1:
+                raise RuntimeError(f"Integration failed with code {res}")
         undo = np.argsort(idx)
         if self.save_all:
             w = out[0][:, undo]  # (ntimes, nbodies, 6)

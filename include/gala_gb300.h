@@ -380,6 +380,46 @@ int gx_mockstream_dop853(const gx_potential* pot, const gx_frame* frame, int64_t
                          double* stream_w_out, double* nbody_w_out, int32_t* status,
                          int64_t* stats, int64_t* queue_counter, void* stream);
 
+/* DirectNBody.integrate_orbit with LeapfrogIntegrator: leapfrog_integrate_nbody
+ * (src/gala/integrate/cyintegrators/leapfrog.pyx:161-255) for n_systems
+ * independent systems of nparticles <= 8 bodies, the first `nbody` massive.  Within
+ * a step the bodies are updated in order, each feeling the others at their
+ * current positions (c_nbody_gradient_symplectic, cpotential.cpp:418-442).
+ * Static frame.  dt = t[1] - t[0] (read from the device array).
+ *   w0     DEVICE (n_systems, nparticles, 6)
+ *   w_out  DEVICE (n_systems, ntimes, nparticles, 6) if save_all else
+ *          (n_systems, nparticles, 6) */
+int gx_nbody_leapfrog(const gx_potential* pot, int64_t n_systems, int32_t nparticles,
+                      int32_t nbody, const gx_body* bodies, const double* w0, const double* t,
+                      int64_t ntimes, int32_t save_all, double* w_out, void* stream);
+
+/* The release systems of mockstream_leapfrog (src/gala/dynamics/mockstream/
+ * mockstream.pyx:442-610) for n_streams progenitor systems on one release grid:
+ * release i integrates [bodies at release i, its particles] for
+ * (int)((t_final - release_t[i]) / dt + 0.5) steps of dt.  Arguments as
+ * gx_mockstream_dop853; nbody_w holds the bodies at each release time (gala takes
+ * them from the bodies' Leapfrog trajectory on the full grid).  nbody +
+ * max_per_release <= 8.  status: 1, 0 where nothing was released, -1 for a
+ * release whose rows fall outside the particle array. */
+int gx_mockstream_leapfrog(const gx_potential* pot, int64_t n_streams, int32_t nbody,
+                           const gx_body* bodies, const double* nbody_w, int64_t n_release,
+                           const double* release_t, const int64_t* release_offset,
+                           int32_t max_per_release, const double* stream_w0,
+                           int64_t n_particles, double t_final, double dt,
+                           double* stream_w_out, double* nbody_w_out, int32_t* status,
+                           void* stream);
+
+/* The same release systems in FP32 with compensated (Kahan) positions and
+ * velocities and FP32 forces (no gala counterpart: the fast form; closed-form
+ * components only).  Identical arguments. */
+int gx_mockstream_leapfrog_fp32(const gx_potential* pot, int64_t n_streams, int32_t nbody,
+                                const gx_body* bodies, const double* nbody_w, int64_t n_release,
+                                const double* release_t, const int64_t* release_offset,
+                                int32_t max_per_release, const double* stream_w0,
+                                int64_t n_particles, double t_final, double dt,
+                                double* stream_w_out, double* nbody_w_out, int32_t* status,
+                                void* stream);
+
 /* FardalStreamDF._sample (src/gala/dynamics/mockstream/df.pyx:363-457) with
  * get_rj_vj_R (:61-92) and transform_from_sat (:94-106) for n_streams
  * progenitor orbits on one time grid; the Jacobi radius uses c_d2_dr2

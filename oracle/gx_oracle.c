@@ -1212,3 +1212,162 @@ void orc_fardal_sample(const gx_potential *pot, int64_t ntimes, const double *pr
         }
     }
 }
+
+/* ------------------------------------------------------------------------- */
+/* Leapfrog n-body and mock streams (leapfrog.pyx:126-255,                   */
+/* cpotential.cpp:418-442, mockstream.pyx:442-610)                           */
+/* ------------------------------------------------------------------------- */
+
+/* c_nbody_gradient_symplectic (cpotential.cpp:418-442): grad += the gradient of
+ * every non-null massive body j != self, shifted to body j's current position
+ * x_nbody[6 j]. */
+static void nbody_gradient_symplectic(const gx_body *bodies, int nbody, int self, const double *x_nbody,
+                                      const double *x, double *grad) {
+    for (int j = 0; j < nbody; j++) {
+        if (bodies[j].type == GX_POT_NULL || j == self) continue;
+        double f2[3];
+        body_gradient(&bodies[j], x_nbody + 6 * j, x, f2);
+        for (int k = 0; k < 3; k++) grad[k] += f2[k];
+    }
+}
+
+/* c_init_velocity_nbody (leapfrog.pyx:126-138) for body i of the AoS state w. */
+static void lf_init_nbody(const gx_potential *pot, const gx_body *bodies, int nbody, double *w, int i, double dt,
+                          double *v_half) {
+    double grad[3];
+    gradient_point(pot, w + 6 * i, grad);
+    nbody_gradient_symplectic(bodies, nbody, i, w, w + 6 * i, grad);
+    for (int k = 0; k < 3; k++) v_half[3 * i + k] = w[6 * i + 3 + k] - grad[k] * dt / 2.;
+}
+
+/* c_leapfrog_step_nbody (leapfrog.pyx:140-158) for body i: drift, gradient with
+ * the other bodies' CURRENT positions, kick. */
+static void lf_step_nbody(const gx_potential *pot, const gx_body *bodies, int nbody, double *w, int i, double dt,
+                          double *v_half) {
+    double *x = w + 6 * i, *v = x + 3, *vh = v_half + 3 * i;
+    for (int k = 0; k < 3; k++) x[k] = x[k] + vh[k] * dt;
+    double grad[3];
+    gradient_point(pot, x, grad);
+    nbody_gradient_symplectic(bodies, nbody, i, w, x, grad);
+    for (int k = 0; k < 3; k++) {
+        v[k] = vh[k] - grad[k] * dt / 2.;
+        vh[k] = vh[k] - grad[k] * dt;
+    }
+}
+
+/* leapfrog_integrate_nbody (leapfrog.pyx:161-255) on one system of n bodies,
+ * the first nbody massive: w0 (n, 6); w_out (ntimes, n, 6) if save_all else (n, 6). */
+int orc_leapfrog_nbody(const gx_potential *pot, int n, int nbody, const gx_body *bodies, const double *w0,
+                       const double *t, int64_t ntimes, int save_all, double *w_out) {
+    if (ntimes < 2 || n < 1 || nbody < 0 || nbody > n) return -1;
+    const double dt = t[1] - t[0];
+    double *w = (double *)malloc(sizeof(double) * 6 * (size_t)n);
+    double *vh = (double *)calloc(3 * (size_t)n, sizeof(double));
+    memcpy(w, w0, sizeof(double) * 6 * (size_t)n);
+    if (save_all) memcpy(w_out, w0, sizeof(double) * 6 * (size_t)n);
+    for (int i = 0; i < n; i++) lf_init_nbody(pot, bodies, nbody, w, i, dt, vh);
+    for (int64_t j = 1; j < ntimes; j++) {
+        for (int i = 0; i < n; i++) lf_step_nbody(pot, bodies, nbody, w, i, dt, vh);
+        if (save_all) memcpy(w_out + (size_t)j * 6 * (size_t)n, w, sizeof(double) * 6 * (size_t)n);
+    }
+    if (!save_all) memcpy(w_out, w, sizeof(double) * 6 * (size_t)n);
+    free(w);
+    free(vh);
+    return 0;
+}
+
+/* The release systems of mockstream_leapfrog (mockstream.pyx:548-593) for many
+ * streams sharing one release grid, the layout of orc_mockstream_systems:
+ * nbody_w (S, n_release, nb, 6) bodies at each release time; each system takes
+ * n_steps = (int)((t_final - release_t[i]) / dt + 0.5) steps of dt. */
+typedef struct {
+    const gx_potential *pot;
+    int64_t n_streams, n_release, ntot;
+    int nbodies;
+    const gx_body *bodies;
+    const double *nbody_w, *release_t, *stream_w0;
+    const int32_t *nstream;
+    const int64_t *offset;
+    double t_final, dt;
+    double *stream_w_out, *nbody_w_out;
+    int64_t last_release, sys_base;
+} mslf_ctx;
+
+static void mslf_chunk(void *vctx, int64_t lo, int64_t hi) {
+    const mslf_ctx *C = (const mslf_ctx *)vctx;
+    int maxn = 0;
+    for (int64_t i = 0; i < C->n_release; i++) maxn = C->nstream[i] > maxn ? C->nstream[i] : maxn;
+    const int nb = C->nbodies;
+    double *w = (double *)malloc(sizeof(double) * 6 * (size_t)(nb + maxn));
+    double *vh = (double *)malloc(sizeof(double) * 3 * (size_t)(nb + maxn));
+    for (int64_t sys = C->sys_base + lo; sys < C->sys_base + hi; sys++) {
+        const int64_t i = sys / C->n_streams, s = sys % C->n_streams;
+        const int np = C->nstream[i];
+        if (np == 0) continue;
+        const int nsys = nb + np;
+        const gx_body *bod = C->bodies + s * nb;
+        memcpy(w, C->nbody_w + ((size_t)(s * C->n_release + i)) * 6 * (size_t)nb, sizeof(double) * 6 * (size_t)nb);
+        memcpy(w + 6 * nb, C->stream_w0 + ((size_t)(s * C->ntot + C->offset[i])) * 6, sizeof(double) * 6 * (size_t)np);
+        for (int j = 0; j < nsys; j++) lf_init_nbody(C->pot, bod, nb, w, j, C->dt, vh);
+        const int n_steps = (int)((C->t_final - C->release_t[i]) / C->dt + 0.5);
+        for (int j = 0; j < n_steps; j++)
+            for (int k = 0; k < nsys; k++) lf_step_nbody(C->pot, bod, nb, w, k, C->dt, vh);
+        memcpy(C->stream_w_out + ((size_t)(s * C->ntot + C->offset[i])) * 6, w + 6 * nb, sizeof(double) * 6 * (size_t)np);
+        if (i == C->last_release && C->nbody_w_out)
+            memcpy(C->nbody_w_out + (size_t)s * 6 * (size_t)nb, w, sizeof(double) * 6 * (size_t)nb);
+    }
+    free(w);
+    free(vh);
+}
+
+int orc_mockstream_leapfrog_systems(const gx_potential *pot, int64_t n_streams, int nbodies, const gx_body *bodies,
+                                    const double *nbody_w, int64_t n_release, const double *release_t,
+                                    const int32_t *nstream, const double *stream_w0, double t_final, double dt,
+                                    double *stream_w_out, double *nbody_w_out, int64_t sys_lo, int64_t sys_hi,
+                                    int nthreads) {
+    if (n_streams < 1 || n_release < 1 || nbodies < 1 || dt == 0.0) return -1;
+    int64_t *offset = (int64_t *)malloc(sizeof(int64_t) * (size_t)(n_release + 1));
+    offset[0] = 0;
+    int64_t last = -1;
+    for (int64_t i = 0; i < n_release; i++) {
+        offset[i + 1] = offset[i] + nstream[i];
+        if (nstream[i] > 0) last = i;
+    }
+    if (sys_hi > n_streams * n_release) sys_hi = n_streams * n_release;
+    mslf_ctx C = {pot, n_streams, n_release, offset[n_release], nbodies, bodies, nbody_w, release_t, stream_w0,
+                  nstream, offset, t_final, dt, stream_w_out, nbody_w_out, last, sys_lo};
+    if (sys_lo < sys_hi) parallel_for(nthreads, sys_hi - sys_lo, 16, mslf_chunk, &C);
+    free(offset);
+    return 0;
+}
+
+/* mockstream_leapfrog (mockstream.pyx:442-610) for one progenitor system:
+ * the bodies are integrated over full_time (leapfrog_integrate_nbody), taken at
+ * each spawn time by index (int)((stream_t1[i] - full_time[0]) / dt + 0.5),
+ * then every release system is integrated to tfinal. */
+int orc_mockstream_leapfrog(const gx_potential *pot, int nbodies, const gx_body *bodies, const double *nbody_w0,
+                            const double *full_time, int64_t nfull, const double *stream_w0, const double *stream_t1,
+                            int64_t ntimes, double tfinal, const int32_t *nstream, double *nbody_w_final,
+                            double *stream_w_final) {
+    if (nfull < 2 || nbodies < 1) return -1;
+    const double dt = full_time[1] - full_time[0];
+    double *traj = (double *)malloc(sizeof(double) * (size_t)nfull * 6 * (size_t)nbodies);
+    orc_leapfrog_nbody(pot, nbodies, nbodies, bodies, nbody_w0, full_time, nfull, 1, traj);
+    double *nbody_w = (double *)malloc(sizeof(double) * (size_t)ntimes * 6 * (size_t)nbodies);
+    for (int64_t i = 0; i < ntimes; i++) {
+        const int idx = (int)((stream_t1[i] - full_time[0]) / dt + 0.5);
+        memcpy(nbody_w + (size_t)i * 6 * (size_t)nbodies, traj + (size_t)idx * 6 * (size_t)nbodies,
+               sizeof(double) * 6 * (size_t)nbodies);
+    }
+    int64_t total = 0;
+    for (int64_t i = 0; i < ntimes; i++) total += nstream[i];
+    double *nb_out = (double *)malloc(sizeof(double) * 6 * (size_t)nbodies);
+    int rc = orc_mockstream_leapfrog_systems(pot, 1, nbodies, bodies, nbody_w, ntimes, stream_t1, nstream, stream_w0,
+                                             tfinal, dt, stream_w_final, nb_out, 0, ntimes, 1);
+    memcpy(nbody_w_final, nb_out, sizeof(double) * 6 * (size_t)nbodies);
+    (void)total;
+    free(nb_out);
+    free(nbody_w);
+    free(traj);
+    return rc;
+}

@@ -265,6 +265,61 @@ class Oracle:
                                    C.c_double(G), C.c_int(int(lead)), C.c_int(int(trail)),
                                    C.c_int(int(gala_modified)), _p(out))
         return out
+    def leapfrog_nbody(self, pot, bodies, nbody, w0, t, save_all=True):
+        """leapfrog_integrate_nbody on one system: bodies (n,), w0 (n, 6).
+        Returns (ntimes, n, 6) or (n, 6)."""
+        b = self._bodies(bodies)
+        w0 = _f64(w0)
+        t = _f64(t)
+        n = w0.shape[0]
+        out = np.zeros((len(t), n, 6) if save_all else (n, 6))
+        fn = self.lib.ref_leapfrog_nbody if self.is_ref else self.lib.orc_leapfrog_nbody
+        rc = fn(pot.packed().for_host(), C.c_int(n), C.c_int(nbody), _p(b), _p(w0), _p(t), C.c_int64(len(t)),
+                C.c_int(int(save_all)), _p(out))
+        if rc != 0:
+            raise RuntimeError(f"leapfrog n-body oracle failed ({rc})")
+        return out
+
+    def mockstream_leapfrog(self, pot, bodies, nbody_w0, full_time, stream_w0, stream_t1, tfinal, nstream):
+        """mockstream_leapfrog for one progenitor system.  Returns
+        (nbody_w_final (nbodies, 6), stream_w_final (ntot, 6))."""
+        b = self._bodies(bodies)
+        nbody_w0 = _f64(nbody_w0)
+        full_time = _f64(full_time)
+        stream_w0 = _f64(stream_w0).reshape(-1, 6)
+        stream_t1 = _f64(stream_t1)
+        nstream = np.ascontiguousarray(np.asarray(nstream, dtype=np.int32))
+        nb = nbody_w0.shape[0]
+        nb_out = np.zeros((nb, 6))
+        st_out = np.zeros_like(stream_w0)
+        fn = self.lib.ref_mockstream_leapfrog if self.is_ref else self.lib.orc_mockstream_leapfrog
+        rc = fn(pot.packed().for_host(), C.c_int(nb), _p(b), _p(nbody_w0), _p(full_time), C.c_int64(len(full_time)),
+                _p(stream_w0), _p(stream_t1), C.c_int64(len(stream_t1)), C.c_double(tfinal), _p(nstream), _p(nb_out),
+                _p(st_out))
+        if rc != 0:
+            raise RuntimeError(f"leapfrog mockstream oracle failed ({rc})")
+        return nb_out, st_out
+
+    def mockstream_leapfrog_systems(self, pot, bodies, nbody_w, release_t, nstream, stream_w0, t_final, dt,
+                                    sys_lo=0, sys_hi=None, nthreads=1):
+        """The Leapfrog release systems of many streams (GPU layout).
+        Returns (stream_w (S, ntot, 6), nbody_w_final (S, nb, 6))."""
+        b = self._bodies(bodies)
+        nbody_w = _f64(nbody_w)
+        S, nrel, nb = nbody_w.shape[:3]
+        release_t = _f64(release_t)
+        nstream = np.ascontiguousarray(np.asarray(nstream, dtype=np.int32))
+        stream_w0 = _f64(stream_w0)
+        out = np.zeros_like(stream_w0)
+        nb_out = np.zeros((S, nb, 6))
+        hi = S * nrel if sys_hi is None else sys_hi
+        rc = self.lib.orc_mockstream_leapfrog_systems(
+            pot.packed().for_host(), C.c_int64(S), C.c_int(nb), _p(b), _p(nbody_w), C.c_int64(nrel), _p(release_t),
+            _p(nstream), _p(stream_w0), C.c_double(t_final), C.c_double(dt), _p(out), _p(nb_out), C.c_int64(sys_lo),
+            C.c_int64(hi), C.c_int(nthreads))
+        if rc != 0:
+            raise RuntimeError(f"oracle leapfrog mockstream systems failed ({rc})")
+        return out, nb_out
 
 def host_threads() -> int:
     try:

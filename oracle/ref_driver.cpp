@@ -19,7 +19,10 @@
  *     dop853_step (mockstream.pyx:176-303, dop853.pyx:27-75): gala's dop853()
  *     with Fwrapper_direct_nbody and an array of per-body CPotentials built as
  *     the particle potentials are (NullWrapper sets `null = 1`,
- *     builtin/cybuiltin.pyx:365-372).
+ *     builtin/cybuiltin.pyx:365-372);
+ *   - leapfrog_integrate_nbody (leapfrog.pyx:126-255) and the release loop of
+ *     mockstream_leapfrog (mockstream.pyx:442-610): the Cython loops restated
+ *     around gala's c_gradient and c_nbody_gradient_symplectic.
  */
 #include <math.h>
 #include <pthread.h>
@@ -340,6 +343,27 @@ int nbody_helper(RefPot &rp, CPotential **pots, int nparticles, int nbody, doubl
     return res;
 }
 
+/* c_init_velocity_nbody / c_leapfrog_step_nbody (leapfrog.pyx:126-158) around
+ * gala's c_gradient and c_nbody_gradient_symplectic. */
+void ref_lf_init(CPotential *cp, CPotential **pots, int nbody, double *w, int i, double t, double dt, double *vh) {
+    double grad[3] = {0., 0., 0.};
+    c_gradient(cp, 1, t, w + 6 * i, grad);
+    c_nbody_gradient_symplectic(pots, t, w + 6 * i, w, nbody, i, 3, grad);
+    for (int k = 0; k < 3; k++) vh[3 * i + k] = w[6 * i + 3 + k] - grad[k] * dt / 2.;
+}
+
+void ref_lf_step(CPotential *cp, CPotential **pots, int nbody, double *w, int i, double t, double dt, double *vh) {
+    double *x = w + 6 * i, *v = x + 3, *h = vh + 3 * i;
+    for (int k = 0; k < 3; k++) x[k] = x[k] + h[k] * dt;
+    double grad[3] = {0., 0., 0.};
+    c_gradient(cp, 1, t, x, grad);
+    c_nbody_gradient_symplectic(pots, t, x, w, nbody, i, 3, grad);
+    for (int k = 0; k < 3; k++) {
+        v[k] = h[k] - grad[k] * dt / 2.;
+        h[k] = h[k] - grad[k] * dt;
+    }
+}
+
 } // namespace
 
 extern "C" {
@@ -523,6 +547,110 @@ int ref_d2_dr2_n(const gx_potential *pot, double t, const double *q, int64_t N, 
     for (int64_t i = 0; i < N; i++) out[i] = c_d2_dr2(rp.cp, t, const_cast<double *>(q + 3 * i), eps);
     release(&rp);
     return 0;
+}
+
+/* leapfrog_integrate_nbody (leapfrog.pyx:161-255): bodies (n) with the massive
+ * ones first (nbody of them), w0 (n, 6), w_out (ntimes, n, 6) or (n, 6). */
+int ref_leapfrog_nbody(const gx_potential *pot, int n, int nbody, const gx_body *bodies, const double *w0,
+                       const double *t, int64_t ntimes, int save_all, double *w_out) {
+    RefPot rp;
+    if (!build(pot, NULL, &rp)) { release(&rp); return -100; }
+    RefBody *rb = (RefBody *)calloc((size_t)n, sizeof(RefBody));
+    CPotential **pots = (CPotential **)malloc(sizeof(CPotential *) * (size_t)n);
+    int ok = 1;
+    for (int i = 0; i < n; i++) {
+        if (!build_body(&bodies[i], &rb[i])) ok = 0;
+        pots[i] = rb[i].cp;
+    }
+    if (ok) {
+        const double dt = t[1] - t[0];
+        double *w = (double *)malloc(sizeof(double) * 6 * (size_t)n);
+        double *vh = (double *)calloc(3 * (size_t)n, sizeof(double));
+        memcpy(w, w0, sizeof(double) * 6 * (size_t)n);
+        if (save_all) memcpy(w_out, w0, sizeof(double) * 6 * (size_t)n);
+        for (int i = 0; i < n; i++) ref_lf_init(rp.cp, pots, nbody, w, i, t[0], dt, vh);
+        for (int64_t j = 1; j < ntimes; j++) {
+            for (int i = 0; i < n; i++) ref_lf_step(rp.cp, pots, nbody, w, i, t[j], dt, vh);
+            if (save_all) memcpy(w_out + (size_t)j * 6 * (size_t)n, w, sizeof(double) * 6 * (size_t)n);
+        }
+        if (!save_all) memcpy(w_out, w, sizeof(double) * 6 * (size_t)n);
+        free(w);
+        free(vh);
+    }
+    for (int i = 0; i < n; i++)
+        if (rb[i].cp) free_cpotential(rb[i].cp);
+    free(rb);
+    free(pots);
+    release(&rp);
+    return ok ? 0 : -100;
+}
+
+/* mockstream_leapfrog (mockstream.pyx:442-610) for one progenitor system; the
+ * same arguments and outputs as the oracle's orc_mockstream_leapfrog. */
+int ref_mockstream_leapfrog(const gx_potential *pot, int nbodies, const gx_body *bodies, const double *nbody_w0,
+                            const double *full_time, int64_t nfull, const double *stream_w0, const double *stream_t1,
+                            int64_t ntimes, double tfinal, const int32_t *nstream, double *nbody_w_final,
+                            double *stream_w_final) {
+    RefPot rp;
+    if (!build(pot, NULL, &rp)) { release(&rp); return -100; }
+    int64_t total = 0;
+    int maxn = 0;
+    for (int64_t i = 0; i < ntimes; i++) {
+        total += nstream[i];
+        maxn = nstream[i] > maxn ? nstream[i] : maxn;
+    }
+    const int64_t total_bodies = nbodies + total;
+    RefBody *rb = (RefBody *)calloc((size_t)nbodies + 1, sizeof(RefBody));
+    CPotential **pots = (CPotential **)malloc(sizeof(CPotential *) * (size_t)total_bodies);
+    int ok = 1;
+    for (int i = 0; i < nbodies; i++) {
+        if (!build_body(&bodies[i], &rb[i])) ok = 0;
+        pots[i] = rb[i].cp;
+    }
+    gx_body null_body;
+    memset(&null_body, 0, sizeof(null_body));
+    null_body.type = GX_POT_NULL;
+    if (!build_body(&null_body, &rb[nbodies])) ok = 0;
+    for (int64_t i = nbodies; i < total_bodies; i++) pots[i] = rb[nbodies].cp;
+    if (ok) {
+        const double dt = full_time[1] - full_time[0];
+        double *traj = (double *)malloc(sizeof(double) * (size_t)nfull * 6 * (size_t)nbodies);
+        double *w = (double *)malloc(sizeof(double) * 6 * (size_t)(nbodies + maxn));
+        double *vh = (double *)calloc(3 * (size_t)(nbodies + maxn), sizeof(double));
+        /* the bodies over full_time (leapfrog_integrate_nbody, mockstream.pyx:524-528) */
+        memcpy(w, nbody_w0, sizeof(double) * 6 * (size_t)nbodies);
+        memcpy(traj, w, sizeof(double) * 6 * (size_t)nbodies);
+        for (int i = 0; i < nbodies; i++) ref_lf_init(rp.cp, pots, nbodies, w, i, full_time[0], dt, vh);
+        for (int64_t j = 1; j < nfull; j++) {
+            for (int i = 0; i < nbodies; i++) ref_lf_step(rp.cp, pots, nbodies, w, i, full_time[j], dt, vh);
+            memcpy(traj + (size_t)j * 6 * (size_t)nbodies, w, sizeof(double) * 6 * (size_t)nbodies);
+        }
+        int64_t n = 0;
+        for (int64_t i = 0; i < ntimes; i++) {
+            if (nstream[i] == 0) continue;
+            const int idx = (int)((stream_t1[i] - full_time[0]) / dt + 0.5);
+            memcpy(w, traj + (size_t)idx * 6 * (size_t)nbodies, sizeof(double) * 6 * (size_t)nbodies);
+            memcpy(w + 6 * nbodies, stream_w0 + 6 * n, sizeof(double) * 6 * (size_t)nstream[i]);
+            const int nsys = nbodies + nstream[i];
+            for (int j = 0; j < nsys; j++) ref_lf_init(rp.cp, pots, nbodies, w, j, stream_t1[i], dt, vh);
+            const int n_steps = (int)((tfinal - stream_t1[i]) / dt + 0.5);
+            for (int j = 0; j < n_steps; j++)
+                for (int k = 0; k < nsys; k++)
+                    ref_lf_step(rp.cp, pots, nbodies, w, k, stream_t1[i] + (j + 1) * dt, dt, vh);
+            memcpy(stream_w_final + 6 * n, w + 6 * nbodies, sizeof(double) * 6 * (size_t)nstream[i]);
+            memcpy(nbody_w_final, w, sizeof(double) * 6 * (size_t)nbodies);
+            n += nstream[i];
+        }
+        free(traj);
+        free(w);
+        free(vh);
+    }
+    for (int i = 0; i <= nbodies; i++)
+        if (rb[i].cp) free_cpotential(rb[i].cp);
+    free(rb);
+    free(pots);
+    release(&rp);
+    return ok ? 0 : -100;
 }
 
 } // extern "C"

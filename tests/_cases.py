@@ -26,11 +26,12 @@ def potentials():
     }
 
 
-def stream_case(n_streams=2, n_steps=150, dt=1.0, seed=21, n_per_tail=1, release_every=1):
+def stream_case(n_streams=2, n_steps=150, dt=1.0, seed=21, n_per_tail=1, release_every=1, leapfrog=False):
     """A small batch of mock streams in the MW composite, built with the oracle:
     Plummer progenitors, progenitor orbits from gala's own n-body DOP853
     semantics, Fardal release states from seeded draws.  Returns a dict of the
-    inputs of the release stage (layout of the GPU entry points)."""
+    inputs of the release stage (layout of the GPU entry points).  With
+    leapfrog=True the progenitor orbits come from gala's Leapfrog n-body loop."""
     import numpy as np
 
     from gala_gb300.mockstream import FardalStreamDF
@@ -48,8 +49,11 @@ def stream_case(n_streams=2, n_steps=150, dt=1.0, seed=21, n_per_tail=1, release
     offset = np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)
     orbits, stream_w0 = [], []
     for s in range(n_streams):
-        orb, res = orc.nbody_dop853(mw, bodies[s], 1, w0[:, s].reshape(1, 6), t, nstiff=-1)
-        assert res == 1
+        if leapfrog:
+            orb = orc.leapfrog_nbody(mw, bodies[s], 1, w0[:, s].reshape(1, 6), t)
+        else:
+            orb, res = orc.nbody_dop853(mw, bodies[s], 1, w0[:, s].reshape(1, 6), t, nstiff=-1)
+            assert res == 1
         orbits.append(orb)
         draws = df._draws(int(offset[-1]))
         stream_w0.append(orc.fardal_sample(mw, orb.reshape(len(t), 6), np.full(len(t), m[s]), t, offset, draws,

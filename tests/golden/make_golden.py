@@ -146,6 +146,19 @@ def make_stream_fixtures(ref: Oracle):
     np.savez_compressed(OUT / "mockstream_dop853.npz", stream=np.stack(streams), nbody=np.stack(nbodies),
                         status=np.stack(status), **out)
 
+    # Leapfrog: leapfrog_integrate_nbody and mockstream_leapfrog
+    from tests.test_mockstream_oracle import _lf_nbody_args, _lf_stream_args
+
+    c = stream_case(n_streams=n_streams, n_steps=n_steps, leapfrog=True)
+    streams, nbodies = [], []
+    for s in range(n_streams):
+        nb, st = ref.mockstream_leapfrog(c["pot"], **_lf_stream_args(c, s))
+        streams.append(st)
+        nbodies.append(nb)
+    np.savez_compressed(OUT / "mockstream_leapfrog.npz", stream=np.stack(streams), nbody=np.stack(nbodies),
+                        n_streams=n_streams, n_steps=n_steps, stream_w0=c["stream_w0"],
+                        nbody_leapfrog=ref.leapfrog_nbody(c["pot"], *_lf_nbody_args()))
+
 
 if __name__ == "__main__":
     # python tests/golden/make_golden.py [potentials integrators scf streams]

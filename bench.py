@@ -54,7 +54,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gx", choices=["gx", "reference"])
     p.add_argument("--workload", default="mw_dop853",
-                   choices=["mw_dop853", "uneven_batch", "scf_surrogate", "mock_streams"],
+                   choices=["mw_dop853", "uneven_batch", "scf_surrogate", "mock_streams", "orbit_reductions"],
                    help="mw_dop853: the headline line; uneven_batch / scf_surrogate: only that variant "
                         "(used for profiling)")
     p.add_argument("--batch-orbits", type=int, default=262_144)
@@ -66,6 +66,9 @@ def parse_args():
     p.add_argument("--surrogate-orbits", type=int, default=262_144)
     p.add_argument("--surrogate-nsteps", type=int, default=5000)
     p.add_argument("--no-streams", action="store_true", help="skip the mock-stream variant")
+    p.add_argument("--no-reductions", action="store_true", help="skip the orbit-reduction variant")
+    p.add_argument("--reduce-orbits", type=int, default=100_000)
+    p.add_argument("--reduce-nsteps", type=int, default=2000)
     p.add_argument("--stream-progenitors", type=int, default=512)
     p.add_argument("--stream-nsteps", type=int, default=2000)
     p.add_argument("--stream-cpu-streams", type=int, default=8, help="streams in the CPU-baseline sample")
@@ -544,6 +547,82 @@ def run_mock_streams(args, torch, stream):
     return result
 
 
+def run_orbit_reductions(args, torch, stream):
+    """Orbit extrema (pericentre, apocentre, z maximum statistics of gala's
+    Orbit.pericenter / apocenter / zmax) over stored snapshots: 100,000
+    MW-composite orbits x 2,001 Leapfrog snapshots (9.6 GB resident in HBM), one
+    fused pass reading x, y, z (24 B per orbit-snapshot).  HBM-bound; L2 flushed
+    before each timed pass.  CPU baseline: gala's own per-orbit algorithm
+    (argrelmax + polyfit per extremum, numpy / scipy) on a sample of orbits."""
+    from gala_gb300 import _abi
+    from gala_gb300 import workloads as W
+    from gala_gb300._device import ptr
+
+    n, nsteps = args.reduce_orbits, args.reduce_nsteps
+    mw = W.mw_composite()
+    w0 = W.mw_ics(n, seed=W.SEED_BASE + 7)
+    orbit = mw.integrate_orbit(w0, dt=1.0, n_steps=nsteps, Integrator="leapfrog", return_device=True)
+    wd = orbit.w_device.contiguous()
+    td = torch.from_numpy(np.ascontiguousarray(orbit.t)).cuda()
+    nt = int(wd.shape[1])
+    count = torch.zeros((3, n), dtype=torch.int32, device="cuda")
+    sm, mn, mx = (torch.zeros((3, n), dtype=torch.float64, device="cuda") for _ in range(3))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def call():
+        _abi.call("gx_orbit_extrema", ptr(wd), ptr(td), nt, n, 0, 0, ptr(count), ptr(sm), ptr(mn), ptr(mx), None,
+                  None, int(stream.cuda_stream))
+
+    for _ in range(max(3, args.warmup)):
+        call()
+    times = []
+    for _ in range(max(3, args.steps)):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.median(times))
+    algo_bytes = 3 * nt * n * 8 + nt * 8 + 3 * n * (4 + 3 * 8)
+    peaks = {}
+    try:
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except Exception:
+        pass
+    hbm = None
+    for k in ("hbm_gbs", "hbm_GBps", "hbm"):
+        if isinstance(peaks.get(k), (int, float)):
+            hbm = float(peaks[k])
+    hbm = hbm or 6791.0
+    res = {
+        "workload": f"orbit_reductions: {n} MW-composite orbits x {nt} Leapfrog snapshots, peri/apo/zmax "
+                    "statistics in one pass",
+        "value": n * nt / (ms * 1e-3), "unit": "orbit-snapshots/s", "ms": ms,
+        "roofline": {"bound": "hbm", "achieved": algo_bytes / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": algo_bytes / (ms * 1e-3) / 1e9 / hbm, "bytes_per_launch": algo_bytes},
+        "extrema_per_orbit_mean": {"peri": float(count[0].float().mean()), "apo": float(count[1].float().mean()),
+                                   "zmax": float(count[2].float().mean())},
+    }
+    if not args.no_cpu_baseline:
+        from oracle import orbit_oracle as OO
+
+        ns = 200
+        wh = wd[:, :, :ns].cpu().numpy()
+        t0 = time.perf_counter()
+        for kind in ("peri", "apo", "zmax"):
+            OO.reduce(wh, orbit.t, kind)
+        cpu_s = time.perf_counter() - t0
+        gpu_mean = (sm / count)[:, :ns].cpu().numpy()
+        ref = np.stack([OO.reduce(wh, orbit.t, k) for k in ("peri", "apo", "zmax")])
+        res["cpu_baseline"] = {"value": ns * nt / cpu_s, "unit": "orbit-snapshots/s", "cores": 1, "kind": "port",
+                               "sample": f"{ns} orbits, gala's _max_helper (scipy argrelmax + numpy polyfit), "
+                                         "3 statistics, 1 thread",
+                               "gpu_vs_cpu_max_rel": float(np.nanmax(np.abs(gpu_mean - ref) / np.abs(ref)))}
+    return res
+
+
 def run_gx(args):
     import torch
 
@@ -560,9 +639,9 @@ def run_gx(args):
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
     sh = int(stream.cuda_stream)
-    if args.workload in ("uneven_batch", "scf_surrogate", "mock_streams"):
+    if args.workload in ("uneven_batch", "scf_surrogate", "mock_streams", "orbit_reductions"):
         fn = {"uneven_batch": run_uneven_batch, "scf_surrogate": run_scf_surrogate,
-              "mock_streams": run_mock_streams}[args.workload]
+              "mock_streams": run_mock_streams, "orbit_reductions": run_orbit_reductions}[args.workload]
         res = fn(args, torch, stream)
         if rank == 0:
             print(json.dumps(res), flush=True)
@@ -656,6 +735,8 @@ def run_gx(args):
         variants["scf_surrogate"] = run_scf_surrogate(args, torch, stream)
     if not args.no_streams:
         variants["mock_streams"] = run_mock_streams(args, torch, stream)
+    if not args.no_reductions:
+        variants["orbit_reductions"] = run_orbit_reductions(args, torch, stream)
 
     if rank != 0:
         return

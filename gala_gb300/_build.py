@@ -28,6 +28,7 @@ UNITS = {
     "gx_dop853.cu": ["-fmad=false"],
     "gx_nbody.cu": ["-fmad=false"],
     "gx_lfnbody.cu": ["-fmad=false"],
+    "gx_orbit.cu": ["-fmad=false"],
     "gx_peaks.cu": [],
     "gx_batch.cu": [],
     "gx_stream32.cu": [],

@@ -125,10 +125,14 @@ class Orbit(PhaseSpacePosition):
 
     @property
     def ntimes(self):
+        if self.__dict__.get("_w_dev") is not None and self.__dict__.get("_w_host") is None:
+            return int(self._w_dev.shape[1])
         return self.pos.shape[1]
 
     @property
     def norbits(self):
+        if self.__dict__.get("_w_dev") is not None and self.__dict__.get("_w_host") is None:
+            return 1 if self._w_dev.ndim < 3 else int(self._w_dev.shape[2])
         return 1 if self.pos.ndim < 3 else self.pos.shape[2]
 
     def energy(self, hamiltonian=None):
@@ -151,3 +155,91 @@ class Orbit(PhaseSpacePosition):
         if wi.ndim >= 2 and t is not None and np.ndim(t) > 0:
             return Orbit.from_w(wi, t=t, hamiltonian=self.hamiltonian)
         return PhaseSpacePosition.from_w(wi)
+
+    # -- extrema (src/gala/dynamics/orbit.py:391-681), computed on the GPU ------
+    _KINDS = {"peri": 0, "apo": 1, "zmax": 2}
+
+    def _device_w_t(self):
+        import torch
+
+        from ._device import as_device_f64, require_cuda
+
+        dev = require_cuda()
+        if self.t is None:
+            raise ValueError("extrema need the orbit's time array")
+        w = self._w_dev if self._w_dev is not None else self.w()
+        wd = as_device_f64(w, dev)
+        if wd.ndim == 2:
+            wd = wd[:, :, None]
+        return wd.contiguous(), torch.from_numpy(np.ascontiguousarray(self.t, dtype=np.float64)).to(dev)
+
+    def _extrema_run(self, approximate, keep):
+        import torch
+
+        from . import _abi
+        from ._device import ptr, stream_handle
+
+        wd, td = self._device_w_t()
+        nt, n = int(wd.shape[1]), int(wd.shape[2])
+        dev = wd.device
+        count = torch.zeros((3, n), dtype=torch.int32, device=dev)
+        sm, mn, mx = (torch.zeros((3, n), dtype=torch.float64, device=dev) for _ in range(3))
+        vals = torch.zeros((3, n, keep), dtype=torch.float64, device=dev) if keep else None
+        times = torch.zeros((3, n, keep), dtype=torch.float64, device=dev) if keep else None
+        _abi.call("gx_orbit_extrema", ptr(wd), ptr(td), nt, n, int(bool(approximate)), int(keep), ptr(count),
+                  ptr(sm), ptr(mn), ptr(mx), ptr(vals) if keep else None, ptr(times) if keep else None,
+                  stream_handle())
+        out = {"count": count.cpu().numpy(), "sum": sm.cpu().numpy(), "min": mn.cpu().numpy(),
+               "max": mx.cpu().numpy()}
+        if keep:
+            out["vals"] = vals.cpu().numpy()
+            out["times"] = times.cpu().numpy()
+        return out
+
+    def _extrema(self, kind, return_times, func, approximate):
+        if return_times and func is not None:
+            raise ValueError("Cannot return times if reducing using an input function. Pass `func=None` if you "
+                             "want to return all individual values and times.")
+        k = self._KINDS[kind]
+        cache = self.__dict__.setdefault("_ext_cache", {})
+        if approximate not in cache:
+            cache[approximate] = self._extrema_run(approximate, 0)
+        st = cache[approximate]
+        cnt = st["count"][k]
+        single = self.norbits == 1
+        if func is np.mean or func is np.min or func is np.max:
+            with np.errstate(invalid="ignore", divide="ignore"):
+                v = {np.mean: st["sum"][k] / cnt, np.min: st["min"][k], np.max: st["max"][k]}[func]
+            v = np.where(cnt > 0, v, np.nan)
+            return float(v[0]) if single else v
+        keep = max(int(cnt.max()), 1)
+        full = self._extrema_run(approximate, keep)
+        vals = [full["vals"][k, i, :cnt[i]] for i in range(len(cnt))]
+        tms = [full["times"][k, i, :cnt[i]] for i in range(len(cnt))]
+        if func is not None:
+            v = np.array([func(x) for x in vals])
+            return float(v[0]) if single else v
+        if return_times:
+            return (vals[0], tms[0]) if single else (vals, tms)
+        return vals[0] if single else vals
+
+    def pericenter(self, return_times=False, func=np.mean, approximate=False):
+        """Pericentres from the local minima of r, each refined by a parabola
+        (Orbit.pericenter, orbit.py:439-495)."""
+        return self._extrema("peri", return_times, func, approximate)
+
+    def apocenter(self, return_times=False, func=np.mean, approximate=False):
+        """Apocentres from the local maxima of r (Orbit.apocenter, orbit.py:497-553)."""
+        return self._extrema("apo", return_times, func, approximate)
+
+    def zmax(self, return_times=False, func=np.mean, approximate=False):
+        """Maximum |z| excursions (Orbit.zmax, orbit.py:600-656)."""
+        return self._extrema("zmax", return_times, func, approximate)
+
+    def eccentricity(self, **kw):
+        """(r_apo - r_peri) / (r_apo + r_peri) from the mean apo- and pericentre
+        (Orbit.eccentricity, orbit.py:658-681)."""
+        ra = self.apocenter(**kw)
+        rp = self.pericenter(**kw)
+        return (ra - rp) / (ra + rp)
+

@@ -420,6 +420,21 @@ int gx_mockstream_leapfrog_fp32(const gx_potential* pot, int64_t n_streams, int3
                                 double* stream_w_out, double* nbody_w_out, int32_t* status,
                                 void* stream);
 
+/* Orbit.pericenter / apocenter / zmax statistics (src/gala/dynamics/orbit.py:
+ * 391-656) of N orbits stored as (6, ntimes, N) snapshots at times t, in one
+ * pass: per orbit and kind (0 pericentre, 1 apocentre, 2 z maximum) the number
+ * of interior strict extrema of r or |z|, each refined by the vertex of the
+ * parabola through its three samples (approximate != 0: the sample itself),
+ * and their sum (in increasing time), minimum and maximum.  A grid with
+ * t[ntimes-1] < t[0] is scanned from the end, as gala reverses it.
+ *   count             DEVICE int32 (3, N)
+ *   sum, vmin, vmax   DEVICE double (3, N)
+ *   vals, times       DEVICE double (3, N, keep): the first `keep` extrema, or
+ *                     NULL with keep = 0 */
+int gx_orbit_extrema(const double* w, const double* t, int64_t ntimes, int64_t n,
+                     int32_t approximate, int32_t keep, int32_t* count, double* sum,
+                     double* vmin, double* vmax, double* vals, double* times, void* stream);
+
 /* FardalStreamDF._sample (src/gala/dynamics/mockstream/df.pyx:363-457) with
  * get_rj_vj_R (:61-92) and transform_from_sat (:94-106) for n_streams
  * progenitor orbits on one time grid; the Jacobi radius uses c_d2_dr2

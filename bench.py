@@ -316,12 +316,20 @@ def run_scf_surrogate(args, torch, stream):
         e1.synchronize()
         return e0.elapsed_time(e1) / reps, out
 
-    ms_sur, (wsur, fb) = timed(lambda: sp.integrate_leapfrog(w0, 1.0, n_steps), 1)
+    ms_sur, (wsur, fb) = timed(lambda: sp.integrate_leapfrog(w0, 1.0, n_steps, engine="tcgen05"), 1)
+    ms_mma, (wmma, _) = timed(lambda: sp.integrate_leapfrog(w0, 1.0, n_steps, engine="mma"), 1)
+    tc_vs_mma = (np.linalg.norm((wsur - wmma)[:3].cpu().numpy(), axis=0) /
+                 np.linalg.norm(wmma[:3].cpu().numpy(), axis=0))
     n32 = min(65536, n_orbits)
     ms_f32, _ = timed(lambda: sp.integrate_leapfrog(w0[:, :n32], 1.0, 200, analytic=True), 1)
     ms_f64, _ = timed(lambda: scf.integrate_orbit(w0, dt=1.0, n_steps=20, Integrator="leapfrog", save_all=False,
                                                   return_device=True), 1)
     v_sur = n_orbits * n_steps / (ms_sur * 1e-3)
+    flops_run = float(n_orbits * (n_steps + 1)) * 6 * 2 * 2 * 256 * 256
+    try:
+        bf16_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops_sustained"])
+    except Exception:
+        bf16_peak = 1700.0
     v_f32 = n32 * 200 / (ms_f32 * 1e-3)
     v_f64 = n_orbits * 20 / (ms_f64 * 1e-3)
     sub = w0[:, :min(2048, n_orbits)]
@@ -342,7 +350,18 @@ def run_scf_surrogate(args, torch, stream):
                     f"{n_steps} Leapfrog steps",
         "fp32_surrogate": {"value": v_sur, "unit": UNIT, "ms_per_run": ms_sur,
                            "fallback_force_evaluations": int(fb.item()),
-                           "tensor_core": "mma.sync m16n8k16 BF16, FP32 accumulate, activations BF16 hi+lo"},
+                           "tensor_core": "tcgen05.mma kind::f16 128x256x16, BF16 operands from swizzled SMEM, "
+                                          "FP32 accumulators in TMEM, activations BF16 hi+lo",
+                           "flops_per_run": flops_run,
+                           "roofline": {"bound": "tensor", "unit": "TFLOP/s",
+                                        "achieved": flops_run / (ms_sur * 1e-3) / 1e12,
+                                        "peak": bf16_peak, "frac": flops_run / (ms_sur * 1e-3) / 1e12 / bf16_peak,
+                                        "work": "executed BF16 MMA flops (6 GEMMs x 2 parts x 2 x 128 x 256 x 256 "
+                                                "per 128-position tile and step)"}},
+        "fp32_surrogate_mma_sync": {"value": n_orbits * n_steps / (ms_mma * 1e-3), "unit": UNIT, "ms_per_run": ms_mma,
+                                    "tensor_core": "mma.sync m16n8k16 BF16 (legacy warp-level path)",
+                                    "speedup_tcgen05_vs_mma": ms_mma / ms_sur,
+                                    "position_diff_vs_tcgen05_median": float(np.median(tc_vs_mma))},
         "fp32_analytic_scf": {"value": v_f32, "unit": UNIT, "sample": f"{n32} orbits x 200 steps"},
         "fp64_analytic_scf_plain": {"value": v_f64, "unit": UNIT, "sample": f"{n_orbits} orbits x 20 steps"},
         "speedup_surrogate_vs_fp64": v_sur / v_f64,

@@ -34,6 +34,7 @@ UNITS = {
     "gx_stream32.cu": [],
     "gx_mlp_train.cu": [],
     "gx_mlp_infer.cu": [],
+    "gx_mlp_tc.cu": [],
 }
 
 

@@ -117,6 +117,8 @@ class SurrogatePotential:
         self.params = torch.from_numpy(init_params(seed)).to(self.dev)
         self.scf_f32 = torch.from_numpy(scf.packed().params.astype(np.float32)).to(self.dev)
         self.wbf16 = None
+        self.wimg = None
+        self.engine = "tcgen05"
         self.split = int(split)
         self.history = []
 
@@ -232,23 +234,33 @@ class SurrogatePotential:
         return self.history
 
     def export(self):
-        """BF16 weight pack for inference: W2, W3, W4, W4^T, W3^T, W2^T."""
+        """BF16 weight pack for inference: W2, W3, W4, W4^T, W3^T, W2^T, and its
+        tensor-core image (64-wide K chunks, 128-byte swizzle; see
+        gx_surrogate_gradient_tc in include/gala_gb300.h)."""
         import torch
 
         Ws = [self.params[o:o + H * H].view(H, H) for o in (OFF_W2, OFF_W3, OFF_W4)]
         pack = [Ws[0], Ws[1], Ws[2], Ws[2].T, Ws[1].T, Ws[0].T]
         self.wbf16 = torch.stack([w.contiguous() for w in pack]).to(torch.bfloat16).contiguous()
+        # [matrix][row][chunk][granule][8] -> [matrix][chunk][row][granule ^ (row & 7)][8]
+        v = self.wbf16.view(6, H, H // 64, 8, 8).permute(0, 2, 1, 3, 4).contiguous()
+        rows = torch.arange(H, device=v.device)
+        src = (torch.arange(8, device=v.device)[None, :] ^ (rows[:, None] & 7))  # [row][dest granule] -> source
+        idx = src.view(1, 1, H, 8, 1).expand(6, H // 64, H, 8, 8)
+        self.wimg = torch.gather(v, 3, idx).contiguous()
         return self.wbf16
 
     # ------------------------------------------------------------ inference
-    def _grid(self, n):
+    def _grid(self, n, tile=64):
         import torch
 
         sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
-        return int(max(1, min(sms, (n + 63) // 64)))
+        return int(max(1, min(sms, (n + tile - 1) // tile)))
 
-    def gradient_and_energy(self, q):
-        """grad Phi (3, N) and Phi (N) at positions q (3, N), via the BF16 kernel."""
+    def gradient_and_energy(self, q, engine=None):
+        """grad Phi (3, N) and Phi (N) at positions q (3, N), on the tensor cores:
+        engine "tcgen05" (default) or "mma" (warp-level mma.sync)."""
+        engine = engine or self.engine
         import torch
 
         from ._device import as_device_f64, ptr, stream_handle
@@ -259,12 +271,24 @@ class SurrogatePotential:
         n = qd.shape[1]
         grad = torch.empty((3, n), dtype=torch.float64, device=self.dev)
         phi = torch.empty(n, dtype=torch.float64, device=self.dev)
-        _abi.call("gx_surrogate_gradient", ptr(self.params), ptr(self.wbf16), ptr(self.scf_f32), self.r_min,
-                  self.r_max, self.GM, self.r_s, self.split, ptr(qd), n, ptr(grad), ptr(phi), self._grid(n),
-                  stream_handle())
+        if engine == "tcgen05":
+            status = torch.zeros(1, dtype=torch.int32, device=self.dev)
+            _abi.call("gx_surrogate_gradient_tc", ptr(self.params), ptr(self.wimg), ptr(self.scf_f32), self.r_min,
+                      self.r_max, self.GM, self.r_s, ptr(qd), n, ptr(grad), ptr(phi), self._grid(n, 128),
+                      ptr(status), stream_handle())
+            self._check(status)
+        else:
+            _abi.call("gx_surrogate_gradient", ptr(self.params), ptr(self.wbf16), ptr(self.scf_f32), self.r_min,
+                      self.r_max, self.GM, self.r_s, self.split, ptr(qd), n, ptr(grad), ptr(phi), self._grid(n),
+                      stream_handle())
         return grad, phi
 
-    def integrate_leapfrog(self, w0, dt, n_steps, grid=None, analytic=False):
+    @staticmethod
+    def _check(status):
+        if int(status.item()) != 0:
+            raise _abi.GxError("the tensor-core surrogate kernel ran out of a bounded wait (results incomplete)")
+
+    def integrate_leapfrog(self, w0, dt, n_steps, grid=None, analytic=False, engine=None):
         """FP32 leapfrog of every orbit in w0 (6, N) in the surrogate potential;
         returns the final states (6, N) and the number of fallback force calls.
         analytic=True: the same integrator with the analytic SCF force (FP32)
@@ -279,6 +303,13 @@ class SurrogatePotential:
         n = w0d.shape[1]
         out = torch.empty_like(w0d)
         fb = torch.zeros(1, dtype=torch.int64, device=self.dev)
+        if (engine or self.engine) == "tcgen05" and not analytic:
+            status = torch.zeros(1, dtype=torch.int32, device=self.dev)
+            _abi.call("gx_surrogate_leapfrog_tc", ptr(self.params), ptr(self.wimg), ptr(self.scf_f32), self.r_min,
+                      self.r_max, self.GM, self.r_s, ptr(w0d), n, int(n_steps), float(dt), ptr(out), ptr(fb),
+                      grid or self._grid(n, 128), ptr(status), stream_handle())
+            self._check(status)
+            return out, fb
         wb = ptr(self.wbf16) if self.wbf16 is not None else None
         _abi.call("gx_surrogate_leapfrog", ptr(self.params), wb, ptr(self.scf_f32), self.r_min,
                   self.r_max, self.GM, self.r_s, self.split, int(bool(analytic)), ptr(w0d), n, int(n_steps),

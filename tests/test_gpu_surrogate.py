@@ -83,13 +83,15 @@ def test_adam_matches_numpy():
     np.testing.assert_allclose(tp.cpu().numpy(), p2, rtol=1e-5, atol=1e-7)
 
 
-def test_bf16_inference_matches_fp64_network(scf):
-    """The tensor-core kernel evaluates the same function as the FP64 oracle of
-    the network (to BF16 precision)."""
+@pytest.mark.parametrize("engine", ["tcgen05", "mma"])
+def test_bf16_inference_matches_fp64_network(scf, engine):
+    """The tensor-core kernels (tcgen05 with TMEM accumulators, and warp-level
+    mma.sync) evaluate the same function as the FP64 oracle of the network (to
+    BF16 precision)."""
     sp = S.SurrogatePotential(scf, seed=6)
     sp.export()
     x = sp.sample_positions(3000, seed=7)
-    grad, phi = sp.gradient_and_energy(x)
+    grad, phi = sp.gradient_and_energy(x, engine=engine)
     xd = x.cpu().numpy()
     xh, r, n, rho, drho = S.input_map(xd, sp.r_min, sp.r_max)
     p = sp.params.cpu().numpy().astype(np.float64)
@@ -165,3 +167,32 @@ def test_surrogate_leapfrog_runs_and_matches_fp32_forces(scf):
     assert np.isfinite(o).all()
     assert not np.array_equal(o, w0)
     assert int(fb.item()) == 0
+
+
+def test_tcgen05_matches_mma_engine(scf):
+    """Both tensor-core engines run BF16 weights with BF16 hi + lo activations
+    and FP32 accumulation; they differ only in accumulation order, far below
+    the BF16 weight rounding.  Sizes that are not a multiple of the 128-row
+    tile exercise the partial last tile."""
+    sp = S.SurrogatePotential(scf, seed=8)
+    sp.export()
+    for n in (1, 127, 129, 5000):
+        x = sp.sample_positions(n, seed=9)
+        g_tc, p_tc = sp.gradient_and_energy(x, engine="tcgen05")
+        g_mm, p_mm = sp.gradient_and_energy(x, engine="mma")
+        d = np.linalg.norm((g_tc - g_mm).cpu().numpy(), axis=0) / np.linalg.norm(g_mm.cpu().numpy(), axis=0)
+        assert np.median(d) < 1e-4 and np.max(d) < 1e-2, (n, np.median(d), np.max(d))
+        np.testing.assert_allclose(p_tc.cpu().numpy(), p_mm.cpu().numpy(), rtol=0,
+                                   atol=1e-4 * np.abs(p_mm.cpu().numpy()).max())
+
+
+def test_tcgen05_leapfrog_matches_mma_leapfrog(scf):
+    sp = S.SurrogatePotential(scf, seed=10)
+    sp.export()
+    w0 = W.scf_ics(700, seed=11)
+    o_tc, fb_tc = sp.integrate_leapfrog(w0, 1.0, 50, engine="tcgen05")
+    o_mm, fb_mm = sp.integrate_leapfrog(w0, 1.0, 50, engine="mma")
+    err = np.linalg.norm((o_tc - o_mm)[:3].cpu().numpy(), axis=0) / np.linalg.norm(o_mm[:3].cpu().numpy(), axis=0)
+    assert np.median(err) < 1e-5, np.median(err)
+    assert int(fb_tc.item()) == int(fb_mm.item())
+

@@ -324,6 +324,12 @@ def run_scf_surrogate(args, torch, stream):
     ms_f32, _ = timed(lambda: sp.integrate_leapfrog(w0[:, :n32], 1.0, 200, analytic=True), 1)
     ms_f64, _ = timed(lambda: scf.integrate_orbit(w0, dt=1.0, n_steps=20, Integrator="leapfrog", save_all=False,
                                                   return_device=True), 1)
+    # BF16-only activations (one MMA per K step instead of hi + lo)
+    sp.split = 1
+    ms_s1, (ws1, _) = timed(lambda: sp.integrate_leapfrog(w0, 1.0, n_steps, engine="tcgen05"), 1)
+    g1, _ = sp.gradient_and_energy(x)
+    ferr1 = np.linalg.norm(g1.cpu().numpy() - ref, axis=0) / np.linalg.norm(ref, axis=0)
+    sp.split = 2
     v_sur = n_orbits * n_steps / (ms_sur * 1e-3)
     flops_run = float(n_orbits * (n_steps + 1)) * 6 * 2 * 2 * 256 * 256
     try:
@@ -358,6 +364,10 @@ def run_scf_surrogate(args, torch, stream):
                                         "peak": bf16_peak, "frac": flops_run / (ms_sur * 1e-3) / 1e12 / bf16_peak,
                                         "work": "executed BF16 MMA flops (6 GEMMs x 2 parts x 2 x 128 x 256 x 256 "
                                                 "per 128-position tile and step)"}},
+        "fp32_surrogate_bf16_activations": {"value": n_orbits * n_steps / (ms_s1 * 1e-3), "unit": UNIT,
+                                            "ms_per_run": ms_s1,
+                                            "force_error_vs_analytic_median": float(np.median(ferr1)),
+                                            "force_error_vs_analytic_p90": float(np.percentile(ferr1, 90))},
         "fp32_surrogate_mma_sync": {"value": n_orbits * n_steps / (ms_mma * 1e-3), "unit": UNIT, "ms_per_run": ms_mma,
                                     "tensor_core": "mma.sync m16n8k16 BF16 (legacy warp-level path)",
                                     "speedup_tcgen05_vs_mma": ms_mma / ms_sur,

@@ -96,8 +96,9 @@ SIGNATURES = {
     "gx_surrogate_leapfrog": (C.c_int, [_P, _P, _P, _D, _D, _D, _D, _I32, _I32, _P, _I64, _I64, _D, _P, _P, _I32,
                                         _P]),
     "gx_surrogate_smem_bytes": (C.c_int, []),
-    "gx_surrogate_gradient_tc": (C.c_int, [_P, _P, _P, _D, _D, _D, _D, _P, _I64, _P, _P, _I32, _P, _P]),
-    "gx_surrogate_leapfrog_tc": (C.c_int, [_P, _P, _P, _D, _D, _D, _D, _P, _I64, _I64, _D, _P, _P, _I32, _P, _P]),
+    "gx_surrogate_gradient_tc": (C.c_int, [_P, _P, _P, _D, _D, _D, _D, _I32, _P, _I64, _P, _P, _I32, _P, _P]),
+    "gx_surrogate_leapfrog_tc": (C.c_int, [_P, _P, _P, _D, _D, _D, _D, _I32, _P, _I64, _I64, _D, _P, _P, _I32, _P,
+                                           _P]),
     "gx_surrogate_tc_smem_bytes": (C.c_int, []),
     "gx_nbody_dop853": (C.c_int, [_PP, _PF, _I64, _I32, _I32, _P, _P, _P, _I64, _D, _D, _I64, _D, _I64, _I32, _I64,
                                   _P, _P, _P, _P, _P]),

@@ -65,6 +65,9 @@ struct Shared {
     float fbg[TM * 3];
     float xh[TM * 3];        // network inputs of the tile
     float part[4][TM * 4];   // per-slice partial sums: y and G (4 per row)
+    float4 w1b1[H];          // layer 1: {W1[j][0], W1[j][1], W1[j][2], b1[j]}
+    float bias[3][H];        // b2, b3, b4
+    float w5[H];
 };
 constexpr int SMEM_BYTES = 1024 + 2 * A_PART + 2 * W_CHUNK + (int)sizeof(Shared);
 
@@ -150,15 +153,23 @@ __device__ __forceinline__ void tm_st16(uint32_t addr, const uint32_t (&r)[16]) 
         : "memory");
 }
 
-// SiLU and its derivative (gx_mlp.cuh silu3 without the second derivative).
+// SiLU and its derivative with the logistic function as 0.5 + 0.5 tanh(z / 2):
+// one MUFU instruction (tanh.approx, max relative error ~2^-11, below the BF16
+// rounding the activations get anyway).
+__device__ __forceinline__ float tanh_approx(float x) {
+    float r;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
 __device__ __forceinline__ void silu2(float z, float &a, float &s1) {
-    const float sg = __fdividef(1.0f, 1.0f + __expf(-z));
+    const float sg = fmaf(0.5f, tanh_approx(0.5f * z), 0.5f);
     a = z * sg;
-    s1 = sg * (1.0f + z * (1.0f - sg));
+    s1 = sg * fmaf(z, 1.0f - sg, 1.0f);
 }
 
 // Write 32 consecutive values (columns j0..j0+31, j0 a multiple of 32) of row
 // `row` of the A operand: BF16 hi part and the BF16 rounding remainder (lo).
+template <int SPLIT>
 __device__ __forceinline__ void put_a(uint8_t *sA, int row, int j0, const float (&v)[32]) {
     const int c = j0 >> 6, g0 = (j0 & 63) >> 3;
 #pragma unroll
@@ -168,14 +179,19 @@ __device__ __forceinline__ void put_a(uint8_t *sA, int row, int j0, const float 
         for (int e = 0; e < 4; e++) {
             const float a = v[u * 8 + 2 * e], b = v[u * 8 + 2 * e + 1];
             const __nv_bfloat162 hi = __floats2bfloat162_rn(a, b);
-            const float2 hf = __bfloat1622float2(hi);
-            const __nv_bfloat162 lo = __floats2bfloat162_rn(a - hf.x, b - hf.y);
             hw[e] = *reinterpret_cast<const uint32_t *>(&hi);
-            lw[e] = *reinterpret_cast<const uint32_t *>(&lo);
+            if constexpr (SPLIT == 2) {
+                const float2 hf = __bfloat1622float2(hi);
+                const __nv_bfloat162 lo = __floats2bfloat162_rn(a - hf.x, b - hf.y);
+                lw[e] = *reinterpret_cast<const uint32_t *>(&lo);
+            } else {
+                lw[e] = 0u;
+            }
         }
         const int off = c * A_CHUNK + row * 128 + (((g0 + u) ^ (row & 7)) << 4);
         *reinterpret_cast<uint4 *>(sA + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-        *reinterpret_cast<uint4 *>(sA + A_PART + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        if constexpr (SPLIT == 2)
+            *reinterpret_cast<uint4 *>(sA + A_PART + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
     }
 }
 
@@ -197,6 +213,7 @@ __device__ __forceinline__ void issue_copy(Issuer &I, Shared &S) {
 // One 128 x 256 x 256 GEMM into TMEM columns [0, 256): A from sA (hi and lo
 // parts), B = the next four weight chunks.  Thread 0 only.  Returns false on a
 // wait timeout.
+template <int SPLIT>
 __device__ bool issue_gemm(Issuer &I, Shared &S, uint8_t *sA, uint32_t tmem) {
     for (int c = 0; c < KCH; c++) {
         const uint32_t q = I.q, b = q & 1;
@@ -207,7 +224,7 @@ __device__ bool issue_gemm(Issuer &I, Shared &S, uint8_t *sA, uint32_t tmem) {
         for (int s = 0; s < 4; s++) {
             const uint64_t bd = desc_sw128(wbase + s * 32);
 #pragma unroll
-            for (int part = 0; part < 2; part++) {
+            for (int part = 0; part < SPLIT; part++) {
                 const uint64_t ad = desc_sw128(su32(sA + part * A_PART + c * A_CHUNK + s * 32));
                 mma(tmem, ad, bd, (c | s | part) ? 1u : 0u);
             }
@@ -234,9 +251,10 @@ __device__ __forceinline__ void to_mma() {
 }
 
 // Run one GEMM and wait for its result (all threads).  False on timeout.
+template <int SPLIT>
 __device__ __forceinline__ bool gemm(Issuer &I, Shared &S, uint8_t *sA, uint32_t tmem, uint32_t &phase) {
     to_mma();
-    if (threadIdx.x == 0 && !S.abort && !issue_gemm(I, S, sA, tmem)) S.abort = 1;
+    if (threadIdx.x == 0 && !S.abort && !issue_gemm<SPLIT>(I, S, sA, tmem)) S.abort = 1;
     __syncthreads();
     if (S.abort) return false;
     if (!mbar_wait(&S.mma_done, phase)) S.abort = 1;
@@ -249,6 +267,7 @@ __device__ __forceinline__ bool gemm(Issuer &I, Shared &S, uint8_t *sA, uint32_t
 // One surrogate evaluation of the tile whose inputs are in S.xh.  Every thread
 // works on row `row`, columns [col0, col0 + 64); threads 0..127 (slice 0) get
 // the row's value yv and input gradient G.  Returns false on a wait timeout.
+template <int SPLIT>
 __device__ bool tile_eval(const float *__restrict__ P, Issuer &I, Shared &S, uint8_t *sA, uint32_t tmem,
                           uint32_t &phase, float &yv, float (&G)[3]) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -262,20 +281,19 @@ __device__ bool tile_eval(const float *__restrict__ P, Issuer &I, Shared &S, uin
         float v[32];
 #pragma unroll
         for (int k = 0; k < 32; k++) {
-            const int j = j0 + k;
-            const float z = __ldg(P + OFF_W1 + j * 3) * x0 + __ldg(P + OFF_W1 + j * 3 + 1) * x1 +
-                            __ldg(P + OFF_W1 + j * 3 + 2) * x2 + __ldg(P + OFF_B1 + j);
+            const float4 w = S.w1b1[j0 + k];
+            const float z = fmaf(w.x, x0, fmaf(w.y, x1, fmaf(w.z, x2, w.w)));
             float s1;
             silu2(z, v[k], s1);
         }
-        put_a(sA, row, j0, v);
+        put_a<SPLIT>(sA, row, j0, v);
     }
     // layers 2..4
     float y = 0.f;
 #pragma unroll 1
     for (int l = 2; l <= 4; l++) {
-        if (!gemm(I, S, sA, tmem, phase)) return false;
-        const float *b = P + off_b(l);
+        if (!gemm<SPLIT>(I, S, sA, tmem, phase)) return false;
+        const float *b = S.bias[l - 2];
 #pragma unroll 1
         for (int j0 = col0; j0 < col0 + SLICE; j0 += 32) {
             float v[32];
@@ -284,10 +302,12 @@ __device__ bool tile_eval(const float *__restrict__ P, Issuer &I, Shared &S, uin
 #pragma unroll
             for (int k = 0; k < 32; k += 2) {
                 float a0, s0, a1, s1;
-                silu2(v[k] + __ldg(b + j0 + k), a0, s0);
-                silu2(v[k + 1] + __ldg(b + j0 + k + 1), a1, s1);
+                const float2 bb = *reinterpret_cast<const float2 *>(b + j0 + k);
+                silu2(v[k] + bb.x, a0, s0);
+                silu2(v[k + 1] + bb.y, a1, s1);
                 if (l == 4) {
-                    const float w0 = __ldg(P + OFF_W5 + j0 + k), w1 = __ldg(P + OFF_W5 + j0 + k + 1);
+                    const float2 ww = *reinterpret_cast<const float2 *>(S.w5 + j0 + k);
+                    const float w0 = ww.x, w1 = ww.y;
                     y += a0 * w0 + a1 * w1;
                     v[k] = w0 * s0;  // backward seed delta_4 = w5 * silu'(z4)
                     v[k + 1] = w1 * s1;
@@ -299,7 +319,7 @@ __device__ bool tile_eval(const float *__restrict__ P, Issuer &I, Shared &S, uin
                 }
             }
             if (l < 4) tm_st16(tmem + lane_base + (l == 2 ? COL_SP2 : COL_SP3) + (j0 >> 1), sp);
-            put_a(sA, row, j0, v);
+            put_a<SPLIT>(sA, row, j0, v);
         }
         asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
     }
@@ -308,7 +328,7 @@ __device__ bool tile_eval(const float *__restrict__ P, Issuer &I, Shared &S, uin
     float g0 = 0.f, g1 = 0.f, g2 = 0.f;
 #pragma unroll 1
     for (int l = 3; l >= 1; l--) {
-        if (!gemm(I, S, sA, tmem, phase)) return false;
+        if (!gemm<SPLIT>(I, S, sA, tmem, phase)) return false;
 #pragma unroll 1
         for (int j0 = col0; j0 < col0 + SLICE; j0 += 32) {
             float v[32];
@@ -322,20 +342,18 @@ __device__ bool tile_eval(const float *__restrict__ P, Issuer &I, Shared &S, uin
                     v[k] *= sv.x;
                     v[k + 1] *= sv.y;
                 }
-                put_a(sA, row, j0, v);
+                put_a<SPLIT>(sA, row, j0, v);
             } else {
 #pragma unroll
                 for (int k = 0; k < 32; k++) {
-                    const int j = j0 + k;
-                    const float w0 = __ldg(P + OFF_W1 + j * 3), w1 = __ldg(P + OFF_W1 + j * 3 + 1),
-                                w2 = __ldg(P + OFF_W1 + j * 3 + 2);
-                    const float z = w0 * x0 + w1 * x1 + w2 * x2 + __ldg(P + OFF_B1 + j);
+                    const float4 w = S.w1b1[j0 + k];
+                    const float z = fmaf(w.x, x0, fmaf(w.y, x1, fmaf(w.z, x2, w.w)));
                     float a, s1;
                     silu2(z, a, s1);
                     const float d = v[k] * s1;
-                    g0 += d * w0;
-                    g1 += d * w1;
-                    g2 += d * w2;
+                    g0 = fmaf(d, w.x, g0);
+                    g1 = fmaf(d, w.y, g1);
+                    g2 = fmaf(d, w.z, g2);
                 }
             }
         }
@@ -387,7 +405,7 @@ struct Ctx {
 };
 
 // Set up shared state, barriers and TMEM; start the first two weight copies.
-__device__ __forceinline__ void ctx_init(Ctx &C, const uint8_t *wimg, char *smem_raw) {
+__device__ __forceinline__ void ctx_init(Ctx &C, const float *__restrict__ P, const uint8_t *wimg, char *smem_raw) {
     uint8_t *base = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     C.sA = base;
     C.I.sW = base + 2 * A_PART;
@@ -404,6 +422,13 @@ __device__ __forceinline__ void ctx_init(Ctx &C, const uint8_t *wimg, char *smem
         mbar_init(&S.mma_done, 1);
         S.abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int j = threadIdx.x; j < H; j += blockDim.x) {
+        S.w1b1[j] = make_float4(P[OFF_W1 + j * 3], P[OFF_W1 + j * 3 + 1], P[OFF_W1 + j * 3 + 2], P[OFF_B1 + j]);
+        S.bias[0][j] = P[OFF_B2 + j];
+        S.bias[1][j] = P[OFF_B3 + j];
+        S.bias[2][j] = P[OFF_B4 + j];
+        S.w5[j] = P[OFF_W5 + j];
     }
     if ((threadIdx.x >> 5) == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(&S.tmem_base)),
@@ -438,6 +463,7 @@ __device__ __forceinline__ void ctx_finish(Ctx &C, int *status) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(C.tmem), "r"(TMEM_COLS));
 }
 
+template <int SPLIT>
 __global__ void __launch_bounds__(NT, 1) surrogate_eval_tc_kernel(InferArgs A, const float *__restrict__ P,
                                                                    const uint8_t *__restrict__ wimg,
                                                                    const double *__restrict__ q, int64_t n,
@@ -445,7 +471,7 @@ __global__ void __launch_bounds__(NT, 1) surrogate_eval_tc_kernel(InferArgs A, c
                                                                    int *status) {
     extern __shared__ char smem_raw[];
     Ctx C;
-    ctx_init(C, wimg, smem_raw);
+    ctx_init(C, P, wimg, smem_raw);
     Shared &S = *C.S;
     const bool owner = threadIdx.x < TM;
     const int64_t ntiles = (n + TM - 1) / TM;
@@ -467,7 +493,7 @@ __global__ void __launch_bounds__(NT, 1) surrogate_eval_tc_kernel(InferArgs A, c
         if (threadIdx.x == 0) S.fbcnt = 0;
         __syncthreads();
         float yv = 0.f, G[3] = {0.f, 0.f, 0.f};
-        if (!tile_eval(P, C.I, S, C.sA, C.tmem, C.phase, yv, G)) break;
+        if (!tile_eval<SPLIT>(P, C.I, S, C.sA, C.tmem, C.phase, yv, G)) break;
         const bool outside = owner && i < n && !(m.r >= A.r_min && m.r <= A.r_max);
         if (outside) {
             const int e = atomicAdd(&S.fbcnt, 1);
@@ -508,6 +534,7 @@ __device__ __forceinline__ void kahan(float &s, float &c, float d) {
 // Leapfrog (kick-drift-kick as c_leapfrog_step, leapfrog.pyx:35-51) in the
 // surrogate potential, FP32 state with Kahan compensation (as
 // surrogate_leapfrog_kernel of gx_mlp_infer.cu, with 128-orbit tiles).
+template <int SPLIT>
 __global__ void __launch_bounds__(NT, 1) surrogate_leapfrog_tc_kernel(InferArgs A, const float *__restrict__ P,
                                                                        const uint8_t *__restrict__ wimg,
                                                                        const double *__restrict__ w0, int64_t n,
@@ -517,7 +544,7 @@ __global__ void __launch_bounds__(NT, 1) surrogate_leapfrog_tc_kernel(InferArgs 
                                                                        int *status) {
     extern __shared__ char smem_raw[];
     Ctx C;
-    ctx_init(C, wimg, smem_raw);
+    ctx_init(C, P, wimg, smem_raw);
     Shared &S = *C.S;
     const int64_t ntiles = (n + TM - 1) / TM;
     bool ok = true;
@@ -546,7 +573,7 @@ __global__ void __launch_bounds__(NT, 1) surrogate_leapfrog_tc_kernel(InferArgs 
             if (threadIdx.x == 0) S.fbcnt = 0;
             __syncthreads();
             float yv = 0.f, G[3] = {0.f, 0.f, 0.f};
-            if (!tile_eval(P, C.I, S, C.sA, C.tmem, C.phase, yv, G)) {
+            if (!tile_eval<SPLIT>(P, C.I, S, C.sA, C.tmem, C.phase, yv, G)) {
                 ok = false;
                 break;
             }
@@ -600,18 +627,22 @@ static int tc_args(const float *scf_params, double r_min, double r_max, double G
     A->scf = scf_params;
     static bool configured = false;
     if (!configured) {
-        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_eval_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_eval_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          SMEM_BYTES));
-        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_leapfrog_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_eval_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          SMEM_BYTES));
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_leapfrog_tc_kernel<1>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_leapfrog_tc_kernel<2>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
         configured = true;
     }
     return GX_OK;
 }
 
 extern "C" int gx_surrogate_gradient_tc(const float *params, const void *wimg, const float *scf_params, double r_min,
-                                        double r_max, double GM, double r_s, const double *q, int64_t n, double *grad,
-                                        double *phi, int32_t grid, int32_t *status, void *stream) {
+                                        double r_max, double GM, double r_s, int32_t split, const double *q, int64_t n,
+                                        double *grad, double *phi, int32_t grid, int32_t *status, void *stream) {
     InferArgs A;
     int rc = tc_args(scf_params, r_min, r_max, GM, r_s, &A);
     if (rc) return rc;
@@ -619,15 +650,20 @@ extern "C" int gx_surrogate_gradient_tc(const float *params, const void *wimg, c
     if (n == 0) return GX_OK;
     GX_CHECK_ARG(params && wimg && q && grad && status && grid >= 1, "NULL array or bad grid");
     GX_CHECK_ARG(((uintptr_t)wimg & 15) == 0, "weight image must be 16-byte aligned");
-    surrogate_eval_tc_kernel<<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
-        A, params, static_cast<const uint8_t *>(wimg), q, n, grad, phi, status);
+    GX_CHECK_ARG(split == 1 || split == 2, "split must be 1 (BF16 activations) or 2 (BF16 hi + lo)");
+    if (split == 2)
+        surrogate_eval_tc_kernel<2><<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
+            A, params, static_cast<const uint8_t *>(wimg), q, n, grad, phi, status);
+    else
+        surrogate_eval_tc_kernel<1><<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
+            A, params, static_cast<const uint8_t *>(wimg), q, n, grad, phi, status);
     return gx::check_launch("surrogate_gradient_tc");
 }
 
 extern "C" int gx_surrogate_leapfrog_tc(const float *params, const void *wimg, const float *scf_params, double r_min,
-                                        double r_max, double GM, double r_s, const double *w0, int64_t n,
-                                        int64_t n_steps, double dt, double *w_out, unsigned long long *fallbacks,
-                                        int32_t grid, int32_t *status, void *stream) {
+                                        double r_max, double GM, double r_s, int32_t split, const double *w0,
+                                        int64_t n, int64_t n_steps, double dt, double *w_out,
+                                        unsigned long long *fallbacks, int32_t grid, int32_t *status, void *stream) {
     InferArgs A;
     int rc = tc_args(scf_params, r_min, r_max, GM, r_s, &A);
     if (rc) return rc;
@@ -635,8 +671,13 @@ extern "C" int gx_surrogate_leapfrog_tc(const float *params, const void *wimg, c
     if (n == 0) return GX_OK;
     GX_CHECK_ARG(params && wimg && w0 && w_out && fallbacks && status && grid >= 1, "NULL array or bad grid");
     GX_CHECK_ARG(((uintptr_t)wimg & 15) == 0, "weight image must be 16-byte aligned");
-    surrogate_leapfrog_tc_kernel<<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
-        A, params, static_cast<const uint8_t *>(wimg), w0, n, n_steps, (float)dt, w_out, fallbacks, status);
+    GX_CHECK_ARG(split == 1 || split == 2, "split must be 1 (BF16 activations) or 2 (BF16 hi + lo)");
+    if (split == 2)
+        surrogate_leapfrog_tc_kernel<2><<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
+            A, params, static_cast<const uint8_t *>(wimg), w0, n, n_steps, (float)dt, w_out, fallbacks, status);
+    else
+        surrogate_leapfrog_tc_kernel<1><<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
+            A, params, static_cast<const uint8_t *>(wimg), w0, n, n_steps, (float)dt, w_out, fallbacks, status);
     return gx::check_launch("surrogate_leapfrog_tc");
 }
 

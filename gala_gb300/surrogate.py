@@ -274,8 +274,8 @@ class SurrogatePotential:
         if engine == "tcgen05":
             status = torch.zeros(1, dtype=torch.int32, device=self.dev)
             _abi.call("gx_surrogate_gradient_tc", ptr(self.params), ptr(self.wimg), ptr(self.scf_f32), self.r_min,
-                      self.r_max, self.GM, self.r_s, ptr(qd), n, ptr(grad), ptr(phi), self._grid(n, 128),
-                      ptr(status), stream_handle())
+                      self.r_max, self.GM, self.r_s, self.split, ptr(qd), n, ptr(grad), ptr(phi),
+                      self._grid(n, 128), ptr(status), stream_handle())
             self._check(status)
         else:
             _abi.call("gx_surrogate_gradient", ptr(self.params), ptr(self.wbf16), ptr(self.scf_f32), self.r_min,
@@ -306,8 +306,8 @@ class SurrogatePotential:
         if (engine or self.engine) == "tcgen05" and not analytic:
             status = torch.zeros(1, dtype=torch.int32, device=self.dev)
             _abi.call("gx_surrogate_leapfrog_tc", ptr(self.params), ptr(self.wimg), ptr(self.scf_f32), self.r_min,
-                      self.r_max, self.GM, self.r_s, ptr(w0d), n, int(n_steps), float(dt), ptr(out), ptr(fb),
-                      grid or self._grid(n, 128), ptr(status), stream_handle())
+                      self.r_max, self.GM, self.r_s, self.split, ptr(w0d), n, int(n_steps), float(dt), ptr(out),
+                      ptr(fb), grid or self._grid(n, 128), ptr(status), stream_handle())
             self._check(status)
             return out, fb
         wb = ptr(self.wbf16) if self.wbf16 is not None else None

@@ -310,15 +310,17 @@ int gx_surrogate_smem_bytes(void);
  * W3^T, W2^T (BF16, [256 out][256 in] row-major) four 32 KB K-chunks of 64
  * columns, each 256 rows x 128 bytes, the 16-byte granule g of row r stored at
  * position g ^ (r & 7) (the 128-byte swizzle); 786,432 bytes, 16-byte aligned.
- * `status` (DEVICE int32) is set to 1 if a bounded wait inside the kernel ran
- * out (the results are then incomplete); the caller zeroes it. */
+ * split = 2 multiplies BF16 hi and lo parts of every activation (two MMAs per
+ * K step), split = 1 the BF16 activations only.  `status` (DEVICE int32) is set
+ * to 1 if a bounded wait inside the kernel ran out (the results are then
+ * incomplete); the caller zeroes it. */
 int gx_surrogate_gradient_tc(const float* params, const void* wimg, const float* scf_params,
-                             double r_min, double r_max, double GM, double r_s, const double* q,
-                             int64_t n, double* grad, double* phi, int32_t grid, int32_t* status,
-                             void* stream);
+                             double r_min, double r_max, double GM, double r_s, int32_t split,
+                             const double* q, int64_t n, double* grad, double* phi, int32_t grid,
+                             int32_t* status, void* stream);
 int gx_surrogate_leapfrog_tc(const float* params, const void* wimg, const float* scf_params,
-                             double r_min, double r_max, double GM, double r_s, const double* w0,
-                             int64_t n, int64_t n_steps, double dt, double* w_out,
+                             double r_min, double r_max, double GM, double r_s, int32_t split,
+                             const double* w0, int64_t n, int64_t n_steps, double dt, double* w_out,
                              unsigned long long* fallbacks, int32_t grid, int32_t* status,
                              void* stream);
 int gx_surrogate_tc_smem_bytes(void);

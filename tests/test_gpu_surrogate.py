@@ -171,7 +171,8 @@ def test_surrogate_leapfrog_runs_and_matches_fp32_forces(scf):
 
 def test_tcgen05_matches_mma_engine(scf):
     """Both tensor-core engines run BF16 weights with BF16 hi + lo activations
-    and FP32 accumulation; they differ only in accumulation order, far below
+    and FP32 accumulation; they differ in accumulation order and in the SiLU
+    (the tcgen05 kernel uses tanh.approx, relative error ~2^-11), both below
     the BF16 weight rounding.  Sizes that are not a multiple of the 128-row
     tile exercise the partial last tile."""
     sp = S.SurrogatePotential(scf, seed=8)
@@ -181,9 +182,9 @@ def test_tcgen05_matches_mma_engine(scf):
         g_tc, p_tc = sp.gradient_and_energy(x, engine="tcgen05")
         g_mm, p_mm = sp.gradient_and_energy(x, engine="mma")
         d = np.linalg.norm((g_tc - g_mm).cpu().numpy(), axis=0) / np.linalg.norm(g_mm.cpu().numpy(), axis=0)
-        assert np.median(d) < 1e-4 and np.max(d) < 1e-2, (n, np.median(d), np.max(d))
+        assert np.median(d) < 1e-3 and np.max(d) < 2e-2, (n, np.median(d), np.max(d))
         np.testing.assert_allclose(p_tc.cpu().numpy(), p_mm.cpu().numpy(), rtol=0,
-                                   atol=1e-4 * np.abs(p_mm.cpu().numpy()).max())
+                                   atol=1e-3 * np.abs(p_mm.cpu().numpy()).max())
 
 
 def test_tcgen05_leapfrog_matches_mma_leapfrog(scf):
@@ -193,6 +194,6 @@ def test_tcgen05_leapfrog_matches_mma_leapfrog(scf):
     o_tc, fb_tc = sp.integrate_leapfrog(w0, 1.0, 50, engine="tcgen05")
     o_mm, fb_mm = sp.integrate_leapfrog(w0, 1.0, 50, engine="mma")
     err = np.linalg.norm((o_tc - o_mm)[:3].cpu().numpy(), axis=0) / np.linalg.norm(o_mm[:3].cpu().numpy(), axis=0)
-    assert np.median(err) < 1e-5, np.median(err)
+    assert np.median(err) < 1e-4, np.median(err)
     assert int(fb_tc.item()) == int(fb_mm.item())
 

@@ -449,9 +449,11 @@ int gx_mockstream_leapfrog_fp32(const gx_potential* pot, int64_t n_streams, int3
  * and their sum (in increasing time), minimum and maximum.  A grid with
  * t[ntimes-1] < t[0] is scanned from the end, as gala reverses it.
  *   count             DEVICE int32 (3, N)
- *   sum, vmin, vmax   DEVICE double (3, N)
+ *   sum, vmin, vmax   DEVICE double (3, N); vmin and vmax are NaN where
+ *                     count is 0
  *   vals, times       DEVICE double (3, N, keep): the first `keep` extrema, or
- *                     NULL with keep = 0 */
+ *                     NULL with keep = 0
+ * ntimes must be below 2^31. */
 int gx_orbit_extrema(const double* w, const double* t, int64_t ntimes, int64_t n,
                      int32_t approximate, int32_t keep, int32_t* count, double* sum,
                      double* vmin, double* vmax, double* vals, double* times, void* stream);

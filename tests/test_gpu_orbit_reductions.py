@@ -63,3 +63,57 @@ def test_too_short_orbit_gives_nan():
     mw = W.mw_composite()
     o = mw.integrate_orbit(W.mw_ics(3, seed=79), dt=1.0, n_steps=1, Integrator="leapfrog")
     assert np.all(np.isnan(o.pericenter()))
+
+
+def _check_all(orbit, approx_rtol=1e-14):
+    w, t = orbit.w(), orbit.t
+    span = abs(t[-1] - t[0])
+    for kind, meth in (("peri", orbit.pericenter), ("apo", orbit.apocenter), ("zmax", orbit.zmax)):
+        ref = OO.extrema(w, t, kind)
+        vals, times = meth(func=None, return_times=True)
+        for (rv, rt), v, tt in zip(ref, vals, times):
+            assert len(v) == len(rv)
+            np.testing.assert_allclose(v, rv, rtol=1e-9, atol=0)
+            np.testing.assert_allclose(tt, rt, rtol=0, atol=1e-9 * span)
+        cnt = np.array([len(rv) for rv, _ in ref])
+        for func in (np.mean, np.min, np.max):
+            got = meth(func=func)
+            exp = np.array([func(rv) if len(rv) else np.nan for rv, _ in ref])
+            np.testing.assert_allclose(got, exp, rtol=1e-9)
+            assert np.array_equal(np.isnan(got), cnt == 0)
+        np.testing.assert_allclose(meth(approximate=True),
+                                   np.array([np.mean(rv) if len(rv) else np.nan
+                                             for rv, _ in OO.extrema(w, t, kind, approximate=True)]),
+                                   rtol=approx_rtol)
+
+
+def test_dense_extrema_fill_the_staging_rings():
+    """Zig-zag samples: about a third of all samples are strict local maxima of
+    |z| and of r, so every warp stages and checks its candidates many times per
+    chunk of samples; 300 orbits (two full 128-orbit blocks and a ragged one)
+    and 1,003 samples (not a multiple of the 8-sample chunk)."""
+    rng = np.random.default_rng(5)
+    n, nt = 300, 1003
+    t = np.linspace(0.0, 50.0, nt)
+    sign = np.where(np.arange(nt) % 2 == 0, 1.0, -1.0)[:, None]
+    pos = np.empty((3, nt, n))
+    pos[0] = 5.0 + rng.uniform(-1, 1, (nt, n))
+    pos[1] = rng.uniform(-2, 2, (nt, n))
+    pos[2] = sign * (1.0 + 0.5 * rng.uniform(0, 1, (nt, n)))
+    vel = np.zeros_like(pos)
+    _check_all(g.Orbit(pos=pos, vel=vel, t=t), approx_rtol=1e-13)
+
+
+def test_planar_and_smooth_orbits_ragged_sizes():
+    """Orbits in the plane z = 0 (no z maxima at all: NaN statistics) beside
+    smooth epicyclic orbits, with a descending time grid and 37 orbits."""
+    n, nt = 37, 2005
+    t = np.linspace(100.0, 0.0, nt)
+    ph = np.linspace(0, 2 * np.pi, n, endpoint=False)[None, :]
+    tt = t[:, None]
+    R = 8.0 + 1.5 * np.cos(0.37 * tt + ph)
+    pos = np.stack([R * np.cos(0.11 * tt), R * np.sin(0.11 * tt), 0.7 * np.sin(0.53 * tt + 2 * ph)])
+    pos[2, :, ::3] = 0.0
+    _check_all(g.Orbit(pos=pos, vel=np.zeros_like(pos), t=t))
+    z = g.Orbit(pos=pos, vel=np.zeros_like(pos), t=t).zmax()
+    assert np.all(np.isnan(z[::3])) and not np.any(np.isnan(np.delete(z, np.s_[::3])))

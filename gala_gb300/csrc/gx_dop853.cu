@@ -19,6 +19,7 @@
 #include "gx_host.h"
 #include "gx_scf.cuh"
 #include "gx_dop853_tableau.cuh"
+#include "gx_fast64.cuh"
 
 namespace gx {
 
@@ -63,7 +64,7 @@ __device__ __forceinline__ double max_d(double a, double b) { return (a > b) ? a
         if (active) {                                                    \
             V6 a_;                                                       \
             for (int c_ = 0; c_ < 6; c_++) a_.v[c_] = yin[c_];           \
-            const V6 r_ = rhs_call<SCF>(pot, fr, a_);                    \
+            const V6 r_ = fast::rhs_call_f<SCF>(pot, fr, a_);            \
             for (int c_ = 0; c_ < 6; c_++) kout[c_] = r_.v[c_];          \
         } else {                                                         \
             for (int c_ = 0; c_ < 6; c_++) kout[c_] = 0.;                \
@@ -94,7 +95,7 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
     double h = t[1] - t[0];
     double hmax = A.dt_max;
     const double uround = 2.220446049250313e-16;
-    const double safe = 0.9, fac1 = 0.333, fac2 = 6.0, beta = 0.0;
+    const double safe = 0.9, fac1 = 0.333, fac2 = 6.0;  // and beta = 0
     int64_t nmax = A.nmax, nstiff = A.nstiff;
     if (!nmax) nmax = 1000000;
     if (!nstiff) nstiff = 1000;
@@ -102,7 +103,6 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
     if (hmax == 0.0) hmax = xend - x;
 
     double facold = 1.0E-4;
-    const double expo1 = 1.0 / 8.0 - beta * 0.2;
     const double facc1 = 1.0 / fac1, facc2 = 1.0 / fac2;
     const double posneg = sign_d(1.0, xend - x);
     const double atoli = A.atol, rtoli = A.rtol;
@@ -155,56 +155,60 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
         nstep++;
 
         // the twelve stages (dop853.cpp:368-414)
-        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * a21 * k1[c];
+        // stage sums as fused multiply-add chains in gala's term order
+        for (int c = 0; c < 6; c++) yy1[c] = fma(h * a21, k1[c], y[c]);
         RHS(yy1, k2);
-        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a31 * k1[c] + a32 * k2[c]);
+        for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a32, k2[c], a31 * k1[c]), y[c]);
         RHS(yy1, k3);
-        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a41 * k1[c] + a43 * k3[c]);
+        for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a43, k3[c], a41 * k1[c]), y[c]);
         RHS(yy1, k4);
-        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a51 * k1[c] + a53 * k3[c] + a54 * k4[c]);
+        for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a54, k4[c], fma(a53, k3[c], a51 * k1[c])), y[c]);
         RHS(yy1, k5);
-        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a61 * k1[c] + a64 * k4[c] + a65 * k5[c]);
+        for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a65, k5[c], fma(a64, k4[c], a61 * k1[c])), y[c]);
         RHS(yy1, k6);
-        for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a71 * k1[c] + a74 * k4[c] + a75 * k5[c] + a76 * k6[c]);
+        for (int c = 0; c < 6; c++)
+            yy1[c] = fma(h, fma(a76, k6[c], fma(a75, k5[c], fma(a74, k4[c], a71 * k1[c]))), y[c]);
         RHS(yy1, k7);
         for (int c = 0; c < 6; c++)
-            yy1[c] = y[c] + h * (a81 * k1[c] + a84 * k4[c] + a85 * k5[c] + a86 * k6[c] + a87 * k7[c]);
+            yy1[c] = fma(h, fma(a87, k7[c], fma(a86, k6[c], fma(a85, k5[c], fma(a84, k4[c], a81 * k1[c])))), y[c]);
         RHS(yy1, k8);
         for (int c = 0; c < 6; c++)
-            yy1[c] = y[c] + h * (a91 * k1[c] + a94 * k4[c] + a95 * k5[c] + a96 * k6[c] + a97 * k7[c] + a98 * k8[c]);
+            yy1[c] = fma(h, fma(a98, k8[c], fma(a97, k7[c], fma(a96, k6[c], fma(a95, k5[c], fma(a94, k4[c],
+                                                                                                a91 * k1[c]))))),
+                         y[c]);
         RHS(yy1, k9);
         for (int c = 0; c < 6; c++)
-            yy1[c] = y[c] + h * (a101 * k1[c] + a104 * k4[c] + a105 * k5[c] + a106 * k6[c] + a107 * k7[c] +
-                                 a108 * k8[c] + a109 * k9[c]);
+            yy1[c] = fma(h, fma(a109, k9[c], fma(a108, k8[c], fma(a107, k7[c], fma(a106, k6[c], fma(a105, k5[c],
+                                fma(a104, k4[c], a101 * k1[c])))))), y[c]);
         RHS(yy1, k10);
         for (int c = 0; c < 6; c++)
-            yy1[c] = y[c] + h * (a111 * k1[c] + a114 * k4[c] + a115 * k5[c] + a116 * k6[c] + a117 * k7[c] +
-                                 a118 * k8[c] + a119 * k9[c] + a1110 * k10[c]);
+            yy1[c] = fma(h, fma(a1110, k10[c], fma(a119, k9[c], fma(a118, k8[c], fma(a117, k7[c], fma(a116, k6[c],
+                                fma(a115, k5[c], fma(a114, k4[c], a111 * k1[c]))))))), y[c]);
         RHS(yy1, k2);
         const double xph = x + h;
         for (int c = 0; c < 6; c++)
-            yy1[c] = y[c] + h * (a121 * k1[c] + a124 * k4[c] + a125 * k5[c] + a126 * k6[c] + a127 * k7[c] +
-                                 a128 * k8[c] + a129 * k9[c] + a1210 * k10[c] + a1211 * k2[c]);
+            yy1[c] = fma(h, fma(a1211, k2[c], fma(a1210, k10[c], fma(a129, k9[c], fma(a128, k8[c], fma(a127, k7[c],
+                                fma(a126, k6[c], fma(a125, k5[c], fma(a124, k4[c], a121 * k1[c])))))))), y[c]);
         RHS(yy1, k3);
         nfcn += 11;
         for (int c = 0; c < 6; c++) {
-            k4[c] = b1 * k1[c] + b6 * k6[c] + b7 * k7[c] + b8 * k8[c] + b9 * k9[c] + b10 * k10[c] + b11 * k2[c] +
-                    b12 * k3[c];
-            k5[c] = y[c] + h * k4[c];
+            k4[c] = fma(b12, k3[c], fma(b11, k2[c], fma(b10, k10[c], fma(b9, k9[c], fma(b8, k8[c], fma(b7, k7[c],
+                        fma(b6, k6[c], b1 * k1[c])))))));
+            k5[c] = fma(h, k4[c], y[c]);
         }
 
         // error estimation (:416-444), summed over the whole batch
         double err = 0.0, err2 = 0.0;
         if (active) {
             for (int c = 0; c < 6; c++) {
-                const double sk = atoli + rtoli * max_d(fabs(y[c]), fabs(k5[c]));
-                double erri = k4[c] - bhh1 * k1[c] - bhh2 * k9[c] - bhh3 * k3[c];
-                double sqr = erri / sk;
-                err2 += sqr * sqr;
-                erri = er1 * k1[c] + er6 * k6[c] + er7 * k7[c] + er8 * k8[c] + er9 * k9[c] + er10 * k10[c] +
-                       er11 * k2[c] + er12 * k3[c];
-                sqr = erri / sk;
-                err += sqr * sqr;
+                const double isk = fast::rcp_f(fma(rtoli, fmax(fabs(y[c]), fabs(k5[c])), atoli));
+                double erri = fma(-bhh3, k3[c], fma(-bhh2, k9[c], fma(-bhh1, k1[c], k4[c])));
+                double sqr = erri * isk;
+                err2 = fma(sqr, sqr, err2);
+                erri = fma(er12, k3[c], fma(er11, k2[c], fma(er10, k10[c], fma(er9, k9[c], fma(er8, k8[c],
+                           fma(er7, k7[c], fma(er6, k6[c], er1 * k1[c])))))));
+                sqr = erri * isk;
+                err = fma(sqr, sqr, err);
             }
         }
         block_sum2(err, err2, red);
@@ -213,7 +217,9 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
         err = fabs(h) * err * sqrt(1.0 / (deno * (double)nsys));
 
         // computation of hnew (:446-452)
-        const double fac11 = pow(err, expo1);
+        // gala's pow(err, expo1) with expo1 = 1/8 (beta = 0): three square roots
+        // instead of pow's ~84 FP64-pipe instructions
+        const double fac11 = sqrt(sqrt(sqrt(err)));
         double fac = fac11;  // gala divides by pow(facold, beta) == 1 for its beta = 0
         fac = max_d(facc2, min_d(facc1, fac / safe));
         double hnew = h / fac;
@@ -251,41 +257,41 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
             if (A.save_all) {
                 // dense output preparation (:492-582)
                 double r5[6], r6[6], r7[6], r8[6];
+#define GX_D8(p, k1_, k6_, k7_, k8_, k9_, k10_, k2_, k3_)                                                      \
+    fma(p##12, k3_, fma(p##11, k2_, fma(p##10, k10_, fma(p##9, k9_, fma(p##8, k8_, fma(p##7, k7_,              \
+        fma(p##6, k6_, p##1 * k1_)))))))
                 for (int c = 0; c < 6; c++) {
-                    r5[c] = d41 * k1[c] + d46 * k6[c] + d47 * k7[c] + d48 * k8[c] + d49 * k9[c] + d410 * k10[c] +
-                            d411 * k2[c] + d412 * k3[c];
-                    r6[c] = d51 * k1[c] + d56 * k6[c] + d57 * k7[c] + d58 * k8[c] + d59 * k9[c] + d510 * k10[c] +
-                            d511 * k2[c] + d512 * k3[c];
-                    r7[c] = d61 * k1[c] + d66 * k6[c] + d67 * k7[c] + d68 * k8[c] + d69 * k9[c] + d610 * k10[c] +
-                            d611 * k2[c] + d612 * k3[c];
-                    r8[c] = d71 * k1[c] + d76 * k6[c] + d77 * k7[c] + d78 * k8[c] + d79 * k9[c] + d710 * k10[c] +
-                            d711 * k2[c] + d712 * k3[c];
+                    r5[c] = GX_D8(d4, k1[c], k6[c], k7[c], k8[c], k9[c], k10[c], k2[c], k3[c]);
+                    r6[c] = GX_D8(d5, k1[c], k6[c], k7[c], k8[c], k9[c], k10[c], k2[c], k3[c]);
+                    r7[c] = GX_D8(d6, k1[c], k6[c], k7[c], k8[c], k9[c], k10[c], k2[c], k3[c]);
+                    r8[c] = GX_D8(d7, k1[c], k6[c], k7[c], k8[c], k9[c], k10[c], k2[c], k3[c]);
                 }
+#undef GX_D8
                 for (int c = 0; c < 6; c++)
-                    yy1[c] = y[c] + h * (a141 * k1[c] + a147 * k7[c] + a148 * k8[c] + a149 * k9[c] +
-                                         a1410 * k10[c] + a1411 * k2[c] + a1412 * k3[c] + a1413 * k4[c]);
+                    yy1[c] = fma(h, fma(a1413, k4[c], fma(a1412, k3[c], fma(a1411, k2[c], fma(a1410, k10[c],
+                                 fma(a149, k9[c], fma(a148, k8[c], fma(a147, k7[c], a141 * k1[c]))))))), y[c]);
                 RHS(yy1, k10);
                 for (int c = 0; c < 6; c++)
-                    yy1[c] = y[c] + h * (a151 * k1[c] + a156 * k6[c] + a157 * k7[c] + a158 * k8[c] +
-                                         a1511 * k2[c] + a1512 * k3[c] + a1513 * k4[c] + a1514 * k10[c]);
+                    yy1[c] = fma(h, fma(a1514, k10[c], fma(a1513, k4[c], fma(a1512, k3[c], fma(a1511, k2[c],
+                                 fma(a158, k8[c], fma(a157, k7[c], fma(a156, k6[c], a151 * k1[c]))))))), y[c]);
                 RHS(yy1, k2);
                 for (int c = 0; c < 6; c++)
-                    yy1[c] = y[c] + h * (a161 * k1[c] + a166 * k6[c] + a167 * k7[c] + a168 * k8[c] +
-                                         a169 * k9[c] + a1613 * k4[c] + a1614 * k10[c] + a1615 * k2[c]);
+                    yy1[c] = fma(h, fma(a1615, k2[c], fma(a1614, k10[c], fma(a1613, k4[c], fma(a169, k9[c],
+                                 fma(a168, k8[c], fma(a167, k7[c], fma(a166, k6[c], a161 * k1[c]))))))), y[c]);
                 RHS(yy1, k3);
                 nfcn += 3;
                 double r1[6], r2[6], r3[6], r4[6];
                 for (int c = 0; c < 6; c++) {
-                    r5[c] = h * (r5[c] + d413 * k4[c] + d414 * k10[c] + d415 * k2[c] + d416 * k3[c]);
-                    r6[c] = h * (r6[c] + d513 * k4[c] + d514 * k10[c] + d515 * k2[c] + d516 * k3[c]);
-                    r7[c] = h * (r7[c] + d613 * k4[c] + d614 * k10[c] + d615 * k2[c] + d616 * k3[c]);
-                    r8[c] = h * (r8[c] + d713 * k4[c] + d714 * k10[c] + d715 * k2[c] + d716 * k3[c]);
+                    r5[c] = h * fma(d416, k3[c], fma(d415, k2[c], fma(d414, k10[c], fma(d413, k4[c], r5[c]))));
+                    r6[c] = h * fma(d516, k3[c], fma(d515, k2[c], fma(d514, k10[c], fma(d513, k4[c], r6[c]))));
+                    r7[c] = h * fma(d616, k3[c], fma(d615, k2[c], fma(d614, k10[c], fma(d613, k4[c], r7[c]))));
+                    r8[c] = h * fma(d716, k3[c], fma(d715, k2[c], fma(d714, k10[c], fma(d713, k4[c], r8[c]))));
                     r1[c] = y[c];
                     const double ydiff = k5[c] - y[c];
                     r2[c] = ydiff;
-                    const double bspl = h * k1[c] - ydiff;
+                    const double bspl = fma(h, k1[c], -ydiff);
                     r3[c] = bspl;
-                    r4[c] = ydiff - h * k4[c] - bspl;
+                    r4[c] = fma(-h, k4[c], ydiff) - bspl;
                 }
 
                 // every output time inside [xold, xold + hout] (:584-612)
@@ -299,8 +305,8 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
                         if (active) {
                             for (int c = 0; c < 6; c++) {
                                 const double v =
-                                    r1[c] + s * (r2[c] + s1 * (r3[c] + s * (r4[c] +
-                                                 s1 * (r5[c] + s * (r6[c] + s1 * (r7[c] + s * r8[c]))))));
+                                    fma(s, fma(s1, fma(s, fma(s1, fma(s, fma(s1, fma(s, r8[c], r7[c]), r6[c]),
+                                                                      r5[c]), r4[c]), r3[c]), r2[c]), r1[c]);
                                 __stcs(&out[((int64_t)c * A.n_out + out_slot) * n + i0 + j], v);
                             }
                         }

@@ -254,7 +254,22 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
                 }
             }
 
+            // Output times inside [xold, xold + hout] (:584-612): [out_idx, out_end).
+            // Only every out_stride-th time is stored; the three dense-output stages
+            // are evaluated only for a step that holds a stored time (their results
+            // feed nothing else: the next step starts from k4 = f(k5) and recomputes
+            // every other stage), so the trajectory is unchanged.
+            int64_t out_end = out_idx, first_kept = 0;
             if (A.save_all) {
+                const double x0 = xold, x1 = x0 + hout;
+                while (out_end < A.ntimes) {
+                    const double t_out = t[out_end];
+                    if (!((x0 <= t_out && t_out <= x1) || (x1 <= t_out && t_out <= x0))) break;
+                    out_end++;
+                }
+                first_kept = (out_idx + A.out_stride - 1) / A.out_stride * A.out_stride;
+            }
+            if (A.save_all && first_kept < out_end) {
                 // dense output preparation (:492-582)
                 double r5[6], r6[6], r7[6], r8[6];
 #define GX_D8(p, k1_, k6_, k7_, k8_, k9_, k10_, k2_, k3_)                                                      \
@@ -294,27 +309,21 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
                     r4[c] = fma(-h, k4[c], ydiff) - bspl;
                 }
 
-                // every output time inside [xold, xold + hout] (:584-612)
-                const double x0 = xold, x1 = x0 + hout;
-                while (out_idx < A.ntimes) {
-                    const double t_out = t[out_idx];
-                    if (!((x0 <= t_out && t_out <= x1) || (x1 <= t_out && t_out <= x0))) break;
-                    if (out_idx % A.out_stride == 0) {
-                        const double s = (t_out - xold) / hout;
-                        const double s1 = 1.0 - s;
-                        if (active) {
-                            for (int c = 0; c < 6; c++) {
-                                const double v =
-                                    fma(s, fma(s1, fma(s, fma(s1, fma(s, fma(s1, fma(s, r8[c], r7[c]), r6[c]),
-                                                                      r5[c]), r4[c]), r3[c]), r2[c]), r1[c]);
-                                __stcs(&out[((int64_t)c * A.n_out + out_slot) * n + i0 + j], v);
-                            }
+                for (int64_t oi = first_kept; oi < out_end; oi += A.out_stride) {
+                    const double s = (t[oi] - xold) / hout;
+                    const double s1 = 1.0 - s;
+                    if (active) {
+                        for (int c = 0; c < 6; c++) {
+                            const double v =
+                                fma(s, fma(s1, fma(s, fma(s1, fma(s, fma(s1, fma(s, r8[c], r7[c]), r6[c]), r5[c]),
+                                                          r4[c]), r3[c]), r2[c]), r1[c]);
+                            __stcs(&out[((int64_t)c * A.n_out + out_slot) * n + i0 + j], v);
                         }
-                        out_slot++;
                     }
-                    out_idx++;
+                    out_slot++;
                 }
             }
+            out_idx = out_end;
 
             for (int c = 0; c < 6; c++) {
                 k1[c] = k4[c];

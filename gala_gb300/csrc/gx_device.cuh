@@ -32,6 +32,11 @@ struct DevComp {
     int32_t inl;      // 1: parameters are in DevPot::p; 0: in pdev (SCF)
     double q0[3];
     double R[9];
+    // Constants derived from the parameters on the host (for the forms of
+    // gx_fast64.cuh): dc[0] = G m; Plummer, Miyamoto-Nagai: dc[1] = b^2;
+    // NFW: dc[1] = 1 / r_s, dc[2..4] = 1 / a^2, 1 / b^2, 1 / c^2 (1 where the
+    // shape has no such axis).
+    double dc[5];
 };
 
 struct DevPot {

@@ -73,7 +73,8 @@ __device__ __forceinline__ double norm3_sq_f(const double *q) { return fma(q[0],
 // references as comp_gradient in gx_device.cuh.
 template <bool SCF>
 __device__ __forceinline__ void comp_gradient_f(const DevPot &pot, int ci, const double *q, double *g) {
-    const int type = pot.c[ci].type;
+    const DevComp &C = pot.c[ci];
+    const int type = C.type;
 #define P(k) GX_PARAM(pot, ci, k)
     double fac;
     switch (type) {
@@ -81,25 +82,25 @@ __device__ __forceinline__ void comp_gradient_f(const DevPot &pot, int ci, const
         return;
     case GX_POT_KEPLER: {
         const double r = sqrt_f(norm3_sq_f(q));
-        fac = P(0) * P(1) * rcp_f(r * r * r);
+        fac = C.dc[0] * rcp_f(r * r * r);
         break;
     }
     case GX_POT_HERNQUIST: {
         const double r = sqrt_f(norm3_sq_f(q));
         const double rc = r + P(2);
-        fac = P(0) * P(1) * rcp_f(rc * rc * r);
+        fac = C.dc[0] * rcp_f(rc * rc * r);
         break;
     }
     case GX_POT_PLUMMER: {
-        const double R2b = fma(P(2), P(2), norm3_sq_f(q));
-        fac = P(0) * P(1) * rcp_f(R2b * sqrt_f(R2b));
+        const double R2b = norm3_sq_f(q) + C.dc[1];
+        fac = C.dc[0] * rcp_f(R2b * sqrt_f(R2b));
         break;
     }
     case GX_POT_MIYAMOTONAGAI: {
-        const double sqrtz = sqrt_f(fma(q[2], q[2], P(3) * P(3)));
+        const double sqrtz = sqrt_f(fma(q[2], q[2], C.dc[1]));
         const double zd = P(2) + sqrtz;
         const double W = fma(q[0], q[0], fma(q[1], q[1], zd * zd));
-        fac = P(0) * P(1) * rcp_f(W * sqrt_f(W));
+        fac = C.dc[0] * rcp_f(W * sqrt_f(W));
         g[0] = fma(fac, q[0], g[0]);
         g[1] = fma(fac, q[1], g[1]);
         g[2] = fma(fac * q[2], fma(P(2), rcp_f(sqrtz), 1.), g[2]);
@@ -110,21 +111,18 @@ __device__ __forceinline__ void comp_gradient_f(const DevPot &pot, int ci, const
     case GX_POT_TRIAXIALNFW: {
         // gala: v_h^2 / u^3 / r_s^2 (log(1 + u) - u / (1 + u)) with v_h^2 = G m / r_s
         // and u = m_r / r_s, m_r the (scaled) radius: G m / m_r^3 (...)
-        double sx = 1., sy = 1., sz = 1.;
-        if (type != GX_POT_SPHERICALNFW) sz = rcp_f(P(5) * P(5));
-        if (type == GX_POT_TRIAXIALNFW) {
-            sx = rcp_f(P(3) * P(3));
-            sy = rcp_f(P(4) * P(4));
-        }
-        const double mr2 = fma(q[0] * q[0], sx, fma(q[1] * q[1], sy, q[2] * q[2] * sz));
+        const bool sph = type == GX_POT_SPHERICALNFW;
+        const double mr2 = sph ? norm3_sq_f(q)
+                               : fma(q[0] * q[0], C.dc[2], fma(q[1] * q[1], C.dc[3], q[2] * q[2] * C.dc[4]));
         const double mr = sqrt_f(mr2);
-        const double u = mr * rcp_f(P(2));
+        const double u = mr * C.dc[1];
         const double mr3 = mr2 * mr, u1 = 1. + u;
         const double R = rcp_f(mr3 * u1);  // 1 / (m_r^3 (1 + u))
-        fac = P(0) * P(1) * (u1 * R) * fma(-u, mr3 * R, log(u1));
-        g[0] = fma(fac * sx, q[0], g[0]);
-        g[1] = fma(fac * sy, q[1], g[1]);
-        g[2] = fma(fac * sz, q[2], g[2]);
+        fac = C.dc[0] * (u1 * R) * fma(-u, mr3 * R, log(u1));
+        if (sph) break;
+        g[0] = fma(fac * C.dc[2], q[0], g[0]);
+        g[1] = fma(fac * C.dc[3], q[1], g[1]);
+        g[2] = fma(fac * C.dc[4], q[2], g[2]);
         return;
     }
     case GX_POT_SCF:

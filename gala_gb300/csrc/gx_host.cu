@@ -81,6 +81,21 @@ int pack_potential(const gx_potential *pot, DevPot *out) {
             d.poff = ninl;
             for (int k = 0; k < need; k++) out->p[ninl + k] = pot->params[c.param_offset + k];
             ninl += need;
+            const double *P = pot->params + c.param_offset;
+            d.dc[0] = P[0] * P[1];
+            switch (c.type) {
+            case GX_POT_PLUMMER: d.dc[1] = P[2] * P[2]; break;
+            case GX_POT_MIYAMOTONAGAI: d.dc[1] = P[3] * P[3]; break;
+            case GX_POT_SPHERICALNFW:
+            case GX_POT_FLATTENEDNFW:
+            case GX_POT_TRIAXIALNFW:
+                d.dc[1] = 1.0 / P[2];
+                d.dc[2] = c.type == GX_POT_TRIAXIALNFW ? 1.0 / (P[3] * P[3]) : 1.0;
+                d.dc[3] = c.type == GX_POT_TRIAXIALNFW ? 1.0 / (P[4] * P[4]) : 1.0;
+                d.dc[4] = c.type != GX_POT_SPHERICALNFW ? 1.0 / (P[5] * P[5]) : 1.0;
+                break;
+            default: break;
+            }
         }
     }
     out->n_inline = ninl;

@@ -19,13 +19,15 @@
 //
 // GPU mapping: a system is a GROUP of `gs` consecutive lanes of a warp, one
 // lane per body (32 / gs groups per warp).
-//   * Stage algebra runs per lane on its six components, in gala's expression
-//     order (this unit is compiled with -fmad=false).
+//   * Stage algebra runs per lane on its six components, in gala's term order
+//     as fused multiply-add chains, with the external force and the step
+//     controller in the FP64-pipe-lean forms of gx_fast64.cuh (this unit is
+//     compiled with -fmad=false: only the explicit fma calls fuse).
 //   * The n-body force broadcasts body j's position to the group with warp
 //     shuffles; each other lane adds -grad of body j's potential, j ascending.
 //   * The error norms and the stiffness sums are SEQUENTIAL sums in gala's
 //     component order: the running sum travels lane to lane (shuffle), each lane
-//     adding its six terms, so every norm has the bits of gala's loop.
+//     adding its six terms, so every norm sums in gala's order.
 //   * Groups take systems from a global counter, longest first; a group that
 //     finishes takes the next system at once, so a warp never idles on its
 //     slowest system.  Every loop is bounded by nmax like gala's.
@@ -33,6 +35,7 @@
 #include "gx_scf.cuh"
 #include "gx_dop853_tableau.cuh"
 #include "gx_body.cuh"
+#include "gx_fast64.cuh"
 
 static_assert(sizeof(gx_body) == 64, "gx_body layout");
 
@@ -80,7 +83,7 @@ __device__ __forceinline__ double nb_max(double a, double b) { return (a > b) ? 
 template <bool SCF>
 __device__ __noinline__ V6 group_rhs_call(const DevPot &pot, const DevFrame &fr, unsigned mask, int base, int member,
                                           int nmem, int nbody, const gx_body *__restrict__ bod, V6 yin) {
-    V6 k = rhs_call<SCF>(pot, fr, yin);
+    V6 k = fast::rhs_call_f<SCF>(pot, fr, yin);
     for (int j = 0; j < nbody; j++) {
         const double q0x = __shfl_sync(mask, yin.v[0], base + j);
         const double q0y = __shfl_sync(mask, yin.v[1], base + j);
@@ -144,8 +147,7 @@ nbody_dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
     const bool lane_ok = g < 32 / gs;
     const unsigned gmask = lane_ok ? (((gs == 32) ? 0xffffffffu : ((1u << gs) - 1u)) << base) : 0u;
 
-    const double safe = 0.9, fac1 = 0.333, fac2 = 6.0, beta = 0.0;
-    const double expo1 = 1.0 / 8.0 - beta * 0.2;
+    const double safe = 0.9, fac1 = 0.333, fac2 = 6.0;  // and beta = 0
     const double facc1 = 1.0 / fac1, facc2 = 1.0 / fac2;
     const double atoli = A.atol, rtoli = A.rtol;
 
@@ -313,55 +315,51 @@ nbody_dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
 
             // the twelve stages (dop853.cpp:368-414)
 #pragma unroll
-            for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * a21 * k1[c];
+            for (int c = 0; c < 6; c++) yy1[c] = fma(h * a21, k1[c], y[c]);
             GRHS(am, yy1, k2);
 #pragma unroll
-            for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a31 * k1[c] + a32 * k2[c]);
+            for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a32, k2[c], a31 * k1[c]), y[c]);
             GRHS(am, yy1, k3);
 #pragma unroll
-            for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a41 * k1[c] + a43 * k3[c]);
+            for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a43, k3[c], a41 * k1[c]), y[c]);
             GRHS(am, yy1, k4);
 #pragma unroll
-            for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a51 * k1[c] + a53 * k3[c] + a54 * k4[c]);
+            for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a54, k4[c], fma(a53, k3[c], a51 * k1[c])), y[c]);
             GRHS(am, yy1, k5);
 #pragma unroll
-            for (int c = 0; c < 6; c++) yy1[c] = y[c] + h * (a61 * k1[c] + a64 * k4[c] + a65 * k5[c]);
+            for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a65, k5[c], fma(a64, k4[c], a61 * k1[c])), y[c]);
             GRHS(am, yy1, k6);
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                yy1[c] = y[c] + h * (a71 * k1[c] + a74 * k4[c] + a75 * k5[c] + a76 * k6[c]);
+                yy1[c] = fma(h, fma(a76, k6[c], fma(a75, k5[c], fma(a74, k4[c], a71 * k1[c]))), y[c]);
             GRHS(am, yy1, k7);
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                yy1[c] = y[c] + h * (a81 * k1[c] + a84 * k4[c] + a85 * k5[c] + a86 * k6[c] + a87 * k7[c]);
+                yy1[c] = fma(h, fma(a87, k7[c], fma(a86, k6[c], fma(a85, k5[c], fma(a84, k4[c], a81 * k1[c])))), y[c]);
             GRHS(am, yy1, k8);
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                yy1[c] = y[c] + h * (a91 * k1[c] + a94 * k4[c] + a95 * k5[c] + a96 * k6[c] + a97 * k7[c] +
-                                     a98 * k8[c]);
+                yy1[c] = fma(h, fma(a98, k8[c], fma(a97, k7[c], fma(a96, k6[c], fma(a95, k5[c], fma(a94, k4[c], a91 * k1[c]))))), y[c]);
             GRHS(am, yy1, k9);
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                yy1[c] = y[c] + h * (a101 * k1[c] + a104 * k4[c] + a105 * k5[c] + a106 * k6[c] + a107 * k7[c] +
-                                     a108 * k8[c] + a109 * k9[c]);
+                yy1[c] = fma(h, fma(a109, k9[c], fma(a108, k8[c], fma(a107, k7[c], fma(a106, k6[c], fma(a105, k5[c], fma(a104, k4[c], a101 * k1[c])))))), y[c]);
             GRHS(am, yy1, k10);
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                yy1[c] = y[c] + h * (a111 * k1[c] + a114 * k4[c] + a115 * k5[c] + a116 * k6[c] + a117 * k7[c] +
-                                     a118 * k8[c] + a119 * k9[c] + a1110 * k10[c]);
+                yy1[c] = fma(h, fma(a1110, k10[c], fma(a119, k9[c], fma(a118, k8[c], fma(a117, k7[c], fma(a116, k6[c], fma(a115, k5[c], fma(a114, k4[c], a111 * k1[c]))))))), y[c]);
             GRHS(am, yy1, k2);
             const double xph = x + h;
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                yy1[c] = y[c] + h * (a121 * k1[c] + a124 * k4[c] + a125 * k5[c] + a126 * k6[c] + a127 * k7[c] +
-                                     a128 * k8[c] + a129 * k9[c] + a1210 * k10[c] + a1211 * k2[c]);
+                yy1[c] = fma(h, fma(a1211, k2[c], fma(a1210, k10[c], fma(a129, k9[c], fma(a128, k8[c], fma(a127, k7[c], fma(a126, k6[c], fma(a125, k5[c], fma(a124, k4[c], a121 * k1[c])))))))), y[c]);
             GRHS(am, yy1, k3);
             nfcn += 11;
 #pragma unroll
             for (int c = 0; c < 6; c++) {
-                k4[c] = b1 * k1[c] + b6 * k6[c] + b7 * k7[c] + b8 * k8[c] + b9 * k9[c] + b10 * k10[c] +
-                        b11 * k2[c] + b12 * k3[c];
-                k5[c] = y[c] + h * k4[c];
+                k4[c] = fma(b12, k3[c], fma(b11, k2[c], fma(b10, k10[c], fma(b9, k9[c], fma(b8, k8[c], fma(b7, k7[c],
+                            fma(b6, k6[c], b1 * k1[c])))))));
+                k5[c] = fma(h, k4[c], y[c]);
             }
 
             // error estimation (:416-444), sequential over the system
@@ -370,13 +368,13 @@ nbody_dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
                 double t1[6], t2[6];
 #pragma unroll
                 for (int c = 0; c < 6; c++) {
-                    const double sk = atoli + rtoli * nb_max(fabs(y[c]), fabs(k5[c]));
-                    double erri = k4[c] - bhh1 * k1[c] - bhh2 * k9[c] - bhh3 * k3[c];
-                    double sqr = erri / sk;
+                    const double isk = fast::rcp_f(fma(rtoli, fmax(fabs(y[c]), fabs(k5[c])), atoli));
+                    double erri = fma(-bhh3, k3[c], fma(-bhh2, k9[c], fma(-bhh1, k1[c], k4[c])));
+                    double sqr = erri * isk;
                     t2[c] = sqr * sqr;
-                    erri = er1 * k1[c] + er6 * k6[c] + er7 * k7[c] + er8 * k8[c] + er9 * k9[c] + er10 * k10[c] +
-                           er11 * k2[c] + er12 * k3[c];
-                    sqr = erri / sk;
+                    erri = fma(er12, k3[c], fma(er11, k2[c], fma(er10, k10[c], fma(er9, k9[c], fma(er8, k8[c],
+                               fma(er7, k7[c], fma(er6, k6[c], er1 * k1[c])))))));
+                    sqr = erri * isk;
                     t1[c] = sqr * sqr;
                 }
                 chain_sum2(am, gs, base, member, in_sys, t1, t2, err, err2);
@@ -386,7 +384,8 @@ nbody_dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
             err = fabs(h) * err * sqrt(1.0 / (deno * (double)(6 * nmem)));
 
             // computation of hnew (:446-452)
-            const double fac11 = pow(err, expo1);
+            // pow(err, expo1) with expo1 = 1/8 (beta = 0): three square roots
+            const double fac11 = sqrt(sqrt(sqrt(err)));
             double fac = fac11;  // gala divides by pow(facold, beta) == 1 for its beta = 0
             (void)facold;
             fac = nb_max(facc2, nb_min(facc1, fac / safe));
@@ -445,18 +444,15 @@ nbody_dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
                 }
 #pragma unroll
                 for (int c = 0; c < 6; c++)
-                    yy1[c] = y[c] + h * (a141 * k1[c] + a147 * k7[c] + a148 * k8[c] + a149 * k9[c] +
-                                         a1410 * k10[c] + a1411 * k2[c] + a1412 * k3[c] + a1413 * k4[c]);
+                    yy1[c] = fma(h, fma(a1413, k4[c], fma(a1412, k3[c], fma(a1411, k2[c], fma(a1410, k10[c], fma(a149, k9[c], fma(a148, k8[c], fma(a147, k7[c], a141 * k1[c]))))))), y[c]);
                 GRHS(am, yy1, k10);
 #pragma unroll
                 for (int c = 0; c < 6; c++)
-                    yy1[c] = y[c] + h * (a151 * k1[c] + a156 * k6[c] + a157 * k7[c] + a158 * k8[c] +
-                                         a1511 * k2[c] + a1512 * k3[c] + a1513 * k4[c] + a1514 * k10[c]);
+                    yy1[c] = fma(h, fma(a1514, k10[c], fma(a1513, k4[c], fma(a1512, k3[c], fma(a1511, k2[c], fma(a158, k8[c], fma(a157, k7[c], fma(a156, k6[c], a151 * k1[c]))))))), y[c]);
                 GRHS(am, yy1, k2);
 #pragma unroll
                 for (int c = 0; c < 6; c++)
-                    yy1[c] = y[c] + h * (a161 * k1[c] + a166 * k6[c] + a167 * k7[c] + a168 * k8[c] +
-                                         a169 * k9[c] + a1613 * k4[c] + a1614 * k10[c] + a1615 * k2[c]);
+                    yy1[c] = fma(h, fma(a1615, k2[c], fma(a1614, k10[c], fma(a1613, k4[c], fma(a169, k9[c], fma(a168, k8[c], fma(a167, k7[c], fma(a166, k6[c], a161 * k1[c]))))))), y[c]);
                 GRHS(am, yy1, k3);
                 if (acc && !stiff) {
                     nfcn += 3;

@@ -111,7 +111,9 @@ def test_nbody_final_state_and_stride(oracle):
     final, _ = integrate_systems(pot, bodies, w0, t, save_all=False)
     full = full.cpu().numpy()
     np.testing.assert_array_equal(strided.cpu().numpy(), full[:, ::7])
-    np.testing.assert_array_equal(final.cpu().numpy(), full[:, -1])
+    # the last stored row is the dense-output polynomial at s = 1, y_old + (y_new - y_old),
+    # which can differ from y_new by an ulp (in gala as well)
+    np.testing.assert_allclose(final.cpu().numpy(), full[:, -1], rtol=1e-15, atol=1e-300)
 
 
 def test_directnbody_api_reorders_like_gala(oracle):

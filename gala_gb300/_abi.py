@@ -85,6 +85,7 @@ SIGNATURES = {
     "gx_leapfrog_integrate_hamiltonian": (C.c_int, [_PP, _PF, _P, _I64, _P, _I64, _I32, _P, _P]),
     "gx_ruth4_integrate_hamiltonian": (C.c_int, [_PP, _PF, _P, _I64, _P, _I64, _I32, _P, _P]),
     "gx_calibrate_fma": (C.c_int, [_I32, _I32, _I32, _I64, _P, _P]),
+    "gx_selfcheck_fast64": (C.c_int, [_P, _I64, _P, _P]),
     "gx_batch_integrate_fp32": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P]),
     "gx_batch_integrate_fp32_noalloc": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _I32, _I32, _P, _P]),
     "gx_mlp_param_count": (C.c_int64, []),

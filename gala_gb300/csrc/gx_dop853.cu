@@ -404,3 +404,23 @@ extern "C" int gx_dop853_integrate_hamiltonian(const gx_potential *pot, const gx
         gx::dop853_kernel<1024, true><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
     return gx::check_launch("dop853");
 }
+
+namespace gx {
+__global__ void selfcheck_fast64_kernel(const double *__restrict__ x, int64_t n, double *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    out[i] = fast::log_f(v);
+    out[n + i] = log(v);
+    out[2 * n + i] = fast::sqrt_f(v);
+    out[3 * n + i] = fast::rcp_f(v);
+}
+}  // namespace gx
+
+extern "C" int gx_selfcheck_fast64(const double *x, int64_t n, double *out, void *stream) {
+    GX_CHECK_ARG(n >= 0, "n < 0");
+    if (n == 0) return GX_OK;
+    GX_CHECK_ARG(x && out, "NULL array");
+    gx::selfcheck_fast64_kernel<<<(unsigned)((n + 255) / 256), 256, 0, gx::as_stream(stream)>>>(x, n, out);
+    return gx::check_launch("selfcheck_fast64");
+}

@@ -335,6 +335,12 @@ int gx_surrogate_tc_smem_bytes(void);
 int gx_calibrate_fma(int32_t fp64, int32_t blocks, int32_t threads, int64_t iters,
                      void* sink, void* stream);
 
+/* Numerics self-check of the FP64 forms the DOP853 force uses instead of the
+ * library functions (no counterpart in gala): for n DEVICE doubles x, out is
+ * (4, n) DEVICE doubles: the table-driven ln x, the library log(x), the
+ * seeded-Newton sqrt(x) and 1/x. */
+int gx_selfcheck_fast64(const double* x, int64_t n, double* out, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Direct n-body systems and mock streams                                    */
 /* ------------------------------------------------------------------------- */

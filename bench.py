@@ -193,6 +193,9 @@ def cpu_reference_run(n_orbits, nsteps, target_s, steps, warmup):
                   f"gala's DOP853 restated in C, -Ofast, {nthreads} threads",
         "seconds_per_step": per,
         "sample_orbits": int(sample.shape[1]),
+        # gala itself runs one thread: the same restatement on one core, one batch
+        "single_thread": {"value": 100 * nsteps / one, "unit": UNIT, "cores": 1,
+                          "sample": f"one 100-orbit batch x {nsteps} steps, 1 thread"},
     }, sample, out
 
 
@@ -218,7 +221,7 @@ def run_reference(args):
         "config": {"workload": "mw_dop853: MW composite, DOP853 rtol 1e-10 atol 1e-12 FP64, 100-orbit batches, "
                                f"dt 0.5 Myr, {args.nsteps} steps, every 100th output kept",
                    "orbits_per_gpu": args.orbits, "sample_orbits": base["sample_orbits"]},
-        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample", "single_thread")},
         "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -811,7 +814,7 @@ def run_gx(args):
         rel = np.linalg.norm(gpu_sample - cpu_out, axis=0) / np.linalg.norm(cpu_out, axis=0)
         base["gpu_vs_cpu_max_rel"] = float(np.max(rel))
         line["cpu_baseline"] = {k: base[k] for k in ("value", "unit", "cores", "kind", "sample",
-                                                     "gpu_vs_cpu_max_rel")}
+                                                     "gpu_vs_cpu_max_rel", "single_thread")}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -132,21 +132,22 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def measure_fp64_peak(torch, stream):
-    """FP64 multiply-add throughput (TFLOP/s) from the library's FMA-chain probe."""
+def measure_fp64_peak(torch, stream, fp64=True):
+    """FP64 (or FP32) multiply-add throughput (TFLOP/s) from the library's FMA-chain probe."""
     from gala_gb300 import _abi
 
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    blocks, threads, iters = sms * 8, 256, 4096
-    sink = torch.zeros(blocks * threads, dtype=torch.float64, device="cuda")
+    blocks, threads, iters = sms * 8, 256, 4096 if fp64 else 65536
+    sink = torch.zeros(blocks * threads, dtype=torch.float64 if fp64 else torch.float32, device="cuda")
     h = int(stream.cuda_stream)
+    f = 1 if fp64 else 0
     for _ in range(2):
-        _abi.call("gx_calibrate_fma", 1, blocks, threads, iters, int(sink.data_ptr()), h)
+        _abi.call("gx_calibrate_fma", f, blocks, threads, iters, int(sink.data_ptr()), h)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     best = None
     for _ in range(3):
         e0.record(stream)
-        _abi.call("gx_calibrate_fma", 1, blocks, threads, iters, int(sink.data_ptr()), h)
+        _abi.call("gx_calibrate_fma", f, blocks, threads, iters, int(sink.data_ptr()), h)
         e1.record(stream)
         e1.synchronize()
         ms = e0.elapsed_time(e1)
@@ -247,6 +248,11 @@ def run_uneven_batch(args, torch, stream):
                        f"{args.batch_step_scale}, dt in {{0.1,0.5,1}} Myr, half Leapfrog half Ruth4",
            "orbit_steps": total}
     outs = {}
+    # algorithmic flops per step (add/mul 1, FMA 2, div/sqrt/log 1): composite force 81,
+    # Leapfrog 21 + one force, Ruth4 72 + four forces
+    is_ruth4 = np.asarray(method) == 1
+    flops = float(np.sum(nsteps * np.where(is_ruth4, 72 + 4 * 81, 21 + 81)))
+    peaks = {"fp32c": measure_fp64_peak(torch, stream, fp64=False), "fp64": measure_fp64_peak(torch, stream)}
     precs = ["fp32c", "fp64"] if args.batch_precision == "both" else [args.batch_precision]
     for prec in precs:
         b = BatchIntegrator(pot, w0, nsteps, dt, method, precision=prec)
@@ -269,7 +275,12 @@ def run_uneven_batch(args, torch, stream):
         outs[prec] = b.w_out.cpu().numpy()
         res[prec] = {"value": total / (ms * 1e-3), "unit": UNIT, "ms_per_run": ms, "config": b.config,
                      "dE_over_E_median": float(np.median(dE)), "dE_over_E_p99": float(np.percentile(dE, 99)),
-                     "gpu_launches_per_run": 3}
+                     "gpu_launches_per_run": 3,
+                     "roofline": {"bound": "fp32" if prec == "fp32c" else "fp64", "unit": "TFLOP/s",
+                                  "achieved": flops / (ms * 1e-3) / 1e12, "peak": peaks[prec],
+                                  "frac": flops / (ms * 1e-3) / 1e12 / peaks[prec],
+                                  "peak_source": "FMA-chain probe (gx_calibrate_fma), same run",
+                                  "work": "algorithmic flops: Leapfrog 102, Ruth4 396 per step (force 81)"}}
     if len(outs) == 2:
         err = np.linalg.norm(outs["fp32c"][:3] - outs["fp64"][:3], axis=0) / np.linalg.norm(outs["fp64"][:3], axis=0)
         res["fp32c_position_error_vs_fp64"] = {"median": float(np.median(err)),
@@ -517,6 +528,7 @@ def run_mock_streams(args, torch, stream):
     # 6 drift + 12 kick flops) + 2 progenitor pulls
     lf_flops = S * float(np.sum(np.round(t_final - t))) * (3 * (F_RHS_MW - 6 + 18) + 2 * F_PLUMMER_PULL)
 
+    fp64_peak = measure_fp64_peak(torch, stream)
     result = {
         "workload": f"mock_streams: {S} Plummer progenitors on MW-composite disk orbits, FardalStreamDF 1 particle "
                     f"per tail per step, dt 1 Myr, {nsteps} steps, DOPRI853 atol=rtol=1e-10, err_if_fail=0",
@@ -527,6 +539,7 @@ def run_mock_streams(args, torch, stream):
         "release_kernel": {"value": particle_steps / (ms_rel * 1e-3), "unit": "particle-steps/s", "ms": ms_rel,
                            "matches_pipeline_output": same,
                            "roofline": {"bound": "fp64", "achieved": flops / (ms_rel * 1e-3) / 1e12,
+                                        "peak": fp64_peak, "frac": flops / (ms_rel * 1e-3) / 1e12 / fp64_peak,
                                         "unit": "TFLOP/s", "work": "algorithmic FP64 flops from the per-system "
                                         "nfcn/nstep/naccpt counters"}},
         "e2e": {"value": particle_steps / (e2e_ms * 1e-3), "unit": "particle-steps/s", "ms": e2e_ms,
@@ -539,7 +552,9 @@ def run_mock_streams(args, torch, stream):
                                     "unit": "particle-steps/s", "ms": lf_ms["gx_mockstream_leapfrog"],
                                     "roofline": {"bound": "fp64", "unit": "TFLOP/s",
                                                  "achieved": lf_flops / (lf_ms["gx_mockstream_leapfrog"] * 1e-3)
-                                                 / 1e12}},
+                                                 / 1e12, "peak": fp64_peak,
+                                                 "frac": lf_flops / (lf_ms["gx_mockstream_leapfrog"] * 1e-3)
+                                                 / 1e12 / fp64_peak}},
             "fp32c_release_kernel": {"value": particle_steps / (lf_ms["gx_mockstream_leapfrog_fp32"] * 1e-3),
                                      "unit": "particle-steps/s", "ms": lf_ms["gx_mockstream_leapfrog_fp32"]},
             "speedup_fp32c_vs_fp64": lf_ms["gx_mockstream_leapfrog"] / lf_ms["gx_mockstream_leapfrog_fp32"],

@@ -545,7 +545,8 @@ def run_mock_streams(args, torch, stream):
         "e2e": {"value": particle_steps / (e2e_ms * 1e-3), "unit": "particle-steps/s", "ms": e2e_ms,
                 "h2d_bytes": int(w0.nbytes + m.nbytes + S * n_rows * 4 * 8),
                 "d2h_bytes": int(host_stream.nbytes + host_nbody.nbytes)},
-        "release_systems": {"count": int(np.sum(status != 0)), "stiff_exit_fraction": float(np.mean(status[status != 0] == -4)),
+        "release_systems": {"count": int(np.sum(status != 0)),
+                            "stiff_exit_fraction": float(np.mean(status[status != 0] == -4)),
                             "accepted_steps": int(np.sum(stats[..., 2])), "rejected_steps": int(np.sum(stats[..., 3]))},
         "leapfrog": {
             "fp64_release_kernel": {"value": particle_steps / (lf_ms["gx_mockstream_leapfrog"] * 1e-3),
@@ -693,9 +694,16 @@ def run_gx(args):
         if rank == 0:
             print(json.dumps(res), flush=True)
         return
+    from gala_gb300.shard import max_over_ranks, shard_range
+
     mw = W.mw_composite()
-    n, nsteps, stride, nbatch = args.orbits, args.nsteps, 100, 100
-    w0 = W.mw_ics(n, seed=W.SEED_BASE + 2 + 1000 * rank)
+    nsteps, stride, nbatch = args.nsteps, 100, 100
+    # weak scaling: args.orbits per GPU; this rank's contiguous range of the
+    # global set, cut on whole 100-orbit batches
+    n_global = args.orbits * world
+    lo, hi = shard_range(n_global, rank, world, nbatch)
+    n = hi - lo
+    w0 = np.ascontiguousarray(W.mw_ics(n_global, seed=W.SEED_BASE + 2)[:, lo:hi])
     t = g.parse_time_specification(dt=0.5, n_steps=nsteps)
     ntimes = len(t)
     n_out = (ntimes - 1) // stride + 1
@@ -735,11 +743,7 @@ def run_gx(args):
         wall = time.perf_counter() - wall0
     barrier()
     step_ms = [e0.elapsed_time(e1) for e0, e1 in ev]
-    mean_ms = float(np.mean(step_ms))
-    if world > 1:
-        tt = torch.tensor([mean_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        mean_ms = float(tt.item())
+    mean_ms = max_over_ranks(float(np.mean(step_ms)))
     st = status.cpu().numpy()
     if np.any(st != 1):
         raise RuntimeError(f"integration failed in {int(np.sum(st != 1))} batches: {np.unique(st)}")
@@ -748,7 +752,7 @@ def run_gx(args):
     nb_sizes[-1] = n - nbatch * (nb - 1)
     flops = float(np.sum(nb_sizes * (stt[:, 0] * F_RHS_MW + stt[:, 1] * F_STEP_PER_ORBIT +
                                      stt[:, 2] * F_DENSE_PER_ORBIT)) + n * n_out * F_OUTPUT_PER_ORBIT)
-    value = n * nsteps * world / (mean_ms * 1e-3)
+    value = n_global * nsteps / (mean_ms * 1e-3)
 
     # energy conservation of this run (first vs last kept output), on the GPU
     H = g.Hamiltonian(mw)
@@ -768,11 +772,7 @@ def run_gx(args):
         dt_ = (time.perf_counter() - t0) * 1e3
         if i >= args.warmup:
             e2e_ms.append(dt_)
-    e2e_mean = float(np.mean(e2e_ms))
-    if world > 1:
-        tt = torch.tensor([e2e_mean], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_mean = float(tt.item())
+    e2e_mean = max_over_ranks(float(np.mean(e2e_ms)))
     same = bool(np.array_equal(wout, out.cpu().numpy()))
 
     peak = measure_fp64_peak(torch, stream)
@@ -803,10 +803,11 @@ def run_gx(args):
         "config": {
             "workload": "mw_dop853: MW composite, DOP853 rtol 1e-10 atol 1e-12 FP64 (plain drop-in form), "
                         f"100-orbit batches, dt 0.5 Myr, {nsteps} steps, every 100th output kept",
-            "orbits_per_gpu": n, "n_steps": nsteps, "out_stride": stride, "nbatch": nbatch,
+            "orbits_per_gpu": args.orbits, "orbits_total": n_global, "n_steps": nsteps, "out_stride": stride,
+            "nbatch": nbatch,
             "l2": "flushed (256 MB write) between timed iterations",
         },
-        "e2e": {"value": n * nsteps * world / (e2e_mean * 1e-3), "unit": UNIT,
+        "e2e": {"value": n_global * nsteps / (e2e_mean * 1e-3), "unit": UNIT,
                 "h2d_bytes_per_step": int(w0.nbytes + t.nbytes),
                 "d2h_bytes_per_step": int(wout.nbytes + status.numel() * 4),
                 "ms_per_step": e2e_mean, "matches_device_run": same},

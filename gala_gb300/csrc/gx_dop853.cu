@@ -4,15 +4,19 @@
 // n = 6 * nb: one shared step size, one RMS error norm over all 6 * nb
 // components, one accept/reject decision, one dense-output grid
 // (dop853.pyx:228-245 -> dop853_helper :90-193 -> dopcor, dopri/dop853.cpp:89-650).
-// Here a batch is one CTA and each thread owns one orbit's six components:
+// Here a batch is a group of consecutive threads of a CTA -- two batches per CTA
+// when that fills the warps better (100 orbits alone leave 28 idle lanes), the
+// two stepping in lock-step -- and each thread owns one orbit's six components:
 //   * the twelve stages, FSAL evaluation and the three dense-output stages are
 //     evaluated per thread in registers with gala's expression order;
 //   * the error norms (err, err2) and the stiffness sums (stnum, stden) are
-//     CTA-wide sums: a fixed-order warp butterfly plus an ordered sum over warps,
-//     so the step-size sequence is deterministic run to run;
+//     per-batch sums: a fixed-order warp butterfly plus an ordered sum over
+//     warps, so the step-size sequence is deterministic run to run;
 //   * every scalar of the step-size controller (x, h, facold, reject, last,
-//     naccpt, ...) is computed identically by all threads from the same sums,
-//     so control flow stays uniform inside the CTA;
+//     naccpt, ...) is computed identically by all threads of a batch from the
+//     same sums, so control flow is uniform inside a batch; every thread of
+//     the CTA takes part in each step's two reductions, and a CTA leaves its
+//     loop when none of its batches is stepping;
 //   * dense output (contd8_threadsafe, :869-904) is written directly into the
 //     (6, n_out, N) result for every requested time inside [xold, xold + h].
 // The loop is bounded by nmax like gala's; no thread ever waits on another CTA.
@@ -32,23 +36,31 @@ struct DopArgs {
 
 constexpr int DOP_MAX_WARPS = 32;
 
-// Deterministic CTA-wide sum of two values.  Every thread returns the same bits.
-__device__ __forceinline__ void block_sum2(double &a, double &b, double *red) {
+// Deterministic sums of two values over each batch of the CTA (BPC batches;
+// bl is the caller's batch): a fixed-order warp butterfly, with the lanes of
+// the other batch contributing zeros, then an ordered sum over warps.  Every
+// thread of a batch returns the same bits.
+template <int BPC>
+__device__ __forceinline__ void block_sum2(double &a, double &b, double *red, int bl) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    double v[2 * BPC];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, o);
-        b += __shfl_xor_sync(0xffffffffu, b, o);
+    for (int q = 0; q < BPC; q++) {
+        v[q] = (bl == q) ? a : 0.0;
+        v[BPC + q] = (bl == q) ? b : 0.0;
     }
-    if (lane == 0) {
-        red[wid] = a;
-        red[DOP_MAX_WARPS + wid] = b;
-    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int q = 0; q < 2 * BPC; q++) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 2 * BPC; q++) red[q * DOP_MAX_WARPS + wid] = v[q];
     __syncthreads();
     double sa = 0., sb = 0.;
     for (int w = 0; w < nw; w++) {
-        sa += red[w];
-        sb += red[DOP_MAX_WARPS + w];
+        sa += red[bl * DOP_MAX_WARPS + w];
+        sb += red[(BPC + bl) * DOP_MAX_WARPS + w];
     }
     __syncthreads();
     a = sa;
@@ -71,19 +83,25 @@ __device__ __forceinline__ double max_d(double a, double b) { return (a > b) ? a
         }                                                                \
     } while (0)
 
-template <int MAXT, bool SCF>
+template <int MAXT, bool SCF, int BPC>
 __global__ void __launch_bounds__(MAXT, 1)
-dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFrame fr, DopArgs A, const double *__restrict__ w0, int64_t n,
-              const double *__restrict__ t, double *__restrict__ out, int32_t *__restrict__ status,
+dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFrame fr, DopArgs A,
+              const double *__restrict__ w0, int64_t n, const double *__restrict__ t, double *__restrict__ out,
+              int32_t *__restrict__ status,
               int64_t *__restrict__ stats) {
     using namespace dop;
-    __shared__ double red[2 * DOP_MAX_WARPS];
+    __shared__ double red[4 * DOP_MAX_WARPS];
 
-    const int64_t b = blockIdx.x;
-    const int64_t i0 = b * A.nbatch;
-    const int nb = (int)((i0 + A.nbatch <= n) ? A.nbatch : n - i0);
-    const int j = threadIdx.x;
-    const bool active = j < nb;
+    // BPC batches per CTA, batch bl on threads [bl * nbatch, (bl + 1) * nbatch)
+    const int nbs = A.nbatch;
+    const int bl = (BPC == 1) ? 0 : min((int)threadIdx.x / nbs, BPC - 1);
+    const int j = threadIdx.x - bl * nbs;  // lane within the batch
+    const int64_t b = (int64_t)blockIdx.x * BPC + bl;
+    const int64_t nbt = (n + nbs - 1) / nbs;
+    const bool batch_ok = b < nbt && j < nbs;
+    const int64_t i0 = b * nbs;
+    const int nb = batch_ok ? (int)((i0 + nbs <= n) ? nbs : n - i0) : 0;
+    const bool active = batch_ok && j < nb;
     const int nsys = 6 * nb;
 
     double y[6], k1[6], k2[6], k3[6], k4[6], k5[6], k6[6], k7[6], k8[6], k9[6], k10[6], yy1[6];
@@ -123,7 +141,7 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
             sqr = y[c] / sk;
             dny += active ? sqr * sqr : 0.;
         }
-        block_sum2(dnf, dny, red);
+        block_sum2<BPC>(dnf, dny, red, bl);
         double hh = ((dnf <= 1.0E-10) || (dny <= 1.0E-10)) ? 1.0E-6 : sqrt(dny / dnf) * 0.01;
         hh = min_d(hh, hmax);
         hh = sign_d(hh, posneg);
@@ -135,7 +153,7 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
             const double sqr = (k2[c] - k1[c]) / sk;
             der2 += active ? sqr * sqr : 0.;
         }
-        block_sum2(der2, unused, red);
+        block_sum2<BPC>(der2, unused, red, bl);
         der2 = sqrt(der2) / hh;
         const double der12 = max_d(fabs(der2), sqrt(dnf));
         const double h1 = (der12 <= 1.0E-15) ? max_d(1.0E-6, fabs(hh) * 1.0E-3) : pow(0.01 / der12, 1.0 / 8.0);
@@ -144,62 +162,80 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
     }
     nfcn += 2;
 
+    bool done = !batch_ok;
+    double xold = 0.0, hout = 0.0, xph = 0.0;
     for (;;) {
-        if (nstep > nmax) { idid = -2; break; }
-        if (0.1 * fabs(h) <= fabs(x) * uround) { idid = -3; break; }
-        if ((x + 1.01 * h - xend) * posneg > 0.0) {
-            h = xend - x;
-            last = 1;
+        // the batches of a CTA step in lock-step: every thread takes part in the
+        // two CTA reductions of each step, and the loop ends when no batch of
+        // the CTA is stepping any more
+        if (!__syncthreads_or(done ? 0 : 1)) break;
+        bool stepping = !done;
+        if (stepping && nstep > nmax) {
+            idid = -2;
+            done = true;
+            stepping = false;
         }
-        const double xold = x, hout = h;
-        nstep++;
+        if (stepping && 0.1 * fabs(h) <= fabs(x) * uround) {
+            idid = -3;
+            done = true;
+            stepping = false;
+        }
+        if (stepping) {
+            if ((x + 1.01 * h - xend) * posneg > 0.0) {
+                h = xend - x;
+                last = 1;
+            }
+            xold = x;
+            hout = h;
+            nstep++;
 
-        // the twelve stages (dop853.cpp:368-414)
-        // stage sums as fused multiply-add chains in gala's term order
-        for (int c = 0; c < 6; c++) yy1[c] = fma(h * a21, k1[c], y[c]);
-        RHS(yy1, k2);
-        for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a32, k2[c], a31 * k1[c]), y[c]);
-        RHS(yy1, k3);
-        for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a43, k3[c], a41 * k1[c]), y[c]);
-        RHS(yy1, k4);
-        for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a54, k4[c], fma(a53, k3[c], a51 * k1[c])), y[c]);
-        RHS(yy1, k5);
-        for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a65, k5[c], fma(a64, k4[c], a61 * k1[c])), y[c]);
-        RHS(yy1, k6);
-        for (int c = 0; c < 6; c++)
-            yy1[c] = fma(h, fma(a76, k6[c], fma(a75, k5[c], fma(a74, k4[c], a71 * k1[c]))), y[c]);
-        RHS(yy1, k7);
-        for (int c = 0; c < 6; c++)
-            yy1[c] = fma(h, fma(a87, k7[c], fma(a86, k6[c], fma(a85, k5[c], fma(a84, k4[c], a81 * k1[c])))), y[c]);
-        RHS(yy1, k8);
-        for (int c = 0; c < 6; c++)
-            yy1[c] = fma(h, fma(a98, k8[c], fma(a97, k7[c], fma(a96, k6[c], fma(a95, k5[c], fma(a94, k4[c],
-                                                                                                a91 * k1[c]))))),
-                         y[c]);
-        RHS(yy1, k9);
-        for (int c = 0; c < 6; c++)
-            yy1[c] = fma(h, fma(a109, k9[c], fma(a108, k8[c], fma(a107, k7[c], fma(a106, k6[c], fma(a105, k5[c],
-                                fma(a104, k4[c], a101 * k1[c])))))), y[c]);
-        RHS(yy1, k10);
-        for (int c = 0; c < 6; c++)
-            yy1[c] = fma(h, fma(a1110, k10[c], fma(a119, k9[c], fma(a118, k8[c], fma(a117, k7[c], fma(a116, k6[c],
-                                fma(a115, k5[c], fma(a114, k4[c], a111 * k1[c]))))))), y[c]);
-        RHS(yy1, k2);
-        const double xph = x + h;
-        for (int c = 0; c < 6; c++)
-            yy1[c] = fma(h, fma(a1211, k2[c], fma(a1210, k10[c], fma(a129, k9[c], fma(a128, k8[c], fma(a127, k7[c],
-                                fma(a126, k6[c], fma(a125, k5[c], fma(a124, k4[c], a121 * k1[c])))))))), y[c]);
-        RHS(yy1, k3);
-        nfcn += 11;
-        for (int c = 0; c < 6; c++) {
-            k4[c] = fma(b12, k3[c], fma(b11, k2[c], fma(b10, k10[c], fma(b9, k9[c], fma(b8, k8[c], fma(b7, k7[c],
-                        fma(b6, k6[c], b1 * k1[c])))))));
-            k5[c] = fma(h, k4[c], y[c]);
+            // the twelve stages (dop853.cpp:368-414)
+            // stage sums as fused multiply-add chains in gala's term order
+            for (int c = 0; c < 6; c++) yy1[c] = fma(h * a21, k1[c], y[c]);
+            RHS(yy1, k2);
+            for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a32, k2[c], a31 * k1[c]), y[c]);
+            RHS(yy1, k3);
+            for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a43, k3[c], a41 * k1[c]), y[c]);
+            RHS(yy1, k4);
+            for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a54, k4[c], fma(a53, k3[c], a51 * k1[c])), y[c]);
+            RHS(yy1, k5);
+            for (int c = 0; c < 6; c++) yy1[c] = fma(h, fma(a65, k5[c], fma(a64, k4[c], a61 * k1[c])), y[c]);
+            RHS(yy1, k6);
+            for (int c = 0; c < 6; c++)
+                yy1[c] = fma(h, fma(a76, k6[c], fma(a75, k5[c], fma(a74, k4[c], a71 * k1[c]))), y[c]);
+            RHS(yy1, k7);
+            for (int c = 0; c < 6; c++)
+                yy1[c] = fma(h, fma(a87, k7[c], fma(a86, k6[c], fma(a85, k5[c], fma(a84, k4[c], a81 * k1[c])))), y[c]);
+            RHS(yy1, k8);
+            for (int c = 0; c < 6; c++)
+                yy1[c] = fma(h, fma(a98, k8[c], fma(a97, k7[c], fma(a96, k6[c], fma(a95, k5[c], fma(a94, k4[c],
+                                                                                                    a91 * k1[c]))))),
+                             y[c]);
+            RHS(yy1, k9);
+            for (int c = 0; c < 6; c++)
+                yy1[c] = fma(h, fma(a109, k9[c], fma(a108, k8[c], fma(a107, k7[c], fma(a106, k6[c], fma(a105, k5[c],
+                                    fma(a104, k4[c], a101 * k1[c])))))), y[c]);
+            RHS(yy1, k10);
+            for (int c = 0; c < 6; c++)
+                yy1[c] = fma(h, fma(a1110, k10[c], fma(a119, k9[c], fma(a118, k8[c], fma(a117, k7[c], fma(a116, k6[c],
+                                    fma(a115, k5[c], fma(a114, k4[c], a111 * k1[c]))))))), y[c]);
+            RHS(yy1, k2);
+            xph = x + h;
+            for (int c = 0; c < 6; c++)
+                yy1[c] = fma(h, fma(a1211, k2[c], fma(a1210, k10[c], fma(a129, k9[c], fma(a128, k8[c], fma(a127, k7[c],
+                                    fma(a126, k6[c], fma(a125, k5[c], fma(a124, k4[c], a121 * k1[c])))))))), y[c]);
+            RHS(yy1, k3);
+            nfcn += 11;
+            for (int c = 0; c < 6; c++) {
+                k4[c] = fma(b12, k3[c], fma(b11, k2[c], fma(b10, k10[c], fma(b9, k9[c], fma(b8, k8[c], fma(b7, k7[c],
+                            fma(b6, k6[c], b1 * k1[c])))))));
+                k5[c] = fma(h, k4[c], y[c]);
+            }
         }
 
-        // error estimation (:416-444), summed over the whole batch
+        // error estimation (:416-444), summed over each batch
         double err = 0.0, err2 = 0.0;
-        if (active) {
+        if (stepping && active) {
             for (int c = 0; c < 6; c++) {
                 const double isk = fast::rcp_f(fma(rtoli, fmax(fabs(y[c]), fabs(k5[c])), atoli));
                 double erri = fma(-bhh3, k3[c], fma(-bhh2, k9[c], fma(-bhh1, k1[c], k4[c])));
@@ -211,49 +247,57 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
                 err = fma(sqr, sqr, err);
             }
         }
-        block_sum2(err, err2, red);
-        double deno = err + 0.01 * err2;
-        if (deno <= 0.0) deno = 1.0;
-        err = fabs(h) * err * sqrt(1.0 / (deno * (double)nsys));
-
-        // computation of hnew (:446-452)
-        // gala's pow(err, expo1) with expo1 = 1/8 (beta = 0): three square roots
-        // instead of pow's ~84 FP64-pipe instructions
-        const double fac11 = sqrt(sqrt(sqrt(err)));
-        double fac = fac11;  // gala divides by pow(facold, beta) == 1 for its beta = 0
-        fac = max_d(facc2, min_d(facc1, fac / safe));
-        double hnew = h / fac;
-
-        if (err <= 1.0) {
-            facold = max_d(err, 1.0E-4);
-            naccpt++;
-            RHS(k5, k4);
-            nfcn++;
-
-            // stiffness detection (:463-486); like gala, the first detection returns -4
-            if (!(naccpt % nstiff) || (iasti > 0)) {
-                double stnum = 0.0, stden = 0.0;
-                if (active) {
-                    for (int c = 0; c < 6; c++) {
-                        double sqr = k4[c] - k3[c];
-                        stnum += sqr * sqr;
-                        sqr = k5[c] - yy1[c];
-                        stden += sqr * sqr;
-                    }
-                }
-                block_sum2(stnum, stden, red);
-                if (stden > 0.0) hlamb = h * sqrt(stnum / stden);
-                if (hlamb > 6.1) {
-                    nonsti = 0;
-                    iasti++;
-                    idid = -4;
-                    break;
-                } else {
-                    nonsti++;
-                    if (nonsti == 6) iasti = 0;
-                }
+        block_sum2<BPC>(err, err2, red, bl);
+        double hnew = h, fac11 = 1.0;
+        bool acc = false;
+        if (stepping) {
+            double deno = err + 0.01 * err2;
+            if (deno <= 0.0) deno = 1.0;
+            err = fabs(h) * err * sqrt(1.0 / (deno * (double)nsys));
+            // computation of hnew (:446-452); gala's pow(err, expo1) with expo1 = 1/8
+            // (beta = 0) as three square roots instead of pow's ~84 FP64-pipe instructions
+            fac11 = sqrt(sqrt(sqrt(err)));
+            double fac = fac11;  // gala divides by pow(facold, beta) == 1 for its beta = 0
+            fac = max_d(facc2, min_d(facc1, fac / safe));
+            hnew = h / fac;
+            acc = err <= 1.0;
+            if (acc) {
+                facold = max_d(err, 1.0E-4);
+                naccpt++;
+                RHS(k5, k4);
+                nfcn++;
             }
+        }
 
+        // stiffness detection (:463-486); like gala, the first detection returns -4.
+        // The sums are formed every step (zero where no test is due) so that all
+        // batches of the CTA share the barrier.
+        const bool stiff_due = stepping && acc && (!(naccpt % nstiff) || (iasti > 0));
+        double stnum = 0.0, stden = 0.0;
+        if (stiff_due && active) {
+            for (int c = 0; c < 6; c++) {
+                double sqr = k4[c] - k3[c];
+                stnum += sqr * sqr;
+                sqr = k5[c] - yy1[c];
+                stden += sqr * sqr;
+            }
+        }
+        block_sum2<BPC>(stnum, stden, red, bl);
+        if (stiff_due) {
+            if (stden > 0.0) hlamb = h * sqrt(stnum / stden);
+            if (hlamb > 6.1) {
+                nonsti = 0;
+                iasti++;
+                idid = -4;
+                done = true;
+                stepping = false;
+            } else {
+                nonsti++;
+                if (nonsti == 6) iasti = 0;
+            }
+        }
+
+        if (stepping && acc) {
             // Output times inside [xold, xold + hout] (:584-612): [out_idx, out_end).
             // Only every out_stride-th time is stored; the three dense-output stages
             // are evaluated only for a step that holds a stored time (their results
@@ -325,28 +369,33 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
             }
             out_idx = out_end;
 
+
             for (int c = 0; c < 6; c++) {
                 k1[c] = k4[c];
                 y[c] = k5[c];
             }
             x = xph;
-            if (last) { idid = 1; break; }
-            if (fabs(hnew) > hmax) hnew = posneg * hmax;
-            if (reject) hnew = posneg * min_d(fabs(hnew), fabs(h));
-            reject = 0;
-        } else {
+            if (last) {
+                idid = 1;
+                done = true;
+            } else {
+                if (fabs(hnew) > hmax) hnew = posneg * hmax;
+                if (reject) hnew = posneg * min_d(fabs(hnew), fabs(h));
+                reject = 0;
+            }
+        } else if (stepping) {
             hnew = h / min_d(facc1, fac11 / safe);
             reject = 1;
             if (naccpt >= 1) nrejct = nrejct + 1;
             last = 0;
         }
-        h = hnew;
+        if (stepping && !done) h = hnew;
     }
     (void)nonsti;
 
     if (!A.save_all && active)
         for (int c = 0; c < 6; c++) out[c * n + i0 + j] = y[c];
-    if (j == 0) {
+    if (j == 0 && batch_ok) {
         status[b] = idid;
         if (stats) {
             stats[4 * b + 0] = nfcn;
@@ -391,17 +440,24 @@ extern "C" int gx_dop853_integrate_hamiltonian(const gx_potential *pot, const gx
     A.save_all = save_all ? 1 : 0;
     A.nbatch = nbatch;
     const int64_t nbatches = (n + nbatch - 1) / nbatch;
-    const int threads = ((nbatch + 31) / 32) * 32;
     cudaStream_t st = gx::as_stream(stream);
-    const unsigned grid = (unsigned)nbatches;
-    if (threads <= 256 && !dp.has_scf)
-        gx::dop853_kernel<256, false><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
+    // Two batches share a CTA when that fills the warps better (a 100-orbit batch
+    // alone leaves 28 lanes of its fourth warp idle, and the FP64 pipe costs a
+    // warp instruction whatever its mask); they step in lock-step.
+    const int t1 = ((nbatch + 31) / 32) * 32, t2 = ((2 * nbatch + 31) / 32) * 32;
+    const bool pair = !dp.has_scf && t2 <= 256 && t2 < 2 * t1;
+    const int threads = pair ? t2 : t1;
+    const unsigned grid = (unsigned)(pair ? (nbatches + 1) / 2 : nbatches);
+    if (pair)
+        gx::dop853_kernel<256, false, 2><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
+    else if (threads <= 256 && !dp.has_scf)
+        gx::dop853_kernel<256, false, 1><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
     else if (threads <= 256)
-        gx::dop853_kernel<256, true><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
+        gx::dop853_kernel<256, true, 1><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
     else if (!dp.has_scf)
-        gx::dop853_kernel<1024, false><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
+        gx::dop853_kernel<1024, false, 1><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
     else
-        gx::dop853_kernel<1024, true><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
+        gx::dop853_kernel<1024, true, 1><<<grid, threads, 0, st>>>(dp, df, A, w0, n, t, w_out, status, stats);
     return gx::check_launch("dop853");
 }
 

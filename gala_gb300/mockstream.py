@@ -36,7 +36,8 @@ from .integrate import DOPRI853Integrator, LeapfrogIntegrator, get_integrator, p
 from .nbody import DirectNBody, bodies_to_device, integrate_systems, integrate_systems_leapfrog, pack_bodies
 from .potential import PotentialBase
 
-__all__ = ["MockStream", "BaseStreamDF", "FardalStreamDF", "MockStreamGenerator", "MockStreamBatch"]
+__all__ = ["MockStream", "BaseStreamDF", "FardalStreamDF", "StreaklineStreamDF", "MockStreamGenerator",
+           "MockStreamBatch"]
 
 
 class MockStream(PhaseSpacePosition):
@@ -201,6 +202,25 @@ class FardalStreamDF(BaseStreamDF):
         w, rt, lt, _ = self.sample_device(H.potential, as_device_f64(prog_w, dev), t, m[None, :], counts)
         w = w[0].cpu().numpy()
         return MockStream(pos=w[:, :3].T, vel=w[:, 3:].T, frame=H.frame, release_time=rt, lead_trail=lt)
+
+
+class StreaklineStreamDF(FardalStreamDF):
+    """Kuepper et al. (2012) streakline release (StreaklineStreamDF,
+    df.pyx:242-319): every particle at -/+ r_J along the satellite-frame x axis
+    (trailing / leading) with -/+ v_J along its y axis, nothing drawn.  That is
+    the Fardal placement with k_R = 1, k_z = 0, k_vt = 1, k_vz = 0, so the same
+    GPU sampler runs it with those constants in place of the normal draws; the
+    random state is not consumed, as in gala."""
+
+    def __init__(self, lead=True, trail=True, random_state=None):
+        BaseStreamDF.__init__(self, lead=lead, trail=trail, random_state=random_state)
+        self._gala_modified = 1  # multiplies v_t by k_R = 1: no effect
+
+    def _k(self):
+        return np.array([1.0, 0.0, 1.0, 0.0]), np.zeros(4)
+
+    def _draws(self, n_rows):
+        return np.tile(np.array([1.0, 0.0, 1.0, 0.0]), (n_rows, 1))
 
 
 class MockStreamBatch:

@@ -212,6 +212,27 @@ def test_fardal_sampler_matches_oracle(oracle):
     np.testing.assert_array_equal(rt, np.repeat(t, 2 * c["counts"]))
 
 
+def test_streakline_sampler_matches_oracle(oracle):
+    """The streakline DF runs the same GPU sampler with constant placement."""
+    import torch
+
+    from gala_gb300.mockstream import StreaklineStreamDF
+
+    c = stream_case(n_streams=2, n_steps=60)
+    t = c["t"]
+    S = c["orbits"].shape[0]
+    df = StreaklineStreamDF()
+    prog_w = torch.from_numpy(np.ascontiguousarray(c["orbits"].reshape(S, len(t), 6))).cuda()
+    m = np.repeat(c["m"][:, None], len(t), axis=1)
+    w, rt, lt, off = df.sample_device(c["pot"], prog_w, t, m, c["counts"])
+    w = w.cpu().numpy()
+    for s in range(S):
+        ref = oracle.fardal_sample(c["pot"], c["orbits"][s].reshape(len(t), 6), m[s], t, off,
+                                   df._draws(int(off[-1])), g.units.G)
+        base = np.repeat(c["orbits"][s, :, 0], 2 * c["counts"], axis=0)
+        assert _scale_err(w[s] - base, ref - base) < 2e-9
+
+
 # ---------------------------------------------------------------- generator
 def _oracle_run(oracle, pot, prog_pot, w0, m, t, seed, release_every=1, n_per_tail=1):
     """gala's MockStreamGenerator.run with the oracle for every numerical step."""

@@ -218,3 +218,36 @@ def test_mockstream_leapfrog_golden(oracle, golden):
 def _lf_nbody_args():
     mw, bodies, w0, t = _nbody_system()
     return bodies, 2, w0, t
+
+
+def test_streakline_release_geometry(oracle):
+    """StreaklineStreamDF (df.pyx:242-319): particles at -/+ r_J along the
+    progenitor's radius vector, -/+ v_J along e_y = -(x_hat x L_hat), nothing
+    drawn -- the Fardal placement with constants (1, 0, 1, 0); the random state
+    is not consumed."""
+    from gala_gb300.mockstream import StreaklineStreamDF
+
+    rs = np.random.RandomState(3)
+    state = rs.get_state()[1].copy()
+    df = StreaklineStreamDF(random_state=rs)
+    draws = df._draws(8)
+    assert np.array_equal(rs.get_state()[1], state)
+    np.testing.assert_array_equal(draws, np.tile([1.0, 0.0, 1.0, 0.0], (8, 1)))
+    mw = W.mw_composite()
+    w = W.mw_ics(4, seed=9).T.copy()
+    t = np.arange(4.0)
+    m = np.full(4, 2e5)
+    offset = np.array([0, 2, 4, 6, 8])
+    out = oracle.fardal_sample(mw, w, m, t, offset, draws, g.units.G)
+    d2 = oracle.d2_dr2(mw, w[:, :3])
+    for i in range(4):
+        x, v = w[i, :3], w[i, 3:]
+        L = np.cross(x, v)
+        Om = np.linalg.norm(L) / np.dot(x, x)
+        rj = (g.units.G * m[i] / (Om * Om - d2[i])) ** (1 / 3)
+        e0, e2 = x / np.linalg.norm(x), L / np.linalg.norm(L)
+        e1 = -np.cross(e0, e2)
+        for k, sgn in enumerate((1.0, -1.0)):
+            row = offset[i] + k
+            np.testing.assert_allclose(out[row, :3] - x, sgn * rj * e0, rtol=0, atol=1e-12 * rj)
+            np.testing.assert_allclose(out[row, 3:] - v, sgn * Om * rj * e1, rtol=0, atol=1e-12 * Om * rj)

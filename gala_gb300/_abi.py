@@ -112,6 +112,8 @@ SIGNATURES = {
                                               _P, _P]),
     "gx_orbit_extrema": (C.c_int, [_P, _P, _I64, _I64, _I32, _I32, _P, _P, _P, _P, _P, _P, _P]),
     "gx_fardal_sample": (C.c_int, [_PP, _I64, _I64, _P, _I64, _P, _P, _P, _I64, _P, _D, _I32, _I32, _I32, _P, _P]),
+    "gx_stream_sample": (C.c_int, [_PP, _I64, _I64, _P, _I64, _P, _P, _P, _I64, _I32, _P, _D, _I32, _I32, _I32, _P,
+                                   _P]),
     "gx_batch_integrate_fp64": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P]),
     "gx_dop853_integrate_hamiltonian": (
         C.c_int,

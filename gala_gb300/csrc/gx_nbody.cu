@@ -339,20 +339,24 @@ nbody_dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
             GRHS(am, yy1, k8);
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                yy1[c] = fma(h, fma(a98, k8[c], fma(a97, k7[c], fma(a96, k6[c], fma(a95, k5[c], fma(a94, k4[c], a91 * k1[c]))))), y[c]);
+                yy1[c] = fma(h, fma(a98, k8[c], fma(a97, k7[c], fma(a96, k6[c], fma(a95, k5[c],
+                    fma(a94, k4[c], a91 * k1[c]))))), y[c]);
             GRHS(am, yy1, k9);
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                yy1[c] = fma(h, fma(a109, k9[c], fma(a108, k8[c], fma(a107, k7[c], fma(a106, k6[c], fma(a105, k5[c], fma(a104, k4[c], a101 * k1[c])))))), y[c]);
+                yy1[c] = fma(h, fma(a109, k9[c], fma(a108, k8[c], fma(a107, k7[c], fma(a106, k6[c], fma(a105, k5[c],
+                    fma(a104, k4[c], a101 * k1[c])))))), y[c]);
             GRHS(am, yy1, k10);
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                yy1[c] = fma(h, fma(a1110, k10[c], fma(a119, k9[c], fma(a118, k8[c], fma(a117, k7[c], fma(a116, k6[c], fma(a115, k5[c], fma(a114, k4[c], a111 * k1[c]))))))), y[c]);
+                yy1[c] = fma(h, fma(a1110, k10[c], fma(a119, k9[c], fma(a118, k8[c], fma(a117, k7[c], fma(a116, k6[c],
+                    fma(a115, k5[c], fma(a114, k4[c], a111 * k1[c]))))))), y[c]);
             GRHS(am, yy1, k2);
             const double xph = x + h;
 #pragma unroll
             for (int c = 0; c < 6; c++)
-                yy1[c] = fma(h, fma(a1211, k2[c], fma(a1210, k10[c], fma(a129, k9[c], fma(a128, k8[c], fma(a127, k7[c], fma(a126, k6[c], fma(a125, k5[c], fma(a124, k4[c], a121 * k1[c])))))))), y[c]);
+                yy1[c] = fma(h, fma(a1211, k2[c], fma(a1210, k10[c], fma(a129, k9[c], fma(a128, k8[c], fma(a127, k7[c],
+                    fma(a126, k6[c], fma(a125, k5[c], fma(a124, k4[c], a121 * k1[c])))))))), y[c]);
             GRHS(am, yy1, k3);
             nfcn += 11;
 #pragma unroll
@@ -444,15 +448,18 @@ nbody_dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
                 }
 #pragma unroll
                 for (int c = 0; c < 6; c++)
-                    yy1[c] = fma(h, fma(a1413, k4[c], fma(a1412, k3[c], fma(a1411, k2[c], fma(a1410, k10[c], fma(a149, k9[c], fma(a148, k8[c], fma(a147, k7[c], a141 * k1[c]))))))), y[c]);
+                    yy1[c] = fma(h, fma(a1413, k4[c], fma(a1412, k3[c], fma(a1411, k2[c], fma(a1410, k10[c],
+                        fma(a149, k9[c], fma(a148, k8[c], fma(a147, k7[c], a141 * k1[c]))))))), y[c]);
                 GRHS(am, yy1, k10);
 #pragma unroll
                 for (int c = 0; c < 6; c++)
-                    yy1[c] = fma(h, fma(a1514, k10[c], fma(a1513, k4[c], fma(a1512, k3[c], fma(a1511, k2[c], fma(a158, k8[c], fma(a157, k7[c], fma(a156, k6[c], a151 * k1[c]))))))), y[c]);
+                    yy1[c] = fma(h, fma(a1514, k10[c], fma(a1513, k4[c], fma(a1512, k3[c], fma(a1511, k2[c],
+                        fma(a158, k8[c], fma(a157, k7[c], fma(a156, k6[c], a151 * k1[c]))))))), y[c]);
                 GRHS(am, yy1, k2);
 #pragma unroll
                 for (int c = 0; c < 6; c++)
-                    yy1[c] = fma(h, fma(a1615, k2[c], fma(a1614, k10[c], fma(a1613, k4[c], fma(a169, k9[c], fma(a168, k8[c], fma(a167, k7[c], fma(a166, k6[c], a161 * k1[c]))))))), y[c]);
+                    yy1[c] = fma(h, fma(a1615, k2[c], fma(a1614, k10[c], fma(a1613, k4[c], fma(a169, k9[c],
+                        fma(a168, k8[c], fma(a167, k7[c], fma(a166, k6[c], a161 * k1[c]))))))), y[c]);
                 GRHS(am, yy1, k3);
                 if (acc && !stiff) {
                     nfcn += 3;
@@ -576,11 +583,57 @@ struct FardalArgs {
     const double *prog_m;   // (n_streams, ntimes)
     const double *t;        // (ntimes)
     const int64_t *offset;  // (ntimes + 1) first row of the particles released at each time
-    const double *draws;    // (n_streams, n_particles, 4): kx, kz, kvt, kvz
+    const double *draws;    // (n_streams, n_particles, ndraw), see release_offsets
     double G;
     int32_t lead, trail, gala_modified;
+    int32_t kind, ndraw;    // 0 Fardal (4 draws), 1 Lagrange cloud (3), 2 Chen (6)
     double *w_out;          // (n_streams, n_particles, 6)
 };
+
+// Release placement in the satellite frame (x along the progenitor's radius
+// vector, z along its angular momentum) of one particle of tail `tail` (0
+// trailing, 1 leading):
+//   kind 0, FardalStreamDF (df.pyx:410-450): draws kx, kz, kvt, kvz;
+//   kind 1, LagrangeCloudStreamDF (df.pyx:515-552): (+-rj, 0, 0), velocity the
+//     three draws (each normal(0, v_disp), drawn by the caller);
+//   kind 2, ChenStreamDF (df.pyx:614-700): the six multivariate-normal draws
+//     r, phi, theta, v, alpha, beta (degrees); Dr = r rj, Dv = v sqrt(2 G m / Dr);
+//     the leading tail adds pi to phi and alpha.
+// Components gala leaves unset are zero.
+__device__ __forceinline__ void release_offsets(int kind, int gala_modified, const double *d, int tail, double rj,
+                                                double vj, double G, double m, double *tx, double *tv) {
+    const double sr = (tail == 0) ? rj : -rj, sv = (tail == 0) ? vj : -vj;
+    tx[0] = tx[1] = tx[2] = 0.;
+    tv[0] = tv[1] = tv[2] = 0.;
+    if (kind == 0) {
+        const double kx = d[0];
+        tx[0] = kx * sr;
+        tx[2] = d[1] * sr;
+        tv[1] = d[2] * sv;
+        if (gala_modified) tv[1] *= kx;
+        tv[2] = d[3] * sv;
+    } else if (kind == 1) {
+        tx[0] = sr;
+        tv[0] = d[0];
+        tv[1] = d[1];
+        tv[2] = d[2];
+    } else {
+        const double pi = 3.14159265358979323846;
+        const double Dr = d[0] * rj;
+        const double Dv = d[3] * sqrt(2 * G * m / Dr);
+        double p1 = d[1] * (pi / 180), p2 = d[2] * (pi / 180), p4 = d[4] * (pi / 180), p5 = d[5] * (pi / 180);
+        if (tail == 1) {
+            p1 = p1 + pi;
+            p4 = p4 + pi;
+        }
+        tx[0] = Dr * cos(p2) * cos(p1);
+        tx[1] = Dr * cos(p2) * sin(p1);
+        tx[2] = Dr * sin(p2);
+        tv[0] = Dv * cos(p5) * cos(p4);
+        tv[1] = Dv * cos(p5) * sin(p4);
+        tv[2] = Dv * sin(p5);
+    }
+}
 
 // c_potential at one point (cpotential.cpp:170-189).
 template <bool SCF>
@@ -645,15 +698,10 @@ __global__ void __launch_bounds__(128) fardal_sample_kernel(const __grid_constan
     for (int tail = 0; tail < 2; tail++) {
         if (tail == 0 && !A.trail) continue;
         if (tail == 1 && !A.lead) continue;
-        const double sr = (tail == 0) ? rj : -rj;
-        const double sv = (tail == 0) ? vj : -vj;
         for (int64_t k = 0; k < np; k++, row++) {
-            const double *d = A.draws + (s * A.n_particles + row) * 4;
-            const double kx = d[0];
-            const double tx[3] = {kx * sr, 0., d[1] * sr};
-            double tv1 = d[2] * sv;
-            if (A.gala_modified) tv1 *= kx;
-            const double tv[3] = {0., tv1, d[3] * sv};
+            double tx[3], tv[3];
+            release_offsets(A.kind, A.gala_modified, A.draws + (s * A.n_particles + row) * A.ndraw, tail, rj, vj,
+                            A.G, m, tx, tv);
             double *o = A.w_out + (s * A.n_particles + row) * 6;
             for (int n = 0; n < 3; n++) {
                 double ox = R[0][n] * tx[0] + R[1][n] * tx[1] + R[2][n] * tx[2];
@@ -794,10 +842,12 @@ extern "C" int gx_mockstream_dop853(const gx_potential *pot, const gx_frame *fra
     return gx::launch_nbody<true, false>(dp, df, A, gx::as_stream(stream));
 }
 
-extern "C" int gx_fardal_sample(const gx_potential *pot, int64_t n_streams, int64_t ntimes, const double *prog_w,
+extern "C" int gx_stream_sample(const gx_potential *pot, int64_t n_streams, int64_t ntimes, const double *prog_w,
                                 int64_t row_stride, const double *prog_m, const double *t,
-                                const int64_t *release_offset, int64_t n_particles, const double *draws, double G,
-                                int32_t lead, int32_t trail, int32_t gala_modified, double *w_out, void *stream) {
+                                const int64_t *release_offset, int64_t n_particles, int32_t kind,
+                                const double *draws, double G, int32_t lead, int32_t trail, int32_t gala_modified,
+                                double *w_out, void *stream) {
+    GX_CHECK_ARG(kind >= 0 && kind <= 2, "kind must be 0 (Fardal), 1 (Lagrange cloud) or 2 (Chen)");
     gx::DevPot dp;
     int rc = gx::pack_potential(pot, &dp);
     if (rc) return rc;
@@ -820,6 +870,8 @@ extern "C" int gx_fardal_sample(const gx_potential *pot, int64_t n_streams, int6
     A.lead = lead ? 1 : 0;
     A.trail = trail ? 1 : 0;
     A.gala_modified = gala_modified ? 1 : 0;
+    A.kind = kind;
+    A.ndraw = kind == 0 ? 4 : kind == 1 ? 3 : 6;
     A.w_out = w_out;
     const int64_t n = n_streams * ntimes;
     const unsigned grid = (unsigned)((n + 127) / 128);
@@ -828,5 +880,13 @@ extern "C" int gx_fardal_sample(const gx_potential *pot, int64_t n_streams, int6
         gx::fardal_sample_kernel<true><<<grid, 128, 0, st>>>(dp, A);
     else
         gx::fardal_sample_kernel<false><<<grid, 128, 0, st>>>(dp, A);
-    return gx::check_launch("fardal_sample");
+    return gx::check_launch("stream_sample");
+}
+
+extern "C" int gx_fardal_sample(const gx_potential *pot, int64_t n_streams, int64_t ntimes, const double *prog_w,
+                                int64_t row_stride, const double *prog_m, const double *t,
+                                const int64_t *release_offset, int64_t n_particles, const double *draws, double G,
+                                int32_t lead, int32_t trail, int32_t gala_modified, double *w_out, void *stream) {
+    return gx_stream_sample(pot, n_streams, ntimes, prog_w, row_stride, prog_m, t, release_offset, n_particles, 0,
+                            draws, G, lead, trail, gala_modified, w_out, stream);
 }

@@ -29,15 +29,15 @@ import warnings
 
 import numpy as np
 
-from . import _abi
+from . import _abi, units
 from .dynamics import PhaseSpacePosition
 from .hamiltonian import Hamiltonian, StaticFrame
 from .integrate import DOPRI853Integrator, LeapfrogIntegrator, get_integrator, parse_time_specification
 from .nbody import DirectNBody, bodies_to_device, integrate_systems, integrate_systems_leapfrog, pack_bodies
 from .potential import PotentialBase
 
-__all__ = ["MockStream", "BaseStreamDF", "FardalStreamDF", "StreaklineStreamDF", "MockStreamGenerator",
-           "MockStreamBatch"]
+__all__ = ["MockStream", "BaseStreamDF", "FardalStreamDF", "StreaklineStreamDF", "LagrangeCloudStreamDF",
+           "ChenStreamDF", "MockStreamGenerator", "MockStreamBatch"]
 
 
 class MockStream(PhaseSpacePosition):
@@ -97,8 +97,79 @@ class BaseStreamDF:
         n[::release_every] = int(n_particles)
         return n
 
+    # kind of release placement of the GPU sampler, and draws per particle
+    _KIND, _NDRAW = 0, 4
+
     def _draws(self, n_rows):
         raise NotImplementedError
+
+    # -- sampling ---------------------------------------------------------------
+    def sample_device(self, potential, prog_w, prog_t, prog_m, counts, stream=None):
+        """Release states for n_streams progenitor orbits on one time grid.
+
+        prog_w : CUDA tensor (n_streams, ntimes, k >= 6): progenitor x, v first
+        prog_t : (ntimes,) float64; prog_m : (n_streams, ntimes)
+        counts : (ntimes,) particles per tail
+        Returns (w (n_streams, n_rows, 6) CUDA tensor, release_time (n_rows,),
+        lead_trail (n_rows,), offset (ntimes + 1,) int64).
+        """
+        import torch
+
+        from ._device import as_device_f64, ptr, stream_handle
+
+        ns, ntimes = int(prog_w.shape[0]), int(prog_w.shape[1])
+        ntail = self._lead + self._trail
+        counts = np.asarray(counts, dtype=np.int64)
+        offset = np.concatenate([[0], np.cumsum(ntail * counts)]).astype(np.int64)
+        n_rows = int(offset[-1])
+        prog_m = np.broadcast_to(np.asarray(prog_m, dtype=np.float64), (ns, ntimes))
+        if np.any((counts > 0)[None, :] & (prog_m == 0)):
+            raise NotImplementedError("a zero progenitor mass at a release time is not supported")
+        draws = (np.stack([self._draws(n_rows) for _ in range(ns)]) if ns
+                 else np.zeros((0, n_rows, self._NDRAW)))
+        dev = prog_w.device
+        out = torch.empty((ns, n_rows, 6), dtype=torch.float64, device=dev)
+        pw = prog_w.contiguous()
+        dd = as_device_f64(draws, dev)
+        md = as_device_f64(np.ascontiguousarray(prog_m), dev)
+        td = as_device_f64(prog_t, dev)
+        od = torch.from_numpy(offset).to(dev)
+        _abi.call("gx_stream_sample", potential.packed().for_device(), ns, ntimes, ptr(pw), int(pw.shape[2]),
+                  ptr(md), ptr(td), ptr(od), n_rows, self._KIND, ptr(dd), float(potential.G), self._lead,
+                  self._trail, getattr(self, "_gala_modified", 0), ptr(out), stream_handle(stream))
+        release_time = np.repeat(np.asarray(prog_t, dtype=np.float64), ntail * counts)
+        lt = []
+        for n in counts:
+            if self._trail:
+                lt += ["t"] * int(n)
+            if self._lead:
+                lt += ["l"] * int(n)
+        return out, release_time, np.array(lt, dtype="U1"), offset
+
+    def sample(self, prog_orbit, prog_mass, hamiltonian=None, release_every=1, n_particles=1):
+        """Stream initial conditions around a progenitor orbit (df.pyx:125-242)."""
+        from ._device import as_device_f64, require_cuda
+
+        if getattr(prog_orbit, "hamiltonian", None) is not None:
+            H = prog_orbit.hamiltonian
+        elif hamiltonian is not None:
+            H = hamiltonian if isinstance(hamiltonian, Hamiltonian) else Hamiltonian(hamiltonian)
+        else:
+            raise ValueError("a Hamiltonian is needed to sample stream particles")
+        if not isinstance(H.frame, StaticFrame):
+            raise NotImplementedError("stream sampling is implemented for a static frame")
+        x = np.asarray(prog_orbit.xyz, dtype=np.float64)
+        v = np.asarray(prog_orbit.v_xyz, dtype=np.float64)
+        t = np.asarray(prog_orbit.t, dtype=np.float64)
+        ntimes = len(t)
+        prog_w = np.ascontiguousarray(np.vstack([x, v]).T.reshape(1, ntimes, 6))
+        m = np.squeeze(np.asarray(getattr(prog_mass, "value", prog_mass), dtype=np.float64))
+        m = np.full(ntimes, float(m)) if m.shape == () else m
+        counts = self.release_counts(ntimes, release_every, n_particles)
+        dev = require_cuda()
+        w, rt, lt, _ = self.sample_device(H.potential, as_device_f64(prog_w, dev), t, m[None, :], counts)
+        w = w[0].cpu().numpy()
+        return MockStream(pos=w[:, :3].T, vel=w[:, 3:].T, frame=H.frame, release_time=rt, lead_trail=lt)
 
 
 class FardalStreamDF(BaseStreamDF):
@@ -136,74 +207,6 @@ class FardalStreamDF(BaseStreamDF):
         scale = np.tile(disp, n_rows)
         return np.asarray(self.random_state.normal(loc, scale), dtype=np.float64).reshape(n_rows, 4)
 
-    # -- sampling ---------------------------------------------------------------
-    def sample_device(self, potential, prog_w, prog_t, prog_m, counts, stream=None):
-        """Release states for n_streams progenitor orbits on one time grid.
-
-        prog_w : CUDA tensor (n_streams, ntimes, k >= 6): progenitor x, v first
-        prog_t : (ntimes,) float64; prog_m : (n_streams, ntimes)
-        counts : (ntimes,) particles per tail
-        Returns (w (n_streams, n_rows, 6) CUDA tensor, release_time (n_rows,),
-        lead_trail (n_rows,), offset (ntimes + 1,) int64).
-        """
-        import torch
-
-        from ._device import as_device_f64, ptr, stream_handle
-
-        ns, ntimes = int(prog_w.shape[0]), int(prog_w.shape[1])
-        ntail = self._lead + self._trail
-        counts = np.asarray(counts, dtype=np.int64)
-        offset = np.concatenate([[0], np.cumsum(ntail * counts)]).astype(np.int64)
-        n_rows = int(offset[-1])
-        prog_m = np.broadcast_to(np.asarray(prog_m, dtype=np.float64), (ns, ntimes))
-        if np.any((counts > 0)[None, :] & (prog_m == 0)):
-            raise NotImplementedError("a zero progenitor mass at a release time is not supported")
-        draws = np.stack([self._draws(n_rows) for _ in range(ns)]) if ns else np.zeros((0, n_rows, 4))
-        dev = prog_w.device
-        out = torch.empty((ns, n_rows, 6), dtype=torch.float64, device=dev)
-        pw = prog_w.contiguous()
-        dd = as_device_f64(draws, dev)
-        md = as_device_f64(np.ascontiguousarray(prog_m), dev)
-        td = as_device_f64(prog_t, dev)
-        od = torch.from_numpy(offset).to(dev)
-        _abi.call("gx_fardal_sample", potential.packed().for_device(), ns, ntimes, ptr(pw), int(pw.shape[2]),
-                  ptr(md), ptr(td), ptr(od), n_rows, ptr(dd), float(potential.G), self._lead, self._trail,
-                  self._gala_modified, ptr(out), stream_handle(stream))
-        release_time = np.repeat(np.asarray(prog_t, dtype=np.float64), ntail * counts)
-        lt = []
-        for n in counts:
-            if self._trail:
-                lt += ["t"] * int(n)
-            if self._lead:
-                lt += ["l"] * int(n)
-        return out, release_time, np.array(lt, dtype="U1"), offset
-
-    def sample(self, prog_orbit, prog_mass, hamiltonian=None, release_every=1, n_particles=1):
-        """Stream initial conditions around a progenitor orbit (df.pyx:125-242)."""
-        from ._device import as_device_f64, require_cuda
-
-        if getattr(prog_orbit, "hamiltonian", None) is not None:
-            H = prog_orbit.hamiltonian
-        elif hamiltonian is not None:
-            H = hamiltonian if isinstance(hamiltonian, Hamiltonian) else Hamiltonian(hamiltonian)
-        else:
-            raise ValueError("a Hamiltonian is needed to sample stream particles")
-        if not isinstance(H.frame, StaticFrame):
-            raise NotImplementedError("stream sampling is implemented for a static frame")
-        x = np.asarray(prog_orbit.xyz, dtype=np.float64)
-        v = np.asarray(prog_orbit.v_xyz, dtype=np.float64)
-        t = np.asarray(prog_orbit.t, dtype=np.float64)
-        ntimes = len(t)
-        prog_w = np.ascontiguousarray(np.vstack([x, v]).T.reshape(1, ntimes, 6))
-        m = np.squeeze(np.asarray(getattr(prog_mass, "value", prog_mass), dtype=np.float64))
-        m = np.full(ntimes, float(m)) if m.shape == () else m
-        counts = self.release_counts(ntimes, release_every, n_particles)
-        dev = require_cuda()
-        w, rt, lt, _ = self.sample_device(H.potential, as_device_f64(prog_w, dev), t, m[None, :], counts)
-        w = w[0].cpu().numpy()
-        return MockStream(pos=w[:, :3].T, vel=w[:, 3:].T, frame=H.frame, release_time=rt, lead_trail=lt)
-
-
 class StreaklineStreamDF(FardalStreamDF):
     """Kuepper et al. (2012) streakline release (StreaklineStreamDF,
     df.pyx:242-319): every particle at -/+ r_J along the satellite-frame x axis
@@ -221,6 +224,52 @@ class StreaklineStreamDF(FardalStreamDF):
 
     def _draws(self, n_rows):
         return np.tile(np.array([1.0, 0.0, 1.0, 0.0]), (n_rows, 1))
+
+
+class LagrangeCloudStreamDF(BaseStreamDF):
+    """Lagrange-cloud stripping (Gibbons et al. 2014, as modified by Erkal et al.
+    2019; LagrangeCloudStreamDF, df.pyx:460-555): every particle at -/+ r_J
+    along the satellite-frame x axis, its satellite-frame velocity three normal
+    draws of dispersion v_disp (km/s), drawn per particle in gala's order."""
+
+    _KIND, _NDRAW = 1, 3
+
+    def __init__(self, v_disp, lead=True, trail=True, random_state=None):
+        super().__init__(lead=lead, trail=trail, random_state=random_state)
+        self.v_disp = float(getattr(v_disp, "value", v_disp))
+        self._v_disp = self.v_disp * units.KMS_TO_KPC_MYR
+
+    def _draws(self, n_rows):
+        if n_rows == 0:
+            return np.zeros((0, 3))
+        return np.asarray(self.random_state.normal(0, self._v_disp, size=(n_rows, 3)), dtype=np.float64)
+
+
+class ChenStreamDF(BaseStreamDF):
+    """Chen et al. (2024) release (ChenStreamDF, df.pyx:557-703): per particle one
+    multivariate-normal sample of (r/r_J, phi, theta, v/v_esc, alpha, beta) with
+    gala's mean and covariance; position Dr = r r_J at angles (phi, theta),
+    velocity Dv = v sqrt(2 G m / Dr) at angles (alpha, beta); the leading tail
+    turns phi and alpha by pi.  The samples are drawn one particle at a time, as
+    gala does, so the random state is consumed identically."""
+
+    _KIND, _NDRAW = 2, 6
+
+    _MEAN = np.array([1.6, -30.0, 0.0, 1.0, 20.0, 0.0])
+
+    @staticmethod
+    def _cov():
+        cov = np.zeros((6, 6))
+        cov[0, 0], cov[1, 1], cov[2, 2], cov[3, 3], cov[4, 4], cov[5, 5] = 0.1225, 529.0, 144.0, 0.0, 400.0, 484.0
+        cov[0, 4] = cov[4, 0] = -4.9
+        return cov
+
+    def _draws(self, n_rows):
+        cov = self._cov()
+        out = np.zeros((n_rows, 6))
+        for r in range(n_rows):
+            out[r] = self.random_state.multivariate_normal(self._MEAN, cov)
+        return out
 
 
 class MockStreamBatch:

@@ -484,6 +484,19 @@ int gx_fardal_sample(const gx_potential* pot, int64_t n_streams, int64_t ntimes,
                      const double* draws, double G, int32_t lead, int32_t trail,
                      int32_t gala_modified, double* w_out, void* stream);
 
+/* The same release sampler for the other stream DFs of gala (df.pyx): kind 0
+ * FardalStreamDF as above (4 draws per particle; the streakline DF is kind 0
+ * with draws 1, 0, 1, 0), kind 1 LagrangeCloudStreamDF (df.pyx:460-555; 3
+ * draws: the satellite-frame velocity, each normal(0, v_disp)), kind 2
+ * ChenStreamDF (df.pyx:557-703; 6 draws: one multivariate_normal sample of
+ * r, phi, theta, v, alpha, beta in degrees).  draws is DEVICE (n_streams,
+ * n_particles, 4 | 3 | 6); the other arguments are those of gx_fardal_sample. */
+int gx_stream_sample(const gx_potential* pot, int64_t n_streams, int64_t ntimes,
+                     const double* prog_w, int64_t row_stride, const double* prog_m,
+                     const double* t, const int64_t* release_offset, int64_t n_particles,
+                     int32_t kind, const double* draws, double G, int32_t lead, int32_t trail,
+                     int32_t gala_modified, double* w_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

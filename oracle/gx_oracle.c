@@ -1151,9 +1151,62 @@ void orc_d2_dr2_n(const gx_potential *pot, double t, const double *q, int64_t N,
  *   offset (ntimes + 1) first particle row per time (trailing rows first)
  *   draws (n_particles, 4) the normal draws kx, kz, kvt, kvz
  *   w_out (n_particles, 6) */
+void orc_stream_sample(const gx_potential *pot, int64_t ntimes, const double *prog_w, int64_t row_stride,
+                       const double *prog_m, const double *t, const int64_t *offset, int kind, int ndraw,
+                       const double *draws, double G, int lead, int trail, int gala_modified, double *w_out);
+
 void orc_fardal_sample(const gx_potential *pot, int64_t ntimes, const double *prog_w, int64_t row_stride,
                        const double *prog_m, const double *t, const int64_t *offset, const double *draws, double G,
                        int lead, int trail, int gala_modified, double *w_out) {
+    orc_stream_sample(pot, ntimes, prog_w, row_stride, prog_m, t, offset, 0, 4, draws, G, lead, trail, gala_modified,
+                      w_out);
+}
+
+/* Release placement of the stream DFs in the satellite frame, per particle.
+ * kind 0, FardalStreamDF (df.pyx:410-450): draws kx, kz, kvt, kvz;
+ * kind 1, LagrangeCloudStreamDF (df.pyx:515-552): position (+-rj, 0, 0), velocity
+ *   the three draws (normal(0, v_disp) each, drawn by the caller);
+ * kind 2, ChenStreamDF (df.pyx:614-700): the six draws of multivariate_normal
+ *   (r, phi, theta, v, alpha, beta; degrees), Dr = r rj, Dv = v sqrt(2 G m / Dr),
+ *   the leading tail adds pi to phi and alpha. */
+static void orc_release_offsets(int kind, int gala_modified, const double *d, int lead_tail, double rj, double vj,
+                                double G, double m, double *tx, double *tv) {
+    const double sr = lead_tail == 0 ? rj : -rj, sv = lead_tail == 0 ? vj : -vj;
+    tx[0] = tx[1] = tx[2] = 0.;
+    tv[0] = tv[1] = tv[2] = 0.;
+    if (kind == 0) {
+        const double kx = d[0];
+        tx[0] = kx * sr;
+        tx[2] = d[1] * sr;
+        tv[1] = d[2] * sv;
+        if (gala_modified) tv[1] *= kx;
+        tv[2] = d[3] * sv;
+    } else if (kind == 1) {
+        tx[0] = sr;
+        tv[0] = d[0];
+        tv[1] = d[1];
+        tv[2] = d[2];
+    } else {
+        const double pi = 3.14159265358979323846;
+        const double Dr = d[0] * rj;
+        const double Dv = d[3] * sqrt(2 * G * m / Dr);
+        double p1 = d[1] * (pi / 180), p2 = d[2] * (pi / 180), p4 = d[4] * (pi / 180), p5 = d[5] * (pi / 180);
+        if (lead_tail == 1) {
+            p1 = p1 + pi;
+            p4 = p4 + pi;
+        }
+        tx[0] = Dr * cos(p2) * cos(p1);
+        tx[1] = Dr * cos(p2) * sin(p1);
+        tx[2] = Dr * sin(p2);
+        tv[0] = Dv * cos(p5) * cos(p4);
+        tv[1] = Dv * cos(p5) * sin(p4);
+        tv[2] = Dv * sin(p5);
+    }
+}
+
+void orc_stream_sample(const gx_potential *pot, int64_t ntimes, const double *prog_w, int64_t row_stride,
+                       const double *prog_m, const double *t, const int64_t *offset, int kind, int ndraw,
+                       const double *draws, double G, int lead, int trail, int gala_modified, double *w_out) {
     const int ntail = lead + trail;
     for (int64_t i = 0; i < ntimes; i++) {
         const int64_t o0 = offset[i], o1 = offset[i + 1];
@@ -1189,16 +1242,9 @@ void orc_fardal_sample(const gx_potential *pot, int64_t ntimes, const double *pr
         for (int tail = 0; tail < 2; tail++) {
             if (tail == 0 && !trail) continue;
             if (tail == 1 && !lead) continue;
-            const double sr = tail == 0 ? rj : -rj, sv = tail == 0 ? vj : -vj;
             for (int64_t k = 0; k < np_; k++, row++) {
-                const double *d = draws + row * 4;
-                const double kx = d[0];
-                double tx[3] = {0., 0., 0.}, tv[3] = {0., 0., 0.};
-                tx[0] = kx * sr;
-                tx[2] = d[1] * sr;
-                tv[1] = d[2] * sv;
-                if (gala_modified) tv[1] *= kx;
-                tv[2] = d[3] * sv;
+                double tx[3], tv[3];
+                orc_release_offsets(kind, gala_modified, draws + row * ndraw, tail, rj, vj, G, m, tx, tv);
                 double *o = w_out + row * 6;
                 for (int n = 0; n < 3; n++) {
                     o[n] = R[0][n] * tx[0] + R[1][n] * tx[1] + R[2][n] * tx[2];

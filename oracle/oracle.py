@@ -265,6 +265,24 @@ class Oracle:
                                    C.c_double(G), C.c_int(int(lead)), C.c_int(int(trail)),
                                    C.c_int(int(gala_modified)), _p(out))
         return out
+
+    def stream_sample(self, pot, prog_w, prog_m, t, offset, kind, draws, G, lead=True, trail=True,
+                      gala_modified=True):
+        """The release placement of a stream DF for one orbit (kind 0 Fardal,
+        1 Lagrange cloud, 2 Chen; df.pyx:410-450, 515-552, 614-700)."""
+        ndraw = {0: 4, 1: 3, 2: 6}[kind]
+        prog_w = _f64(prog_w)
+        prog_m = _f64(prog_m)
+        t = _f64(t)
+        offset = np.ascontiguousarray(np.asarray(offset, dtype=np.int64))
+        draws = _f64(draws).reshape(-1, ndraw)
+        out = np.zeros((draws.shape[0], 6))
+        self.lib.orc_stream_sample(pot.packed().for_host(), C.c_int64(len(t)), _p(prog_w),
+                                   C.c_int64(prog_w.shape[1]), _p(prog_m), _p(t), _p(offset), C.c_int(kind),
+                                   C.c_int(ndraw), _p(draws), C.c_double(G), C.c_int(int(lead)),
+                                   C.c_int(int(trail)), C.c_int(int(gala_modified)), _p(out))
+        return out
+
     def leapfrog_nbody(self, pot, bodies, nbody, w0, t, save_all=True):
         """leapfrog_integrate_nbody on one system: bodies (n,), w0 (n, 6).
         Returns (ntimes, n, 6) or (n, 6)."""

@@ -233,9 +233,35 @@ def test_streakline_sampler_matches_oracle(oracle):
         assert _scale_err(w[s] - base, ref - base) < 2e-9
 
 
+@pytest.mark.parametrize("kind", [1, 2])
+def test_lagrange_cloud_and_chen_samplers_match_oracle(oracle, kind):
+    """The Lagrange-cloud (kind 1) and Chen (kind 2) DFs on the GPU sampler."""
+    import torch
+
+    from gala_gb300.mockstream import ChenStreamDF, LagrangeCloudStreamDF
+
+    c = stream_case(n_streams=2, n_steps=60)
+    t = c["t"]
+    S = c["orbits"].shape[0]
+    df = (LagrangeCloudStreamDF(v_disp=1.5, random_state=np.random.RandomState(7)) if kind == 1
+          else ChenStreamDF(random_state=np.random.RandomState(7)))
+    prog_w = torch.from_numpy(np.ascontiguousarray(c["orbits"].reshape(S, len(t), 6))).cuda()
+    m = np.repeat(c["m"][:, None], len(t), axis=1)
+    w, rt, lt, off = df.sample_device(c["pot"], prog_w, t, m, c["counts"])
+    w = w.cpu().numpy()
+    rs = np.random.RandomState(7)  # the draws of stream s follow those of streams 0..s-1
+    df_ref = (LagrangeCloudStreamDF(v_disp=1.5, random_state=rs) if kind == 1 else ChenStreamDF(random_state=rs))
+    for s in range(S):
+        draws = df_ref._draws(int(off[-1]))
+        ref = oracle.stream_sample(c["pot"], c["orbits"][s].reshape(len(t), 6), m[s], t, off, kind, draws, g.units.G)
+        base = np.repeat(c["orbits"][s, :, 0], 2 * c["counts"], axis=0)
+        assert _scale_err(w[s] - base, ref - base) < 2e-9
+
+
 # ---------------------------------------------------------------- generator
-def _oracle_run(oracle, pot, prog_pot, w0, m, t, seed, release_every=1, n_per_tail=1):
-    """gala's MockStreamGenerator.run with the oracle for every numerical step."""
+def _oracle_run(oracle, pot, prog_pot, w0, m, t, seed, release_every=1, n_per_tail=1, df=None, kind=0):
+    """gala's MockStreamGenerator.run with the oracle for every numerical step
+    (FardalStreamDF unless another DF and its sampler kind are given)."""
     bodies = pack_bodies([prog_pot])
     orb, res = oracle.nbody_dop853(pot, bodies, 1, w0.reshape(1, 6), t)
     assert res == 1
@@ -243,10 +269,11 @@ def _oracle_run(oracle, pot, prog_pot, w0, m, t, seed, release_every=1, n_per_ta
     if t[1] < t[0]:
         orb = orb[::-1].copy()
         orbit_t = t[::-1].copy()
-    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(seed))
+    if df is None:
+        df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(seed))
     counts = df.release_counts(len(t), release_every, n_per_tail)
     offset = np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)
-    sw0 = oracle.fardal_sample(pot, orb.reshape(len(t), 6), np.full(len(t), m), orbit_t, offset,
+    sw0 = oracle.stream_sample(pot, orb.reshape(len(t), 6), np.full(len(t), m), orbit_t, offset, kind,
                                df._draws(int(offset[-1])), g.units.G)
     rel = np.nonzero(counts > 0)[0]
     if 0 not in rel:
@@ -278,6 +305,36 @@ def test_generator_run_matches_oracle(oracle, case):
     assert _scale_err(got, ref_st) < 1e-10
     assert _scale_err(np.vstack([nbody.xyz, nbody.v_xyz]).T, ref_nb) < 1e-10
     assert set(np.unique(stream.lead_trail)) == {"t", "l"}
+
+
+@pytest.mark.parametrize("which", ["streakline", "lagrange", "chen"])
+def test_generator_with_other_dfs_matches_oracle(oracle, which):
+    """Whole runs with the streakline, Lagrange-cloud and Chen DFs against the
+    oracle.  These release particles at the Jacobi radius itself (Fardal's sit
+    near 2 r_J), where the progenitor's pull amplifies the ulp-level
+    differences of the force forms more: 1e-9 of the stream's extent
+    (measured 1.2e-10 and 1.6e-10 for the first two)."""
+    from gala_gb300.mockstream import ChenStreamDF, LagrangeCloudStreamDF, StreaklineStreamDF
+
+    def make(seed):
+        rs = np.random.RandomState(seed)
+        return {"streakline": lambda: StreaklineStreamDF(random_state=rs),
+                "lagrange": lambda: LagrangeCloudStreamDF(v_disp=1.0, random_state=rs),
+                "chen": lambda: ChenStreamDF(random_state=rs)}[which]()
+
+    kind = {"streakline": 0, "lagrange": 1, "chen": 2}[which]
+    pot = W.mw_composite()
+    w0 = W.mw_ics(1, seed=61)[:, 0]
+    prog_pot = g.PlummerPotential(m=2e5, b=0.01)
+    kw = dict(dt=1.0, n_steps=120)
+    gen = MockStreamGenerator(make(9), g.Hamiltonian(pot), progenitor_potential=prog_pot)
+    stream, nbody = gen.run(g.PhaseSpacePosition.from_w(w0), 2e5, **kw)
+    t = g.parse_time_specification(**kw)
+    ref_st, ref_nb = _oracle_run(oracle, pot, prog_pot, w0, 2e5, t, 9, df=make(9), kind=kind)
+    got = np.vstack([stream.xyz, stream.v_xyz]).T
+    assert got.shape == ref_st.shape
+    assert _scale_err(got, ref_st) < 1e-9
+    assert _scale_err(np.vstack([nbody.xyz, nbody.v_xyz]).T, ref_nb) < 1e-10
 
 
 def test_run_batch_equals_sequential_runs():

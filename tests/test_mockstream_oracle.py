@@ -251,3 +251,74 @@ def test_streakline_release_geometry(oracle):
             row = offset[i] + k
             np.testing.assert_allclose(out[row, :3] - x, sgn * rj * e0, rtol=0, atol=1e-12 * rj)
             np.testing.assert_allclose(out[row, 3:] - v, sgn * Om * rj * e1, rtol=0, atol=1e-12 * Om * rj)
+
+
+def _sat_frame(oracle, mw, w, m):
+    d2 = oracle.d2_dr2(mw, w[:, :3])
+    frames = []
+    for i in range(len(w)):
+        x, v = w[i, :3], w[i, 3:]
+        L = np.cross(x, v)
+        Om = np.linalg.norm(L) / np.dot(x, x)
+        rj = (g.units.G * m[i] / (Om * Om - d2[i])) ** (1 / 3)
+        e0, e2 = x / np.linalg.norm(x), L / np.linalg.norm(L)
+        frames.append((rj, Om * rj, e0, -np.cross(e0, e2), e2))
+    return frames
+
+
+def test_lagrange_cloud_release_geometry(oracle):
+    """LagrangeCloudStreamDF (df.pyx:460-555): -/+ r_J along x, the satellite-frame
+    velocity three normal(0, v_disp) draws per particle, drawn in gala's order."""
+    from gala_gb300.mockstream import LagrangeCloudStreamDF
+
+    df = LagrangeCloudStreamDF(v_disp=2.0, random_state=np.random.RandomState(5))
+    draws = df._draws(8)
+    rs = np.random.RandomState(5)
+    seq = np.array([[rs.normal(0, 2.0 * g.units.KMS_TO_KPC_MYR) for _ in range(3)] for _ in range(8)])
+    np.testing.assert_array_equal(draws, seq)
+    mw = W.mw_composite()
+    w = W.mw_ics(4, seed=10).T.copy()
+    m = np.full(4, 2e5)
+    offset = np.array([0, 2, 4, 6, 8])
+    out = oracle.stream_sample(mw, w, m, np.arange(4.0), offset, 1, draws, g.units.G)
+    for i, (rj, vj, e0, e1, e2) in enumerate(_sat_frame(oracle, mw, w, m)):
+        for k, sgn in enumerate((1.0, -1.0)):
+            row = offset[i] + k
+            d = draws[row]
+            np.testing.assert_allclose(out[row, :3] - w[i, :3], sgn * rj * e0, rtol=0, atol=1e-12 * rj)
+            np.testing.assert_allclose(out[row, 3:] - w[i, 3:], d[0] * e0 + d[1] * e1 + d[2] * e2, rtol=0,
+                                       atol=1e-15)
+
+
+def test_chen_release_geometry(oracle):
+    """ChenStreamDF (df.pyx:557-703): offset Dr = r r_J in the direction (theta,
+    phi) of the satellite frame, velocity Dv = v sqrt(2 G m / Dr) in the direction
+    (beta, alpha); the leading tail turns phi and alpha by pi; one
+    multivariate-normal sample per particle in gala's order."""
+    from gala_gb300.mockstream import ChenStreamDF
+
+    df = ChenStreamDF(random_state=np.random.RandomState(6))
+    draws = df._draws(8)
+    rs = np.random.RandomState(6)
+    seq = np.array([rs.multivariate_normal(ChenStreamDF._MEAN, ChenStreamDF._cov()) for _ in range(8)])
+    np.testing.assert_array_equal(draws, seq)
+    mw = W.mw_composite()
+    w = W.mw_ics(4, seed=11).T.copy()
+    m = np.full(4, 2e5)
+    offset = np.array([0, 2, 4, 6, 8])
+    out = oracle.stream_sample(mw, w, m, np.arange(4.0), offset, 2, draws, g.units.G)
+    for i, (rj, vj, e0, e1, e2) in enumerate(_sat_frame(oracle, mw, w, m)):
+        for k in range(2):
+            row = offset[i] + k
+            r, ph, th, vv, al, be = draws[row]
+            ph, th, al, be = np.radians([ph, th, al, be])
+            if k == 1:
+                ph, al = ph + np.pi, al + np.pi
+            Dr = r * rj
+            Dv = vv * np.sqrt(2 * g.units.G * m[i] / Dr)
+            dx = Dr * np.array([np.cos(th) * np.cos(ph), np.cos(th) * np.sin(ph), np.sin(th)])
+            dv = Dv * np.array([np.cos(be) * np.cos(al), np.cos(be) * np.sin(al), np.sin(be)])
+            np.testing.assert_allclose(out[row, :3] - w[i, :3], dx @ np.stack([e0, e1, e2]), rtol=0,
+                                       atol=1e-12 * rj)
+            np.testing.assert_allclose(out[row, 3:] - w[i, 3:], dv @ np.stack([e0, e1, e2]), rtol=0,
+                                       atol=1e-12 * abs(Dv) + 1e-15)

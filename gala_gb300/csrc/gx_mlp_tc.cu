@@ -26,6 +26,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <atomic>
+
 #include "gx_host.h"
 #include "gx_mlp.cuh"
 #include "gx_mlp_map.cuh"
@@ -625,8 +627,12 @@ static int tc_args(const float *scf_params, double r_min, double r_max, double G
     A->GM = (float)GM;
     A->r_s = (float)r_s;
     A->scf = scf_params;
-    static bool configured = false;
-    if (!configured) {
+    // the shared-memory opt-in belongs to a device's context: once per device
+    static std::atomic<unsigned long long> configured{0};
+    int dev = 0;
+    GX_CUDA_TRY(cudaGetDevice(&dev));
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(configured.load() & bit)) {
         GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_eval_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          SMEM_BYTES));
         GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_eval_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -635,7 +641,7 @@ static int tc_args(const float *scf_params, double r_min, double r_max, double G
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
         GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_leapfrog_tc_kernel<2>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-        configured = true;
+        configured.fetch_or(bit);
     }
     return GX_OK;
 }

@@ -14,7 +14,6 @@ from __future__ import annotations
 import hashlib
 import json
 import os
-import time
 from pathlib import Path
 
 import numpy as np

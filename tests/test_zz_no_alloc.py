@@ -11,7 +11,6 @@ both, so the results must agree bit for bit.
 
 This file is named so that pytest collects it last.
 """
-import ctypes as C
 
 import numpy as np
 import pytest

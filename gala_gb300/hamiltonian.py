@@ -149,47 +149,29 @@ class Hamiltonian:
                 "Using a symplectic integrator with a non-static frame can lead to wildly incorrect orbits. "
                 "It is recommended that you use DOPRI853Integrator instead.", RuntimeWarning)
 
-        dev = require_cuda()
+        # Every argument is checked before the device is touched, in gala's order:
+        # initial-condition shape (chamiltonian.pyx:309-310), time specification
+        # (timespec.py:91-145), then the integrator's own checks (leapfrog.pyx:61-68).
         if isinstance(w0, PhaseSpacePosition):
             arr_w0 = w0.w()
         elif isinstance(w0, torch.Tensor):
             arr_w0 = w0
         else:
             arr_w0 = np.asarray(w0, dtype=np.float64)
-        if arr_w0.shape[0] != 6:
+        if arr_w0.ndim == 0 or arr_w0.shape[0] != 6:
             raise ValueError(
                 f"Invalid initial conditions shape {tuple(arr_w0.shape)}. Expected shape (6, ...) but got shape "
                 f"{tuple(arr_w0.shape)}.")
-        orig_shape = tuple(arr_w0.shape)
-        if isinstance(arr_w0, torch.Tensor):
-            w0d = arr_w0.reshape(6, -1).to(device=dev, dtype=torch.float64).contiguous()
-        else:
-            host = torch.from_numpy(np.ascontiguousarray(arr_w0.reshape(6, -1)))
-            if torch.cuda.is_available():
-                host = host.pin_memory()
-            w0d = host.to(dev, non_blocking=True)
-        n = w0d.shape[1]
-
         t = np.ascontiguousarray(parse_time_specification(self.units, **time_spec), dtype=np.float64)
         ntimes = len(t)
         if ntimes < 2:
             raise ValueError("ntimes must be greater than 1")
-        td = torch.from_numpy(t).to(dev)
-        st = stream_handle(stream)
-        pot = self.potential.packed().for_device()
-        frame = self._frame_ref()
-
-        if Integrator in (LeapfrogIntegrator, Ruth4Integrator):
-            if not isinstance(self.frame, StaticFrame):
-                raise TypeError(
-                    f"{'Leapfrog' if Integrator is LeapfrogIntegrator else 'Ruth4'} integration is currently only "
-                    f"supported for StaticFrame, not {self.frame.__class__.__name__}")
-            out = torch.empty((6, ntimes, n) if save_all else (6, n), dtype=torch.float64, device=dev)
-            name = ("gx_leapfrog_integrate_hamiltonian" if Integrator is LeapfrogIntegrator
-                    else "gx_ruth4_integrate_hamiltonian")
-            _abi.call(name, pot, frame, ptr(w0d), n, ptr(td), ntimes, int(bool(save_all)), ptr(out), st)
-            t_out = t
-        else:
+        symplectic = Integrator in (LeapfrogIntegrator, Ruth4Integrator)
+        if symplectic and not isinstance(self.frame, StaticFrame):
+            raise TypeError(
+                f"{'Leapfrog' if Integrator is LeapfrogIntegrator else 'Ruth4'} integration is currently only "
+                f"supported for StaticFrame, not {self.frame.__class__.__name__}")
+        if not symplectic:
             kw = dict(Integrator_kwargs)
             atol = float(kw.get("atol", 1e-10))
             rtol = float(kw.get("rtol", 1e-10))
@@ -203,6 +185,29 @@ class Hamiltonian:
                 raise ValueError(f"nbatch must be in [1, 1024] (got {nbatch})")
             if stride < 1:
                 raise ValueError(f"out_stride must be >= 1 (got {stride})")
+
+        dev = require_cuda()
+        if isinstance(arr_w0, torch.Tensor):
+            w0d = arr_w0.reshape(6, -1).to(device=dev, dtype=torch.float64).contiguous()
+        else:
+            host = torch.from_numpy(np.ascontiguousarray(arr_w0.reshape(6, -1)))
+            if torch.cuda.is_available():
+                host = host.pin_memory()
+            w0d = host.to(dev, non_blocking=True)
+        n = w0d.shape[1]
+
+        td = torch.from_numpy(t).to(dev)
+        st = stream_handle(stream)
+        pot = self.potential.packed().for_device()
+        frame = self._frame_ref()
+
+        if symplectic:
+            out = torch.empty((6, ntimes, n) if save_all else (6, n), dtype=torch.float64, device=dev)
+            name = ("gx_leapfrog_integrate_hamiltonian" if Integrator is LeapfrogIntegrator
+                    else "gx_ruth4_integrate_hamiltonian")
+            _abi.call(name, pot, frame, ptr(w0d), n, ptr(td), ntimes, int(bool(save_all)), ptr(out), st)
+            t_out = t
+        else:
             n_out = (ntimes - 1) // stride + 1
             nb = (n + nbatch - 1) // nbatch
             out = torch.empty((6, n_out, n) if save_all else (6, n), dtype=torch.float64, device=dev)

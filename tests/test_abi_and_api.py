@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import gala_gb300 as g
-from gala_gb300 import _abi
+from gala_gb300 import _abi, workloads
 from gala_gb300.integrate import parse_time_specification
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -128,3 +128,67 @@ def test_product_path_fails_loudly_without_gpu():
         pot.integrate_orbit(np.ones((6, 2)), dt=1.0, n_steps=10)
     with pytest.raises(RuntimeError, match="CUDA"):
         pot.gradient(np.ones((3, 2)))
+
+
+def test_integrate_orbit_argument_errors_come_before_the_device():
+    """gala's argument errors (chamiltonian.pyx:282-310, leapfrog.pyx:61-68,
+    timespec.py:91-145) are raised whether or not a GPU is present."""
+    pot = g.HernquistPotential(m=1e11, c=1.0)
+    w0 = np.ones((6, 2))
+    with pytest.raises(ValueError, match="shape"):
+        pot.integrate_orbit(np.ones((5, 2)), dt=1.0, n_steps=10)
+    with pytest.raises(ValueError):
+        pot.integrate_orbit(w0, dt=0.0, t1=0.0, t2=1.0)
+    with pytest.raises(ValueError, match="ntimes"):
+        pot.integrate_orbit(w0, t=np.array([0.0]))
+    H = g.Hamiltonian(pot, frame=g.ConstantRotatingFrame(Omega=[0.0, 0.0, 1e-2]))
+    for integ, name in ((g.LeapfrogIntegrator, "Leapfrog"), (g.Ruth4Integrator, "Ruth4")):
+        with pytest.warns(RuntimeWarning, match="non-static frame"):
+            with pytest.raises(TypeError, match=f"{name} integration is currently only supported for StaticFrame"):
+                H.integrate_orbit(w0, Integrator=integ, dt=1.0, n_steps=10)
+    for kw, msg in ((dict(nbatch=0), "nbatch"), (dict(nbatch=2000), "nbatch"), (dict(out_stride=0), "out_stride")):
+        with pytest.raises(ValueError, match=msg):
+            pot.integrate_orbit(w0, Integrator=g.DOPRI853Integrator, Integrator_kwargs=kw, dt=1.0, n_steps=10)
+    with pytest.raises(ValueError):
+        pot.integrate_orbit(w0, Integrator="euler", dt=1.0, n_steps=10)
+
+
+def test_nbody_and_mockstream_argument_errors():
+    """Constructor and argument checks of DirectNBody (nbody/core.py:25-95) and
+    MockStreamGenerator / stream DFs (mockstream_generator.py:20-100, df.pyx:48-60)."""
+    from gala_gb300.mockstream import FardalStreamDF, MockStreamGenerator
+    from gala_gb300.nbody import DirectNBody
+
+    pot = workloads.mw_composite()
+    psp = g.PhaseSpacePosition(pos=np.ones((3, 2)), vel=np.zeros((3, 2)))
+    with pytest.raises(TypeError, match="PhaseSpacePosition"):
+        DirectNBody(np.ones((6, 2)), [None, None], external_potential=pot)
+    with pytest.raises(ValueError, match="must match the number of particle"):
+        DirectNBody(psp, [None], external_potential=pot)
+    nb = DirectNBody(psp, [g.PlummerPotential(m=1e6, b=0.01), None], external_potential=pot)
+    with pytest.raises(NotImplementedError):
+        nb.integrate_orbit(Integrator=g.Ruth4Integrator, dt=1.0, n_steps=4)
+    with pytest.raises(ValueError, match="leading or trailing"):
+        FardalStreamDF(gala_modified=True, lead=False, trail=False)
+    df = FardalStreamDF(gala_modified=True)
+    with pytest.warns(FutureWarning):
+        FardalStreamDF()
+    with pytest.raises(ValueError, match="n_particles"):
+        df.release_counts(10, n_particles=np.ones(9))
+    with pytest.raises(TypeError, match="BaseStreamDF"):
+        MockStreamGenerator(object(), pot)
+    with pytest.raises(TypeError, match="progenitor_potential"):
+        MockStreamGenerator(df, pot, progenitor_potential=1.0)
+    gen = MockStreamGenerator(df, pot, progenitor_potential=g.PlummerPotential(m=1e5, b=0.01))
+    prog = g.PhaseSpacePosition(pos=[10.0, 0, 0], vel=[0, 0.2, 0])
+    with pytest.raises(ValueError, match="DOPRI853Integrator and LeapfrogIntegrator"):
+        gen.run(prog, 1e5, Integrator=g.Ruth4Integrator, dt=1.0, n_steps=4)
+    with pytest.raises(NotImplementedError, match="output_every"):
+        gen.run(prog, 1e5, output_every=2, dt=1.0, n_steps=4)
+    other = DirectNBody(psp, [None, None], external_potential=g.HernquistPotential(m=1e11, c=1.0))
+    with pytest.raises(ValueError, match="external potential"):
+        gen.run(prog, 1e5, nbody=other, dt=1.0, n_steps=4)
+    with pytest.raises(ValueError, match="prog_w0"):
+        gen.run_batch(np.ones((5, 3)), 1e5, dt=1.0, n_steps=4)
+    with pytest.raises(ValueError, match="one progenitor potential"):
+        gen.run_batch(np.ones((6, 3)), 1e5, progenitor_potentials=[None], dt=1.0, n_steps=4)

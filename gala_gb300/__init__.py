@@ -2,11 +2,13 @@
 
 The public surface mirrors gala's: potential classes
 (``gala_gb300.potential``), ``Hamiltonian`` with ``integrate_orbit``, frames,
-``Orbit`` / ``PhaseSpacePosition`` and ``parse_time_specification``.  All
+``Orbit`` / ``PhaseSpacePosition`` (with gala's HDF5 files, ``gala_gb300.hdf5``),
+potential YAML files (``gala_gb300.potential_io``) and
+``parse_time_specification``.  All
 evaluation and integration runs in the CUDA library built from
 ``gala_gb300/csrc`` (C ABI: include/gala_gb300.h).
 """
-from . import units
+from . import hdf5, potential_io, units
 from .dynamics import Orbit, PhaseSpacePosition
 from .hamiltonian import ConstantRotatingFrame, Hamiltonian, StaticFrame
 from .integrate import (DOPRI853Integrator, LeapfrogIntegrator, Ruth4Integrator, get_integrator,
@@ -16,7 +18,7 @@ from .potential import (CCompositePotential, CompositePotential, HernquistPotent
                         PlummerPotential, SCFPotential)
 
 __all__ = [
-    "units", "Orbit", "PhaseSpacePosition", "Hamiltonian", "StaticFrame", "ConstantRotatingFrame",
+    "hdf5", "potential_io", "units", "Orbit", "PhaseSpacePosition", "Hamiltonian", "StaticFrame", "ConstantRotatingFrame",
     "LeapfrogIntegrator", "Ruth4Integrator", "DOPRI853Integrator", "get_integrator", "parse_time_specification",
     "CCompositePotential", "CompositePotential", "HernquistPotential", "KeplerPotential", "MilkyWayPotential",
     "MiyamotoNagaiPotential", "NFWPotential", "NullPotential", "PlummerPotential", "SCFPotential",

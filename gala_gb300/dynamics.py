@@ -16,6 +16,76 @@ def _to_numpy(a):
     return np.asarray(a)
 
 
+# -- HDF5 serialisation helpers (gala's layout: src/gala/io.py:4-47,
+#    src/gala/dynamics/core.py:572-640) ----------------------------------------
+_FRAME_MODULE = "gala.potential.frame.builtin.frames"
+_FRAME_UNITS = [b"kpc", b"Myr", b"solMass", b"rad", b"km / s"]
+
+
+def _h5_open(f, mode):
+    """(file or group, opened here): a file name is opened with this library's
+    HDF5 module; an open h5py or gala_gb300.hdf5 file or group is used as is."""
+    import os
+
+    if isinstance(f, (str, os.PathLike)):
+        from .hdf5 import File
+
+        return File(f, mode), True
+    return f, False
+
+
+def _attr_text(v):
+    if isinstance(v, bytes):
+        return v.decode("utf-8")
+    if isinstance(v, np.ndarray) and v.ndim == 0:
+        return _attr_text(v[()])
+    return None if v is None else str(v)
+
+
+def quantity_to_hdf5(f, key, value, unit):
+    """A dataset with a 'unit' attribute (quantity_to_hdf5, src/gala/io.py:28-47)."""
+    f[key] = np.asarray(value)
+    f[key].attrs["unit"] = unit
+
+
+def quantity_from_hdf5(dset, physical_type=None):
+    """The dataset's values in galactic units (quantity_from_hdf5, src/gala/io.py:4-25):
+    values stored with another unit of the same physical type are converted."""
+    from .potential_io import _unit_factor
+
+    values = np.asarray(dset[()], dtype=np.float64)
+    unit = _attr_text(dset.attrs["unit"]) if "unit" in dset.attrs else None
+    if unit:
+        values = values * _unit_factor(unit, physical_type)
+    return values
+
+
+def _frame_to_hdf5(f, frame):
+    from .hamiltonian import ConstantRotatingFrame
+
+    g = f.create_group("frame")
+    g.attrs["module"] = _FRAME_MODULE
+    g.attrs["class"] = frame.__class__.__name__
+    g.create_dataset("units", data=list(_FRAME_UNITS))
+    pars = g.create_group("parameters")
+    if isinstance(frame, ConstantRotatingFrame):
+        quantity_to_hdf5(pars, "Omega", frame.Omega, "1 / Myr")
+
+
+def _frame_from_hdf5(f):
+    from .hamiltonian import ConstantRotatingFrame, StaticFrame
+
+    if "frame" not in f:
+        return None
+    g = f["frame"]
+    cls = _attr_text(g.attrs["class"])
+    if cls == "StaticFrame":
+        return StaticFrame()
+    if cls == "ConstantRotatingFrame":
+        return ConstantRotatingFrame(Omega=quantity_from_hdf5(g["parameters/Omega"], "frequency"))
+    raise ValueError(f"frame class {cls!r} is not available in gala_gb300")
+
+
 class PhaseSpacePosition:
     """Positions and velocities with gala's axis convention: (ndim, ...)."""
 
@@ -66,6 +136,34 @@ class PhaseSpacePosition:
 
         H = hamiltonian if isinstance(hamiltonian, Hamiltonian) else Hamiltonian(hamiltonian)
         return H.energy(self.w())
+
+    # -- HDF5 (PhaseSpacePosition.to_hdf5 / from_hdf5, dynamics/core.py:572-640)
+    def _write_hdf5(self, f):
+        if self.frame is not None:
+            _frame_to_hdf5(f, self.frame)
+        quantity_to_hdf5(f, "pos", self.pos, "kpc")
+        quantity_to_hdf5(f, "vel", self.vel, "kpc / Myr")
+
+    def to_hdf5(self, f):
+        """Write to an HDF5 file name (created, or overwritten) or an open file or
+        group, in gala's layout: ``pos`` and ``vel`` datasets with a ``unit``
+        attribute and a ``frame`` group.  Returns the file or group."""
+        f, close = _h5_open(f, "w")
+        self._write_hdf5(f)
+        if close:
+            f.close()
+        return f
+
+    @classmethod
+    def from_hdf5(cls, f):
+        """Read what ``to_hdf5`` (or gala's) wrote; values in galactic units."""
+        f, close = _h5_open(f, "r")
+        try:
+            return cls(pos=quantity_from_hdf5(f["pos"], "length"), vel=quantity_from_hdf5(f["vel"], "speed"),
+                       frame=_frame_from_hdf5(f))
+        finally:
+            if close:
+                f.close()
 
 
 class Orbit(PhaseSpacePosition):
@@ -145,6 +243,44 @@ class Orbit(PhaseSpacePosition):
         if not isinstance(H, Hamiltonian):
             H = Hamiltonian(H)
         return H.energy(self.w())
+
+    # -- HDF5 (Orbit.to_hdf5 / from_hdf5, src/gala/dynamics/orbit.py:236-323) --
+    def _write_hdf5(self, f):
+        super()._write_hdf5(f)
+        if self.potential is not None:
+            from .potential_io import to_dict, yaml_dump
+
+            f["potential"] = yaml_dump(to_dict(self.potential)).encode("utf-8")
+        if self.t is not None:
+            quantity_to_hdf5(f, "time", self.t, "Myr")
+
+    @classmethod
+    def from_hdf5(cls, f):
+        """Read an orbit written by ``to_hdf5`` or by gala.  The potential is
+        rebuilt from its YAML when its classes exist here; otherwise a
+        warning is issued and the orbit has no potential."""
+        import warnings
+
+        from .potential_io import from_dict, yaml_load
+
+        f, close = _h5_open(f, "r")
+        try:
+            pos = quantity_from_hdf5(f["pos"], "length")
+            vel = quantity_from_hdf5(f["vel"], "speed")
+            t = quantity_from_hdf5(f["time"], "time") if "time" in f else None
+            frame = _frame_from_hdf5(f)
+            potential = None
+            if "potential" in f:
+                text = f["potential"][()]
+                text = text.decode("utf-8") if isinstance(text, bytes) else str(text)
+                try:
+                    potential = from_dict(yaml_load(text))
+                except (ValueError, KeyError, TypeError, NotImplementedError) as e:
+                    warnings.warn(f"the orbit's potential could not be rebuilt: {e}", RuntimeWarning)
+        finally:
+            if close:
+                f.close()
+        return cls(pos=pos, vel=vel, t=t, frame=frame, potential=potential)
 
     def __getitem__(self, idx):
         w = self.w()

@@ -30,7 +30,7 @@ import warnings
 import numpy as np
 
 from . import _abi, units
-from .dynamics import PhaseSpacePosition
+from .dynamics import PhaseSpacePosition, _h5_open, quantity_from_hdf5, quantity_to_hdf5
 from .hamiltonian import Hamiltonian, StaticFrame
 from .integrate import DOPRI853Integrator, LeapfrogIntegrator, get_integrator, parse_time_specification
 from .nbody import DirectNBody, bodies_to_device, integrate_systems, integrate_systems_leapfrog, pack_bodies
@@ -61,6 +61,28 @@ class MockStream(PhaseSpacePosition):
                                  f"input phase-space data, minus the component dimension. expected {n}, got "
                                  f"{len(lead_trail)}")
         self.lead_trail = lead_trail
+
+    # -- HDF5 (MockStream.to_hdf5 / from_hdf5, mockstream/core.py:106-150) -----
+    def _write_hdf5(self, f):
+        super()._write_hdf5(f)
+        if self.release_time is not None and len(self.release_time):
+            quantity_to_hdf5(f, "release_time", self.release_time, "Myr")
+        if self.lead_trail is not None:
+            f["lead_trail"] = np.asarray(self.lead_trail).astype("S1")
+
+    @classmethod
+    def from_hdf5(cls, f):
+        f, close = _h5_open(f, "r")
+        try:
+            obj = PhaseSpacePosition.from_hdf5(f)
+            t = quantity_from_hdf5(f["release_time"], "time") if "release_time" in f else None
+            lt = f["lead_trail"][()] if "lead_trail" in f else None
+        finally:
+            if close:
+                f.close()
+        if lt is not None:
+            lt = np.array([x.decode() if isinstance(x, bytes) else str(x) for x in np.ravel(lt)], dtype="U1")
+        return cls(pos=obj.pos, vel=obj.vel, frame=obj.frame, release_time=t, lead_trail=lt)
 
 
 class BaseStreamDF:

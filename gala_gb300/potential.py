@@ -385,9 +385,15 @@ class CCompositePotential(CompositePotential):
 
 class MilkyWayPotential(CCompositePotential):
     """gala's MilkyWayPotential (version v1, src/gala/potential/potential/builtin/special.py:98-124):
-    Miyamoto-Nagai disk + Hernquist bulge + Hernquist nucleus + spherical NFW halo."""
+    Miyamoto-Nagai disk + Hernquist bulge + Hernquist nucleus + spherical NFW halo.
 
-    def __init__(self, disk=None, halo=None, bulge=None, nucleus=None, units=None):
+    ``version`` is gala's selector (special.py:186-216); only "v1" is
+    implemented here (v2 needs the MN3 exponential disk)."""
+
+    def __init__(self, disk=None, halo=None, bulge=None, nucleus=None, units=None, version="v1"):
+        self.version = str(version).lower()
+        if self.version != "v1":
+            raise NotImplementedError(f"MilkyWayPotential version {version!r}: only 'v1' is implemented")
         super().__init__()
         disk = dict({"m": 6.8e10, "a": 3.0, "b": 0.28}, **(disk or {}))
         bulge = dict({"m": 5e9, "c": 1.0}, **(bulge or {}))

@@ -160,9 +160,31 @@ def make_stream_fixtures(ref: Oracle):
                         nbody_leapfrog=ref.leapfrog_nbody(c["pot"], *_lf_nbody_args()))
 
 
+def make_io_fixture():
+    """gala's own serialisation test inputs, kept as text: the potential YAML
+    files of tests/potential/potential/ (read by test_io.py) and one HDF5 file
+    written by libhdf5 (an EXP coefficient file read by test_exp.py), base64."""
+    import base64
+    import json
+
+    pdir = GALA_TESTS / "potential" / "potential"
+    data = {
+        "yaml": {n: (pdir / n).read_text() for n in ("Plummer.yml", "Composite.yml", "ccomposite.yml", "lm10.yml",
+                                                      "HarmonicOscillator1D.yml")},
+        "hdf5_base64": {n: base64.b64encode((pdir / n).read_bytes()).decode()
+                        for n in ("EXP-Hernquist-single-coefs.hdf5",)},
+    }
+    (OUT / "io_reference_files.json").write_text(json.dumps(data, indent=1) + "\n")
+
+
 if __name__ == "__main__":
-    # python tests/golden/make_golden.py [potentials integrators scf streams]
-    which = set(sys.argv[1:]) or {"potentials", "integrators", "scf", "streams"}
+    # python tests/golden/make_golden.py [potentials integrators scf streams io]
+    which = set(sys.argv[1:]) or {"potentials", "integrators", "scf", "streams", "io"}
+    if "io" in which and GALA_TESTS.exists():
+        make_io_fixture()
+    which.discard("io")
+    if not which:
+        sys.exit(0)
     build(ref=True)
     ref = Oracle("ref")
     if "potentials" in which:

@@ -192,3 +192,35 @@ def test_nbody_and_mockstream_argument_errors():
         gen.run_batch(np.ones((5, 3)), 1e5, dt=1.0, n_steps=4)
     with pytest.raises(ValueError, match="one progenitor potential"):
         gen.run_batch(np.ones((6, 3)), 1e5, progenitor_potentials=[None], dt=1.0, n_steps=4)
+
+
+def _int_entry_points():
+    return [n for n, (res, args) in _abi.SIGNATURES.items() if res is C.c_int and args]
+
+
+@pytest.mark.parametrize("variant", ["null_descriptor_negative_sizes", "null_buffers"])
+@pytest.mark.parametrize("name", _int_entry_points())
+def test_every_entry_point_rejects_bad_arguments_on_the_host(name, variant):
+    """Each C entry point validates its descriptor, sizes and pointers before
+    any CUDA call: NULL descriptors with negative sizes, or a valid descriptor
+    with positive sizes and NULL buffers, return GX_ERR_INVALID_ARGUMENT with
+    a message (no GPU is needed to see it)."""
+    lib = _abi.load()
+    _, args = _abi.SIGNATURES[name]
+    pk = g.HernquistPotential(m=1e11, c=1.0).packed()
+    frame = g.StaticFrame().c_frame()
+    vals = []
+    for a in args:
+        if a in (_abi._I64, _abi._I32):
+            vals.append(-1 if variant == "null_descriptor_negative_sizes" else 4)
+        elif a in (C.c_double, C.c_float):
+            vals.append(1e-3)
+        elif a is _abi._PP:
+            vals.append(None if variant == "null_descriptor_negative_sizes" else pk.for_host())
+        elif a is _abi._P:
+            vals.append(None)
+        else:  # the frame descriptor
+            vals.append(None if variant == "null_descriptor_negative_sizes" else C.byref(frame))
+    rc = getattr(lib, name)(*vals)
+    assert rc == _abi.GX_ERR_INVALID_ARGUMENT
+    assert lib.gx_last_error_message()

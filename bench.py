@@ -173,8 +173,11 @@ def cpu_reference_run(n_orbits, nsteps, target_s, steps, warmup):
     t0 = time.perf_counter()
     fast.dop853(mw, probe, t, atol=1e-12, rtol=1e-10, out_stride=100, nthreads=1)
     one = time.perf_counter() - t0
-    nb = int(max(nthreads, min(n_orbits // 100, round(target_s * nthreads / max(one, 1e-3)))))
+    # whole rounds of batches over the threads, at most the batches the workload has
+    nb = int(round(target_s * nthreads / max(one, 1e-3)))
     nb = max(nthreads, (nb // nthreads) * nthreads)
+    nb = max(1, min(nb, (n_orbits + 99) // 100))
+    nthreads = min(nthreads, nb)  # threads without a batch would idle
     sample = np.ascontiguousarray(w0_all[:, : nb * 100])
     times = []
     out = None
@@ -195,8 +198,8 @@ def cpu_reference_run(n_orbits, nsteps, target_s, steps, warmup):
         "seconds_per_step": per,
         "sample_orbits": int(sample.shape[1]),
         # gala itself runs one thread: the same restatement on one core, one batch
-        "single_thread": {"value": 100 * nsteps / one, "unit": UNIT, "cores": 1,
-                          "sample": f"one 100-orbit batch x {nsteps} steps, 1 thread"},
+        "single_thread": {"value": probe.shape[1] * nsteps / one, "unit": UNIT, "cores": 1,
+                          "sample": f"one {probe.shape[1]}-orbit batch x {nsteps} steps, 1 thread"},
     }, sample, out
 
 

@@ -1,0 +1,42 @@
+"""The benchmark's reference arm on a tiny workload (CPU only): one JSON line
+with the contract's keys, a cpu_baseline describing the run, zero transfer
+bytes; under torchrun only rank 0 works and prints."""
+import json
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+ARGS = ["--impl", "reference", "--steps", "3", "--warmup", "3", "--orbits", "250", "--nsteps", "120",
+        "--cpu-seconds", "0.2"]
+
+
+def _run(env_extra=None):
+    env = dict(os.environ, **(env_extra or {}))
+    return subprocess.run([sys.executable, str(ROOT / "bench.py"), *ARGS], cwd=ROOT, env=env, capture_output=True,
+                          text=True, timeout=600)
+
+
+def test_reference_arm_prints_one_contract_line():
+    r = _run()
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip().startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in d, key
+    assert d["impl"] == "reference" and d["steps"] == 3 and d["warmup"] == 3 and d["n_gpus"] == 1
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["unit"] == "orbit-steps/s"
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["unit"] == d["unit"]
+    # 250 orbits are three 100-orbit batches: at most three threads have work
+    assert 1 <= cb["cores"] <= 3 and "3 batches" in cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert d["config"]["workload"].startswith("mw_dop853")
+
+
+def test_reference_arm_other_ranks_exit_quietly():
+    r = _run({"RANK": "1", "LOCAL_RANK": "1", "WORLD_SIZE": "2"})
+    assert r.returncode == 0 and not r.stdout.strip()

@@ -16,7 +16,8 @@ those files use, with an interface shaped like h5py's:
   symbol-table nodes (SNOD) and a local heap of link names;
 * datasets with a version-1/2 dataspace (scalar or simple), a fill-value
   message and a version-3 layout message (contiguous or compact; chunked
-  layouts with an optional deflate filter are read);
+  layouts with deflate and shuffle filters are read as the specification
+  describes them, untested: no chunked file written by libhdf5 was at hand);
 * datatypes: IEEE floats, integers, fixed-length strings and variable-length
   strings (stored in global heap collections);
 * version-1 attribute messages (versions 2 and 3 are read too).
@@ -356,34 +357,36 @@ class _Reader:
         cdims = struct.unpack_from(f"<{rank}I", layout, 11)
         chunk = tuple(cdims[:-1])
         esize = cdims[-1]
-        deflate = False
+        pipeline = []  # filter ids in the order they were applied on writing
         if filters is not None:
             fver, nf = filters[0], filters[1]
             q = 8 if fver == 1 else 2
             for _ in range(nf):
                 fid = struct.unpack_from("<H", filters, q)[0]
-                if fver == 1 or fid >= 256:
-                    namelen = struct.unpack_from("<H", filters, q + 2)[0]
-                else:
-                    namelen = 0
-                fl, ncv = struct.unpack_from("<HH", filters, q + 4 if (fver == 1 or fid >= 256) else q + 2)
-                hdr = 8 if (fver == 1 or fid >= 256) else 6
-                q += hdr + (_pad8(namelen) if fver == 1 else namelen) + 4 * ncv
+                named = fver == 1 or fid >= 256
+                namelen = struct.unpack_from("<H", filters, q + 2)[0] if named else 0
+                _flags, ncv = struct.unpack_from("<HH", filters, q + 4 if named else q + 2)
+                q += (8 if named else 6) + (_pad8(namelen) if fver == 1 else namelen) + 4 * ncv
                 if fver == 1 and ncv % 2:
                     q += 4
-                if fid == 1:
-                    deflate = True
-                elif fid == 2:
-                    pass  # shuffle is undone below
-                else:
+                if fid not in (1, 2):  # deflate, shuffle
                     raise NotImplementedError(f"HDF5 filter {fid}")
+                pipeline.append(fid)
         out = np.zeros(int(np.prod(shape)) * esize, dtype=np.uint8).reshape(tuple(shape) + (esize,))
+        nchunk = int(np.prod(chunk))
         for offs, fmask, raw in self._chunks(btree, rank):
-            data = zlib.decompress(raw) if deflate and not (fmask & 1) else raw
-            arr = np.frombuffer(data, dtype=np.uint8)
-            if filters is not None and b"\x02\x00" in bytes(filters[:64]) and esize > 1:
-                arr = arr.reshape(esize, -1).T.copy().ravel()
-            arr = arr[:int(np.prod(chunk)) * esize].reshape(chunk + (esize,))
+            data = raw
+            # undo the filters in reverse; bit k of the mask marks filter k as skipped
+            for k in reversed(range(len(pipeline))):
+                if fmask & (1 << k):
+                    continue
+                if pipeline[k] == 1:
+                    data = zlib.decompress(data)
+                elif esize > 1:
+                    arr = np.frombuffer(data, dtype=np.uint8)
+                    body = arr[:nchunk * esize].reshape(esize, nchunk).T.ravel()
+                    data = body.tobytes() + arr[nchunk * esize:].tobytes()
+            arr = np.frombuffer(data, dtype=np.uint8)[:nchunk * esize].reshape(chunk + (esize,))
             sl = tuple(slice(o, min(o + c, s)) for o, c, s in zip(offs, chunk, shape))
             out[sl] = arr[tuple(slice(0, s.stop - s.start) for s in sl)]
         return out.tobytes()

@@ -119,12 +119,28 @@ def _flow(text: str):
     return _scalar(s)
 
 
+def _strip_comment(line: str) -> str:
+    """The line without a trailing comment (a '#' at the start or after a space,
+    outside quotes)."""
+    quote = None
+    for i, ch in enumerate(line):
+        if quote:
+            if ch == quote:
+                quote = None
+        elif ch in "\"'":
+            quote = ch
+        elif ch == "#" and (i == 0 or line[i - 1] in " \t"):
+            return line[:i].rstrip()
+    return line
+
+
 def _lines(text: str):
     """(indent, content) of each meaningful line; flow collections that span
     lines are joined onto their first line."""
     out = []
     pending = None
     for raw in text.splitlines():
+        raw = _strip_comment(raw)
         stripped = raw.strip()
         if pending is not None:
             pending[1] += " " + stripped

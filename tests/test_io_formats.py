@@ -249,3 +249,42 @@ def test_orbit_and_stream_files_in_galas_layout(tmp_path):
     p = g.PhaseSpacePosition(pos=w[:3, 0], vel=w[3:, 0])
     p.to_hdf5(tmp_path / "p.h5")
     assert g.PhaseSpacePosition.from_hdf5(tmp_path / "p.h5").frame is None
+
+
+def test_yaml_subset_edge_cases():
+    text = """# hand-written file
+class: HernquistPotential   # trailing comment
+parameters:
+  m: 5.0e9
+  c: 1.
+  note: "a # inside \\"quotes\\""
+  other: 'it''s'
+  tag: x#y
+  arr: [[1.0, 2.0],   # rows may wrap
+        [3.0, -4.5e-3]]
+  empty: {}
+  none: []
+  flag: true
+  nothing: null
+list:
+- 1
+- two
+- key: v
+  deeper:
+    - 3
+"""
+    d = pio.yaml_load(text)
+    assert d["class"] == "HernquistPotential"
+    p = d["parameters"]
+    assert p["m"] == 5e9 and p["c"] == 1.0 and p["note"] == 'a # inside "quotes"' and p["other"] == "it's"
+    assert p["tag"] == "x#y" and p["arr"] == [[1.0, 2.0], [3.0, -4.5e-3]]
+    assert p["empty"] == {} and p["none"] == [] and p["flag"] is True and p["nothing"] is None
+    assert d["list"] == [1, "two", {"key": "v", "deeper": [3]}]
+    assert pio.yaml_load(pio.yaml_dump(d)) == d
+    # numbers that must stay numbers, strings that must stay strings
+    vals = {"a": 1e-5, "b": 1e20, "c": -0.0, "d": "1.5", "e": "true", "f": "", "g": "km / s", "h": 7}
+    back = pio.yaml_load(pio.yaml_dump(vals))
+    assert back == vals and isinstance(back["d"], str) and isinstance(back["h"], int)
+    assert "1.0e-05" in pio.yaml_dump({"a": 1e-5})   # YAML 1.1 needs the dot before the exponent
+    with pytest.raises(ValueError, match="tag"):
+        pio.yaml_load("a: !!python/object:foo.Bar {}\n")

@@ -86,6 +86,114 @@ def _frame_from_hdf5(f):
     raise ValueError(f"frame class {cls!r} is not available in gala_gb300")
 
 
+# -- guiding radius and periods (src/gala/dynamics/orbit.py:555-599, 683-727) --
+_D_DR_STEP = 1e-4  # c_d_dr's fixed step (cpotential.cpp:327)
+
+
+def _d_dr_midplane(energy, R, t):
+    """dPhi/dr at (R, 0, 0) as c_d_dr forms it (cpotential.cpp:317-343): the
+    central difference (Phi(R + h) - Phi(R - h)) / (2 h), h = 1e-4; every R in
+    one call of energy(q (3, 2n), t)."""
+    R = np.asarray(R, dtype=np.float64)
+    n = R.size
+    q = np.zeros((3, 2 * n))
+    q[0, :n] = R + _D_DR_STEP
+    q[0, n:] = R - _D_DR_STEP
+    phi = np.asarray(energy(q, t), dtype=np.float64)
+    return (phi[:n] - phi[n:]) / (2.0 * _D_DR_STEP)
+
+
+def _guiding_radius_solve(R0, Lz, dphi_dr, max_expand=60, max_iter=200):
+    """Root R > 0 of |Lz| - R sqrt(R |dPhi/dR(R)|) for every orbit at once
+    (the function of _guiding_radius_rootfunc, src/gala/dynamics/core.py:943-948).
+
+    The root is bracketed by doubling / halving from R0, then found by the
+    Illinois form of regula falsi until the bracket stops shrinking; each step
+    evaluates dphi_dr (one call for all orbits).  |Lz| = 0 gives R = 0; an orbit
+    whose root cannot be bracketed gives nan, as gala's failed roots do."""
+    R0 = np.atleast_1d(np.asarray(R0, dtype=np.float64))
+    L = np.abs(np.atleast_1d(np.asarray(Lz, dtype=np.float64)))
+    out = np.full(R0.shape, np.nan)
+    live = np.isfinite(R0) & (R0 > 0) & np.isfinite(L)
+    zero = live & (L == 0)
+    out[zero] = 0.0
+    live &= ~zero
+
+    def f(R):
+        Rs = np.where(live, R, 1.0)  # placeholders keep the batched call finite
+        return L - Rs * np.sqrt(Rs * np.abs(dphi_dr(Rs)))
+
+    fr = f(R0)
+    out[live & (fr == 0)] = R0[live & (fr == 0)]
+    live &= fr != 0
+    a, fa = R0.copy(), fr.copy()   # side with f > 0 (R too small)
+    b, fb = R0.copy(), fr.copy()   # side with f < 0 (R too large)
+    need_hi = live & (fr > 0)
+    need_lo = live & (fr < 0)
+    for _ in range(max_expand):
+        if not (need_hi.any() or need_lo.any()):
+            break
+        trial = np.where(need_hi, b * 2.0, np.where(need_lo, a * 0.5, b))
+        ft = f(trial)
+        hi_done = need_hi & (ft <= 0)
+        b = np.where(need_hi, trial, b)
+        fb = np.where(need_hi, ft, fb)
+        a = np.where(need_hi & ~hi_done, trial, a)
+        fa = np.where(need_hi & ~hi_done, ft, fa)
+        lo_done = need_lo & (ft >= 0)
+        a = np.where(need_lo, trial, a)
+        fa = np.where(need_lo, ft, fa)
+        b = np.where(need_lo & ~lo_done, trial, b)
+        fb = np.where(need_lo & ~lo_done, ft, fb)
+        need_hi &= ~hi_done
+        need_lo &= ~lo_done
+    live &= ~(need_hi | need_lo)       # never bracketed: nan
+    exact = live & ((fa == 0) | (fb == 0))
+    out[exact] = np.where(fa[exact] == 0, a[exact], b[exact])
+    live &= ~exact
+    side = np.zeros(R0.shape, dtype=np.int8)  # Illinois: which end was kept last
+    for _ in range(max_iter):
+        if not live.any():
+            break
+        with np.errstate(divide="ignore", invalid="ignore"):
+            x = b - fb * (b - a) / (fb - fa)
+        x = np.where(live & (x > np.minimum(a, b)) & (x < np.maximum(a, b)), x, 0.5 * (a + b))
+        fx = f(x)
+        done = live & ((fx == 0) | (np.abs(b - a) <= 4.0 * np.finfo(float).eps * np.abs(x)))
+        out[done] = x[done]
+        live &= ~done
+        pos = live & (fx > 0)
+        neg = live & (fx < 0)
+        a = np.where(pos, x, a)
+        b = np.where(neg, x, b)
+        fb = np.where(pos & (side == 1), 0.5 * fb, fb)
+        fa = np.where(neg & (side == -1), 0.5 * fa, fa)
+        fa = np.where(pos, fx, fa)
+        fb = np.where(neg, fx, fb)
+        side = np.where(pos, 1, np.where(neg, -1, side)).astype(np.int8)
+    out[live] = 0.5 * (a[live] + b[live])
+    return out
+
+
+def peak_to_peak_period(t, f, amplitude_threshold=1e-2):
+    """Period of a time series from its interior peaks and troughs
+    (peak_to_peak_period, src/gala/dynamics/util.py:14-69): the mean spacing
+    of the strict local maxima and of the strict local minima (the two ends
+    excluded), averaged; nan when the mean peak minus the mean trough is
+    below amplitude_threshold."""
+    t = np.asarray(t, dtype=np.float64)
+    f = np.asarray(f, dtype=np.float64)
+    mid = f[1:-1]
+    peaks = np.nonzero((mid > f[:-2]) & (mid > f[2:]))[0] + 1
+    troughs = np.nonzero((mid < f[:-2]) & (mid < f[2:]))[0] + 1
+    # gala's result is nan whenever either set has fewer than two members
+    if len(peaks) < 2 or len(troughs) < 2:
+        return np.nan
+    if abs(np.mean(f[peaks]) - np.mean(f[troughs])) < amplitude_threshold:
+        return np.nan
+    return np.mean([np.mean(np.diff(t[peaks])), np.mean(np.diff(t[troughs]))])
+
+
 class PhaseSpacePosition:
     """Positions and velocities with gala's axis convention: (ndim, ...)."""
 
@@ -127,6 +235,11 @@ class PhaseSpacePosition:
 
     def kinetic_energy(self):
         return 0.5 * np.sum(self.vel ** 2, axis=0)
+
+    def angular_momentum(self):
+        """L = x cross v, shape (3, ...) (PhaseSpacePosition.angular_momentum,
+        src/gala/dynamics/core.py)."""
+        return np.cross(self.pos, self.vel, axis=0)
 
     def potential_energy(self, potential):
         return potential.energy(self.pos)
@@ -243,6 +356,54 @@ class Orbit(PhaseSpacePosition):
         if not isinstance(H, Hamiltonian):
             H = Hamiltonian(H)
         return H.energy(self.w())
+
+    def guiding_radius(self, potential=None, t=0.0, **root_kwargs):
+        """Guiding-center radius R_g of each orbit: R_g v_c(R_g) = |<L_z>| with
+        v_c from dPhi/dR in the midplane (Orbit.guiding_radius, orbit.py:555-599).
+
+        The potential is evaluated on the GPU, all orbits in each call.  Each orbit
+        starts from its own time-averaged cylindrical radius (gala averages over
+        all orbits, so only single orbits work there) and the root is solved to
+        full precision (``root_kwargs``, gala's options for scipy's root, are
+        accepted and not needed).  Orbits whose L_z varies by more than 1e-8
+        relative get gala's RuntimeWarning about axisymmetry.
+        """
+        import warnings
+
+        if potential is None:
+            potential = self.potential
+        if potential is None:
+            raise ValueError("You must specify a potential if it is not already defined on the orbit")
+        x, y = self.pos[0], self.pos[1]
+        R0 = np.atleast_1d(np.mean(np.hypot(x, y), axis=0))
+        Lzs = self.angular_momentum()[2]
+        mean_Lz = np.atleast_1d(np.mean(Lzs, axis=0))
+        with np.errstate(divide="ignore", invalid="ignore"):
+            check = np.abs(np.atleast_1d(np.std(Lzs, axis=0)) / mean_Lz) > 1e-8
+        if np.any(check):
+            warnings.warn(
+                f"{check.sum()} orbits do not have constant Lz (see orbits at indices: "
+                f"{list(np.where(check)[0][:10])}, ...). Are you sure you are using an axisymmetric potential?",
+                RuntimeWarning)
+        Rg = _guiding_radius_solve(R0, mean_Lz, lambda R: _d_dr_midplane(potential.energy, R, t))
+        return Rg.reshape(self.pos.shape[2:]) if self.pos.ndim > 2 else Rg[0]
+
+    def estimate_period(self):
+        """Period of each Cartesian coordinate of each orbit from its peaks and
+        troughs (Orbit.estimate_period, orbit.py:683-727): a dict of arrays of
+        shape (norbits,) keyed 'x', 'y', 'z' (gala returns a table with these
+        columns)."""
+        if self.t is None:
+            raise ValueError("To compute the period, a time array is needed. Specify a time array when creating "
+                             "this object.")
+        periods = {}
+        for k, name in enumerate("xyz"):
+            q = self.pos[k]
+            if q.ndim == 1:
+                periods[name] = np.atleast_1d(peak_to_peak_period(self.t, q))
+            else:
+                periods[name] = np.array([peak_to_peak_period(self.t, q[:, n]) for n in range(q.shape[1])])
+        return periods
 
     # -- HDF5 (Orbit.to_hdf5 / from_hdf5, src/gala/dynamics/orbit.py:236-323) --
     def _write_hdf5(self, f):

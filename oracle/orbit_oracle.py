@@ -10,6 +10,11 @@ degree 2 through the three samples around it, vertex at -c1 / (2 c2) -- and
 running backwards is reversed first, as gala does.  The spherical radius is
 astropy's (hypot(hypot(x, y), z), PhysicsSphericalRepresentation.from_cartesian),
 the cylindrical z is z.
+
+Also restated: ``guiding_radius`` (orbit.py:555-599 with core.py:943-967 and
+c_d_dr, cpotential.cpp:317-343) through scipy.optimize.root as gala calls it,
+and ``peak_to_peak_period`` (src/gala/dynamics/util.py:14-69) with argrelmax /
+argrelmin, behind ``Orbit.estimate_period`` (orbit.py:683-727).
 """
 from __future__ import annotations
 
@@ -74,3 +79,63 @@ def eccentricity(w, t, approximate=False):
     ra = reduce(w, t, "apo", approximate=approximate)
     rp = reduce(w, t, "peri", approximate=approximate)
     return (ra - rp) / (ra + rp)
+
+
+def d_dr(energy, R, t=0.0):
+    """c_d_dr (src/gala/potential/potential/src/cpotential.cpp:317-343) at (R, 0, 0):
+    (Phi(q + h q/r) - Phi(q - h q/r)) / (2 h) with h = 1e-4."""
+    R = np.atleast_1d(np.asarray(R, dtype=np.float64))
+    h = 1e-4
+    z = np.zeros_like(R)
+    plus = energy(np.stack([R + h * (R / R), z, z]), t)
+    minus = energy(np.stack([R - h * (R / R), z, z]), t)
+    return (plus - minus) / (2.0 * h)
+
+
+def guiding_radius(w, energy, t=0.0, **root_kwargs):
+    """Orbit.guiding_radius (orbit.py:555-599) with _guiding_radius_helper and
+    _guiding_radius_rootfunc (src/gala/dynamics/core.py:943-967): for each orbit,
+    scipy.optimize.root (method 'hybr', xtol 1e-5 by default) on
+    |Lz| - R sqrt(R |dPhi/dR|) from the mean cylindrical radius, nan where root
+    reports failure.  Each orbit starts from its own mean radius (gala takes the
+    mean over all orbits, which only works for one orbit).  w: (6, ntimes[, N]);
+    energy(q (3, n), t) -> (n,)."""
+    from scipy.optimize import root
+
+    root_kwargs.setdefault("options", {"xtol": 1e-5})
+    root_kwargs.setdefault("method", "hybr")
+    w = np.asarray(w, dtype=np.float64)
+    w2 = w if w.ndim == 3 else w[..., None]
+    out = np.zeros(w2.shape[2])
+    for i in range(w2.shape[2]):
+        x, y, _, vx, vy, _ = w2[:, :, i]
+        R0 = np.mean(np.hypot(x, y))
+        Lz = np.mean(x * vy - y * vx)
+
+        def rootfunc(R, Lz):
+            dphi = d_dr(energy, R[0], t)
+            return Lz - R * np.sqrt(R * np.abs(dphi))
+
+        res = root(rootfunc, R0, args=(np.abs(Lz),), **root_kwargs)
+        out[i] = res.x[0] if res.success else np.nan
+    return out if w.ndim == 3 else out[0]
+
+
+def peak_to_peak_period(t, f, amplitude_threshold=1e-2):
+    """peak_to_peak_period (src/gala/dynamics/util.py:14-69): mean spacing of the
+    interior maxima and of the interior minima (argrelmax / argrelmin with
+    mode 'wrap', ends removed), averaged; nan when the mean peak-to-trough
+    amplitude is below the threshold."""
+    from scipy.signal import argrelmin
+
+    t = np.asarray(t, dtype=np.float64)
+    f = np.asarray(f, dtype=np.float64)
+    max_ix = argrelmax(f, mode="wrap")[0]
+    max_ix = max_ix[(max_ix != 0) & (max_ix != (len(f) - 1))]
+    min_ix = argrelmin(f, mode="wrap")[0]
+    min_ix = min_ix[(min_ix != 0) & (min_ix != (len(f) - 1))]
+    if abs(np.mean(f[max_ix]) - np.mean(f[min_ix])) < amplitude_threshold:
+        return np.nan
+    T_max = np.mean(t[max_ix[1:]] - t[max_ix[:-1]]) if len(max_ix) > 0 else np.nan
+    T_min = np.mean(t[min_ix[1:]] - t[min_ix[:-1]]) if len(min_ix) > 0 else np.nan
+    return np.mean([T_max, T_min])

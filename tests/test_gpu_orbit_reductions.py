@@ -117,3 +117,22 @@ def test_planar_and_smooth_orbits_ragged_sizes():
     _check_all(g.Orbit(pos=pos, vel=np.zeros_like(pos), t=t))
     z = g.Orbit(pos=pos, vel=np.zeros_like(pos), t=t).zmax()
     assert np.all(np.isnan(z[::3])) and not np.any(np.isnan(np.delete(z, np.s_[::3])))
+
+
+def test_guiding_radius_and_periods_match_oracle(oracle):
+    """Orbit.guiding_radius evaluates the potential on the GPU (one call per
+    solver step for all orbits) and must agree with gala's scipy 'hybr' solve on
+    the oracle's potential to 1e-7.  The central difference of step 1e-4 in
+    c_d_dr amplifies a relative difference of the two potentials about 1e6-fold
+    in R_g (2e-15 of noise gives 2e-9); the potential tests bound that
+    difference by 1e-14, so 1e-7 keeps a tenfold margin.  estimate_period runs
+    gala's peak-to-peak estimate on the orbit."""
+    orbit = _mw_orbits(n=32, dt=1.0, n_steps=3000)
+    w, t = orbit.w(), orbit.t
+    mw = orbit.potential
+    Rg = orbit.guiding_radius()
+    ref = OO.guiding_radius(w, lambda q, tt: oracle.energy(mw, q, tt))
+    np.testing.assert_allclose(Rg, ref, rtol=1e-7)
+    P = orbit.estimate_period()
+    for k, name in enumerate("xyz"):
+        np.testing.assert_array_equal(P[name], [OO.peak_to_peak_period(t, w[k, :, n]) for n in range(32)])

@@ -288,3 +288,64 @@ list:
     assert "1.0e-05" in pio.yaml_dump({"a": 1e-5})   # YAML 1.1 needs the dot before the exponent
     with pytest.raises(ValueError, match="tag"):
         pio.yaml_load("a: !!python/object:foo.Bar {}\n")
+
+
+def test_hdf5_random_trees_round_trip(tmp_path):
+    """Seeded random trees: nested groups, unicode names, every supported type,
+    attributes everywhere, strings longer than a 4 KB heap collection, more
+    strings than one collection holds, and groups near the 256-link limit."""
+    rng = np.random.default_rng(11)
+    alphabet = list("abcdefghijklmnopqrstuvwxyz_0123456789") + ["é", "ß", "λ"]
+
+    def name():
+        return "".join(rng.choice(alphabet, size=int(rng.integers(1, 24))))
+
+    def value():
+        kind = int(rng.integers(0, 7))
+        shape = tuple(int(s) for s in rng.integers(0, 5, size=int(rng.integers(0, 4))))
+        if kind == 0:
+            return rng.normal(size=shape)
+        if kind == 1:
+            return rng.integers(-2**40, 2**40, size=shape)
+        if kind == 2:
+            return rng.normal(size=shape).astype(np.float32)
+        if kind == 3:
+            return "".join(rng.choice(alphabet, size=int(rng.integers(0, 6000))))
+        if kind == 4:
+            return ("".join(rng.choice(alphabet[:37], size=int(rng.integers(0, 50))))).encode()
+        if kind == 5:
+            return [name() for _ in range(int(rng.integers(1, 400)))]
+        return np.array([name().encode()[:3] for _ in range(int(rng.integers(1, 9)))], dtype="S3")
+
+    expect = {}
+
+    def fill(group, path, depth):
+        for _ in range(int(rng.integers(1, 12 if depth else 250))):
+            nm = name()
+            if nm in group:
+                continue
+            if depth < 3 and rng.random() < 0.25:
+                sub = group.create_group(nm)
+                sub.attrs[name()] = rng.normal()
+                fill(sub, f"{path}/{nm}", depth + 1)
+            else:
+                v = value()
+                group[nm] = v
+                an = name()
+                group[nm].attrs[an] = name()
+                expect[f"{path}/{nm}"] = (v, an, group[nm].attrs[an])
+
+    fn = tmp_path / "random.h5"
+    with hdf5.File(fn, "w") as f:
+        fill(f, "", 0)
+    r = hdf5.File(fn, "r")
+    assert len(expect) > 150
+    for path, (v, an, av) in expect.items():
+        got = r[path][()]
+        if isinstance(v, list):
+            assert list(got) == v, path
+        elif isinstance(v, (str, bytes)):
+            assert got == v, path
+        else:
+            assert np.array_equal(got, v) and np.asarray(got).dtype == np.asarray(v).dtype, path
+        assert r[path].attrs[an] == av

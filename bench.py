@@ -47,6 +47,18 @@ F_DENSE_PER_ORBIT = 6 * 153       # dense-output coefficients and the 3 extra st
 F_OUTPUT_PER_ORBIT = 6 * 14 + 2   # one contd8 evaluation of 6 components
 
 
+def measured_peak(key, fallback):
+    """(value, source) of a MEASURED_PEAKS.json entry; without the file or the
+    key, the fallback figure (an earlier measurement on a GB300) and 'fallback'."""
+    try:
+        v = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())[key]
+        if isinstance(v, (int, float)) and v > 0:
+            return float(v), "measured (MEASURED_PEAKS.json)"
+    except (OSError, ValueError, KeyError, TypeError):
+        pass
+    return float(fallback), "fallback"
+
+
 def parse_args():
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument("--gpus", type=int, default=1)
@@ -349,10 +361,7 @@ def run_scf_surrogate(args, torch, stream):
     sp.split = 2
     v_sur = n_orbits * n_steps / (ms_sur * 1e-3)
     flops_run = float(n_orbits * (n_steps + 1)) * 6 * 2 * 2 * 256 * 256
-    try:
-        bf16_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops_sustained"])
-    except Exception:
-        bf16_peak = 1700.0
+    bf16_peak, bf16_src = measured_peak("bf16_tflops_sustained", 1700.0)
     v_f32 = n32 * 200 / (ms_f32 * 1e-3)
     v_f64 = n_orbits * 20 / (ms_f64 * 1e-3)
     sub = w0[:, :min(2048, n_orbits)]
@@ -379,6 +388,7 @@ def run_scf_surrogate(args, torch, stream):
                            "roofline": {"bound": "tensor", "unit": "TFLOP/s",
                                         "achieved": flops_run / (ms_sur * 1e-3) / 1e12,
                                         "peak": bf16_peak, "frac": flops_run / (ms_sur * 1e-3) / 1e12 / bf16_peak,
+                                        "peak_source": f"{bf16_src}, cuBLAS BF16 sustained",
                                         "work": "executed BF16 MMA flops (6 GEMMs x 2 parts x 2 x 128 x 256 x 256 "
                                                 "per 128-position tile and step)"}},
         "fp32_surrogate_bf16_activations": {"value": n_orbits * n_steps / (ms_s1 * 1e-3), "unit": UNIT,
@@ -637,22 +647,14 @@ def run_orbit_reductions(args, torch, stream):
         times.append(e0.elapsed_time(e1))
     ms = float(np.median(times))
     algo_bytes = 3 * nt * n * 8 + nt * 8 + 3 * n * (4 + 3 * 8)
-    peaks = {}
-    try:
-        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
-    except Exception:
-        pass
-    hbm = None
-    for k in ("hbm_gbs", "hbm_GBps", "hbm"):
-        if isinstance(peaks.get(k), (int, float)):
-            hbm = float(peaks[k])
-    hbm = hbm or 6791.0
+    hbm, hbm_src = measured_peak("hbm_gbs", 6800.0)
     res = {
         "workload": f"orbit_reductions: {n} MW-composite orbits x {nt} Leapfrog snapshots, peri/apo/zmax "
                     "statistics in one pass",
         "value": n * nt / (ms * 1e-3), "unit": "orbit-snapshots/s", "ms": ms,
         "roofline": {"bound": "hbm", "achieved": algo_bytes / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
-                     "frac": algo_bytes / (ms * 1e-3) / 1e9 / hbm, "bytes_per_launch": algo_bytes},
+                     "frac": algo_bytes / (ms * 1e-3) / 1e9 / hbm, "bytes_per_launch": algo_bytes,
+                     "peak_source": hbm_src},
         "extrema_per_orbit_mean": {"peri": float(count[0].float().mean()), "apo": float(count[1].float().mean()),
                                    "zmax": float(count[2].float().mean())},
     }

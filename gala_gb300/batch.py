@@ -229,5 +229,8 @@ class BatchIntegrator:
             except (FileNotFoundError, ValueError):
                 data = {}
             data[self._cache_key()] = best
-            CACHE.write_text(json.dumps(data, indent=1))
+            # write-then-rename: ranks tuning at once never leave a torn file
+            tmp = CACHE.with_name(f"{CACHE.name}.{os.getpid()}.tmp")
+            tmp.write_text(json.dumps(data, indent=1))
+            os.replace(tmp, CACHE)
         return best

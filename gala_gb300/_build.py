@@ -57,10 +57,27 @@ def _sources_newer(target: Path) -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile every CUDA translation unit and link the shared library."""
+    """Compile every CUDA translation unit and link the shared library.
+
+    Processes that build at once (ranks of one job, parallel test workers)
+    take turns on a lock file; a process that waited finds the library fresh
+    and returns."""
+    import fcntl
+
     if not force and not _sources_newer(LIB):
         return LIB
     OUT.mkdir(exist_ok=True)
+    with open(OUT / ".build.lock", "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            if not force and not _sources_newer(LIB):
+                return LIB
+            return _build_locked(verbose)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build_locked(verbose: bool) -> Path:
     cc = nvcc()
 
     def compile_unit(item):
@@ -78,7 +95,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
 
     with ThreadPoolExecutor(max_workers=min(len(UNITS), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_unit, UNITS.items()))
-    tmp = OUT / "libgala_gb300.so.tmp"
+    tmp = OUT / f"libgala_gb300.so.{os.getpid()}.tmp"
     cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -19,10 +19,19 @@ _P = C.c_void_p
 
 
 def build(ref: bool = True) -> None:
-    """Build the restatement (always) and gala's own objects (when its sources exist)."""
-    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
-    if ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+    """Build the restatement (always) and gala's own objects (when its sources
+    exist); processes building at once take turns on a lock file."""
+    import fcntl
+
+    (HERE / "_build").mkdir(exist_ok=True)
+    with open(HERE / "_build" / ".build.lock", "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+            if ref:
+                subprocess.run(["make", "-s", "-C", str(HERE), "ref"], check=True)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
 
 
 def ref_available() -> bool:

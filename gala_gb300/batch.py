@@ -19,6 +19,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _abi
+from ._trace import traced
 
 LEAPFROG, RUTH4 = 0, 1
 COST = {LEAPFROG: 1.0, RUTH4: 3.0}   # gradient evaluations per step
@@ -144,6 +145,7 @@ class BatchIntegrator:
         _abi.call("gx_hamiltonian_value", desc, C.byref(frame), 0.0, ptr(self.w_out), self.n, ptr(self.E1),
                   stream_handle)
 
+    @traced("batch_run")
     def run(self):
         """Integrate every orbit once (eager launch sequence)."""
         from ._device import stream_handle

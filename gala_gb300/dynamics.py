@@ -7,6 +7,8 @@ from __future__ import annotations
 
 import numpy as np
 
+from ._trace import traced
+
 __all__ = ["PhaseSpacePosition", "Orbit"]
 
 
@@ -470,6 +472,7 @@ class Orbit(PhaseSpacePosition):
             wd = wd[:, :, None]
         return wd.contiguous(), torch.from_numpy(np.ascontiguousarray(self.t, dtype=np.float64)).to(dev)
 
+    @traced("orbit_extrema")
     def _extrema_run(self, approximate, keep):
         import torch
 

@@ -19,6 +19,7 @@ from .dynamics import Orbit, PhaseSpacePosition
 from .integrate import (DOPRI853Integrator, LeapfrogIntegrator, Ruth4Integrator, get_integrator,
                         parse_time_specification)
 from .potential import PotentialBase
+from ._trace import traced
 
 __all__ = ["StaticFrame", "ConstantRotatingFrame", "Hamiltonian"]
 
@@ -92,6 +93,7 @@ class Hamiltonian:
             raise ValueError(f"Invalid phase-space shape {w.shape}: expected (6, ...)")
         return w
 
+    @traced("hamiltonian_energy")
     def energy(self, w, t=0.0):
         """Value of the Hamiltonian (chamiltonian.pyx:107-128) at w of shape (6, ...)."""
         import torch
@@ -107,6 +109,7 @@ class Hamiltonian:
                   ptr(wd), n, ptr(out), stream_handle())
         return out.cpu().numpy().reshape(shape[1:])
 
+    @traced("hamiltonian_gradient")
     def gradient(self, w, t=0.0):
         """(qdot, pdot) at w (hamiltonian_gradient_T, chamiltonian.cpp:38-57); note gala's
         Hamiltonian.gradient returns dH/dw with the momentum half negated (:88-99)."""
@@ -124,6 +127,7 @@ class Hamiltonian:
         return out.cpu().numpy().reshape(shape)
 
     # --- integration ---------------------------------------------------------
+    @traced("integrate_orbit")
     def integrate_orbit(self, w0, Integrator=None, Integrator_kwargs=dict(), cython_if_possible=True,
                         save_all=True, return_device=False, stream=None, **time_spec):
         """Integrate orbits from w0 (shape (6,) or (6, N)) and return an Orbit.

@@ -35,6 +35,7 @@ from .hamiltonian import Hamiltonian, StaticFrame
 from .integrate import DOPRI853Integrator, LeapfrogIntegrator, get_integrator, parse_time_specification
 from .nbody import DirectNBody, bodies_to_device, integrate_systems, integrate_systems_leapfrog, pack_bodies
 from .potential import PotentialBase
+from ._trace import traced
 
 __all__ = ["MockStream", "BaseStreamDF", "FardalStreamDF", "StreaklineStreamDF", "LagrangeCloudStreamDF",
            "ChenStreamDF", "MockStreamGenerator", "MockStreamBatch"]
@@ -493,6 +494,7 @@ class MockStreamGenerator:
             raise RuntimeError(f"release systems rejected: {int(np.sum(res < 0))}")
         return MockStreamBatch(stream_out, nbody_out, release_time, lead_trail, status, None, H.frame, orbit_t)
 
+    @traced("mockstream_run")
     def run(self, prog_w0, prog_mass, nbody=None, release_every=1, n_particles=1, output_every=None,
             output_filename=None, check_filesize=True, overwrite=False, progress=False, Integrator=None,
             Integrator_kwargs=None, **time_spec):
@@ -521,6 +523,7 @@ class MockStreamGenerator:
                              precision=precision)
         return res.stream(0), res.nbody(0)
 
+    @traced("mockstream_run_batch")
     def run_batch(self, prog_w0, prog_mass, progenitor_potentials=None, release_every=1, n_particles=1,
                   Integrator=None, Integrator_kwargs=None, return_stats=False, stream=None, **time_spec):
         """Many independent streams on one time grid (no extra bodies).

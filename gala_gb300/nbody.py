@@ -22,6 +22,7 @@ from .dynamics import Orbit, PhaseSpacePosition
 from .hamiltonian import Hamiltonian, StaticFrame
 from .integrate import DOPRI853Integrator, LeapfrogIntegrator, get_integrator, parse_time_specification
 from .potential import NullPotential, PotentialBase
+from ._trace import traced
 
 __all__ = ["DirectNBody", "BODY_DTYPE", "body_record", "pack_bodies", "integrate_systems",
            "integrate_systems_leapfrog"]
@@ -206,6 +207,7 @@ class DirectNBody:
         end = [i for i, p in enumerate(self.particle_potentials) if is_null(p)]
         return np.array(front + end, dtype=np.int64), len(front)
 
+    @traced("nbody_integrate_orbit")
     def integrate_orbit(self, Integrator=None, Integrator_kwargs=None, return_device=False, **time_spec):
         """Integrate the bodies; returns an Orbit of shape (3, ntimes, nbodies) if
         save_all, else a PhaseSpacePosition (3, nbodies) (core.py:166-280)."""

@@ -19,6 +19,7 @@ import numpy as np
 from . import _abi
 from .units import G as G_GALACTIC
 from .units import galactic
+from ._trace import traced
 
 __all__ = [
     "PotentialBase",
@@ -165,6 +166,7 @@ class PotentialBase:
         return True
 
     # --- evaluation (GPU) ----------------------------------------------------
+    @traced("potential_eval")
     def _eval(self, kind, q, t=0.0):
         import torch
 

@@ -28,6 +28,7 @@ import math
 import numpy as np
 
 from . import _abi
+from ._trace import traced
 from .units import G as G_GALACTIC
 
 H = 256
@@ -182,6 +183,7 @@ class SurrogatePotential:
         return self.X.shape[0]
 
     # ------------------------------------------------------------ training
+    @traced("surrogate_train")
     def train(self, steps=6000, batch=8192, lr=1e-3, lr_min=1e-5, beta=4.0, seed=2, log_every=500,
               qat_fraction=0.3):
         """Adam with cosine learning-rate decay on minibatches of the dataset.
@@ -257,6 +259,7 @@ class SurrogatePotential:
         sms = torch.cuda.get_device_properties(self.dev).multi_processor_count
         return int(max(1, min(sms, (n + tile - 1) // tile)))
 
+    @traced("surrogate_gradient")
     def gradient_and_energy(self, q, engine=None):
         """grad Phi (3, N) and Phi (N) at positions q (3, N), on the tensor cores:
         engine "tcgen05" (default) or "mma" (warp-level mma.sync)."""
@@ -288,6 +291,7 @@ class SurrogatePotential:
         if int(status.item()) != 0:
             raise _abi.GxError("the tensor-core surrogate kernel ran out of a bounded wait (results incomplete)")
 
+    @traced("surrogate_leapfrog")
     def integrate_leapfrog(self, w0, dt, n_steps, grid=None, analytic=False, engine=None):
         """FP32 leapfrog of every orbit in w0 (6, N) in the surrogate potential;
         returns the final states (6, N) and the number of fallback force calls.

@@ -224,3 +224,26 @@ def test_every_entry_point_rejects_bad_arguments_on_the_host(name, variant):
     rc = getattr(lib, name)(*vals)
     assert rc == _abi.GX_ERR_INVALID_ARGUMENT
     assert lib.gx_last_error_message()
+
+
+def test_public_calls_open_nvtx_ranges(monkeypatch):
+    """Each public GPU call runs inside an NVTX range named gala_gb300.<call>
+    (the range opens before any argument check, so a failing call shows too)."""
+    import contextlib
+
+    import torch
+
+    seen = []
+
+    @contextlib.contextmanager
+    def fake_range(name):
+        seen.append(name)
+        yield
+
+    monkeypatch.setattr(torch.cuda.nvtx, "range", fake_range)
+    pot = g.HernquistPotential(m=1e11, c=1.0)
+    with pytest.raises(ValueError):
+        pot.integrate_orbit(np.ones((5, 2)), dt=1.0, n_steps=4)
+    with pytest.raises(ValueError):
+        pot.energy(np.ones((2, 2)))
+    assert seen == ["gala_gb300.integrate_orbit", "gala_gb300.potential_eval"]

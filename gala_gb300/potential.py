@@ -174,7 +174,7 @@ class PotentialBase:
 
         q = np.asarray(q, dtype=np.float64) if not isinstance(q, torch.Tensor) else q
         shape = tuple(q.shape)
-        if shape[0] != 3:
+        if not shape or shape[0] != 3:  # a scalar is refused, as in gala (regression 165)
             raise ValueError(f"positions must have shape (3, ...), got {shape}")
         qd = as_device_f64(q).reshape(3, -1).contiguous()
         n = qd.shape[1]
@@ -205,9 +205,24 @@ class PotentialBase:
     def circular_velocity(self, q, t=0.0):
         """sqrt(r |dPhi/dr|) from the gradient (PotentialBase.circular_velocity)."""
         q = np.asarray(q, dtype=np.float64)
+        if q.ndim == 0 or q.shape[0] != 3:
+            raise ValueError(f"positions must have shape (3, ...), got {q.shape}")
         r = np.sqrt(np.sum(q ** 2, axis=0))
         dPhi_dr = np.sum(self.gradient(q, t) * q, axis=0) / r
         return np.sqrt(r * np.abs(dPhi_dr))
+
+    def replicate(self, **kwargs):
+        """A copy with some parameters, the origin or the rotation R replaced
+        (PotentialBase.replicate, src/gala/potential/potential/core.py)."""
+        params = dict(self.parameters)
+        origin = kwargs.pop("origin", self.origin)
+        R = kwargs.pop("R", self.R)
+        kwargs.pop("units", None)
+        unknown = set(kwargs) - set(params)
+        if unknown:
+            raise TypeError(f"{type(self).__name__} has no parameters {sorted(unknown)}")
+        params.update(kwargs)
+        return type(self)(**params, origin=origin, R=R)
 
     # --- integration ---------------------------------------------------------
     def integrate_orbit(self, *args, **kwargs):

@@ -1,0 +1,155 @@
+"""gala's own potential and integrator checks, run twice: on the oracle (CPU)
+and on the CUDA path (marked gpu).
+
+* numerical gradient vs gradient: 16 random points within twice |w0|,
+  finite-difference step 1e-3 |w0|, rtol 1e-5 (potential_helpers.py:265-299);
+* numerical Laplacian vs 4 pi G rho, rtol 1e-2 (:301-347);
+* rotation / shift: a rotated or shifted copy equals the original evaluated at
+  R (x - x0), gradients rotated back (:518-546);
+* scalar positions are refused with ValueError (test_regression_165, :505-516);
+* point-mass closure: a circular orbit returns to its start after one period
+  at atol 1e-6 (tests/integrate/test_pyintegrators.py:96-104).
+
+The canonical instances are gala's (canonical_potentials.py:18-70) in galactic
+units; gala's Kepler instance is in solar-system units, so here the point mass
+is 1e11 Msun at 10 kpc.  gala differentiates with the findiff package on a
+9-point stencil; this file uses fourth-order central differences.
+"""
+import numpy as np
+import pytest
+
+import gala_gb300 as g
+
+CANONICAL = {
+    # name: (potential, w0, has density)
+    "kepler": (g.KeplerPotential(m=1e11), [10.0, 0.0, 0.0, 0.0, 0.2, 0.0], False),
+    "hernquist": (g.HernquistPotential(m=1e11, c=0.26), [1.0, 0.0, 0.0, 0.0, 0.1, 0.1], True),
+    "plummer": (g.PlummerPotential(m=1e11, b=0.26), [1.0, 0.0, 0.0, 0.0, 0.1, 0.1], True),
+    "miyamotonagai": (g.MiyamotoNagaiPotential(m=1e11, a=6.5, b=0.26), [8.0, 0.0, 0.0, 0.0, 0.22, 0.1], True),
+    "sphericalnfw": (g.NFWPotential(m=1e11, r_s=12.0), [19.0, 2.7, -6.9, 0.0352238, -0.03579493, 0.075], True),
+    "flattenednfw": (g.NFWPotential(m=1e11, r_s=12.0, c=0.7), [19.0, 2.7, -6.9, 0.0352238, -0.03579493, 0.075],
+                     False),
+    "triaxialnfw": (g.NFWPotential(m=1e11, r_s=12.0, a=1.0, b=0.95, c=0.9),
+                    [19.0, 2.7, -6.9, 0.0352238, -0.03579493, 0.075], False),
+    "milkyway": (g.MilkyWayPotential(), [8.0, 0.0, 0.0, 0.0, 0.22, 0.1], True),
+}
+ROTATED = ("miyamotonagai", "flattenednfw", "triaxialnfw")
+
+
+def _points(name, seed=42):
+    w0 = np.asarray(CANONICAL[name][1])
+    r = np.linalg.norm(w0[:3])
+    rng = np.random.default_rng(seed)
+    return rng.uniform(-2 * r, 2 * r, size=(3, 16)), 1e-3 * r
+
+
+def _stencil(pts, dx):
+    """(3, 16, 3, 5) points: for each axis the offsets -2..2 dx around each point."""
+    out = np.repeat(pts[:, :, None, None], 3, axis=2).repeat(5, axis=3)
+    for k in range(3):
+        out[k, :, k, :] += np.arange(-2, 3) * dx
+    return out
+
+
+def check_gradient(name, energy, gradient):
+    pts, dx = _points(name)
+    phi = energy(_stencil(pts, dx).reshape(3, -1)).reshape(16, 3, 5)
+    num = (phi[..., 0] - 8 * phi[..., 1] + 8 * phi[..., 3] - phi[..., 4]) / (12 * dx)
+    assert np.allclose(gradient(pts), num.T, rtol=1e-5)
+
+
+def check_density(name, energy, density):
+    pts, dx = _points(name)
+    phi = energy(_stencil(pts, dx).reshape(3, -1)).reshape(16, 3, 5)
+    d2 = (-phi[..., 0] + 16 * phi[..., 1] - 30 * phi[..., 2] + 16 * phi[..., 3] - phi[..., 4]) / (12 * dx * dx)
+    assert np.allclose(4 * np.pi * g.units.G * density(pts), d2.sum(axis=1), rtol=1e-2)
+
+
+def check_rotation_shift(name, evaluate):
+    """evaluate(potential, kind, x) -> values (kind: energy / gradient / density)."""
+    pot = CANONICAL[name][0]
+    x = np.array([10.0, 5.0, 3.0])[:, None]
+    x0 = np.array([1.0, 1.0, 3.0])
+    R = np.array([[0.0, 1.0, 0.0], [-1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    kinds = ("energy", "gradient") + (("density",) if CANONICAL[name][2] else ())
+    for kind in kinds:
+        base = lambda q: evaluate(pot, kind, q)  # noqa: E731
+        back = (lambda v: R.T @ v) if kind == "gradient" else (lambda v: v)
+        np.testing.assert_allclose(evaluate(pot.replicate(R=R), kind, x), back(base(R @ x)), rtol=1e-13)
+        np.testing.assert_allclose(evaluate(pot.replicate(origin=x0), kind, x), base(x - x0[:, None]), rtol=1e-13)
+        np.testing.assert_allclose(evaluate(pot.replicate(R=R, origin=x0), kind, x),
+                                   back(base(R @ (x - x0[:, None]))), rtol=1e-13)
+
+
+def _unit_point_mass():
+    """G m = 1: the circular orbit at r = 1 kpc has v = 1 kpc/Myr, period 2 pi Myr."""
+    pot = g.KeplerPotential(m=1.0 / g.units.G)
+    w0 = np.array([[1.0], [0.0], [0.0], [0.0], [1.0], [0.0]])
+    t = g.parse_time_specification(t1=0.0, t2=2 * np.pi, n_steps=10_000)
+    return pot, w0, t
+
+
+# ---------------------------------------------------------------- oracle (CPU)
+@pytest.mark.parametrize("name", sorted(CANONICAL))
+def test_oracle_gradient_is_the_numerical_gradient(oracle, name):
+    pot = CANONICAL[name][0]
+    check_gradient(name, lambda q: oracle.energy(pot, q), lambda q: oracle.gradient(pot, q))
+
+
+@pytest.mark.parametrize("name", sorted(n for n in CANONICAL if CANONICAL[n][2]))
+def test_oracle_density_is_the_laplacian(oracle, name):
+    pot = CANONICAL[name][0]
+    check_density(name, lambda q: oracle.energy(pot, q), lambda q: oracle.density(pot, q))
+
+
+@pytest.mark.parametrize("name", ROTATED)
+def test_oracle_rotation_shift(oracle, name):
+    check_rotation_shift(name, lambda p, kind, q: getattr(oracle, kind)(p, q))
+
+
+def test_scalar_positions_are_refused():
+    pot = CANONICAL["miyamotonagai"][0]
+    for meth in (pot.energy, pot.gradient, pot.circular_velocity):
+        with pytest.raises(ValueError):
+            meth(8.0)
+
+
+@pytest.mark.parametrize("method", ["leapfrog", "ruth4", "dop853"])
+def test_oracle_point_mass_orbit_closes(oracle, method):
+    pot, w0, t = _unit_point_mass()
+    if method == "dop853":
+        w, st, _ = oracle.dop853(pot, w0, t, atol=1e-10, rtol=1e-10)
+        assert np.all(st == 1)
+    else:
+        w = oracle.fixed(pot, w0, t, method)
+    assert np.allclose(w[:, 0, 0], w[:, -1, 0], atol=1e-6)
+
+
+# ---------------------------------------------------------------- CUDA path
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(CANONICAL))
+def test_gpu_gradient_is_the_numerical_gradient(name):
+    pot = CANONICAL[name][0]
+    check_gradient(name, pot.energy, pot.gradient)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(n for n in CANONICAL if CANONICAL[n][2]))
+def test_gpu_density_is_the_laplacian(name):
+    pot = CANONICAL[name][0]
+    check_density(name, pot.energy, pot.density)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ROTATED)
+def test_gpu_rotation_shift(name):
+    check_rotation_shift(name, lambda p, kind, q: getattr(p, kind)(q))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["leapfrog", "ruth4", "dop853"])
+def test_gpu_point_mass_orbit_closes(method):
+    pot, w0, t = _unit_point_mass()
+    kw = dict(Integrator_kwargs=dict(atol=1e-10, rtol=1e-10)) if method == "dop853" else {}
+    w = pot.integrate_orbit(w0, t=t, Integrator=method, **kw).w()
+    assert np.allclose(w[:, 0], w[:, -1], atol=1e-6)

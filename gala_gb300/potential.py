@@ -383,6 +383,9 @@ class CompositePotential(PotentialBase, OrderedDict):
     def __hash__(self):
         return id(self)
 
+    def replicate(self, **kwargs):
+        raise NotImplementedError("replicate the components and compose them again")
+
     def __eq__(self, other):
         return self is other
 

@@ -153,3 +153,47 @@ def test_gpu_point_mass_orbit_closes(method):
     kw = dict(Integrator_kwargs=dict(atol=1e-10, rtol=1e-10)) if method == "dop853" else {}
     w = pot.integrate_orbit(w0, t=t, Integrator=method, **kw).w()
     assert np.allclose(w[:, 0], w[:, -1], atol=1e-6)
+
+
+# ---------------------------------------------------------------- rotating frames
+# tests/potential/hamiltonian/test_with_frame_potential.py:118-177, with G m = 1
+# (the same numbers as gala's dimensionless units): a circular orbit co-rotating
+# with the frame stays put; with Omega = (1, 1, 1) the Jacobi constant
+# H - Omega . L (H = p^2/2 + Phi - Omega . L, builtin_frames.cpp:73-94) holds to 1e-9.
+def _rotating_cases():
+    pot = g.KeplerPotential(m=1.0 / g.units.G)
+    co = (g.ConstantRotatingFrame(Omega=[0.0, 0.0, 1.0]), np.array([[1.0], [0], [0], [0], [1.0], [0]]),
+          g.parse_time_specification(dt=1.0, n_steps=1000), dict(atol=1e-10, rtol=1e-10))
+    off = (g.ConstantRotatingFrame(Omega=[1.0, 1.0, 1.0]), np.array([[1.0], [0], [0], [0], [1.1], [0]]),
+           g.parse_time_specification(dt=0.1, n_steps=10000), dict(atol=1e-12, rtol=1e-12))
+    return pot, co, off
+
+
+def check_rotating(integrate, hamiltonian_value):
+    pot, co, off = _rotating_cases()
+    frame, w0, t, kw = co
+    w = integrate(pot, frame, w0, t, kw)
+    assert np.allclose(w[0], 1.0, atol=1e-7) and np.allclose(w[1:3], 0.0, atol=1e-7)
+    frame, w0, t, kw = off
+    w = integrate(pot, frame, w0, t, kw)
+    L = np.cross(w[:3], w[3:], axis=0)
+    C = hamiltonian_value(pot, frame, w) - np.sum(frame.Omega[:, None] * L, axis=0)
+    assert np.all(np.abs((C[1:] - C[0]) / C[0]) < 1e-9)
+
+
+def test_oracle_rotating_frame_kepler(oracle):
+    def integrate(pot, frame, w0, t, kw):
+        w, st, _ = oracle.dop853(pot, w0, t, frame=frame, **kw)
+        assert np.all(st == 1)
+        return w[:, :, 0]
+
+    check_rotating(integrate, lambda pot, frame, w: oracle.hamiltonian_value(pot, w, frame=frame))
+
+
+@pytest.mark.gpu
+def test_gpu_rotating_frame_kepler():
+    def integrate(pot, frame, w0, t, kw):
+        return g.Hamiltonian(pot, frame=frame).integrate_orbit(w0, t=t, Integrator="dop853",
+                                                               Integrator_kwargs=kw).w()
+
+    check_rotating(integrate, lambda pot, frame, w: g.Hamiltonian(pot, frame=frame).energy(w))

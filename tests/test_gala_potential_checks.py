@@ -197,3 +197,83 @@ def test_gpu_rotating_frame_kepler():
                                                                Integrator_kwargs=kw).w()
 
     check_rotating(integrate, lambda pot, frame, w: g.Hamiltonian(pot, frame=frame).energy(w))
+
+
+# ---------------------------------------------------------------- composite vs Python integrators
+# tests/potential/potential/test_composite.py:58-88: Kepler (1 Msun) + Hernquist
+# (0.5 Msun, c = 0.1 au) in solar-system units from (1 au, 2 pi au/yr), dt 0.01,
+# 1000 steps; the C integrators (DOP853 at atol = rtol = 1e-14, Leapfrog) agree
+# with gala's Python ones -- scipy's dop853 and the Python leapfrog
+# (pyintegrators/leapfrog.py:131-138) -- within np.allclose.  gala runs scipy at
+# its default rtol 1e-6, whose own error puts one velocity near a zero crossing
+# 1.1e-7 off (outside allclose's atol 1e-8); here scipy runs at 1e-14 as well,
+# and the two DOP853 codes agree to 5e-10.  G m = 4 pi^2 and 2 pi^2 in galactic
+# units give the same numbers as gala's solar-system units.
+def _composite_case():
+    pot = g.CCompositePotential(one=g.KeplerPotential(m=4 * np.pi ** 2 / g.units.G),
+                                two=g.HernquistPotential(m=2 * np.pi ** 2 / g.units.G, c=0.1))
+    w0 = np.array([1.0, 0, 0, 0, 2 * np.pi, 0])
+    t = g.parse_time_specification(dt=0.01, n_steps=1000)
+    return pot, w0, t
+
+
+def _python_dop853(gradient, w0, t):
+    """gala's DOPRI853Integrator: scipy's ode('dop853') stepped to each output time."""
+    from scipy.integrate import ode
+
+    def rhs(_, w):
+        return np.concatenate([w[3:], -gradient(w[:3, None])[:, 0]])
+
+    solver = ode(rhs).set_integrator("dop853", atol=1e-14, rtol=1e-14)
+    solver.set_initial_value(w0, t[0])
+    out = [w0]
+    for tk in t[1:]:
+        solver.integrate(tk)
+        assert solver.successful()
+        out.append(solver.y)
+    return np.array(out).T
+
+
+def _python_leapfrog(gradient, w0, t):
+    """gala's Python LeapfrogIntegrator: half-kick start, drift, kick (leapfrog.py:90-138)."""
+    dt = t[1] - t[0]
+    x, v = w0[:3].copy(), w0[3:].copy()
+    v_half = v - 0.5 * dt * gradient(x[:, None])[:, 0]
+    out = [w0]
+    for _ in t[1:]:
+        x = x + v_half * dt
+        a = -gradient(x[:, None])[:, 0]
+        v = v_half + 0.5 * dt * a
+        v_half = v_half + dt * a
+        out.append(np.concatenate([x, v]))
+    return np.array(out).T
+
+
+def check_composite(integrate, gradient):
+    pot, w0, t = _composite_case()
+    w_c = integrate(pot, w0, t, "dop853")
+    w_py = _python_dop853(lambda q: gradient(pot, q), w0, t)
+    assert np.allclose(w_c[:3], w_py[:3]) and np.allclose(w_c[3:], w_py[3:])
+    w_c = integrate(pot, w0, t, "leapfrog")
+    w_py = _python_leapfrog(lambda q: gradient(pot, q), w0, t)
+    assert np.allclose(w_c[:3], w_py[:3]) and np.allclose(w_c[3:], w_py[3:])
+
+
+def test_oracle_composite_matches_python_integrators(oracle):
+    def integrate(pot, w0, t, method):
+        if method == "dop853":
+            w, st, _ = oracle.dop853(pot, w0[:, None], t, atol=1e-14, rtol=1e-14)
+            assert np.all(st == 1)
+            return w[:, :, 0]
+        return oracle.fixed(pot, w0[:, None], t, method)[:, :, 0]
+
+    check_composite(integrate, oracle.gradient)
+
+
+@pytest.mark.gpu
+def test_gpu_composite_matches_python_integrators():
+    def integrate(pot, w0, t, method):
+        kw = dict(Integrator_kwargs=dict(atol=1e-14, rtol=1e-14)) if method == "dop853" else {}
+        return pot.integrate_orbit(w0, t=t, Integrator=method, **kw).w()
+
+    check_composite(integrate, lambda pot, q: pot.gradient(q))

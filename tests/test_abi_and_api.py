@@ -247,3 +247,15 @@ def test_public_calls_open_nvtx_ranges(monkeypatch):
     with pytest.raises(ValueError):
         pot.energy(np.ones((2, 2)))
     assert seen == ["gala_gb300.integrate_orbit", "gala_gb300.potential_eval"]
+
+
+def test_symplectic_entry_points_refuse_rotating_frames_on_the_host():
+    """leapfrog.pyx:61-68 / ruth4.pyx: a non-static frame is refused with gala's
+    message; the C entry points return GX_ERR_UNSUPPORTED before any CUDA call."""
+    lib = _abi.load()
+    pk = g.HernquistPotential(m=1e11, c=1.0).packed()
+    fr = g.ConstantRotatingFrame(Omega=[0.0, 0.0, 0.1]).c_frame()
+    for name, label in (("gx_leapfrog_integrate_hamiltonian", b"Leapfrog"), ("gx_ruth4_integrate_hamiltonian", b"Ruth4")):
+        rc = getattr(lib, name)(pk.for_host(), C.byref(fr), None, 0, None, 3, 1, None, None)
+        assert rc == _abi.GX_ERR_UNSUPPORTED
+        assert lib.gx_last_error_message() == label + b" integration is currently only supported for StaticFrame"

@@ -58,7 +58,9 @@ def quantity_from_hdf5(dset, physical_type=None):
     values = np.asarray(dset[()], dtype=np.float64)
     unit = _attr_text(dset.attrs["unit"]) if "unit" in dset.attrs else None
     if unit:
-        values = values * _unit_factor(unit, physical_type)
+        factor = _unit_factor(unit, physical_type)
+        if factor != 1.0:
+            values = values * factor
     return values
 
 

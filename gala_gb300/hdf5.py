@@ -346,7 +346,7 @@ class _Reader:
             addr, size = struct.unpack_from("<QQ", layout, 2)
             if addr == _UNDEF:
                 return b"\x00" * nbytes
-            return self.b[addr:addr + size]
+            return memoryview(self.b)[addr:addr + size]
         if cls == 2:
             return self._read_chunked(layout, filters, dt, shape)
         raise NotImplementedError(f"layout class {cls}")
@@ -692,8 +692,14 @@ class File(Group):
         self.mode = mode
         self._closed = False
         if mode == "r":
+            import mmap
+
             with open(self.filename, "rb") as fh:
-                data = fh.read()
+                size = fh.seek(0, 2)
+                if size < len(_SIG):
+                    raise OSError("not an HDF5 file (signature not found at offset 0)")
+                # mapped, not read: each dataset is copied once, straight from the map
+                data = mmap.mmap(fh.fileno(), 0, access=mmap.ACCESS_READ)
             self._load(data)
         elif mode in ("w", "x", "w-"):
             if mode in ("x", "w-"):
@@ -749,9 +755,12 @@ class File(Group):
         if self._closed:
             return
         if self.mode != "r":
-            data = _Writer().layout(self)  # laid out first: an error leaves no file behind
+            meta, arrays = _Writer().layout(self)  # laid out first: an error leaves no file behind
             with open(self.filename, "wb") as fh:
-                fh.write(data)
+                fh.write(meta)
+                for arr in arrays:  # streamed from the arrays themselves, no copies
+                    fh.write(arr.reshape(-1).view(np.uint8).data)
+                    fh.write(b"\x00" * (_pad8(arr.nbytes) - arr.nbytes))
         self._closed = True
 
     def flush(self):
@@ -773,14 +782,18 @@ class File(Group):
 # ============================================================================
 class _Writer:
     """Lays out a File tree: superblock, then for each group its object header,
-    B-tree node, symbol-table nodes and local heap, then each dataset's object
-    header and raw data, then the global heap collections of variable-length
-    strings."""
+    B-tree node, symbol-table nodes and local heap, each dataset's object header
+    (variable-length string data beside it), the global heap collections of the
+    strings, and last the numeric dataset payloads, written from the arrays
+    themselves."""
 
     def __init__(self):
         self.buf = bytearray()
         self.gcols = []   # [(address, [bytes objects], size)]
         self.vlen_refs = []
+        # numeric dataset payloads: (file offset of the layout message's address
+        # field, array); placed after all metadata and streamed from the arrays
+        self.external = []
 
     def alloc(self, n):
         addr = len(self.buf)
@@ -854,19 +867,25 @@ class _Writer:
             p += len(e)
         return addr, body_at
 
-    def layout(self, root: File) -> bytes:
+    def layout(self, root: File):
+        """(metadata bytes, numeric payload arrays): the file is the metadata
+        followed by each array padded to 8 bytes, in order."""
         self.alloc(96)  # superblock with the root symbol-table entry
         self.vlen_sites = []  # (file offset of the vlen IDs, count)
         root_addr, btree, heap = self._group(root)
         self._write_gcols()
-        eof = len(self.buf)
+        addr = len(self.buf)
+        for site, arr in self.external:
+            struct.pack_into("<Q", self.buf, site, addr)
+            addr += _pad8(arr.nbytes)
+        eof = addr
         sb = bytearray(_SIG)
         sb += bytes([0, 0, 0, 0, 0, 8, 8, 0])
         sb += struct.pack("<HHI", _LEAF_K, _INTERNAL_K, 0)
         sb += struct.pack("<QQQQ", 0, _UNDEF, eof, _UNDEF)
         sb += struct.pack("<QQII", 0, root_addr, 1, 0) + struct.pack("<QQ", btree, heap)
         self.put(0, bytes(sb))
-        return bytes(self.buf)
+        return self.buf, [arr for _, arr in self.external]
 
     def _group(self, g: Group):
         """Writes the group's subtree; returns (header, B-tree, local heap)."""
@@ -932,20 +951,26 @@ class _Writer:
     def _dataset(self, ds: Dataset) -> int:
         arr, dt = ds._data, ds.dtype
         shape = np.shape(arr)
-        raw, is_vlen = self._raw(arr, dt)
-        if raw:
-            data_addr = self.alloc(len(raw))
-            self.put(data_addr, raw)
-            if is_vlen:
-                self.vlen_sites.append((data_addr, len(raw) // 16))
+        ext = None
+        data_addr = _UNDEF
+        if isinstance(dt, _VlenStr):
+            raw, _ = self._raw(arr, dt)
+            nbytes = len(raw)
+            if raw:
+                data_addr = self.alloc(nbytes)
+                self.put(data_addr, raw)
+                self.vlen_sites.append((data_addr, nbytes // 16))
         else:
-            data_addr = _UNDEF
+            ext = np.ascontiguousarray(arr, dtype=dt)
+            nbytes = ext.nbytes  # its address is set when the metadata is complete
         fill = bytes([2, 2, 2, 1]) + struct.pack("<I", 0)
-        layout = bytes([3, 1]) + struct.pack("<QQ", data_addr, len(raw))
+        layout = bytes([3, 1]) + struct.pack("<QQ", data_addr, nbytes)
         msgs = [(0x01, _encode_space(shape), None), (0x03, _encode_dtype(dt), None), (0x05, fill, None),
                 (0x08, layout, None)] + self._attr_messages(ds, None)
         hdr, body_at = self._header(msgs)
         self._note_vlen_sites(msgs, body_at)
+        if ext is not None and nbytes:
+            self.external.append((body_at[3] + 2, ext))
         return hdr
 
     def _write_gcols(self):

@@ -401,11 +401,19 @@ static void parallel_for(int nthreads, int64_t n, int64_t chunk, range_fn fn, vo
         fn(ctx, 0, n);
         return;
     }
-    pool_t P = {fn, ctx, n, chunk, 0};
+    pool_t P;
+    P.fn = fn;
+    P.ctx = ctx;
+    P.n = n;
+    P.chunk = chunk;
+    P.next = 0;
     pthread_mutex_init(&P.mu, NULL);
     pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)nthreads);
-    for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, pool_worker, &P);
-    for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+    int started = 0;
+    if (th)
+        while (started < nthreads - 1 && pthread_create(&th[started], NULL, pool_worker, &P) == 0) started++;
+    pool_worker(&P); /* the caller is the last worker, so the work ends even without threads */
+    for (int i = 0; i < started; i++) pthread_join(th[i], NULL);
     free(th);
     pthread_mutex_destroy(&P.mu);
 }

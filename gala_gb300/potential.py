@@ -211,6 +211,26 @@ class PotentialBase:
         dPhi_dr = np.sum(self.gradient(q, t) * q, axis=0) / r
         return np.sqrt(r * np.abs(dPhi_dr))
 
+    def mass_enclosed(self, q, t=0.0):
+        """Mass within the spherical radius of each position, r^2 |dPhi/dr| / G
+        with dPhi/dr the central difference of step 1e-3 along the radial
+        direction (PotentialBase.mass_enclosed, src/gala/potential/potential/core.py:649-707);
+        negated when the potential's mass parameter is negative, as gala does.
+        Both sides of every difference are evaluated in one GPU call."""
+        q = np.asarray(q, dtype=np.float64)
+        if q.ndim == 0 or q.shape[0] != 3:
+            raise ValueError(f"positions must have shape (3, ...), got {q.shape}")
+        shape = q.shape[1:]
+        q2 = q.reshape(3, -1)
+        n = q2.shape[1]
+        h = 1e-3
+        r = np.sqrt(np.sum(q2 ** 2, axis=0))
+        eps = h * q2 / r
+        phi = np.asarray(self.energy(np.concatenate([q2 + eps, q2 - eps], axis=1), t))
+        menc = np.abs(r * r * (phi[:n] - phi[n:]) / self.G / (2.0 * h))
+        sgn = -1.0 if float(np.sum(self.parameters.get("m", 1.0))) < 0 else 1.0
+        return (sgn * menc).reshape(shape)
+
     def replicate(self, **kwargs):
         """A copy with some parameters, the origin or the rotation R replaced
         (PotentialBase.replicate, src/gala/potential/potential/core.py)."""

@@ -277,3 +277,32 @@ def test_gpu_composite_matches_python_integrators():
         return pot.integrate_orbit(w0, t=t, Integrator=method, **kw).w()
 
     check_composite(integrate, lambda pot, q: pot.gradient(q))
+
+
+# ---------------------------------------------------------------- enclosed mass
+def check_mass_enclosed(with_energy):
+    """r^2 |dPhi/dr| / G with gala's step 1e-3 (core.py:649-707): the Hernquist
+    M(<r) = m r^2 / (r + c)^2 and the Kepler mass, to the difference's accuracy."""
+    hern = with_energy(g.HernquistPotential(m=1e11, c=0.26))
+    q = np.array([[1.0, 5.0, 30.0], [0.5, 0.0, -4.0], [0.2, 2.0, 1.0]])
+    r = np.linalg.norm(q, axis=0)
+    np.testing.assert_allclose(hern.mass_enclosed(q), 1e11 * r ** 2 / (r + 0.26) ** 2, rtol=1e-5)
+    kep = with_energy(g.KeplerPotential(m=3e10))
+    np.testing.assert_allclose(kep.mass_enclosed(q[:, :, None]), np.full((3, 1), 3e10), rtol=1e-5)
+    neg = with_energy(g.KeplerPotential(m=-3e10))
+    assert np.all(neg.mass_enclosed(q) < 0)
+
+
+def test_oracle_mass_enclosed(oracle):
+    def with_energy(pot):
+        pot.energy = lambda q, t=0.0: oracle.energy(pot, q, t)  # the oracle behind the API
+        return pot
+
+    check_mass_enclosed(with_energy)
+    with pytest.raises(ValueError):
+        g.KeplerPotential(m=1.0).mass_enclosed(3.0)
+
+
+@pytest.mark.gpu
+def test_gpu_mass_enclosed():
+    check_mass_enclosed(lambda pot: pot)

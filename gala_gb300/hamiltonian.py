@@ -55,7 +55,12 @@ class ConstantRotatingFrame(FrameBase):
 
     def __init__(self, Omega, units=None):
         super().__init__(units=units)
-        self.Omega = np.asarray(getattr(Omega, "value", Omega), dtype=np.float64).reshape(3)
+        if hasattr(Omega, "unit") and hasattr(Omega, "to_value"):
+            # a quantity: to 1/Myr, angles dimensionless as gala's Omega parameter takes them
+            import astropy.units as u
+
+            Omega = Omega.to_value(1 / u.Myr, equivalencies=u.dimensionless_angles())
+        self.Omega = np.asarray(Omega, dtype=np.float64).reshape(3)
 
     def _params(self):
         return list(self.Omega)

@@ -136,10 +136,19 @@ class PotentialBase:
         self.R = None if R is None else _rotation_matrix(R)
         self._packed = None
 
-    @staticmethod
-    def _coerce(name, v):
-        if hasattr(v, "value"):
-            v = v.value
+    _GALACTIC_UNIT = {"mass": "Msun", "length": "kpc", "dimensionless": ""}
+
+    def _coerce(self, name, v):
+        """A parameter value in galactic units.  A quantity (an object with
+        ``unit`` and ``to_value``, e.g. astropy's) is converted to the unit of the
+        parameter's physical type; a plain number is taken as galactic."""
+        if hasattr(v, "unit") and hasattr(v, "to_value"):
+            from .potential_io import _PARAM_TYPES
+
+            ptype = _PARAM_TYPES.get(type(self).__name__, {}).get(name)
+            if ptype is None:
+                raise TypeError(f"{type(self).__name__}: no unit is known for parameter {name!r}")
+            v = v.to_value(self._GALACTIC_UNIT[ptype])
         a = np.asarray(v, dtype=np.float64)
         return float(a) if a.ndim == 0 else a
 

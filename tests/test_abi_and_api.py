@@ -259,3 +259,26 @@ def test_symplectic_entry_points_refuse_rotating_frames_on_the_host():
         rc = getattr(lib, name)(pk.for_host(), C.byref(fr), None, 0, None, 3, 1, None, None)
         assert rc == _abi.GX_ERR_UNSUPPORTED
         assert lib.gx_last_error_message() == label + b" integration is currently only supported for StaticFrame"
+
+
+class _Quantity:
+    """A stand-in for an astropy Quantity: value, unit and to_value(unit)."""
+
+    SCALE = {"Msun": 1.0, "kpc": 1.0, "pc": 1e-3, "": 1.0, "Gyr": 1e3}
+
+    def __init__(self, value, unit):
+        self.value, self.unit = value, unit
+
+    def to_value(self, unit):
+        if (self.unit in ("kpc", "pc")) != (unit == "kpc") and unit != "":
+            raise ValueError(f"cannot convert {self.unit} to {unit}")
+        return np.asarray(self.value) * self.SCALE[self.unit] / self.SCALE[unit]
+
+
+def test_quantity_parameters_are_converted_not_stripped():
+    pot = g.HernquistPotential(m=_Quantity(1e11, "Msun"), c=_Quantity(260.0, "pc"))
+    assert pot.parameters["c"] == pytest.approx(0.26) and pot.parameters["m"] == 1e11
+    with pytest.raises(ValueError):
+        g.HernquistPotential(m=1e11, c=_Quantity(1.0, "Gyr"))
+    nfw = g.NFWPotential(m=1e11, r_s=_Quantity(12000.0, "pc"), c=_Quantity(0.9, ""))
+    assert nfw.parameters["r_s"] == pytest.approx(12.0) and nfw.parameters["c"] == 0.9

@@ -18,6 +18,25 @@ def _to_numpy(a):
     return np.asarray(a)
 
 
+def _galactic(x, unit):
+    """x as float64 in the given galactic unit: quantities (anything with
+    ``to_value``) are converted, plain arrays are taken as galactic."""
+    if hasattr(x, "to_value"):
+        return np.asarray(x.to_value(unit), dtype=np.float64)
+    return np.asarray(x, dtype=np.float64)
+
+
+def phase_space_array(w):
+    """(6, ...) float64 array of a phase-space position: this library's
+    PhaseSpacePosition, any object with ``xyz`` / ``v_xyz`` (gala's
+    PhaseSpacePosition, converted to kpc and kpc/Myr), or an array."""
+    if isinstance(w, PhaseSpacePosition):
+        return w.w()
+    if hasattr(w, "xyz") and hasattr(w, "v_xyz"):
+        return np.concatenate([_galactic(w.xyz, "kpc"), _galactic(w.v_xyz, "kpc / Myr")], axis=0)
+    return w
+
+
 # -- HDF5 serialisation helpers (gala's layout: src/gala/io.py:4-47,
 #    src/gala/dynamics/core.py:572-640) ----------------------------------------
 _FRAME_MODULE = "gala.potential.frame.builtin.frames"

@@ -15,7 +15,7 @@ import warnings
 import numpy as np
 
 from . import _abi
-from .dynamics import Orbit, PhaseSpacePosition
+from .dynamics import Orbit, phase_space_array
 from .integrate import (DOPRI853Integrator, LeapfrogIntegrator, Ruth4Integrator, get_integrator,
                         parse_time_specification)
 from .potential import PotentialBase
@@ -91,9 +91,7 @@ class Hamiltonian:
 
     # --- evaluation ----------------------------------------------------------
     def _prepare_w(self, w):
-        if isinstance(w, PhaseSpacePosition):
-            w = w.w()
-        w = np.asarray(w, dtype=np.float64)
+        w = np.asarray(phase_space_array(w), dtype=np.float64)
         if w.shape[0] != 6:
             raise ValueError(f"Invalid phase-space shape {w.shape}: expected (6, ...)")
         return w
@@ -161,9 +159,8 @@ class Hamiltonian:
         # Every argument is checked before the device is touched, in gala's order:
         # initial-condition shape (chamiltonian.pyx:309-310), time specification
         # (timespec.py:91-145), then the integrator's own checks (leapfrog.pyx:61-68).
-        if isinstance(w0, PhaseSpacePosition):
-            arr_w0 = w0.w()
-        elif isinstance(w0, torch.Tensor):
+        w0 = phase_space_array(w0)
+        if isinstance(w0, torch.Tensor):
             arr_w0 = w0
         else:
             arr_w0 = np.asarray(w0, dtype=np.float64)

@@ -282,3 +282,26 @@ def test_quantity_parameters_are_converted_not_stripped():
         g.HernquistPotential(m=1e11, c=_Quantity(1.0, "Gyr"))
     nfw = g.NFWPotential(m=1e11, r_s=_Quantity(12000.0, "pc"), c=_Quantity(0.9, ""))
     assert nfw.parameters["r_s"] == pytest.approx(12.0) and nfw.parameters["c"] == 0.9
+
+
+def test_phase_space_objects_with_units_are_converted():
+    """Any object with xyz / v_xyz (gala's PhaseSpacePosition) gives kpc and kpc/Myr."""
+    from gala_gb300.dynamics import phase_space_array
+
+    class _PSP:
+        def __init__(self, xyz, v_xyz):
+            self.xyz, self.v_xyz = xyz, v_xyz
+
+    class _Q(_Quantity):
+        SCALE = {"pc": 1e-3, "kpc": 1.0, "kpc / Myr": 1.0, "km / s": g.units.KMS_TO_KPC_MYR}
+
+        def to_value(self, unit):
+            return np.asarray(self.value) * self.SCALE[self.unit] / self.SCALE[unit]
+
+    w = phase_space_array(_PSP(_Q([[8000.0], [0.0], [0.0]], "pc"), _Q([[0.0], [220.0], [0.0]], "km / s")))
+    np.testing.assert_allclose(w[:, 0], [8.0, 0, 0, 0, 220 * g.units.KMS_TO_KPC_MYR, 0])
+    own = g.PhaseSpacePosition(pos=[1.0, 2, 3], vel=[4.0, 5, 6])
+    assert np.array_equal(phase_space_array(own), [1.0, 2, 3, 4, 5, 6])
+    with pytest.raises(ValueError, match="shape"):   # still validated before the device
+        g.HernquistPotential(m=1e11, c=1.0).integrate_orbit(_PSP(np.ones((2, 1)), np.ones((2, 1))), dt=1.0,
+                                                            n_steps=3)

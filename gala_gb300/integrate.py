@@ -21,6 +21,9 @@ def parse_time_specification(units=None, dt=None, n_steps=None, t1=None, t2=None
     ``t``; ``dt, n_steps[, t1]``; ``dt, t1, t2``; array ``dt, t1``;
     ``n_steps, t1, t2``.
     """
+    # times given as quantities (anything with to_value) are converted to Myr,
+    # as gala decomposes them in the unit system (timespec.py:74-89)
+    dt, t1, t2, t = (x.to_value("Myr") if hasattr(x, "to_value") else x for x in (dt, t1, t2, t))
     if n_steps is not None:
         n_steps = int(n_steps)
 

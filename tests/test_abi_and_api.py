@@ -305,3 +305,16 @@ def test_phase_space_objects_with_units_are_converted():
     with pytest.raises(ValueError, match="shape"):   # still validated before the device
         g.HernquistPotential(m=1e11, c=1.0).integrate_orbit(_PSP(np.ones((2, 1)), np.ones((2, 1))), dt=1.0,
                                                             n_steps=3)
+
+
+def test_time_specification_with_quantities():
+    class _T(_Quantity):
+        SCALE = {"Myr": 1.0, "Gyr": 1e3}
+
+        def to_value(self, unit):
+            return np.asarray(self.value) * self.SCALE[self.unit] / self.SCALE[unit]
+
+    t = parse_time_specification(None, dt=_T(0.001, "Gyr"), n_steps=3)
+    np.testing.assert_allclose(t, [0.0, 1.0, 2.0, 3.0])
+    t = parse_time_specification(None, t=_T([0.0, 0.5], "Gyr"))
+    np.testing.assert_allclose(t, [0.0, 500.0])

@@ -344,12 +344,20 @@ class NFWPotential(PotentialBase):
 
     @classmethod
     def from_circular_velocity(cls, v_c, r_s, a=1.0, b=1.0, c=1.0, r_ref=None, units=None, origin=None, R=None):
-        """NFW from the circular velocity v_c (kpc/Myr) at r_ref (default r_s):
-        G m / r_s = v_c^2 / u_ref [u_ref / (1 + u_ref) - ln(1 + u_ref) / u_ref^2]^-1."""
+        """NFW from the circular velocity v_c (kpc/Myr) at r_ref (default r_s),
+        as gala computes it (NFWPotential._vc_rs_rref_to_m,
+        src/gala/potential/potential/builtin/core.py:866-870): with u = r_ref / r_s,
+        G m / r_s = v_c^2 / u / (ln(1 + u) / u^2 - 1 / (u (1 + u))), i.e. the circular
+        speed at r_ref is v_c.  (The formula in gala's docstring differs from its code.)"""
+        def galactic(x, unit):  # quantities (anything with to_value) to galactic units
+            return x.to_value(unit) if hasattr(x, "to_value") else x
+
+        v_c, r_s = galactic(v_c, "kpc / Myr"), galactic(r_s, "kpc")
         if r_ref is None:
             r_ref = r_s
+        r_ref = galactic(r_ref, "kpc")
         u = r_ref / r_s
-        m = v_c ** 2 / u / (u / (1 + u) - np.log(1 + u) / u ** 2) * r_s / G_GALACTIC
+        m = r_s * (v_c ** 2 / u / (np.log(1 + u) / u ** 2 - 1 / (u * (1 + u)))) / G_GALACTIC
         return cls(m=m, r_s=r_s, a=a, b=b, c=c, units=units, origin=origin, R=R)
 
 

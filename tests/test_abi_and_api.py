@@ -318,3 +318,24 @@ def test_time_specification_with_quantities():
     np.testing.assert_allclose(t, [0.0, 1.0, 2.0, 3.0])
     t = parse_time_specification(None, t=_T([0.0, 0.5], "Gyr"))
     np.testing.assert_allclose(t, [0.0, 500.0])
+
+
+def test_nfw_from_circular_velocity_with_quantities():
+    """gala's TestSphericalNFWFromCircVel setting (test_all_builtin.py:286-300):
+    v_c = 220 km/s at r_ref = 8 kpc with r_s = 20 kpc; the circular speed at
+    r_ref is v_c (checked with the closed-form NFW enclosed mass)."""
+    class _V(_Quantity):
+        SCALE = {"km / s": g.units.KMS_TO_KPC_MYR, "kpc / Myr": 1.0, "kpc": 1.0}
+
+        def to_value(self, unit):
+            return np.asarray(self.value) * self.SCALE[self.unit] / self.SCALE[unit]
+
+    pot = g.NFWPotential.from_circular_velocity(v_c=_V(220.0, "km / s"), r_s=_V(20.0, "kpc"), r_ref=_V(8.0, "kpc"))
+    m, r_s, r = pot.parameters["m"], pot.parameters["r_s"], 8.0
+    menc = m * (np.log(1 + r / r_s) - (r / r_s) / (1 + r / r_s))
+    np.testing.assert_allclose(np.sqrt(g.units.G * menc / r), 220.0 * g.units.KMS_TO_KPC_MYR, rtol=1e-12)
+    for r_ref in (3.0, 8.0, 21.7234):                # gala's test_circ_vel radii, plain floats
+        p = g.NFWPotential.from_circular_velocity(v_c=0.22, r_s=20.0, r_ref=r_ref)
+        m, u = p.parameters["m"], r_ref / 20.0
+        v = np.sqrt(g.units.G * m * (np.log(1 + u) - u / (1 + u)) / r_ref)
+        np.testing.assert_allclose(v, 0.22, rtol=1e-12)

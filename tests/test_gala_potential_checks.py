@@ -306,3 +306,39 @@ def test_oracle_mass_enclosed(oracle):
 @pytest.mark.gpu
 def test_gpu_mass_enclosed():
     check_mass_enclosed(lambda pot: pot)
+
+
+# ---------------------------------------------------------------- NFW (test_all_builtin.py:255-342)
+def check_nfw(gradient, mass_enclosed):
+    """Flattened NFW differs from spherical (regression for gala issue #254);
+    from_circular_velocity gives v_c at r_ref; the enclosed mass follows
+    m (ln(1 + r/r_s) - (r/r_s) / (1 + r/r_s)) to 1e-6 for r in [1, 400] kpc."""
+    w0 = np.array([19.0, 2.7, -6.9])[:, None]
+    flat = g.NFWPotential(m=1e11, r_s=12.0, c=0.7)
+    sph = g.NFWPotential(m=1e11, r_s=12.0)
+    assert not np.allclose(gradient(flat, w0), gradient(sph, w0))
+    vc = 220.0 * g.units.KMS_TO_KPC_MYR
+    for r_ref in (3.0, 8.0, 21.7234):
+        pot = g.NFWPotential.from_circular_velocity(v_c=vc, r_s=20.0, r_ref=r_ref)
+        q = np.array([[r_ref], [0.0], [0.0]])
+        assert np.allclose(np.sqrt(r_ref * np.abs(gradient(pot, q)[0, 0])), vc)
+    pot = g.NFWPotential.from_circular_velocity(v_c=vc, r_s=20.0, r_ref=8.0)
+    m, rs = pot.parameters["m"], pot.parameters["r_s"]
+    r = np.linspace(1.0, 400.0, 100)
+    R = np.zeros((3, len(r)))
+    R[0] = r
+    true = m * (np.log(1 + r / rs) - (r / rs) / (1 + r / rs))
+    assert np.allclose(true, mass_enclosed(pot, R), rtol=1e-6)
+
+
+def test_oracle_nfw_checks(oracle):
+    def menc(pot, R):
+        pot.energy = lambda q, t=0.0: oracle.energy(pot, q, t)
+        return pot.mass_enclosed(R)
+
+    check_nfw(lambda pot, q: oracle.gradient(pot, q), menc)
+
+
+@pytest.mark.gpu
+def test_gpu_nfw_checks():
+    check_nfw(lambda pot, q: pot.gradient(q), lambda pot, R: pot.mass_enclosed(R))

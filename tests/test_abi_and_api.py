@@ -339,3 +339,13 @@ def test_nfw_from_circular_velocity_with_quantities():
         m, u = p.parameters["m"], r_ref / 20.0
         v = np.sqrt(g.units.G * m * (np.log(1 + u) - u / (1 + u)) / r_ref)
         np.testing.assert_allclose(v, 0.22, rtol=1e-12)
+
+
+def test_component_limit_is_refused_clearly():
+    """More than GX_MAX_COMPONENTS components cannot be packed (gala has no limit)."""
+    comp = g.CompositePotential(**{f"h{i}": g.HernquistPotential(m=1e9, c=0.1, origin=[0.01 * i, 0, 0])
+                                   for i in range(_abi.GX_MAX_COMPONENTS + 1)})
+    with pytest.raises(ValueError, match="exceed the limit"):
+        comp.packed()
+    ok = g.CompositePotential(**{f"h{i}": g.HernquistPotential(m=1e9, c=0.1) for i in range(_abi.GX_MAX_COMPONENTS)})
+    assert ok.packed().desc.n_components == _abi.GX_MAX_COMPONENTS

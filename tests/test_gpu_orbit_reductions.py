@@ -136,3 +136,47 @@ def test_guiding_radius_and_periods_match_oracle(oracle):
     P = orbit.estimate_period()
     for k, name in enumerate("xyz"):
         np.testing.assert_array_equal(P[name], [OO.peak_to_peak_period(t, w[k, :, n]) for n in range(32)])
+
+
+def test_gala_orbit_settings():
+    """gala's test_orbit.py on the CUDA path:
+    * test_guiding_radius (:363-380): Hernquist runs quietly, NFW with b = 0.95 warns;
+    * test_apocenter_pericenter_period (:383-446), point mass with G m = 4 pi^2 (gala's
+      solar-system numbers): apo- and pericentre within 1e-2 of the roots of
+      2 (E - Phi(r)) - L^2 / r^2, scatter of the individual extrema below 1e-4,
+      and the multi-orbit approximate calls."""
+    import warnings
+
+    from scipy import optimize as so
+
+    for pot, warns in ((g.HernquistPotential(m=1e10, c=10.0), False),
+                       (g.NFWPotential(m=1e10, r_s=10.0, b=0.95), True)):
+        vc = pot.circular_velocity(np.array([[10.0], [0.0], [0.0]]))[0]
+        orbit = pot.integrate_orbit(np.array([10.0, 0, 0, 0, 1.3 * vc, 0]), dt=0.5, n_steps=1000,
+                                    Integrator="dop853")
+        if warns:
+            with pytest.warns(RuntimeWarning):
+                orbit.guiding_radius()
+        else:
+            with warnings.catch_warnings():
+                warnings.simplefilter("error")
+                assert np.isfinite(orbit.guiding_radius())
+
+    pot = g.KeplerPotential(m=4 * np.pi ** 2 / g.units.G)
+    w = pot.integrate_orbit(np.array([1.0, 0, 0, 0, 1.5 * np.pi, 0]), dt=0.01, n_steps=10000, Integrator="dop853")
+    apo, per, zmax = w.apocenter(), w.pericenter(), w.zmax()
+    assert np.shape(apo) == np.shape(per) == np.shape(zmax) == () and apo > per
+    E = np.mean(w.energy())
+    L = np.mean(np.linalg.norm(w.angular_momentum(), axis=0))
+
+    def func(r):
+        return 2 * (E - pot.energy(np.array([[r], [0.0], [0.0]]))[0]) - L ** 2 / r ** 2
+
+    assert np.isclose(apo, so.brentq(func, 0.9, 1.0), rtol=1e-2)
+    assert np.isclose(per, so.brentq(func, 0.3, 0.5), rtol=1e-2)
+    apos, pers = np.asarray(w.apocenter(func=None)), np.asarray(w.pericenter(func=None))
+    assert 0 < np.std(apos) / np.mean(apos) < 1e-4 and 0 < np.std(pers) / np.mean(pers) < 1e-4
+    w2 = pot.integrate_orbit(np.array([[1.0, 1.1], [0, 0], [0, 0], [0, 0], [1.5 * np.pi] * 2, [0, 0]]), dt=0.01,
+                             n_steps=10000)
+    for f in (w2.pericenter, w2.apocenter, w2.zmax, w2.eccentricity):
+        assert np.shape(f(approximate=True)) == (2,)

@@ -152,3 +152,57 @@ def test_estimate_period_known_answer_and_gala(oracle):
     assert np.isnan(D.peak_to_peak_period(np.arange(5.0), np.zeros(5)))
     with pytest.raises(ValueError, match="time array"):
         g.Orbit(pos=w2[:3], vel=w2[3:]).estimate_period()
+
+
+# -------------------------------------------------- gala's tests/dynamics/test_orbit.py settings
+def test_peak_to_peak_period_known_answer():
+    """test_estimate_period (test_orbit.py:449-470): R(t) = 0.25 sin(2 pi t / T) + 1
+    over t in [0, 10] with 16384 samples gives T to 1e-3; the azimuth 2 pi t mod
+    2 pi gives 1."""
+    from gala_gb300.dynamics import peak_to_peak_period
+
+    t = np.linspace(0, 10.0, 16384)
+    for true_T in (1.0, 2.0, 4.123):
+        R = 0.25 * np.sin(2 * np.pi / true_T * t) + 1.0
+        assert np.isclose(peak_to_peak_period(t, R), true_T, rtol=1e-3)
+        assert np.isclose(OO.peak_to_peak_period(t, R), true_T, rtol=1e-3)
+    phi = (2 * np.pi * t) % (2 * np.pi)
+    assert np.isclose(peak_to_peak_period(t, phi), 1.0, rtol=1e-3)
+    pos = np.zeros((3, len(t)))
+    pos[0], pos[1] = np.cos(phi), np.sin(phi)
+    P = g.Orbit(pos=pos, vel=np.zeros_like(pos), t=t).estimate_period()
+    assert set(P) == {"x", "y", "z"}
+
+
+def _gala_guiding_cases():
+    """test_guiding_radius (test_orbit.py:363-380): from (10, 0, 0) kpc at 1.3 v_c in
+    a Hernquist sphere (no warning) and in an NFW halo with b = 0.95 (warning)."""
+    cases = []
+    for pot, warns in ((g.HernquistPotential(m=1e10, c=10.0), False),
+                       (g.NFWPotential(m=1e10, r_s=10.0, b=0.95), True)):
+        cases.append((pot, warns))
+    return cases
+
+
+def test_gala_guiding_radius_setting_oracle(oracle):
+    import warnings
+
+    import pytest
+
+    t = g.parse_time_specification(dt=0.5, n_steps=1000)
+    for pot, warns in _gala_guiding_cases():
+        q = np.array([[10.0], [0.0], [0.0]])
+        vc = np.sqrt(10.0 * np.abs(oracle.gradient(pot, q)[0, 0]))
+        w0 = np.array([[10.0], [0.0], [0.0], [0.0], [1.3 * vc], [0.0]])
+        w, st, _ = oracle.dop853(pot, w0, t)
+        assert np.all(st == 1)
+        orbit = g.Orbit.from_w(w[:, :, 0], t=t)
+        hp = _HostPotential(oracle, pot)
+        if warns:
+            with pytest.warns(RuntimeWarning):
+                orbit.guiding_radius(potential=hp)
+        else:
+            with warnings.catch_warnings():
+                warnings.simplefilter("error")
+                Rg = orbit.guiding_radius(potential=hp)
+            assert 10.0 < Rg < 30.0   # 1.3 v_c: outside the start, the orbit's apocentre side

@@ -349,3 +349,33 @@ def test_hdf5_random_trees_round_trip(tmp_path):
         else:
             assert np.array_equal(got, v) and np.asarray(got).dtype == np.asarray(v).dtype, path
         assert r[path].attrs[an] == av
+
+
+@pytest.mark.parametrize("config", ["plain", "time", "frame", "frame+potential"])
+def test_gala_orbit_io_cases(tmpdir, config):
+    """gala's test_io (tests/dynamics/test_orbit.py:610-641): the four orbits written
+    into an open file and read back by name, with frame and potential equal."""
+    x = np.array([[1, 2, 3.0], [1, 2, 3.0]]).T
+    v = np.array([[1, 2, 3.0], [1, 2, 3.0]]).T * g.units.KMS_TO_KPC_MYR
+    kw = {}
+    if config != "plain":
+        kw["t"] = [5.0, 99.0]
+    if "frame" in config:
+        kw["frame"] = g.StaticFrame()
+    if "potential" in config:
+        kw["potential"] = g.HernquistPotential(m=1e10, c=0.5)
+    obj = g.Orbit(pos=x, vel=v, **kw)
+    fn = str(tmpdir.join("thing.hdf5"))
+    with hdf5.File(fn, "w") as f:
+        obj.to_hdf5(f)
+    obj2 = g.Orbit.from_hdf5(fn)
+    assert np.allclose(obj.xyz, obj2.xyz) and np.allclose(obj.v_xyz, obj2.v_xyz)
+    if obj.t is not None:
+        assert np.allclose(obj.t, obj2.t)
+    else:
+        assert obj2.t is None
+    assert type(obj.frame) is type(obj2.frame)
+    if obj.potential is None:
+        assert obj2.potential is None
+    else:
+        assert pio.to_dict(obj.potential) == pio.to_dict(obj2.potential)

@@ -550,3 +550,24 @@ def test_directnbody_leapfrog(oracle):
     idx = np.array([1, 2, 0])
     ref = oracle.leapfrog_nbody(pot, pack_bodies([pps[i] for i in idx]), 2, w0[:, idx].T, t)[:, np.argsort(idx)]
     assert _scale_err(np.moveaxis(orbit.w(), 0, -1), ref) < 1e-11
+
+
+@pytest.mark.parametrize("sparse", [False, True])
+def test_leapfrog_progenitor_reaches_the_final_time(sparse):
+    """gala's regression tests (tests/dynamics/mockstream/test_mockstream.py:663-753): with
+    the Leapfrog integrator the progenitor (a test particle here) ends where a direct
+    Leapfrog orbit ends, whether particles are released every step or every fifth step
+    with none at the last one.  gala uses MilkyWayPotential(version="latest"); v1 here.
+    On the oracle the two agree bit for bit."""
+    from gala_gb300.mockstream import ChenStreamDF
+
+    mw = g.MilkyWayPotential()
+    K = g.units.KMS_TO_KPC_MYR
+    w0 = np.array([13.0, 0.0, 20.0, 0.0, 130.0 * K, 50.0 * K])
+    t = np.arange(0.0, 200.0 if sparse else 100.0, 1.0)
+    n = np.zeros(len(t), dtype=int)
+    n[:: 5 if sparse else 1] = 1
+    gen = MockStreamGenerator(ChenStreamDF(random_state=np.random.RandomState(1)), g.Hamiltonian(mw))
+    _, prog = gen.run(g.PhaseSpacePosition.from_w(w0), 2.5e4, n_particles=n, t=t, Integrator="leapfrog")
+    expected = mw.integrate_orbit(w0, t=t, Integrator="leapfrog").w()[:3, -1]
+    np.testing.assert_allclose(prog.xyz.squeeze(), expected, rtol=1e-10, atol=1e-10)

@@ -322,3 +322,33 @@ def test_chen_release_geometry(oracle):
                                        atol=1e-12 * rj)
             np.testing.assert_allclose(out[row, 3:] - w[i, 3:], dv @ np.stack([e0, e1, e2]), rtol=0,
                                        atol=1e-12 * abs(Dv) + 1e-15)
+
+
+def test_leapfrog_progenitor_reaches_the_final_time_oracle(oracle):
+    """gala's Leapfrog regression tests (test_mockstream.py:663-753) on the oracle's
+    mockstream_leapfrog: with releases every step, or every fifth step and none at
+    the last, the progenitor's final position is the direct Leapfrog orbit's, bit for
+    bit (gala compares positions); its velocity is within an ulp, since the release
+    stage restarts Leapfrog from (x, v) at the last release and re-forms the
+    half-step velocity there."""
+    from gala_gb300.mockstream import ChenStreamDF
+    from gala_gb300.nbody import pack_bodies
+
+    mw = g.MilkyWayPotential()
+    K = g.units.KMS_TO_KPC_MYR
+    w0 = np.array([13.0, 0, 20.0, 0, 130 * K, 50 * K])
+    bodies = pack_bodies([None])
+    for sparse in (False, True):
+        t = np.arange(0, 200.0 if sparse else 100.0, 1.0)
+        counts = np.zeros(len(t), dtype=np.int64)
+        counts[:: 5 if sparse else 1] = 1
+        orb = oracle.leapfrog_nbody(mw, bodies, 1, w0.reshape(1, 6), t)
+        offset = np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)
+        draws = ChenStreamDF(random_state=np.random.RandomState(1))._draws(int(offset[-1]))
+        sw0 = oracle.stream_sample(mw, orb.reshape(len(t), 6), np.full(len(t), 2.5e4), t, offset, 2, draws, g.units.G)
+        rel = np.nonzero(counts > 0)[0]
+        ref_nb, _ = oracle.mockstream_leapfrog(mw, bodies, orb[0].reshape(1, 6), t, sw0, t[rel], t[-1],
+                                               2 * counts[rel])
+        direct = oracle.fixed(mw, w0[:, None], t, "leapfrog")[:, -1, 0]
+        assert np.array_equal(ref_nb.reshape(-1)[:3], direct[:3])
+        np.testing.assert_allclose(ref_nb.reshape(-1)[3:6], direct[3:], rtol=1e-15, atol=0)

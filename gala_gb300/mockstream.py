@@ -86,6 +86,26 @@ class MockStream(PhaseSpacePosition):
         return cls(pos=obj.pos, vel=obj.vel, frame=obj.frame, release_time=t, lead_trail=lt)
 
 
+def split_releases(nstream, cap):
+    """Release systems of at most ``cap`` particles: a release with more is cut
+    into consecutive groups at the same time, each integrated with its own copy
+    of the bodies.  Returns (src, sizes): the release each group belongs to and
+    its particle count, in row order.  With Leapfrog this is exact -- the
+    particles are test particles on fixed steps, so the bodies' trajectory and
+    each particle's are the same in any grouping."""
+    src, sizes = [], []
+    for i, n in enumerate(np.asarray(nstream, dtype=np.int64)):
+        n = int(n)
+        if n <= cap:
+            src.append(i)
+            sizes.append(n)
+            continue
+        for k in range(0, n, cap):
+            src.append(i)
+            sizes.append(min(cap, n - k))
+    return np.array(src, dtype=np.int64), np.array(sizes, dtype=np.int64)
+
+
 class BaseStreamDF:
     """Release distribution of stream particles (df.pyx:34-121)."""
 
@@ -443,7 +463,10 @@ class MockStreamGenerator:
                                             **dop)
             check(st, "nbody")
         if nb + max_per > 32:
-            raise NotImplementedError(f"{nb} bodies + {max_per} particles per release exceed the 32-lane system")
+            raise NotImplementedError(
+                f"{nb} bodies + {max_per} particles released at one time exceed the 32-lane DOP853 system; gala "
+                "integrates a release as one system sharing a step size, so it cannot be split without changing "
+                "the result: release fewer particles per time, or use the Leapfrog integrator (splits exactly)")
         n_rel = len(time)
         stream_out = torch.empty((S, n_rows, 6), dtype=torch.float64, device=dev)
         nbody_out = torch.empty((S, nb, 6), dtype=torch.float64, device=dev)
@@ -470,8 +493,14 @@ class MockStreamGenerator:
         H = self.hamiltonian
         S, nb = bodies.shape
         dev = orbit.device
-        if nb + max_per > 8:
-            raise NotImplementedError(f"{nb} bodies + {max_per} particles per release exceed the 8-body system")
+        cap = 8 - nb  # the kernel's systems hold 8 bodies and particles
+        if cap < 1:
+            raise NotImplementedError(f"{nb} bodies exceed the 8-body Leapfrog system")
+        if max_per > cap:  # larger releases in groups at the same time (exact, see split_releases)
+            src, sizes = split_releases(nstream, cap)
+            time, nstream = time[src], sizes
+            rel_off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+            max_per = int(sizes.max())
         # the bodies' trajectory on the full grid; the same call as stage 1 when the grid runs forwards
         traj = orbit if forward else integrate_systems_leapfrog(H, bodies, nbody0, orbit_t, save_all=True,
                                                                 stream=stream)

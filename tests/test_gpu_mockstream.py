@@ -571,3 +571,37 @@ def test_leapfrog_progenitor_reaches_the_final_time(sparse):
     _, prog = gen.run(g.PhaseSpacePosition.from_w(w0), 2.5e4, n_particles=n, t=t, Integrator="leapfrog")
     expected = mw.integrate_orbit(w0, t=t, Integrator="leapfrog").w()[:3, -1]
     np.testing.assert_allclose(prog.xyz.squeeze(), expected, rtol=1e-10, atol=1e-10)
+
+
+def test_large_leapfrog_release_and_dop853_burst(oracle):
+    """gala's one-burst setting (test_mockstream_class.py:41-97) through the generator:
+    with Leapfrog the 2000 particles released at once run as groups of 7 with copies
+    of the progenitor (split_releases, bit-identical to one system on the oracle) and
+    match the oracle's single system; with DOP853 a release larger than a 32-lane
+    system is refused.  The particles are released at the pericentre of a near-radial
+    orbit, next to a 4 pc progenitor: a few of them amplify any rounding difference
+    (the sampler's d2Phi/dr2, CUDA's log) up to 1e-4 of the scale, while the bulk is
+    unaffected.  So the stream is held to its distribution -- median below 1e-8 and
+    90th percentile below 1e-7 of the scale (1e-10 and 2e-10 when the oracle's own
+    release states are perturbed by 2e-9) -- and the progenitor to 1e-10."""
+    from .test_mockstream_oracle import _one_burst
+
+    pot, bodies, orb, t, sw0, rel, counts = _one_burst(oracle, leapfrog=True)
+    ref_nb, ref_st = oracle.mockstream_leapfrog(pot, bodies, orb[0].reshape(1, 6), t, sw0, t[rel], t[-1],
+                                                2 * counts[rel])
+    K = g.units.KMS_TO_KPC_MYR
+    w0 = np.array([10.0, 0, 0, 0, 10 * K, 0])
+
+    def gen():
+        return MockStreamGenerator(FardalStreamDF(gala_modified=True, random_state=np.random.default_rng(seed=42)),
+                                   g.Hamiltonian(pot), progenitor_potential=g.PlummerPotential(m=2.5e4, b=0.004))
+
+    stream, nbody = gen().run(g.PhaseSpacePosition.from_w(w0), 2.5e4, n_particles=counts, dt=1.0, n_steps=100,
+                              Integrator="leapfrog")
+    got = np.vstack([stream.xyz, stream.v_xyz]).T
+    assert got.shape == ref_st.shape
+    err = np.linalg.norm(got - ref_st, axis=1) / np.abs(ref_st).max()
+    assert np.median(err) < 1e-8 and np.quantile(err, 0.9) < 1e-7, np.quantile(err, [0.5, 0.9, 1.0])
+    assert _scale_err(np.vstack([nbody.xyz, nbody.v_xyz]).T, ref_nb) < 1e-10
+    with pytest.raises(NotImplementedError, match="32-lane"):
+        gen().run(g.PhaseSpacePosition.from_w(w0), 2.5e4, n_particles=counts, dt=1.0, n_steps=100)

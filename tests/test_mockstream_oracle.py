@@ -352,3 +352,59 @@ def test_leapfrog_progenitor_reaches_the_final_time_oracle(oracle):
         direct = oracle.fixed(mw, w0[:, None], t, "leapfrog")[:, -1, 0]
         assert np.array_equal(ref_nb.reshape(-1)[:3], direct[:3])
         np.testing.assert_allclose(ref_nb.reshape(-1)[3:6], direct[3:], rtol=1e-15, atol=0)
+
+
+def _one_burst(oracle, leapfrog=False):
+    """gala's test_one_burst setting (tests/dynamics/mockstream/test_mockstream_class.py:41-97):
+    NFW from v_c = 232.8 km/s at 8.2 kpc (r_s = 15), progenitor from (10, 0, 0) kpc at
+    10 km/s with a Plummer potential (2.5e4 Msun, b = 4 pc), 1000 particles per tail
+    released at the minimum radius of the 100-step Leapfrog orbit, Fardal draws from
+    numpy.random.default_rng(42)."""
+    from gala_gb300.mockstream import FardalStreamDF
+
+    K = g.units.KMS_TO_KPC_MYR
+    pot = g.NFWPotential.from_circular_velocity(v_c=232.8 * K, r_s=15.0, r_ref=8.2)
+    w0 = np.array([10.0, 0, 0, 0, 10 * K, 0])
+    t = g.parse_time_specification(dt=1.0, n_steps=100)
+    r = np.linalg.norm(oracle.fixed(pot, w0[:, None], t, "leapfrog")[:3, :, 0], axis=0)
+    counts = np.zeros(len(t), dtype=np.int64)
+    counts[r[0:150].argmin()] = 1000
+    bodies = pack_bodies([g.PlummerPotential(m=2.5e4, b=0.004)])
+    if leapfrog:
+        orb = oracle.leapfrog_nbody(pot, bodies, 1, w0.reshape(1, 6), t)
+    else:
+        orb, res = oracle.nbody_dop853(pot, bodies, 1, w0.reshape(1, 6), t)
+        assert res == 1
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.default_rng(seed=42))
+    offset = np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)
+    sw0 = oracle.stream_sample(pot, orb.reshape(len(t), 6), np.full(len(t), 2.5e4), t, offset, 0,
+                               df._draws(int(offset[-1])), g.units.G)
+    rel = np.insert(np.nonzero(counts > 0)[0], 0, 0)
+    return pot, bodies, orb, t, sw0, rel, counts
+
+
+def test_one_burst_reproduces_galas_values(oracle):
+    """The whole stream pipeline on the oracle -- sampling, the progenitor's n-body
+    DOP853 and one 2001-particle release system -- reproduces the values gala's test
+    asserts (test_mockstream_class.py:84-97, given to 8-9 digits)."""
+    pot, bodies, orb, t, sw0, rel, counts = _one_burst(oracle)
+    nb, st, status = oracle.mockstream_dop853(pot, bodies, orb[0].reshape(1, 6), t[rel], sw0, t[rel], t[-1],
+                                              2 * counts[rel])
+    stream0 = [-10.07444187, -1.37424641, 0.06310397, -0.05672946, -0.01837671, 0.00038504]
+    prog = [-9.72388107, -1.28632464, 0.0, -0.04714419, -0.016754, 0.0]
+    np.testing.assert_allclose(st[0], stream0, rtol=0, atol=1e-8)
+    np.testing.assert_allclose(nb.reshape(-1)[:6], prog, rtol=0, atol=1e-8)
+
+
+def test_leapfrog_release_split_is_exact(oracle):
+    """Releases larger than a Leapfrog system are integrated in groups at the same
+    time (split_releases); the result is bit-identical to one system per release."""
+    from gala_gb300.mockstream import split_releases
+
+    src, sizes = split_releases([0, 20, 3, 7], 7)
+    assert src.tolist() == [0, 1, 1, 1, 2, 3] and sizes.tolist() == [0, 7, 7, 6, 3, 7]
+    pot, bodies, orb, t, sw0, rel, counts = _one_burst(oracle, leapfrog=True)
+    nb1, st1 = oracle.mockstream_leapfrog(pot, bodies, orb[0].reshape(1, 6), t, sw0, t[rel], t[-1], 2 * counts[rel])
+    src, sizes = split_releases(2 * counts[rel], 7)
+    nb2, st2 = oracle.mockstream_leapfrog(pot, bodies, orb[0].reshape(1, 6), t, sw0, t[rel][src], t[-1], sizes)
+    assert len(src) > 200 and np.array_equal(st1, st2) and np.array_equal(nb1, nb2)

@@ -241,6 +241,14 @@ class PhaseSpacePosition:
     def xyz(self):
         return self.pos
 
+    # gala's component attributes
+    x = property(lambda self: self.pos[0])
+    y = property(lambda self: self.pos[1])
+    z = property(lambda self: self.pos[2])
+    v_x = property(lambda self: self.vel[0])
+    v_y = property(lambda self: self.vel[1])
+    v_z = property(lambda self: self.vel[2])
+
     @property
     def v_xyz(self):
         return self.vel

@@ -30,7 +30,7 @@ import warnings
 import numpy as np
 
 from . import _abi, units
-from .dynamics import PhaseSpacePosition, _h5_open, quantity_from_hdf5, quantity_to_hdf5
+from .dynamics import PhaseSpacePosition, _galactic, _h5_open, quantity_from_hdf5, quantity_to_hdf5
 from .hamiltonian import Hamiltonian, StaticFrame
 from .integrate import DOPRI853Integrator, LeapfrogIntegrator, get_integrator, parse_time_specification
 from .nbody import DirectNBody, bodies_to_device, integrate_systems, integrate_systems_leapfrog, pack_bodies
@@ -206,7 +206,7 @@ class BaseStreamDF:
         t = np.asarray(prog_orbit.t, dtype=np.float64)
         ntimes = len(t)
         prog_w = np.ascontiguousarray(np.vstack([x, v]).T.reshape(1, ntimes, 6))
-        m = np.squeeze(np.asarray(getattr(prog_mass, "value", prog_mass), dtype=np.float64))
+        m = np.squeeze(_galactic(prog_mass, "Msun"))
         m = np.full(ntimes, float(m)) if m.shape == () else m
         counts = self.release_counts(ntimes, release_every, n_particles)
         dev = require_cuda()
@@ -279,7 +279,7 @@ class LagrangeCloudStreamDF(BaseStreamDF):
 
     def __init__(self, v_disp, lead=True, trail=True, random_state=None):
         super().__init__(lead=lead, trail=trail, random_state=random_state)
-        self.v_disp = float(getattr(v_disp, "value", v_disp))
+        self.v_disp = float(_galactic(v_disp, "km / s"))  # km/s, as gala's parameter is given
         self._v_disp = self.v_disp * units.KMS_TO_KPC_MYR
 
     def _draws(self, n_rows):
@@ -543,7 +543,7 @@ class MockStreamGenerator:
             raise NotImplementedError("null-potential bodies must come after the massive ones")
         nb = len(prog_nbody.particle_potentials)
         bodies = pack_bodies([prog_nbody.particle_potentials])
-        m = np.squeeze(np.asarray(getattr(prog_mass, "value", prog_mass), dtype=np.float64))
+        m = np.squeeze(_galactic(prog_mass, "Msun"))
         m = np.full(len(t), float(m)) if m.shape == () else m
         counts = self.df.release_counts(len(t), release_every, n_particles)
         dop, err_if_fail = self._dop_kwargs(kw_in if Integrator is DOPRI853Integrator else {})
@@ -573,7 +573,7 @@ class MockStreamGenerator:
         if len(progenitor_potentials) != S:
             raise ValueError("one progenitor potential per stream is needed")
         bodies = pack_bodies([[p] for p in progenitor_potentials]).reshape(S, 1)
-        m = np.asarray(prog_mass, dtype=np.float64)
+        m = _galactic(prog_mass, "Msun")
         if m.ndim == 0:
             m = np.full((S, len(t)), float(m))
         elif m.ndim == 1:

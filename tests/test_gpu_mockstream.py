@@ -605,3 +605,26 @@ def test_large_leapfrog_release_and_dop853_burst(oracle):
     assert _scale_err(np.vstack([nbody.xyz, nbody.v_xyz]).T, ref_nb) < 1e-10
     with pytest.raises(NotImplementedError, match="32-lane"):
         gen().run(g.PhaseSpacePosition.from_w(w0), 2.5e4, n_particles=counts, dt=1.0, n_steps=100)
+
+
+_DF_CASES = [("streakline", {}), ("fardal", {"gala_modified": True}), ("lagrange", {"v_disp": 1.0})]
+
+
+@pytest.mark.parametrize("which,kw", _DF_CASES)
+@pytest.mark.parametrize("pot", ["hernquist", "milkyway"])
+def test_df_sample_like_gala(which, kw, pot):
+    """gala's test_init_sample (tests/dynamics/mockstream/test_df.py:24-52): two particles
+    per time with both tails, one with either tail off, identical output for identical
+    random states (gala zips its kwargs list, so ChenStreamDF is not sampled there)."""
+    from gala_gb300.mockstream import LagrangeCloudStreamDF, StreaklineStreamDF
+
+    DF = {"streakline": StreaklineStreamDF, "fardal": FardalStreamDF, "lagrange": LagrangeCloudStreamDF}[which]
+    p = g.HernquistPotential(m=1e12, c=5.0) if pot == "hernquist" else g.MilkyWayPotential()
+    orbit = g.Hamiltonian(p).integrate_orbit(np.array([10.0, 0, 0, 0, 0.2, 0]), dt=1.0, n_steps=100)
+    n = len(orbit.t)
+    assert len(DF(**kw).sample(orbit, 1e4).x) == 2 * n
+    assert len(DF(lead=False, **kw).sample(orbit, 1e4).x) == n
+    assert len(DF(trail=False, **kw).sample(orbit, 1e4).x) == n
+    o1 = DF(random_state=np.random.RandomState(42), **kw).sample(orbit, 1e4)
+    o2 = DF(random_state=np.random.RandomState(42), **kw).sample(orbit, 1e4)
+    assert np.array_equal(o1.xyz, o2.xyz) and np.array_equal(o1.v_xyz, o2.v_xyz) and len(o1.x) == 2 * n

@@ -408,3 +408,13 @@ def test_leapfrog_release_split_is_exact(oracle):
     src, sizes = split_releases(2 * counts[rel], 7)
     nb2, st2 = oracle.mockstream_leapfrog(pot, bodies, orb[0].reshape(1, 6), t, sw0, t[rel][src], t[-1], sizes)
     assert len(src) > 200 and np.array_equal(st1, st2) and np.array_equal(nb1, nb2)
+
+
+def test_dfs_refuse_no_tails():
+    """gala's test_expected_failure (test_df.py:55-58) for every DF."""
+    from gala_gb300.mockstream import ChenStreamDF, FardalStreamDF, LagrangeCloudStreamDF, StreaklineStreamDF
+
+    for DF, kw in ((StreaklineStreamDF, {}), (FardalStreamDF, {"gala_modified": True}),
+                   (LagrangeCloudStreamDF, {"v_disp": 1.0}), (ChenStreamDF, {})):
+        with pytest.raises(ValueError):
+            DF(lead=False, trail=False, **kw)

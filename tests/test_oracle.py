@@ -125,3 +125,24 @@ def test_dop853_out_stride_consistent(oracle):
     full, _, _ = oracle.dop853(mw, w0, t, nbatch=4)
     strided, _, _ = oracle.dop853(mw, w0, t, nbatch=4, out_stride=7)
     assert np.array_equal(full[:, ::7, :], strided)
+
+
+def test_dop853_status_for_non_finite_initial_conditions():
+    """A NaN or infinite initial condition: gala's dop853() built with IEEE arithmetic
+    reports -2 (nmax exceeded) and its -Ofast release build -3 (step too small) -- the
+    comparisons that decide it are undefined under fast-math.  The restatement gives
+    the same code in either build; the other orbit's batch is unaffected."""
+    from oracle import Oracle
+    from oracle.oracle import ref_available
+
+    if not ref_available():
+        pytest.skip("gala's own objects are not built here")
+    pot = g.HernquistPotential(m=1e11, c=1.0)
+    t = g.parse_time_specification(dt=1.0, n_steps=50)
+    for bad in (np.nan, np.inf):
+        w0 = np.array([[8.0, 8.0], [0, 0], [0, 0], [0, 0], [0.2, 0.2], [0, 0]])
+        w0[0, 1] = bad
+        for mine, gala, code in (("strict", "ref_strict", -2), ("fast", "ref", -3)):
+            st_mine = Oracle(mine).dop853(pot, w0, t, nbatch=1)[1]
+            st_gala = Oracle(gala).dop853(pot, w0, t, nbatch=1)[1]
+            assert st_mine.tolist() == st_gala.tolist() == [1, code]

@@ -20,7 +20,9 @@ def as_device_f64(a, device=None) -> torch.Tensor:
     """Contiguous float64 CUDA tensor view/copy of ``a`` (numpy, list or tensor)."""
     dev = device or require_cuda()
     if isinstance(a, torch.Tensor):
-        return a.to(device=dev, dtype=torch.float64).contiguous()
+        # a pinned host tensor is copied asynchronously on the current stream
+        nb = a.device.type == "cpu" and a.is_pinned()
+        return a.to(device=dev, dtype=torch.float64, non_blocking=nb).contiguous()
     arr = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
     if not arr.flags.writeable:
         arr = arr.copy()

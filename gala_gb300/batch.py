@@ -60,6 +60,17 @@ def schedule(n_steps, method, chunk):
     return chunks[order].reshape(-1).contiguous()
 
 
+def _to_device(a, tdtype, ndtype, dev):
+    """Contiguous CUDA tensor of `a` (numpy, list, or tensor); a pinned host
+    tensor is copied asynchronously on the current stream."""
+    import torch
+
+    if isinstance(a, torch.Tensor):
+        nb = a.device.type == "cpu" and a.is_pinned()
+        return a.to(device=dev, dtype=tdtype, non_blocking=nb).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=ndtype))).to(dev)
+
+
 def _potential_key(potential):
     pk = potential.packed()
     h = hashlib.sha1(pk.params.tobytes())
@@ -95,11 +106,9 @@ class BatchIntegrator:
         if self.w0.dim() != 2 or self.w0.shape[0] != 6:
             raise ValueError(f"w0 must have shape (6, N), got {tuple(self.w0.shape)}")
         self.n = self.w0.shape[1]
-        self.n_steps = torch.as_tensor(np.asarray(n_steps, dtype=np.int64) if not isinstance(n_steps, torch.Tensor)
-                                       else n_steps, dtype=torch.int64).to(self.dev).contiguous()
+        self.n_steps = _to_device(n_steps, torch.int64, np.int64, self.dev)
         self.dt = as_device_f64(dt)
-        self.method = torch.as_tensor(np.asarray(method, dtype=np.int32) if not isinstance(method, torch.Tensor)
-                                      else method, dtype=torch.int32).to(self.dev).contiguous()
+        self.method = _to_device(method, torch.int32, np.int32, self.dev)
         for name, a in (("n_steps", self.n_steps), ("dt", self.dt), ("method", self.method)):
             if a.shape != (self.n,):
                 raise ValueError(f"{name} must have shape ({self.n},), got {tuple(a.shape)}")
@@ -236,3 +245,53 @@ class BatchIntegrator:
             tmp.write_text(json.dumps(data, indent=1))
             os.replace(tmp, CACHE)
         return best
+
+
+_METHODS = {"leapfrog": LEAPFROG, "ruth4": RUTH4}
+
+
+def _method_codes(integrator, n):
+    if isinstance(integrator, str):
+        if integrator.lower() not in _METHODS:
+            raise ValueError(f"integrator must be 'leapfrog' or 'ruth4', got {integrator!r}")
+        return np.full(n, _METHODS[integrator.lower()], dtype=np.int32)
+    arr = np.asarray(integrator)
+    if arr.dtype.kind in "US":
+        bad = sorted({str(x) for x in arr.ravel() if str(x).lower() not in _METHODS})
+        if bad:
+            raise ValueError(f"unknown integrators {bad}: use 'leapfrog' or 'ruth4'")
+        return np.array([_METHODS[str(x).lower()] for x in arr.ravel()], dtype=np.int32)
+    return integrator
+
+
+@traced("integrate_batch")
+def integrate_batch(potential, w0, n_steps, dt, integrator, precision="fp32c", config=None, out=None):
+    """Integrate N orbits, each with its own ``n_steps``, ``dt`` and integrator,
+    in one launch of the persistent batch kernel.
+
+    ``integrator`` is 'leapfrog', 'ruth4', or an (N,) array of those names or of
+    codes 0 / 1.  Host inputs (numpy arrays or pinned CPU tensors) are copied
+    to the GPU on the current stream; the results come back the same way.
+
+    Returns ``(w, dE_over_E)``: the final states (6, N) at t = n_steps * dt
+    and the FP64 relative energy change |E(t_end) - E(0)| / |E(0)| per orbit --
+    numpy arrays for host inputs, CUDA tensors for device inputs.  ``out``
+    (host, optional) is a pair of pinned CPU tensors (6, N) and (N,) that
+    receive the results.
+    """
+    import torch
+
+    on_host = not (isinstance(w0, torch.Tensor) and w0.is_cuda)
+    n = (w0.shape[1] if hasattr(w0, "shape") else np.asarray(w0).shape[1])
+    method = _method_codes(integrator, n)
+    b = BatchIntegrator(potential, w0, n_steps, dt, method, config=config, precision=precision)
+    w = b.run()
+    dE = b.energy_drift()
+    if not on_host:
+        return w, dE
+    if out is not None:
+        out[0].copy_(w, non_blocking=True)
+        out[1].copy_(dE, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return out[0].numpy(), out[1].numpy()
+    return w.cpu().numpy(), dE.cpu().numpy()

@@ -90,70 +90,113 @@ static double comp_value(int type, const double *p, const double *q) {
 
 /* *_gradient_single: kepler :66-76, hernquist :221-233, plummer :302-314,
  * miyamotonagai :1298-1312, sphericalnfw :835-850, flattenednfw :944-962,
- * triaxialnfw :1051-1072, scf_gradient (bfe.cpp:229-259).  Accumulates into g. */
-static void comp_gradient(int type, const double *p, const double *q, double *g) {
-    double fac;
-    switch (type) {
-    case GX_POT_NULL:
-        return;
-    case GX_POT_KEPLER:
-        fac = p[0] * p[1] / pow(sqrt(norm3_sq(q)), 3);
-        break;
-    case GX_POT_HERNQUIST: {
-        const double r = sqrt(norm3_sq(q));
-        fac = p[0] * p[1] / ((r + p[2]) * (r + p[2]) * r);
-        break;
-    }
-    case GX_POT_PLUMMER: {
-        const double R2b = norm3_sq(q) + p[2] * p[2];
-        fac = p[0] * p[1] / sqrt(R2b) / R2b;
-        break;
-    }
-    case GX_POT_MIYAMOTONAGAI: {
-        const double sqrtz = sqrt(q[2] * q[2] + p[3] * p[3]);
-        const double zd = p[2] + sqrtz;
-        fac = p[0] * p[1] * pow(q[0] * q[0] + q[1] * q[1] + zd * zd, -1.5);
-        g[0] = g[0] + fac * q[0];
-        g[1] = g[1] + fac * q[1];
-        g[2] = g[2] + fac * q[2] * (1. + p[2] / sqrtz);
-        return;
-    }
-    case GX_POT_SPHERICALNFW: {
-        const double v_h2 = p[0] * p[1] / p[2];
-        const double u = sqrt(norm3_sq(q)) / p[2];
-        fac = v_h2 / (u * u * u) / (p[2] * p[2]) * (log(1 + u) - u / (1 + u));
-        break;
-    }
-    case GX_POT_FLATTENEDNFW: {
-        const double v_h2 = p[0] * p[1] / p[2];
-        const double u = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] / (p[5] * p[5])) / p[2];
-        fac = v_h2 / (u * u * u) / (p[2] * p[2]) * (log(1 + u) - u / (1 + u));
-        g[0] = g[0] + fac * q[0];
-        g[1] = g[1] + fac * q[1];
-        g[2] = g[2] + fac * q[2] / (p[5] * p[5]);
-        return;
-    }
-    case GX_POT_TRIAXIALNFW: {
-        const double v_h2 = p[0] * p[1] / p[2];
-        const double u = sqrt(q[0] * q[0] / (p[3] * p[3]) + q[1] * q[1] / (p[4] * p[4]) +
-                              q[2] * q[2] / (p[5] * p[5])) / p[2];
-        fac = v_h2 / (u * u * u) / (p[2] * p[2]) * (log(1 + u) - u / (1 + u));
-        g[0] = g[0] + fac * q[0] / (p[3] * p[3]);
-        g[1] = g[1] + fac * q[1] / (p[4] * p[4]);
-        g[2] = g[2] + fac * q[2] / (p[5] * p[5]);
-        return;
-    }
-    case GX_POT_SCF:
-        orc_scf_gradient(p, q, g);
-        return;
-    default:
-        g[0] = NAN; g[1] = NAN; g[2] = NAN;
-        return;
-    }
-    g[0] = g[0] + fac * q[0];
-    g[1] = g[1] + fac * q[1];
-    g[2] = g[2] + fac * q[2];
+ * triaxialnfw :1051-1072.  One point (x, y, z); accumulates into (gx, gy, gz).
+ * Written as inline functions so that the loops over points below vectorise
+ * as gala's gradientv loops do (vectorization.h): same per-point arithmetic. */
+static inline void grad_kepler(const double *p, double x, double y, double z, double *gx, double *gy, double *gz) {
+    const double fac = p[0] * p[1] / pow(sqrt(x * x + y * y + z * z), 3);
+    *gx = *gx + fac * x;
+    *gy = *gy + fac * y;
+    *gz = *gz + fac * z;
 }
+static inline void grad_hernquist(const double *p, double x, double y, double z, double *gx, double *gy,
+                                  double *gz) {
+    const double r = sqrt(x * x + y * y + z * z);
+    const double fac = p[0] * p[1] / ((r + p[2]) * (r + p[2]) * r);
+    *gx = *gx + fac * x;
+    *gy = *gy + fac * y;
+    *gz = *gz + fac * z;
+}
+static inline void grad_plummer(const double *p, double x, double y, double z, double *gx, double *gy, double *gz) {
+    const double R2b = x * x + y * y + z * z + p[2] * p[2];
+    const double fac = p[0] * p[1] / sqrt(R2b) / R2b;
+    *gx = *gx + fac * x;
+    *gy = *gy + fac * y;
+    *gz = *gz + fac * z;
+}
+static inline void grad_mn(const double *p, double x, double y, double z, double *gx, double *gy, double *gz) {
+    const double sqrtz = sqrt(z * z + p[3] * p[3]);
+    const double zd = p[2] + sqrtz;
+    const double fac = p[0] * p[1] * pow(x * x + y * y + zd * zd, -1.5);
+    *gx = *gx + fac * x;
+    *gy = *gy + fac * y;
+    *gz = *gz + fac * z * (1. + p[2] / sqrtz);
+}
+static inline void grad_snfw(const double *p, double x, double y, double z, double *gx, double *gy, double *gz) {
+    const double v_h2 = p[0] * p[1] / p[2];
+    const double u = sqrt(x * x + y * y + z * z) / p[2];
+    const double fac = v_h2 / (u * u * u) / (p[2] * p[2]) * (log(1 + u) - u / (1 + u));
+    *gx = *gx + fac * x;
+    *gy = *gy + fac * y;
+    *gz = *gz + fac * z;
+}
+static inline void grad_fnfw(const double *p, double x, double y, double z, double *gx, double *gy, double *gz) {
+    const double v_h2 = p[0] * p[1] / p[2];
+    const double u = sqrt(x * x + y * y + z * z / (p[5] * p[5])) / p[2];
+    const double fac = v_h2 / (u * u * u) / (p[2] * p[2]) * (log(1 + u) - u / (1 + u));
+    *gx = *gx + fac * x;
+    *gy = *gy + fac * y;
+    *gz = *gz + fac * z / (p[5] * p[5]);
+}
+static inline void grad_tnfw(const double *p, double x, double y, double z, double *gx, double *gy, double *gz) {
+    const double v_h2 = p[0] * p[1] / p[2];
+    const double u = sqrt(x * x / (p[3] * p[3]) + y * y / (p[4] * p[4]) + z * z / (p[5] * p[5])) / p[2];
+    const double fac = v_h2 / (u * u * u) / (p[2] * p[2]) * (log(1 + u) - u / (1 + u));
+    *gx = *gx + fac * x / (p[3] * p[3]);
+    *gy = *gy + fac * y / (p[4] * p[4]);
+    *gz = *gz + fac * z / (p[5] * p[5]);
+}
+
+/* One point of one component (scf_gradient: bfe.cpp:229-259).  Accumulates into g. */
+static void comp_gradient(int type, const double *p, const double *q, double *g) {
+    switch (type) {
+    case GX_POT_NULL: return;
+    case GX_POT_KEPLER: grad_kepler(p, q[0], q[1], q[2], &g[0], &g[1], &g[2]); return;
+    case GX_POT_HERNQUIST: grad_hernquist(p, q[0], q[1], q[2], &g[0], &g[1], &g[2]); return;
+    case GX_POT_PLUMMER: grad_plummer(p, q[0], q[1], q[2], &g[0], &g[1], &g[2]); return;
+    case GX_POT_MIYAMOTONAGAI: grad_mn(p, q[0], q[1], q[2], &g[0], &g[1], &g[2]); return;
+    case GX_POT_SPHERICALNFW: grad_snfw(p, q[0], q[1], q[2], &g[0], &g[1], &g[2]); return;
+    case GX_POT_FLATTENEDNFW: grad_fnfw(p, q[0], q[1], q[2], &g[0], &g[1], &g[2]); return;
+    case GX_POT_TRIAXIALNFW: grad_tnfw(p, q[0], q[1], q[2], &g[0], &g[1], &g[2]); return;
+    case GX_POT_SCF: orc_scf_gradient(p, q, g); return;
+    default: g[0] = NAN; g[1] = NAN; g[2] = NAN; return;
+    }
+}
+
+/* One component over N points, SoA q[3, N], accumulated into g[3, N]: the
+ * gradientv loop of vectorization.h (one pass per component). */
+#define GX_POINT_LOOP(FN)                                                                  \
+    for (size_t i = 0; i < N; i++) {                                                       \
+        double a = gx[i], b = gy[i], c = gz[i];                                            \
+        FN(p, qx[i], qy[i], qz[i], &a, &b, &c);                                            \
+        gx[i] = a;                                                                         \
+        gy[i] = b;                                                                         \
+        gz[i] = c;                                                                         \
+    }
+static void comp_gradient_n(int type, const double *p, size_t N, const double *restrict q, double *restrict g) {
+    const double *restrict qx = q, *restrict qy = q + N, *restrict qz = q + 2 * N;
+    double *restrict gx = g, *restrict gy = g + N, *restrict gz = g + 2 * N;
+    switch (type) {
+    case GX_POT_NULL: return;
+    case GX_POT_KEPLER: GX_POINT_LOOP(grad_kepler) return;
+    case GX_POT_HERNQUIST: GX_POINT_LOOP(grad_hernquist) return;
+    case GX_POT_PLUMMER: GX_POINT_LOOP(grad_plummer) return;
+    case GX_POT_MIYAMOTONAGAI: GX_POINT_LOOP(grad_mn) return;
+    case GX_POT_SPHERICALNFW: GX_POINT_LOOP(grad_snfw) return;
+    case GX_POT_FLATTENEDNFW: GX_POINT_LOOP(grad_fnfw) return;
+    case GX_POT_TRIAXIALNFW: GX_POINT_LOOP(grad_tnfw) return;
+    default:
+        for (size_t i = 0; i < N; i++) {
+            double qi[3] = {qx[i], qy[i], qz[i]}, gi[3] = {gx[i], gy[i], gz[i]};
+            comp_gradient(type, p, qi, gi);
+            gx[i] = gi[0];
+            gy[i] = gi[1];
+            gz[i] = gi[2];
+        }
+        return;
+    }
+}
+#undef GX_POINT_LOOP
 
 /* kepler_density :78-88, hernquist_density :235-244, plummer_density :316-324,
  * miyamotonagai_density :1314-1332, sphericalnfw_density :852-864,
@@ -283,15 +326,44 @@ static void gradient_point(const gx_potential *pot, const double *q, double *g) 
     }
 }
 
-/* c_gradient over N points, SoA q[3, N] -> grad[3, N] (overwritten). */
+/* c_gradient over N points, SoA q[3, N] -> grad[3, N] (overwritten): zero,
+ * then component by component over all points (:214-287).  A shifted/rotated
+ * component is evaluated on transformed points into a zeroed temporary, its
+ * gradients rotated back and added, in blocks of points. */
 void orc_gradient(const gx_potential *pot, size_t N, double t, const double *q, double *grad) {
     (void)t;
-    for (size_t i = 0; i < N; i++) {
-        double qi[3] = {q[i], q[N + i], q[2 * N + i]}, g[3];
-        gradient_point(pot, qi, g);
-        grad[i] = g[0];
-        grad[N + i] = g[1];
-        grad[2 * N + i] = g[2];
+    enum { BLK = 256 };
+    for (size_t i = 0; i < 3 * N; i++) grad[i] = 0.;
+    for (int ci = 0; ci < pot->n_components; ci++) {
+        const gx_component *c = &pot->components[ci];
+        const double *p = pot->params + c->param_offset;
+        if (c->do_shift_rotate == 0) {
+            comp_gradient_n(c->type, p, N, q, grad);
+            continue;
+        }
+        for (size_t lo = 0; lo < N; lo += BLK) {
+            const size_t m = (N - lo < BLK) ? N - lo : BLK;
+            double qt[3 * BLK], gt[3 * BLK];
+            for (size_t i = 0; i < m; i++) {
+                const double x = q[lo + i] - c->q0[0], y = q[N + lo + i] - c->q0[1], z = q[2 * N + lo + i] - c->q0[2];
+                const double *R = c->R;
+                qt[i] = R[0] * x + R[1] * y + R[2] * z;
+                qt[m + i] = R[3] * x + R[4] * y + R[5] * z;
+                qt[2 * m + i] = R[6] * x + R[7] * y + R[8] * z;
+                gt[i] = 0.;
+                gt[m + i] = 0.;
+                gt[2 * m + i] = 0.;
+            }
+            comp_gradient_n(c->type, p, m, qt, gt);
+            for (size_t i = 0; i < m; i++) {
+                const double g1[3] = {gt[i], gt[m + i], gt[2 * m + i]};
+                double gr[3];
+                rotate_back(c, g1, gr);
+                grad[lo + i] += gr[0];
+                grad[N + lo + i] += gr[1];
+                grad[2 * N + lo + i] += gr[2];
+            }
+        }
     }
 }
 
@@ -323,13 +395,11 @@ double orc_hamiltonian_value(const gx_potential *pot, const gx_frame *fr, double
     return orc_potential(pot, t, w) + frame_energy(fr, w);
 }
 
-/* Fwrapper_T -> hamiltonian_gradient_T (chamiltonian.cpp:38-57) for one point:
- * f[3:6] = grad Phi (c_gradient), frame gradient fills f[0:3] (and for the
- * rotating frame adds Omega x p to f[3:6], builtin_frames.cpp:96-112), then the
- * momentum half is negated. */
-static void rhs_point(const gx_potential *pot, const gx_frame *fr, const double *w, double *f) {
-    double g[3];
-    gradient_point(pot, w, g);
+/* Fwrapper_T -> hamiltonian_gradient_T (chamiltonian.cpp:38-57) for one point
+ * whose potential gradient g is already known: f[3:6] = g, the frame gradient
+ * fills f[0:3] (and for the rotating frame adds Omega x p to f[3:6],
+ * builtin_frames.cpp:96-112), then the momentum half is negated. */
+static void rhs_from_gradient(const gx_frame *fr, const double *w, const double *g, double *f) {
     if (fr == NULL || fr->type == GX_FRAME_STATIC) {
         f[0] = w[3];
         f[1] = w[4];
@@ -357,14 +427,23 @@ static void rhs_point(const gx_potential *pot, const gx_frame *fr, const double 
     f[5] *= -1;
 }
 
-/* hamiltonian_gradient_T over SoA w[6, N] -> f[6, N]. */
+static void rhs_point(const gx_potential *pot, const gx_frame *fr, const double *w, double *f) {
+    double g[3];
+    gradient_point(pot, w, g);
+    rhs_from_gradient(fr, w, g, f);
+}
+
+/* hamiltonian_gradient_T over SoA w[6, N] -> f[6, N]: c_gradient over all N
+ * positions first (written into the momentum half, as gala does), then the
+ * frame part and the negation point by point. */
 void orc_hamiltonian_gradient(const gx_potential *pot, const gx_frame *fr, size_t N, double t,
                               const double *w, double *f) {
-    (void)t;
+    orc_gradient(pot, N, t, w, f + 3 * N);
     for (size_t i = 0; i < N; i++) {
         double wi[6], fi[6];
+        const double g[3] = {f[3 * N + i], f[4 * N + i], f[5 * N + i]};
         for (int k = 0; k < 6; k++) wi[k] = w[k * N + i];
-        rhs_point(pot, fr, wi, fi);
+        rhs_from_gradient(fr, wi, g, fi);
         for (int k = 0; k < 6; k++) f[k * N + i] = fi[k];
     }
 }
@@ -507,6 +586,57 @@ int orc_fixed_integrate(const gx_potential *pot, int method, const double *w0, i
     return 0;
 }
 
+/* Many orbits of uneven length, step and integrator, each integrated the way
+ * gala integrates one orbit with its own time grid: integrate_orbit(w0_i,
+ * dt=dt_i, n_steps=n_i) builds t = cumsum([0, dt_i, ..., dt_i]) (timespec.py:
+ * 98-102) and runs leapfrog_integrate_hamiltonian or ruth4_integrate_hamiltonian
+ * on the (6, 1) array (leapfrog.pyx:99-116, ruth4.pyx:98-108).  w_out (6, n)
+ * receives the final states.  Orbits are spread over nthreads. */
+typedef struct {
+    const gx_potential *pot;
+    const double *w0, *dt;
+    const int64_t *nsteps;
+    const int32_t *method;
+    int64_t n;
+    double *w_out;
+} batch_fixed_ctx;
+
+static void batch_fixed_chunk(void *vctx, int64_t lo, int64_t hi) {
+    batch_fixed_ctx *B = (batch_fixed_ctx *)vctx;
+    for (int64_t i = lo; i < hi; i++) {
+        double w0[6], w1[6];
+        for (int k = 0; k < 6; k++) w0[k] = B->w0[k * B->n + i];
+        const int64_t ns = B->nsteps[i];
+        if (ns <= 0) {
+            for (int k = 0; k < 6; k++) B->w_out[k * B->n + i] = w0[k];
+            continue;
+        }
+        double *t = (double *)malloc(sizeof(double) * (size_t)(ns + 1));
+        if (!t) continue;
+        double acc = 0.0;
+        t[0] = 0.0;
+        for (int64_t j = 1; j <= ns; j++) {
+            acc += B->dt[i];
+            t[j] = acc;
+        }
+        fixed_ctx C = {B->pot, w0, t, 1, ns + 1, 0, B->method[i] ? 1 : 0, w1};
+        fixed_chunk(&C, 0, 1);
+        for (int k = 0; k < 6; k++) B->w_out[k * B->n + i] = w1[k];
+        free(t);
+    }
+}
+
+int orc_batch_fixed(const gx_potential *pot, const double *w0, int64_t n, const int64_t *nsteps,
+                    const double *dt, const int32_t *method, double *w_out, int nthreads) {
+    if (n < 0) return -1;
+    batch_fixed_ctx B = {pot, w0, dt, nsteps, method, n, w_out};
+    int64_t chunk = 16;
+    if (nthreads > 1 && n / nthreads < chunk) chunk = (n + nthreads - 1) / nthreads;
+    if (chunk < 1) chunk = 1;
+    parallel_for(nthreads, n, chunk, batch_fixed_chunk, &B);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------- */
 /* DOP853 (dop853.cpp)                                                        */
 /* ------------------------------------------------------------------------- */
@@ -523,12 +653,7 @@ typedef struct {
 /* Fwrapper_T on a batch held as y[6 * nb] in SoA order (component k of orbit j
  * at k * nb + j), as dop853_helper lays it out (dop853.pyx:135-136, 157-182). */
 static void batch_rhs(const gx_potential *pot, const gx_frame *fr, int nb, const double *y, double *f) {
-    for (int j = 0; j < nb; j++) {
-        double wi[6], fi[6];
-        for (int k = 0; k < 6; k++) wi[k] = y[k * nb + j];
-        rhs_point(pot, fr, wi, fi);
-        for (int k = 0; k < 6; k++) f[k * nb + j] = fi[k];
-    }
+    orc_hamiltonian_gradient(pot, fr, (size_t)nb, 0.0, y, f);
 }
 
 typedef struct {

@@ -139,6 +139,25 @@ class Oracle:
             raise RuntimeError(f"oracle fixed-step integration failed ({rc})")
         return out
 
+    def batch_fixed(self, pot, w0, nsteps, dt, method, nthreads=1):
+        """Per-orbit Leapfrog (method 0) / Ruth4 (1) with per-orbit n_steps and dt,
+        each orbit on its own gala time grid; final states (6, N)."""
+        if self.is_ref:
+            raise ValueError("batch_fixed is a restatement-only entry point")
+        w0 = _f64(w0)
+        n = w0.shape[1]
+        ns = np.ascontiguousarray(np.asarray(nsteps, dtype=np.int64))
+        dt = _f64(dt)
+        m = np.ascontiguousarray(np.asarray(method, dtype=np.int32))
+        if ns.shape != (n,) or dt.shape != (n,) or m.shape != (n,):
+            raise ValueError("nsteps, dt and method must each have one entry per orbit")
+        out = np.zeros((6, n))
+        rc = self.lib.orc_batch_fixed(pot.packed().for_host(), _p(w0), C.c_int64(n), _p(ns), _p(dt), _p(m),
+                                      _p(out), C.c_int(nthreads))
+        if rc != 0:
+            raise RuntimeError(f"oracle batch integration failed ({rc})")
+        return out
+
     def dop853(self, pot, w0, t, atol=1e-10, rtol=1e-10, nmax=0, dt_max=0.0, nstiff=0, save_all=True,
                nbatch=100, out_stride=1, frame=None, nthreads=1):
         """dop853_integrate_hamiltonian. Returns (w, status[, stats])."""

@@ -8,8 +8,8 @@ import sys
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parents[1]
-ARGS = ["--impl", "reference", "--steps", "3", "--warmup", "3", "--orbits", "250", "--nsteps", "120",
-        "--cpu-seconds", "0.2"]
+ARGS = ["--impl", "reference", "--steps", "3", "--warmup", "3", "--batch-orbits", "300", "--batch-step-scale",
+        "0.01", "--cpu-seconds", "0.05"]
 
 
 def _run(env_extra=None):
@@ -31,10 +31,10 @@ def test_reference_arm_prints_one_contract_line():
     assert d["value"] > 0 and d["higher_is_better"] is True and d["unit"] == "orbit-steps/s"
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["unit"] == d["unit"]
-    # 250 orbits are three 100-orbit batches: at most three threads have work
-    assert 1 <= cb["cores"] <= 3 and "3 batches" in cb["sample"]
+    assert cb["cores"] >= 1 and "of the 300 orbits" in cb["sample"]
+    assert 0 < d["config"]["sample_orbits"] <= 300
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
-    assert d["config"]["workload"].startswith("mw_dop853")
+    assert d["config"]["workload"].startswith("uneven_batch: 300 MW orbits")
 
 
 def test_reference_arm_other_ranks_exit_quietly():

@@ -146,3 +146,54 @@ def test_dop853_status_for_non_finite_initial_conditions():
             st_mine = Oracle(mine).dop853(pot, w0, t, nbatch=1)[1]
             st_gala = Oracle(gala).dop853(pot, w0, t, nbatch=1)[1]
             assert st_mine.tolist() == st_gala.tolist() == [1, code]
+
+
+def test_batch_fixed_matches_per_orbit_calls(oracle):
+    """The uneven-batch restatement (per-orbit n_steps, dt, integrator) gives the
+    bits of one gala call per orbit, threaded or not."""
+    pot = W.mw_composite()
+    n = 40
+    w0 = W.mw_ics(n, seed=21)
+    rng = np.random.default_rng(22)
+    nsteps = rng.integers(0, 300, n)
+    dt = rng.choice(np.array([0.1, 0.5, 1.0]), n)
+    method = rng.integers(0, 2, n).astype(np.int32)
+    ref = np.empty_like(w0)
+    for i in range(n):
+        if nsteps[i] == 0:
+            ref[:, i] = w0[:, i]
+            continue
+        t = g.parse_time_specification(dt=float(dt[i]), n_steps=int(nsteps[i]))
+        ref[:, i] = oracle.fixed(pot, w0[:, i:i + 1], t, "ruth4" if method[i] else "leapfrog", save_all=False)[:, 0]
+    for nth in (1, 4):
+        assert np.array_equal(oracle.batch_fixed(pot, w0, nsteps, dt, method, nthreads=nth), ref)
+
+
+def test_cpu_baseline_is_as_fast_as_gala(gala_ref):
+    """The -Ofast restatement timed as the CPU baseline runs no slower than
+    gala's own -Ofast objects on the same problems (one thread, best of 3), so
+    the GPU/CPU ratios are not inflated by a slow baseline."""
+    import time
+
+    from oracle import Oracle
+
+    fast = Oracle("fast")
+    mw = W.mw_composite()
+
+    def best(fn):
+        out = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            fn()
+            out.append(time.perf_counter() - t0)
+        return min(out)
+
+    w0 = W.mw_ics(100, seed=5)
+    t = g.parse_time_specification(dt=0.5, n_steps=1500)
+    for kind in ("leapfrog", "ruth4"):
+        ours = best(lambda: fast.fixed(mw, w0, t, kind, save_all=False))
+        gala = best(lambda: gala_ref.fixed(mw, w0, t, kind, save_all=False))
+        assert ours <= 1.10 * gala, (kind, ours, gala)
+    ours = best(lambda: fast.dop853(mw, w0, t, atol=1e-12, rtol=1e-10))
+    gala = best(lambda: gala_ref.dop853(mw, w0, t, atol=1e-12, rtol=1e-10))
+    assert ours <= 1.10 * gala, ("dop853", ours, gala)

@@ -97,8 +97,8 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gx", choices=["gx", "reference"])
     p.add_argument("--workload", default="all",
-                   choices=["all", "uneven_batch", "mw_dop853", "hernquist_leapfrog", "scf_surrogate",
-                            "mock_streams", "orbit_reductions"],
+                   choices=["all", "uneven_batch", "mw_dop853", "mw_dop853_fp32", "hernquist_leapfrog",
+                            "scf_surrogate", "mock_streams", "orbit_reductions"],
                    help="all: the headline line with every variant; otherwise that workload alone "
                         "(profiling), printed as its detailed record")
     p.add_argument("--detail", default=None, help="write the detailed record of every workload to this file")
@@ -464,6 +464,7 @@ def run_mw_dop853(args, torch, stream, reps, warmup, world=1, rank=0):
         if i >= 1:
             e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = max_over_ranks(float(np.mean(e2e))) if world > 1 else float(np.mean(e2e))
+    f32 = run_dop853_fp32(args, torch, stream, mw, w0d, td, ntimes, stride, n, flush, out.cpu().numpy(), H, E0)
     peak = fma_peak(torch, stream, True)
     ach = flops / (ms * 1e-3) / 1e12
     res = {"workload": f"mw_dop853: MW composite, DOP853 rtol 1e-10 atol 1e-12 FP64, {args.orbits} orbits, "
@@ -477,13 +478,67 @@ def run_mw_dop853(args, torch, stream, reps, warmup, world=1, rank=0):
                         "traffic": (TRAFFIC_PER_ORBIT.get("dop853", 0) * n) or None},
            "dE_over_E_median": float(np.median(dE)), "dE_over_E_p99": float(np.percentile(dE, 99)),
            "counters_per_orbit": {"nfcn": float(np.mean(stt[:, 0])), "attempted": float(np.mean(stt[:, 1])),
-                                  "accepted": float(np.mean(stt[:, 2])), "dense": float(np.mean(n_dense))}}
+                                  "accepted": float(np.mean(stt[:, 2])), "dense": float(np.mean(n_dense))},
+           "fp32": f32}
+    f32["speedup_vs_fp64"] = f32["value"] / res["value"]
     if world == 1 and not args.no_cpu_baseline:
         base, sample, cpu_out = cpu_dop853_run(mw, w0, t, args.cpu_seconds)
         gpu_sample = out[:, :, : sample.shape[1]].cpu().numpy()
         rel = np.linalg.norm(gpu_sample - cpu_out, axis=0) / np.linalg.norm(cpu_out, axis=0)
         base["gpu_vs_cpu_max_rel"] = float(np.max(rel))
         res["cpu_baseline"] = base
+    return res
+
+
+DOP32_ATOL, DOP32_RTOL = 1e-10, 1e-8
+
+
+def run_dop853_fp32(args, torch, stream, mw, w0d, td, ntimes, stride, n, flush, ref=None, H=None, E0=None):
+    """The FP32-stage / FP64-control DOP853 (per-orbit step control) on the same
+    orbits at atol 1e-10, rtol 1e-8 (FP32 stages resolve ~1e-8 relative per
+    step), against the FP64 form's outputs when given."""
+    from gala_gb300 import _abi
+
+    n_out = (ntimes - 1) // stride + 1
+    out = torch.empty((6, n_out, n), dtype=torch.float64, device="cuda")
+    status = torch.zeros(n, dtype=torch.int32, device="cuda")
+    stats = torch.zeros((n, 4), dtype=torch.int64, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    desc = mw.packed().for_device()
+    sh = int(stream.cuda_stream)
+
+    from gala_gb300.hamiltonian import cost_order
+
+    order = cost_order(mw, w0d, sh)
+
+    def launch():
+        _abi.call("gx_dop853_fp32", desc, None, int(w0d.data_ptr()), n, int(td.data_ptr()), ntimes, DOP32_ATOL,
+                  DOP32_RTOL, 0, 0.0, 0, 1, stride, int(order.data_ptr()), int(out.data_ptr()),
+                  int(status.data_ptr()), int(stats.data_ptr()), int(cnt.data_ptr()), sh)
+
+    launch()
+    torch.cuda.synchronize()
+    ms = event_time(torch, stream, launch, max(2, args.dop_reps), flush)
+    stt = stats.cpu().numpy()
+    nsteps = ntimes - 1
+    n_dense = (stt[:, 0] - 2 - 11 * stt[:, 1] - stt[:, 2]) // 3
+    flops = float(np.sum(stt[:, 0] * F_RHS_MW + stt[:, 1] * F_DOP_STEP + n_dense * F_DOP_DENSE)
+                  + n * n_out * F_DOP_OUTPUT)
+    peak = fma_peak(torch, stream, False)
+    res = {"value": n * nsteps / (ms * 1e-3), "ms": ms, "atol": DOP32_ATOL, "rtol": DOP32_RTOL,
+           "status_ok_fraction": float(np.mean(status.cpu().numpy() == 1)),
+           "roofline": {"bound": "fp32", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+                        "frac": flops / (ms * 1e-3) / 1e12 / peak},
+           "counters_per_orbit": {"nfcn": float(np.mean(stt[:, 0])), "attempted": float(np.mean(stt[:, 1])),
+                                  "accepted": float(np.mean(stt[:, 2]))}}
+    if ref is not None:
+        w = out.cpu().numpy()
+        pe = np.linalg.norm(w[:3, -1] - ref[:3, -1], axis=0) / np.linalg.norm(ref[:3, -1], axis=0)
+        dE = np.abs((H.energy(w[:, -1]) - E0) / E0)
+        res.update({"position_error_vs_fp64_median": float(np.median(pe)),
+                    "position_error_vs_fp64_p99": float(np.percentile(pe, 99)),
+                    "position_error_vs_fp64_max": float(np.max(pe)),
+                    "dE_over_E_median": float(np.median(dE)), "dE_over_E_p99": float(np.percentile(dE, 99))})
     return res
 
 
@@ -891,9 +946,15 @@ def run_orbit_reductions(args, torch, stream):
 def compact(name, r):
     cb = r.get("cpu_baseline", {})
     if name == "mw_dop853":
+        f = r["fp32"]
         return {"value": sig(r["value"]), "e2e": sig(r["e2e"]["value"]), "frac_fp64": sig(r["roofline"]["frac"], 3),
                 "dE_over_E_median": sig(r["dE_over_E_median"], 2), "cpu_16c": sig(cb.get("value")),
-                "gpu_vs_cpu_max_rel": sig(cb.get("gpu_vs_cpu_max_rel"), 2)}
+                "gpu_vs_cpu_max_rel": sig(cb.get("gpu_vs_cpu_max_rel"), 2),
+                "fp32_rtol1e-8": {"value": sig(f["value"]), "speedup": sig(f["speedup_vs_fp64"], 3),
+                                  "frac_fp32": sig(f["roofline"]["frac"], 3),
+                                  "pos_err_median": sig(f["position_error_vs_fp64_median"], 2),
+                                  "pos_err_p99": sig(f["position_error_vs_fp64_p99"], 2),
+                                  "dE_median": sig(f["dE_over_E_median"], 2)}}
     if name == "hernquist_leapfrog":
         return {"value": sig(r["value"]), "hbm_gbs": sig(r["roofline"]["achieved"]),
                 "frac_hbm": sig(r["roofline"]["frac"], 3), "e2e": sig(r["e2e"]["value"]), "cpu": sig(cb.get("value")),
@@ -942,6 +1003,14 @@ def run_gx(args):
             res = run_uneven_batch(args, torch, stream, args.steps, args.warmup)
         elif args.workload == "mw_dop853":
             res = run_mw_dop853(args, torch, stream, args.dop_reps, 1)
+        elif args.workload == "mw_dop853_fp32":
+            from gala_gb300 import workloads as W
+
+            t = g.parse_time_specification(dt=0.5, n_steps=args.nsteps)
+            w0d = torch.from_numpy(W.mw_ics(args.orbits, seed=W.SEED_BASE + 2)).cuda()
+            td = torch.from_numpy(t).cuda()
+            flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+            res = run_dop853_fp32(args, torch, stream, W.mw_composite(), w0d, td, len(t), 100, args.orbits, flush)
         else:
             res = VARIANTS[args.workload](args, torch, stream)
         if rank == 0:

@@ -119,6 +119,9 @@ SIGNATURES = {
         C.c_int,
         [_PP, _PF, _P, _I64, _P, _I64, _D, _D, _I64, _D, _I64, _I32, _I32, _I64, _P, _P, _P, _P],
     ),
+    "gx_fixed_fp32": (C.c_int, [_PP, _I32, _P, _I64, _P, _I64, _I32, _I64, _P, _P]),
+    "gx_dop853_fp32": (C.c_int, [_PP, _PF, _P, _I64, _P, _I64, _D, _D, _I64, _D, _I64, _I32, _I64, _P, _P, _P, _P,
+                                 _P, _P]),
 }
 
 _lib = None

@@ -31,6 +31,7 @@ UNITS = {
     "gx_orbit.cu": ["-fmad=false"],
     "gx_peaks.cu": [],
     "gx_batch.cu": [],
+    "gx_dop853_fp32.cu": [],
     "gx_stream32.cu": [],
     "gx_mlp_train.cu": [],
     "gx_mlp_infer.cu": [],

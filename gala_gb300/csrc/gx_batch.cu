@@ -214,6 +214,134 @@ extern "C" int gx_batch_integrate_fp32(const gx_potential *pot, const double *w0
 }
 
 // ===========================================================================
+// Fixed-step FP32-compensated integration on one time grid with snapshots:
+// the FP32 form of leapfrog_integrate_hamiltonian / ruth4_integrate_hamiltonian
+// (leapfrog.pyx:54-121, ruth4.pyx:37-113).  One thread per orbit; the step is
+// t[1] - t[0]; every out_stride-th of the ntimes grid points is stored as FP64
+// (hi + lo), in gala's (6, n_out, N) layout, or only the final state.
+// ===========================================================================
+namespace gx {
+
+struct FixedArgs {
+    int64_t n, nsteps, out_stride, n_out;
+    int32_t save_all, method;
+    float c[4], d[4];
+};
+
+__device__ __forceinline__ void store_state(double *out, int64_t n_out, int64_t n, int64_t slot, int64_t i,
+                                            const float *xh, const float *xl, const double *v) {
+    for (int k = 0; k < 3; k++) {
+        __stcs(&out[((int64_t)k * n_out + slot) * n + i], (double)xh[k] + (double)xl[k]);
+        __stcs(&out[((int64_t)(3 + k) * n_out + slot) * n + i], v[k]);
+    }
+}
+
+template <typename S>
+__global__ void __launch_bounds__(128) fixed_fp32_kernel(const __grid_constant__ DevPotF pot, FixedArgs A,
+                                                         const double *__restrict__ w0,
+                                                         const double *__restrict__ t, double *__restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.n) return;
+    const int64_t n = A.n;
+    const float h = (float)(t[1] - t[0]);
+    float xh[3], xl[3], vh[3], vl[3], g[3];
+    double v[3];
+    for (int k = 0; k < 3; k++) {
+        split(w0[k * n + i], xh[k], xl[k]);
+        split(w0[(3 + k) * n + i], vh[k], vl[k]);
+        v[k] = w0[(3 + k) * n + i];
+    }
+    int64_t slot = 0;
+    if (A.save_all) {
+        // snapshot 0 is the initial state, exactly
+        for (int k = 0; k < 6; k++) __stcs(&out[((int64_t)k * A.n_out + slot) * n + i], w0[k * n + i]);
+        slot++;
+    }
+    if (A.method == 0) {
+        potential_gradient_f<S>(pot, xh, g);
+        for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h * 0.5f);
+        for (int64_t j = 1; j <= A.nsteps; j++) {
+            for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], h, vl[k] * h));
+            potential_gradient_f<S>(pot, xh, g);
+            for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h);
+            if (A.save_all && j % A.out_stride == 0) {
+                // output velocity of c_leapfrog_step: v_{j+1/2} + g h / 2
+                for (int k = 0; k < 3; k++) v[k] = (double)vh[k] + ((double)vl[k] + (double)(g[k] * h * 0.5f));
+                store_state(out, A.n_out, n, slot++, i, xh, xl, v);
+            }
+        }
+        for (int k = 0; k < 3; k++) v[k] = (double)vh[k] + ((double)vl[k] + (double)(g[k] * h * 0.5f));
+    } else {
+        for (int64_t j = 1; j <= A.nsteps; j++) {
+            for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], A.c[0] * fmaf(vh[k], h, vl[k] * h));
+#pragma unroll
+            for (int s = 1; s < 4; s++) {
+                potential_gradient_f<S>(pot, xh, g);
+                for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -A.d[s] * g[k] * h);
+                for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], A.c[s] * fmaf(vh[k], h, vl[k] * h));
+            }
+            if (A.save_all && j % A.out_stride == 0) {
+                for (int k = 0; k < 3; k++) v[k] = (double)vh[k] + (double)vl[k];
+                store_state(out, A.n_out, n, slot++, i, xh, xl, v);
+            }
+        }
+        for (int k = 0; k < 3; k++) v[k] = (double)vh[k] + (double)vl[k];
+    }
+    if (!A.save_all)
+        for (int k = 0; k < 3; k++) {
+            out[k * n + i] = (double)xh[k] + (double)xl[k];
+            out[(3 + k) * n + i] = v[k];
+        }
+}
+
+}  // namespace gx
+
+extern "C" int gx_fixed_fp32(const gx_potential *pot, int32_t method, const double *w0, int64_t n,
+                             const double *t, int64_t ntimes, int32_t save_all, int64_t out_stride, double *w_out,
+                             void *stream) {
+    gx::DevPotF dp;
+    int rc = gx::pack_potential_f32(pot, &dp);
+    if (rc) return rc;
+    GX_CHECK_ARG(method == 0 || method == 1, "method must be 0 (leapfrog) or 1 (ruth4)");
+    GX_CHECK_ARG(n >= 0, "n < 0");
+    GX_CHECK_ARG(ntimes >= 2, "ntimes must be >= 2 (got %lld)", (long long)ntimes);
+    GX_CHECK_ARG(out_stride >= 1, "out_stride must be >= 1");
+    if (n == 0) return GX_OK;
+    GX_CHECK_ARG(w0 && t && w_out, "NULL array");
+    gx::FixedArgs A;
+    memset(&A, 0, sizeof(A));
+    A.n = n;
+    A.nsteps = ntimes - 1;
+    A.out_stride = out_stride;
+    A.n_out = (ntimes - 1) / out_stride + 1;
+    A.save_all = save_all ? 1 : 0;
+    A.method = method;
+    const double two_13 = std::pow(2., 1. / 3.);
+    const double c[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
+                         (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};
+    const double d[4] = {0., 1. / (2. - two_13), -two_13 / (2. - two_13), 1. / (2. - two_13)};
+    for (int k = 0; k < 4; k++) {
+        A.c[k] = (float)c[k];
+        A.d[k] = (float)d[k];
+    }
+    cudaStream_t st = gx::as_stream(stream);
+    const unsigned grid = (unsigned)((n + 127) / 128);
+    auto is = [&](int a) { return dp.ncomp == 1 && dp.c[0].type == a && !dp.c[0].do_sr; };
+    const bool mw = dp.ncomp == 4 && dp.c[0].type == GX_POT_HERNQUIST && dp.c[1].type == GX_POT_HERNQUIST &&
+                    dp.c[2].type == GX_POT_MIYAMOTONAGAI && dp.c[3].type == GX_POT_SPHERICALNFW &&
+                    !(dp.c[0].do_sr | dp.c[1].do_sr | dp.c[2].do_sr | dp.c[3].do_sr);
+    using namespace gx;
+    if (mw)
+        fixed_fp32_kernel<PotSig<GX_POT_HERNQUIST, GX_POT_HERNQUIST, GX_POT_MIYAMOTONAGAI, GX_POT_SPHERICALNFW>>
+            <<<grid, 128, 0, st>>>(dp, A, w0, t, w_out);
+    else if (is(GX_POT_HERNQUIST))
+        fixed_fp32_kernel<PotSig<GX_POT_HERNQUIST, -1, -1, -1>><<<grid, 128, 0, st>>>(dp, A, w0, t, w_out);
+    else
+        fixed_fp32_kernel<SigGeneric><<<grid, 128, 0, st>>>(dp, A, w0, t, w_out);
+    return gx::check_launch("fixed_fp32");
+}
+
+// ===========================================================================
 // Allocation-free variant of the batched FP32 integrator.
 //
 // Some callers cannot allocate device memory: an application whose memory

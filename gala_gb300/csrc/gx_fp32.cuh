@@ -3,8 +3,8 @@
 // The closed-form potentials of gx_device.cuh, evaluated in FP32 on the
 // special-function unit: 1/sqrt, reciprocal and log2 are single approximate
 // MUFU instructions (relative error a few 1e-8), and the NFW radial factor
-// f(u) = ln(1+u) - u/(1+u) is computed without cancellation (for u < 1 as the
-// positive series in w = u/(1+u): f = sum_{k>=2} w^k / k; for u >= 1 directly).
+// f(u) = ln(1+u) - u/(1+u) is computed without cancellation (for u < 1 as a
+// positive series in s = u/(2+u), see nfw_f_over_u3; for u >= 1 directly).
 // The integrators accumulate positions and velocities in compensated (Kahan)
 // form, so FP32 rounding of the state does not build up; the force error (a
 // few FP32 ulps) acts like a slightly perturbed potential.
@@ -53,19 +53,30 @@ __device__ __forceinline__ float lg2_approx(float x) {
     return r;
 }
 
-// f(u)/u^3 for the NFW force, u = r / r_s.
+// f(u)/u^3 for the NFW force, u = r / r_s.  For u < 1, with s = u / (2 + u)
+// (so ln(1 + u) = 2 atanh(s), u / (1 + u) = 2 s / (1 + s), 1 - s = 2 / (2 + u)):
+//   f(u) / u^3 = (1 - s)^3 / 4 * [1 / (s (1 + s)) + P(s^2)],
+//   P(t) = sum_{k>=0} t^k / (2k + 3),
+// every term positive (no cancellation); s < 1/3, so six terms of P leave a
+// truncation below 2^-24 of the bracket.  For u >= 1 the direct form has no
+// harmful cancellation.
 __device__ __forceinline__ float nfw_f_over_u3(float u) {
+    if (u < 1.0f) {
+        const float r = rcp_approx(2.0f + u);
+        const float s = u * r;
+        const float t = s * s;
+        float P = 1.0f / 13.0f;
+        P = fmaf(P, t, 1.0f / 11.0f);
+        P = fmaf(P, t, 1.0f / 9.0f);
+        P = fmaf(P, t, 1.0f / 7.0f);
+        P = fmaf(P, t, 1.0f / 5.0f);
+        P = fmaf(P, t, 1.0f / 3.0f);
+        const float br = rcp_approx(fmaf(s, s, s)) + P;
+        const float om = 2.0f * r;
+        return om * om * om * 0.25f * br;
+    }
     const float opu = 1.0f + u;
     const float iopu = rcp_approx(opu);
-    if (u < 1.0f) {
-        const float w = u * iopu;
-        // sum_{k=2}^{25} w^k / k as w^2 * s, Horner in w (w < 1/2: truncation < 2^-25)
-        float s = 1.0f / 25.0f;
-#pragma unroll
-        for (int k = 24; k >= 2; k--) s = fmaf(s, w, 1.0f / (float)k);
-        // w^2 / u^3 = 1 / (u (1+u)^2)
-        return s * rcp_approx(u) * iopu * iopu;
-    }
     const float f = lg2_approx(opu) * 0.69314718055994531f - u * iopu;
     const float iu = rcp_approx(u);
     return f * iu * iu * iu;

@@ -24,6 +24,27 @@ from ._trace import traced
 __all__ = ["StaticFrame", "ConstantRotatingFrame", "Hamiltonian"]
 
 
+def cost_order(potential, w0d, stream_handle_):
+    """Processing order for per-orbit adaptive integration: orbits by their
+    dynamical frequency at the start, max(sqrt(|grad Phi| / r), |v| / r), highest
+    first -- the step count of an adaptive integrator over a fixed time span
+    grows with it -- so the lanes of a warp get orbits of similar cost.  (N,)
+    int32 CUDA tensor."""
+    import torch
+
+    from ._device import ptr
+
+    n = w0d.shape[1]
+    q = w0d[:3].contiguous()
+    g = torch.empty((3, n), dtype=torch.float64, device=w0d.device)
+    _abi.call("gx_potential_gradient", potential.packed().for_device(), 0.0, ptr(q), n, ptr(g), stream_handle_)
+    r = torch.linalg.vector_norm(q, dim=0).clamp_min(1e-300)
+    key = torch.maximum(torch.sqrt(torch.linalg.vector_norm(g, dim=0) / r),
+                        torch.linalg.vector_norm(w0d[3:], dim=0) / r)
+    key = torch.nan_to_num(key, nan=0.0, posinf=1e300)
+    return torch.argsort(key, descending=True, stable=True).to(torch.int32).contiguous()
+
+
 class FrameBase:
     _type = None
 
@@ -138,8 +159,16 @@ class Hamiltonian:
         Extra keyword (not in gala): ``return_device=True`` keeps the result on
         the GPU (``Orbit.w_device``); the host copy is made on first access.
         DOP853 accepts gala's Integrator_kwargs (atol, rtol, nmax, err_if_fail,
-        log_output, nbatch) plus ``out_stride`` (keep every k-th output time),
-        ``dt_max`` and ``nstiff``.
+        log_output, nbatch) plus ``dt_max`` and ``nstiff``.  Every integrator
+        accepts two more Integrator_kwargs:
+
+        * ``out_stride`` -- keep every k-th output time (t[0], t[k], ...);
+        * ``precision`` -- ``"fp64"`` (default: gala's arithmetic, the parity
+          form) or ``"fp32c"``: FP32 forces with compensated FP32 state (Leapfrog,
+          Ruth4), or FP32 DOP853 stages with FP64 time / error norm /
+          accept-reject and per-orbit step control (DOP853; ``nbatch`` does not
+          apply).  Closed-form potentials only; results are not bit-compatible
+          with gala (FP32 force accuracy, ~1e-7 relative per evaluation).
         """
         import torch
 
@@ -177,20 +206,23 @@ class Hamiltonian:
             raise TypeError(
                 f"{'Leapfrog' if Integrator is LeapfrogIntegrator else 'Ruth4'} integration is currently only "
                 f"supported for StaticFrame, not {self.frame.__class__.__name__}")
+        kw = dict(Integrator_kwargs)
+        precision = str(kw.get("precision", "fp64")).lower()
+        if precision not in ("fp64", "fp32c"):
+            raise ValueError(f"precision must be 'fp64' or 'fp32c' (got {precision!r})")
+        stride = int(kw.get("out_stride", 1))
+        if stride < 1:
+            raise ValueError(f"out_stride must be >= 1 (got {stride})")
         if not symplectic:
-            kw = dict(Integrator_kwargs)
             atol = float(kw.get("atol", 1e-10))
             rtol = float(kw.get("rtol", 1e-10))
             nmax = int(kw.get("nmax", 0))
             err_if_fail = int(kw.get("err_if_fail", 1))
             nbatch = int(kw.get("nbatch", 100))
-            stride = int(kw.get("out_stride", 1))
             dt_max = float(kw.get("dt_max", 0.0))
             nstiff = int(kw.get("nstiff", 0))
             if not 1 <= nbatch <= 1024:
                 raise ValueError(f"nbatch must be in [1, 1024] (got {nbatch})")
-            if stride < 1:
-                raise ValueError(f"out_stride must be >= 1 (got {stride})")
 
         dev = require_cuda()
         if isinstance(arr_w0, torch.Tensor):
@@ -207,12 +239,35 @@ class Hamiltonian:
         pot = self.potential.packed().for_device()
         frame = self._frame_ref()
 
-        if symplectic:
+        if symplectic and precision == "fp32c":
+            n_out = (ntimes - 1) // stride + 1
+            out = torch.empty((6, n_out, n) if save_all else (6, n), dtype=torch.float64, device=dev)
+            _abi.call("gx_fixed_fp32", pot, 0 if Integrator is LeapfrogIntegrator else 1, ptr(w0d), n, ptr(td),
+                      ntimes, int(bool(save_all)), stride, ptr(out), st)
+            t_out = t[::stride]
+        elif symplectic:
             out = torch.empty((6, ntimes, n) if save_all else (6, n), dtype=torch.float64, device=dev)
             name = ("gx_leapfrog_integrate_hamiltonian" if Integrator is LeapfrogIntegrator
                     else "gx_ruth4_integrate_hamiltonian")
             _abi.call(name, pot, frame, ptr(w0d), n, ptr(td), ntimes, int(bool(save_all)), ptr(out), st)
             t_out = t
+            if save_all and stride > 1:
+                out = out[:, ::stride].contiguous()
+                t_out = t[::stride]
+        elif precision == "fp32c":
+            n_out = (ntimes - 1) // stride + 1
+            out = torch.empty((6, n_out, n) if save_all else (6, n), dtype=torch.float64, device=dev)
+            status = torch.zeros(max(n, 1), dtype=torch.int32, device=dev)
+            counter = torch.zeros(1, dtype=torch.int32, device=dev)
+            order = cost_order(self.potential, w0d, st)
+            _abi.call("gx_dop853_fp32", pot, frame, ptr(w0d), n, ptr(td), ntimes, atol, rtol, nmax, dt_max, nstiff,
+                      int(bool(save_all)), stride, ptr(order), ptr(out), ptr(status), None, ptr(counter), st)
+            if err_if_fail == 1 and n > 0:
+                res = status.cpu().numpy()
+                bad = res[res < 0]
+                if bad.size:
+                    raise RuntimeError(f"Integration failed with code {int(bad[0])}")
+            t_out = t[::stride]
         else:
             n_out = (ntimes - 1) // stride + 1
             nb = (n + nbatch - 1) // nbatch

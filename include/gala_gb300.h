@@ -204,6 +204,41 @@ int gx_dop853_integrate_hamiltonian(const gx_potential* pot, const gx_frame* fra
                                     int64_t out_stride, double* w_out,
                                     int32_t* status, int64_t* stats, void* stream);
 
+/* FP32-compensated form of leapfrog_integrate_hamiltonian / ruth4_integrate_
+ * hamiltonian (src/gala/integrate/cyintegrators/leapfrog.pyx:54-121,
+ * ruth4.pyx:37-113) on gala's time grid (step t[1] - t[0]): FP32 forces,
+ * Kahan-compensated FP32 state, FP64 input and output.  method 0 = leapfrog,
+ * 1 = ruth4.  save_all != 0: w_out (6, n_out, N) with every out_stride-th of
+ * the ntimes grid points (n_out = (ntimes - 1) / out_stride + 1); save_all == 0:
+ * w_out (6, N) at t[ntimes-1].  Static frames, closed-form components only. */
+int gx_fixed_fp32(const gx_potential* pot, int32_t method, const double* w0, int64_t n,
+                  const double* t, int64_t ntimes, int32_t save_all, int64_t out_stride,
+                  double* w_out, void* stream);
+
+/* DOP853 with FP32 stages and forces and FP64 step control.  gala's
+ * dop853_integrate_hamiltonian (src/gala/integrate/cyintegrators/dop853.pyx:
+ * 196-250) with nbatch = 1 -- every orbit is its own system with its own step
+ * size -- over gala's dopcor (dopri/dop853.cpp:89-650): the stages, forces and
+ * dense-output polynomial are FP32, the state is a double-float pair, and the
+ * time, step size, error-norm combination (:441-444) and accept/reject are FP64.
+ * Results are not bit-compatible with gala; accuracy is that of an FP32 force
+ * (relative ~1e-7 per evaluation).  Tolerances below ~1e-8 relative ask for
+ * more than FP32 stages resolve and only shrink the steps.
+ *   arguments as gx_dop853_integrate_hamiltonian (no nbatch), plus
+ *   order         : DEVICE int32[N] processing order (a permutation of the
+ *                   orbits), or NULL for 0..N-1; orbits of similar cost next to
+ *                   each other keep a warp's lanes busy together.  Each orbit's
+ *                   result does not depend on the order.
+ *   status        : DEVICE int32[N], gala's return code per orbit
+ *   stats         : DEVICE int64[4 * N] or NULL: nfcn, nstep, naccpt, nrejct
+ *   queue_counter : DEVICE int32 scratch (zeroed by the call)
+ * Closed-form components only (SCF -> GX_ERR_UNSUPPORTED). */
+int gx_dop853_fp32(const gx_potential* pot, const gx_frame* frame, const double* w0,
+                   int64_t n, const double* t, int64_t ntimes, double atol, double rtol,
+                   int64_t nmax, double dt_max, int64_t nstiff, int32_t save_all,
+                   int64_t out_stride, const int32_t* order, double* w_out, int32_t* status,
+                   int64_t* stats, int32_t* queue_counter, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Batched FP32 integration with compensated state (no single gala function:  */
 /* it runs many leapfrog_integrate_hamiltonian / ruth4_integrate_hamiltonian  */

@@ -17,6 +17,8 @@
 //             skipped here (FP32 form, no bit-parity claim)
 #include <mutex>
 
+#include <cuda.h>
+
 #include "gx_host.h"
 #include "gx_fp32.cuh"
 #include "gx_scf.cuh"
@@ -418,11 +420,40 @@ __global__ void noalloc_scatter(int32_t *s, const int64_t *__restrict__ nsteps, 
     }
 }
 
-// Device address of g_noalloc_scratch, looked up once per device (with that
-// device current) by cudaGetSymbolAddress.
+// Identity of the CUDA context current on this thread (cuCtxGetId through the
+// runtime's driver entry points, so the library links no driver library).
+typedef CUresult (*ctx_get_current_fn)(CUcontext *);
+typedef CUresult (*ctx_get_id_fn)(CUcontext, unsigned long long *);
+
+static int current_context_id(unsigned long long *id) {
+    static ctx_get_current_fn get_cur = nullptr;
+    static ctx_get_id_fn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<ctx_get_current_fn>(fn);
+        fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<ctx_get_id_fn>(fn);
+    });
+    CUcontext ctx = nullptr;
+    if (!get_cur || !get_id || get_cur(&ctx) != CUDA_SUCCESS || ctx == nullptr || get_id(ctx, id) != CUDA_SUCCESS)
+        *id = 0;  // unknown: look the address up again
+    return GX_OK;
+}
+
+// Device address of g_noalloc_scratch in the current context.  It is looked up
+// with cudaGetSymbolAddress (that device current) on a device's first call and
+// again whenever the context has changed since (after cudaDeviceReset the
+// module is loaded again and the array may sit elsewhere).
 static int noalloc_scratch_address(int32_t **out) {
     static std::mutex mu;
     static int32_t *addr[64] = {nullptr};
+    static unsigned long long ctx_of[64] = {0};
     int dev = 0;
     GX_CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) {
@@ -430,7 +461,9 @@ static int noalloc_scratch_address(int32_t **out) {
         return GX_ERR_INVALID_ARGUMENT;
     }
     std::lock_guard<std::mutex> lock(mu);
-    if (addr[dev] == nullptr) {
+    unsigned long long ctx = 0;
+    current_context_id(&ctx);
+    if (addr[dev] == nullptr || ctx == 0 || ctx != ctx_of[dev]) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) {
@@ -438,6 +471,8 @@ static int noalloc_scratch_address(int32_t **out) {
             return GX_ERR_CUDA;
         }
         addr[dev] = static_cast<int32_t *>(p);
+        // the lookup makes the context current if it was not yet: record its id now
+        current_context_id(&ctx_of[dev]);
     }
     *out = addr[dev];
     return GX_OK;

@@ -13,6 +13,19 @@ __all__ = [
 ]
 
 
+def _march(t1, t2, dt):
+    """t1, t1 + dt, (t1 + dt) + dt, ... -- each time the previous one plus dt, so
+    the rounding is that of a running sum -- for as long as the time lies
+    strictly before t2 in the direction of dt."""
+    m = int(np.ceil((t2 - t1) / dt)) + 2
+    while True:
+        seq = np.cumsum(np.concatenate([[t1], np.full(m, dt)]))
+        before = (seq < t2) if dt > 0 else (seq > t2)
+        if not before[-1]:
+            return seq[: int(np.argmin(before))]
+        m *= 2
+
+
 def parse_time_specification(units=None, dt=None, n_steps=None, t1=None, t2=None, t=None):
     """Array of times from a time specification.
 
@@ -39,26 +52,12 @@ def parse_time_specification(units=None, dt=None, n_steps=None, t1=None, t2=None
         times = parse_time_specification(units, dt=np.ones(n_steps + 1) * dt, t1=t1)
 
     elif dt is not None and t1 is not None and t2 is not None:
-        if t2 < t1 and dt < 0:
-            t_i = t1
-            times = []
-            ii = 0
-            while (t_i > t2) and (ii < 1e6):
-                times.append(t_i)
-                t_i += dt
-            if times[-1] != t2:
-                times.append(t2)
-            return np.array(times, dtype=np.float64)
-
-        if t2 > t1 and dt > 0:
-            t_i = t1
-            times = []
-            ii = 0
-            while (t_i < t2) and (ii < 1e6):
-                times.append(t_i)
-                t_i += dt
-            return np.array(times, dtype=np.float64)
-
+        if (t2 < t1 and dt < 0) or (t2 > t1 and dt > 0):
+            times = _march(float(t1), float(t2), float(dt))
+            # a backward grid ends exactly on t2, a forward one stops short of it
+            if dt < 0 and times[-1] != t2:
+                times = np.append(times, float(t2))
+            return times
         if dt == 0:
             raise ValueError("dt must be non-zero.")
         raise ValueError("If t2 < t1, dt must be negative. If t1 < t2, dt must be positive.")

@@ -496,6 +496,7 @@ class MockStreamGenerator:
         cap = 8 - nb  # the kernel's systems hold 8 bodies and particles
         if cap < 1:
             raise NotImplementedError(f"{nb} bodies exceed the 8-body Leapfrog system")
+        n_rel0, src = len(time), None
         if max_per > cap:  # larger releases in groups at the same time (exact, see split_releases)
             src, sizes = split_releases(nstream, cap)
             time, nstream = time[src], sizes
@@ -518,6 +519,11 @@ class MockStreamGenerator:
         _abi.call(name, H.potential.packed().for_device(), S, nb, ptr(bd), ptr(nbody_w), n_rel, ptr(td), ptr(od),
                   max_per, ptr(stream_w0), n_rows, float(orbit_t[-1]), dt, ptr(stream_out), ptr(nbody_out),
                   ptr(status), stream_handle(stream))
+        if src is not None:
+            # one status per release, as documented: the worst code over its groups
+            idx = torch.from_numpy(src).to(dev).expand(S, -1)
+            status = torch.ones((S, n_rel0), dtype=torch.int32, device=dev).scatter_reduce(
+                1, idx, status, reduce="amin", include_self=False)
         res = status.cpu().numpy()
         if np.any(res < 0):
             raise RuntimeError(f"release systems rejected: {int(np.sum(res < 0))}")

@@ -281,6 +281,8 @@ int gx_batch_integrate_fp64(const gx_potential* pot, const double* w0, int64_t n
  *   Per-orbit results are bit-identical to gx_batch_integrate_fp32.
  *   The first call on a device looks up that array's device address (with
  *   that device current); make that first call before any stream capture.
+ *   A call in a new context of the device (after cudaDeviceReset) looks the
+ *   address up again.
  *   Every call on a device shares the one array: calls that overlap on the GPU
  *   (different streams, no ordering) race and must not be issued.
  * The library holds the array (about 1 MB) on every GPU it is loaded on until

@@ -349,3 +349,27 @@ def test_component_limit_is_refused_clearly():
         comp.packed()
     ok = g.CompositePotential(**{f"h{i}": g.HernquistPotential(m=1e9, c=0.1) for i in range(_abi.GX_MAX_COMPONENTS)})
     assert ok.packed().desc.n_components == _abi.GX_MAX_COMPONENTS
+
+
+def test_stepped_time_grids_are_running_sums():
+    """dt, t1, t2 grids: each time is the previous one plus dt (gala's running
+    sum, timespec.py:100-121); a forward grid stops short of t2, a backward one
+    ends on t2 exactly."""
+    rng = np.random.default_rng(0)
+
+    def running(t1, t2, dt):
+        out, x = [], t1
+        while (x < t2) if dt > 0 else (x > t2):
+            out.append(x)
+            x += dt
+        if dt < 0 and out[-1] != t2:
+            out.append(t2)
+        return np.array(out)
+
+    for _ in range(500):
+        t1 = rng.uniform(-100, 100)
+        span = rng.uniform(0.1, 500)
+        dt = rng.choice([0.1, 1 / 3, 0.7, 1.0, rng.uniform(0.01, 5)])
+        for sgn in (1, -1):
+            got = g.parse_time_specification(dt=sgn * dt, t1=t1, t2=t1 + sgn * span)
+            assert np.array_equal(got, running(t1, t1 + sgn * span, sgn * dt))

@@ -603,6 +603,12 @@ def test_large_leapfrog_release_and_dop853_burst(oracle):
     err = np.linalg.norm(got - ref_st, axis=1) / np.abs(ref_st).max()
     assert np.median(err) < 1e-8 and np.quantile(err, 0.9) < 1e-7, np.quantile(err, [0.5, 0.9, 1.0])
     assert _scale_err(np.vstack([nbody.xyz, nbody.v_xyz]).T, ref_nb) < 1e-10
+    # the batch result keeps one status per release time, however the releases were split
+    res = gen().run_batch(w0.reshape(6, 1), np.array([2.5e4]), progenitor_potentials=[g.PlummerPotential(m=2.5e4,
+                          b=0.004)], n_particles=counts, dt=1.0, n_steps=100, Integrator="leapfrog")
+    rel_t = np.nonzero(np.asarray(counts) > 0)[0]
+    assert tuple(res.status.shape) == (1, len(rel_t) + (0 not in rel_t))
+    assert np.all(res.status.cpu().numpy() == 1)
     with pytest.raises(NotImplementedError, match="32-lane"):
         gen().run(g.PhaseSpacePosition.from_w(w0), 2.5e4, n_particles=counts, dt=1.0, n_steps=100)
 

@@ -55,6 +55,29 @@ def test_noalloc_matches_regular_entry_point_twice():
         assert np.array_equal(a, b), f"call {call}: max |diff| {np.nanmax(np.abs(a - b))}"
 
 
+def test_noalloc_call_allocates_no_device_memory():
+    """After one warm-up call, a further call leaves the device's free memory
+    unchanged: the work queue is the library's own array."""
+    import torch
+
+    lib = _abi.load()
+    desc = W.mw_composite().packed().for_device()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    stream = torch.cuda.current_stream().cuda_stream
+    n = 4000
+    w0, nsteps, dt, method = _inputs(n, 303)
+    out = torch.empty((6, n), dtype=torch.float64, device="cuda")
+    args = (desc, w0.data_ptr(), n, nsteps.data_ptr(), dt.data_ptr(), method.data_ptr(), 128, 4 * sms,
+            out.data_ptr(), stream)
+    assert lib.gx_batch_integrate_fp32_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    assert lib.gx_batch_integrate_fp32_noalloc(*args) == 0
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     lib = _abi.load()
     desc = W.mw_composite().packed().for_device()

@@ -56,6 +56,7 @@ class gx_potential(C.Structure):
         ("params", C.POINTER(C.c_double)),
         ("params_device", C.c_void_p),
         ("n_params_total", C.c_int64),
+        ("table_device", C.c_void_p),
     ]
 
 
@@ -76,6 +77,8 @@ _PF = C.POINTER(gx_frame)
 
 SIGNATURES = {
     "gx_abi_version": (C.c_int, []),
+    "gx_component_table_bytes": (C.c_int64, [C.c_int32]),
+    "gx_pack_component_table": (C.c_int, [_PP, _P, _I64]),
     "gx_last_error_message": (C.c_char_p, []),
     "gx_potential_value": (C.c_int, [_PP, _D, _P, _I64, _P, _P]),
     "gx_potential_gradient": (C.c_int, [_PP, _D, _P, _I64, _P, _P]),
@@ -156,7 +159,7 @@ def load(build_if_missing: bool = True):
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
-        if lib.gx_abi_version() != 1:
+        if lib.gx_abi_version() != 2:
             raise RuntimeError("gala_gb300 library ABI version mismatch")
         _lib = lib
         return lib

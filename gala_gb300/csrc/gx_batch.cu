@@ -110,6 +110,11 @@ int pack_potential_f32(const gx_potential *pot, DevPotF *out) {
     DevPot dp;
     int rc = pack_potential(pot, &dp);
     if (rc) return rc;
+    if (dp.cdev) {
+        set_error("the FP32 forms take at most GX_MAX_COMPONENTS = %d components (got %d)", GX_MAX_COMPONENTS,
+                  dp.ncomp);
+        return GX_ERR_CAPACITY;
+    }
     if (dp.has_scf) {
         set_error("the FP32 batched integrator supports closed-form components only (no SCF)");
         return GX_ERR_UNSUPPORTED;

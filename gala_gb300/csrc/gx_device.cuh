@@ -45,9 +45,23 @@ struct DevPot {
     int32_t has_scf;      // selects the SCF = true instantiation on the host
     int32_t pad;
     const double *pdev;   // device copy of the packed parameters (may be null)
+    const DevComp *cdev;  // component table in device memory (more than
+                          // GX_MAX_COMPONENTS components), else null
     DevComp c[GX_MAX_COMPONENTS];
     double p[GX_MAX_INLINE_PARAMS];
 };
+
+// A large composite seen through its device table: the same members as DevPot
+// (c, p, pdev, ncomp), so the component evaluators below serve both; every
+// table component reads its parameters from the device copy (inl == 0).
+struct TabPot {
+    int32_t ncomp;
+    const DevComp *c;
+    const double *p;
+    const double *pdev;
+};
+
+__device__ __forceinline__ TabPot table_view(const DevPot &pot) { return TabPot{pot.ncomp, pot.cdev, pot.pdev, pot.pdev}; }
 
 struct DevFrame {
     int32_t type;   // gx_frame_type
@@ -84,8 +98,8 @@ __device__ __forceinline__ double cube(double r) { return r * r * r; }
 // Value of one component at q (kepler_value :58-64, hernquist_value :211-219,
 // plummer_value :292-300, miyamotonagai_value :1287-1296, sphericalnfw_value
 // :819-833, flattenednfw_value :925-942, triaxialnfw_value :1028-1049).
-template <bool SCF>
-__device__ __forceinline__ double comp_value(const DevPot &pot, int ci, const double *q) {
+template <bool SCF, typename PV>
+__device__ __forceinline__ double comp_value(const PV &pot, int ci, const double *q) {
     const int type = pot.c[ci].type;
 #define P(k) GX_PARAM(pot, ci, k)
     switch (type) {
@@ -136,8 +150,8 @@ __device__ __forceinline__ double comp_value(const DevPot &pot, int ci, const do
 // Gradient of one component, accumulated into g (kepler :66-76, hernquist
 // :221-233, plummer :302-314, miyamotonagai :1298-1312, sphericalnfw :835-850,
 // flattenednfw :944-962, triaxialnfw :1051-1072).
-template <bool SCF>
-__device__ __forceinline__ void comp_gradient(const DevPot &pot, int ci, const double *q, double *g) {
+template <bool SCF, typename PV>
+__device__ __forceinline__ void comp_gradient(const PV &pot, int ci, const double *q, double *g) {
     const int type = pot.c[ci].type;
 #define P(k) GX_PARAM(pot, ci, k)
     double fac;
@@ -214,8 +228,8 @@ __device__ __forceinline__ void comp_gradient(const DevPot &pot, int ci, const d
 // plummer_density :316-324, miyamotonagai_density :1314-1332,
 // sphericalnfw_density :852-864).  Flattened/triaxial NFW have no density in
 // gala (nan_density).
-template <bool SCF>
-__device__ __forceinline__ double comp_density(const DevPot &pot, int ci, const double *q) {
+template <bool SCF, typename PV>
+__device__ __forceinline__ double comp_density(const PV &pot, int ci, const double *q) {
     const int type = pot.c[ci].type;
     const double PI = 3.14159265358979323846;
 #define P(k) GX_PARAM(pot, ci, k)
@@ -266,8 +280,8 @@ __device__ __forceinline__ void shift_rotate(const DevComp &c, const double *q, 
 
 // c_potential (cpotential.cpp:170-189).  The shifted path of gala builds q'
 // as 0 + R0 x + ...; for finite values that equals R0 x + ..., bit for bit.
-template <bool SCF>
-__device__ __forceinline__ double potential_value(const DevPot &pot, const double *q) {
+template <bool SCF, typename PV>
+__device__ __forceinline__ double potential_value_t(const PV &pot, const double *q) {
     double v = 0;
     for (int i = 0; i < pot.ncomp; i++) {
         if (pot.c[i].do_sr == 0) {
@@ -282,8 +296,8 @@ __device__ __forceinline__ double potential_value(const DevPot &pot, const doubl
 }
 
 // c_density (cpotential.cpp:192-211).
-template <bool SCF>
-__device__ __forceinline__ double potential_density(const DevPot &pot, const double *q) {
+template <bool SCF, typename PV>
+__device__ __forceinline__ double potential_density_t(const PV &pot, const double *q) {
     double v = 0;
     for (int i = 0; i < pot.ncomp; i++) {
         if (pot.c[i].do_sr == 0) {
@@ -300,8 +314,8 @@ __device__ __forceinline__ double potential_density(const DevPot &pot, const dou
 // c_gradient at one point (cpotential.cpp:214-287): zero, accumulate each
 // component in order; shifted/rotated components go through a zeroed
 // temporary, are rotated back with R^T (apply_rotate_T, :103-134) and added.
-template <bool SCF>
-__device__ __forceinline__ void potential_gradient(const DevPot &pot, const double *q, double *g) {
+template <bool SCF, typename PV>
+__device__ __forceinline__ void potential_gradient_t(const PV &pot, const double *q, double *g) {
     g[0] = 0.; g[1] = 0.; g[2] = 0.;
     for (int i = 0; i < pot.ncomp; i++) {
         if (pot.c[i].do_sr == 0) {
@@ -316,6 +330,27 @@ __device__ __forceinline__ void potential_gradient(const DevPot &pot, const doub
             g[2] += c.R[2] * gt[0] + c.R[5] * gt[1] + c.R[8] * gt[2];
         }
     }
+}
+
+// The descriptor's components: the by-value array, or the device table of a
+// large composite (the branch is uniform over the grid).
+template <bool SCF>
+__device__ __forceinline__ double potential_value(const DevPot &pot, const double *q) {
+    if (pot.cdev) return potential_value_t<SCF>(table_view(pot), q);
+    return potential_value_t<SCF>(pot, q);
+}
+template <bool SCF>
+__device__ __forceinline__ double potential_density(const DevPot &pot, const double *q) {
+    if (pot.cdev) return potential_density_t<SCF>(table_view(pot), q);
+    return potential_density_t<SCF>(pot, q);
+}
+template <bool SCF>
+__device__ __forceinline__ void potential_gradient(const DevPot &pot, const double *q, double *g) {
+    if (pot.cdev) {
+        potential_gradient_t<SCF>(table_view(pot), q, g);
+        return;
+    }
+    potential_gradient_t<SCF>(pot, q, g);
 }
 
 // Frame energy: static_frame_hamiltonian (builtin_frames.cpp:8-16) or

@@ -106,8 +106,8 @@ __device__ __forceinline__ double norm3_sq_f(const double *q) { return fma(q[0],
 
 // Gradient of one component accumulated into g; the same cases and gala
 // references as comp_gradient in gx_device.cuh.
-template <bool SCF>
-__device__ __forceinline__ void comp_gradient_f(const DevPot &pot, int ci, const double *q, double *g) {
+template <bool SCF, typename PV>
+__device__ __forceinline__ void comp_gradient_f(const PV &pot, int ci, const double *q, double *g) {
     const DevComp &C = pot.c[ci];
     const int type = C.type;
 #define P(k) GX_PARAM(pot, ci, k)
@@ -179,8 +179,8 @@ __device__ __forceinline__ void comp_gradient_f(const DevPot &pot, int ci, const
 #undef P
 }
 
-template <bool SCF>
-__device__ __forceinline__ void potential_gradient_f(const DevPot &pot, const double *q, double *g) {
+template <bool SCF, typename PV>
+__device__ __forceinline__ void potential_gradient_ft(const PV &pot, const double *q, double *g) {
     g[0] = 0.; g[1] = 0.; g[2] = 0.;
     for (int i = 0; i < pot.ncomp; i++) {
         if (pot.c[i].do_sr == 0) {
@@ -195,6 +195,15 @@ __device__ __forceinline__ void potential_gradient_f(const DevPot &pot, const do
             g[2] += fma(c.R[2], gt[0], fma(c.R[5], gt[1], c.R[8] * gt[2]));
         }
     }
+}
+
+template <bool SCF>
+__device__ __forceinline__ void potential_gradient_f(const DevPot &pot, const double *q, double *g) {
+    if (pot.cdev) {
+        potential_gradient_ft<SCF>(table_view(pot), q, g);
+        return;
+    }
+    potential_gradient_ft<SCF>(pot, q, g);
 }
 
 // Hamilton's equations (hamiltonian_rhs in gx_device.cuh) with the fast force.

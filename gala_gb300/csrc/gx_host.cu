@@ -38,27 +38,76 @@ int expected_params(int type, const double *p, int64_t avail) {
     }
 }
 
-int pack_potential(const gx_potential *pot, DevPot *out) {
+// Host-derived constants of a component for the FP64-pipe-lean forms
+// (gx_fast64.cuh); P is the component's [G, ...] block.
+static void derived_constants(int type, const double *P, DevComp &d) {
+    d.dc[0] = P[0] * P[1];
+    switch (type) {
+    case GX_POT_PLUMMER: d.dc[1] = P[2] * P[2]; break;
+    case GX_POT_MIYAMOTONAGAI: d.dc[1] = P[3] * P[3]; break;
+    case GX_POT_SPHERICALNFW:
+    case GX_POT_FLATTENEDNFW:
+    case GX_POT_TRIAXIALNFW:
+        d.dc[1] = 1.0 / P[2];
+        d.dc[2] = type == GX_POT_TRIAXIALNFW ? 1.0 / (P[3] * P[3]) : 1.0;
+        d.dc[3] = type == GX_POT_TRIAXIALNFW ? 1.0 / (P[4] * P[4]) : 1.0;
+        d.dc[4] = type != GX_POT_SPHERICALNFW ? 1.0 / (P[5] * P[5]) : 1.0;
+        break;
+    default: break;
+    }
+}
+
+// Validate the descriptor's header and component i; *need = the doubles its type uses.
+static int check_header(const gx_potential *pot) {
     GX_CHECK_ARG(pot != nullptr, "potential descriptor is NULL");
     GX_CHECK_ARG(pot->n_dim == 3, "n_dim must be 3 (got %d)", pot->n_dim);
     GX_CHECK_ARG(pot->n_components >= 0, "n_components < 0");
-    if (pot->n_components > GX_MAX_COMPONENTS) {
-        set_error("%d components exceed GX_MAX_COMPONENTS = %d", pot->n_components, GX_MAX_COMPONENTS);
-        return GX_ERR_CAPACITY;
-    }
     GX_CHECK_ARG(pot->n_components == 0 || (pot->components && pot->params), "NULL component or param array");
+    return GX_OK;
+}
+
+static int check_component(const gx_potential *pot, int i, int *need) {
+    const gx_component &c = pot->components[i];
+    GX_CHECK_ARG(c.param_offset >= 0 && c.param_offset + c.n_params <= pot->n_params_total,
+                 "component %d parameter range outside params[]", i);
+    GX_CHECK_ARG(c.param_offset < (int64_t)INT32_MAX, "component %d: parameter offset too large", i);
+    *need = expected_params(c.type, pot->params + c.param_offset, c.n_params);
+    GX_CHECK_ARG(*need > 0, "component %d: unknown type %d or bad SCF header", i, c.type);
+    GX_CHECK_ARG(c.n_params >= *need, "component %d: %d parameters, type %d needs %d", i, c.n_params, c.type,
+                 *need);
+    return GX_OK;
+}
+
+int pack_potential(const gx_potential *pot, DevPot *out) {
+    int rc = check_header(pot);
+    if (rc) return rc;
     memset(out, 0, sizeof(*out));
     out->ncomp = pot->n_components;
     out->pdev = pot->params_device;
+    if (pot->n_components > GX_MAX_COMPONENTS) {
+        // a large composite: components from the device table, parameters
+        // from the device copy
+        if (pot->table_device == nullptr || pot->params_device == nullptr) {
+            set_error("%d components exceed GX_MAX_COMPONENTS = %d: pass the component table in device memory "
+                      "(table_device, packed by gx_pack_component_table) and params_device",
+                      pot->n_components, GX_MAX_COMPONENTS);
+            return GX_ERR_CAPACITY;
+        }
+        for (int i = 0; i < pot->n_components; i++) {
+            int need = 0;
+            rc = check_component(pot, i, &need);
+            if (rc) return rc;
+            if (pot->components[i].type == GX_POT_SCF) out->has_scf = 1;
+        }
+        out->cdev = static_cast<const DevComp *>(pot->table_device);
+        return GX_OK;
+    }
     int ninl = 0;
     for (int i = 0; i < pot->n_components; i++) {
         const gx_component &c = pot->components[i];
-        GX_CHECK_ARG(c.param_offset >= 0 && c.param_offset + c.n_params <= pot->n_params_total,
-                     "component %d parameter range outside params[]", i);
-        const int need = expected_params(c.type, pot->params + c.param_offset, c.n_params);
-        GX_CHECK_ARG(need > 0, "component %d: unknown type %d or bad SCF header", i, c.type);
-        GX_CHECK_ARG(c.n_params >= need, "component %d: %d parameters, type %d needs %d", i, c.n_params,
-                     c.type, need);
+        int need = 0;
+        rc = check_component(pot, i, &need);
+        if (rc) return rc;
         DevComp &d = out->c[i];
         d.type = c.type;
         d.do_sr = c.do_shift_rotate ? 1 : 0;
@@ -81,21 +130,7 @@ int pack_potential(const gx_potential *pot, DevPot *out) {
             d.poff = ninl;
             for (int k = 0; k < need; k++) out->p[ninl + k] = pot->params[c.param_offset + k];
             ninl += need;
-            const double *P = pot->params + c.param_offset;
-            d.dc[0] = P[0] * P[1];
-            switch (c.type) {
-            case GX_POT_PLUMMER: d.dc[1] = P[2] * P[2]; break;
-            case GX_POT_MIYAMOTONAGAI: d.dc[1] = P[3] * P[3]; break;
-            case GX_POT_SPHERICALNFW:
-            case GX_POT_FLATTENEDNFW:
-            case GX_POT_TRIAXIALNFW:
-                d.dc[1] = 1.0 / P[2];
-                d.dc[2] = c.type == GX_POT_TRIAXIALNFW ? 1.0 / (P[3] * P[3]) : 1.0;
-                d.dc[3] = c.type == GX_POT_TRIAXIALNFW ? 1.0 / (P[4] * P[4]) : 1.0;
-                d.dc[4] = c.type != GX_POT_SPHERICALNFW ? 1.0 / (P[5] * P[5]) : 1.0;
-                break;
-            default: break;
-            }
+            derived_constants(c.type, pot->params + c.param_offset, d);
         }
     }
     out->n_inline = ninl;
@@ -194,6 +229,36 @@ static int launch_ham(const gx_potential *pot, const gx_frame *fr, const double 
 extern "C" {
 
 int gx_abi_version(void) { return GX_ABI_VERSION; }
+
+int64_t gx_component_table_bytes(int32_t n_components) {
+    return n_components > 0 ? (int64_t)n_components * (int64_t)sizeof(gx::DevComp) : 0;
+}
+
+int gx_pack_component_table(const gx_potential *pot, void *host_out, int64_t bytes) {
+    int rc = gx::check_header(pot);
+    if (rc) return rc;
+    const int64_t want = gx_component_table_bytes(pot->n_components);
+    GX_CHECK_ARG(bytes >= want, "table buffer of %lld bytes, %lld needed", (long long)bytes, (long long)want);
+    GX_CHECK_ARG(want == 0 || host_out != nullptr, "NULL table buffer");
+    gx::DevComp *t = static_cast<gx::DevComp *>(host_out);
+    for (int i = 0; i < pot->n_components; i++) {
+        int need = 0;
+        rc = gx::check_component(pot, i, &need);
+        if (rc) return rc;
+        const gx_component &c = pot->components[i];
+        gx::DevComp d;
+        memset(&d, 0, sizeof(d));
+        d.type = c.type;
+        d.do_sr = c.do_shift_rotate ? 1 : 0;
+        d.inl = 0;  // parameters from the device copy of params[]
+        d.poff = (int32_t)c.param_offset;
+        for (int k = 0; k < 3; k++) d.q0[k] = c.q0[k];
+        for (int k = 0; k < 9; k++) d.R[k] = c.R[k];
+        if (c.type != GX_POT_SCF) gx::derived_constants(c.type, pot->params + c.param_offset, d);
+        memcpy(&t[i], &d, sizeof(d));
+    }
+    return GX_OK;
+}
 
 const char *gx_last_error_message(void) { return gx::g_errmsg; }
 

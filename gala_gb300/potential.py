@@ -52,8 +52,6 @@ class PackedPotential:
 
     def __init__(self, comps):
         n = len(comps)
-        if n > _abi.GX_MAX_COMPONENTS:
-            raise ValueError(f"{n} components exceed the limit of {_abi.GX_MAX_COMPONENTS}")
         params = [np.asarray(p, dtype=np.float64).ravel() for (_, p, _, _) in comps]
         offsets = np.cumsum([0] + [len(p) for p in params])[:-1]
         self.params = np.ascontiguousarray(np.concatenate(params) if params else np.zeros(1))
@@ -81,17 +79,32 @@ class PackedPotential:
         self.desc.params = self.params.ctypes.data_as(C.POINTER(C.c_double))
         self.desc.params_device = None
         self.desc.n_params_total = len(self.params)
+        self.desc.table_device = None
         self._dev = None
+        self._table = None
+        # more components than the by-value descriptor holds: the kernels read
+        # them from a component table in device memory
+        self.large = n > _abi.GX_MAX_COMPONENTS
 
     def for_device(self):
-        """Descriptor with ``params_device`` filled (uploads the parameters once)."""
-        if self.has_scf and self._dev is None:
+        """Descriptor with ``params_device`` filled (uploads the parameters once)
+        and, for a large composite, the component table in device memory."""
+        if (self.has_scf or self.large) and self._dev is None:
             import torch
 
             from ._device import require_cuda
 
             self._dev = torch.from_numpy(self.params).to(require_cuda())
             self.desc.params_device = int(self._dev.data_ptr())
+        if self.large and self._table is None:
+            import torch
+
+            lib = _abi.load()
+            nbytes = int(lib.gx_component_table_bytes(self.desc.n_components))
+            host = np.zeros(nbytes, dtype=np.uint8)
+            _abi.call("gx_pack_component_table", C.byref(self.desc), host.ctypes.data, nbytes)
+            self._table = torch.from_numpy(host).to(self._dev.device)
+            self.desc.table_device = int(self._table.data_ptr())
         return C.byref(self.desc)
 
     def for_host(self):

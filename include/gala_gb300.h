@@ -30,9 +30,12 @@
 extern "C" {
 #endif
 
-#define GX_ABI_VERSION 1
+#define GX_ABI_VERSION 2
 
-/* Capacity of the by-value potential descriptor handed to every kernel. */
+/* Capacity of the by-value potential descriptor handed to every kernel.  A
+ * potential with more components (gala's composites have no limit) is read by
+ * the FP64 kernels from a component table in device memory instead
+ * (gx_potential.table_device); the FP32 forms take at most GX_MAX_COMPONENTS. */
 #define GX_MAX_COMPONENTS 16
 #define GX_MAX_INLINE_PARAMS 128
 
@@ -90,9 +93,14 @@ typedef struct gx_potential {
     int32_t n_dim;             /* insertion order); n_dim must be 3                 */
     const gx_component* components;   /* HOST array[n_components]                   */
     const double* params;             /* HOST packed parameters                     */
-    const double* params_device;      /* DEVICE copy of params; required only when a */
-                                      /* component is GX_POT_SCF, else may be NULL  */
+    const double* params_device;      /* DEVICE copy of params; required when a      */
+                                      /* component is GX_POT_SCF or when there are  */
+                                      /* more than GX_MAX_COMPONENTS, else may be NULL */
     int64_t n_params_total;
+    const void* table_device;         /* DEVICE component table for more than        */
+                                      /* GX_MAX_COMPONENTS components: the bytes     */
+                                      /* gx_pack_component_table wrote for this same */
+                                      /* descriptor, copied to the device; else NULL */
 } gx_potential;
 
 /* Reference frame: gala's CFrameType (src/gala/potential/frame/src/cframe.h:7-17). */
@@ -122,6 +130,20 @@ typedef struct gx_body {
 /* ------------------------------------------------------------------------- */
 /* Library                                                                   */
 /* ------------------------------------------------------------------------- */
+/* Component table for a potential of more than GX_MAX_COMPONENTS components.
+ * gala keeps the component pointers of a composite in host arrays (struct
+ * _CPotential, cpotential.h:10-36); on the GPU a large composite lives in a
+ * device table that every thread reads through the L1 cache.
+ *   gx_component_table_bytes(n)      bytes of the table for n components
+ *   gx_pack_component_table(pot, host_out, bytes)
+ *       validates pot (its components and params, HOST) and writes the table
+ *       into host_out; copy those bytes to device memory and set
+ *       pot->table_device (and pot->params_device) before calling any FP64
+ *       entry point with this descriptor.  The table is valid for the
+ *       descriptor it was packed from.  Returns GX_OK or an error code. */
+int64_t gx_component_table_bytes(int32_t n_components);
+int gx_pack_component_table(const gx_potential* pot, void* host_out, int64_t bytes);
+
 /* ABI version of the loaded library (compare with GX_ABI_VERSION). */
 int gx_abi_version(void);
 

@@ -31,14 +31,14 @@ def test_library_loads_and_exports_every_declared_symbol():
     missing = [n for n in declared if not hasattr(lib, n)]
     assert not missing, missing
     assert set(_abi.SIGNATURES) >= declared, declared - set(_abi.SIGNATURES)
-    assert lib.gx_abi_version() == 1
+    assert lib.gx_abi_version() == 2
 
 
 def test_struct_layout_matches_header():
     # gx_component: 4+4+8+4+4 + 3*8 + 9*8 = 120 bytes, 8-byte aligned
     assert C.sizeof(_abi.gx_component) == 120
     assert _abi.gx_component.q0.offset == 24
-    assert C.sizeof(_abi.gx_potential) == 40
+    assert C.sizeof(_abi.gx_potential) == 48
     assert C.sizeof(_abi.gx_frame) == 32
 
 
@@ -341,14 +341,26 @@ def test_nfw_from_circular_velocity_with_quantities():
         np.testing.assert_allclose(v, 0.22, rtol=1e-12)
 
 
-def test_component_limit_is_refused_clearly():
-    """More than GX_MAX_COMPONENTS components cannot be packed (gala has no limit)."""
+def test_large_composite_packs_a_component_table():
+    """More than GX_MAX_COMPONENTS components (gala has no limit): the packed
+    descriptor keeps every component, the library writes a component table of
+    the stated size, and a bad component is refused before anything is written."""
+    n = _abi.GX_MAX_COMPONENTS + 1
     comp = g.CompositePotential(**{f"h{i}": g.HernquistPotential(m=1e9, c=0.1, origin=[0.01 * i, 0, 0])
-                                   for i in range(_abi.GX_MAX_COMPONENTS + 1)})
-    with pytest.raises(ValueError, match="exceed the limit"):
-        comp.packed()
+                                   for i in range(n)})
+    pk = comp.packed()
+    assert pk.desc.n_components == n and pk.large
+    lib = _abi.load()
+    nbytes = lib.gx_component_table_bytes(n)
+    assert nbytes > 0 and nbytes % n == 0
+    buf = np.zeros(nbytes, dtype=np.uint8)
+    assert lib.gx_pack_component_table(pk.for_host(), buf.ctypes.data, nbytes) == _abi.GX_OK
+    assert buf.any()
+    assert lib.gx_pack_component_table(pk.for_host(), buf.ctypes.data, nbytes - 1) == _abi.GX_ERR_INVALID_ARGUMENT
+    pk.components[3].type = 99
+    assert lib.gx_pack_component_table(pk.for_host(), buf.ctypes.data, nbytes) == _abi.GX_ERR_INVALID_ARGUMENT
     ok = g.CompositePotential(**{f"h{i}": g.HernquistPotential(m=1e9, c=0.1) for i in range(_abi.GX_MAX_COMPONENTS)})
-    assert ok.packed().desc.n_components == _abi.GX_MAX_COMPONENTS
+    assert not ok.packed().large
 
 
 def test_stepped_time_grids_are_running_sums():

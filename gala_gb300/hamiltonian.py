@@ -150,7 +150,55 @@ class Hamiltonian:
                   ptr(wd), n, ptr(out), stream_handle())
         return out.cpu().numpy().reshape(shape)
 
-    # --- integration ---------------------------------------------------------
+    def _integrate_surrogate(self, w0, kw, save_all, return_device, Integrator, **time_spec):
+        """Leapfrog with a learned surrogate force (Integrator_kwargs surrogate=)."""
+        import torch
+
+        from .surrogate import SurrogatePotential
+
+        if Integrator is not LeapfrogIntegrator:
+            raise ValueError("the surrogate integrates with the LeapfrogIntegrator only")
+        if not isinstance(self.frame, StaticFrame):
+            raise TypeError("the surrogate integrates in a StaticFrame only")
+        sp = kw["surrogate"]
+        if not isinstance(sp, SurrogatePotential):
+            sp = SurrogatePotential.load(sp, self.potential)
+        elif sp.scf is not self.potential and not np.array_equal(sp.scf.packed().params,
+                                                                 self.potential.packed().params):
+            raise ValueError("the surrogate was trained for a different potential")
+        stride = int(kw.get("out_stride", 1))
+        if stride < 1:
+            raise ValueError(f"out_stride must be >= 1 (got {stride})")
+        arr = w0 if isinstance(w0, torch.Tensor) else np.asarray(w0, dtype=np.float64)
+        if arr.ndim == 0 or arr.shape[0] != 6:
+            raise ValueError(f"Invalid initial conditions shape {tuple(arr.shape)}. Expected shape (6, ...)")
+        t = np.ascontiguousarray(parse_time_specification(self.units, **time_spec), dtype=np.float64)
+        if len(t) < 2:
+            raise ValueError("ntimes must be greater than 1")
+        dt = float(t[1] - t[0])
+        n_steps = len(t) - 1
+        if isinstance(arr, torch.Tensor):
+            w = arr.reshape(6, -1).to(device=sp.dev, dtype=torch.float64).contiguous()
+        else:
+            w = torch.from_numpy(np.ascontiguousarray(arr.reshape(6, -1))).to(sp.dev)
+        if not save_all:
+            w, _ = sp.integrate_leapfrog(w, dt, n_steps)
+            out, t_out = w[:, None], t[-1:]
+        else:
+            snaps, t_out = [w], [t[0]]
+            for j in range(stride, n_steps + 1, stride):
+                w, _ = sp.integrate_leapfrog(w, dt, stride)
+                snaps.append(w)
+                t_out.append(t[j])
+            out, t_out = torch.stack(snaps, dim=1), np.array(t_out)
+        wr = out if return_device else out.cpu().numpy()
+        if wr.shape[-1] == 1:
+            wr = wr[..., 0]
+        if return_device:
+            return Orbit.from_w(wr, t=t_out, hamiltonian=self)
+        return Orbit.from_w(w=wr, t=t_out, hamiltonian=self, copy=False)
+
+    # --- integration ---------------------------------------------------------    # --- integration ---------------------------------------------------------
     @traced("integrate_orbit")
     def integrate_orbit(self, w0, Integrator=None, Integrator_kwargs=dict(), cython_if_possible=True,
                         save_all=True, return_device=False, stream=None, **time_spec):
@@ -169,6 +217,11 @@ class Hamiltonian:
           accept-reject and per-orbit step control (DOP853; ``nbatch`` does not
           apply).  Closed-form potentials only; results are not bit-compatible
           with gala (FP32 force accuracy, ~1e-7 relative per evaluation).
+        * ``surrogate`` -- a trained ``SurrogatePotential`` of this (SCF)
+          potential, or the path of one saved with ``SurrogatePotential.save``:
+          Leapfrog in FP32 with the learned force on the tensor cores (the
+          analytic force outside its trained radii).  Snapshots are taken every
+          ``out_stride`` steps (the run is continued from each snapshot).
         """
         import torch
 
@@ -207,6 +260,8 @@ class Hamiltonian:
                 f"{'Leapfrog' if Integrator is LeapfrogIntegrator else 'Ruth4'} integration is currently only "
                 f"supported for StaticFrame, not {self.frame.__class__.__name__}")
         kw = dict(Integrator_kwargs)
+        if kw.get("surrogate") is not None:
+            return self._integrate_surrogate(w0, kw, save_all, return_device, Integrator, **time_spec)
         precision = str(kw.get("precision", "fp64")).lower()
         if precision not in ("fp64", "fp32c"):
             raise ValueError(f"precision must be 'fp64' or 'fp32c' (got {precision!r})")

@@ -320,6 +320,27 @@ class SurrogatePotential:
                   float(dt), ptr(out), ptr(fb), grid or self._grid(n), stream_handle())
         return out, fb
 
+    # ------------------------------------------------------------ files
+    def save(self, path):
+        """Write the trained network (FP32 weights with the target scale folded
+        in) and its input box to an .npz file."""
+        np.savez(path, params=self.params.cpu().numpy(), r_min=self.r_min, r_max=self.r_max, split=self.split,
+                 scf_params=self.scf.packed().params)
+
+    @classmethod
+    def load(cls, path, scf):
+        """A network written by save(), for the same SCF potential `scf` (its
+        packed parameters must match the file's)."""
+        import torch
+
+        d = np.load(path)
+        if not np.array_equal(d["scf_params"], scf.packed().params):
+            raise ValueError(f"{path} was trained for a different SCF potential")
+        sp = cls(scf, r_min=float(d["r_min"]), r_max=float(d["r_max"]), split=int(d["split"]))
+        sp.params = torch.from_numpy(np.ascontiguousarray(d["params"], dtype=np.float32)).to(sp.dev)
+        sp.export()
+        return sp
+
     def forward_fp32(self, xh):
         """Network value and input gradient in FP32 (training kernels), xh (N, 3)."""
         import torch

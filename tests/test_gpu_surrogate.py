@@ -197,3 +197,35 @@ def test_tcgen05_leapfrog_matches_mma_leapfrog(scf):
     assert np.median(err) < 1e-4, np.median(err)
     assert int(fb_tc.item()) == int(fb_mm.item())
 
+
+
+def test_integrate_orbit_with_surrogate_and_file_round_trip(scf, tmp_path):
+    """The surrogate through the drop-in call: integrate_orbit with
+    Integrator_kwargs surrogate= (an object or a saved file), snapshots every
+    out_stride steps, equal to the same chunked run through the surrogate's own
+    call; refused for other integrators."""
+    import torch
+
+    sp = S.SurrogatePotential(scf, seed=14)
+    sp.export()
+    w0 = W.scf_ics(300, seed=15)
+    o = scf.integrate_orbit(w0, dt=1.0, n_steps=40, Integrator="leapfrog",
+                            Integrator_kwargs=dict(surrogate=sp, out_stride=10))
+    w = o.w()
+    assert w.shape == (6, 5, 300)
+    np.testing.assert_array_equal(o.t, np.arange(0.0, 41.0, 10.0))
+    np.testing.assert_array_equal(w[:, 0], w0)
+    wd = torch.from_numpy(w0).cuda()
+    for _ in range(4):
+        wd, _ = sp.integrate_leapfrog(wd, 1.0, 10)
+    np.testing.assert_array_equal(w[:, -1], wd.cpu().numpy())
+    path = tmp_path / "surrogate.npz"
+    sp.save(path)
+    o2 = scf.integrate_orbit(w0, dt=1.0, n_steps=40, Integrator="leapfrog",
+                             Integrator_kwargs=dict(surrogate=str(path), out_stride=10))
+    np.testing.assert_array_equal(o2.w(), w)
+    last = scf.integrate_orbit(w0, dt=1.0, n_steps=40, Integrator="leapfrog",
+                               Integrator_kwargs=dict(surrogate=sp), save_all=False)
+    assert last.w().shape == (6, 1, 300)
+    with pytest.raises(ValueError, match="LeapfrogIntegrator"):
+        scf.integrate_orbit(w0, dt=1.0, n_steps=4, Integrator="dop853", Integrator_kwargs=dict(surrogate=sp))

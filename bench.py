@@ -106,7 +106,9 @@ def parse_args():
     p.add_argument("--batch-step-scale", type=float, default=1.0, help="multiply the batch step counts")
     p.add_argument("--batch-precision", default="both", choices=["both", "fp32c", "fp64"])
     p.add_argument("--no-autotune", action="store_true", help="use the cached or default launch shape")
-    p.add_argument("--surrogate-steps", type=int, default=6000, help="training steps of the SCF surrogate")
+    p.add_argument("--surrogate-steps", type=int, default=30000, help="training steps of the SCF surrogate")
+    p.add_argument("--surrogate-split", type=int, default=2, choices=[1, 2, 3],
+                   help="tensor-core operands: 1 BF16, 2 BF16 hi+lo activations, 3 FP16")
     p.add_argument("--surrogate-orbits", type=int, default=262_144)
     p.add_argument("--surrogate-nsteps", type=int, default=5000)
     p.add_argument("--skip", default="", help="comma-separated variants to leave out")
@@ -642,18 +644,21 @@ def run_scf_surrogate(args, torch, stream):
     """SCF(m=1e12, r_s=20, nmax=12, lmax=8) with random coefficients, 262,144
     orbits, dt = 1 Myr, 5,000 Leapfrog steps.  A surrogate is trained on 16M
     analytic samples (timed separately), then the same FP32 leapfrog runs with
-    (a) the BF16 tensor-core surrogate, (b) the analytic SCF force in FP32; the
-    plain FP64 form (gala's arithmetic, analytic SCF) is timed on a 20-step run
-    of all orbits.  Accuracy: force error on 50k held-out points, orbit position
-    error and analytic-energy drift against the FP64 form on 2,048 orbits over
-    1,000 steps."""
+    (a) the tensor-core surrogate, (b) the analytic SCF force in FP32; the plain
+    FP64 form (gala's arithmetic, analytic SCF) is timed on a 20-step run of all
+    orbits.  Accuracy: force and potential error on 50k held-out points; orbit
+    position error and energy change against the FP64 form on 2,048 orbits over
+    1,000 steps (the energy change minus the FP64 orbit's own, which carries
+    Leapfrog's truncation oscillation).  Gain at equal accuracy: the analytic
+    SCF cut at the lowest degree L whose force error does not exceed the
+    surrogate's, timed the same way."""
     import gala_gb300 as g
     from gala_gb300 import surrogate as S
     from gala_gb300 import workloads as W
 
     n_orbits, n_steps = args.surrogate_orbits, args.surrogate_nsteps
     scf = W.scf_potential()
-    sp = S.SurrogatePotential(scf, seed=0)
+    sp = S.SurrogatePotential(scf, seed=0, split=args.surrogate_split)
     t0 = time.perf_counter()
     sp.make_dataset(n_samples=16 << 20)
     torch.cuda.synchronize()
@@ -663,9 +668,16 @@ def run_scf_surrogate(args, torch, stream):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     x = sp.sample_positions(50000, seed=99)
-    grad, _ = sp.gradient_and_energy(x)
-    ref = scf.gradient(x.cpu().numpy())
-    ferr = np.linalg.norm(grad.cpu().numpy() - ref, axis=0) / np.linalg.norm(ref, axis=0)
+    xh = x.cpu().numpy()
+    ref = scf.gradient(xh)
+    pref = scf.energy(xh)
+
+    def ferr(gr):
+        return np.linalg.norm(gr - ref, axis=0) / np.linalg.norm(ref, axis=0)
+
+    grad, phi = sp.gradient_and_energy(x)
+    fe = ferr(grad.cpu().numpy())
+    pe = np.abs(phi.cpu().numpy() - pref) / np.abs(pref)
     w0 = W.scf_ics(n_orbits)
 
     def timed(fn):
@@ -684,40 +696,59 @@ def run_scf_surrogate(args, torch, stream):
     ms_f64, _ = timed(lambda: scf.integrate_orbit(w0, dt=1.0, n_steps=20, Integrator="leapfrog", save_all=False,
                                                   return_device=True))
     v_sur = n_orbits * n_steps / (ms_sur * 1e-3)
-    flops_run = float(n_orbits * (n_steps + 1)) * 6 * 2 * 2 * 256 * 256
+    flops_run = float(n_orbits * (n_steps + 1)) * 6 * 2 * 256 * 256 * (2 if sp.split == 2 else 1)
     bf16_peak, bf16_src = measured_peak("bf16_tflops_sustained", 1700.0)
     v_f32 = n32 * 200 / (ms_f32 * 1e-3)
     v_f64 = n_orbits * 20 / (ms_f64 * 1e-3)
+
+    # the analytic SCF cut to the surrogate's force accuracy
+    trunc = None
+    for L in range(0, int(scf.parameters["Snlm"].shape[1])):
+        sc = S.truncated_scf(scf, L)
+        e_L = ferr(sc.gradient(xh))
+        if np.median(e_L) <= np.median(fe):
+            sp_L = S.SurrogatePotential(sc, seed=0)
+            ms_L, _ = timed(lambda: sp_L.integrate_leapfrog(w0[:, :n32], 1.0, 200, analytic=True))
+            trunc = {"lmax": L, "force_error_median": float(np.median(e_L)), "value": n32 * 200 / (ms_L * 1e-3)}
+            break
+
     sub = w0[:, :min(2048, n_orbits)]
     o64 = scf.integrate_orbit(sub, dt=1.0, n_steps=1000, Integrator="leapfrog", save_all=False).w().reshape(6, -1)
     osur = sp.integrate_leapfrog(sub, 1.0, 1000)[0].cpu().numpy()
     o32 = sp.integrate_leapfrog(sub, 1.0, 1000, analytic=True)[0].cpu().numpy()
     H = g.Hamiltonian(scf)
     E0 = H.energy(sub)
+    dE64 = (H.energy(o64) - E0) / E0
 
     def errs(o):
-        pe = np.linalg.norm(o[:3] - o64[:3], axis=0) / np.linalg.norm(o64[:3], axis=0)
-        dE = np.abs((H.energy(o) - E0) / E0)
-        return {"position_error_median": float(np.median(pe)), "position_error_p90": float(np.percentile(pe, 90)),
-                "dE_over_E_analytic_median": float(np.median(dE))}
+        pe_ = np.linalg.norm(o[:3] - o64[:3], axis=0) / np.linalg.norm(o64[:3], axis=0)
+        dE = (H.energy(o) - E0) / E0
+        return {"position_error_median": float(np.median(pe_)), "position_error_p90": float(np.percentile(pe_, 90)),
+                "dE_over_E_median": float(np.median(np.abs(dE))),
+                "dE_over_E_vs_fp64_median": float(np.median(np.abs(dE - dE64)))}
 
     return {
         "workload": f"scf_surrogate: SCF m=1e12 r_s=20 nmax=12 lmax=8, {n_orbits} orbits, dt 1 Myr, "
                     f"{n_steps} Leapfrog steps",
-        "surrogate": {"value": v_sur, "ms": ms_sur, "fallback_force_evaluations": int(fb.item()),
+        "surrogate": {"value": v_sur, "ms": ms_sur, "operands": {1: "BF16", 2: "BF16 hi+lo", 3: "FP16"}[sp.split],
+                      "fallback_force_evaluations": int(fb.item()),
                       "roofline": {"bound": "tensor", "unit": "TFLOP/s",
                                    "achieved": flops_run / (ms_sur * 1e-3) / 1e12, "peak": bf16_peak,
                                    "frac": flops_run / (ms_sur * 1e-3) / 1e12 / bf16_peak,
                                    "peak_source": f"{bf16_src}, cuBLAS BF16 sustained"}},
         "fp32_analytic": {"value": v_f32, "sample": f"{n32} orbits x 200 steps"},
         "fp64_analytic_plain": {"value": v_f64, "sample": f"{n_orbits} orbits x 20 steps"},
+        "equal_accuracy_analytic": trunc,
         "speedup_surrogate_vs_fp64": v_sur / v_f64,
         "speedup_surrogate_vs_fp32_analytic": v_sur / v_f32,
+        "speedup_at_equal_accuracy": (v_sur / trunc["value"]) if trunc else None,
         "training": {"samples": int(sp.X.shape[0]), "steps": args.surrogate_steps, "dataset_s": t_data,
                      "train_s": t_train, "loss_history": hist},
-        "force_error": {"median": float(np.median(ferr)), "p90": float(np.percentile(ferr, 90)),
-                        "p99": float(np.percentile(ferr, 99))},
-        "orbits_vs_fp64_2048x1000": {"surrogate": errs(osur), "fp32_analytic": errs(o32)},
+        "force_error": {"median": float(np.median(fe)), "p90": float(np.percentile(fe, 90)),
+                        "p99": float(np.percentile(fe, 99))},
+        "potential_error": {"median": float(np.median(pe)), "p90": float(np.percentile(pe, 90))},
+        "orbits_vs_fp64_2048x1000": {"surrogate": errs(osur), "fp32_analytic": errs(o32),
+                                     "fp64_leapfrog_own_dE_median": float(np.median(np.abs(dE64)))},
     }
 
 
@@ -961,13 +992,16 @@ def compact(name, r):
                 "gpu_vs_cpu_max_rel": sig(cb.get("gpu_vs_cpu_max_rel"), 2)}
     if name == "scf_surrogate":
         o = r["orbits_vs_fp64_2048x1000"]
-        return {"surrogate": sig(r["surrogate"]["value"]), "fp32_analytic": sig(r["fp32_analytic"]["value"]),
-                "fp64_plain": sig(r["fp64_analytic_plain"]["value"]),
+        t = r["equal_accuracy_analytic"] or {}
+        return {"surrogate": sig(r["surrogate"]["value"]), "operands": r["surrogate"]["operands"],
+                "fp32_analytic": sig(r["fp32_analytic"]["value"]), "fp64_plain": sig(r["fp64_analytic_plain"]["value"]),
+                "force_err_median": sig(r["force_error"]["median"], 2),
                 "sur_pos_err_median": sig(o["surrogate"]["position_error_median"], 2),
-                "sur_dE_median": sig(o["surrogate"]["dE_over_E_analytic_median"], 2),
+                "sur_dE_vs_fp64_median": sig(o["surrogate"]["dE_over_E_vs_fp64_median"], 2),
                 "fp32_pos_err_median": sig(o["fp32_analytic"]["position_error_median"], 2),
-                "fp32_dE_median": sig(o["fp32_analytic"]["dE_over_E_analytic_median"], 2),
-                "frac_bf16": sig(r["surrogate"]["roofline"]["frac"], 3)}
+                "fp32_dE_vs_fp64_median": sig(o["fp32_analytic"]["dE_over_E_vs_fp64_median"], 2),
+                "equal_acc_lmax": t.get("lmax"), "speedup_at_equal_accuracy": sig(r["speedup_at_equal_accuracy"], 3),
+                "frac_tensor": sig(r["surrogate"]["roofline"]["frac"], 3)}
     if name == "mock_streams":
         return {"unit": "particle-steps/s", "pipeline": sig(r["pipeline"]["value"]),
                 "release_kernel": sig(r["release_kernel"]["value"]),

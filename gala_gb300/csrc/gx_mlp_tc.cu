@@ -7,10 +7,11 @@
 // access) and column slice w / 4 (64 columns), so each row's epilogue is shared
 // by four threads and every scheduler has four warps to hide latency.  Per tile:
 //   * layer 1 (3 -> 256) in FP32 on the CUDA cores;
-//   * layers 2-4 and the three input-gradient GEMMs are 128 x 256 x 256 BF16
-//     tcgen05.mma (kind::f16, FP32 accumulation into TMEM columns 0..255), the
-//     A operand (activations / deltas) as BF16 hi + lo parts, both K-major in
-//     shared memory with the 128-byte swizzle;
+//   * layers 2-4 and the three input-gradient GEMMs are 128 x 256 x 256
+//     tcgen05.mma (kind::f16, FP32 accumulation into TMEM columns 0..255) with
+//     BF16 operands (the A operand -- activations / deltas -- optionally as
+//     BF16 hi + lo parts) or FP16 operands, both K-major in shared memory with
+//     the 128-byte swizzle;
 //   * the weights (W2, W3, W4, W4^T, W3^T, W2^T) are kept in global memory as
 //     pre-swizzled 32 KB images of 64-wide K chunks (768 KB, L2-resident) and
 //     streamed into two shared buffers with cp.async.bulk, one chunk ahead of
@@ -82,8 +83,17 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
            ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
-// Instruction descriptor: BF16 x BF16 -> FP32, both K-major, M = 128, N = 256.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(H >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+// Operand modes (the `split` argument): 1 = BF16 operands, 2 = BF16 weights
+// with the activations as BF16 hi + lo parts (two MMAs per K step), 3 = FP16
+// operands (11-bit mantissa for weights and activations, one MMA per K step).
+template <int SPLIT>
+constexpr int NPART = SPLIT == 2 ? 2 : 1;
+
+// Instruction descriptor (kind::f16): FP32 accumulator, A and B of the same
+// type -- BF16 (type code 1) or FP16 (code 0) -- both K-major, M = 128, N = 256.
+template <int SPLIT>
+constexpr uint32_t IDESC = (1u << 4) | ((SPLIT == 3 ? 0u : 1u) << 7) | ((SPLIT == 3 ? 0u : 1u) << 10) |
+                           ((uint32_t)(H >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
 
 __device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count));
@@ -111,10 +121,11 @@ __device__ __forceinline__ void bulk_copy(void *dst, const void *src, uint32_t b
         : "memory");
 }
 
+template <int SPLIT>
 __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t acc) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
-        "l"(a), "l"(b), "r"(IDESC), "r"(acc));
+        "l"(a), "l"(b), "r"(IDESC<SPLIT>), "r"(acc));
 }
 
 __device__ __forceinline__ void commit(uint64_t *bar) {
@@ -170,7 +181,8 @@ __device__ __forceinline__ void silu2(float z, float &a, float &s1) {
 }
 
 // Write 32 consecutive values (columns j0..j0+31, j0 a multiple of 32) of row
-// `row` of the A operand: BF16 hi part and the BF16 rounding remainder (lo).
+// `row` of the A operand: BF16 hi part and the BF16 rounding remainder (lo), or
+// FP16 values (SPLIT 3).
 template <int SPLIT>
 __device__ __forceinline__ void put_a(uint8_t *sA, int row, int j0, const float (&v)[32]) {
     const int c = j0 >> 6, g0 = (j0 & 63) >> 3;
@@ -180,6 +192,12 @@ __device__ __forceinline__ void put_a(uint8_t *sA, int row, int j0, const float 
 #pragma unroll
         for (int e = 0; e < 4; e++) {
             const float a = v[u * 8 + 2 * e], b = v[u * 8 + 2 * e + 1];
+            if constexpr (SPLIT == 3) {
+                const __half2 hh = __floats2half2_rn(a, b);
+                hw[e] = *reinterpret_cast<const uint32_t *>(&hh);
+                lw[e] = 0u;
+                continue;
+            }
             const __nv_bfloat162 hi = __floats2bfloat162_rn(a, b);
             hw[e] = *reinterpret_cast<const uint32_t *>(&hi);
             if constexpr (SPLIT == 2) {
@@ -226,9 +244,9 @@ __device__ bool issue_gemm(Issuer &I, Shared &S, uint8_t *sA, uint32_t tmem) {
         for (int s = 0; s < 4; s++) {
             const uint64_t bd = desc_sw128(wbase + s * 32);
 #pragma unroll
-            for (int part = 0; part < SPLIT; part++) {
+            for (int part = 0; part < NPART<SPLIT>; part++) {
                 const uint64_t ad = desc_sw128(su32(sA + part * A_PART + c * A_CHUNK + s * 32));
-                mma(tmem, ad, bd, (c | s | part) ? 1u : 0u);
+                mma<SPLIT>(tmem, ad, bd, (c | s | part) ? 1u : 0u);
             }
         }
         commit(&S.wempty[b]);
@@ -641,6 +659,10 @@ static int tc_args(const float *scf_params, double r_min, double r_max, double G
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
         GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_leapfrog_tc_kernel<2>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_eval_tc_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         SMEM_BYTES));
+        GX_CUDA_TRY(cudaFuncSetAttribute(surrogate_leapfrog_tc_kernel<3>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
         configured.fetch_or(bit);
     }
     return GX_OK;
@@ -656,8 +678,12 @@ extern "C" int gx_surrogate_gradient_tc(const float *params, const void *wimg, c
     if (n == 0) return GX_OK;
     GX_CHECK_ARG(params && wimg && q && grad && status && grid >= 1, "NULL array or bad grid");
     GX_CHECK_ARG(((uintptr_t)wimg & 15) == 0, "weight image must be 16-byte aligned");
-    GX_CHECK_ARG(split == 1 || split == 2, "split must be 1 (BF16 activations) or 2 (BF16 hi + lo)");
-    if (split == 2)
+    GX_CHECK_ARG(split >= 1 && split <= 3,
+                 "split must be 1 (BF16 activations), 2 (BF16 hi + lo) or 3 (FP16 operands)");
+    if (split == 3)
+        surrogate_eval_tc_kernel<3><<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
+            A, params, static_cast<const uint8_t *>(wimg), q, n, grad, phi, status);
+    else if (split == 2)
         surrogate_eval_tc_kernel<2><<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
             A, params, static_cast<const uint8_t *>(wimg), q, n, grad, phi, status);
     else
@@ -677,8 +703,12 @@ extern "C" int gx_surrogate_leapfrog_tc(const float *params, const void *wimg, c
     if (n == 0) return GX_OK;
     GX_CHECK_ARG(params && wimg && w0 && w_out && fallbacks && status && grid >= 1, "NULL array or bad grid");
     GX_CHECK_ARG(((uintptr_t)wimg & 15) == 0, "weight image must be 16-byte aligned");
-    GX_CHECK_ARG(split == 1 || split == 2, "split must be 1 (BF16 activations) or 2 (BF16 hi + lo)");
-    if (split == 2)
+    GX_CHECK_ARG(split >= 1 && split <= 3,
+                 "split must be 1 (BF16 activations), 2 (BF16 hi + lo) or 3 (FP16 operands)");
+    if (split == 3)
+        surrogate_leapfrog_tc_kernel<3><<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
+            A, params, static_cast<const uint8_t *>(wimg), w0, n, n_steps, (float)dt, w_out, fallbacks, status);
+    else if (split == 2)
         surrogate_leapfrog_tc_kernel<2><<<grid, NT, SMEM_BYTES, gx::as_stream(stream)>>>(
             A, params, static_cast<const uint8_t *>(wimg), w0, n, n_steps, (float)dt, w_out, fallbacks, status);
     else

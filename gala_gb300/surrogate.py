@@ -97,6 +97,17 @@ def scf_l0(scf, r, xp=np):
     return -GM / rs * sp * i1, GM / rs ** 2 * sd * i1
 
 
+def truncated_scf(scf, L):
+    """The SCF potential with its expansion cut at degree l <= L (the same n
+    range): the analytic method at a chosen lower accuracy, the baseline a
+    surrogate of the same accuracy is compared with."""
+    from .potential import SCFPotential
+
+    S, T = scf.parameters["Snlm"], scf.parameters["Tnlm"]
+    return SCFPotential(m=scf.parameters["m"], r_s=scf.parameters["r_s"], Snlm=np.asarray(S)[:, :L + 1, :L + 1],
+                        Tnlm=np.asarray(T)[:, :L + 1, :L + 1])
+
+
 class SurrogatePotential:
     """Surrogate of an SCFPotential (or any potential whose monopole is the
     Hernquist sphere (m, r_s)), trained on the GPU."""
@@ -209,6 +220,7 @@ class SurrogatePotential:
         h = stream_handle()
         qp = self.params.clone()
         qat_start = int(steps * (1.0 - qat_fraction)) + 1
+        qdt = torch.float16 if self.split == 3 else torch.bfloat16   # the inference operand type
         big = [(o, o + H * H) for o in (OFF_W2, OFF_W3, OFF_W4)]
         for step in range(1, steps + 1):
             idx = torch.randint(0, N, (batch,), generator=gen, device=self.dev)
@@ -218,7 +230,7 @@ class SurrogatePotential:
             if step >= qat_start:
                 qp.copy_(self.params)
                 for a, b in big:
-                    qp[a:b] = self.params[a:b].to(torch.bfloat16).float()
+                    qp[a:b] = self.params[a:b].to(qdt).float()
                 use = qp
             _abi.call("gx_mlp_train_step", ptr(use), ptr(grads), ptr(xb), ptr(yb), ptr(gb), ptr(wb), batch,
                       C.c_float(1.0), C.c_float(beta), ptr(ws), ptr(loss), h)
@@ -245,12 +257,24 @@ class SurrogatePotential:
         pack = [Ws[0], Ws[1], Ws[2], Ws[2].T, Ws[1].T, Ws[0].T]
         self.wbf16 = torch.stack([w.contiguous() for w in pack]).to(torch.bfloat16).contiguous()
         # [matrix][row][chunk][granule][8] -> [matrix][chunk][row][granule ^ (row & 7)][8]
-        v = self.wbf16.view(6, H, H // 64, 8, 8).permute(0, 2, 1, 3, 4).contiguous()
+        self.wimg = self._image(self.wbf16)
+        self.wimg16 = self._image(torch.stack([w.contiguous() for w in pack]).to(torch.float16).contiguous())
+        return self.wbf16
+
+    @staticmethod
+    def _image(w16):
+        """Tensor-core image of six 256 x 256 16-bit matrices (BF16 or FP16):
+        64-wide K chunks with the 128-byte swizzle."""
+        import torch
+
+        v = w16.view(6, H, H // 64, 8, 8).permute(0, 2, 1, 3, 4).contiguous()
         rows = torch.arange(H, device=v.device)
         src = (torch.arange(8, device=v.device)[None, :] ^ (rows[:, None] & 7))  # [row][dest granule] -> source
         idx = src.view(1, 1, H, 8, 1).expand(6, H // 64, H, 8, 8)
-        self.wimg = torch.gather(v, 3, idx).contiguous()
-        return self.wbf16
+        return torch.gather(v, 3, idx).contiguous()
+
+    def _tc_image(self):
+        return self.wimg16 if self.split == 3 else self.wimg
 
     # ------------------------------------------------------------ inference
     def _grid(self, n, tile=64):
@@ -276,13 +300,14 @@ class SurrogatePotential:
         phi = torch.empty(n, dtype=torch.float64, device=self.dev)
         if engine == "tcgen05":
             status = torch.zeros(1, dtype=torch.int32, device=self.dev)
-            _abi.call("gx_surrogate_gradient_tc", ptr(self.params), ptr(self.wimg), ptr(self.scf_f32), self.r_min,
+            _abi.call("gx_surrogate_gradient_tc", ptr(self.params), ptr(self._tc_image()), ptr(self.scf_f32), self.r_min,
                       self.r_max, self.GM, self.r_s, self.split, ptr(qd), n, ptr(grad), ptr(phi),
                       self._grid(n, 128), ptr(status), stream_handle())
             self._check(status)
         else:
+            # the warp-level engine has BF16 operands only (split 1 or 2)
             _abi.call("gx_surrogate_gradient", ptr(self.params), ptr(self.wbf16), ptr(self.scf_f32), self.r_min,
-                      self.r_max, self.GM, self.r_s, self.split, ptr(qd), n, ptr(grad), ptr(phi), self._grid(n),
+                      self.r_max, self.GM, self.r_s, min(self.split, 2), ptr(qd), n, ptr(grad), ptr(phi), self._grid(n),
                       stream_handle())
         return grad, phi
 
@@ -309,14 +334,14 @@ class SurrogatePotential:
         fb = torch.zeros(1, dtype=torch.int64, device=self.dev)
         if (engine or self.engine) == "tcgen05" and not analytic:
             status = torch.zeros(1, dtype=torch.int32, device=self.dev)
-            _abi.call("gx_surrogate_leapfrog_tc", ptr(self.params), ptr(self.wimg), ptr(self.scf_f32), self.r_min,
+            _abi.call("gx_surrogate_leapfrog_tc", ptr(self.params), ptr(self._tc_image()), ptr(self.scf_f32), self.r_min,
                       self.r_max, self.GM, self.r_s, self.split, ptr(w0d), n, int(n_steps), float(dt), ptr(out),
                       ptr(fb), grid or self._grid(n, 128), ptr(status), stream_handle())
             self._check(status)
             return out, fb
         wb = ptr(self.wbf16) if self.wbf16 is not None else None
         _abi.call("gx_surrogate_leapfrog", ptr(self.params), wb, ptr(self.scf_f32), self.r_min,
-                  self.r_max, self.GM, self.r_s, self.split, int(bool(analytic)), ptr(w0d), n, int(n_steps),
+                  self.r_max, self.GM, self.r_s, min(self.split, 2), int(bool(analytic)), ptr(w0d), n, int(n_steps),
                   float(dt), ptr(out), ptr(fb), grid or self._grid(n), stream_handle())
         return out, fb
 

@@ -132,30 +132,65 @@ def test_fallback_outside_trained_radii(scf, oracle):
     np.testing.assert_allclose(grad.cpu().numpy(), ref, rtol=1e-4)
 
 
-def test_trained_surrogate_accuracy_and_gain(scf, oracle):
-    import torch
-
+def test_trained_surrogate_accuracy(scf, oracle):
+    """A short training run on the small SCF halo: the loss falls, and force and
+    potential reach the accuracy this network class reaches at that length
+    (median force error < 2e-2, potential < 2e-3; the config-4 network trained
+    30,000 steps reaches ~3e-3 and ~2e-4, see the bench)."""
     sp = S.SurrogatePotential(scf, seed=9)
     sp.make_dataset(n_samples=1 << 20)
     hist = sp.train(steps=1500, batch=8192, log_every=500)
     assert hist[-1][1] < hist[0][1]
     x = sp.sample_positions(20000, seed=10)
     grad, phi = sp.gradient_and_energy(x)
-    ref = scf.gradient(x.cpu().numpy())
+    xh = x.cpu().numpy()
+    ref = scf.gradient(xh)
     err = np.linalg.norm(grad.cpu().numpy() - ref, axis=0) / np.linalg.norm(ref, axis=0)
     assert np.median(err) < 2e-2, np.median(err)
-    # gain: surrogate force vs the analytic SCF force in FP64 at the same points
-    xs = sp.sample_positions(1 << 18, seed=11)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    sp.gradient_and_energy(xs)
-    torch.cuda.synchronize()
-    t_sur = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    scf.gradient(xs.cpu().numpy())
-    torch.cuda.synchronize()
-    t_scf = time.perf_counter() - t0
-    assert t_sur < t_scf, (t_sur, t_scf)
+    perr = np.abs(phi.cpu().numpy() - scf.energy(xh)) / np.abs(scf.energy(xh))
+    assert np.median(perr) < 2e-3, np.median(perr)
+
+
+def test_surrogate_gain_at_equal_accuracy():
+    """What the trained network gains over the method without it, at equal
+    accuracy, both timed on the GPU: the config-4 SCF host (nmax 12, lmax 8)
+    and its surrogate after a short training; the analytic SCF cut at the
+    lowest degree L whose force error is no larger than the surrogate's is the
+    method without the network at the same accuracy.  The surrogate's FP32
+    leapfrog must outrun that analytic leapfrog."""
+    import torch
+
+    full = W.scf_potential()
+    sp = S.SurrogatePotential(full, seed=21)
+    sp.make_dataset(n_samples=1 << 21)
+    sp.train(steps=3000, batch=8192, log_every=1000)
+    x = sp.sample_positions(20000, seed=22)
+    xh = x.cpu().numpy()
+    ref = full.gradient(xh)
+
+    def ferr(gr):
+        return np.median(np.linalg.norm(gr - ref, axis=0) / np.linalg.norm(ref, axis=0))
+
+    e_sur = ferr(sp.gradient_and_energy(x)[0].cpu().numpy())
+    cut = None
+    for L in range(full.lmax + 1):
+        if ferr(S.truncated_scf(full, L).gradient(xh)) <= e_sur:
+            cut = S.SurrogatePotential(S.truncated_scf(full, L), seed=0)
+            break
+    assert cut is not None and cut.scf.lmax < full.lmax, "the surrogate should be worth a truncation"
+    w0 = W.scf_ics(1 << 16, seed=23)
+
+    def rate(fn):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return (1 << 16) * 50 / (time.perf_counter() - t0)
+
+    v_sur = rate(lambda: sp.integrate_leapfrog(w0, 1.0, 50))
+    v_cut = rate(lambda: cut.integrate_leapfrog(w0, 1.0, 50, analytic=True))
+    assert v_sur > v_cut, (v_sur, v_cut, cut.scf.lmax, e_sur)
 
 
 def test_surrogate_leapfrog_runs_and_matches_fp32_forces(scf):

@@ -27,6 +27,7 @@ UNITS = {
     "gx_fixed.cu": ["-fmad=false"],
     "gx_dop853.cu": ["-fmad=false"],
     "gx_nbody.cu": ["-fmad=false"],
+    "gx_nbody_wide.cu": ["-fmad=false"],
     "gx_lfnbody.cu": ["-fmad=false"],
     "gx_orbit.cu": ["-fmad=false"],
     "gx_peaks.cu": [],

@@ -1,0 +1,365 @@
+// gx_nbody_wide.cu -- FP64 DOP853 for mock-stream release systems wider than a
+// warp: one CTA per system, the system's state in device scratch.
+//
+// gala integrates every release of mockstream_dop853 (src/gala/dynamics/
+// mockstream/mockstream.pyx:176-303) as ONE dop853_step problem (dop853.pyx:
+// 27-75 -> dopcor, dopri/dop853.cpp:89-650) over [massive bodies, the particles
+// released at that time]: one step size, one error norm, one accept/reject and
+// stiffness decision for the whole system.  A release of thousands of particles
+// (gala's one-burst setting) does not fit the 32-lane groups of gx_nbody.cu, so
+// such systems run here:
+//   * one CTA per system; thread t owns members t, t + blockDim, ...;
+//   * the state (y, the stage derivatives, the stage argument) lives in device
+//     scratch as SoA rows [array][component][member] (L2-resident);
+//   * every stage is two passes separated by a barrier: all stage arguments,
+//     then all right-hand sides -- a member's right-hand side reads the massive
+//     bodies' stage positions (c_nbody_acceleration, cpotential.cpp:389-415);
+//   * the error and stiffness sums are CTA sums in a fixed order (each thread
+//     over its members in order, a warp butterfly, then the warps in order), so
+//     the run is deterministic; the order differs from gala's sequential loop,
+//     so results agree with gala to rounding, not bit for bit;
+//   * every scalar of the controller is computed identically by all threads from
+//     the same sums (uniform control flow), and the loop is bounded by nmax.
+#include "gx_host.h"
+#include "gx_scf.cuh"
+#include "gx_dop853_tableau.cuh"
+#include "gx_body.cuh"
+#include "gx_fast64.cuh"
+
+namespace gx {
+
+constexpr int WD_THREADS = 256;
+constexpr int WD_ARRAYS = 12;  // Y, K1..K10, YY1
+
+enum { A_Y = 0, A_K1, A_K2, A_K3, A_K4, A_K5, A_K6, A_K7, A_K8, A_K9, A_K10, A_YY1 };
+
+struct WideArgs {
+    int32_t nbody;
+    int32_t max_members;
+    int64_t n_streams, n_release, n_particles;
+    const gx_body *bodies;    // (n_streams, nbody)
+    const double *nbody_w;    // (n_streams, n_release, nbody, 6)
+    const double *release_t;  // (n_release)
+    const int64_t *offset;    // (n_release + 1)
+    const double *stream_w0;  // (n_streams, n_particles, 6)
+    double t_final, dt0, atol, rtol;
+    int64_t nmax;
+    const int64_t *systems;   // system ids si * n_streams + ss handled here
+    int64_t n_systems;
+    double *scratch;          // n_systems x WD_ARRAYS x 6 x max_members doubles
+    double *stream_w_out, *nbody_w_out;
+    int32_t *status;
+    int64_t *stats;
+};
+
+// Deterministic CTA sums of two values (each thread passes its partials).
+__device__ __forceinline__ void cta_sum2(double &a, double &b, double *red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+        red[wid] = a;
+        red[32 + wid] = b;
+    }
+    __syncthreads();
+    double sa = 0., sb = 0.;
+    for (int w = 0; w < nw; w++) {
+        sa += red[w];
+        sb += red[32 + w];
+    }
+    __syncthreads();
+    a = sa;
+    b = sb;
+}
+
+// Fwrapper_direct_nbody (dop853.cpp:990-1006) for member m of the system:
+// Hamilton's equations in the external potential, then the pull of every
+// non-null massive body j != m at its stage position.
+template <bool SCF>
+__device__ __forceinline__ void wide_rhs(const DevPot &pot, const DevFrame &fr, const gx_body *__restrict__ bod,
+                                         int nbody, const double *__restrict__ arg, int64_t M, int m,
+                                         double *__restrict__ kout) {
+    V6 w;
+#pragma unroll
+    for (int c = 0; c < 6; c++) w.v[c] = arg[c * M + m];
+    V6 k = fast::rhs_call_f<SCF>(pot, fr, w);
+    for (int j = 0; j < nbody; j++) {
+        const int type = __ldg(&bod[j].type);
+        if (j == m || type == GX_POT_NULL) continue;
+        double f2[3];
+        body_gradient(type, bod[j].params, w.v[0] - arg[j], w.v[1] - arg[M + j], w.v[2] - arg[2 * M + j], f2);
+        k.v[3] += -f2[0];
+        k.v[4] += -f2[1];
+        k.v[5] += -f2[2];
+    }
+#pragma unroll
+    for (int c = 0; c < 6; c++) kout[c * M + m] = k.v[c];
+}
+
+template <bool SCF>
+__global__ void __launch_bounds__(WD_THREADS)
+nbody_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFrame fr,
+                  const __grid_constant__ WideArgs A) {
+    using namespace dop;
+    __shared__ double red[64];
+    const int64_t b = blockIdx.x;
+    if (b >= A.n_systems) return;
+    const int64_t sys = A.systems[b];
+    const int64_t si = sys / A.n_streams, ss = sys - si * A.n_streams;
+    if (si < 0 || si >= A.n_release) return;  // an id outside the release grid: nothing to address
+    const int64_t o0 = A.offset[si], o1 = A.offset[si + 1];
+    const int64_t M = A.max_members;
+    const int nbody = A.nbody;
+    if (o1 < o0 || o0 < 0 || o1 > A.n_particles || nbody + (o1 - o0) > M) {
+        if (threadIdx.x == 0) A.status[ss * A.n_release + si] = -1;  // inconsistent offsets: no access
+        return;
+    }
+    const int nmem = nbody + (int)(o1 - o0);
+    const gx_body *bod = A.bodies + ss * nbody;
+    double *base = A.scratch + b * (int64_t)WD_ARRAYS * 6 * M;
+    double *Ar[WD_ARRAYS];
+#pragma unroll
+    for (int a = 0; a < WD_ARRAYS; a++) Ar[a] = base + (int64_t)a * 6 * M;
+    const int tid = threadIdx.x, nt = blockDim.x;
+
+    // the system at the release time: bodies, then the released particles
+    for (int m = tid; m < nmem; m += nt) {
+        const double *src = (m < nbody) ? A.nbody_w + ((ss * A.n_release + si) * nbody + m) * 6
+                                        : A.stream_w0 + (ss * A.n_particles + o0 + (m - nbody)) * 6;
+#pragma unroll
+        for (int c = 0; c < 6; c++) Ar[A_Y][c * M + m] = src[c];
+    }
+    __syncthreads();
+    for (int m = tid; m < nmem; m += nt) wide_rhs<SCF>(pot, fr, bod, nbody, Ar[A_Y], M, m, Ar[A_K1]);
+    __syncthreads();
+
+    // dop853_step's dop853() arguments (dop853.pyx:46-72) and front-end defaults
+    double x = A.release_t[si];
+    const double xend = A.t_final;
+    double h = A.dt0;
+    const double uround = 2.3E-16;
+    const int64_t nmax = A.nmax ? A.nmax : 1000000;
+    const int64_t nstiff = 1;
+    const double hmax = fabs(xend - x);
+    const double posneg = (xend - x < 0.0) ? -1.0 : 1.0;
+    const double safe = 0.9, facc1 = 1.0 / 0.333, facc2 = 1.0 / 6.0;
+    const double atoli = A.atol, rtoli = A.rtol;
+    int last = 0, reject = 0, iasti = 0, nonsti = 0, idid = 0;
+    double hlamb = 0.0;
+    int64_t nfcn = 2, nstep = 0, naccpt = 0, nrejct = 0;
+
+#define WSTAGE(dst, expr)                                                                              \
+    for (int m = tid; m < nmem; m += nt)                                                               \
+        for (int c = 0; c < 6; c++) {                                                                  \
+            const int64_t o = c * M + m;                                                               \
+            Ar[A_YY1][o] = (expr);                                                                     \
+        }                                                                                              \
+    __syncthreads();                                                                                   \
+    for (int m = tid; m < nmem; m += nt) wide_rhs<SCF>(pot, fr, bod, nbody, Ar[A_YY1], M, m, Ar[dst]); \
+    __syncthreads()
+#define K(a) Ar[a][o]
+
+    for (;;) {
+        if (nstep > nmax || h != h) {
+            idid = -2;  // a NaN step never recovers: gala's -2 after nmax rejections, at once
+            break;
+        }
+        if (0.1 * fabs(h) <= fabs(x) * uround) {
+            idid = -3;
+            break;
+        }
+        if ((x + 1.01 * h - xend) * posneg > 0.0) {
+            h = xend - x;
+            last = 1;
+        }
+        nstep++;
+        // the twelve stages (dop853.cpp:368-414), gala's term order as FMA chains
+        WSTAGE(A_K2, fma(h * a21, K(A_K1), K(A_Y)));
+        WSTAGE(A_K3, fma(h, fma(a32, K(A_K2), a31 * K(A_K1)), K(A_Y)));
+        WSTAGE(A_K4, fma(h, fma(a43, K(A_K3), a41 * K(A_K1)), K(A_Y)));
+        WSTAGE(A_K5, fma(h, fma(a54, K(A_K4), fma(a53, K(A_K3), a51 * K(A_K1))), K(A_Y)));
+        WSTAGE(A_K6, fma(h, fma(a65, K(A_K5), fma(a64, K(A_K4), a61 * K(A_K1))), K(A_Y)));
+        WSTAGE(A_K7, fma(h, fma(a76, K(A_K6), fma(a75, K(A_K5), fma(a74, K(A_K4), a71 * K(A_K1)))), K(A_Y)));
+        WSTAGE(A_K8, fma(h, fma(a87, K(A_K7), fma(a86, K(A_K6), fma(a85, K(A_K5), fma(a84, K(A_K4),
+                     a81 * K(A_K1))))), K(A_Y)));
+        WSTAGE(A_K9, fma(h, fma(a98, K(A_K8), fma(a97, K(A_K7), fma(a96, K(A_K6), fma(a95, K(A_K5),
+                     fma(a94, K(A_K4), a91 * K(A_K1)))))), K(A_Y)));
+        WSTAGE(A_K10, fma(h, fma(a109, K(A_K9), fma(a108, K(A_K8), fma(a107, K(A_K7), fma(a106, K(A_K6),
+                      fma(a105, K(A_K5), fma(a104, K(A_K4), a101 * K(A_K1))))))), K(A_Y)));
+        WSTAGE(A_K2, fma(h, fma(a1110, K(A_K10), fma(a119, K(A_K9), fma(a118, K(A_K8), fma(a117, K(A_K7),
+                     fma(a116, K(A_K6), fma(a115, K(A_K5), fma(a114, K(A_K4), a111 * K(A_K1)))))))), K(A_Y)));
+        const double xph = x + h;
+        WSTAGE(A_K3, fma(h, fma(a1211, K(A_K2), fma(a1210, K(A_K10), fma(a129, K(A_K9), fma(a128, K(A_K8),
+                     fma(a127, K(A_K7), fma(a126, K(A_K6), fma(a125, K(A_K5), fma(a124, K(A_K4),
+                     a121 * K(A_K1))))))))), K(A_Y)));
+        nfcn += 11;
+        // 8th-order solution (k4), new state (k5) and error terms (:416-444)
+        double err = 0.0, err2 = 0.0;
+        for (int m = tid; m < nmem; m += nt)
+            for (int c = 0; c < 6; c++) {
+                const int64_t o = c * M + m;
+                const double k4 = fma(b12, K(A_K3), fma(b11, K(A_K2), fma(b10, K(A_K10), fma(b9, K(A_K9),
+                                  fma(b8, K(A_K8), fma(b7, K(A_K7), fma(b6, K(A_K6), b1 * K(A_K1))))))));
+                const double k5 = fma(h, k4, K(A_Y));
+                const double isk = fast::rcp_f(fma(rtoli, fmax(fabs(K(A_Y)), fabs(k5)), atoli));
+                double erri = fma(-bhh3, K(A_K3), fma(-bhh2, K(A_K9), fma(-bhh1, K(A_K1), k4)));
+                double sqr = erri * isk;
+                err2 = fma(sqr, sqr, err2);
+                erri = fma(er12, K(A_K3), fma(er11, K(A_K2), fma(er10, K(A_K10), fma(er9, K(A_K9), fma(er8, K(A_K8),
+                       fma(er7, K(A_K7), fma(er6, K(A_K6), er1 * K(A_K1))))))));
+                sqr = erri * isk;
+                err = fma(sqr, sqr, err);
+                K(A_K4) = k4;
+                K(A_K5) = k5;
+            }
+        cta_sum2(err, err2, red);
+        double deno = err + 0.01 * err2;
+        if (deno <= 0.0) deno = 1.0;
+        err = fabs(h) * err * sqrt(1.0 / (deno * (double)(6 * nmem)));
+        const double fac11 = sqrt(sqrt(sqrt(err)));  // gala's pow(err, 1/8) (beta = 0)
+        const double fac = fmax(facc2, fmin(facc1, fac11 / safe));
+        double hnew = h / fac;
+        if (err <= 1.0) {
+            naccpt++;
+            // FSAL: k4 = f(k5), the new state; k5 holds the positions the pulls need
+            for (int m = tid; m < nmem; m += nt) wide_rhs<SCF>(pot, fr, bod, nbody, Ar[A_K5], M, m, Ar[A_K4]);
+            __syncthreads();
+            nfcn++;
+            // stiffness detection (:463-486) after every accepted step (nstiff =
+            // 1); the first detection returns -4 as in gala
+            double stnum = 0.0, stden = 0.0;
+            for (int m = tid; m < nmem; m += nt)
+                for (int c = 0; c < 6; c++) {
+                    const int64_t o = c * M + m;
+                    double d = K(A_K4) - K(A_K3);
+                    stnum += d * d;
+                    d = K(A_K5) - K(A_YY1);
+                    stden += d * d;
+                }
+            cta_sum2(stnum, stden, red);
+            if (!(naccpt % nstiff) || iasti > 0) {
+                if (stden > 0.0) hlamb = h * sqrt(stnum / stden);
+                if (hlamb > 6.1) {
+                    nonsti = 0;
+                    iasti++;
+                    idid = -4;
+                    break;
+                }
+                nonsti++;
+                if (nonsti == 6) iasti = 0;
+            }
+            for (int m = tid; m < nmem; m += nt)
+                for (int c = 0; c < 6; c++) {
+                    const int64_t o = c * M + m;
+                    K(A_K1) = K(A_K4);
+                    K(A_Y) = K(A_K5);
+                }
+            __syncthreads();
+            x = xph;
+            if (last) {
+                idid = 1;
+                break;
+            }
+            if (fabs(hnew) > hmax) hnew = posneg * hmax;
+            if (reject) hnew = posneg * fmin(fabs(hnew), fabs(h));
+            reject = 0;
+        } else {
+            hnew = h / fmin(facc1, fac11 / safe);
+            reject = 1;
+            if (naccpt >= 1) nrejct++;
+            last = 0;
+        }
+        h = hnew;
+    }
+#undef K
+#undef WSTAGE
+    (void)nonsti;
+    __syncthreads();
+    for (int m = tid; m < nmem; m += nt) {
+        double *dst = nullptr;
+        if (m >= nbody) dst = A.stream_w_out + (ss * A.n_particles + o0 + (m - nbody)) * 6;
+        else if (A.nbody_w_out && o1 == A.offset[A.n_release]) dst = A.nbody_w_out + (ss * nbody + m) * 6;
+        if (dst)
+            for (int c = 0; c < 6; c++) dst[c] = Ar[A_Y][c * M + m];
+    }
+    if (tid == 0) {
+        const int64_t k = ss * A.n_release + si;
+        A.status[k] = idid;
+        if (A.stats) {
+            A.stats[4 * k + 0] = nfcn;
+            A.stats[4 * k + 1] = nstep;
+            A.stats[4 * k + 2] = naccpt;
+            A.stats[4 * k + 3] = nrejct;
+        }
+    }
+}
+
+}  // namespace gx
+
+extern "C" int64_t gx_mockstream_wide_scratch_bytes(int64_t n_systems, int32_t max_members) {
+    if (n_systems <= 0 || max_members <= 0) return 0;
+    return n_systems * (int64_t)gx::WD_ARRAYS * 6 * (int64_t)max_members * (int64_t)sizeof(double);
+}
+
+extern "C" int gx_mockstream_dop853_wide(const gx_potential *pot, const gx_frame *frame, int64_t n_streams,
+                                         int32_t nbody, const gx_body *bodies, const double *nbody_w,
+                                         int64_t n_release, const double *release_t, const int64_t *release_offset,
+                                         const double *stream_w0, int64_t n_particles, double t_final, double dt0,
+                                         double atol, double rtol, int64_t nmax, const int64_t *systems,
+                                         int64_t n_systems, int32_t max_members, double *scratch,
+                                         int64_t scratch_bytes, double *stream_w_out, double *nbody_w_out,
+                                         int32_t *status, int64_t *stats, void *stream) {
+    gx::DevPot dp;
+    gx::DevFrame df;
+    int rc = gx::pack_potential(pot, &dp);
+    if (rc) return rc;
+    rc = gx::pack_frame(frame, &df);
+    if (rc) return rc;
+    GX_CHECK_ARG(n_streams >= 1 && n_release >= 0 && n_particles >= 0 && n_systems >= 0, "bad size");
+    GX_CHECK_ARG(nbody >= 1, "nbody must be >= 1 (the progenitor)");
+    GX_CHECK_ARG(max_members > nbody, "max_members must exceed nbody");
+    GX_CHECK_ARG(nmax >= 0, "nmax must be >= 0 (0 = gala's default 1e6)");
+    GX_CHECK_ARG(atol >= 0 && rtol >= 0, "tolerances must be non-negative");
+    GX_CHECK_ARG(dt0 != 0.0, "dt0 (the release grid's step, gala's h0) must be non-zero");
+    if (n_systems == 0) return GX_OK;
+    GX_CHECK_ARG(bodies && nbody_w && release_t && release_offset && stream_w0 && systems && scratch && status &&
+                     stream_w_out,
+                 "NULL array");
+    GX_CHECK_ARG(n_systems <= (int64_t)INT32_MAX, "too many systems");
+    const int64_t need = gx_mockstream_wide_scratch_bytes(n_systems, max_members);
+    GX_CHECK_ARG(scratch_bytes >= need, "scratch of %lld bytes, %lld needed", (long long)scratch_bytes,
+                 (long long)need);
+    gx::WideArgs A;
+    memset(&A, 0, sizeof(A));
+    A.nbody = nbody;
+    A.max_members = max_members;
+    A.n_streams = n_streams;
+    A.n_release = n_release;
+    A.n_particles = n_particles;
+    A.bodies = bodies;
+    A.nbody_w = nbody_w;
+    A.release_t = release_t;
+    A.offset = release_offset;
+    A.stream_w0 = stream_w0;
+    A.t_final = t_final;
+    A.dt0 = dt0;
+    A.atol = atol;
+    A.rtol = rtol;
+    A.nmax = nmax;
+    A.systems = systems;
+    A.n_systems = n_systems;
+    A.scratch = scratch;
+    A.stream_w_out = stream_w_out;
+    A.nbody_w_out = nbody_w_out;
+    A.status = status;
+    A.stats = stats;
+    cudaStream_t st = gx::as_stream(stream);
+    if (dp.has_scf)
+        gx::nbody_wide_kernel<true><<<(unsigned)n_systems, gx::WD_THREADS, 0, st>>>(dp, df, A);
+    else
+        gx::nbody_wide_kernel<false><<<(unsigned)n_systems, gx::WD_THREADS, 0, st>>>(dp, df, A);
+    return gx::check_launch("mockstream_dop853_wide");
+}

@@ -462,11 +462,11 @@ class MockStreamGenerator:
             nbody_w, st = integrate_systems(H, bodies, nbody0, time, save_all=True, nstiff=-1, stream=stream,
                                             **dop)
             check(st, "nbody")
-        if nb + max_per > 32:
-            raise NotImplementedError(
-                f"{nb} bodies + {max_per} particles released at one time exceed the 32-lane DOP853 system; gala "
-                "integrates a release as one system sharing a step size, so it cannot be split without changing "
-                "the result: release fewer particles per time, or use the Leapfrog integrator (splits exactly)")
+        # releases of more than 32 - nb particles are systems wider than a warp:
+        # the 32-lane kernel marks them (-1) and the CTA-per-system kernel then
+        # integrates each as the one system gala makes of it
+        wide_rel = np.nonzero(nb + nstream > 32)[0]
+        max_group = min(max_per, 32 - nb)
         n_rel = len(time)
         stream_out = torch.empty((S, n_rows, 6), dtype=torch.float64, device=dev)
         nbody_out = torch.empty((S, nb, 6), dtype=torch.float64, device=dev)
@@ -476,10 +476,22 @@ class MockStreamGenerator:
         bd = bodies_to_device(bodies, dev)
         td = torch.from_numpy(time).to(dev)
         od = torch.from_numpy(rel_off).to(dev)
+        dt0 = float(time[1] - time[0])
         _abi.call("gx_mockstream_dop853", H.potential.packed().for_device(), H._frame_ref(), S, nb, ptr(bd),
-                  ptr(nbody_w), n_rel, ptr(td), ptr(od), max_per, ptr(stream_w0), n_rows, float(orbit_t[-1]),
-                  float(time[1] - time[0]), dop["atol"], dop["rtol"], dop["nmax"], ptr(stream_out), ptr(nbody_out),
+                  ptr(nbody_w), n_rel, ptr(td), ptr(od), max_group, ptr(stream_w0), n_rows, float(orbit_t[-1]),
+                  dt0, dop["atol"], dop["rtol"], dop["nmax"], ptr(stream_out), ptr(nbody_out),
                   ptr(status), ptr(stats) if stats is not None else None, ptr(counter), stream_handle(stream))
+        if wide_rel.size:
+            sys_ids = (wide_rel[:, None] * S + np.arange(S)[None, :]).ravel().astype(np.int64)
+            members = nb + int(nstream[wide_rel].max())
+            nbytes = int(_abi.load().gx_mockstream_wide_scratch_bytes(len(sys_ids), members))
+            scratch = torch.empty(nbytes // 8, dtype=torch.float64, device=dev)
+            sd = torch.from_numpy(sys_ids).to(dev)
+            _abi.call("gx_mockstream_dop853_wide", H.potential.packed().for_device(), H._frame_ref(), S, nb,
+                      ptr(bd), ptr(nbody_w), n_rel, ptr(td), ptr(od), ptr(stream_w0), n_rows, float(orbit_t[-1]),
+                      dt0, dop["atol"], dop["rtol"], dop["nmax"], ptr(sd), len(sys_ids), members, ptr(scratch),
+                      nbytes, ptr(stream_out), ptr(nbody_out), ptr(status),
+                      ptr(stats) if stats is not None else None, stream_handle(stream))
         check(status, "stream")
         return MockStreamBatch(stream_out, nbody_out, release_time, lead_trail, status, stats, H.frame, orbit_t)
 

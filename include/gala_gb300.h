@@ -466,6 +466,30 @@ int gx_mockstream_dop853(const gx_potential* pot, const gx_frame* frame, int64_t
                          double* stream_w_out, double* nbody_w_out, int32_t* status,
                          int64_t* stats, int64_t* queue_counter, void* stream);
 
+/* Release systems wider than a warp (mockstream.pyx:176-303: gala integrates
+ * each release -- the bodies at the release time plus every particle released
+ * then -- as one dop853_step system, however many particles it holds).  One
+ * CTA per listed system, its state in caller-provided device scratch; the error
+ * and stiffness sums are fixed-order CTA sums (gala sums sequentially), so the
+ * results agree with gala to rounding.  Arguments as gx_mockstream_dop853, plus
+ *   systems      DEVICE int64[n_systems]: ids si * n_streams + ss of the
+ *                (release si, stream ss) systems to integrate here
+ *   max_members  nbody + the largest release among them
+ *   scratch      DEVICE buffer of gx_mockstream_wide_scratch_bytes(n_systems,
+ *                max_members) bytes
+ * Writes the same outputs (particles, the bodies after the last release,
+ * status, stats) for those systems only.  dt0 must be non-zero. */
+int64_t gx_mockstream_wide_scratch_bytes(int64_t n_systems, int32_t max_members);
+int gx_mockstream_dop853_wide(const gx_potential* pot, const gx_frame* frame, int64_t n_streams,
+                              int32_t nbody, const gx_body* bodies, const double* nbody_w,
+                              int64_t n_release, const double* release_t,
+                              const int64_t* release_offset, const double* stream_w0,
+                              int64_t n_particles, double t_final, double dt0, double atol,
+                              double rtol, int64_t nmax, const int64_t* systems,
+                              int64_t n_systems, int32_t max_members, double* scratch,
+                              int64_t scratch_bytes, double* stream_w_out, double* nbody_w_out,
+                              int32_t* status, int64_t* stats, void* stream);
+
 /* DirectNBody.integrate_orbit with LeapfrogIntegrator: leapfrog_integrate_nbody
  * (src/gala/integrate/cyintegrators/leapfrog.pyx:161-255) for n_systems
  * independent systems of nparticles <= 8 bodies, the first `nbody` massive.  Within

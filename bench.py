@@ -107,7 +107,7 @@ def parse_args():
     p.add_argument("--batch-precision", default="both", choices=["both", "fp32c", "fp64"])
     p.add_argument("--no-autotune", action="store_true", help="use the cached or default launch shape")
     p.add_argument("--surrogate-steps", type=int, default=30000, help="training steps of the SCF surrogate")
-    p.add_argument("--surrogate-split", type=int, default=2, choices=[1, 2, 3],
+    p.add_argument("--surrogate-split", type=int, default=3, choices=[1, 2, 3],
                    help="tensor-core operands: 1 BF16, 2 BF16 hi+lo activations, 3 FP16")
     p.add_argument("--surrogate-orbits", type=int, default=262_144)
     p.add_argument("--surrogate-nsteps", type=int, default=5000)

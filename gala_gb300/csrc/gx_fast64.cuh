@@ -197,10 +197,13 @@ __device__ __forceinline__ void potential_gradient_ft(const PV &pot, const doubl
     }
 }
 
+// A large composite (device component table) takes gala's own expressions: the
+// lean forms' ulp-level differences, summed over hundreds of components, would
+// exceed the 1e-12 orbit parity that DOP853 holds with a few components.
 template <bool SCF>
 __device__ __forceinline__ void potential_gradient_f(const DevPot &pot, const double *q, double *g) {
     if (pot.cdev) {
-        potential_gradient_ft<SCF>(table_view(pot), q, g);
+        potential_gradient_t<SCF>(table_view(pot), q, g);
         return;
     }
     potential_gradient_ft<SCF>(pot, q, g);

@@ -112,7 +112,7 @@ class SurrogatePotential:
     """Surrogate of an SCFPotential (or any potential whose monopole is the
     Hernquist sphere (m, r_s)), trained on the GPU."""
 
-    def __init__(self, scf, r_min=0.5, r_max=200.0, seed=0, split=2):
+    def __init__(self, scf, r_min=0.5, r_max=200.0, seed=0, split=3):
         import torch
 
         from ._device import require_cuda

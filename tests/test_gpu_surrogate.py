@@ -83,12 +83,14 @@ def test_adam_matches_numpy():
     np.testing.assert_allclose(tp.cpu().numpy(), p2, rtol=1e-5, atol=1e-7)
 
 
-@pytest.mark.parametrize("engine", ["tcgen05", "mma"])
-def test_bf16_inference_matches_fp64_network(scf, engine):
+@pytest.mark.parametrize("engine,split", [("tcgen05", 3), ("tcgen05", 2), ("mma", 2)])
+def test_tensor_core_inference_matches_fp64_network(scf, engine, split):
     """The tensor-core kernels (tcgen05 with TMEM accumulators, and warp-level
     mma.sync) evaluate the same function as the FP64 oracle of the network (to
-    BF16 precision)."""
-    sp = S.SurrogatePotential(scf, seed=6)
+    the precision of their operands: FP16, or BF16 weights with BF16 hi + lo
+    activations).  FP16 operands carry 11-bit weights against BF16's 8, so the
+    FP16 mode is held to a 2x tighter bound."""
+    sp = S.SurrogatePotential(scf, seed=6, split=split)
     sp.export()
     x = sp.sample_positions(3000, seed=7)
     grad, phi = sp.gradient_and_energy(x, engine=engine)
@@ -104,8 +106,9 @@ def test_bf16_inference_matches_fp64_network(scf, engine):
     grad_ref = (dphi0 + dphiH * y) * n + phiH * J
     phi_ref = phi0 + phiH * y
     err = np.linalg.norm(grad.cpu().numpy() - grad_ref, axis=0) / np.linalg.norm(grad_ref, axis=0)
-    # weights are BF16 in the kernel, FP64 in the oracle; activations are hi + lo pairs
-    assert np.median(err) < 1e-2, np.median(err)
+    # weights are FP16 / BF16 in the kernel, FP64 in the oracle
+    bound = 5e-3 if split == 3 else 1e-2
+    assert np.median(err) < bound, np.median(err)
     # (an untrained network can make Phi cross zero, so compare on the global scale)
     np.testing.assert_allclose(phi.cpu().numpy(), phi_ref, rtol=0, atol=1e-3 * np.abs(phi_ref).max())
 
@@ -210,7 +213,7 @@ def test_tcgen05_matches_mma_engine(scf):
     (the tcgen05 kernel uses tanh.approx, relative error ~2^-11), both below
     the BF16 weight rounding.  Sizes that are not a multiple of the 128-row
     tile exercise the partial last tile."""
-    sp = S.SurrogatePotential(scf, seed=8)
+    sp = S.SurrogatePotential(scf, seed=8, split=2)
     sp.export()
     for n in (1, 127, 129, 5000):
         x = sp.sample_positions(n, seed=9)
@@ -223,7 +226,7 @@ def test_tcgen05_matches_mma_engine(scf):
 
 
 def test_tcgen05_leapfrog_matches_mma_leapfrog(scf):
-    sp = S.SurrogatePotential(scf, seed=10)
+    sp = S.SurrogatePotential(scf, seed=10, split=2)
     sp.export()
     w0 = W.scf_ics(700, seed=11)
     o_tc, fb_tc = sp.integrate_leapfrog(w0, 1.0, 50, engine="tcgen05")

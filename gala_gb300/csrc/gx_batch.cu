@@ -63,14 +63,21 @@ __device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const Bat
         // output velocity at the last step: v_{n+1/2} + g h / 2
         for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], g[k] * h * 0.5f);
     } else {
+        // the coefficients times the step, once (shorter dependent chains per sub-step)
+        float ch[4], dh[4];
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            ch[s] = A.c[s] * h;
+            dh[s] = -A.d[s] * h;
+        }
         for (int64_t j = 0; j < nsteps; j++) {
             // sub-step 0 has d = 0: drift only
-            for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], A.c[0] * fmaf(vh[k], h, vl[k] * h));
+            for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], ch[0], vl[k] * ch[0]));
 #pragma unroll
             for (int s = 1; s < 4; s++) {
                 potential_gradient_f<S>(pot, xh, g);
-                for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -A.d[s] * g[k] * h);
-                for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], A.c[s] * fmaf(vh[k], h, vl[k] * h));
+                for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], dh[s] * g[k]);
+                for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], ch[s], vl[k] * ch[s]));
             }
         }
     }

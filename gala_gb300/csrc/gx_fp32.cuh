@@ -60,9 +60,13 @@ __device__ __forceinline__ float lg2_approx(float x) {
 // every term positive (no cancellation); s < 1/3, so six terms of P leave a
 // truncation below 2^-24 of the bracket.  For u >= 1 the direct form has no
 // harmful cancellation.
+// The two reciprocals both depend on u alone and run side by side:
+// 1 / (s (1 + s)) = (2 + u)^2 / (2 u (1 + u)), (1 - s)^3 / 4 = 2 r^3, r = 1 / (2 + u).
 __device__ __forceinline__ float nfw_f_over_u3(float u) {
     if (u < 1.0f) {
-        const float r = rcp_approx(2.0f + u);
+        const float tu = 2.0f + u;
+        const float r = rcp_approx(tu);
+        const float q = rcp_approx(fmaf(u, u, u));
         const float s = u * r;
         const float t = s * s;
         float P = 1.0f / 13.0f;
@@ -71,9 +75,8 @@ __device__ __forceinline__ float nfw_f_over_u3(float u) {
         P = fmaf(P, t, 1.0f / 7.0f);
         P = fmaf(P, t, 1.0f / 5.0f);
         P = fmaf(P, t, 1.0f / 3.0f);
-        const float br = rcp_approx(fmaf(s, s, s)) + P;
-        const float om = 2.0f * r;
-        return om * om * om * 0.25f * br;
+        const float br = fmaf(0.5f * tu * tu, q, P);
+        return 2.0f * r * r * r * br;
     }
     const float opu = 1.0f + u;
     const float iopu = rcp_approx(opu);

@@ -372,8 +372,23 @@ def test_stream_edge_cases():
                                                random_state=np.random.RandomState(1)), g.Hamiltonian(pot))
     stream_l, _ = gen_l.run(g.PhaseSpacePosition.from_w(w0), 1e5, dt=1.0, n_steps=10)
     assert stream_l.xyz.shape == (3, 11) and set(stream_l.lead_trail) == {"l"}
-    with pytest.raises(NotImplementedError):
-        gen.run(g.PhaseSpacePosition.from_w(w0), 1e5, dt=1.0, n_steps=10, n_particles=20)
+
+
+def test_releases_wider_than_a_warp_match_oracle(oracle):
+    """20 particles per tail at every time: 41-member DOP853 systems, one CTA
+    each (gx_mockstream_dop853_wide), against the oracle's run."""
+    pot = W.mw_composite()
+    w0 = W.mw_ics(1, seed=62)[:, 0]
+    prog_pot = g.PlummerPotential(m=2e5, b=0.01)
+    gen = MockStreamGenerator(FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(7)),
+                              g.Hamiltonian(pot), progenitor_potential=prog_pot)
+    stream, nbody = gen.run(g.PhaseSpacePosition.from_w(w0), 2e5, dt=1.0, n_steps=40, n_particles=20)
+    t = g.parse_time_specification(dt=1.0, n_steps=40)
+    ref_st, ref_nb = _oracle_run(oracle, pot, prog_pot, w0, 2e5, t, 7, 1, 20)
+    got = np.vstack([stream.xyz, stream.v_xyz]).T
+    assert got.shape == ref_st.shape == (41 * 40, 6)
+    assert _scale_err(got, ref_st) < 1e-9
+    assert _scale_err(np.vstack([nbody.xyz, nbody.v_xyz]).T, ref_nb) < 1e-10
 
 
 def test_stiffness_exit_matches_oracle(oracle):
@@ -609,7 +624,8 @@ def test_large_leapfrog_release_and_dop853_burst(oracle):
                           b=0.004)], n_particles=counts, dt=1.0, n_steps=100, Integrator="leapfrog")
     rel_t = np.nonzero(np.asarray(counts) > 0)[0]
     assert tuple(res.status.shape) == (1, len(rel_t) + (0 not in rel_t))
-    assert np.all(res.status.cpu().numpy() == 1)
+    st = res.status.cpu().numpy()[0]
+    assert np.all(st[-len(rel_t):] == 1) and np.all(st[:len(st) - len(rel_t)] == 0)  # 0: nothing released
     # DOP853: the 2001-member release is one system (the CTA-per-system kernel);
     # gala's own asserted values (test_mockstream_class.py:84-97) and the oracle's
     # system, held to the same distribution bounds

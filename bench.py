@@ -67,8 +67,11 @@ F_DOP_OUTPUT = 6 * 14 + 2         # one contd8 evaluation of 6 components
 F_HERNQUIST = 17
 
 # DRAM bytes per launch measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum),
-# per orbit of the launch; the summaries are in profiles/.
-TRAFFIC_PER_ORBIT = {}
+# per orbit of the launch, scaled to the benched launch by its orbit count (the inputs are
+# read once; the outputs are still in the 129 MB L2 when a launch ends):
+#   batch_fp32c  18,895,872 B for 262,144 orbits (full size)  profiles/batch_fp32_kernel_uneven.md
+#   dop853       1,700,864 B for 30,000 orbits                profiles/dop853_fp64_mw_composite.md
+TRAFFIC_PER_ORBIT = {"batch_fp32c": 18_895_872 / 262_144, "dop853": 1_700_864 / 30_000}
 
 
 def sig(x, n=4):
@@ -825,6 +828,29 @@ def run_mock_streams(args, torch, stream):
     e1.synchronize()
     ms_rel = e0.elapsed_time(e1)
     same = bool(torch.equal(out, res.stream_w))
+
+    # the FP32-stage / FP64-control form of the same release systems (rtol 1e-8)
+    out32 = torch.empty_like(sw0)
+    st32 = torch.zeros((S, len(t)), dtype=torch.int32, device="cuda")
+    stats32 = torch.zeros((S, len(t), 4), dtype=torch.int64, device="cuda")
+
+    def release_kernel_fp32():
+        _abi.call("gx_mockstream_dop853_fp32", desc, S, 1, ptr(bd), ptr(orbit), len(t), ptr(td), ptr(off), 2,
+                  ptr(sw0), n_rows, t_final, 1.0, DOP32_ATOL, DOP32_RTOL, 0, ptr(out32), ptr(nb_out), ptr(st32),
+                  ptr(stats32), ptr(counter), int(stream.cuda_stream))
+
+    release_kernel_fp32()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    release_kernel_fp32()
+    e1.record(stream)
+    e1.synchronize()
+    ms_rel32 = e0.elapsed_time(e1)
+    o64, o32_ = out.cpu().numpy(), out32.cpu().numpy()
+    okm = np.repeat((st_k.cpu().numpy() == 1) & (st32.cpu().numpy() == 1), 2, axis=1)[:, :n_rows]
+    perr32 = (np.linalg.norm(o32_[..., :3] - o64[..., :3], axis=-1) / np.linalg.norm(o64[..., :3], axis=-1))[okm]
+    stt32 = stats32.cpu().numpy()
+    flops32 = float(np.sum(stt32[..., 0]) * (F_RHS_MW * 3 + F_PLUMMER_PULL * 2) + np.sum(stt32[..., 1]) * 3 * F_DOP_STEP)
     nsys_p = 2
     flops = float(np.sum(stats[..., 0]) * (F_RHS_MW * (1 + nsys_p) + F_PLUMMER_PULL * nsys_p) +
                   np.sum(stats[..., 1]) * (1 + nsys_p) * F_DOP_STEP +
@@ -874,6 +900,11 @@ def run_mock_streams(args, torch, stream):
         "e2e": {"value": particle_steps / (e2e_ms * 1e-3), "ms": e2e_ms,
                 "h2d_bytes": int(w0.nbytes + m.nbytes + S * n_rows * 4 * 8),
                 "d2h_bytes": int(host_stream.nbytes + host_nbody.nbytes)},
+        "release_kernel_fp32": {"value": particle_steps / (ms_rel32 * 1e-3), "ms": ms_rel32, "atol": DOP32_ATOL,
+                                "rtol": DOP32_RTOL, "speedup_vs_fp64": ms_rel / ms_rel32,
+                                "position_error_vs_fp64_median": float(np.median(perr32)),
+                                "position_error_vs_fp64_p99": float(np.percentile(perr32, 99)),
+                                "frac_fp32": flops32 / (ms_rel32 * 1e-3) / 1e12 / fma_peak(torch, stream, False)},
         "stiff_exit_fraction": float(np.mean(status[status != 0] == -4)),
         "leapfrog_fp64": {"value": particle_steps / (lf_ms["gx_mockstream_leapfrog"] * 1e-3),
                           "frac": lf_flops / (lf_ms["gx_mockstream_leapfrog"] * 1e-3) / 1e12 / fp64_peak},
@@ -1006,6 +1037,8 @@ def compact(name, r):
         return {"unit": "particle-steps/s", "pipeline": sig(r["pipeline"]["value"]),
                 "release_kernel": sig(r["release_kernel"]["value"]),
                 "frac_fp64": sig(r["release_kernel"]["roofline"]["frac"], 3), "e2e": sig(r["e2e"]["value"]),
+                "release_fp32": sig(r["release_kernel_fp32"]["value"]),
+                "release_fp32_pos_err_median": sig(r["release_kernel_fp32"]["position_error_vs_fp64_median"], 2),
                 "leapfrog_fp32c": sig(r["leapfrog_fp32c"]["value"]), "cpu_16c": sig(cb.get("value")),
                 "status_agreement": sig(cb.get("status_agreement"), 5)}
     if name == "orbit_reductions":

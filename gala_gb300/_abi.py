@@ -108,6 +108,8 @@ SIGNATURES = {
                                   _P, _P, _P, _P, _P]),
     "gx_mockstream_dop853": (C.c_int, [_PP, _PF, _I64, _I32, _P, _P, _I64, _P, _P, _I32, _P, _I64, _D, _D, _D, _D,
                                        _I64, _P, _P, _P, _P, _P, _P]),
+    "gx_mockstream_dop853_fp32": (C.c_int, [_PP, _I64, _I32, _P, _P, _I64, _P, _P, _I32, _P, _I64, _D, _D, _D, _D,
+                                            _I64, _P, _P, _P, _P, _P, _P]),
     "gx_mockstream_wide_scratch_bytes": (C.c_int64, [_I64, _I32]),
     "gx_mockstream_dop853_wide": (C.c_int, [_PP, _PF, _I64, _I32, _P, _P, _I64, _P, _P, _P, _I64, _D, _D, _D, _D,
                                             _I64, _P, _I64, _I32, _P, _I64, _P, _P, _P, _P, _P]),

@@ -33,6 +33,7 @@ UNITS = {
     "gx_peaks.cu": [],
     "gx_batch.cu": [],
     "gx_dop853_fp32.cu": [],
+    "gx_nbody_fp32.cu": [],
     "gx_stream32.cu": [],
     "gx_mlp_train.cu": [],
     "gx_mlp_infer.cu": [],

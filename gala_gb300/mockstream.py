@@ -16,7 +16,10 @@ The generator follows gala's MockStreamGenerator.run
    on the full grid gives their state at each release time, and every release
    system takes round((t_final - t_release) / dt) Leapfrog steps
    (gx_mockstream_leapfrog, or its FP32-compensated form with
-   ``precision="fp32c"``).
+   ``precision="fp32c"``).  With DOP853, ``precision="fp32c"`` runs the release
+   systems with FP32 stages and forces and FP64 step control
+   (gx_mockstream_dop853_fp32; tolerances of ~1e-8 relative and looser); the
+   bodies' own integration stays FP64.
 
 ``run`` makes one stream with gala's signature and return values.
 ``run_batch`` makes many independent streams (one progenitor each, all on one
@@ -420,8 +423,8 @@ class MockStreamGenerator:
                 raise RuntimeError(f"Integration failed with code {int(bad[0])}")
 
         leapfrog = integrator == "leapfrog"
-        if precision not in ("fp64", "fp32c") or (precision == "fp32c" and not leapfrog):
-            raise ValueError("precision must be 'fp64', or 'fp32c' with the Leapfrog integrator")
+        if precision not in ("fp64", "fp32c"):
+            raise ValueError("precision must be 'fp64' or 'fp32c'")
 
         # 1. the bodies over the requested grid (DirectNBody.integrate_orbit)
         if leapfrog:
@@ -477,6 +480,19 @@ class MockStreamGenerator:
         td = torch.from_numpy(time).to(dev)
         od = torch.from_numpy(rel_off).to(dev)
         dt0 = float(time[1] - time[0])
+        if precision == "fp32c":
+            # FP32 stages and forces with FP64 step control (gx_mockstream_dop853_fp32)
+            if wide_rel.size:
+                raise NotImplementedError("the FP32 DOP853 release systems fill at most 32 lanes; release fewer "
+                                          "particles per time or use precision='fp64'")
+            if not isinstance(H.frame, StaticFrame):
+                raise NotImplementedError("the FP32 DOP853 release systems run in a static frame")
+            _abi.call("gx_mockstream_dop853_fp32", H.potential.packed().for_device(), S, nb, ptr(bd), ptr(nbody_w),
+                      n_rel, ptr(td), ptr(od), max_group, ptr(stream_w0), n_rows, float(orbit_t[-1]), dt0,
+                      dop["atol"], dop["rtol"], dop["nmax"], ptr(stream_out), ptr(nbody_out), ptr(status),
+                      ptr(stats) if stats is not None else None, ptr(counter), stream_handle(stream))
+            check(status, "stream")
+            return MockStreamBatch(stream_out, nbody_out, release_time, lead_trail, status, stats, H.frame, orbit_t)
         _abi.call("gx_mockstream_dop853", H.potential.packed().for_device(), H._frame_ref(), S, nb, ptr(bd),
                   ptr(nbody_w), n_rel, ptr(td), ptr(od), max_group, ptr(stream_w0), n_rows, float(orbit_t[-1]),
                   dt0, dop["atol"], dop["rtol"], dop["nmax"], ptr(stream_out), ptr(nbody_out),

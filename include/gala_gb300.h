@@ -466,6 +466,23 @@ int gx_mockstream_dop853(const gx_potential* pot, const gx_frame* frame, int64_t
                          double* stream_w_out, double* nbody_w_out, int32_t* status,
                          int64_t* stats, int64_t* queue_counter, void* stream);
 
+/* The release systems of gx_mockstream_dop853 by DOP853 with FP32 stages and
+ * forces and FP64 step control (the arithmetic of gx_dop853_fp32: double-float
+ * state, FP64 time / error-norm combination / accept-reject; the particle-body
+ * separations from the double-float parts).  Same arguments as
+ * gx_mockstream_dop853 without the frame (static frames only); nbody <= 4.
+ * Not bit-compatible with gala; tolerances below ~1e-8 relative only shrink the
+ * steps.  No gala counterpart beyond mockstream_dop853 itself
+ * (src/gala/dynamics/mockstream/mockstream.pyx:176-303). */
+int gx_mockstream_dop853_fp32(const gx_potential* pot, int64_t n_streams, int32_t nbody,
+                              const gx_body* bodies, const double* nbody_w, int64_t n_release,
+                              const double* release_t, const int64_t* release_offset,
+                              int32_t max_per_release, const double* stream_w0,
+                              int64_t n_particles, double t_final, double dt0, double atol,
+                              double rtol, int64_t nmax, double* stream_w_out,
+                              double* nbody_w_out, int32_t* status, int64_t* stats,
+                              int64_t* queue_counter, void* stream);
+
 /* Release systems wider than a warp (mockstream.pyx:176-303: gala integrates
  * each release -- the bodies at the release time plus every particle released
  * then -- as one dop853_step system, however many particles it holds).  One

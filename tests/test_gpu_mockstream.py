@@ -664,3 +664,29 @@ def test_df_sample_like_gala(which, kw, pot):
     o1 = DF(random_state=np.random.RandomState(42), **kw).sample(orbit, 1e4)
     o2 = DF(random_state=np.random.RandomState(42), **kw).sample(orbit, 1e4)
     assert np.array_equal(o1.xyz, o2.xyz) and np.array_equal(o1.v_xyz, o2.v_xyz) and len(o1.x) == 2 * n
+
+
+def test_fp32_dop853_release_systems_match_fp64():
+    """Mock streams with precision="fp32c" and DOP853: the release systems run
+    with FP32 stages and forces and FP64 step control (atol 1e-10, rtol 1e-8)
+    and land on the FP64 form's particles (rtol 1e-10): median final-position
+    difference within 1e-5 of the position, 99 % within 1e-3."""
+    pot = W.mw_composite()
+    S = 16
+    w0, m, b = W.stream_progenitors(S)
+    pots = W.stream_progenitor_potentials(m, b)
+
+    def run(precision, rtol):
+        gen = MockStreamGenerator(FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(3)), pot)
+        return gen.run_batch(w0, m, progenitor_potentials=pots, dt=1.0, n_steps=300,
+                             Integrator_kwargs=dict(precision=precision, atol=1e-10, rtol=rtol, err_if_fail=0))
+
+    r64 = run("fp64", 1e-10)
+    r32 = run("fp32c", 1e-8)
+    s64, s32 = r64.stream_w.cpu().numpy(), r32.stream_w.cpu().numpy()
+    st64, st32 = r64.status.cpu().numpy(), r32.status.cpu().numpy()
+    ok = np.repeat((st64 == 1) & (st32 == 1), 2, axis=1)[:, :s64.shape[1]]
+    err = (np.linalg.norm(s32[..., :3] - s64[..., :3], axis=-1) / np.linalg.norm(s64[..., :3], axis=-1))[ok]
+    assert np.mean(st32[st64 == 1] == 1) > 0.98
+    assert np.median(err) < 1e-5 and np.quantile(err, 0.99) < 1e-3, np.quantile(err, [0.5, 0.99, 1.0])
+    np.testing.assert_allclose(r32.nbody_w.cpu().numpy(), r64.nbody_w.cpu().numpy(), rtol=1e-12)

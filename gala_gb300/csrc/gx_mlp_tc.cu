@@ -180,32 +180,6 @@ __device__ __forceinline__ void silu2(float z, float &a, float &s1) {
     s1 = sg * fmaf(z, 1.0f - sg, 1.0f);
 }
 
-// SiLU and its derivative on FP16 pairs (the FP16-operand mode, whose next A
-// operand is FP16 anyway): z -> a = z sigma(z), s = sigma(z) (1 + z (1 - sigma(z)))
-// with sigma(z) = 0.5 + 0.5 tanh(z / 2), one tanh.approx.f16x2 per pair.
-__device__ __forceinline__ __half2 tanh_h2(__half2 x) {
-    uint32_t r;
-    asm("tanh.approx.f16x2 %0, %1;" : "=r"(r) : "r"(*reinterpret_cast<const uint32_t *>(&x)));
-    return *reinterpret_cast<const __half2 *>(&r);
-}
-__device__ __forceinline__ void silu_h2(__half2 z, __half2 &a, __half2 &s1) {
-    const __half2 half = __float2half2_rn(0.5f), one = __float2half2_rn(1.0f);
-    const __half2 sg = __hfma2(tanh_h2(__hmul2(z, half)), half, half);
-    a = __hmul2(z, sg);
-    s1 = __hmul2(sg, __hfma2(z, __hsub2(one, sg), one));
-}
-
-// Write 32 consecutive FP16 values, given as 16 packed pairs, to row `row` of
-// the A operand (columns j0..j0+31, j0 a multiple of 32; 128-byte swizzle).
-__device__ __forceinline__ void put_a_h2(uint8_t *sA, int row, int j0, const uint32_t (&w)[16]) {
-    const int c = j0 >> 6, g0 = (j0 & 63) >> 3;
-#pragma unroll
-    for (int u = 0; u < 4; u++) {
-        const int off = c * A_CHUNK + row * 128 + (((g0 + u) ^ (row & 7)) << 4);
-        *reinterpret_cast<uint4 *>(sA + off) = make_uint4(w[4 * u], w[4 * u + 1], w[4 * u + 2], w[4 * u + 3]);
-    }
-}
-
 // Write 32 consecutive values (columns j0..j0+31, j0 a multiple of 32) of row
 // `row` of the A operand: BF16 hi part and the BF16 rounding remainder (lo), or
 // FP16 values (SPLIT 3).
@@ -345,22 +319,6 @@ __device__ bool tile_eval(const float *__restrict__ P, Issuer &I, Shared &S, uin
             float v[32];
             tm_ld32(tmem + lane_base + j0, v);
             uint32_t sp[16];
-            if (SPLIT == 3 && l < 4) {
-                // hidden layers of the FP16 mode: bias in FP32, SiLU on FP16 pairs,
-                // the activations straight into the FP16 A operand
-                uint32_t aw[16];
-#pragma unroll
-                for (int k = 0; k < 32; k += 2) {
-                    const float2 bb = *reinterpret_cast<const float2 *>(b + j0 + k);
-                    __half2 a, s1;
-                    silu_h2(__floats2half2_rn(v[k] + bb.x, v[k + 1] + bb.y), a, s1);
-                    aw[k >> 1] = *reinterpret_cast<const uint32_t *>(&a);
-                    sp[k >> 1] = *reinterpret_cast<const uint32_t *>(&s1);
-                }
-                tm_st16(tmem + lane_base + (l == 2 ? COL_SP2 : COL_SP3) + (j0 >> 1), sp);
-                put_a_h2(sA, row, j0, aw);
-                continue;
-            }
 #pragma unroll
             for (int k = 0; k < 32; k += 2) {
                 float a0, s0, a1, s1;
@@ -398,18 +356,6 @@ __device__ bool tile_eval(const float *__restrict__ P, Issuer &I, Shared &S, uin
             if (l > 1) {
                 uint32_t sp[16];
                 tm_ld16(tmem + lane_base + (l == 2 ? COL_SP2 : COL_SP3) + (j0 >> 1), sp);
-                if constexpr (SPLIT == 3) {
-                    // delta = u * silu'(z) on FP16 pairs, straight into the FP16 operand
-                    uint32_t dw[16];
-#pragma unroll
-                    for (int k = 0; k < 32; k += 2) {
-                        const __half2 d = __hmul2(__floats2half2_rn(v[k], v[k + 1]),
-                                                  *reinterpret_cast<const __half2 *>(&sp[k >> 1]));
-                        dw[k >> 1] = *reinterpret_cast<const uint32_t *>(&d);
-                    }
-                    put_a_h2(sA, row, j0, dw);
-                    continue;
-                }
 #pragma unroll
                 for (int k = 0; k < 32; k += 2) {
                     const float2 sv = __half22float2(*reinterpret_cast<const __half2 *>(&sp[k >> 1]));

@@ -69,12 +69,12 @@ __device__ __forceinline__ float nfw_f_over_u3(float u) {
         const float q = rcp_approx(fmaf(u, u, u));
         const float s = u * r;
         const float t = s * s;
-        float P = 1.0f / 13.0f;
-        P = fmaf(P, t, 1.0f / 11.0f);
-        P = fmaf(P, t, 1.0f / 9.0f);
-        P = fmaf(P, t, 1.0f / 7.0f);
-        P = fmaf(P, t, 1.0f / 5.0f);
-        P = fmaf(P, t, 1.0f / 3.0f);
+        // P(t) in the form a + t^2 (b + t^2 c) (three dependent steps instead of five)
+        const float t2 = t * t;
+        const float pa = fmaf(1.0f / 5.0f, t, 1.0f / 3.0f);
+        const float pb = fmaf(1.0f / 9.0f, t, 1.0f / 7.0f);
+        const float pc = fmaf(1.0f / 13.0f, t, 1.0f / 11.0f);
+        const float P = fmaf(fmaf(pc, t2, pb), t2, pa);
         const float br = fmaf(0.5f * tu * tu, q, P);
         return 2.0f * r * r * r * br;
     }

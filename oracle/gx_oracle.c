@@ -1182,6 +1182,63 @@ int orc_mockstream_dop853(const gx_potential *pot, const gx_frame *fr, int nbodi
     return 0;
 }
 
+/* mockstream_dop853_animate (mockstream.pyx:306-440) for one progenitor system:
+ *   nbody_w0  (nbodies, 6)  the bodies at t[0]
+ *   t         (ntimes)      the whole orbit grid; h0 = t[1] - t[0]
+ *   stream_w0 (ntot, 6)     released particles in release order
+ *   nstream   (ntimes)      particles released at t[i] (zeros allowed)
+ * The state holds every body and particle from the start; interval i
+ * (t[i-1] -> t[i]) steps the first nbodies + n of them as one dop853_step
+ * system (nstiff 1), n being the particles released at t[0..i-1], and
+ * n += nstream[i] follows the interval (:402-411).  Snapshots (:393-421):
+ *   snap   (noutput, nbodies + ntot, 6)  the state at t[0] and after every
+ *          interval i with i % output_every == 0 or i == ntimes - 1; members
+ *          not yet released are NaN (the HDF5 datasets' fill value)
+ *   snap_t (noutput)
+ * w_final (nbodies + ntot, 6) is the last state, status (ntimes) the idid of
+ * every interval (status[0] = 1), stats (4) the summed counters or NULL.
+ * Returns the number of snapshots, or -1 on bad arguments. */
+static void anim_snapshot(double *dst, const double *w, int64_t live, int64_t all) {
+    for (int64_t k = 0; k < 6 * all; k++) dst[k] = (k < 6 * live) ? w[k] : NAN;
+}
+
+int orc_mockstream_dop853_animate(const gx_potential *pot, const gx_frame *fr, int nbodies, const gx_body *bodies,
+                                  const double *nbody_w0, const double *t, int64_t ntimes, const double *stream_w0,
+                                  const int32_t *nstream, int64_t output_every, double atol, double rtol,
+                                  int64_t nmax, double *snap, double *snap_t, double *w_final, int32_t *status,
+                                  long *stats) {
+    if (ntimes < 2 || nbodies < 1 || output_every < 1) return -1;
+    int64_t ntot = 0;
+    for (int64_t i = 0; i < ntimes; i++) {
+        if (nstream[i] < 0) return -1;
+        ntot += nstream[i];
+    }
+    const int64_t all = nbodies + ntot;
+    double *w = w_final;
+    memcpy(w, nbody_w0, sizeof(double) * 6 * (size_t)nbodies);
+    memcpy(w + 6 * nbodies, stream_w0, sizeof(double) * 6 * (size_t)ntot);
+    const double dt0 = t[1] - t[0];
+    int64_t n = nstream[0], j = 0;
+    anim_snapshot(snap, w, nbodies + n, all);
+    snap_t[j++] = t[0];
+    status[0] = 1;
+    if (stats)
+        for (int k = 0; k < 4; k++) stats[k] = 0;
+    for (int64_t i = 1; i < ntimes; i++) {
+        long st[4] = {0, 0, 0, 0};
+        status[i] = orc_dop853_step_system(pot, fr, (int)(nbodies + n), nbodies, bodies, w, t[i - 1], t[i], dt0,
+                                           atol, rtol, nmax, st);
+        if (stats)
+            for (int k = 0; k < 4; k++) stats[k] += st[k];
+        n += nstream[i];
+        if (i % output_every == 0 || i == ntimes - 1) {
+            anim_snapshot(snap + (size_t)j * 6 * (size_t)all, w, nbodies + n, all);
+            snap_t[j++] = t[i];
+        }
+    }
+    return (int)j;
+}
+
 /* Release systems of many independent streams that share one release grid,
  * the layout of the GPU library's mock-stream entry point:
  *   bodies    (n_streams, nbodies)

@@ -240,6 +240,36 @@ class Oracle:
             raise RuntimeError(f"mockstream oracle failed ({res})")
         return nb_out, st_out, status
 
+    def mockstream_animate(self, pot, bodies, nbody_w0, t, stream_w0, nstream, output_every=1, atol=1e-10,
+                           rtol=1e-10, nmax=0, frame=None):
+        """mockstream_dop853_animate for one progenitor system on the whole grid t.
+        Returns (snap (noutput, nbodies + ntot, 6) NaN-filled, snap_t (noutput,),
+        w_final (nbodies + ntot, 6), status (ntimes,), stats (4,) or None for gala's code)."""
+        b = self._bodies(bodies)
+        nbody_w0 = _f64(nbody_w0)
+        t = _f64(t)
+        stream_w0 = _f64(stream_w0).reshape(-1, 6)
+        nstream = np.ascontiguousarray(np.asarray(nstream, dtype=np.int32))
+        nb, ntimes = nbody_w0.shape[0], len(t)
+        nout = (ntimes - 1) // output_every + 1 + int((ntimes - 1) % output_every != 0)
+        allm = nb + int(nstream.sum())
+        snap = np.zeros((nout, allm, 6))
+        snap_t = np.zeros(nout)
+        w_final = np.zeros((allm, 6))
+        status = np.zeros(ntimes, dtype=np.int32)
+        args = [pot.packed().for_host(), self._frame(frame), C.c_int(nb), _p(b), _p(nbody_w0), _p(t),
+                C.c_int64(ntimes), _p(stream_w0), _p(nstream), C.c_int64(output_every), C.c_double(atol),
+                C.c_double(rtol), C.c_int64(nmax), _p(snap), _p(snap_t), _p(w_final), _p(status)]
+        stats = None
+        if self.is_ref:
+            res = self.lib.ref_mockstream_dop853_animate(*args)
+        else:
+            stats = np.zeros(4, dtype=np.int64)
+            res = self.lib.orc_mockstream_dop853_animate(*args, _p(stats))
+        if res != nout:
+            raise RuntimeError(f"mockstream animate oracle failed ({res})")
+        return snap, snap_t, w_final, status, stats
+
     def mockstream_systems(self, pot, bodies, nbody_w, release_t, nstream, stream_w0, t_final, dt0, atol=1e-10,
                            rtol=1e-10, nmax=0, sys_lo=0, sys_hi=None, nthreads=1, frame=None):
         """The release systems of many streams (the GPU entry point's layout):

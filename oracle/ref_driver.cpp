@@ -539,6 +539,63 @@ int ref_mockstream_dop853(const gx_potential *pot, const gx_frame *fr, int nbodi
     return res;
 }
 
+/* mockstream_dop853_animate (mockstream.pyx:306-440) for one progenitor system:
+ * gala's dop853() on the growing system, interval by interval, with
+ * dop853_step's argument list; the same arguments and outputs as the oracle's
+ * orc_mockstream_dop853_animate (stats are not kept). */
+int ref_mockstream_dop853_animate(const gx_potential *pot, const gx_frame *fr, int nbodies, const gx_body *bodies,
+                                  const double *nbody_w0, const double *t, int64_t ntimes, const double *stream_w0,
+                                  const int32_t *nstream, int64_t output_every, double atol, double rtol,
+                                  int64_t nmax, double *snap, double *snap_t, double *w_final, int32_t *status) {
+    if (ntimes < 2 || nbodies < 1 || output_every < 1) return -1;
+    RefPot rp;
+    if (!build(pot, fr, &rp)) { release(&rp); return -100; }
+    int64_t ntot = 0;
+    for (int64_t i = 0; i < ntimes; i++) ntot += nstream[i];
+    const int64_t all = nbodies + ntot;
+    RefBody *rb = (RefBody *)calloc((size_t)nbodies, sizeof(RefBody));
+    CPotential **pots = (CPotential **)malloc(sizeof(CPotential *) * (size_t)nbodies);
+    int ok = 1;
+    for (int i = 0; i < nbodies; i++) {
+        if (!build_body(&bodies[i], &rb[i])) ok = 0;
+        pots[i] = rb[i].cp;
+    }
+    int res = -100;
+    if (ok) {
+        double *w = w_final;
+        memcpy(w, nbody_w0, sizeof(double) * 6 * (size_t)nbodies);
+        memcpy(w + 6 * nbodies, stream_w0, sizeof(double) * 6 * (size_t)ntot);
+        const double dt0 = t[1] - t[0];
+        int64_t n = nstream[0], j = 0;
+        auto snapshot = [&](int64_t live) {
+            double *dst = snap + (size_t)j * 6 * (size_t)all;
+            for (int64_t k = 0; k < 6 * all; k++) dst[k] = (k < 6 * live) ? w[k] : NAN;
+        };
+        snapshot(nbodies + n);
+        snap_t[j++] = t[0];
+        status[0] = 1;
+        for (int64_t i = 1; i < ntimes; i++) {
+            double rt = rtol, at = atol;
+            const unsigned nsys = (unsigned)(nbodies + n);
+            status[i] = dop853(6 * nsys, (FcnEqDiff)Fwrapper_direct_nbody, rp.cp, &rp.cf, nsys, (unsigned)nbodies,
+                               (void *)pots, t[i - 1], w, t[i], &rt, &at, 0, NULL, 0, NULL, 0.0, 0.0, 0.0, 0.0,
+                               0.0, 0.0, dt0, (long)nmax, 0, 1, 0, NULL, 0, NULL, NULL, 0, NULL);
+            n += nstream[i];
+            if (i % output_every == 0 || i == ntimes - 1) {
+                snapshot(nbodies + n);
+                snap_t[j++] = t[i];
+            }
+        }
+        res = (int)j;
+    }
+    for (int i = 0; i < nbodies; i++)
+        if (rb[i].cp) free_cpotential(rb[i].cp);
+    free(rb);
+    free(pots);
+    release(&rp);
+    return res;
+}
+
 /* c_d2_dr2 (cpotential.cpp:346-371) at N points q (N, 3). */
 int ref_d2_dr2_n(const gx_potential *pot, double t, const double *q, int64_t N, double *out) {
     RefPot rp;

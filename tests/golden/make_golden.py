@@ -160,6 +160,21 @@ def make_stream_fixtures(ref: Oracle):
                         nbody_leapfrog=ref.leapfrog_nbody(c["pot"], *_lf_nbody_args()))
 
 
+def make_animate_fixture(ref: Oracle):
+    """gala's mockstream_dop853_animate (gala's dop853() on the growing system,
+    interval by interval) on a shared test case: 41 steps, a release every 2nd
+    step, a snapshot every 3rd."""
+    from tests._cases import stream_case
+    from tests.test_mockstream_oracle import _animate_args
+
+    n_steps, release_every, output_every = 41, 2, 3
+    c = stream_case(n_streams=1, n_steps=n_steps, release_every=release_every)
+    snap, snap_t, w, status, _ = ref.mockstream_animate(c["pot"], **_animate_args(c, 0, output_every))
+    np.savez_compressed(OUT / "mockstream_animate.npz", snap=snap, snap_t=snap_t, w=w, status=status,
+                        stream_w0=c["stream_w0"][0], n_steps=n_steps, release_every=release_every,
+                        output_every=output_every)
+
+
 def make_io_fixture():
     """gala's own serialisation test inputs, kept as text: the potential YAML
     files of tests/potential/potential/ (read by test_io.py) and one HDF5 file
@@ -178,8 +193,8 @@ def make_io_fixture():
 
 
 if __name__ == "__main__":
-    # python tests/golden/make_golden.py [potentials integrators scf streams io]
-    which = set(sys.argv[1:]) or {"potentials", "integrators", "scf", "streams", "io"}
+    # python tests/golden/make_golden.py [potentials integrators scf streams animate io]
+    which = set(sys.argv[1:]) or {"potentials", "integrators", "scf", "streams", "animate", "io"}
     if "io" in which and GALA_TESTS.exists():
         make_io_fixture()
     which.discard("io")
@@ -195,5 +210,7 @@ if __name__ == "__main__":
         make_scf_fixture()
     if "streams" in which:
         make_stream_fixtures(ref)
+    if "animate" in which:
+        make_animate_fixture(ref)
     for p in sorted(OUT.glob("*.npz")):
         print(p.name, p.stat().st_size)

@@ -689,4 +689,6 @@ def test_fp32_dop853_release_systems_match_fp64():
     err = (np.linalg.norm(s32[..., :3] - s64[..., :3], axis=-1) / np.linalg.norm(s64[..., :3], axis=-1))[ok]
     assert np.mean(st32[st64 == 1] == 1) > 0.98
     assert np.median(err) < 1e-5 and np.quantile(err, 0.99) < 1e-3, np.quantile(err, [0.5, 0.99, 1.0])
-    np.testing.assert_allclose(r32.nbody_w.cpu().numpy(), r64.nbody_w.cpu().numpy(), rtol=1e-12)
+    # the returned bodies are those of the last release system (mockstream.pyx:291-293),
+    # which the FP32 form integrates with FP32 stages too
+    np.testing.assert_allclose(r32.nbody_w.cpu().numpy(), r64.nbody_w.cpu().numpy(), rtol=1e-5)

@@ -418,3 +418,71 @@ def test_dfs_refuse_no_tails():
                    (LagrangeCloudStreamDF, {"v_disp": 1.0}), (ChenStreamDF, {})):
         with pytest.raises(ValueError):
             DF(lead=False, trail=False, **kw)
+
+
+# ------------------------------------------------------------ animate mode
+def _animate_args(c, s, output_every):
+    """mockstream_dop853_animate's inputs: the whole orbit grid, the bodies at
+    t[0] and the particles released at every grid time (zeros included)."""
+    return dict(bodies=c["bodies"][s], nbody_w0=c["w0"][:, s].reshape(1, 6), t=c["t"], stream_w0=c["stream_w0"][s],
+                nstream=2 * c["counts"], output_every=output_every)
+
+
+def _n_output(nsteps, output_every):
+    """gala's snapshot count (test_mockstream.py:304-306)."""
+    return 1 + nsteps // output_every + int(nsteps % output_every != 0)
+
+
+@pytest.mark.parametrize("n_steps,output_every,release_every", [(61, 3, 2), (40, 1, 1), (17, 2, 4)])
+def test_mockstream_animate_oracle_matches_gala(oracle, gala_ref_strict, n_steps, output_every, release_every):
+    c = stream_case(n_streams=1, n_steps=n_steps, release_every=release_every)
+    a = _animate_args(c, 0, output_every)
+    snap_o, t_o, w_o, st_o, stats = oracle.mockstream_animate(c["pot"], **a)
+    snap_r, t_r, w_r, st_r, _ = gala_ref_strict.mockstream_animate(c["pot"], **a)
+    assert snap_o.shape[0] == _n_output(n_steps, output_every)
+    np.testing.assert_array_equal(st_o, st_r)
+    assert np.all(st_o == 1) and stats[1] >= n_steps
+    np.testing.assert_array_equal(t_o, t_r)
+    np.testing.assert_array_equal(snap_o, snap_r)  # NaNs in the same places
+    np.testing.assert_array_equal(w_o, w_r)
+
+
+def test_mockstream_animate_snapshots(oracle):
+    """Snapshot j holds the bodies and exactly the particles released at or
+    before its time; the first is the initial state, the last the final one."""
+    c = stream_case(n_streams=1, n_steps=30, release_every=4, n_per_tail=2)
+    a = _animate_args(c, 0, 4)
+    snap, snap_t, w_final, status, _ = oracle.mockstream_animate(c["pot"], **a)
+    t, ns = c["t"], a["nstream"]
+    assert snap_t.tolist() == [t[i] for i in (0, 4, 8, 12, 16, 20, 24, 28, 30)]
+    released = np.cumsum(ns)
+    for j, tj in enumerate(snap_t):
+        i = int(np.nonzero(t == tj)[0][0])
+        live = 1 + released[i]
+        assert np.all(np.isfinite(snap[j, :live])) and np.all(np.isnan(snap[j, live:]))
+    np.testing.assert_array_equal(snap[0, 1:1 + ns[0]], c["stream_w0"][0][:ns[0]])
+    np.testing.assert_array_equal(snap[-1], w_final)
+
+
+def test_mockstream_animate_agrees_with_release_systems(oracle):
+    """One growing system and one system per release integrate the same
+    test-particle orbits in the same progenitor field; at rtol 1e-10 the final
+    streams agree to the integration tolerance, not bit for bit."""
+    c = stream_case(n_streams=1, n_steps=60)
+    _, _, w_a, _, _ = oracle.mockstream_animate(c["pot"], **_animate_args(c, 0, 10))
+    nb, st, _ = oracle.mockstream_dop853(c["pot"], **_stream_args(c, 0))
+    scale = np.abs(st).max(axis=0)
+    np.testing.assert_allclose(w_a[1:], st, rtol=0, atol=1e-7 * scale.max())
+    np.testing.assert_allclose(w_a[0], nb[0], rtol=1e-7)
+
+
+def test_mockstream_animate_golden(oracle, golden):
+    d = golden("mockstream_animate.npz")
+    c = stream_case(n_streams=1, n_steps=int(d["n_steps"]), release_every=int(d["release_every"]))
+    np.testing.assert_array_equal(c["stream_w0"][0], d["stream_w0"])
+    snap, snap_t, w, status, _ = oracle.mockstream_animate(c["pot"], **_animate_args(c, 0, int(d["output_every"])))
+    np.testing.assert_array_equal(status, d["status"])
+    np.testing.assert_array_equal(snap_t, d["snap_t"])
+    np.testing.assert_array_equal(np.isnan(snap), np.isnan(d["snap"]))
+    scale = np.nanmax(np.abs(d["snap"]))
+    np.testing.assert_allclose(snap, d["snap"], rtol=0, atol=OFAST_RTOL * scale)

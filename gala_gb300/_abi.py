@@ -80,6 +80,9 @@ SIGNATURES = {
     "gx_component_table_bytes": (C.c_int64, [C.c_int32]),
     "gx_pack_component_table": (C.c_int, [_PP, _P, _I64]),
     "gx_last_error_message": (C.c_char_p, []),
+    "gx_cancel_flag_create": (C.c_int, [_P, _P]),
+    "gx_set_cancel_flag": (None, [_P]),
+    "gx_cancel_flag_destroy": (C.c_int, [_P]),
     "gx_potential_value": (C.c_int, [_PP, _D, _P, _I64, _P, _P]),
     "gx_potential_gradient": (C.c_int, [_PP, _D, _P, _I64, _P, _P]),
     "gx_potential_density": (C.c_int, [_PP, _D, _P, _I64, _P, _P]),
@@ -113,6 +116,9 @@ SIGNATURES = {
     "gx_mockstream_wide_scratch_bytes": (C.c_int64, [_I64, _I32]),
     "gx_mockstream_dop853_wide": (C.c_int, [_PP, _PF, _I64, _I32, _P, _P, _I64, _P, _P, _P, _I64, _D, _D, _D, _D,
                                             _I64, _P, _I64, _I32, _P, _I64, _P, _P, _P, _P, _P]),
+    "gx_mockstream_animate_snapshots": (C.c_int64, [_I64, _I64]),
+    "gx_mockstream_dop853_animate": (C.c_int, [_PP, _PF, _I64, _I32, _P, _P, _I64, _P, _D, _P, _P, _I64, _I64, _D,
+                                               _D, _I64, _P, _I64, _P, _P, _P, _P, _P]),
     "gx_nbody_leapfrog": (C.c_int, [_PP, _I64, _I32, _I32, _P, _P, _P, _I64, _I32, _P, _P]),
     "gx_mockstream_leapfrog": (C.c_int, [_PP, _I64, _I32, _P, _P, _I64, _P, _P, _I32, _P, _I64, _D, _D, _P, _P, _P,
                                          _P]),

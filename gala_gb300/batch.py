@@ -193,6 +193,22 @@ class BatchIntegrator:
         """|E(t_end) - E(0)| / |E(0)| per orbit (FP64 diagnostic)."""
         return ((self.E1 - self.E0) / self.E0).abs()
 
+    def completed(self):
+        """(N,) bool CUDA tensor: the orbits the last run integrated.  All of
+        them unless the run was cancelled (``gala_gb300.cancel``): a cancelled
+        launch takes no further queue chunk, so the orbits of the first
+        min(counter, chunks) chunks of the order are done and the others' rows
+        of the output are untouched."""
+        import torch
+
+        chunk = self.config["chunk"]
+        n_chunks = self.order.numel() // chunk
+        taken = min(int(self.counter.item()), n_chunks)
+        done = torch.zeros(self.n, dtype=torch.bool, device=self.dev)
+        ids = self.order[:taken * chunk].long()
+        done[ids[ids >= 0]] = True
+        return done
+
     # ------------------------------------------------------------- autotune
     def _cache_key(self):
         import torch

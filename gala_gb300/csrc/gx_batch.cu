@@ -31,6 +31,7 @@ struct BatchArgs {
     int32_t chunk;    // orbits per queue item (multiple of 32)
     int32_t pad;
     float c[4], d[4];  // Ruth4 coefficients
+    const int32_t *cancel;  // host cancel flag (mapped memory) or nullptr
 };
 
 __device__ __forceinline__ void split(double x, float &hi, float &lo) {
@@ -98,8 +99,9 @@ __global__ void __launch_bounds__(256) batch_fp32_kernel(const __grid_constant__
     const int lane = threadIdx.x & 31;
     const int64_t nchunks = A.slots / A.chunk;
     for (;;) {
-        int c = 0;
-        if (lane == 0) c = atomicAdd(counter, 1);
+        // a cancelled launch takes no further chunk (lane 0 decides for the warp)
+        int c = INT_MAX;
+        if (lane == 0 && !cancel_requested(A.cancel)) c = atomicAdd(counter, 1);
         c = __shfl_sync(0xffffffffu, c, 0);
         if (c >= nchunks) break;
         for (int r = 0; r < A.chunk; r += 32) {
@@ -213,6 +215,7 @@ extern "C" int gx_batch_integrate_fp32(const gx_potential *pot, const double *w0
     A.slots = n_slots;
     A.chunk = chunk;
     A.pad = 0;
+    A.cancel = gx::cancel_flag();
     const double two_13 = std::pow(2., 1. / 3.);
     const double c[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
                          (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};
@@ -526,6 +529,7 @@ extern "C" int gx_batch_integrate_fp32_noalloc(const gx_potential *pot, const do
     A.slots = slots;
     A.chunk = gx::NA_CHUNK;
     A.pad = 0;
+    A.cancel = gx::cancel_flag();
     const double two_13 = std::pow(2., 1. / 3.);
     const double c[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
                          (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};

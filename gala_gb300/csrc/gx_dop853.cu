@@ -32,6 +32,7 @@ struct DopArgs {
     int64_t nmax, nstiff;
     int64_t ntimes, out_stride, n_out;
     int32_t save_all, nbatch;
+    const int32_t *cancel;  // host cancel flag (mapped memory) or nullptr
 };
 
 constexpr int DOP_MAX_WARPS = 32;
@@ -91,6 +92,8 @@ dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFra
               int64_t *__restrict__ stats) {
     using namespace dop;
     __shared__ double red[4 * DOP_MAX_WARPS];
+    // a CTA that starts after cancellation integrates nothing (one reader, CTA-uniform)
+    if (__syncthreads_or(threadIdx.x == 0 && cancel_requested(A.cancel))) return;
 
     // BPC batches per CTA, batch bl on threads [bl * nbatch, (bl + 1) * nbatch)
     const int nbs = A.nbatch;
@@ -429,6 +432,8 @@ extern "C" int gx_dop853_integrate_hamiltonian(const gx_potential *pot, const gx
     if (n == 0) return GX_OK;
     GX_CHECK_ARG(w0 && t && w_out && status, "NULL array");
     gx::DopArgs A;
+    memset(&A, 0, sizeof(A));
+    A.cancel = gx::cancel_flag();
     A.atol = atol;
     A.rtol = rtol;
     A.dt_max = dt_max;

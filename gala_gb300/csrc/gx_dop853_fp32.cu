@@ -36,6 +36,7 @@ struct Dop32Args {
     int32_t save_all, pad;
     float O[3];   // rotating-frame angular velocity (ROT kernels)
     float pad2;
+    const int32_t *cancel;  // host cancel flag (mapped memory) or nullptr
 };
 
 // s + e = a + b exactly (Knuth's two-sum).
@@ -119,6 +120,7 @@ dop853_fp32_kernel(const __grid_constant__ DevPotF pot, const Dop32Args A, const
 
     for (;;) {
         if (need) {
+            if (cancel_requested(A.cancel)) break;  // no further orbit once cancelled
             const int64_t k = atomicAdd(counter, 1);
             if (k >= n) break;
             i = order ? (int64_t)order[k] : k;
@@ -453,6 +455,7 @@ extern "C" int gx_dop853_fp32(const gx_potential *pot, const gx_frame *frame, co
     A.save_all = save_all ? 1 : 0;
     const bool rotating = df.type != GX_FRAME_STATIC;
     for (int k = 0; k < 3; k++) A.O[k] = (float)df.O[k];
+    A.cancel = gx::cancel_flag();
     cudaStream_t st = gx::as_stream(stream);
     GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, sizeof(int32_t), st));
     return gx::launch_dop853_fp32(dp, rotating, A, w0, t, order, w_out, status, stats, queue_counter, st);

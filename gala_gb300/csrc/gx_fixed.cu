@@ -116,12 +116,14 @@ __global__ void __launch_bounds__(128, 1) batch_fp64_kernel(const __grid_constan
                                                             const int32_t *__restrict__ method,
                                                             const int32_t *__restrict__ order,
                                                             int32_t *__restrict__ counter,
-                                                            double *__restrict__ out) {
+                                                            double *__restrict__ out,
+                                                            const int32_t *__restrict__ cancel) {
     const int lane = threadIdx.x & 31;
     const int64_t nchunks = slots / chunk;
     for (;;) {
-        int c = 0;
-        if (lane == 0) c = atomicAdd(counter, 1);
+        // a cancelled launch takes no further chunk (lane 0 decides for the warp)
+        int c = INT_MAX;
+        if (lane == 0 && !cancel_requested(cancel)) c = atomicAdd(counter, 1);
         c = __shfl_sync(0xffffffffu, c, 0);
         if (c >= nchunks) break;
         for (int r = 0; r < chunk; r += 32) {
@@ -225,10 +227,10 @@ int gx_batch_integrate_fp64(const gx_potential *pot, const double *w0, int64_t n
     GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, sizeof(int32_t), st));
     if (dp.has_scf)
         gx::batch_fp64_kernel<true><<<grid, block, 0, st>>>(dp, co, n, n_slots, chunk, w0, n_steps, dt, method,
-                                                            order, queue_counter, w_out);
+                                                            order, queue_counter, w_out, gx::cancel_flag());
     else
         gx::batch_fp64_kernel<false><<<grid, block, 0, st>>>(dp, co, n, n_slots, chunk, w0, n_steps, dt, method,
-                                                             order, queue_counter, w_out);
+                                                             order, queue_counter, w_out, gx::cancel_flag());
     return gx::check_launch("batch_fp64");
 }
 

@@ -224,6 +224,9 @@ static int launch_ham(const gx_potential *pot, const gx_frame *fr, const double 
     return check_launch("gx_hamiltonian eval");
 }
 
+static thread_local const int32_t *g_cancel = nullptr;
+const int32_t *cancel_flag() { return g_cancel; }
+
 }  // namespace gx
 
 extern "C" {
@@ -261,6 +264,31 @@ int gx_pack_component_table(const gx_potential *pot, void *host_out, int64_t byt
 }
 
 const char *gx_last_error_message(void) { return gx::g_errmsg; }
+
+void gx_set_cancel_flag(const int32_t *flag) { gx::g_cancel = flag; }
+
+int gx_cancel_flag_create(int32_t **host_ptr, int32_t **device_ptr) {
+    GX_CHECK_ARG(host_ptr && device_ptr, "NULL pointer");
+    void *h = nullptr;
+    GX_CUDA_TRY(cudaHostAlloc(&h, 64, cudaHostAllocMapped | cudaHostAllocPortable));
+    *reinterpret_cast<volatile int32_t *>(h) = 0;
+    void *d = nullptr;
+    const cudaError_t e = cudaHostGetDevicePointer(&d, h, 0);
+    if (e != cudaSuccess) {
+        cudaFreeHost(h);
+        gx::set_error("cudaHostGetDevicePointer failed: %s", cudaGetErrorString(e));
+        return GX_ERR_CUDA;
+    }
+    *host_ptr = static_cast<int32_t *>(h);
+    *device_ptr = static_cast<int32_t *>(d);
+    return GX_OK;
+}
+
+int gx_cancel_flag_destroy(int32_t *host_ptr) {
+    GX_CHECK_ARG(host_ptr, "NULL pointer");
+    GX_CUDA_TRY(cudaFreeHost(host_ptr));
+    return GX_OK;
+}
 
 int gx_potential_value(const gx_potential *pot, double t, const double *q, int64_t n, double *out, void *stream) {
     (void)t;

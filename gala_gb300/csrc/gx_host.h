@@ -3,6 +3,7 @@
 // thread-local error message behind gx_last_error_message().
 #pragma once
 
+#include <climits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -39,6 +40,19 @@ int pack_potential(const gx_potential *pot, DevPot *out);
 int pack_frame(const gx_frame *fr, DevFrame *out);
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// The cancel flag that gx_set_cancel_flag installed on the calling host thread
+// (a device-readable int32; nullptr = none).  The persistent kernels launched
+// from that thread receive it and stop taking new work once it reads non-zero.
+const int32_t *cancel_flag();
+
+// Device side: the host has asked the launch to stop.  The flag lives in
+// mapped host memory and is written while the kernel runs, so every reader
+// loads it through a volatile pointer; callers that need one answer for a
+// whole warp or CTA read it on one thread and broadcast it.
+__device__ __forceinline__ bool cancel_requested(const int32_t *flag) {
+    return flag != nullptr && *reinterpret_cast<const volatile int32_t *>(flag) != 0;
+}
 
 // Launch-error check after a <<<>>> launch.
 inline int check_launch(const char *what) {

@@ -70,6 +70,7 @@ struct NbArgs {
     int32_t *status;
     int64_t *stats;
     unsigned long long *counter;
+    const int32_t *cancel;  // host cancel flag (mapped memory) or nullptr
 };
 
 __device__ __forceinline__ double nb_sign(double a, double b) { return (b < 0.0) ? -fabs(a) : fabs(a); }
@@ -164,8 +165,9 @@ nbody_dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
         // -- a group without a system takes the next one (group-local) --------
         if (!have && !done) {
             for (;;) {
-                unsigned long long id = 0ull;
-                if (member == 0) id = atomicAdd(A.counter, 1ull);
+                // a cancelled launch takes no further system (member 0 decides for the group)
+                unsigned long long id = ~0ull;
+                if (member == 0 && !cancel_requested(A.cancel)) id = atomicAdd(A.counter, 1ull);
                 id = __shfl_sync(gmask, id, base);
                 if (id >= (unsigned long long)A.n_sys) {
                     done = true;
@@ -790,6 +792,7 @@ extern "C" int gx_nbody_dop853(const gx_potential *pot, const gx_frame *frame, i
     A.status = status;
     A.stats = stats;
     A.counter = reinterpret_cast<unsigned long long *>(queue_counter);
+    A.cancel = gx::cancel_flag();
     cudaStream_t st = gx::as_stream(stream);
     return save_all ? gx::launch_nbody<false, true>(dp, df, A, st) : gx::launch_nbody<false, false>(dp, df, A, st);
 }
@@ -839,6 +842,7 @@ extern "C" int gx_mockstream_dop853(const gx_potential *pot, const gx_frame *fra
     A.status = status;
     A.stats = stats;
     A.counter = reinterpret_cast<unsigned long long *>(queue_counter);
+    A.cancel = gx::cancel_flag();
     return gx::launch_nbody<true, false>(dp, df, A, gx::as_stream(stream));
 }
 

@@ -47,6 +47,7 @@ struct Ms32Args {
     int32_t *status;
     int64_t *stats;
     unsigned long long *counter;
+    const int32_t *cancel;  // host cancel flag (mapped memory) or nullptr
 };
 
 // The FP32 constants of one body's potential (pack_potential_f32's packing);
@@ -192,8 +193,9 @@ __global__ void __launch_bounds__(128) ms_dop853_fp32_kernel(const __grid_consta
         // -- a group without a system takes the next one ------------------------
         if (!have && !done) {
             for (;;) {
-                unsigned long long id = 0ull;
-                if (member == 0) id = atomicAdd(A.counter, 1ull);
+                // a cancelled launch takes no further system (member 0 decides for the group)
+                unsigned long long id = ~0ull;
+                if (member == 0 && !cancel_requested(A.cancel)) id = atomicAdd(A.counter, 1ull);
                 id = __shfl_sync(gmask, id, base);
                 if (id >= (unsigned long long)A.n_sys) {
                     done = true;
@@ -477,6 +479,7 @@ extern "C" int gx_mockstream_dop853_fp32(const gx_potential *pot, int64_t n_stre
     A.status = status;
     A.stats = stats;
     A.counter = reinterpret_cast<unsigned long long *>(queue_counter);
+    A.cancel = gx::cancel_flag();
     cudaStream_t st = gx::as_stream(stream);
     const bool mw = dp.ncomp == 4 && dp.c[0].type == GX_POT_HERNQUIST && dp.c[1].type == GX_POT_HERNQUIST &&
                     dp.c[2].type == GX_POT_MIYAMOTONAGAI && dp.c[3].type == GX_POT_SPHERICALNFW &&

@@ -50,6 +50,7 @@ struct WideArgs {
     double *stream_w_out, *nbody_w_out;
     int32_t *status;
     int64_t *stats;
+    const int32_t *cancel;    // host cancel flag (mapped memory) or nullptr
 };
 
 // Deterministic CTA sums of two values (each thread passes its partials).
@@ -99,54 +100,30 @@ __device__ __forceinline__ void wide_rhs(const DevPot &pot, const DevFrame &fr, 
     for (int c = 0; c < 6; c++) kout[c * M + m] = k.v[c];
 }
 
+// One dop853() call of dop853_step (dop853.pyx:27-75 -> dopcor, dopri/dop853.cpp:
+// 89-650) on the system of the first nmem members, from x to xend with the
+// initial step h and nstiff 1, run by the whole CTA.  The state is Ar[A_Y]
+// (SoA rows of stride M); the other arrays are the stage derivatives and the
+// stage argument.  Adds {nfcn, nstep, naccpt, nrejct} to ctr and returns gala's
+// idid; every thread returns the same value, after a barrier.
 template <bool SCF>
-__global__ void __launch_bounds__(WD_THREADS)
-nbody_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFrame fr,
-                  const __grid_constant__ WideArgs A) {
+__device__ __forceinline__ int wide_dop853(const DevPot &pot, const DevFrame &fr, const gx_body *__restrict__ bod,
+                                           int nbody, int nmem, int64_t M, double *const *Ar, double *red, double x,
+                                           const double xend, double h, const double atoli, const double rtoli,
+                                           const int64_t nmax_in, int64_t *ctr) {
     using namespace dop;
-    __shared__ double red[64];
-    const int64_t b = blockIdx.x;
-    if (b >= A.n_systems) return;
-    const int64_t sys = A.systems[b];
-    const int64_t si = sys / A.n_streams, ss = sys - si * A.n_streams;
-    if (si < 0 || si >= A.n_release) return;  // an id outside the release grid: nothing to address
-    const int64_t o0 = A.offset[si], o1 = A.offset[si + 1];
-    const int64_t M = A.max_members;
-    const int nbody = A.nbody;
-    if (o1 < o0 || o0 < 0 || o1 > A.n_particles || nbody + (o1 - o0) > M) {
-        if (threadIdx.x == 0) A.status[ss * A.n_release + si] = -1;  // inconsistent offsets: no access
-        return;
-    }
-    const int nmem = nbody + (int)(o1 - o0);
-    const gx_body *bod = A.bodies + ss * nbody;
-    double *base = A.scratch + b * (int64_t)WD_ARRAYS * 6 * M;
-    double *Ar[WD_ARRAYS];
-#pragma unroll
-    for (int a = 0; a < WD_ARRAYS; a++) Ar[a] = base + (int64_t)a * 6 * M;
     const int tid = threadIdx.x, nt = blockDim.x;
-
-    // the system at the release time: bodies, then the released particles
-    for (int m = tid; m < nmem; m += nt) {
-        const double *src = (m < nbody) ? A.nbody_w + ((ss * A.n_release + si) * nbody + m) * 6
-                                        : A.stream_w0 + (ss * A.n_particles + o0 + (m - nbody)) * 6;
-#pragma unroll
-        for (int c = 0; c < 6; c++) Ar[A_Y][c * M + m] = src[c];
-    }
     __syncthreads();
     for (int m = tid; m < nmem; m += nt) wide_rhs<SCF>(pot, fr, bod, nbody, Ar[A_Y], M, m, Ar[A_K1]);
     __syncthreads();
 
     // dop853_step's dop853() arguments (dop853.pyx:46-72) and front-end defaults
-    double x = A.release_t[si];
-    const double xend = A.t_final;
-    double h = A.dt0;
     const double uround = 2.3E-16;
-    const int64_t nmax = A.nmax ? A.nmax : 1000000;
+    const int64_t nmax = nmax_in ? nmax_in : 1000000;
     const int64_t nstiff = 1;
     const double hmax = fabs(xend - x);
     const double posneg = (xend - x < 0.0) ? -1.0 : 1.0;
     const double safe = 0.9, facc1 = 1.0 / 0.333, facc2 = 1.0 / 6.0;
-    const double atoli = A.atol, rtoli = A.rtol;
     int last = 0, reject = 0, iasti = 0, nonsti = 0, idid = 0;
     double hlamb = 0.0;
     int64_t nfcn = 2, nstep = 0, naccpt = 0, nrejct = 0;
@@ -278,6 +255,50 @@ nbody_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ De
 #undef WSTAGE
     (void)nonsti;
     __syncthreads();
+    ctr[0] += nfcn;
+    ctr[1] += nstep;
+    ctr[2] += naccpt;
+    ctr[3] += nrejct;
+    return idid;
+}
+
+template <bool SCF>
+__global__ void __launch_bounds__(WD_THREADS)
+nbody_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFrame fr,
+                  const __grid_constant__ WideArgs A) {
+    __shared__ double red[64];
+    const int64_t b = blockIdx.x;
+    if (b >= A.n_systems) return;
+    // a CTA that starts after cancellation integrates nothing (one reader, CTA-uniform)
+    if (__syncthreads_or(threadIdx.x == 0 && cancel_requested(A.cancel))) return;
+    const int64_t sys = A.systems[b];
+    const int64_t si = sys / A.n_streams, ss = sys - si * A.n_streams;
+    if (si < 0 || si >= A.n_release) return;  // an id outside the release grid: nothing to address
+    const int64_t o0 = A.offset[si], o1 = A.offset[si + 1];
+    const int64_t M = A.max_members;
+    const int nbody = A.nbody;
+    if (o1 < o0 || o0 < 0 || o1 > A.n_particles || nbody + (o1 - o0) > M) {
+        if (threadIdx.x == 0) A.status[ss * A.n_release + si] = -1;  // inconsistent offsets: no access
+        return;
+    }
+    const int nmem = nbody + (int)(o1 - o0);
+    const gx_body *bod = A.bodies + ss * nbody;
+    double *base = A.scratch + b * (int64_t)WD_ARRAYS * 6 * M;
+    double *Ar[WD_ARRAYS];
+#pragma unroll
+    for (int a = 0; a < WD_ARRAYS; a++) Ar[a] = base + (int64_t)a * 6 * M;
+    const int tid = threadIdx.x, nt = blockDim.x;
+
+    // the system at the release time: bodies, then the released particles
+    for (int m = tid; m < nmem; m += nt) {
+        const double *src = (m < nbody) ? A.nbody_w + ((ss * A.n_release + si) * nbody + m) * 6
+                                        : A.stream_w0 + (ss * A.n_particles + o0 + (m - nbody)) * 6;
+#pragma unroll
+        for (int c = 0; c < 6; c++) Ar[A_Y][c * M + m] = src[c];
+    }
+    int64_t ctr[4] = {0, 0, 0, 0};
+    const int idid = wide_dop853<SCF>(pot, fr, bod, nbody, nmem, M, Ar, red, A.release_t[si], A.t_final, A.dt0,
+                                      A.atol, A.rtol, A.nmax, ctr);
     for (int m = tid; m < nmem; m += nt) {
         double *dst = nullptr;
         if (m >= nbody) dst = A.stream_w_out + (ss * A.n_particles + o0 + (m - nbody)) * 6;
@@ -288,13 +309,96 @@ nbody_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ De
     if (tid == 0) {
         const int64_t k = ss * A.n_release + si;
         A.status[k] = idid;
-        if (A.stats) {
-            A.stats[4 * k + 0] = nfcn;
-            A.stats[4 * k + 1] = nstep;
-            A.stats[4 * k + 2] = naccpt;
-            A.stats[4 * k + 3] = nrejct;
-        }
+        if (A.stats)
+            for (int q = 0; q < 4; q++) A.stats[4 * k + q] = ctr[q];
     }
+}
+
+// mockstream_dop853_animate (mockstream.pyx:306-440) for many streams: one CTA
+// per stream steps the growing system [bodies, particles released so far]
+// interval by interval over the whole orbit grid and writes snapshots.
+struct AnimArgs {
+    int32_t nbody;
+    int64_t n_streams, ntimes, n_particles, M;  // M = nbody + n_particles members per stream
+    const gx_body *bodies;     // (n_streams, nbody)
+    const double *nbody_w0;    // (n_streams, nbody, 6) at t[0]
+    const double *t;           // (ntimes)
+    const int32_t *nstream;    // (ntimes), summing to n_particles
+    const double *stream_w0;   // (n_streams, n_particles, 6) in release order
+    int64_t output_every, n_output;
+    double dt0, atol, rtol;
+    int64_t nmax;
+    double *scratch;           // n_streams x WD_ARRAYS x 6 x M doubles
+    double *snap;              // (n_streams, 6, n_output, M) or NULL
+    double *w_out;             // (n_streams, M, 6)
+    int32_t *status;           // (n_streams, ntimes): [0] = 1, [i] = idid of interval i
+    int64_t *stats;            // (n_streams, 4) summed over the intervals, or NULL
+    const int32_t *cancel;     // host cancel flag (mapped memory) or nullptr
+};
+
+template <bool SCF>
+__global__ void __launch_bounds__(WD_THREADS)
+animate_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFrame fr,
+                    const __grid_constant__ AnimArgs A) {
+    __shared__ double red[64];
+    const int64_t s = blockIdx.x;
+    if (s >= A.n_streams) return;
+    const int64_t M = A.M;
+    const int nbody = A.nbody;
+    const gx_body *bod = A.bodies + s * nbody;
+    double *base = A.scratch + s * (int64_t)WD_ARRAYS * 6 * M;
+    double *Ar[WD_ARRAYS];
+#pragma unroll
+    for (int a = 0; a < WD_ARRAYS; a++) Ar[a] = base + (int64_t)a * 6 * M;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int m = tid; m < M; m += nt) {
+        const double *src = (m < nbody) ? A.nbody_w0 + (s * nbody + m) * 6
+                                        : A.stream_w0 + (s * A.n_particles + (m - nbody)) * 6;
+#pragma unroll
+        for (int c = 0; c < 6; c++) Ar[A_Y][c * M + m] = src[c];
+    }
+    __syncthreads();
+    // members beyond the released ones are NaN in a snapshot (the HDF5 fill value)
+    const double qnan = __longlong_as_double(0x7ff8000000000000LL);
+    auto snapshot = [&](int64_t j, int64_t live) {
+        if (!A.snap) return;
+        for (int m = tid; m < M; m += nt)
+#pragma unroll
+            for (int c = 0; c < 6; c++)
+                A.snap[((s * 6 + c) * A.n_output + j) * M + m] = (m < live) ? Ar[A_Y][c * M + m] : qnan;
+    };
+    // the particles released so far, kept within [0, n_particles] whatever the
+    // counts say; an interval whose count breaks the bound reports -1
+    auto grow = [&](int64_t n, int64_t i, int &bad) {
+        const int64_t k = A.nstream[i];
+        bad = (k < 0 || n + k > A.n_particles);
+        return bad ? (k < 0 ? n : A.n_particles) : n + k;
+    };
+    int bad = 0;
+    int64_t n = grow(0, 0, bad), j = 0;
+    snapshot(j++, nbody + n);
+    int64_t ctr[4] = {0, 0, 0, 0};
+    if (tid == 0) A.status[s * A.ntimes] = bad ? -1 : 1;
+    for (int64_t i = 1; i < A.ntimes; i++) {
+        // after cancellation the stream stops between intervals (one reader, CTA-uniform);
+        // the intervals not run keep status 0
+        if (__syncthreads_or(tid == 0 && cancel_requested(A.cancel))) {
+            for (int64_t k = i + tid; k < A.ntimes; k += nt) A.status[s * A.ntimes + k] = 0;
+            while (j < A.n_output) snapshot(j++, 0);  // snapshots not reached: all NaN
+            break;
+        }
+        const int idid = wide_dop853<SCF>(pot, fr, bod, nbody, (int)(nbody + n), M, Ar, red, A.t[i - 1], A.t[i],
+                                          A.dt0, A.atol, A.rtol, A.nmax, ctr);
+        n = grow(n, i, bad);
+        if (tid == 0) A.status[s * A.ntimes + i] = bad ? -1 : idid;
+        if (i % A.output_every == 0 || i == A.ntimes - 1) snapshot(j++, nbody + n);
+    }
+    __syncthreads();
+    for (int m = tid; m < M; m += nt)
+#pragma unroll
+        for (int c = 0; c < 6; c++) A.w_out[(s * M + m) * 6 + c] = Ar[A_Y][c * M + m];
+    if (tid == 0 && A.stats)
+        for (int q = 0; q < 4; q++) A.stats[4 * s + q] = ctr[q];
 }
 
 }  // namespace gx
@@ -356,10 +460,76 @@ extern "C" int gx_mockstream_dop853_wide(const gx_potential *pot, const gx_frame
     A.nbody_w_out = nbody_w_out;
     A.status = status;
     A.stats = stats;
+    A.cancel = gx::cancel_flag();
     cudaStream_t st = gx::as_stream(stream);
     if (dp.has_scf)
         gx::nbody_wide_kernel<true><<<(unsigned)n_systems, gx::WD_THREADS, 0, st>>>(dp, df, A);
     else
         gx::nbody_wide_kernel<false><<<(unsigned)n_systems, gx::WD_THREADS, 0, st>>>(dp, df, A);
     return gx::check_launch("mockstream_dop853_wide");
+}
+
+extern "C" int64_t gx_mockstream_animate_snapshots(int64_t ntimes, int64_t output_every) {
+    if (ntimes < 2 || output_every < 1) return 0;
+    return (ntimes - 1) / output_every + 1 + ((ntimes - 1) % output_every != 0);
+}
+
+extern "C" int gx_mockstream_dop853_animate(const gx_potential *pot, const gx_frame *frame, int64_t n_streams,
+                                            int32_t nbody, const gx_body *bodies, const double *nbody_w0,
+                                            int64_t ntimes, const double *t, double dt0,
+                                            const int32_t *nstream, const double *stream_w0,
+                                            int64_t n_particles, int64_t output_every, double atol, double rtol,
+                                            int64_t nmax, double *scratch, int64_t scratch_bytes, double *snap,
+                                            double *w_out, int32_t *status, int64_t *stats, void *stream) {
+    gx::DevPot dp;
+    gx::DevFrame df;
+    int rc = gx::pack_potential(pot, &dp);
+    if (rc) return rc;
+    rc = gx::pack_frame(frame, &df);
+    if (rc) return rc;
+    GX_CHECK_ARG(n_streams >= 1 && n_particles >= 0, "bad size");
+    GX_CHECK_ARG(ntimes >= 2, "the time grid needs at least two points");
+    GX_CHECK_ARG(nbody >= 1, "nbody must be >= 1 (the progenitor)");
+    GX_CHECK_ARG(output_every >= 1, "output_every must be >= 1");
+    GX_CHECK_ARG(nmax >= 0, "nmax must be >= 0 (0 = gala's default 1e6)");
+    GX_CHECK_ARG(atol >= 0 && rtol >= 0, "tolerances must be non-negative");
+    GX_CHECK_ARG(bodies && nbody_w0 && t && nstream && (stream_w0 || n_particles == 0) && scratch && w_out &&
+                     status,
+                 "NULL array");
+    GX_CHECK_ARG(n_streams <= (int64_t)INT32_MAX && nbody + n_particles <= (int64_t)INT32_MAX, "too large");
+    GX_CHECK_ARG(dt0 != 0.0, "dt0 (t[1] - t[0], gala's h0) must be non-zero");
+    const int64_t M = nbody + n_particles;
+    const int64_t need = gx_mockstream_wide_scratch_bytes(n_streams, (int32_t)M);
+    GX_CHECK_ARG(scratch_bytes >= need, "scratch of %lld bytes, %lld needed", (long long)scratch_bytes,
+                 (long long)need);
+    gx::AnimArgs A;
+    memset(&A, 0, sizeof(A));
+    A.nbody = nbody;
+    A.n_streams = n_streams;
+    A.ntimes = ntimes;
+    A.n_particles = n_particles;
+    A.M = M;
+    A.bodies = bodies;
+    A.nbody_w0 = nbody_w0;
+    A.t = t;
+    A.nstream = nstream;
+    A.stream_w0 = stream_w0;
+    A.output_every = output_every;
+    A.n_output = gx_mockstream_animate_snapshots(ntimes, output_every);
+    A.dt0 = dt0;
+    A.atol = atol;
+    A.rtol = rtol;
+    A.nmax = nmax;
+    A.scratch = scratch;
+    A.snap = snap;
+    A.w_out = w_out;
+    A.status = status;
+    A.stats = stats;
+    A.cancel = gx::cancel_flag();
+    cudaStream_t st = gx::as_stream(stream);
+    if (dp.has_scf)
+        gx::animate_wide_kernel<true><<<(unsigned)n_streams, gx::WD_THREADS, 0, st>>>(dp, df, A);
+    else
+        gx::animate_wide_kernel<false><<<(unsigned)n_streams, gx::WD_THREADS, 0, st>>>(dp, df, A);
+    return gx::check_launch("mockstream_dop853_animate");
 }

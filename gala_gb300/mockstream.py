@@ -21,6 +21,12 @@ The generator follows gala's MockStreamGenerator.run
    (gx_mockstream_dop853_fp32; tolerances of ~1e-8 relative and looser); the
    bodies' own integration stays FP64.
 
+With ``output_every`` (DOP853 only, as in gala) the stream is made by
+mockstream_dop853_animate (mockstream.pyx:306-440) instead of step 3: one
+system per stream that holds the bodies and every particle released so far,
+stepped interval by interval over the whole grid (gx_mockstream_dop853_animate),
+with snapshots written to an HDF5 file in gala's layout.
+
 ``run`` makes one stream with gala's signature and return values.
 ``run_batch`` makes many independent streams (one progenitor each, all on one
 time grid) in the same three launches; stream s consumes the DF's random draws
@@ -326,9 +332,15 @@ class MockStreamBatch:
     release_time (n_particles,), lead_trail (n_particles,)
     status       (n_streams, n_release) dop853() code of each release system
     stats        (n_streams, n_release, 4) or None: nfcn, nstep, naccpt, nrejct
+    With output_every (the animate mode) status is (n_streams, ntimes), one code
+    per interval of the grid, stats (n_streams, 4) summed over the intervals, and
+    snapshots     (n_streams, 6, n_output, nbodies + n_particles) the bodies and
+                  particles at snapshot_t, NaN for particles not yet released
+    snapshot_t    (n_output,)
     """
 
-    def __init__(self, stream_w, nbody_w, release_time, lead_trail, status, stats, frame, t):
+    def __init__(self, stream_w, nbody_w, release_time, lead_trail, status, stats, frame, t, snapshots=None,
+                 snapshot_t=None):
         self.stream_w = stream_w
         self.nbody_w = nbody_w
         self.release_time = release_time
@@ -337,6 +349,8 @@ class MockStreamBatch:
         self.stats = stats
         self.frame = frame
         self.t = t
+        self.snapshots = snapshots
+        self.snapshot_t = snapshot_t
 
     @property
     def n_streams(self):
@@ -350,6 +364,27 @@ class MockStreamBatch:
     def nbody(self, s):
         w = self.nbody_w[s].cpu().numpy()
         return PhaseSpacePosition(pos=w[:, :3].T, vel=w[:, 3:].T, frame=self.frame)
+
+    def write_snapshots(self, s, filename):
+        """Stream s's snapshots as mockstream_dop853_animate writes them
+        (mockstream.pyx:107-175, 393-430): groups ``stream`` and ``nbody``, each
+        with ``pos`` (3, n_output, N) and ``vel`` datasets (NaN where a particle
+        is not yet released) and a ``time`` dataset, all with a ``unit``
+        attribute.  ``filename`` may be a name or an open file."""
+        if self.snapshots is None:
+            raise ValueError("this batch holds no snapshots (run with output_every)")
+        nb = int(self.nbody_w.shape[1])
+        snap = self.snapshots[s].cpu().numpy()
+        f, close = _h5_open(filename, "w")
+        try:
+            for name, part in (("stream", snap[:, :, nb:]), ("nbody", snap[:, :, :nb])):
+                g = f.create_group(name)
+                quantity_to_hdf5(g, "pos", part[:3], "kpc")
+                quantity_to_hdf5(g, "vel", part[3:], "kpc / Myr")
+                quantity_to_hdf5(g, "time", np.asarray(self.snapshot_t, dtype=np.float64), "Myr")
+        finally:
+            if close:
+                f.close()
 
 
 class MockStreamGenerator:
@@ -396,7 +431,7 @@ class MockStreamGenerator:
                     nmax=int(kw.get("nmax", 0)), dt_max=float(kw.get("dt_max", 0.0))), err_if_fail
 
     def _generate(self, bodies, body_w0, prog_m, t, counts, dop, err_if_fail, return_stats=False, stream=None,
-                  integrator="dop853", precision="fp64"):
+                  integrator="dop853", precision="fp64", output_every=None):
         """The three stages for n_streams systems.
 
         bodies  : BODY_DTYPE (S, nb), progenitor first, massive bodies before null ones
@@ -446,6 +481,9 @@ class MockStreamGenerator:
         stream_w0, release_time, lead_trail, _ = self.df.sample_device(H.potential, prog_w, orbit_t, prog_m, counts,
                                                                      stream=stream)
         ntail = self.df.lead + self.df.trail
+        if output_every is not None:
+            return self._animate(bodies, nbody0, orbit_t, ntail * counts, stream_w0, release_time, lead_trail, dop,
+                                 output_every, check, return_stats, stream)
 
         # 3. release grid: times that release particles, plus the first (:271-283)
         rel_idx = np.nonzero(counts > 0)[0]
@@ -511,6 +549,42 @@ class MockStreamGenerator:
         check(status, "stream")
         return MockStreamBatch(stream_out, nbody_out, release_time, lead_trail, status, stats, H.frame, orbit_t)
 
+    def _animate(self, bodies, nbody0, orbit_t, nstream, stream_w0, release_time, lead_trail, dop, output_every,
+                 check, return_stats, stream):
+        """mockstream_dop853_animate's stage (mockstream.pyx:306-440) for every
+        stream: nstream (ntimes,) particles released at each grid time."""
+        import torch
+
+        from ._device import ptr, stream_handle
+
+        H = self.hamiltonian
+        S, nb = bodies.shape
+        dev = nbody0.device
+        ntimes = len(orbit_t)
+        nstream = np.ascontiguousarray(nstream, dtype=np.int32)
+        n_rows = int(nstream.sum())
+        M = nb + n_rows
+        lib = _abi.load()
+        n_out = int(lib.gx_mockstream_animate_snapshots(ntimes, output_every))
+        nbytes = int(lib.gx_mockstream_wide_scratch_bytes(S, M))
+        scratch = torch.empty(nbytes // 8, dtype=torch.float64, device=dev)
+        snap = torch.empty((S, 6, n_out, M), dtype=torch.float64, device=dev)
+        w_out = torch.empty((S, M, 6), dtype=torch.float64, device=dev)
+        status = torch.zeros((S, ntimes), dtype=torch.int32, device=dev)
+        stats = torch.zeros((S, 4), dtype=torch.int64, device=dev) if return_stats else None
+        bd = bodies_to_device(bodies, dev)
+        td = torch.from_numpy(np.ascontiguousarray(orbit_t, dtype=np.float64)).to(dev)
+        nd = torch.from_numpy(nstream).to(dev)
+        nbody0 = nbody0.reshape(S, nb, 6).contiguous()
+        _abi.call("gx_mockstream_dop853_animate", H.potential.packed().for_device(), H._frame_ref(), S, nb, ptr(bd),
+                  ptr(nbody0), ntimes, ptr(td), float(orbit_t[1] - orbit_t[0]), ptr(nd), ptr(stream_w0), n_rows,
+                  int(output_every), dop["atol"], dop["rtol"], dop["nmax"], ptr(scratch), nbytes, ptr(snap),
+                  ptr(w_out), ptr(status), ptr(stats) if stats is not None else None, stream_handle(stream))
+        check(status, "stream")
+        idx = [0] + [i for i in range(1, ntimes) if i % output_every == 0 or i == ntimes - 1]
+        return MockStreamBatch(w_out[:, nb:], w_out[:, :nb], release_time, lead_trail, status, stats, H.frame,
+                               orbit_t, snapshots=snap, snapshot_t=np.asarray(orbit_t)[idx])
+
     def _release_leapfrog(self, bodies, orbit, nbody0, orbit_t, forward, time, nstream, rel_off, n_rows, max_per,
                           stream_w0, release_time, lead_trail, precision, stream):
         """mockstream_leapfrog's release stage (mockstream.pyx:524-593)."""
@@ -568,9 +642,14 @@ class MockStreamGenerator:
                              "stream generation.")
         kw_in = dict(Integrator_kwargs or {})
         precision = kw_in.pop("precision", "fp64")
-        if output_every is not None:
-            raise NotImplementedError("snapshot output (output_every / HDF5) is not implemented")
         t = np.ascontiguousarray(parse_time_specification(self.hamiltonian.units, **time_spec), dtype=np.float64)
+        if output_every is not None:
+            if output_filename is None:
+                raise ValueError("If output_every is specified, you must also pass in a filename to store the "
+                                 "snapshots in")
+            output_every = self._check_animate(output_every, Integrator, precision)
+            self._check_output_file(output_filename, overwrite, check_filesize, output_every, t, release_every,
+                                    n_particles)
         prog_nbody = self._get_nbody(prog_w0, nbody)
         idx, n_massive = prog_nbody._order()
         if not np.array_equal(idx, np.arange(len(idx))):
@@ -583,18 +662,55 @@ class MockStreamGenerator:
         dop, err_if_fail = self._dop_kwargs(kw_in if Integrator is DOPRI853Integrator else {})
         res = self._generate(bodies, prog_nbody._c_w0.reshape(1, nb, 6), m[None, :], t, counts, dop, err_if_fail,
                              integrator="leapfrog" if Integrator is LeapfrogIntegrator else "dop853",
-                             precision=precision)
+                             precision=precision, output_every=output_every)
+        if output_every is not None:
+            res.write_snapshots(0, output_filename)
         return res.stream(0), res.nbody(0)
+
+    @staticmethod
+    def _check_animate(output_every, Integrator, precision):
+        """The animate mode's integrator checks (mockstream_generator.py:318-336)."""
+        if Integrator is LeapfrogIntegrator:
+            raise NotImplementedError("Animation output for LeapfrogIntegrator is not implemented")
+        if precision != "fp64":
+            raise NotImplementedError("animation output runs the FP64 DOP853 form")
+        output_every = int(output_every)
+        if output_every < 1:
+            raise ValueError("output_every must be a positive integer")
+        return output_every
+
+    def _check_output_file(self, output_filename, overwrite, check_filesize, output_every, t, release_every,
+                           n_particles):
+        """The snapshot file's checks, before any integration (_init_hdf5_file,
+        mockstream.pyx:116-134)."""
+        import os
+
+        if not isinstance(output_filename, (str, os.PathLike)):
+            return  # an open file or group
+        n_out = (len(t) - 1) // output_every + 1 + int((len(t) - 1) % output_every != 0)
+        total = (self.df.lead + self.df.trail) * int(self.df.release_counts(len(t), release_every,
+                                                                            n_particles).sum())
+        if total * n_out * 8 >= 8e9 and check_filesize:
+            warnings.warn("Estimated mockstream output file is expected to be >8 GB in size! If you're sure, turn "
+                          "this warning off with `check_filesize=False`")
+        if os.path.exists(output_filename) and not overwrite:
+            raise OSError(f"Mockstream output file {output_filename} already exists! Use overwrite=True to "
+                          "overwrite the file.")
 
     @traced("mockstream_run_batch")
     def run_batch(self, prog_w0, prog_mass, progenitor_potentials=None, release_every=1, n_particles=1,
-                  Integrator=None, Integrator_kwargs=None, return_stats=False, stream=None, **time_spec):
+                  Integrator=None, Integrator_kwargs=None, return_stats=False, stream=None, output_every=None,
+                  **time_spec):
         """Many independent streams on one time grid (no extra bodies).
 
         prog_w0  : (6, S) progenitor phase-space positions (numpy)
         prog_mass: (S,) or (S, ntimes) masses passed to the DF
         progenitor_potentials : list of S potentials (or None: the generator's
                    progenitor_potential for every stream)
+        output_every : snapshots every output_every grid steps (the animate
+                   mode, DOP853): kept on the device in the returned batch
+                   (``snapshots``, ``snapshot_t``; ``write_snapshots`` writes
+                   one stream's file)
         Returns a MockStreamBatch of device tensors.
         """
         t = np.ascontiguousarray(parse_time_specification(self.hamiltonian.units, **time_spec), dtype=np.float64)
@@ -621,7 +737,9 @@ class MockStreamGenerator:
         kw_in = dict(Integrator_kwargs or {})
         precision = kw_in.pop("precision", "fp64")
         dop, err_if_fail = self._dop_kwargs(kw_in if Integrator is DOPRI853Integrator else {})
+        if output_every is not None:
+            output_every = self._check_animate(output_every, Integrator, precision)
         body_w0 = np.ascontiguousarray(w0.T.reshape(S, 1, 6))
         return self._generate(bodies, body_w0, m, t, counts, dop, err_if_fail, return_stats=return_stats,
                               stream=stream, integrator="leapfrog" if Integrator is LeapfrogIntegrator else "dop853",
-                              precision=precision)
+                              precision=precision, output_every=output_every)

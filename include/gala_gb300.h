@@ -150,6 +150,41 @@ int gx_abi_version(void);
 /* Message of the last failed call on this host thread ("" if none). */
 const char* gx_last_error_message(void);
 
+/* Cancelling long launches.  gala's mock-stream loop polls for a keyboard
+ * interrupt between releases (PyErr_CheckSignals, mockstream.pyx:277); the
+ * GPU work of one call is a single launch, so its kernels poll a flag in
+ * mapped host memory instead.
+ *   gx_cancel_flag_create   allocates the flag (pinned, mapped, zero) and
+ *                           returns its host address and the device address
+ *                           kernels read it through
+ *   gx_set_cancel_flag      installs a device address (NULL: none) for the
+ *                           launches made afterwards from the calling host
+ *                           thread
+ *   gx_cancel_flag_destroy  frees it; only after every launch that reads it
+ *                           has completed (a CUDA graph captured while it was
+ *                           installed reads it at every replay)
+ * The host requests cancellation by storing a non-zero int32 through the host
+ * address, at any time.  What a launch then skips, per entry point:
+ *   gx_batch_integrate_fp32, gx_batch_integrate_fp64: no further queue chunk
+ *     is taken; chunks already taken complete.  The queue counter then holds
+ *     the number of chunks taken (at most n_slots / chunk); the orbits of the
+ *     first that many chunks of `order` are integrated, the others untouched;
+ *   gx_dop853_fp32, gx_nbody_dop853, gx_mockstream_dop853,
+ *     gx_mockstream_dop853_fp32: no further orbit or system is taken; ones in
+ *     flight complete; the status of the ones not taken is left as the caller
+ *     initialised it;
+ *   gx_dop853_integrate_hamiltonian: batches whose CTA starts after the request are not
+ *     integrated (their status is left as initialised);
+ *   gx_mockstream_dop853_wide: systems whose CTA starts after the request are
+ *     not integrated;
+ *   gx_mockstream_dop853_animate: each stream stops after its current
+ *     interval; the status of the intervals not run is 0, the snapshots not
+ *     reached are all NaN, and the final state is the one reached.
+ * Every other entry point ignores the flag. */
+int gx_cancel_flag_create(int32_t** host_ptr, int32_t** device_ptr);
+void gx_set_cancel_flag(const int32_t* device_ptr);
+int gx_cancel_flag_destroy(int32_t* host_ptr);
+
 /* ------------------------------------------------------------------------- */
 /* Potential evaluation over N points.                                       */
 /* q is (3, N) SoA; out is (N,) for value/density and (3, N) for gradient.   */
@@ -506,6 +541,43 @@ int gx_mockstream_dop853_wide(const gx_potential* pot, const gx_frame* frame, in
                               int64_t n_systems, int32_t max_members, double* scratch,
                               int64_t scratch_bytes, double* stream_w_out, double* nbody_w_out,
                               int32_t* status, int64_t* stats, void* stream);
+
+/* MockStreamGenerator.run with output_every: mockstream_dop853_animate
+ * (src/gala/dynamics/mockstream/mockstream.pyx:306-440) for n_streams
+ * independent streams, one CTA each.  A stream's state holds its bodies and
+ * every particle from the start; interval i (t[i-1] -> t[i]) integrates the
+ * bodies plus the particles released at t[0..i-1] as one dop853_step system
+ * (h0 = dt0, nstiff 1, whole-system error norm), and the particles released at
+ * t[i] join after it.
+ *   bodies     DEVICE gx_body[n_streams][nbody] (massive first)
+ *   nbody_w0   DEVICE double[n_streams][nbody][6], the bodies at t[0]
+ *   t          DEVICE double[ntimes], the whole orbit grid; dt0 = t[1] - t[0]
+ *   nstream    DEVICE int32[ntimes], particles released at t[i] (zeros allowed;
+ *              they sum to n_particles -- an interval whose count would break
+ *              that bound reports -1 and the count is clamped)
+ *   stream_w0  DEVICE double[n_streams][n_particles][6] in release order
+ *   scratch    DEVICE buffer of gx_mockstream_wide_scratch_bytes(n_streams,
+ *              nbody + n_particles) bytes
+ *   snap       DEVICE double[n_streams][6][n_output][nbody + n_particles] or NULL:
+ *              the state at t[0] and after every interval i with
+ *              i % output_every == 0 or i == ntimes - 1 (n_output =
+ *              gx_mockstream_animate_snapshots(ntimes, output_every)); members
+ *              not yet released are NaN, the fill value of gala's HDF5 datasets
+ *   w_out      DEVICE double[n_streams][nbody + n_particles][6], the final state
+ *   status     DEVICE int32[n_streams][ntimes]: 1 at [0], gala's idid of every
+ *              interval after it
+ *   stats      DEVICE int64[n_streams][4] or NULL: {nfcn, nstep, naccpt, nrejct}
+ *              summed over the intervals
+ * Every interval's error and stiffness sums are fixed-order CTA sums (gala sums
+ * sequentially): results agree with gala to rounding. */
+int64_t gx_mockstream_animate_snapshots(int64_t ntimes, int64_t output_every);
+int gx_mockstream_dop853_animate(const gx_potential* pot, const gx_frame* frame, int64_t n_streams,
+                                 int32_t nbody, const gx_body* bodies, const double* nbody_w0,
+                                 int64_t ntimes, const double* t, double dt0, const int32_t* nstream,
+                                 const double* stream_w0, int64_t n_particles, int64_t output_every,
+                                 double atol, double rtol, int64_t nmax, double* scratch,
+                                 int64_t scratch_bytes, double* snap, double* w_out, int32_t* status,
+                                 int64_t* stats, void* stream);
 
 /* DirectNBody.integrate_orbit with LeapfrogIntegrator: leapfrog_integrate_nbody
  * (src/gala/integrate/cyintegrators/leapfrog.pyx:161-255) for n_systems

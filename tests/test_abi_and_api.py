@@ -153,7 +153,7 @@ def test_integrate_orbit_argument_errors_come_before_the_device():
         pot.integrate_orbit(w0, Integrator="euler", dt=1.0, n_steps=10)
 
 
-def test_nbody_and_mockstream_argument_errors():
+def test_nbody_and_mockstream_argument_errors(tmp_path):
     """Constructor and argument checks of DirectNBody (nbody/core.py:25-95) and
     MockStreamGenerator / stream DFs (mockstream_generator.py:20-100, df.pyx:48-60)."""
     from gala_gb300.mockstream import FardalStreamDF, MockStreamGenerator
@@ -183,8 +183,26 @@ def test_nbody_and_mockstream_argument_errors():
     prog = g.PhaseSpacePosition(pos=[10.0, 0, 0], vel=[0, 0.2, 0])
     with pytest.raises(ValueError, match="DOPRI853Integrator and LeapfrogIntegrator"):
         gen.run(prog, 1e5, Integrator=g.Ruth4Integrator, dt=1.0, n_steps=4)
-    with pytest.raises(NotImplementedError, match="output_every"):
+    # the animate mode's checks, all before any integration (mockstream_generator.py:296-336,
+    # mockstream.pyx:116-134)
+    with pytest.raises(ValueError, match="filename"):
         gen.run(prog, 1e5, output_every=2, dt=1.0, n_steps=4)
+    with pytest.raises(ValueError, match="filename"):
+        gen.run(prog, 1e5, output_every=2, Integrator="leapfrog", dt=1.0, n_steps=4)
+    with pytest.raises(NotImplementedError, match="LeapfrogIntegrator"):
+        gen.run(prog, 1e5, output_every=2, output_filename="x.h5", Integrator="leapfrog", dt=1.0, n_steps=4)
+    with pytest.raises(NotImplementedError, match="FP64"):
+        gen.run(prog, 1e5, output_every=2, output_filename="x.h5", Integrator_kwargs=dict(precision="fp32c"),
+                dt=1.0, n_steps=4)
+    with pytest.raises(ValueError, match="positive"):
+        gen.run(prog, 1e5, output_every=0, output_filename="x.h5", dt=1.0, n_steps=4)
+    existing = tmp_path / "exists.hdf5"
+    existing.write_bytes(b"")
+    with pytest.raises(OSError, match="already exists"):
+        gen.run(prog, 1e5, output_every=2, output_filename=str(existing), dt=1.0, n_steps=4)
+    with pytest.raises(OSError, match="already exists"), pytest.warns(UserWarning, match="8 GB"):
+        gen.run(prog, 1e5, output_every=1, output_filename=str(existing), n_particles=200_000, dt=1.0,
+                n_steps=4000)
     other = DirectNBody(psp, [None, None], external_potential=g.HernquistPotential(m=1e11, c=1.0))
     with pytest.raises(ValueError, match="external potential"):
         gen.run(prog, 1e5, nbody=other, dt=1.0, n_steps=4)

@@ -692,3 +692,120 @@ def test_fp32_dop853_release_systems_match_fp64():
     # the returned bodies are those of the last release system (mockstream.pyx:291-293),
     # which the FP32 form integrates with FP32 stages too
     np.testing.assert_allclose(r32.nbody_w.cpu().numpy(), r64.nbody_w.cpu().numpy(), rtol=1e-5)
+
+
+# ------------------------------------------------------------ animate mode
+def _animate_gpu(c, output_every, pot=None):
+    """gx_mockstream_dop853_animate on a stream_case: every stream's bodies at
+    t[0], the whole grid, particles released at every grid time."""
+    import torch
+
+    from gala_gb300._device import ptr, stream_handle
+
+    pot = c["pot"] if pot is None else pot
+    dev = torch.device("cuda")
+    t = c["t"]
+    S, n_rows = c["stream_w0"].shape[:2]
+    M = 1 + n_rows
+    lib = _abi.load()
+    n_out = int(lib.gx_mockstream_animate_snapshots(len(t), output_every))
+    nbytes = int(lib.gx_mockstream_wide_scratch_bytes(S, M))
+    scratch = torch.empty(nbytes // 8, dtype=torch.float64, device=dev)
+    snap = torch.empty((S, 6, n_out, M), dtype=torch.float64, device=dev)
+    w_out = torch.empty((S, M, 6), dtype=torch.float64, device=dev)
+    status = torch.zeros((S, len(t)), dtype=torch.int32, device=dev)
+    stats = torch.zeros((S, 4), dtype=torch.int64, device=dev)
+    nb0 = torch.from_numpy(np.ascontiguousarray(c["w0"].T.reshape(S, 1, 6))).to(dev)
+    sw0 = torch.from_numpy(np.ascontiguousarray(c["stream_w0"])).to(dev)
+    td = torch.from_numpy(np.ascontiguousarray(t)).to(dev)
+    nd = torch.from_numpy((2 * c["counts"]).astype(np.int32)).to(dev)
+    bd = bodies_to_device(c["bodies"], dev)
+    _abi.call("gx_mockstream_dop853_animate", pot.packed().for_device(), g.Hamiltonian(pot)._frame_ref(), S, 1,
+              ptr(bd), ptr(nb0), len(t), ptr(td), float(t[1] - t[0]), ptr(nd), ptr(sw0), n_rows, output_every,
+              1e-10, 1e-10, 0, ptr(scratch), nbytes, ptr(snap), ptr(w_out), ptr(status), ptr(stats), stream_handle())
+    torch.cuda.synchronize()
+    # (S, 6, n_out, M) -> (S, n_out, M, 6), the oracle's layout
+    return (snap.permute(0, 2, 3, 1).cpu().numpy(), w_out.cpu().numpy(), status.cpu().numpy(),
+            stats.cpu().numpy())
+
+
+@pytest.mark.parametrize("n_steps,output_every,release_every", [(61, 3, 2), (40, 1, 1), (17, 2, 4)])
+def test_animate_matches_oracle(oracle, n_steps, output_every, release_every):
+    """One growing system per stream, stepped interval by interval: the
+    snapshots, final states, per-interval status and summed counters match
+    the oracle (itself bit-identical to gala's dop853 on the same system).
+    The error and stiffness norms are CTA sums in another order than gala's
+    sequential ones, and the MW composite's pow / log differ by an ulp, so the
+    states agree to 1e-10 of their scale, not bit for bit."""
+    c = stream_case(n_streams=3, n_steps=n_steps, release_every=release_every)
+    snap, w, status, stats = _animate_gpu(c, output_every)
+    from tests.test_mockstream_oracle import _animate_args
+
+    for s in range(3):
+        r_snap, _, r_w, r_status, r_stats = oracle.mockstream_animate(c["pot"], **_animate_args(c, s, output_every))
+        assert snap[s].shape == r_snap.shape
+        np.testing.assert_array_equal(np.isnan(snap[s]), np.isnan(r_snap))
+        np.testing.assert_array_equal(status[s], r_status)
+        live = ~np.isnan(r_snap)
+        assert np.abs(snap[s][live] - r_snap[live]).max() < 1e-10 * np.abs(r_snap[live]).max()
+        assert _scale_err(w[s], r_w) < 1e-10
+        # steps, accepted and rejected steps: an accept / reject decision taken on
+        # a rounding-level difference may differ, nothing more
+        assert np.abs(stats[s][1:] - r_stats[1:]).max() <= 2
+
+
+def test_animate_one_burst_system_matches_oracle(oracle):
+    """gala's one-burst setting in the animate mode: 1,000 particles per tail
+    released at t[0] join a 2,001-member system for all of its 40 intervals."""
+    c = stream_case(n_streams=1, n_steps=40)
+    counts = np.zeros(41, dtype=int)
+    counts[0] = 1000
+    from gala_gb300.mockstream import FardalStreamDF as DF
+
+    df = DF(gala_modified=True, random_state=np.random.RandomState(5))
+    offset = np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)
+    orb = c["orbits"][0]
+    c["stream_w0"] = oracle.fardal_sample(c["pot"], orb.reshape(41, 6), np.full(41, c["m"][0]), c["t"], offset,
+                                          df._draws(int(offset[-1])), g.units.G)[None]
+    c["counts"] = counts
+    snap, w, status, _ = _animate_gpu(c, 10)
+    from tests.test_mockstream_oracle import _animate_args
+
+    r_snap, _, r_w, r_status, _ = oracle.mockstream_animate(c["pot"], **_animate_args(c, 0, 10))
+    assert w.shape == (1, 2001, 6)
+    np.testing.assert_array_equal(status[0], r_status)
+    assert _scale_err(w[0], r_w) < 1e-10
+    assert _scale_err(snap[0], r_snap) < 1e-10
+
+
+@pytest.mark.parametrize("dt,nsteps,output_every,release_every,n_particles,trail",
+                         [(1, 16, 1, 1, 1, True), (-1, 17, 2, 4, 4, False), (1, 17, 2, 1, 4, True),
+                          (-1, 16, 1, 4, 1, True)])
+def test_run_with_output_every_writes_galas_file(tmp_path, dt, nsteps, output_every, release_every, n_particles,
+                                                 trail):
+    """gala's test_animate (tests/dynamics/mockstream/test_mockstream.py:259-319):
+    the file's shapes, finite first snapshot, equal times in both groups; and the
+    returned stream equals the file's last snapshot."""
+    pot = W.mw_composite()
+    prog_pot = g.PlummerPotential(m=2e5, b=0.01)
+    gen = MockStreamGenerator(FardalStreamDF(gala_modified=True, trail=trail, random_state=np.random.RandomState(2)),
+                              g.Hamiltonian(pot), progenitor_potential=prog_pot)
+    fn = tmp_path / "animate.hdf5"
+    w0 = g.PhaseSpacePosition.from_w(W.mw_ics(1, seed=64)[:, 0])
+    stream, nbody = gen.run(w0, 2e5, dt=dt, n_steps=nsteps, release_every=release_every, n_particles=n_particles,
+                            output_every=output_every, output_filename=str(fn), overwrite=True)
+    from gala_gb300.hdf5 import File
+
+    with File(str(fn), "r") as f:
+        st = g.Orbit.from_hdf5(f["stream"])
+        nb = g.Orbit.from_hdf5(f["nbody"])
+    n_out = 1 + nsteps // output_every + int(nsteps % output_every != 0)
+    tail_n = (1 + int(trail)) * n_particles
+    assert st.xyz.shape[1:] == (n_out, tail_n * (nsteps // release_every + 1))
+    assert nb.xyz.shape[1:] == (n_out, 1)
+    # gala's stream_orbits[:, 0]: particle 0 (released at the first time) at every snapshot
+    assert np.isfinite(st.xyz[:, :, 0]).all() and np.isfinite(st.v_xyz[:, :, 0]).all()
+    np.testing.assert_array_equal(nb.t, st.t)
+    assert np.isfinite(nb.xyz).all() and np.isfinite(nb.t).all()
+    np.testing.assert_array_equal(st.xyz[:, -1], stream.xyz)
+    np.testing.assert_array_equal(nb.v_xyz[:, -1], nbody.v_xyz)

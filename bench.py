@@ -21,7 +21,9 @@ Variants in the same line (compact; ``--detail FILE`` writes every figure):
                       snapshot stored (HBM snapshot stream)
   scf_surrogate       SCF nmax 12 lmax 8 host, 262,144 orbits x 5,000 Leapfrog
                       steps: learned surrogate vs analytic FP32 / FP64
-  mock_streams        512 progenitors x 2,000 releases, DOP853 release systems
+  mock_streams        512 progenitors x 2,000 releases, DOP853 release systems;
+                      the animate mode (one growing system per stream, 152
+                      streams x 1,000 steps, snapshots every 10 steps)
   orbit_reductions    peri/apo/zmax over 100,000 orbits x 2,001 snapshots
 
 Arms
@@ -120,6 +122,8 @@ def parse_args():
     p.add_argument("--stream-progenitors", type=int, default=512)
     p.add_argument("--stream-nsteps", type=int, default=2000)
     p.add_argument("--stream-cpu-streams", type=int, default=8, help="streams in the CPU-baseline sample")
+    p.add_argument("--animate-streams", type=int, default=152, help="streams of the animate-mode measurement")
+    p.add_argument("--animate-nsteps", type=int, default=1000, help="grid steps of the animate-mode measurement")
     p.add_argument("--orbits", type=int, default=100_000, help="DOP853 variant: orbits per GPU")
     p.add_argument("--nsteps", type=int, default=10_000, help="DOP853 variant: steps")
     p.add_argument("--dop-reps", type=int, default=3, help="DOP853 variant: timed runs")
@@ -886,6 +890,39 @@ def run_mock_streams(args, torch, stream):
         lf_out[name] = o.cpu().numpy()
     o64, o32 = lf_out["gx_mockstream_leapfrog"], lf_out["gx_mockstream_leapfrog_fp32"]
     perr = (np.linalg.norm(o32[..., :3] - o64[..., :3], axis=-1) / np.linalg.norm(o64[..., :3], axis=-1)).ravel()
+
+    # animate mode (output_every): one growing shared-step system per stream over
+    # the first args.animate_nsteps grid steps, a snapshot every 10 steps
+    sa, na = min(S, args.animate_streams), min(nsteps, args.animate_nsteps) + 1
+    rows_a = int(2 * counts[:na].sum())
+    nd_a = torch.from_numpy((2 * counts[:na]).astype(np.int32)).cuda()
+    sw_a = sw0[:sa, :rows_a].contiguous()
+    nb0_a = orbit[:sa, 0].contiguous()
+    td_a = td[:na].contiguous()
+    Ma = 1 + rows_a
+    lib = _abi.load()
+    n_out_a = int(lib.gx_mockstream_animate_snapshots(na, 10))
+    nbytes_a = int(lib.gx_mockstream_wide_scratch_bytes(sa, Ma))
+    scratch_a = torch.empty(nbytes_a // 8, dtype=torch.float64, device="cuda")
+    snap_a = torch.empty((sa, 6, n_out_a, Ma), dtype=torch.float64, device="cuda")
+    w_a = torch.empty((sa, Ma, 6), dtype=torch.float64, device="cuda")
+    st_a = torch.zeros((sa, na), dtype=torch.int32, device="cuda")
+    stats_a = torch.zeros((sa, 4), dtype=torch.int64, device="cuda")
+
+    def animate_call():
+        _abi.call("gx_mockstream_dop853_animate", desc, H._frame_ref(), sa, 1, ptr(bd), ptr(nb0_a), na, ptr(td_a),
+                  1.0, ptr(nd_a), ptr(sw_a), rows_a, 10, 1e-10, 1e-10, 0, ptr(scratch_a), nbytes_a, ptr(snap_a),
+                  ptr(w_a), ptr(st_a), ptr(stats_a), int(stream.cuda_stream))
+
+    e0.record(stream)
+    animate_call()
+    e1.record(stream)
+    e1.synchronize()
+    ms_anim = e0.elapsed_time(e1)
+    # particle-steps: every particle from its release time to the end of the grid
+    live = np.cumsum(2 * counts[:na])[:-1]
+    anim_particle_steps = sa * float(live.sum())
+    st_anim = st_a.cpu().numpy()
     lf_flops = S * float(np.sum(np.round(t_final - t))) * (3 * (F_FORCE_MW + 18) + 2 * F_PLUMMER_PULL)
     fp64_peak = fma_peak(torch, stream, True)
     result = {
@@ -911,6 +948,11 @@ def run_mock_streams(args, torch, stream):
         "leapfrog_fp32c": {"value": particle_steps / (lf_ms["gx_mockstream_leapfrog_fp32"] * 1e-3),
                            "position_error_vs_fp64_median": float(np.median(perr)),
                            "position_error_vs_fp64_p99": float(np.percentile(perr, 99))},
+        "animate": {"workload": f"{sa} streams, {na - 1} steps, one growing DOP853 system per stream "
+                                f"(up to {Ma} members), snapshot every 10 steps ({n_out_a} snapshots)",
+                    "value": anim_particle_steps / (ms_anim * 1e-3), "unit": "particle-steps/s", "ms": ms_anim,
+                    "intervals_ok": float(np.mean(st_anim[:, 1:] == 1)),
+                    "snapshot_bytes": int(snap_a.numel() * 8)},
     }
     if not args.no_cpu_baseline:
         from oracle import Oracle
@@ -936,6 +978,29 @@ def run_mock_streams(args, torch, stream):
             "status_agreement": float(np.mean(gpu_st == cpu_status)),
             "position_diff_kpc_p99": float(np.percentile(pe, 99)) if pe.size else None,
         }
+        # the animate mode's CPU baseline: gala's interval loop restated in C, one
+        # stream per host thread (ctypes releases the GIL), a bounded sample of streams
+        from concurrent.futures import ThreadPoolExecutor
+
+        na_cpu = min(sa, nth)
+        bodies_np = bodies[:na_cpu]
+        nb0_np, sw_np, t_np = nb0_a[:na_cpu].cpu().numpy(), sw_a[:na_cpu].cpu().numpy(), t[:na]
+
+        def one(k):
+            return fast.mockstream_animate(pot, bodies_np[k], nb0_np[k], t_np, sw_np[k], 2 * counts[:na],
+                                           output_every=10)
+
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=nth) as ex:
+            outs = list(ex.map(one, range(na_cpu)))
+        cpu_anim_s = time.perf_counter() - t0
+        w_gpu = w_a[:na_cpu].cpu().numpy()
+        diff = max(float(np.abs(w_gpu[k] - outs[k][2]).max() / np.abs(outs[k][2]).max()) for k in range(na_cpu))
+        result["animate"]["cpu_baseline"] = {
+            "value": na_cpu * float(live.sum()) / cpu_anim_s, "unit": "particle-steps/s", "cores": nth,
+            "kind": "port", "sample": f"{na_cpu} of the {sa} streams, gala's mockstream_dop853_animate loop "
+                                      "restated in C, -Ofast, one stream per thread",
+            "gpu_vs_cpu_max_rel": diff}
     return result
 
 
@@ -1040,7 +1105,10 @@ def compact(name, r):
                 "release_fp32": sig(r["release_kernel_fp32"]["value"]),
                 "release_fp32_pos_err_median": sig(r["release_kernel_fp32"]["position_error_vs_fp64_median"], 2),
                 "leapfrog_fp32c": sig(r["leapfrog_fp32c"]["value"]), "cpu_16c": sig(cb.get("value")),
-                "status_agreement": sig(cb.get("status_agreement"), 5)}
+                "status_agreement": sig(cb.get("status_agreement"), 5),
+                "animate": sig(r["animate"]["value"]),
+                "animate_cpu": sig(r["animate"].get("cpu_baseline", {}).get("value")),
+                "animate_vs_cpu_max_rel": sig(r["animate"].get("cpu_baseline", {}).get("gpu_vs_cpu_max_rel"), 2)}
     if name == "orbit_reductions":
         return {"unit": "orbit-snapshots/s", "value": sig(r["value"]), "frac_hbm": sig(r["roofline"]["frac"], 3),
                 "cpu_1c": sig(cb.get("value"))}

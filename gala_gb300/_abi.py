@@ -6,6 +6,7 @@ cannot be loaded, every call raises: there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import threading
 from pathlib import Path
 
@@ -83,6 +84,8 @@ SIGNATURES = {
     "gx_cancel_flag_create": (C.c_int, [_P, _P]),
     "gx_set_cancel_flag": (None, [_P]),
     "gx_cancel_flag_destroy": (C.c_int, [_P]),
+    "gx_debug_enabled": (C.c_int, []),
+    "gx_debug_read": (C.c_int, [_P, _I32]),
     "gx_potential_value": (C.c_int, [_PP, _D, _P, _I64, _P, _P]),
     "gx_potential_gradient": (C.c_int, [_PP, _D, _P, _I64, _P, _P]),
     "gx_potential_density": (C.c_int, [_PP, _D, _P, _I64, _P, _P]),
@@ -139,6 +142,7 @@ SIGNATURES = {
 }
 
 _lib = None
+_lib_debug = None
 _lock = threading.Lock()
 
 
@@ -151,29 +155,46 @@ class GxError(RuntimeError):
 
 
 def library_path() -> Path:
-    return _build.LIB
+    return _build.LIB_DEBUG if _debug_requested() else _build.LIB
+
+
+def _debug_requested() -> bool:
+    """GALA_GB300_DEBUG=1 makes the debug library the process's library."""
+    return os.environ.get("GALA_GB300_DEBUG", "") not in ("", "0")
+
+
+def _bind(path: Path, debug: bool, build_if_missing: bool):
+    if not path.exists() or _build._sources_newer(path):
+        if not build_if_missing:
+            raise RuntimeError(f"CUDA library not built: {path}")
+        _build.build(debug=debug)
+    lib = C.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.gx_abi_version() != 2:
+        raise RuntimeError("gala_gb300 library ABI version mismatch")
+    return lib
 
 
 def load(build_if_missing: bool = True):
     """Load (building first if needed) the CUDA library and bind every symbol."""
     global _lib
     with _lock:
-        if _lib is not None:
-            return _lib
-        path = library_path()
-        if not path.exists() or _build._sources_newer(path):
-            if not build_if_missing:
-                raise RuntimeError(f"CUDA library not built: {path}")
-            _build.build()
-        lib = C.CDLL(str(path))
-        for name, (res, args) in SIGNATURES.items():
-            fn = getattr(lib, name)
-            fn.restype = res
-            fn.argtypes = args
-        if lib.gx_abi_version() != 2:
-            raise RuntimeError("gala_gb300 library ABI version mismatch")
-        _lib = lib
-        return lib
+        if _lib is None:
+            _lib = _bind(library_path(), _debug_requested(), build_if_missing)
+        return _lib
+
+
+def load_debug(build_if_missing: bool = True):
+    """The debug library (libgala_gb300_debug.so: the same entry points with
+    device-side check records, gx_debug_read), bound beside the release one."""
+    global _lib_debug
+    with _lock:
+        if _lib_debug is None:
+            _lib_debug = _bind(_build.LIB_DEBUG, True, build_if_missing)
+        return _lib_debug
 
 
 def call(name: str, *args) -> int:

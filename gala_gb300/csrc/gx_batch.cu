@@ -107,8 +107,11 @@ __global__ void __launch_bounds__(256) batch_fp32_kernel(const __grid_constant__
         for (int r = 0; r < A.chunk; r += 32) {
             const int64_t slot = (int64_t)c * A.chunk + r + lane;
             const int32_t i = order[slot];
-            if (i >= 0 && i < A.n)
+            // -1 pads the order; any other id outside [0, n) is skipped (and recorded in the debug build)
+            if (i != -1 && GX_DBG_CHECK(i >= 0 && i < A.n, DBG_ORDER, i, A.n)) {
                 integrate_one_fp32<S>(pot, A, w0, A.n, i, nsteps[i], (float)dt[i], method[i], w_out);
+                GX_DBG_DONE(i, nsteps[i]);
+            }
         }
     }
 }

@@ -124,6 +124,8 @@ dop853_fp32_kernel(const __grid_constant__ DevPotF pot, const Dop32Args A, const
             const int64_t k = atomicAdd(counter, 1);
             if (k >= n) break;
             i = order ? (int64_t)order[k] : k;
+            // an order entry outside [0, n) is skipped (and recorded in the debug build)
+            if (!GX_DBG_CHECK(i >= 0 && i < n, DBG_ORDER, i, n)) continue;
             need = false;
             for (int c = 0; c < 6; c++) split_d(w0[c * n + i], yh[c], yl[c]);
             x = x0;
@@ -370,6 +372,7 @@ dop853_fp32_kernel(const __grid_constant__ DevPotF pot, const Dop32Args A, const
             if (!A.save_all)
                 for (int c = 0; c < 6; c++) out[c * n + i] = (double)yh[c] + (double)yl[c];
             status[i] = idid;
+            GX_DBG_DONE(i, nstep);
             if (stats) {
                 stats[4 * i + 0] = nfcn;
                 stats[4 * i + 1] = nstep;

@@ -128,7 +128,9 @@ __global__ void __launch_bounds__(128, 1) batch_fp64_kernel(const __grid_constan
         if (c >= nchunks) break;
         for (int r = 0; r < chunk; r += 32) {
             const int32_t i = order[(int64_t)c * chunk + r + lane];
-            if (i < 0 || i >= n) continue;
+            // -1 pads the order; any other id outside [0, n) is skipped (and recorded in the debug build)
+            if (i == -1 || !GX_DBG_CHECK(i >= 0 && i < n, DBG_ORDER, i, n)) continue;
+            GX_DBG_DONE(i, nsteps[i]);
             double w[6], g[3];
             for (int k = 0; k < 6; k++) w[k] = w0[k * n + i];
             const int64_t ns = nsteps[i];

@@ -2,6 +2,7 @@
 // Hamiltonian evaluation entry points (gx_potential_value, gx_potential_gradient,
 // gx_potential_density, gx_hamiltonian_value, gx_hamiltonian_gradient).
 #include <cmath>
+#include <vector>
 
 #include "gx_host.h"
 #include "gx_scf.cuh"
@@ -227,6 +228,13 @@ static int launch_ham(const gx_potential *pot, const gx_frame *fr, const double 
 static thread_local const int32_t *g_cancel = nullptr;
 const int32_t *cancel_flag() { return g_cancel; }
 
+// Readers of the debug records, one per translation unit (debug build only).
+static std::vector<DbgReader> &dbg_readers() {
+    static std::vector<DbgReader> r;
+    return r;
+}
+void dbg_register(DbgReader r) { dbg_readers().push_back(r); }
+
 }  // namespace gx
 
 extern "C" {
@@ -281,6 +289,43 @@ int gx_cancel_flag_create(int32_t **host_ptr, int32_t **device_ptr) {
     }
     *host_ptr = static_cast<int32_t *>(h);
     *device_ptr = static_cast<int32_t *>(d);
+    return GX_OK;
+}
+
+int gx_debug_enabled(void) {
+#ifdef GX_DEBUG_CHECKS
+    return 1;
+#else
+    return 0;
+#endif
+}
+
+int gx_debug_read(int64_t *out, int32_t reset) {
+    GX_CHECK_ARG(out, "NULL pointer");
+    for (int k = 0; k < 9; k++) out[k] = 0;
+    if (!gx_debug_enabled()) {
+        gx::set_error("the release library keeps no debug records (load libgala_gb300_debug.so)");
+        return GX_ERR_UNSUPPORTED;
+    }
+    GX_CUDA_TRY(cudaDeviceSynchronize());
+    for (gx::DbgReader rd : gx::dbg_readers()) {
+        gx::DbgRecord r;
+        if (rd(&r, reset != 0) != 0) {
+            gx::set_error("reading a debug record failed");
+            return GX_ERR_CUDA;
+        }
+        if (r.first && !out[0]) {
+            out[0] = (int64_t)(r.first >> 32);
+            out[1] = (int64_t)(r.first & 0xffffffffu);
+            out[2] = r.index;
+            out[3] = r.bound;
+        }
+        out[4] += (int64_t)r.fails;
+        out[5] += (int64_t)r.done;
+        out[6] += (int64_t)r.id_sum;
+        out[7] += (int64_t)r.id_sq;
+        out[8] += (int64_t)r.steps;
+    }
     return GX_OK;
 }
 

@@ -9,6 +9,7 @@
 #include <cstring>
 #include <cuda_runtime.h>
 
+#include "gx_debug.cuh"
 #include "gx_device.cuh"
 
 namespace gx {

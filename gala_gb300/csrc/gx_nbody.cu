@@ -183,6 +183,7 @@ nbody_dop853_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
                     const bool bad = o1 < o0 || o0 < 0 || o1 > A.n_particles || o1 - o0 > gs - A.nbody;
                     if (o1 == o0 || bad) {
                         if (member == 0) {
+                            (void)GX_DBG_CHECK(!bad, DBG_OFFSET, si, A.n_release);
                             A.status[ss * A.n_release + si] = bad ? -1 : 0;
                             if (A.stats)
                                 for (int k = 0; k < 4; k++) A.stats[(ss * A.n_release + si) * 4 + k] = 0;

@@ -210,6 +210,7 @@ __global__ void __launch_bounds__(128) ms_dop853_fp32_kernel(const __grid_consta
                 const bool bad = o1 < o0 || o0 < 0 || o1 > A.n_particles || o1 - o0 > gs - nbody;
                 if (o1 == o0 || bad) {
                     if (member == 0) {
+                        (void)GX_DBG_CHECK(!bad, DBG_OFFSET, si, A.n_release);
                         A.status[ss * A.n_release + si] = bad ? -1 : 0;
                         if (A.stats)
                             for (int k = 0; k < 4; k++) A.stats[(ss * A.n_release + si) * 4 + k] = 0;

@@ -273,12 +273,17 @@ nbody_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ De
     if (__syncthreads_or(threadIdx.x == 0 && cancel_requested(A.cancel))) return;
     const int64_t sys = A.systems[b];
     const int64_t si = sys / A.n_streams, ss = sys - si * A.n_streams;
-    if (si < 0 || si >= A.n_release) return;  // an id outside the release grid: nothing to address
+    // an id outside the release grid: nothing to address (recorded in the debug build)
+    if (!GX_DBG_CHECK(si >= 0 && si < A.n_release, DBG_SYSTEM, sys, A.n_release * A.n_streams)) return;
     const int64_t o0 = A.offset[si], o1 = A.offset[si + 1];
     const int64_t M = A.max_members;
     const int nbody = A.nbody;
     if (o1 < o0 || o0 < 0 || o1 > A.n_particles || nbody + (o1 - o0) > M) {
-        if (threadIdx.x == 0) A.status[ss * A.n_release + si] = -1;  // inconsistent offsets: no access
+        // inconsistent offsets: no access
+        if (threadIdx.x == 0) {
+            (void)GX_DBG_CHECK(false, DBG_OFFSET, si, A.n_release);
+            A.status[ss * A.n_release + si] = -1;
+        }
         return;
     }
     const int nmem = nbody + (int)(o1 - o0);
@@ -372,6 +377,7 @@ animate_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
     auto grow = [&](int64_t n, int64_t i, int &bad) {
         const int64_t k = A.nstream[i];
         bad = (k < 0 || n + k > A.n_particles);
+        if (bad && tid == 0) (void)GX_DBG_CHECK(false, DBG_COUNT, i, A.ntimes);
         return bad ? (k < 0 ? n : A.n_particles) : n + k;
     };
     int bad = 0;

@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(128) lf_stream_fp32_kernel(const __grid_consta
         A.status[ss * A.n_release + si] = 0;
         return;
     }
-    if (o1 < o0 || o0 < 0 || o1 > A.n_particles || A.nbody + (o1 - o0) > MAXB) {
+    if (!GX_DBG_CHECK(!(o1 < o0 || o0 < 0 || o1 > A.n_particles || A.nbody + (o1 - o0) > MAXB), DBG_OFFSET, si,
+                      A.n_release)) {
         A.status[ss * A.n_release + si] = -1;
         return;
     }

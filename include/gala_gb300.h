@@ -185,6 +185,24 @@ int gx_cancel_flag_create(int32_t** host_ptr, int32_t** device_ptr);
 void gx_set_cancel_flag(const int32_t* device_ptr);
 int gx_cancel_flag_destroy(int32_t* host_ptr);
 
+/* The debug build.  The kernels test every index that comes from a caller's
+ * device array (queue orders, system ids, release offsets and counts) and skip
+ * what is out of range.  libgala_gb300_debug.so (the same sources compiled with
+ * GX_DEBUG_CHECKS) also records each failed test in device memory, and the
+ * persistent queues of gx_batch_integrate_fp32 / _fp64 and gx_dop853_fp32 add
+ * every orbit they complete to a count, sum(id + 1), sum((id + 1)^2) and a
+ * step total.  No check traps.  gala has no counterpart (its loops are compiled
+ * without bounds checks, boundscheck=False).
+ *   gx_debug_enabled()      1 in the debug build, 0 in the release library
+ *   gx_debug_read(out, r)   synchronises the device and writes int64[9] =
+ *       {code of the first failure (1 order id, 2 system id, 3 release offsets,
+ *        4 release count; 0 none), its source line, index, bound, failures,
+ *        orbits completed, sum(id + 1), sum((id + 1)^2), steps}
+ *     summed over the library's translation units; r != 0 clears the records.
+ *     GX_ERR_UNSUPPORTED in the release library. */
+int gx_debug_enabled(void);
+int gx_debug_read(int64_t* out, int32_t reset);
+
 /* ------------------------------------------------------------------------- */
 /* Potential evaluation over N points.                                       */
 /* q is (3, N) SoA; out is (N,) for value/density and (3, N) for gradient.   */

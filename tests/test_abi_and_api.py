@@ -403,3 +403,16 @@ def test_stepped_time_grids_are_running_sums():
         for sgn in (1, -1):
             got = g.parse_time_specification(dt=sgn * dt, t1=t1, t2=t1 + sgn * span)
             assert np.array_equal(got, running(t1, t1 + sgn * span, sgn * dt))
+
+
+def test_debug_library_reports_its_build():
+    """libgala_gb300_debug.so is the same ABI with the device-side check records
+    (GX_DEBUG_CHECKS); the release library keeps none and says so."""
+    import ctypes as C
+
+    rel, dbg = _abi.load(), _abi.load_debug()
+    assert rel.gx_debug_enabled() == 0 and dbg.gx_debug_enabled() == 1
+    assert dbg.gx_abi_version() == rel.gx_abi_version()
+    out = (C.c_int64 * 9)()
+    assert rel.gx_debug_read(C.cast(out, C.c_void_p), 0) == _abi.GX_ERR_UNSUPPORTED
+    assert b"release library" in rel.gx_last_error_message()

@@ -194,6 +194,33 @@ def test_dop853_nmax_failure_raises():
     mw.integrate_orbit(w0, dt=0.5, n_steps=200, Integrator="dop853", Integrator_kwargs=dict(nmax=3, err_if_fail=0))
 
 
+@pytest.mark.parametrize("bad", [np.nan, np.inf])
+def test_dop853_non_finite_initial_conditions_match_ieee_gala(oracle, bad):
+    """A NaN or infinite initial condition: gala's dop853() with IEEE arithmetic
+    rejects every step until nmax and reports -2 (its -Ofast build differs, see
+    tests/test_oracle.py); the GPU has IEEE arithmetic and reports -2 too, for
+    that orbit's batch only, with the same counters as the oracle."""
+    import torch
+
+    from gala_gb300 import _abi
+    from gala_gb300._device import ptr, stream_handle
+
+    pot = g.HernquistPotential(m=1e11, c=1.0)
+    t = g.parse_time_specification(dt=1.0, n_steps=50)
+    w0 = np.array([[8.0, 8.0], [0, 0], [0, 0], [0, 0], [0.2, 0.2], [0, 0]])
+    w0[0, 1] = bad
+    _, st_ref, stats_ref = oracle.dop853(pot, w0, t, nbatch=1, nmax=500)
+    assert st_ref.tolist() == [1, -2]
+    wd, td = torch.from_numpy(w0).cuda(), torch.from_numpy(t).cuda()
+    out = torch.empty((6, len(t), 2), dtype=torch.float64, device="cuda")
+    st = torch.zeros(2, dtype=torch.int32, device="cuda")
+    stats = torch.zeros((2, 4), dtype=torch.int64, device="cuda")
+    _abi.call("gx_dop853_integrate_hamiltonian", pot.packed().for_device(), g.Hamiltonian(pot)._frame_ref(), ptr(wd),
+              2, ptr(td), len(t), 1e-10, 1e-10, 500, 0.0, 0, 1, 1, 1, ptr(out), ptr(st), ptr(stats), stream_handle())
+    assert st.cpu().tolist() == [1, -2]
+    np.testing.assert_array_equal(stats.cpu().numpy(), stats_ref)
+
+
 # ----------------------------------------------------------------- edge cases
 @pytest.mark.parametrize("method", ["leapfrog", "ruth4", "dop853"])
 def test_single_orbit_shapes_and_save_all(oracle, method):

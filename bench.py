@@ -923,6 +923,23 @@ def run_mock_streams(args, torch, stream):
     live = np.cumsum(2 * counts[:na])[:-1]
     anim_particle_steps = sa * float(live.sum())
     st_anim = st_a.cpu().numpy()
+    # the same streams with FP32 stages and forces and FP64 step control (rtol 1e-8)
+    snap_a32 = torch.empty_like(snap_a)
+    w_a32 = torch.empty_like(w_a)
+    st_a32 = torch.zeros_like(st_a)
+
+    def animate_call_fp32():
+        _abi.call("gx_mockstream_dop853_animate_fp32", desc, sa, 1, ptr(bd), ptr(nb0_a), na, ptr(td_a), 1.0,
+                  ptr(nd_a), ptr(sw_a), rows_a, 10, DOP32_ATOL, DOP32_RTOL, 0, ptr(scratch_a), nbytes_a,
+                  ptr(snap_a32), ptr(w_a32), ptr(st_a32), None, int(stream.cuda_stream))
+
+    e0.record(stream)
+    animate_call_fp32()
+    e1.record(stream)
+    e1.synchronize()
+    ms_anim32 = e0.elapsed_time(e1)
+    wa64, wa32 = w_a.cpu().numpy(), w_a32.cpu().numpy()
+    perr_a = (np.linalg.norm(wa32[..., :3] - wa64[..., :3], axis=-1) / np.linalg.norm(wa64[..., :3], axis=-1)).ravel()
     lf_flops = S * float(np.sum(np.round(t_final - t))) * (3 * (F_FORCE_MW + 18) + 2 * F_PLUMMER_PULL)
     fp64_peak = fma_peak(torch, stream, True)
     result = {
@@ -952,7 +969,12 @@ def run_mock_streams(args, torch, stream):
                                 f"(up to {Ma} members), snapshot every 10 steps ({n_out_a} snapshots)",
                     "value": anim_particle_steps / (ms_anim * 1e-3), "unit": "particle-steps/s", "ms": ms_anim,
                     "intervals_ok": float(np.mean(st_anim[:, 1:] == 1)),
-                    "snapshot_bytes": int(snap_a.numel() * 8)},
+                    "snapshot_bytes": int(snap_a.numel() * 8),
+                    "fp32": {"value": anim_particle_steps / (ms_anim32 * 1e-3), "ms": ms_anim32, "atol": DOP32_ATOL,
+                             "rtol": DOP32_RTOL, "speedup_vs_fp64": ms_anim / ms_anim32,
+                             "intervals_ok": float(np.mean(st_a32.cpu().numpy()[:, 1:] == 1)),
+                             "final_position_error_vs_fp64_median": float(np.median(perr_a)),
+                             "final_position_error_vs_fp64_p99": float(np.percentile(perr_a, 99))}},
     }
     if not args.no_cpu_baseline:
         from oracle import Oracle
@@ -1106,7 +1128,8 @@ def compact(name, r):
                 "release_fp32_pos_err_median": sig(r["release_kernel_fp32"]["position_error_vs_fp64_median"], 2),
                 "leapfrog_fp32c": sig(r["leapfrog_fp32c"]["value"]), "cpu_16c": sig(cb.get("value")),
                 "status_agreement": sig(cb.get("status_agreement"), 5),
-                "animate": sig(r["animate"]["value"]),
+                "animate": sig(r["animate"]["value"]), "animate_fp32": sig(r["animate"]["fp32"]["value"]),
+                "animate_fp32_pos_err_median": sig(r["animate"]["fp32"]["final_position_error_vs_fp64_median"], 2),
                 "animate_cpu": sig(r["animate"].get("cpu_baseline", {}).get("value")),
                 "animate_vs_cpu_max_rel": sig(r["animate"].get("cpu_baseline", {}).get("gpu_vs_cpu_max_rel"), 2)}
     if name == "orbit_reductions":

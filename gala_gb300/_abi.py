@@ -122,6 +122,8 @@ SIGNATURES = {
     "gx_mockstream_animate_snapshots": (C.c_int64, [_I64, _I64]),
     "gx_mockstream_dop853_animate": (C.c_int, [_PP, _PF, _I64, _I32, _P, _P, _I64, _P, _D, _P, _P, _I64, _I64, _D,
                                                _D, _I64, _P, _I64, _P, _P, _P, _P, _P]),
+    "gx_mockstream_dop853_animate_fp32": (C.c_int, [_PP, _I64, _I32, _P, _P, _I64, _P, _D, _P, _P, _I64, _I64, _D,
+                                                    _D, _I64, _P, _I64, _P, _P, _P, _P, _P]),
     "gx_nbody_leapfrog": (C.c_int, [_PP, _I64, _I32, _I32, _P, _P, _P, _I64, _I32, _P, _P]),
     "gx_mockstream_leapfrog": (C.c_int, [_PP, _I64, _I32, _P, _P, _I64, _P, _P, _I32, _P, _I64, _D, _D, _P, _P, _P,
                                          _P]),
@@ -132,6 +134,9 @@ SIGNATURES = {
     "gx_stream_sample": (C.c_int, [_PP, _I64, _I64, _P, _I64, _P, _P, _P, _I64, _I32, _P, _D, _I32, _I32, _I32, _P,
                                    _P]),
     "gx_batch_integrate_fp64": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P]),
+    "gx_batch_schedule_slots": (C.c_int64, [_I64, _I32]),
+    "gx_batch_schedule_work_words": (C.c_int64, [_I64, _I32]),
+    "gx_batch_schedule": (C.c_int, [_P, _P, _I64, _I32, _P, _I64, _P, _I64, _P]),
     "gx_dop853_integrate_hamiltonian": (
         C.c_int,
         [_PP, _PF, _P, _I64, _P, _I64, _D, _D, _I64, _D, _I64, _I32, _I32, _I64, _P, _P, _P, _P],

@@ -38,6 +38,7 @@ UNITS = {
     "gx_batch.cu": [],
     "gx_dop853_fp32.cu": [],
     "gx_nbody_fp32.cu": [],
+    "gx_nbody_wide_fp32.cu": [],
     "gx_stream32.cu": [],
     "gx_mlp_train.cu": [],
     "gx_mlp_infer.cu": [],

@@ -483,7 +483,7 @@ class MockStreamGenerator:
         ntail = self.df.lead + self.df.trail
         if output_every is not None:
             return self._animate(bodies, nbody0, orbit_t, ntail * counts, stream_w0, release_time, lead_trail, dop,
-                                 output_every, check, return_stats, stream)
+                                 output_every, check, return_stats, stream, precision)
 
         # 3. release grid: times that release particles, plus the first (:271-283)
         rel_idx = np.nonzero(counts > 0)[0]
@@ -550,9 +550,11 @@ class MockStreamGenerator:
         return MockStreamBatch(stream_out, nbody_out, release_time, lead_trail, status, stats, H.frame, orbit_t)
 
     def _animate(self, bodies, nbody0, orbit_t, nstream, stream_w0, release_time, lead_trail, dop, output_every,
-                 check, return_stats, stream):
+                 check, return_stats, stream, precision="fp64"):
         """mockstream_dop853_animate's stage (mockstream.pyx:306-440) for every
-        stream: nstream (ntimes,) particles released at each grid time."""
+        stream: nstream (ntimes,) particles released at each grid time.  With
+        precision="fp32c" the systems run with FP32 stages and forces and FP64
+        step control (gx_mockstream_dop853_animate_fp32)."""
         import torch
 
         from ._device import ptr, stream_handle
@@ -576,10 +578,14 @@ class MockStreamGenerator:
         td = torch.from_numpy(np.ascontiguousarray(orbit_t, dtype=np.float64)).to(dev)
         nd = torch.from_numpy(nstream).to(dev)
         nbody0 = nbody0.reshape(S, nb, 6).contiguous()
-        _abi.call("gx_mockstream_dop853_animate", H.potential.packed().for_device(), H._frame_ref(), S, nb, ptr(bd),
-                  ptr(nbody0), ntimes, ptr(td), float(orbit_t[1] - orbit_t[0]), ptr(nd), ptr(stream_w0), n_rows,
-                  int(output_every), dop["atol"], dop["rtol"], dop["nmax"], ptr(scratch), nbytes, ptr(snap),
-                  ptr(w_out), ptr(status), ptr(stats) if stats is not None else None, stream_handle(stream))
+        common = (S, nb, ptr(bd), ptr(nbody0), ntimes, ptr(td), float(orbit_t[1] - orbit_t[0]), ptr(nd),
+                  ptr(stream_w0), n_rows, int(output_every), dop["atol"], dop["rtol"], dop["nmax"], ptr(scratch),
+                  nbytes, ptr(snap), ptr(w_out), ptr(status), ptr(stats) if stats is not None else None,
+                  stream_handle(stream))
+        if precision == "fp32c":
+            _abi.call("gx_mockstream_dop853_animate_fp32", H.potential.packed().for_device(), *common)
+        else:
+            _abi.call("gx_mockstream_dop853_animate", H.potential.packed().for_device(), H._frame_ref(), *common)
         check(status, "stream")
         idx = [0] + [i for i in range(1, ntimes) if i % output_every == 0 or i == ntimes - 1]
         return MockStreamBatch(w_out[:, nb:], w_out[:, :nb], release_time, lead_trail, status, stats, H.frame,
@@ -672,8 +678,8 @@ class MockStreamGenerator:
         """The animate mode's integrator checks (mockstream_generator.py:318-336)."""
         if Integrator is LeapfrogIntegrator:
             raise NotImplementedError("Animation output for LeapfrogIntegrator is not implemented")
-        if precision != "fp64":
-            raise NotImplementedError("animation output runs the FP64 DOP853 form")
+        if precision not in ("fp64", "fp32c"):
+            raise ValueError("precision must be 'fp64' or 'fp32c'")
         output_every = int(output_every)
         if output_every < 1:
             raise ValueError("output_every must be a positive integer")

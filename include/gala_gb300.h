@@ -314,6 +314,21 @@ int gx_dop853_fp32(const gx_potential* pot, const gx_frame* frame, const double*
                    int64_t out_stride, const int32_t* order, double* w_out, int32_t* status,
                    int64_t* stats, int32_t* queue_counter, void* stream);
 
+/* The processing order of a batch for gx_batch_integrate_fp32 / _fp64, built
+ * on the device with no host synchronisation: per integrator the orbits by
+ * cost (n_steps x 1 for Leapfrog, x 3 for Ruth4) in 16 bins per octave, the
+ * most expensive first, cut into chunks of `chunk` padded with -1; the chunks
+ * of both integrators merged by the bin of their first orbit.
+ *   n_steps, method  DEVICE (N,) as for gx_batch_integrate_fp32
+ *   order            DEVICE int32[n_slots], n_slots >= gx_batch_schedule_slots(N, chunk)
+ *                    (every slot written: an orbit index or -1)
+ *   work             DEVICE int32[gx_batch_schedule_work_words(N, chunk)] scratch
+ * No gala counterpart (gala integrates orbits one after another). */
+int64_t gx_batch_schedule_slots(int64_t n, int32_t chunk);
+int64_t gx_batch_schedule_work_words(int64_t n, int32_t chunk);
+int gx_batch_schedule(const int64_t* n_steps, const int32_t* method, int64_t n, int32_t chunk,
+                      int32_t* order, int64_t n_slots, int32_t* work, int64_t work_words, void* stream);
+
 /* ------------------------------------------------------------------------- */
 /* Batched FP32 integration with compensated state (no single gala function:  */
 /* it runs many leapfrog_integrate_hamiltonian / ruth4_integrate_hamiltonian  */
@@ -596,6 +611,21 @@ int gx_mockstream_dop853_animate(const gx_potential* pot, const gx_frame* frame,
                                  double atol, double rtol, int64_t nmax, double* scratch,
                                  int64_t scratch_bytes, double* snap, double* w_out, int32_t* status,
                                  int64_t* stats, void* stream);
+
+/* The animate mode with FP32 stages and forces and FP64 step control (the
+ * arithmetic of gx_mockstream_dop853_fp32: double-float state, FP64 time,
+ * error-norm combination and accept/reject, the particle-body separations
+ * from the double-float parts).  Same arguments and outputs as
+ * gx_mockstream_dop853_animate without the frame (static frames only), and
+ * the same scratch size; nbody <= 32.  Not bit-compatible with gala;
+ * tolerances below ~1e-8 relative only shrink the steps. */
+int gx_mockstream_dop853_animate_fp32(const gx_potential* pot, int64_t n_streams, int32_t nbody,
+                                      const gx_body* bodies, const double* nbody_w0, int64_t ntimes,
+                                      const double* t, double dt0, const int32_t* nstream,
+                                      const double* stream_w0, int64_t n_particles,
+                                      int64_t output_every, double atol, double rtol, int64_t nmax,
+                                      double* scratch, int64_t scratch_bytes, double* snap,
+                                      double* w_out, int32_t* status, int64_t* stats, void* stream);
 
 /* DirectNBody.integrate_orbit with LeapfrogIntegrator: leapfrog_integrate_nbody
  * (src/gala/integrate/cyintegrators/leapfrog.pyx:161-255) for n_systems

@@ -191,8 +191,8 @@ def test_nbody_and_mockstream_argument_errors(tmp_path):
         gen.run(prog, 1e5, output_every=2, Integrator="leapfrog", dt=1.0, n_steps=4)
     with pytest.raises(NotImplementedError, match="LeapfrogIntegrator"):
         gen.run(prog, 1e5, output_every=2, output_filename="x.h5", Integrator="leapfrog", dt=1.0, n_steps=4)
-    with pytest.raises(NotImplementedError, match="FP64"):
-        gen.run(prog, 1e5, output_every=2, output_filename="x.h5", Integrator_kwargs=dict(precision="fp32c"),
+    with pytest.raises(ValueError, match="precision"):
+        gen.run(prog, 1e5, output_every=2, output_filename="x.h5", Integrator_kwargs=dict(precision="fp16"),
                 dt=1.0, n_steps=4)
     with pytest.raises(ValueError, match="positive"):
         gen.run(prog, 1e5, output_every=0, output_filename="x.h5", dt=1.0, n_steps=4)

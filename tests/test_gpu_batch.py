@@ -117,3 +117,44 @@ def test_invalid_batch_arguments():
     scf = g.SCFPotential(m=1e11, r_s=1.0, Snlm=S, Tnlm=S * 0)
     with pytest.raises(TypeError):
         BatchIntegrator(scf, w0, np.ones(8, dtype=np.int64), np.ones(8), np.zeros(8, dtype=np.int32)).run()
+
+
+@pytest.mark.parametrize("chunk", [32, 64])
+def test_device_schedule_is_a_cost_ordered_chunking(chunk):
+    """gx_batch_schedule: every orbit exactly once; every chunk holds one
+    integrator; within each integrator the lists run from the most expensive
+    orbit down (to the 4.4 % bins); chunk heads of the merged order do not
+    increase in cost by more than a bin; the same chunk-head costs as the
+    exact torch order to within a bin."""
+    import torch
+
+    from gala_gb300.batch import COST, schedule
+
+    rng = np.random.default_rng(11)
+    n = 10_001
+    nsteps = torch.from_numpy(np.exp(rng.uniform(np.log(5), np.log(40_000), n)).astype(np.int64)).cuda()
+    method = torch.from_numpy(rng.integers(0, 2, n).astype(np.int32)).cuda()
+    b = BatchIntegrator(W.mw_composite(), W.mw_ics(n, seed=3), nsteps, torch.full((n,), 0.5, device="cuda"), method,
+                        config=dict(block=128, ctas_per_sm=2, chunk=chunk))
+    b._prepare(torch.cuda.current_stream().cuda_stream)
+    order = b.order.cpu().numpy()
+    assert order.size % chunk == 0
+    real = order[order >= 0]
+    assert np.array_equal(np.sort(real), np.arange(n))
+    ns, me = nsteps.cpu().numpy(), method.cpu().numpy()
+    cost = ns * np.where(me == 1, COST[1], COST[0])
+    bin_ratio = 2.0 ** (1 / 16)
+    heads = []
+    for c in order.reshape(-1, chunk):
+        ids = c[c >= 0]
+        if ids.size == 0:
+            continue
+        assert np.unique(me[ids]).size == 1
+        assert np.all(cost[ids][1:] <= cost[ids][:-1] * bin_ratio + 1)
+        heads.append(cost[ids[0]])
+    heads = np.array(heads, dtype=np.float64)
+    assert np.all(heads[1:] <= heads[:-1] * bin_ratio + 1)
+    ref = schedule(nsteps, method, chunk).cpu().numpy().reshape(-1, chunk)
+    ref_heads = np.sort(np.array([cost[c[0]] for c in ref if c[0] >= 0], dtype=np.float64))[::-1]
+    assert ref_heads.size == heads.size
+    np.testing.assert_allclose(heads, ref_heads, rtol=bin_ratio - 1, atol=1)

@@ -287,8 +287,7 @@ def cpu_uneven_run(pot, w0, nsteps, dt, method, target_s, steps, warmup, nthread
     work = float(np.sum(ns_s))
     return {
         "value": work / per, "unit": UNIT, "cores": nth, "kind": "port",
-        "sample": f"{ns} of the {n} orbits (seeded random subset, {work:.3g} orbit-steps), gala's Leapfrog/Ruth4 "
-                  f"loops restated in C, -Ofast, {nth} threads",
+        "sample": f"seeded {ns} of {n} orbits ({work:.3g} orbit-steps), gala's Leapfrog/Ruth4 in C, -Ofast",
         "seconds_per_step": per, "single_thread_value": probe_rate,
     }, idx, out
 
@@ -373,7 +372,7 @@ def run_uneven_batch(args, torch, stream, timed_steps, warmup, world=1, clocks=N
     if len(outs) == 2:
         err = np.linalg.norm(outs["fp32c"][:3] - outs["fp64"][:3], axis=0) / np.linalg.norm(outs["fp64"][:3], axis=0)
         res["position_error_vs_fp64"] = {"median": float(np.median(err)), "p99": float(np.percentile(err, 99)),
-                                         "max": float(np.max(err))}
+                                         "max": float(np.max(err)), "frac_le_1e-4": float(np.mean(err <= 1e-4))}
         res["speedup_fp32c_vs_fp64"] = res["fp32c"]["value"] / res["fp64"]["value"]
 
     if "fp32c" in precs:
@@ -1219,22 +1218,24 @@ def run_gx(args):
         "config": {
             "workload": head["workload"],
             "orbits_per_gpu": head["orbits"], "orbit_steps_per_gpu": head["orbit_steps"],
-            "form": "FP32 force + Kahan-compensated FP32 state, FP64 in/out and energy diagnostic",
+            "form": "FP32 force, Kahan-compensated FP32 state, FP64 in/out and energy",
             "plain_fp64_value": sig(f64.get("value")),
             "speedup_vs_plain_fp64": sig(head.get("speedup_fp32c_vs_fp64")),
             "dE_over_E_median": sig(f32["dE_over_E_median"], 3),
             "dE_over_E_p99": sig(f32["dE_over_E_p99"], 3),
             "position_error_vs_fp64_median": sig(pe.get("median"), 3),
+            "position_error_vs_fp64_p99": sig(pe.get("p99"), 3),
             "position_error_vs_fp64_max": sig(pe.get("max"), 3),
+            "orbits_within_1e-4": sig(pe.get("frac_le_1e-4"), 5),
             "launch": f32["config"],
             "l2": "flushed (256 MB write) between timed iterations",
         },
         "e2e": {k: (sig(v) if isinstance(v, float) else v) for k, v in head["e2e"].items()},
         "gpu_launches": 3 * args.steps,
         "roofline": {**{k: sig(v, 4) for k, v in f32["roofline"].items()},
-                     "kernel": "batch_fp32_kernel (CUDA events, eager launches)",
+                     "kernel": "batch_fp32_kernel, CUDA events",
                      "peak_source": "FP32 FMA-chain probe, same run",
-                     "work": "algorithmic flops per step: Leapfrog 102, Ruth4 396"},
+                     "work": "flops/step: Leapfrog 102, Ruth4 396"},
         "clocks": clocks.summary(),
         "wall_s_timed_region": sig(head.get("wall_s_timed_region")),
         "variants": variants,

@@ -96,6 +96,8 @@ SIGNATURES = {
     "gx_calibrate_fma": (C.c_int, [_I32, _I32, _I32, _I64, _P, _P]),
     "gx_selfcheck_fast64": (C.c_int, [_P, _I64, _P, _P]),
     "gx_batch_integrate_fp32": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P]),
+    "gx_batch_integrate_fp32_state": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _P, _I64, _I32, _I32, _I32, _P, _P, _P, _P,
+                                                _P]),
     "gx_batch_integrate_fp32_noalloc": (C.c_int, [_PP, _P, _I64, _P, _P, _P, _I32, _I32, _P, _P]),
     "gx_mlp_param_count": (C.c_int64, []),
     "gx_mlp_train_workspace_floats": (C.c_int64, [_I64]),

@@ -105,9 +105,16 @@ class BatchIntegrator:
     precision : "fp32c" (FP32 forces, compensated FP32 state; closed-form
         potentials) or "fp64" (gala's arithmetic in FP64, the plain form)
     config : dict with block, ctas_per_sm, chunk; None = autotuned/cached choice
+    checkpoint : keep the integrator state after every run in ``self.state``
+        ((12, N) float32 on the device; fp32c only)
+    state : a ``state`` of an earlier run to resume from (fp32c only): a run of
+        k steps with checkpoint=True, then one of n - k steps with
+        state=<its state> (and the same w0, dt, method), gives the bits of one
+        run of n steps
     """
 
-    def __init__(self, potential, w0, n_steps, dt, method, config=None, precision="fp32c"):
+    def __init__(self, potential, w0, n_steps, dt, method, config=None, precision="fp32c", checkpoint=False,
+                 state=None):
         import torch
 
         from ._device import as_device_f64, require_cuda
@@ -146,6 +153,14 @@ class BatchIntegrator:
         self.E1 = torch.empty(self.n, dtype=torch.float64, device=self.dev)
         self.counter = torch.zeros(1, dtype=torch.int32, device=self.dev)
         self.graph = None
+        if (checkpoint or state is not None) and precision != "fp32c":
+            raise NotImplementedError("integrator checkpoints are kept by the fp32c form")
+        self.state_in = None
+        if state is not None:
+            self.state_in = torch.as_tensor(state, dtype=torch.float32, device=self.dev).contiguous()
+            if self.state_in.shape != (12, self.n):
+                raise ValueError(f"state must have shape (12, {self.n}), got {tuple(self.state_in.shape)}")
+        self.state = torch.empty((12, self.n), dtype=torch.float32, device=self.dev) if checkpoint else None
 
     # ------------------------------------------------------------------ run
     def _prepare(self, stream_handle=None):
@@ -173,9 +188,14 @@ class BatchIntegrator:
         if getattr(self, "_order_chunk", None) != cfg["chunk"]:
             self._prepare(stream_handle)
         desc = self.potential.packed().for_device()
-        _abi.call(ENTRY[self.precision], desc, ptr(self.w0), self.n, ptr(self.n_steps), ptr(self.dt),
-                  ptr(self.method), ptr(self.order), self.order.numel(), cfg["chunk"], cfg["block"],
-                  cfg["ctas_per_sm"] * self.sms, ptr(self.counter), ptr(self.w_out), stream_handle)
+        common = (desc, ptr(self.w0), self.n, ptr(self.n_steps), ptr(self.dt), ptr(self.method), ptr(self.order),
+                  self.order.numel(), cfg["chunk"], cfg["block"], cfg["ctas_per_sm"] * self.sms, ptr(self.counter))
+        if self.state_in is not None or self.state is not None:
+            _abi.call("gx_batch_integrate_fp32_state", *common,
+                      ptr(self.state_in) if self.state_in is not None else None,
+                      ptr(self.state) if self.state is not None else None, ptr(self.w_out), stream_handle)
+        else:
+            _abi.call(ENTRY[self.precision], *common, ptr(self.w_out), stream_handle)
         return desc
 
     def _launch(self, stream_handle):

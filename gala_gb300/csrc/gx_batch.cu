@@ -32,6 +32,10 @@ struct BatchArgs {
     int32_t pad;
     float c[4], d[4];  // Ruth4 coefficients
     const int32_t *cancel;  // host cancel flag (mapped memory) or nullptr
+    // integrator state (12, n) float32: position hi, lo; velocity hi, lo (the
+    // half-step velocity for Leapfrog), read to resume and / or written at the end
+    const float *state_in;
+    float *state_out;
 };
 
 __device__ __forceinline__ void split(double x, float &hi, float &lo) {
@@ -39,27 +43,55 @@ __device__ __forceinline__ void split(double x, float &hi, float &lo) {
     lo = (float)(x - (double)hi);
 }
 
-template <typename S>
+// One orbit.  With STATE, the integrator state is read from A.state_in when
+// given (a resumed run: the Leapfrog half-step velocity is not formed again)
+// and written to A.state_out when given, so that a run of k steps followed by a
+// resumed run of n - k steps gives the bits of one run of n steps.
+template <typename S, bool STATE>
 __device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const BatchArgs &A, const double *w0,
                                                    int64_t n, int64_t i, int64_t nsteps, float h, int meth,
                                                    double *w_out) {
-    if (nsteps == 0) {
+    const bool resume = STATE && A.state_in != nullptr;
+    if (nsteps == 0 && !(STATE && (resume || A.state_out))) {
         for (int k = 0; k < 6; k++) w_out[k * n + i] = w0[k * n + i];
         return;
     }
     float xh[3], xl[3], vh[3], vl[3], g[3];
-    for (int k = 0; k < 3; k++) {
-        split(w0[k * n + i], xh[k], xl[k]);
-        split(w0[(3 + k) * n + i], vh[k], vl[k]);
+    if (resume) {
+        for (int k = 0; k < 3; k++) {
+            xh[k] = A.state_in[k * n + i];
+            xl[k] = A.state_in[(3 + k) * n + i];
+            vh[k] = A.state_in[(6 + k) * n + i];
+            vl[k] = A.state_in[(9 + k) * n + i];
+        }
+    } else {
+        for (int k = 0; k < 3; k++) {
+            split(w0[k * n + i], xh[k], xl[k]);
+            split(w0[(3 + k) * n + i], vh[k], vl[k]);
+        }
     }
     if (meth == 0) {
-        // c_init_velocity: v_{1/2} = v - g h / 2
-        potential_gradient_f<S>(pot, xh, g);
-        for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h * 0.5f);
+        // c_init_velocity: v_{1/2} = v - g h / 2 (a resumed run already holds v_{1/2})
+        if (!resume || nsteps == 0) potential_gradient_f<S>(pot, xh, g);
+        if (!resume)
+            for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h * 0.5f);
         for (int64_t j = 0; j < nsteps; j++) {
             for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], h, vl[k] * h));
             potential_gradient_f<S>(pot, xh, g);
             for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h);
+        }
+        if constexpr (STATE) {
+            if (A.state_out)
+                for (int k = 0; k < 3; k++) {
+                    A.state_out[k * n + i] = xh[k];
+                    A.state_out[(3 + k) * n + i] = xl[k];
+                    A.state_out[(6 + k) * n + i] = vh[k];
+                    A.state_out[(9 + k) * n + i] = vl[k];
+                }
+            if (nsteps == 0 && !resume) {  // no step taken: the initial conditions as given
+                for (int k = 0; k < 6; k++) w_out[k * n + i] = w0[k * n + i];
+                return;
+            }
         }
         // output velocity at the last step: v_{n+1/2} + g h / 2
         for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], g[k] * h * 0.5f);
@@ -81,6 +113,19 @@ __device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const Bat
                 for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], ch[s], vl[k] * ch[s]));
             }
         }
+        if constexpr (STATE) {
+            if (A.state_out)
+                for (int k = 0; k < 3; k++) {
+                    A.state_out[k * n + i] = xh[k];
+                    A.state_out[(3 + k) * n + i] = xl[k];
+                    A.state_out[(6 + k) * n + i] = vh[k];
+                    A.state_out[(9 + k) * n + i] = vl[k];
+                }
+            if (nsteps == 0 && !resume) {
+                for (int k = 0; k < 6; k++) w_out[k * n + i] = w0[k * n + i];
+                return;
+            }
+        }
     }
     for (int k = 0; k < 3; k++) {
         w_out[k * n + i] = (double)xh[k] + (double)xl[k];
@@ -88,7 +133,7 @@ __device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const Bat
     }
 }
 
-template <typename S>
+template <typename S, bool STATE>
 __global__ void __launch_bounds__(256) batch_fp32_kernel(const __grid_constant__ DevPotF pot, BatchArgs A,
                                                          const double *__restrict__ w0,
                                                          const int64_t *__restrict__ nsteps,
@@ -109,7 +154,7 @@ __global__ void __launch_bounds__(256) batch_fp32_kernel(const __grid_constant__
             const int32_t i = order[slot];
             // -1 pads the order; any other id outside [0, n) is skipped (and recorded in the debug build)
             if (i != -1 && GX_DBG_CHECK(i >= 0 && i < A.n, DBG_ORDER, i, A.n)) {
-                integrate_one_fp32<S>(pot, A, w0, A.n, i, nsteps[i], (float)dt[i], method[i], w_out);
+                integrate_one_fp32<S, STATE>(pot, A, w0, A.n, i, nsteps[i], (float)dt[i], method[i], w_out);
                 GX_DBG_DONE(i, nsteps[i]);
             }
         }
@@ -184,7 +229,15 @@ static void launch_batch_fp32(const DevPotF &dp, const BatchArgs &A, const doubl
         return true;
     };
     constexpr int H = GX_POT_HERNQUIST, MN = GX_POT_MIYAMOTONAGAI, NFW = GX_POT_SPHERICALNFW, P = GX_POT_PLUMMER;
-#define GX_LAUNCH(SIG) batch_fp32_kernel<SIG><<<grid, block, 0, st>>>(dp, A, w0, nsteps, dt, method, order, counter, w_out)
+#define GX_LAUNCH(SIG)                                                                                    \
+    do {                                                                                                  \
+        if (A.state_in || A.state_out)                                                                    \
+            batch_fp32_kernel<SIG, true><<<grid, block, 0, st>>>(dp, A, w0, nsteps, dt, method, order,     \
+                                                                 counter, w_out);                         \
+        else                                                                                              \
+            batch_fp32_kernel<SIG, false><<<grid, block, 0, st>>>(dp, A, w0, nsteps, dt, method, order,    \
+                                                                  counter, w_out);                        \
+    } while (0)
     using SigHHMN = PotSig<H, H, MN, NFW>;
     using SigMNHH = PotSig<MN, H, H, NFW>;
     using SigH = PotSig<H, -1, -1, -1>;
@@ -199,10 +252,10 @@ static void launch_batch_fp32(const DevPotF &dp, const BatchArgs &A, const doubl
 
 }  // namespace gx
 
-extern "C" int gx_batch_integrate_fp32(const gx_potential *pot, const double *w0, int64_t n,
-                                       const int64_t *n_steps, const double *dt, const int32_t *method,
-                                       const int32_t *order, int64_t n_slots, int32_t chunk, int32_t block,
-                                       int32_t grid, int32_t *queue_counter, double *w_out, void *stream) {
+static int batch_fp32_entry(const gx_potential *pot, const double *w0, int64_t n, const int64_t *n_steps,
+                            const double *dt, const int32_t *method, const int32_t *order, int64_t n_slots,
+                            int32_t chunk, int32_t block, int32_t grid, int32_t *queue_counter,
+                            const float *state_in, float *state_out, double *w_out, void *stream) {
     gx::DevPotF dp;
     int rc = gx::pack_potential_f32(pot, &dp);
     if (rc) return rc;
@@ -219,6 +272,8 @@ extern "C" int gx_batch_integrate_fp32(const gx_potential *pot, const double *w0
     A.chunk = chunk;
     A.pad = 0;
     A.cancel = gx::cancel_flag();
+    A.state_in = state_in;
+    A.state_out = state_out;
     const double two_13 = std::pow(2., 1. / 3.);
     const double c[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
                          (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};
@@ -231,6 +286,25 @@ extern "C" int gx_batch_integrate_fp32(const gx_potential *pot, const double *w0
     GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, sizeof(int32_t), st));
     gx::launch_batch_fp32(dp, A, w0, n_steps, dt, method, order, queue_counter, w_out, grid, block, st);
     return gx::check_launch("batch_fp32");
+}
+
+extern "C" int gx_batch_integrate_fp32(const gx_potential *pot, const double *w0, int64_t n,
+                                       const int64_t *n_steps, const double *dt, const int32_t *method,
+                                       const int32_t *order, int64_t n_slots, int32_t chunk, int32_t block,
+                                       int32_t grid, int32_t *queue_counter, double *w_out, void *stream) {
+    return batch_fp32_entry(pot, w0, n, n_steps, dt, method, order, n_slots, chunk, block, grid, queue_counter,
+                            nullptr, nullptr, w_out, stream);
+}
+
+extern "C" int gx_batch_integrate_fp32_state(const gx_potential *pot, const double *w0, int64_t n,
+                                             const int64_t *n_steps, const double *dt, const int32_t *method,
+                                             const int32_t *order, int64_t n_slots, int32_t chunk, int32_t block,
+                                             int32_t grid, int32_t *queue_counter, const float *state_in,
+                                             float *state_out, double *w_out, void *stream) {
+    GX_CHECK_ARG(state_in || state_out, "state_in and state_out are both NULL (use gx_batch_integrate_fp32)");
+    GX_CHECK_ARG(state_in != state_out, "state_in and state_out must not alias");
+    return batch_fp32_entry(pot, w0, n, n_steps, dt, method, order, n_slots, chunk, block, grid, queue_counter,
+                            state_in, state_out, w_out, stream);
 }
 
 // ===========================================================================
@@ -533,6 +607,8 @@ extern "C" int gx_batch_integrate_fp32_noalloc(const gx_potential *pot, const do
     A.chunk = gx::NA_CHUNK;
     A.pad = 0;
     A.cancel = gx::cancel_flag();
+    A.state_in = nullptr;
+    A.state_out = nullptr;
     const double two_13 = std::pow(2., 1. / 3.);
     const double c[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
                          (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};

@@ -54,29 +54,42 @@ struct AnimF32Args {
     const int32_t *cancel;     // host cancel flag (mapped memory) or nullptr
 };
 
-// Deterministic CTA sums of two FP32 partials, combined in FP64: each thread's
-// partials over its members in order, a warp butterfly, then the warps in order.
-__device__ __forceinline__ void cta_sum2_f(float pa, float pb, double &sa, double &sb, double *red) {
+// The step controller's decisions, made by thread 0 and read by every thread
+// after a barrier: the FP64 control (time, step size, error-norm combination,
+// accept / reject, stiffness) runs once per step on one thread -- on GB300 a
+// warp instruction of the FP64 pipe costs the same whether one lane or all are
+// active, so the CTA's other warps issue none.
+struct Ctl {
+    double h;
+    float hf;
+    int go;    // take the step
+    int acc;   // the step was accepted
+    int stop;  // the call ends after this step
+    int idid;
+};
+
+// Deterministic CTA sums of two FP32 partials: each thread's partials over its
+// members in order, an FP32 warp butterfly, then thread 0 adds the warps' sums
+// in order in FP64 (only thread 0 receives them).
+__device__ __forceinline__ void cta_sum2_f(float a, float b, double &sa, double &sb, float *redf) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    double a = pa, b = pb;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_xor_sync(0xffffffffu, a, o);
         b += __shfl_xor_sync(0xffffffffu, b, o);
     }
     if (lane == 0) {
-        red[wid] = a;
-        red[32 + wid] = b;
+        redf[wid] = a;
+        redf[32 + wid] = b;
     }
     __syncthreads();
-    double ta = 0., tb = 0.;
-    for (int w = 0; w < nw; w++) {
-        ta += red[w];
-        tb += red[32 + w];
-    }
-    __syncthreads();
-    sa = ta;
-    sb = tb;
+    sa = 0.;
+    sb = 0.;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < nw; w++) {
+            sa += (double)redf[w];
+            sb += (double)redf[32 + w];
+        }
 }
 
 // Fwrapper_direct_nbody (dop853.cpp:990-1006) in FP32 for member m, its
@@ -108,26 +121,27 @@ __device__ __forceinline__ void af_rhs(const DevPotF &pot, const BodyF *bc, int 
 #define F32(c) ((float)(dop::c))
 
 // One dop853_step call in the FP32 form on the first nmem members, from x to
-// xend with the initial step dt0, run by the whole CTA.  Adds {nfcn, nstep,
-// naccpt, nrejct} to ctr; returns gala's idid (the same on every thread).
+// xend with the initial step dt0, run by the whole CTA, the controller on
+// thread 0.  Adds {nfcn, nstep, naccpt, nrejct} to thread 0's ctr; returns
+// gala's idid (the same on every thread).
 template <typename S>
 __device__ __forceinline__ int wide_dop853_f32(const DevPotF &pot, const BodyF *bc, int nbody, int nmem, int64_t M,
-                                               float *const *Ar, double *red, double x, const double xend,
+                                               float *const *Ar, float *redf, Ctl &ctl, double x, const double xend,
                                                const double dt0, const float atol, const float rtol,
                                                const int64_t nmax_in, int64_t *ctr) {
     const int tid = threadIdx.x, nt = blockDim.x;
     __syncthreads();
     for (int m = tid; m < nmem; m += nt) af_rhs<S>(pot, bc, nbody, Ar[F_YH], Ar[F_YL], M, m, Ar[F_K1]);
-    __syncthreads();
 
+    // controller state (meaningful on thread 0)
     const double uround = 2.3E-16;
     const int64_t nmax = nmax_in ? nmax_in : 1000000;
     const double hmax = fabs(xend - x);
     const double posneg = (xend - x < 0.0) ? -1.0 : 1.0;
     const float safe = 0.9f, facc1 = 1.0f / 0.333f, facc2 = 1.0f / 6.0f;
-    double h = (double)(float)dt0;
-    float hlamb = 0.f;
-    int last = 0, reject = 0, iasti = 0, nonsti = 0, idid = 0;
+    double h = (double)(float)dt0, xold = x;
+    float hlamb = 0.f, hnew = 0.f, fac11 = 1.f;
+    int last = 0, reject = 0, nonsti = 0;
     int64_t nfcn = 2, nstep = 0, naccpt = 0, nrejct = 0;
 
 #define FSTAGE(dst, expr)                                                                            \
@@ -142,21 +156,28 @@ __device__ __forceinline__ int wide_dop853_f32(const DevPotF &pot, const BodyF *
 #define K(a) Ar[a][o]
 
     for (;;) {
-        if (nstep > nmax || !(fabsf((float)h) <= 3.0e38f)) {
-            idid = -2;  // a NaN step never recovers: gala's -2 after nmax rejections, at once
-            break;
+        if (tid == 0) {
+            ctl.go = 1;
+            if (nstep > nmax || !(fabsf((float)h) <= 3.0e38f)) {
+                ctl.idid = -2;  // a NaN step never recovers: gala's -2 after nmax rejections, at once
+                ctl.go = 0;
+            } else if (0.1 * fabs(h) <= fabs(x) * uround) {
+                ctl.idid = -3;
+                ctl.go = 0;
+            } else {
+                if ((x + 1.01 * h - xend) * posneg > 0.0) {
+                    h = xend - x;
+                    last = 1;
+                }
+                xold = x;
+                nstep++;
+                ctl.h = h;
+                ctl.hf = (float)h;
+            }
         }
-        if (0.1 * fabs(h) <= fabs(x) * uround) {
-            idid = -3;
-            break;
-        }
-        if ((x + 1.01 * h - xend) * posneg > 0.0) {
-            h = xend - x;
-            last = 1;
-        }
-        const double xold = x;
-        nstep++;
-        const float hf = (float)h;
+        __syncthreads();
+        if (!ctl.go) break;
+        const float hf = ctl.hf;
         // the twelve stages (dop853.cpp:368-414) with FP32 stage sums
         FSTAGE(F_K2, F32(a21) * K(F_K1));
         FSTAGE(F_K3, fmaf(F32(a32), K(F_K2), F32(a31) * K(F_K1)));
@@ -177,7 +198,6 @@ __device__ __forceinline__ int wide_dop853_f32(const DevPotF &pot, const BodyF *
         FSTAGE(F_K3, fmaf(F32(a1211), K(F_K2), fmaf(F32(a1210), K(F_K10), fmaf(F32(a129), K(F_K9),
                      fmaf(F32(a128), K(F_K8), fmaf(F32(a127), K(F_K7), fmaf(F32(a126), K(F_K6),
                      fmaf(F32(a125), K(F_K5), fmaf(F32(a124), K(F_K4), F32(a121) * K(F_K1))))))))));
-        nfcn += 11;
         // 8th-order solution (k4), new state (k5, k5l) and error terms (:416-444)
         float e1 = 0.f, e2 = 0.f;
         for (int m = tid; m < nmem; m += nt)
@@ -202,21 +222,22 @@ __device__ __forceinline__ int wide_dop853_f32(const DevPotF &pot, const BodyF *
                 K(F_K5L) = k5l;
             }
         double E1, E2;
-        cta_sum2_f(e1, e2, E1, E2, red);
-        // err = |h| E1 / sqrt(deno n), n = 6 nmem: accept iff h^2 E1^2 <= deno n
-        double deno = fma(0.01, E2, E1);
-        if (deno <= 0.0) deno = 1.0;
-        const double he = h * E1;
-        const bool acc = fma(he, he, -(double)(6 * nmem) * deno) <= 0.0;
-        const float ratio = (float)(he * he / ((double)(6 * nmem) * deno));
-        const float fac11 = ex2_approx32(lg2_approx(ratio) * 0.0625f);  // err^(1/8) = ratio^(1/16)
-        const float fac = fmaxf(facc2, fminf(facc1, fac11 / safe));
-        float hnew = hf * rcp_approx(fac);
-        if (acc) {
-            naccpt++;
-            nfcn++;
+        cta_sum2_f(e1, e2, E1, E2, redf);
+        if (tid == 0) {
+            nfcn += 11;
+            // err = |h| E1 / sqrt(deno n), n = 6 nmem: accept iff h^2 E1^2 <= deno n
+            double deno = fma(0.01, E2, E1);
+            if (deno <= 0.0) deno = 1.0;
+            const double he = h * E1;
+            ctl.acc = fma(he, he, -(double)(6 * nmem) * deno) <= 0.0;
+            const float ratio = (float)(he * he / ((double)(6 * nmem) * deno));
+            fac11 = ex2_approx32(lg2_approx(ratio) * 0.0625f);  // err^(1/8) = ratio^(1/16)
+            const float fac = fmaxf(facc2, fminf(facc1, fac11 / safe));
+            hnew = hf * rcp_approx(fac);
+        }
+        __syncthreads();
+        if (ctl.acc) {
             // FSAL: k4 = f(new state); the stiffness estimate over the whole step
-            __syncthreads();
             for (int m = tid; m < nmem; m += nt) af_rhs<S>(pot, bc, nbody, Ar[F_K5], Ar[F_K5L], M, m, Ar[F_K4]);
             __syncthreads();
             float tn = 0.f, td = 0.f;
@@ -229,16 +250,32 @@ __device__ __forceinline__ int wide_dop853_f32(const DevPotF &pot, const BodyF *
                     td = fmaf(d, d, td);
                 }
             double stnum, stden;
-            cta_sum2_f(tn, td, stnum, stden, red);
-            if (stden > 0.0) hlamb = hf * (float)sqrt(stnum / stden);
-            if (hlamb > 6.1f) {
-                nonsti = 0;
-                iasti++;
-                idid = -4;
-                break;
+            cta_sum2_f(tn, td, stnum, stden, redf);
+            if (tid == 0) {
+                naccpt++;
+                nfcn++;
+                if (stden > 0.0) hlamb = hf * (float)sqrt(stnum / stden);
+                ctl.stop = 0;
+                if (hlamb > 6.1f) {
+                    nonsti = 0;
+                    ctl.idid = -4;
+                    ctl.stop = 1;
+                } else {
+                    nonsti++;
+                    x = xold + h;
+                    if (last) {
+                        ctl.idid = 1;
+                        ctl.stop = 1;
+                    } else {
+                        if (fabsf(hnew) > (float)hmax) hnew = copysignf((float)hmax, hf);
+                        if (reject) hnew = copysignf(fminf(fabsf(hnew), fabsf(hf)), hf);
+                        reject = 0;
+                        h = (double)hnew;
+                    }
+                }
             }
-            nonsti++;
-            if (nonsti == 6) iasti = 0;
+            __syncthreads();
+            if (ctl.idid == -4 && ctl.stop) break;  // stiff: the state stays that of the last step
             for (int m = tid; m < nmem; m += nt)
                 for (int c = 0; c < 6; c++) {
                     const int64_t o = c * M + m;
@@ -246,38 +283,36 @@ __device__ __forceinline__ int wide_dop853_f32(const DevPotF &pot, const BodyF *
                     K(F_YH) = K(F_K5);
                     K(F_YL) = K(F_K5L);
                 }
+            if (ctl.stop) break;
             __syncthreads();
-            x = xold + h;
-            if (last) {
-                idid = 1;
-                break;
-            }
-            if (fabsf(hnew) > (float)hmax) hnew = copysignf((float)hmax, hf);
-            if (reject) hnew = copysignf(fminf(fabsf(hnew), fabsf(hf)), hf);
-            reject = 0;
-        } else {
+        } else if (tid == 0) {
             hnew = hf * rcp_approx(fminf(facc1, fac11 / safe));
             reject = 1;
             if (naccpt >= 1) nrejct++;
             last = 0;
+            h = (double)hnew;
         }
-        h = (double)hnew;
     }
 #undef K
 #undef FSTAGE
-    (void)iasti;
+    (void)nonsti;
     __syncthreads();
-    ctr[0] += nfcn;
-    ctr[1] += nstep;
-    ctr[2] += naccpt;
-    ctr[3] += nrejct;
+    const int idid = ctl.idid;
+    if (tid == 0) {
+        ctr[0] += nfcn;
+        ctr[1] += nstep;
+        ctr[2] += naccpt;
+        ctr[3] += nrejct;
+    }
+    __syncthreads();
     return idid;
 }
 
 template <typename S>
 __global__ void __launch_bounds__(AF_THREADS, 1)
 animate_f32_kernel(const __grid_constant__ DevPotF pot, const __grid_constant__ AnimF32Args A) {
-    __shared__ double red[64];
+    __shared__ float redf[64];
+    __shared__ Ctl ctl;
     __shared__ BodyF bc[AF_MAXNB];
     const int64_t s = blockIdx.x;
     if (s >= A.n_streams) return;
@@ -332,8 +367,8 @@ animate_f32_kernel(const __grid_constant__ DevPotF pot, const __grid_constant__ 
             while (j < A.n_output) snapshot(j++, 0);  // snapshots not reached: all NaN
             break;
         }
-        const int idid = wide_dop853_f32<S>(pot, bc, nbody, (int)(nbody + n), M, Ar, red, A.t[i - 1], A.t[i],
-                                            A.dt0, (float)A.atol, (float)A.rtol, A.nmax, ctr);
+        const int idid = wide_dop853_f32<S>(pot, bc, nbody, (int)(nbody + n), M, Ar, redf, ctl, A.t[i - 1],
+                                            A.t[i], A.dt0, (float)A.atol, (float)A.rtol, A.nmax, ctr);
         n = grow(n, i, bad);
         if (tid == 0) A.status[s * A.ntimes + i] = bad ? -1 : idid;
         if (i % A.output_every == 0 || i == A.ntimes - 1) snapshot(j++, nbody + n);

@@ -350,6 +350,25 @@ int gx_batch_integrate_fp32(const gx_potential* pot, const double* w0, int64_t n
                             int32_t block, int32_t grid, int32_t* queue_counter,
                             double* w_out, void* stream);
 
+/* The same with the integrator state in device memory, for checkpoints: a run
+ * of k steps that writes its state, then a run of n - k steps that resumes from
+ * it, gives the bits of one run of n steps (orbit by orbit).
+ *   state_in   DEVICE float[12][N] or NULL: position hi (3), lo (3), velocity
+ *              hi (3), lo (3) -- for Leapfrog the half-step velocity v_{1/2},
+ *              which the resumed run uses as is (no second c_init_velocity);
+ *              w0 then serves only orbits without state (unused here) and may
+ *              be the original initial conditions
+ *   state_out  DEVICE float[12][N] or NULL: the state after this run's steps
+ *              (before the output velocity is synchronised); not aliasing state_in
+ * At least one of them is given.  gala keeps no such state: a run started again
+ * from an Orbit's last (x, v) forms v_{1/2} again and takes a new rounding path. */
+int gx_batch_integrate_fp32_state(const gx_potential* pot, const double* w0, int64_t n,
+                                  const int64_t* n_steps, const double* dt, const int32_t* method,
+                                  const int32_t* order, int64_t n_slots, int32_t chunk,
+                                  int32_t block, int32_t grid, int32_t* queue_counter,
+                                  const float* state_in, float* state_out, double* w_out,
+                                  void* stream);
+
 /* The plain FP64 form of the same batched workload: identical arguments and
  * queue; per orbit, gala's Leapfrog / Ruth4 arithmetic in FP64 exactly as
  * gx_leapfrog_integrate_hamiltonian / gx_ruth4_integrate_hamiltonian compute it

@@ -158,3 +158,44 @@ def test_device_schedule_is_a_cost_ordered_chunking(chunk):
     ref_heads = np.sort(np.array([cost[c[0]] for c in ref if c[0] >= 0], dtype=np.float64))[::-1]
     assert ref_heads.size == heads.size
     np.testing.assert_allclose(heads, ref_heads, rtol=bin_ratio - 1, atol=1)
+
+
+def test_checkpoint_resume_is_bit_identical():
+    """A run of k steps that keeps its state, then runs resumed from it (through
+    host memory, as a checkpoint file would), give the bits of one run of n
+    steps, orbit by orbit -- for Leapfrog (whose state is the half-step
+    velocity) and Ruth4, with segments of zero steps among them."""
+    import torch
+
+    n = 3000
+    pot = W.mw_composite()
+    w0 = W.mw_ics(n, seed=91)
+    nsteps, dt, method = _workload(n, 92, 600)
+    k1 = nsteps // 3
+    k2 = (nsteps - k1) // 2
+    k1[:3], k2[:3] = 0, 0                  # first segments of zero steps
+    k1[3:6], k2[3:6] = nsteps[3:6], 0      # everything in the first segment
+    k3 = nsteps - k1 - k2
+    full = BatchIntegrator(pot, w0, nsteps, dt, method).run().clone()
+    a = BatchIntegrator(pot, w0, k1, dt, method, checkpoint=True)
+    a.run()
+    b = BatchIntegrator(pot, w0, k2, dt, method, state=a.state.cpu().numpy(), checkpoint=True)
+    b.run()
+    c = BatchIntegrator(pot, w0, k3, dt, method, state=b.state)
+    out = c.run()
+    torch.cuda.synchronize()
+    assert torch.equal(out, full)
+    # the energy diagnostic of the last segment refers to the original initial conditions
+    ref = BatchIntegrator(pot, w0, nsteps, dt, method)
+    ref.run()
+    assert torch.equal(c.energy_drift(), ref.energy_drift())
+
+
+def test_checkpoint_arguments():
+    pot = W.mw_composite()
+    w0 = W.mw_ics(64, seed=93)
+    nsteps, dt, method = _workload(64, 94, 100)
+    with pytest.raises(NotImplementedError):
+        BatchIntegrator(pot, w0, nsteps, dt, method, precision="fp64", checkpoint=True)
+    with pytest.raises(ValueError, match="shape"):
+        BatchIntegrator(pot, w0, nsteps, dt, method, state=np.zeros((12, 63), dtype=np.float32))

@@ -436,192 +436,6 @@ extern "C" int gx_fixed_fp32(const gx_potential *pot, int32_t method, const doub
 }
 
 // ===========================================================================
-// Allocation-free variant of the batched FP32 integrator.
-//
-// Some callers cannot allocate device memory: an application whose memory
-// manager owns the whole GPU (a framework's caching allocator, or a service
-// that reserves HBM up front) must not have a library call cudaMalloc behind
-// its back; a host in another language that only receives device pointers from
-// a different runtime has no allocator to call; and cudaMalloc / cudaFree can
-// synchronize the device, which a latency-critical asynchronous pipeline cannot
-// afford.  gx_batch_integrate_fp32_noalloc serves them: the caller passes only
-// inputs and outputs, and the work queue (its counter and the processing order,
-// which gx_batch_integrate_fp32 takes from the caller) lives in the file-scope
-// array below, sized for at most GX_NOALLOC_MAX_ORBITS orbits.  The array exists
-// on every GPU that loads this library until the process exits.
-//
-// Scheduling here is a counting sort on the device: orbits are bucketed by
-// integrator (Ruth4 first) and by log2 of their cost (longest first); within a
-// bucket the order comes from atomics, which changes only which warp runs an
-// orbit, never its arithmetic -- results are bit-identical to the caller-order
-// entry point.
-// ===========================================================================
-namespace gx {
-
-constexpr int NA_BINS_PER_METHOD = 64;
-constexpr int NA_BINS = 2 * NA_BINS_PER_METHOD;
-constexpr int NA_CHUNK = 32;
-// int32 layout: [0] queue counter | [64 .. 64+NA_BINS) histogram / offsets | order
-constexpr int64_t NA_HIST_OFF = 64;
-constexpr int64_t NA_ORDER_OFF = NA_HIST_OFF + NA_BINS + 64;
-constexpr int64_t NA_SLOTS = GX_NOALLOC_MAX_ORBITS + NA_CHUNK;
-constexpr int64_t NA_WORDS = NA_ORDER_OFF + NA_SLOTS;
-
-static __device__ __align__(256) int32_t g_noalloc_scratch[NA_WORDS];
-
-__device__ __forceinline__ int noalloc_bin(int64_t nsteps, int32_t method) {
-    const double cost = (double)nsteps * (method == 1 ? 3.0 : 1.0);
-    int b = (cost >= 1.0) ? (int)log2(cost) : 0;  // 0 .. 62 for any int64 count
-    b = b < NA_BINS_PER_METHOD - 1 ? b : NA_BINS_PER_METHOD - 1;
-    // bins ordered so that bin 0 is processed first: Ruth4, longest first
-    const int rank = (NA_BINS_PER_METHOD - 1 - b);
-    return method == 1 ? rank : NA_BINS_PER_METHOD + rank;
-}
-
-// clear counter and histogram, mark every order slot as padding
-__global__ void noalloc_clear(int32_t *s, int64_t slots) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < NA_ORDER_OFF) s[i] = 0;
-    if (i < slots) s[NA_ORDER_OFF + i] = -1;
-}
-
-__global__ void noalloc_histogram(int32_t *s, const int64_t *__restrict__ nsteps,
-                                  const int32_t *__restrict__ method, int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) atomicAdd(&s[NA_HIST_OFF + noalloc_bin(nsteps[i], method[i])], 1);
-}
-
-// exclusive prefix sum of the histogram in place (one thread; NA_BINS entries)
-__global__ void noalloc_scan(int32_t *s) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
-        int32_t acc = 0;
-        for (int b = 0; b < NA_BINS; b++) {
-            const int32_t c = s[NA_HIST_OFF + b];
-            s[NA_HIST_OFF + b] = acc;
-            acc += c;
-        }
-    }
-}
-
-__global__ void noalloc_scatter(int32_t *s, const int64_t *__restrict__ nsteps, const int32_t *__restrict__ method,
-                                int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        const int32_t pos = atomicAdd(&s[NA_HIST_OFF + noalloc_bin(nsteps[i], method[i])], 1);
-        s[NA_ORDER_OFF + pos] = (int32_t)i;
-    }
-}
-
-// Identity of the CUDA context current on this thread (cuCtxGetId through the
-// runtime's driver entry points, so the library links no driver library).
-typedef CUresult (*ctx_get_current_fn)(CUcontext *);
-typedef CUresult (*ctx_get_id_fn)(CUcontext, unsigned long long *);
-
-static int current_context_id(unsigned long long *id) {
-    static ctx_get_current_fn get_cur = nullptr;
-    static ctx_get_id_fn get_id = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        cudaDriverEntryPointQueryResult q;
-        void *fn = nullptr;
-        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            get_cur = reinterpret_cast<ctx_get_current_fn>(fn);
-        fn = nullptr;
-        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            get_id = reinterpret_cast<ctx_get_id_fn>(fn);
-    });
-    CUcontext ctx = nullptr;
-    if (!get_cur || !get_id || get_cur(&ctx) != CUDA_SUCCESS || ctx == nullptr || get_id(ctx, id) != CUDA_SUCCESS)
-        *id = 0;  // unknown: look the address up again
-    return GX_OK;
-}
-
-// Device address of g_noalloc_scratch in the current context.  It is looked up
-// with cudaGetSymbolAddress (that device current) on a device's first call and
-// again whenever the context has changed since (after cudaDeviceReset the
-// module is loaded again and the array may sit elsewhere).
-static int noalloc_scratch_address(int32_t **out) {
-    static std::mutex mu;
-    static int32_t *addr[64] = {nullptr};
-    static unsigned long long ctx_of[64] = {0};
-    int dev = 0;
-    GX_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) {
-        set_error("device ordinal %d out of range", dev);
-        return GX_ERR_INVALID_ARGUMENT;
-    }
-    std::lock_guard<std::mutex> lock(mu);
-    unsigned long long ctx = 0;
-    current_context_id(&ctx);
-    if (addr[dev] == nullptr || ctx == 0 || ctx != ctx_of[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) {
-            set_error("cudaGetSymbolAddress(g_noalloc_scratch) failed on device %d: %s", dev, cudaGetErrorString(e));
-            return GX_ERR_CUDA;
-        }
-        addr[dev] = static_cast<int32_t *>(p);
-        // the lookup makes the context current if it was not yet: record its id now
-        current_context_id(&ctx_of[dev]);
-    }
-    *out = addr[dev];
-    return GX_OK;
-}
-
-}  // namespace gx
-
-extern "C" int gx_batch_integrate_fp32_noalloc(const gx_potential *pot, const double *w0, int64_t n,
-                                               const int64_t *n_steps, const double *dt, const int32_t *method,
-                                               int32_t block, int32_t grid, double *w_out, void *stream) {
-    gx::DevPotF dp;
-    int rc = gx::pack_potential_f32(pot, &dp);
-    if (rc) return rc;
-    if (n < 0 || n > GX_NOALLOC_MAX_ORBITS) {
-        gx::set_error("gx_batch_integrate_fp32_noalloc: n = %lld is outside [0, %d]; its fixed work-queue "
-                      "scratch holds at most GX_NOALLOC_MAX_ORBITS orbits (use gx_batch_integrate_fp32 for more)",
-                      (long long)n, GX_NOALLOC_MAX_ORBITS);
-        return GX_ERR_CAPACITY;
-    }
-    if (n == 0) return GX_OK;
-    GX_CHECK_ARG(w0 && n_steps && dt && method && w_out, "NULL array");
-    GX_CHECK_ARG(block >= 32 && block <= 256 && block % 32 == 0, "block must be a multiple of 32 in [32, 256]");
-    GX_CHECK_ARG(grid >= 1, "grid must be >= 1");
-    int32_t *s = nullptr;
-    rc = gx::noalloc_scratch_address(&s);
-    if (rc) return rc;
-    const int64_t slots = ((n + gx::NA_CHUNK - 1) / gx::NA_CHUNK) * gx::NA_CHUNK;
-    cudaStream_t st = gx::as_stream(stream);
-    const int tb = 256;
-    const int64_t clear_n = slots > gx::NA_ORDER_OFF ? slots : gx::NA_ORDER_OFF;
-    gx::noalloc_clear<<<(unsigned)((clear_n + tb - 1) / tb), tb, 0, st>>>(s, slots);
-    gx::noalloc_histogram<<<(unsigned)((n + tb - 1) / tb), tb, 0, st>>>(s, n_steps, method, n);
-    gx::noalloc_scan<<<1, 32, 0, st>>>(s);
-    gx::noalloc_scatter<<<(unsigned)((n + tb - 1) / tb), tb, 0, st>>>(s, n_steps, method, n);
-    rc = gx::check_launch("noalloc schedule");
-    if (rc) return rc;
-    gx::BatchArgs A;
-    A.n = n;
-    A.slots = slots;
-    A.chunk = gx::NA_CHUNK;
-    A.pad = 0;
-    A.cancel = gx::cancel_flag();
-    A.state_in = nullptr;
-    A.state_out = nullptr;
-    const double two_13 = std::pow(2., 1. / 3.);
-    const double c[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
-                         (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};
-    const double d[4] = {0., 1. / (2. - two_13), -two_13 / (2. - two_13), 1. / (2. - two_13)};
-    for (int k = 0; k < 4; k++) {
-        A.c[k] = (float)c[k];
-        A.d[k] = (float)d[k];
-    }
-    gx::launch_batch_fp32(dp, A, w0, n_steps, dt, method, s + gx::NA_ORDER_OFF, s, w_out, grid, block, st);
-    return gx::check_launch("batch_fp32 (noalloc)");
-}
-
-// ===========================================================================
 // The processing order of a batch, built on the device without a host sync:
 // per integrator the orbits sorted by cost (n_steps x gradient evaluations per
 // step, 1 for Leapfrog and 3 for Ruth4) into 16 bins per octave -- a 4.4 %
@@ -720,6 +534,31 @@ __global__ void sched_merge(const int32_t *info, const int32_t *__restrict__ tmp
 
 }  // namespace gx
 
+namespace gx {
+
+// Build the order of n orbits (see above) into order[0 .. n_slots) with the
+// work words `work`; sizes checked by the caller.
+static int launch_schedule(const int64_t *n_steps, const int32_t *method, int64_t n, int32_t chunk, int32_t *order,
+                           int64_t n_slots, int64_t slots, int32_t *work, cudaStream_t st) {
+    int32_t *hist = work, *info = work + SB_HIST, *heads = info + SB_INFO;
+    int32_t *tmp = heads + slots / chunk;
+    GX_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int32_t) * (SB_HIST + SB_INFO), st));
+    GX_CUDA_TRY(cudaMemsetAsync(tmp, 0xff, sizeof(int32_t) * slots, st));    // -1: padding
+    GX_CUDA_TRY(cudaMemsetAsync(order, 0xff, sizeof(int32_t) * n_slots, st));
+    if (n == 0) return GX_OK;
+    const int tb = 256;
+    const unsigned gn = (unsigned)((n + tb - 1) / tb);
+    const int64_t max_chunks = slots / chunk;
+    sched_histogram<<<gn, tb, 0, st>>>(hist, n_steps, method, n);
+    sched_scan<<<1, SB_BINS, 0, st>>>(hist, info, chunk);
+    sched_scatter<<<gn, tb, 0, st>>>(hist, tmp, n_steps, method, n);
+    sched_heads<<<(unsigned)((max_chunks + tb - 1) / tb), tb, 0, st>>>(info, tmp, heads, n_steps, method, chunk);
+    sched_merge<<<(unsigned)((max_chunks * 32 + tb - 1) / tb), tb, 0, st>>>(info, tmp, heads, order, chunk);
+    return check_launch("batch_schedule");
+}
+
+}  // namespace gx
+
 extern "C" int64_t gx_batch_schedule_slots(int64_t n, int32_t chunk) {
     if (n < 0 || chunk < 1) return 0;
     return ((n + chunk - 1) / chunk + 1) * (int64_t)chunk;
@@ -740,20 +579,143 @@ extern "C" int gx_batch_schedule(const int64_t *n_steps, const int32_t *method, 
     GX_CHECK_ARG(work_words >= gx_batch_schedule_work_words(n, chunk), "work of %lld words, %lld needed",
                  (long long)work_words, (long long)gx_batch_schedule_work_words(n, chunk));
     GX_CHECK_ARG(order && work && (n == 0 || (n_steps && method)), "NULL array");
-    cudaStream_t st = gx::as_stream(stream);
-    int32_t *hist = work, *info = work + gx::SB_HIST, *heads = info + gx::SB_INFO;
-    int32_t *tmp = heads + slots / chunk;
-    GX_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int32_t) * (gx::SB_HIST + gx::SB_INFO), st));
-    GX_CUDA_TRY(cudaMemsetAsync(tmp, 0xff, sizeof(int32_t) * slots, st));    // -1: padding
-    GX_CUDA_TRY(cudaMemsetAsync(order, 0xff, sizeof(int32_t) * n_slots, st));
+    return gx::launch_schedule(n_steps, method, n, chunk, order, n_slots, slots, work, gx::as_stream(stream));
+}
+
+// ===========================================================================
+// Allocation-free variant of the batched FP32 integrator.
+//
+// Some callers cannot allocate device memory: an application whose memory
+// manager owns the whole GPU (a framework's caching allocator, or a service
+// that reserves HBM up front) must not have a library call cudaMalloc behind
+// its back; a host in another language that only receives device pointers from
+// a different runtime has no allocator to call; and cudaMalloc / cudaFree can
+// synchronize the device, which a latency-critical asynchronous pipeline cannot
+// afford.  gx_batch_integrate_fp32_noalloc serves them: the caller passes only
+// inputs and outputs, and the work queue (its counter and the processing order,
+// which gx_batch_integrate_fp32 takes from the caller) lives in the file-scope
+// array below, sized for at most GX_NOALLOC_MAX_ORBITS orbits.  The array exists
+// on every GPU that loads this library until the process exits.
+//
+// The processing order is built in the array as gx_batch_schedule builds it
+// (cost bins, chunk lists merged by head cost); the order within a bin comes
+// from atomics, which changes only which warp runs an orbit, never its
+// arithmetic -- results are bit-identical to the caller-order entry point.
+// ===========================================================================
+namespace gx {
+
+constexpr int NA_CHUNK = 32;
+constexpr int64_t NA_SLOTS = GX_NOALLOC_MAX_ORBITS + 2 * NA_CHUNK;   // >= gx_batch_schedule_slots(max, 32)
+constexpr int64_t NA_WORK = SB_HIST + SB_INFO + NA_SLOTS / NA_CHUNK + NA_SLOTS;
+// int32 layout: [0] queue counter | [64 .. 64 + NA_WORK) schedule work | order
+constexpr int64_t NA_WORK_OFF = 64;
+constexpr int64_t NA_ORDER_OFF = ((NA_WORK_OFF + NA_WORK + 63) / 64) * 64;
+constexpr int64_t NA_WORDS = NA_ORDER_OFF + NA_SLOTS;
+
+static __device__ __align__(256) int32_t g_noalloc_scratch[NA_WORDS];
+
+// Identity of the CUDA context current on this thread (cuCtxGetId through the
+// runtime's driver entry points, so the library links no driver library).
+typedef CUresult (*ctx_get_current_fn)(CUcontext *);
+typedef CUresult (*ctx_get_id_fn)(CUcontext, unsigned long long *);
+
+static int current_context_id(unsigned long long *id) {
+    static ctx_get_current_fn get_cur = nullptr;
+    static ctx_get_id_fn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<ctx_get_current_fn>(fn);
+        fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<ctx_get_id_fn>(fn);
+    });
+    CUcontext ctx = nullptr;
+    if (!get_cur || !get_id || get_cur(&ctx) != CUDA_SUCCESS || ctx == nullptr || get_id(ctx, id) != CUDA_SUCCESS)
+        *id = 0;  // unknown: look the address up again
+    return GX_OK;
+}
+
+// Device address of g_noalloc_scratch in the current context.  It is looked up
+// with cudaGetSymbolAddress (that device current) on a device's first call and
+// again whenever the context has changed since (after cudaDeviceReset the
+// module is loaded again and the array may sit elsewhere).
+static int noalloc_scratch_address(int32_t **out) {
+    static std::mutex mu;
+    static int32_t *addr[64] = {nullptr};
+    static unsigned long long ctx_of[64] = {0};
+    int dev = 0;
+    GX_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_error("device ordinal %d out of range", dev);
+        return GX_ERR_INVALID_ARGUMENT;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    unsigned long long ctx = 0;
+    current_context_id(&ctx);
+    if (addr[dev] == nullptr || ctx == 0 || ctx != ctx_of[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) {
+            set_error("cudaGetSymbolAddress(g_noalloc_scratch) failed on device %d: %s", dev, cudaGetErrorString(e));
+            return GX_ERR_CUDA;
+        }
+        addr[dev] = static_cast<int32_t *>(p);
+        // the lookup makes the context current if it was not yet: record its id now
+        current_context_id(&ctx_of[dev]);
+    }
+    *out = addr[dev];
+    return GX_OK;
+}
+
+}  // namespace gx
+
+extern "C" int gx_batch_integrate_fp32_noalloc(const gx_potential *pot, const double *w0, int64_t n,
+                                               const int64_t *n_steps, const double *dt, const int32_t *method,
+                                               int32_t block, int32_t grid, double *w_out, void *stream) {
+    gx::DevPotF dp;
+    int rc = gx::pack_potential_f32(pot, &dp);
+    if (rc) return rc;
+    if (n < 0 || n > GX_NOALLOC_MAX_ORBITS) {
+        gx::set_error("gx_batch_integrate_fp32_noalloc: n = %lld is outside [0, %d]; its fixed work-queue "
+                      "scratch holds at most GX_NOALLOC_MAX_ORBITS orbits (use gx_batch_integrate_fp32 for more)",
+                      (long long)n, GX_NOALLOC_MAX_ORBITS);
+        return GX_ERR_CAPACITY;
+    }
     if (n == 0) return GX_OK;
-    const int tb = 256;
-    const unsigned gn = (unsigned)((n + tb - 1) / tb);
-    const int64_t max_chunks = slots / chunk;
-    gx::sched_histogram<<<gn, tb, 0, st>>>(hist, n_steps, method, n);
-    gx::sched_scan<<<1, gx::SB_BINS, 0, st>>>(hist, info, chunk);
-    gx::sched_scatter<<<gn, tb, 0, st>>>(hist, tmp, n_steps, method, n);
-    gx::sched_heads<<<(unsigned)((max_chunks + tb - 1) / tb), tb, 0, st>>>(info, tmp, heads, n_steps, method, chunk);
-    gx::sched_merge<<<(unsigned)((max_chunks * 32 + tb - 1) / tb), tb, 0, st>>>(info, tmp, heads, order, chunk);
-    return gx::check_launch("batch_schedule");
+    GX_CHECK_ARG(w0 && n_steps && dt && method && w_out, "NULL array");
+    GX_CHECK_ARG(block >= 32 && block <= 256 && block % 32 == 0, "block must be a multiple of 32 in [32, 256]");
+    GX_CHECK_ARG(grid >= 1, "grid must be >= 1");
+    int32_t *s = nullptr;
+    rc = gx::noalloc_scratch_address(&s);
+    if (rc) return rc;
+    const int64_t slots = gx_batch_schedule_slots(n, gx::NA_CHUNK);
+    static_assert(gx::NA_SLOTS >= GX_NOALLOC_MAX_ORBITS + gx::NA_CHUNK, "order capacity");
+    cudaStream_t st = gx::as_stream(stream);
+    GX_CUDA_TRY(cudaMemsetAsync(s, 0, sizeof(int32_t), st));  // queue counter
+    rc = gx::launch_schedule(n_steps, method, n, gx::NA_CHUNK, s + gx::NA_ORDER_OFF, slots, slots,
+                             s + gx::NA_WORK_OFF, st);
+    if (rc) return rc;
+    gx::BatchArgs A;
+    A.n = n;
+    A.slots = slots;
+    A.chunk = gx::NA_CHUNK;
+    A.pad = 0;
+    A.cancel = gx::cancel_flag();
+    A.state_in = nullptr;
+    A.state_out = nullptr;
+    const double two_13 = std::pow(2., 1. / 3.);
+    const double c[4] = {1. / (2. * (2. - two_13)), (1. - two_13) / (2. * (2. - two_13)),
+                         (1. - two_13) / (2. * (2. - two_13)), 1. / (2. * (2. - two_13))};
+    const double d[4] = {0., 1. / (2. - two_13), -two_13 / (2. - two_13), 1. / (2. - two_13)};
+    for (int k = 0; k < 4; k++) {
+        A.c[k] = (float)c[k];
+        A.d[k] = (float)d[k];
+    }
+    gx::launch_batch_fp32(dp, A, w0, n_steps, dt, method, s + gx::NA_ORDER_OFF, s, w_out, grid, block, st);
+    return gx::check_launch("batch_fp32 (noalloc)");
 }

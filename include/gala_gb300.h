@@ -394,7 +394,7 @@ int gx_batch_integrate_fp64(const gx_potential* pot, const double* w0, int64_t n
  *   address up again.
  *   Every call on a device shares the one array: calls that overlap on the GPU
  *   (different streams, no ordering) race and must not be issued.
- * The library holds the array (about 1 MB) on every GPU it is loaded on until
+ * The library holds the array (about 2.1 MB) on every GPU it is loaded on until
  * the process exits. */
 #define GX_NOALLOC_MAX_ORBITS 262144
 int gx_batch_integrate_fp32_noalloc(const gx_potential* pot, const double* w0, int64_t n,

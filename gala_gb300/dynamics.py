@@ -217,6 +217,17 @@ def peak_to_peak_period(t, f, amplitude_threshold=1e-2):
     return np.mean([np.mean(np.diff(t[peaks])), np.mean(np.diff(t[troughs]))])
 
 
+def _frame_times(t, w):
+    """Times for a frame rotation of the rows w (..., 6): an orbit's time axis
+    is the first axis after the components (ntimes[, norbits])."""
+    if t is None:
+        raise ValueError("Time array must be provided if not passing an Orbit subclass.")
+    t = np.asarray(t, dtype=np.float64)
+    if t.ndim == 1 and w.ndim == 3 and t.shape[0] == w.shape[0]:
+        return t[:, None]  # (ntimes, norbits)
+    return t
+
+
 class PhaseSpacePosition:
     """Positions and velocities with gala's axis convention: (ndim, ...)."""
 
@@ -266,6 +277,35 @@ class PhaseSpacePosition:
 
     def kinetic_energy(self):
         return 0.5 * np.sum(self.vel ** 2, axis=0)
+
+    def to_frame(self, frame, current_frame=None, t=None):
+        """The same points in another frame (PhaseSpacePosition.to_frame,
+        src/gala/dynamics/core.py:384-428): static <-> ConstantRotatingFrame by
+        gala's rotation (transformations.py:96-191; `t` is required unless
+        this is an Orbit, whose times are used), static <-> static is the
+        identity.  Other pairs raise ValueError as in gala."""
+        from .hamiltonian import ConstantRotatingFrame, StaticFrame, rotate_frame
+
+        cur = self.frame if current_frame is None else current_frame
+        if cur is None:
+            raise ValueError(f"If no frame was specified when this {self.__class__.__name__} was initialized, you "
+                             "must pass the current frame in via the current_frame argument to transform to a new "
+                             "frame.")
+        if t is None:
+            t = getattr(self, "t", None)
+        w = np.moveaxis(self.w(), 0, -1)  # (..., 6)
+        if isinstance(cur, StaticFrame) and isinstance(frame, StaticFrame):
+            out = w
+        elif isinstance(cur, StaticFrame) and isinstance(frame, ConstantRotatingFrame):
+            out = rotate_frame(w, _frame_times(t, w), frame.Omega, to_rotating=True)
+        elif isinstance(cur, ConstantRotatingFrame) and isinstance(frame, StaticFrame):
+            out = rotate_frame(w, _frame_times(t, w), cur.Omega, to_rotating=False)
+        else:
+            raise ValueError(f"Unsupported frame transformation: {cur} to {frame}")
+        out = np.moveaxis(out, -1, 0)
+        if isinstance(self, Orbit):
+            return Orbit(pos=out[:3], vel=out[3:], t=self.t, frame=frame)
+        return PhaseSpacePosition(pos=out[:3], vel=out[3:], frame=frame)
 
     def angular_momentum(self):
         """L = x cross v, shape (3, ...) (PhaseSpacePosition.angular_momentum,

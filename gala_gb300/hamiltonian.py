@@ -87,6 +87,45 @@ class ConstantRotatingFrame(FrameBase):
         return list(self.Omega)
 
 
+def rotate_frame(w, t, Omega, to_rotating):
+    """Phase-space rows between a static frame and ConstantRotatingFrame(Omega),
+    gala's static_to_constantrotating / constantrotating_to_static
+    (src/gala/potential/frame/builtin/transformations.py:96-191): positions and
+    velocities (the canonical momenta of the rotating Hamiltonian) are both
+    turned about the axis -Omega/|Omega| by +|Omega| t (to the rotating frame)
+    or -|Omega| t (to the static one), by Rodrigues' formula.
+
+    w : (..., 6) numpy array or torch tensor; t : times broadcasting against
+    w[..., 0].  Returns the same kind as w."""
+    Omega = np.asarray(Omega, dtype=np.float64).reshape(3)
+    om = float(np.linalg.norm(Omega))
+    if om == 0.0:
+        return w
+    k = -Omega / om
+    sign = 1.0 if to_rotating else -1.0
+    try:
+        import torch
+    except ImportError:  # pragma: no cover
+        torch = None
+    if torch is not None and isinstance(w, torch.Tensor):
+        kt = torch.as_tensor(k, dtype=w.dtype, device=w.device)
+        th = sign * om * torch.as_tensor(t, dtype=w.dtype, device=w.device)[..., None]
+        c, sn = torch.cos(th), torch.sin(th)
+
+        def rot(x):
+            return c * x + sn * torch.cross(kt.expand_as(x), x, dim=-1) + (1 - c) * (x * kt).sum(-1, keepdim=True) * kt
+
+        return torch.cat([rot(w[..., :3]), rot(w[..., 3:])], dim=-1)
+    w = np.asarray(w, dtype=np.float64)
+    th = sign * om * np.asarray(t, dtype=np.float64)[..., None]
+    c, sn = np.cos(th), np.sin(th)
+
+    def rot(x):
+        return c * x + sn * np.cross(k, x) + (1 - c) * (x * k).sum(-1, keepdims=True) * k
+
+    return np.concatenate([rot(w[..., :3]), rot(w[..., 3:])], axis=-1)
+
+
 class Hamiltonian:
     """A potential in a reference frame (chamiltonian.pyx:40-77)."""
 

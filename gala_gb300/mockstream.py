@@ -40,7 +40,7 @@ import numpy as np
 
 from . import _abi, units
 from .dynamics import PhaseSpacePosition, _galactic, _h5_open, quantity_from_hdf5, quantity_to_hdf5
-from .hamiltonian import Hamiltonian, StaticFrame
+from .hamiltonian import Hamiltonian, StaticFrame, rotate_frame
 from .integrate import DOPRI853Integrator, LeapfrogIntegrator, get_integrator, parse_time_specification
 from .nbody import DirectNBody, bodies_to_device, integrate_systems, integrate_systems_leapfrog, pack_bodies
 from .potential import PotentialBase
@@ -156,12 +156,15 @@ class BaseStreamDF:
         raise NotImplementedError
 
     # -- sampling ---------------------------------------------------------------
-    def sample_device(self, potential, prog_w, prog_t, prog_m, counts, stream=None):
+    def sample_device(self, potential, prog_w, prog_t, prog_m, counts, stream=None, frame=None):
         """Release states for n_streams progenitor orbits on one time grid.
 
         prog_w : CUDA tensor (n_streams, ntimes, k >= 6): progenitor x, v first
         prog_t : (ntimes,) float64; prog_m : (n_streams, ntimes)
         counts : (ntimes,) particles per tail
+        frame  : the frame of prog_w and of the result; a rotating frame is
+                 sampled in the static frame, the orbit turned there at its times
+                 and every particle back at its release time (df.pyx:172-233)
         Returns (w (n_streams, n_rows, 6) CUDA tensor, release_time (n_rows,),
         lead_trail (n_rows,), offset (ntimes + 1,) int64).
         """
@@ -169,6 +172,10 @@ class BaseStreamDF:
 
         from ._device import as_device_f64, ptr, stream_handle
 
+        rotating = frame is not None and not isinstance(frame, StaticFrame)
+        if rotating:
+            td = torch.as_tensor(np.asarray(prog_t, dtype=np.float64), device=prog_w.device)
+            prog_w = rotate_frame(prog_w[..., :6], td[None, :], frame.Omega, to_rotating=False)
         ns, ntimes = int(prog_w.shape[0]), int(prog_w.shape[1])
         ntail = self._lead + self._trail
         counts = np.asarray(counts, dtype=np.int64)
@@ -190,6 +197,8 @@ class BaseStreamDF:
                   ptr(md), ptr(td), ptr(od), n_rows, self._KIND, ptr(dd), float(potential.G), self._lead,
                   self._trail, getattr(self, "_gala_modified", 0), ptr(out), stream_handle(stream))
         release_time = np.repeat(np.asarray(prog_t, dtype=np.float64), ntail * counts)
+        if rotating:
+            out = rotate_frame(out, torch.from_numpy(release_time).to(dev)[None, :], frame.Omega, to_rotating=True)
         lt = []
         for n in counts:
             if self._trail:
@@ -208,8 +217,6 @@ class BaseStreamDF:
             H = hamiltonian if isinstance(hamiltonian, Hamiltonian) else Hamiltonian(hamiltonian)
         else:
             raise ValueError("a Hamiltonian is needed to sample stream particles")
-        if not isinstance(H.frame, StaticFrame):
-            raise NotImplementedError("stream sampling is implemented for a static frame")
         x = np.asarray(prog_orbit.xyz, dtype=np.float64)
         v = np.asarray(prog_orbit.v_xyz, dtype=np.float64)
         t = np.asarray(prog_orbit.t, dtype=np.float64)
@@ -219,7 +226,8 @@ class BaseStreamDF:
         m = np.full(ntimes, float(m)) if m.shape == () else m
         counts = self.release_counts(ntimes, release_every, n_particles)
         dev = require_cuda()
-        w, rt, lt, _ = self.sample_device(H.potential, as_device_f64(prog_w, dev), t, m[None, :], counts)
+        w, rt, lt, _ = self.sample_device(H.potential, as_device_f64(prog_w, dev), t, m[None, :], counts,
+                                          frame=H.frame)
         w = w[0].cpu().numpy()
         return MockStream(pos=w[:, :3].T, vel=w[:, 3:].T, frame=H.frame, release_time=rt, lead_trail=lt)
 
@@ -444,8 +452,12 @@ class MockStreamGenerator:
         from ._device import ptr, require_cuda, stream_handle
 
         H = self.hamiltonian
-        if not isinstance(H.frame, StaticFrame):
-            raise NotImplementedError("mock streams are implemented for a static frame")
+        rotating = not isinstance(H.frame, StaticFrame)
+        if rotating and integrator == "leapfrog":
+            raise TypeError(f"Leapfrog integration is currently only supported for StaticFrame, not "
+                            f"{H.frame.__class__.__name__}")
+        if rotating and precision == "fp32c":
+            raise NotImplementedError("the FP32 DOP853 forms of mock streams run in a static frame")
         dev = require_cuda()
         S, nb = bodies.shape
         if nb > 31:
@@ -479,7 +491,7 @@ class MockStreamGenerator:
         # 2. release states from the progenitor orbit (body 0)
         prog_w = orbit.reshape(S, len(orbit_t), nb * 6)
         stream_w0, release_time, lead_trail, _ = self.df.sample_device(H.potential, prog_w, orbit_t, prog_m, counts,
-                                                                     stream=stream)
+                                                                     stream=stream, frame=H.frame)
         ntail = self.df.lead + self.df.trail
         if output_every is not None:
             return self._animate(bodies, nbody0, orbit_t, ntail * counts, stream_w0, release_time, lead_trail, dop,

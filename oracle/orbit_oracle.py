@@ -11,7 +11,9 @@ running backwards is reversed first, as gala does.  The spherical radius is
 astropy's (hypot(hypot(x, y), z), PhysicsSphericalRepresentation.from_cartesian),
 the cylindrical z is z.
 
-Also restated: ``guiding_radius`` (orbit.py:555-599 with core.py:943-967 and
+Also restated: the static <-> constant-rotating frame transformations
+(src/gala/potential/frame/builtin/transformations.py:10-56, 96-191) used by the
+mock-stream DFs in a rotating frame (df.pyx:172-233); ``guiding_radius`` (orbit.py:555-599 with core.py:943-967 and
 c_d_dr, cpotential.cpp:317-343) through scipy.optimize.root as gala calls it,
 and ``peak_to_peak_period`` (src/gala/dynamics/util.py:14-69) with argrelmax /
 argrelmin, behind ``Orbit.estimate_period`` (orbit.py:683-727).
@@ -139,3 +141,25 @@ def peak_to_peak_period(t, f, amplitude_threshold=1e-2):
     T_max = np.mean(t[max_ix[1:]] - t[max_ix[:-1]]) if len(max_ix) > 0 else np.nan
     T_min = np.mean(t[min_ix[1:]] - t[min_ix[:-1]]) if len(min_ix) > 0 else np.nan
     return np.mean([T_max, T_min])
+
+
+def rodrigues_axis_angle_rotate(x, vec, theta):
+    """Rodrigues' rotation of x (3, N) about the unit axis vec by theta (N,)
+    (transformations.py:10-56, the same expression)."""
+    x = np.array(x).T
+    vec = np.array(vec).T
+    theta = np.array(theta).T[..., None]
+    out = np.cos(theta) * x + np.sin(theta) * np.cross(vec, x) + (1 - np.cos(theta)) * (vec * x).sum(axis=-1)[
+        ..., None] * vec
+    return out.T
+
+
+def constantrotating_static(Omega, pos, vel, t, sign):
+    """_constantrotating_static_helper (transformations.py:96-153) for a 3D
+    Omega: sign +1 static -> rotating, -1 rotating -> static; pos, vel (3, N),
+    t (N,).  Returns (pos, vel)."""
+    Omega = -np.asarray(Omega, dtype=np.float64)
+    vec = Omega / np.linalg.norm(Omega)
+    theta = np.linalg.norm(Omega) * np.asarray(t, dtype=np.float64)
+    return (rodrigues_axis_angle_rotate(pos, vec, sign * theta),
+            rodrigues_axis_angle_rotate(vel, vec, sign * theta))

@@ -416,3 +416,31 @@ def test_debug_library_reports_its_build():
     out = (C.c_int64 * 9)()
     assert rel.gx_debug_read(C.cast(out, C.c_void_p), 0) == _abi.GX_ERR_UNSUPPORTED
     assert b"release library" in rel.gx_last_error_message()
+
+
+def test_rotating_frame_transform_matches_galas_rotation():
+    """rotate_frame / PhaseSpacePosition.to_frame against the oracle's restatement
+    of gala's static <-> constant-rotating transformations
+    (transformations.py:96-191), and the round trip."""
+    from gala_gb300.hamiltonian import rotate_frame
+    from oracle import orbit_oracle as OO
+
+    rng = np.random.default_rng(3)
+    Omega = np.array([0.01, -0.02, 0.03])
+    w = rng.normal(size=(40, 6))
+    t = rng.uniform(-500, 500, 40)
+    for to_rot, sign in ((True, 1.0), (False, -1.0)):
+        got = rotate_frame(w, t, Omega, to_rotating=to_rot)
+        px, pv = OO.constantrotating_static(Omega, w[:, :3].T, w[:, 3:].T, t, sign)
+        np.testing.assert_allclose(got, np.vstack([px, pv]).T, rtol=0, atol=1e-14)
+    fr = g.ConstantRotatingFrame(Omega=Omega)
+    o = g.Orbit(pos=w[:, :3].T.reshape(3, 8, 5), vel=w[:, 3:].T.reshape(3, 8, 5), t=np.linspace(0, 70, 8),
+                frame=g.StaticFrame())
+    back = o.to_frame(fr).to_frame(g.StaticFrame())
+    np.testing.assert_allclose(back.pos, o.pos, atol=1e-13)
+    np.testing.assert_allclose(back.vel, o.vel, atol=1e-13)
+    psp = g.PhaseSpacePosition(pos=[1.0, 2.0, 3.0], vel=[0.1, 0.2, 0.3], frame=g.StaticFrame())
+    with pytest.raises(ValueError, match="Time"):
+        psp.to_frame(fr)
+    with pytest.raises(ValueError, match="current_frame"):
+        g.PhaseSpacePosition(pos=[1.0, 2.0, 3.0], vel=[0.1, 0.2, 0.3]).to_frame(fr)

@@ -835,3 +835,61 @@ def test_fp32_animate_matches_fp64_animate():
     d = np.linalg.norm(s32[:, :3] - s64[:, :3], axis=1)[live] / np.linalg.norm(s64[:, :3], axis=1)[live]
     assert np.median(d) < 1e-5 and np.quantile(d, 0.99) < 1e-3, np.quantile(d, [0.5, 0.99, 1.0])
     np.testing.assert_array_equal(r32.stream_w.cpu().numpy(), np.transpose(s32[:, :, -1, 1:], (0, 2, 1)))
+
+
+@pytest.mark.parametrize("mode", ["releases", "animate"])
+def test_rotating_frame_stream_matches_oracle(oracle, mode):
+    """A mock stream in a ConstantRotatingFrame: the progenitor integrated in the
+    rotating frame, the DF sampled in the static frame (the orbit turned there at
+    its times, each particle back at its release time, df.pyx:172-233), the
+    release systems -- or the animate mode's growing system -- integrated in the
+    rotating frame; against the oracle's pipeline (gala's rotation restated,
+    oracle/orbit_oracle.py)."""
+    from oracle import orbit_oracle as OO
+
+    pot = W.mw_composite()
+    Omega = np.array([0.0, 0.0, 0.025])
+    frame = g.ConstantRotatingFrame(Omega=Omega)
+    w0 = W.mw_ics(1, seed=66)[:, 0]
+    prog_pot = g.PlummerPotential(m=2e5, b=0.01)
+    seed, n_steps = 9, 80
+    gen = MockStreamGenerator(FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(seed)),
+                              g.Hamiltonian(pot, frame=frame), progenitor_potential=prog_pot)
+    kw = dict(dt=1.0, n_steps=n_steps)
+    if mode == "animate":
+        res = gen.run_batch(w0[:, None], 2e5, progenitor_potentials=[prog_pot], output_every=8, **kw)
+        got = res.stream_w[0].cpu().numpy()
+        got_nb = res.nbody_w[0].cpu().numpy()
+    else:
+        stream, nbody = gen.run(g.PhaseSpacePosition.from_w(w0), 2e5, **kw)
+        got = np.vstack([stream.xyz, stream.v_xyz]).T
+        got_nb = np.vstack([nbody.xyz, nbody.v_xyz]).T
+
+    # the oracle's pipeline
+    t = g.parse_time_specification(**kw)
+    bodies = pack_bodies([prog_pot])
+    orb, res_o = oracle.nbody_dop853(pot, bodies, 1, w0.reshape(1, 6), t, frame=frame)
+    assert res_o == 1
+    prog = orb.reshape(len(t), 6)
+    px, pv = OO.constantrotating_static(Omega, prog[:, :3].T, prog[:, 3:].T, t, -1.0)
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(seed))
+    counts = df.release_counts(len(t))
+    offset = np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)
+    sw_static = oracle.fardal_sample(pot, np.vstack([px, pv]).T, np.full(len(t), 2e5), t, offset,
+                                     df._draws(int(offset[-1])), g.units.G)
+    rt = np.repeat(t, 2 * counts)
+    sx, sv = OO.constantrotating_static(Omega, sw_static[:, :3].T, sw_static[:, 3:].T, rt, 1.0)
+    sw0 = np.vstack([sx, sv]).T
+    if mode == "animate":
+        _, _, w_fin, status, _ = oracle.mockstream_animate(pot, bodies, orb[0].reshape(1, 6), t, sw0, 2 * counts,
+                                                           output_every=8, frame=frame)
+        assert np.all(status == 1)
+        ref, ref_nb = w_fin[1:], w_fin[:1]
+    else:
+        rel = np.nonzero(counts > 0)[0]
+        ref_nb, ref, status = oracle.mockstream_dop853(pot, bodies, orb[0].reshape(1, 6), t[rel], sw0, t[rel], t[-1],
+                                                       2 * counts[rel], frame=frame)
+        assert np.all(status[counts[rel] > 0] == 1)
+    assert got.shape == ref.shape
+    assert _scale_err(got, ref) < 1e-9
+    assert _scale_err(got_nb, ref_nb) < 1e-10

@@ -121,6 +121,9 @@ SIGNATURES = {
     "gx_mockstream_wide_scratch_bytes": (C.c_int64, [_I64, _I32]),
     "gx_mockstream_dop853_wide": (C.c_int, [_PP, _PF, _I64, _I32, _P, _P, _I64, _P, _P, _P, _I64, _D, _D, _D, _D,
                                             _I64, _P, _I64, _I32, _P, _I64, _P, _P, _P, _P, _P]),
+    "gx_nbody_wide_scratch_bytes": (C.c_int64, [_I64, _I32]),
+    "gx_nbody_dop853_wide": (C.c_int, [_PP, _PF, _I64, _I32, _I32, _P, _P, _P, _I64, _D, _D, _I64, _D, _I64, _I32,
+                                       _I64, _P, _I64, _P, _P, _P, _P]),
     "gx_mockstream_animate_snapshots": (C.c_int64, [_I64, _I64]),
     "gx_mockstream_dop853_animate": (C.c_int, [_PP, _PF, _I64, _I32, _P, _P, _I64, _P, _D, _P, _P, _I64, _I64, _D,
                                                _D, _I64, _P, _I64, _P, _P, _P, _P, _P]),

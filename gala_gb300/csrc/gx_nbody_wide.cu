@@ -29,9 +29,10 @@
 namespace gx {
 
 constexpr int WD_THREADS = 256;
-constexpr int WD_ARRAYS = 12;  // Y, K1..K10, YY1
+constexpr int WD_ARRAYS = 12;     // Y, K1..K10, YY1
+constexpr int WD_ARRAYS_D = 16;   // and the dense-output coefficients R5..R8 (DirectNBody)
 
-enum { A_Y = 0, A_K1, A_K2, A_K3, A_K4, A_K5, A_K6, A_K7, A_K8, A_K9, A_K10, A_YY1 };
+enum { A_Y = 0, A_K1, A_K2, A_K3, A_K4, A_K5, A_K6, A_K7, A_K8, A_K9, A_K10, A_YY1, A_R5, A_R6, A_R7, A_R8 };
 
 struct WideArgs {
     int32_t nbody;
@@ -100,28 +101,47 @@ __device__ __forceinline__ void wide_rhs(const DevPot &pot, const DevFrame &fr, 
     for (int c = 0; c < 6; c++) kout[c * M + m] = k.v[c];
 }
 
-// One dop853() call of dop853_step (dop853.pyx:27-75 -> dopcor, dopri/dop853.cpp:
-// 89-650) on the system of the first nmem members, from x to xend with the
-// initial step h and nstiff 1, run by the whole CTA.  The state is Ar[A_Y]
-// (SoA rows of stride M); the other arrays are the stage derivatives and the
-// stage argument.  Adds {nfcn, nstep, naccpt, nrejct} to ctr and returns gala's
-// idid; every thread returns the same value, after a barrier.
-template <bool SCF>
+// The dop853() arguments that differ between gala's two callers of these
+// systems: dop853_step (dop853.pyx:27-75; mock-stream releases and the animate
+// mode: uround 2.3e-16, nstiff 1, hmax = the interval) and dop853_helper
+// (dop853.pyx:90-193; DirectNBody: uround = eps, nstiff and dt_max as given).
+struct WideOpts {
+    double uround;
+    int64_t nstiff;  // after the front-end defaults (0 -> 1000, < 0 -> nmax + 10)
+    double hmax;     // > 0
+};
+
+// Dense output of a DirectNBody system onto the output grid: w_out (n_systems,
+// n_out, nparticles, 6) for every out_stride-th time of t (dop853.cpp:584-612).
+struct WideDense {
+    const double *t;
+    int64_t ntimes, out_stride, n_out, sys;
+    double *w_out;
+    int64_t out_idx, out_slot;  // the same on every thread
+};
+
+// One dop853() call on the system of the first nmem members, from x to xend
+// with the initial step h, run by the whole CTA.  The state is Ar[A_Y] (SoA rows
+// of stride M); the other arrays are the stage derivatives, the stage argument
+// and, with DENSE, the dense-output coefficients.  Adds {nfcn, nstep, naccpt,
+// nrejct} to ctr and returns gala's idid; every thread returns the same value,
+// after a barrier.
+template <bool SCF, bool DENSE = false>
 __device__ __forceinline__ int wide_dop853(const DevPot &pot, const DevFrame &fr, const gx_body *__restrict__ bod,
                                            int nbody, int nmem, int64_t M, double *const *Ar, double *red, double x,
                                            const double xend, double h, const double atoli, const double rtoli,
-                                           const int64_t nmax_in, int64_t *ctr) {
+                                           const int64_t nmax_in, int64_t *ctr, const WideOpts &opt,
+                                           WideDense *dn = nullptr) {
     using namespace dop;
     const int tid = threadIdx.x, nt = blockDim.x;
     __syncthreads();
     for (int m = tid; m < nmem; m += nt) wide_rhs<SCF>(pot, fr, bod, nbody, Ar[A_Y], M, m, Ar[A_K1]);
     __syncthreads();
 
-    // dop853_step's dop853() arguments (dop853.pyx:46-72) and front-end defaults
-    const double uround = 2.3E-16;
+    const double uround = opt.uround;
     const int64_t nmax = nmax_in ? nmax_in : 1000000;
-    const int64_t nstiff = 1;
-    const double hmax = fabs(xend - x);
+    const int64_t nstiff = opt.nstiff;
+    const double hmax = opt.hmax;
     const double posneg = (xend - x < 0.0) ? -1.0 : 1.0;
     const double safe = 0.9, facc1 = 1.0 / 0.333, facc2 = 1.0 / 6.0;
     int last = 0, reject = 0, iasti = 0, nonsti = 0, idid = 0;
@@ -228,6 +248,67 @@ __device__ __forceinline__ int wide_dop853(const DevPot &pot, const DevFrame &fr
                 nonsti++;
                 if (nonsti == 6) iasti = 0;
             }
+            if constexpr (DENSE) {
+                // dense output (dop853.cpp:492-612) for a step that holds an output
+                // time (the trajectory does not depend on it): the coefficients
+                // from the stages, three more stages, then contd8 at each time
+                const double x0 = x, x1 = x + h;
+                auto inside = [&](double to) { return (x0 <= to && to <= x1) || (x1 <= to && to <= x0); };
+                if (dn->out_idx < dn->ntimes && inside(dn->t[dn->out_idx])) {
+                    for (int m = tid; m < nmem; m += nt)
+                        for (int c = 0; c < 6; c++) {
+                            const int64_t o = c * M + m;
+                            K(A_R5) = d41 * K(A_K1) + d46 * K(A_K6) + d47 * K(A_K7) + d48 * K(A_K8) + d49 * K(A_K9) +
+                                      d410 * K(A_K10) + d411 * K(A_K2) + d412 * K(A_K3);
+                            K(A_R6) = d51 * K(A_K1) + d56 * K(A_K6) + d57 * K(A_K7) + d58 * K(A_K8) + d59 * K(A_K9) +
+                                      d510 * K(A_K10) + d511 * K(A_K2) + d512 * K(A_K3);
+                            K(A_R7) = d61 * K(A_K1) + d66 * K(A_K6) + d67 * K(A_K7) + d68 * K(A_K8) + d69 * K(A_K9) +
+                                      d610 * K(A_K10) + d611 * K(A_K2) + d612 * K(A_K3);
+                            K(A_R8) = d71 * K(A_K1) + d76 * K(A_K6) + d77 * K(A_K7) + d78 * K(A_K8) + d79 * K(A_K9) +
+                                      d710 * K(A_K10) + d711 * K(A_K2) + d712 * K(A_K3);
+                        }
+                    __syncthreads();
+                    WSTAGE(A_K10, fma(h, fma(a1413, K(A_K4), fma(a1412, K(A_K3), fma(a1411, K(A_K2),
+                                  fma(a1410, K(A_K10), fma(a149, K(A_K9), fma(a148, K(A_K8), fma(a147, K(A_K7),
+                                  a141 * K(A_K1)))))))), K(A_Y)));
+                    WSTAGE(A_K2, fma(h, fma(a1514, K(A_K10), fma(a1513, K(A_K4), fma(a1512, K(A_K3),
+                                 fma(a1511, K(A_K2), fma(a158, K(A_K8), fma(a157, K(A_K7), fma(a156, K(A_K6),
+                                 a151 * K(A_K1)))))))), K(A_Y)));
+                    WSTAGE(A_K3, fma(h, fma(a1615, K(A_K2), fma(a1614, K(A_K10), fma(a1613, K(A_K4),
+                                 fma(a169, K(A_K9), fma(a168, K(A_K8), fma(a167, K(A_K7), fma(a166, K(A_K6),
+                                 a161 * K(A_K1)))))))), K(A_Y)));
+                    nfcn += 3;
+                    int64_t oi = dn->out_idx, os = dn->out_slot;
+                    while (oi < dn->ntimes && inside(dn->t[oi])) {
+                        if (oi % dn->out_stride == 0) {
+                            const double s_ = (dn->t[oi] - x0) / h, s1 = 1.0 - s_;
+                            for (int m = tid; m < nmem; m += nt) {
+                                double *w = dn->w_out + ((dn->sys * dn->n_out + os) * (int64_t)M + m) * 6;
+                                for (int c = 0; c < 6; c++) {
+                                    const int64_t o = c * M + m;
+                                    const double r1 = K(A_Y), ydiff = K(A_K5) - K(A_Y);
+                                    const double bspl = h * K(A_K1) - ydiff;
+                                    const double r4 = ydiff - h * K(A_K4) - bspl;
+                                    const double r5 = h * (K(A_R5) + d413 * K(A_K4) + d414 * K(A_K10) +
+                                                           d415 * K(A_K2) + d416 * K(A_K3));
+                                    const double r6 = h * (K(A_R6) + d513 * K(A_K4) + d514 * K(A_K10) +
+                                                           d515 * K(A_K2) + d516 * K(A_K3));
+                                    const double r7 = h * (K(A_R7) + d613 * K(A_K4) + d614 * K(A_K10) +
+                                                           d615 * K(A_K2) + d616 * K(A_K3));
+                                    const double r8 = h * (K(A_R8) + d713 * K(A_K4) + d714 * K(A_K10) +
+                                                           d715 * K(A_K2) + d716 * K(A_K3));
+                                    w[c] = r1 + s_ * (ydiff + s1 * (bspl + s_ * (r4 + s1 * (r5 + s_ * (r6 +
+                                                 s1 * (r7 + s_ * r8))))));
+                                }
+                            }
+                            os++;
+                        }
+                        oi++;
+                    }
+                    dn->out_idx = oi;
+                    dn->out_slot = os;
+                }
+            }
             for (int m = tid; m < nmem; m += nt)
                 for (int c = 0; c < 6; c++) {
                     const int64_t o = c * M + m;
@@ -302,8 +383,9 @@ nbody_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ De
         for (int c = 0; c < 6; c++) Ar[A_Y][c * M + m] = src[c];
     }
     int64_t ctr[4] = {0, 0, 0, 0};
+    const WideOpts opt = {2.3E-16, 1, fabs(A.t_final - A.release_t[si])};  // dop853_step (dop853.pyx:46-72)
     const int idid = wide_dop853<SCF>(pot, fr, bod, nbody, nmem, M, Ar, red, A.release_t[si], A.t_final, A.dt0,
-                                      A.atol, A.rtol, A.nmax, ctr);
+                                      A.atol, A.rtol, A.nmax, ctr, opt);
     for (int m = tid; m < nmem; m += nt) {
         double *dst = nullptr;
         if (m >= nbody) dst = A.stream_w_out + (ss * A.n_particles + o0 + (m - nbody)) * 6;
@@ -393,8 +475,9 @@ animate_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
             while (j < A.n_output) snapshot(j++, 0);  // snapshots not reached: all NaN
             break;
         }
+        const WideOpts opt = {2.3E-16, 1, fabs(A.t[i] - A.t[i - 1])};  // dop853_step (dop853.pyx:46-72)
         const int idid = wide_dop853<SCF>(pot, fr, bod, nbody, (int)(nbody + n), M, Ar, red, A.t[i - 1], A.t[i],
-                                          A.dt0, A.atol, A.rtol, A.nmax, ctr);
+                                          A.dt0, A.atol, A.rtol, A.nmax, ctr, opt);
         n = grow(n, i, bad);
         if (tid == 0) A.status[s * A.ntimes + i] = bad ? -1 : idid;
         if (i % A.output_every == 0 || i == A.ntimes - 1) snapshot(j++, nbody + n);
@@ -405,6 +488,66 @@ animate_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ 
         for (int c = 0; c < 6; c++) A.w_out[(s * M + m) * 6 + c] = Ar[A_Y][c * M + m];
     if (tid == 0 && A.stats)
         for (int q = 0; q < 4; q++) A.stats[4 * s + q] = ctr[q];
+}
+
+// DirectNBody systems of any size (direct_nbody_dop853, nbody.pyx:30-115 ->
+// dop853_helper, dop853.pyx:90-193): one CTA per system, gala's dop853_helper
+// arguments, dense output onto the time grid when save_all.
+struct NbWideArgs {
+    int32_t nparticles, nbody, save_all;
+    int64_t n_systems, ntimes, out_stride, n_out;
+    const gx_body *bodies;   // (n_systems, max(nbody, 1))
+    const double *w0;        // (n_systems, nparticles, 6)
+    const double *t;         // (ntimes)
+    double atol, rtol, dt_max;
+    int64_t nmax, nstiff;
+    double *scratch;         // n_systems x WD_ARRAYS_D x 6 x nparticles doubles
+    double *w_out;           // (n_systems, n_out, nparticles, 6) or (n_systems, nparticles, 6)
+    int32_t *status;
+    int64_t *stats;
+    const int32_t *cancel;
+};
+
+template <bool SCF, bool DENSE>
+__global__ void __launch_bounds__(WD_THREADS)
+nbody_system_wide_kernel(const __grid_constant__ DevPot pot, const __grid_constant__ DevFrame fr,
+                         const __grid_constant__ NbWideArgs A) {
+    __shared__ double red[64];
+    const int64_t sys = blockIdx.x;
+    if (sys >= A.n_systems) return;
+    // a CTA that starts after cancellation integrates nothing (one reader, CTA-uniform)
+    if (__syncthreads_or(threadIdx.x == 0 && cancel_requested(A.cancel))) return;
+    const int64_t M = A.nparticles;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    double *base = A.scratch + sys * (int64_t)WD_ARRAYS_D * 6 * M;
+    double *Ar[WD_ARRAYS_D];
+#pragma unroll
+    for (int a = 0; a < WD_ARRAYS_D; a++) Ar[a] = base + (int64_t)a * 6 * M;
+    for (int m = tid; m < M; m += nt)
+#pragma unroll
+        for (int c = 0; c < 6; c++) Ar[A_Y][c * M + m] = A.w0[(sys * M + m) * 6 + c];
+    // dop853_helper's dop853() arguments (dop853.pyx:157-182) and front-end defaults
+    const double x0 = A.t[0], xend = A.t[A.ntimes - 1];
+    const int64_t nmax = A.nmax ? A.nmax : 1000000;
+    WideOpts opt;
+    opt.uround = 2.220446049250313e-16;  // np.finfo(float).eps
+    opt.nstiff = A.nstiff == 0 ? 1000 : (A.nstiff < 0 ? nmax + 10 : A.nstiff);
+    opt.hmax = fabs(A.dt_max == 0.0 ? xend - x0 : A.dt_max);
+    WideDense dn = {A.t, A.ntimes, A.out_stride, A.n_out, sys, A.w_out, 0, 0};
+    int64_t ctr[4] = {0, 0, 0, 0};
+    const gx_body *bod = A.bodies + sys * (A.nbody > 0 ? A.nbody : 1);
+    const int idid = wide_dop853<SCF, DENSE>(pot, fr, bod, A.nbody, (int)M, M, Ar, red, x0, xend, A.t[1] - A.t[0],
+                                             A.atol, A.rtol, A.nmax, ctr, opt, &dn);
+    if constexpr (!DENSE) {
+        for (int m = tid; m < M; m += nt)
+#pragma unroll
+            for (int c = 0; c < 6; c++) A.w_out[(sys * M + m) * 6 + c] = Ar[A_Y][c * M + m];
+    }
+    if (tid == 0) {
+        A.status[sys] = idid;
+        if (A.stats)
+            for (int q = 0; q < 4; q++) A.stats[4 * sys + q] = ctr[q];
+    }
 }
 
 }  // namespace gx
@@ -538,4 +681,66 @@ extern "C" int gx_mockstream_dop853_animate(const gx_potential *pot, const gx_fr
     else
         gx::animate_wide_kernel<false><<<(unsigned)n_streams, gx::WD_THREADS, 0, st>>>(dp, df, A);
     return gx::check_launch("mockstream_dop853_animate");
+}
+
+extern "C" int64_t gx_nbody_wide_scratch_bytes(int64_t n_systems, int32_t nparticles) {
+    if (n_systems <= 0 || nparticles <= 0) return 0;
+    return n_systems * (int64_t)gx::WD_ARRAYS_D * 6 * (int64_t)nparticles * (int64_t)sizeof(double);
+}
+
+extern "C" int gx_nbody_dop853_wide(const gx_potential *pot, const gx_frame *frame, int64_t n_systems,
+                                    int32_t nparticles, int32_t nbody, const gx_body *bodies, const double *w0,
+                                    const double *t, int64_t ntimes, double atol, double rtol, int64_t nmax,
+                                    double dt_max, int64_t nstiff, int32_t save_all, int64_t out_stride,
+                                    double *scratch, int64_t scratch_bytes, double *w_out, int32_t *status,
+                                    int64_t *stats, void *stream) {
+    gx::DevPot dp;
+    gx::DevFrame df;
+    int rc = gx::pack_potential(pot, &dp);
+    if (rc) return rc;
+    rc = gx::pack_frame(frame, &df);
+    if (rc) return rc;
+    GX_CHECK_ARG(n_systems >= 0 && nparticles >= 1 && nbody >= 0 && nbody <= nparticles, "bad size");
+    GX_CHECK_ARG(ntimes >= 2, "ntimes must be >= 2 (got %lld)", (long long)ntimes);
+    GX_CHECK_ARG(out_stride >= 1, "out_stride must be >= 1");
+    GX_CHECK_ARG(nmax >= 0, "nmax must be >= 0 (0 = gala's default 1e6)");
+    GX_CHECK_ARG(atol >= 0 && rtol >= 0, "tolerances must be non-negative");
+    if (n_systems == 0) return GX_OK;
+    GX_CHECK_ARG(bodies && w0 && t && scratch && w_out && status, "NULL array");
+    GX_CHECK_ARG(n_systems <= (int64_t)INT32_MAX, "too many systems");
+    const int64_t need = gx_nbody_wide_scratch_bytes(n_systems, nparticles);
+    GX_CHECK_ARG(scratch_bytes >= need, "scratch of %lld bytes, %lld needed", (long long)scratch_bytes,
+                 (long long)need);
+    gx::NbWideArgs A;
+    memset(&A, 0, sizeof(A));
+    A.nparticles = nparticles;
+    A.nbody = nbody;
+    A.save_all = save_all ? 1 : 0;
+    A.n_systems = n_systems;
+    A.ntimes = ntimes;
+    A.out_stride = out_stride;
+    A.n_out = (ntimes - 1) / out_stride + 1;
+    A.bodies = bodies;
+    A.w0 = w0;
+    A.t = t;
+    A.atol = atol;
+    A.rtol = rtol;
+    A.dt_max = dt_max;
+    A.nmax = nmax;
+    A.nstiff = nstiff;
+    A.scratch = scratch;
+    A.w_out = w_out;
+    A.status = status;
+    A.stats = stats;
+    A.cancel = gx::cancel_flag();
+    cudaStream_t st = gx::as_stream(stream);
+    const unsigned grid = (unsigned)n_systems;
+    if (dp.has_scf) {
+        if (save_all) gx::nbody_system_wide_kernel<true, true><<<grid, gx::WD_THREADS, 0, st>>>(dp, df, A);
+        else gx::nbody_system_wide_kernel<true, false><<<grid, gx::WD_THREADS, 0, st>>>(dp, df, A);
+    } else {
+        if (save_all) gx::nbody_system_wide_kernel<false, true><<<grid, gx::WD_THREADS, 0, st>>>(dp, df, A);
+        else gx::nbody_system_wide_kernel<false, false><<<grid, gx::WD_THREADS, 0, st>>>(dp, df, A);
+    }
+    return gx::check_launch("nbody_dop853_wide");
 }

@@ -460,8 +460,6 @@ class MockStreamGenerator:
             raise NotImplementedError("the FP32 DOP853 forms of mock streams run in a static frame")
         dev = require_cuda()
         S, nb = bodies.shape
-        if nb > 31:
-            raise NotImplementedError("at most 31 massive bodies per stream on the GPU")
 
         def check(status, what):
             res = status.cpu().numpy().ravel()
@@ -517,9 +515,11 @@ class MockStreamGenerator:
             check(st, "nbody")
         # releases of more than 32 - nb particles are systems wider than a warp:
         # the 32-lane kernel marks them (-1) and the CTA-per-system kernel then
-        # integrates each as the one system gala makes of it
-        wide_rel = np.nonzero(nb + nstream > 32)[0]
-        max_group = min(max_per, 32 - nb)
+        # integrates each as the one system gala makes of it (every release, when
+        # the bodies alone fill a warp); releases of no particle are skipped, as
+        # gala skips them
+        wide_rel = np.nonzero((nb + nstream > 32) & (nstream > 0))[0]
+        max_group = max(0, min(max_per, 32 - nb))
         n_rel = len(time)
         stream_out = torch.empty((S, n_rows, 6), dtype=torch.float64, device=dev)
         nbody_out = torch.empty((S, nb, 6), dtype=torch.float64, device=dev)
@@ -543,10 +543,11 @@ class MockStreamGenerator:
                       ptr(stats) if stats is not None else None, ptr(counter), stream_handle(stream))
             check(status, "stream")
             return MockStreamBatch(stream_out, nbody_out, release_time, lead_trail, status, stats, H.frame, orbit_t)
-        _abi.call("gx_mockstream_dop853", H.potential.packed().for_device(), H._frame_ref(), S, nb, ptr(bd),
-                  ptr(nbody_w), n_rel, ptr(td), ptr(od), max_group, ptr(stream_w0), n_rows, float(orbit_t[-1]),
-                  dt0, dop["atol"], dop["rtol"], dop["nmax"], ptr(stream_out), ptr(nbody_out),
-                  ptr(status), ptr(stats) if stats is not None else None, ptr(counter), stream_handle(stream))
+        if nb < 32:
+            _abi.call("gx_mockstream_dop853", H.potential.packed().for_device(), H._frame_ref(), S, nb, ptr(bd),
+                      ptr(nbody_w), n_rel, ptr(td), ptr(od), max_group, ptr(stream_w0), n_rows, float(orbit_t[-1]),
+                      dt0, dop["atol"], dop["rtol"], dop["nmax"], ptr(stream_out), ptr(nbody_out),
+                      ptr(status), ptr(stats) if stats is not None else None, ptr(counter), stream_handle(stream))
         if wide_rel.size:
             sys_ids = (wide_rel[:, None] * S + np.arange(S)[None, :]).ravel().astype(np.int64)
             members = nb + int(nstream[wide_rel].max())

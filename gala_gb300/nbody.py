@@ -107,8 +107,8 @@ def integrate_systems(hamiltonian, bodies, w0, t, atol=1e-10, rtol=1e-10, nmax=0
     if bodies.ndim != 2 or bodies.shape[0] != ns:
         raise ValueError(f"bodies must have shape (n_systems, nbody), got {bodies.shape}")
     nbody = int(bodies.shape[1])
-    if not 1 <= npart <= 32:
-        raise NotImplementedError(f"systems of {npart} particles: the GPU kernel takes 1 to 32")
+    if npart < 1:
+        raise ValueError("a system needs at least one particle")
     if nbody > npart:
         raise ValueError("more massive bodies than particles")
     t = np.ascontiguousarray(np.asarray(t, dtype=np.float64))
@@ -124,10 +124,18 @@ def integrate_systems(hamiltonian, bodies, w0, t, atol=1e-10, rtol=1e-10, nmax=0
     status = torch.zeros(max(ns, 1), dtype=torch.int32, device=dev)
     stats = torch.zeros((max(ns, 1), 4), dtype=torch.int64, device=dev) if return_stats else None
     counter = torch.zeros(1, dtype=torch.int64, device=dev)
-    _abi.call("gx_nbody_dop853", H.potential.packed().for_device(), H._frame_ref(), ns, npart, nbody, ptr(bd),
-              ptr(w0d), ptr(td), ntimes, float(atol), float(rtol), int(nmax), float(dt_max), int(nstiff),
-              int(bool(save_all)), int(out_stride), ptr(out), ptr(status),
-              ptr(stats) if stats is not None else None, ptr(counter), stream_handle(stream))
+    if npart <= 32:  # a system is a group of lanes of one warp
+        _abi.call("gx_nbody_dop853", H.potential.packed().for_device(), H._frame_ref(), ns, npart, nbody, ptr(bd),
+                  ptr(w0d), ptr(td), ntimes, float(atol), float(rtol), int(nmax), float(dt_max), int(nstiff),
+                  int(bool(save_all)), int(out_stride), ptr(out), ptr(status),
+                  ptr(stats) if stats is not None else None, ptr(counter), stream_handle(stream))
+    else:  # wider systems: one CTA each, the state in device scratch
+        nbytes = int(_abi.load().gx_nbody_wide_scratch_bytes(ns, npart))
+        scratch = torch.empty(max(nbytes // 8, 1), dtype=torch.float64, device=dev)
+        _abi.call("gx_nbody_dop853_wide", H.potential.packed().for_device(), H._frame_ref(), ns, npart, nbody,
+                  ptr(bd), ptr(w0d), ptr(td), ntimes, float(atol), float(rtol), int(nmax), float(dt_max),
+                  int(nstiff), int(bool(save_all)), int(out_stride), ptr(scratch), nbytes, ptr(out), ptr(status),
+                  ptr(stats) if stats is not None else None, stream_handle(stream))
     if return_stats:
         return out, status[:ns], stats[:ns]
     return out, status[:ns]

@@ -509,7 +509,7 @@ int gx_selfcheck_fast64(const double* x, int64_t n, double* out, void* stream);
  *   status  DEVICE int32 (n_systems): gala's dop853() code per system
  *   stats   DEVICE int64 (n_systems, 4) or NULL: nfcn, nstep, naccpt, nrejct
  *   queue_counter  DEVICE int64 scratch (zeroed by the call)
- * 1 <= nparticles <= 32. */
+ * 1 <= nparticles <= 32 (wider systems: gx_nbody_dop853_wide). */
 int gx_nbody_dop853(const gx_potential* pot, const gx_frame* frame, int64_t n_systems,
                     int32_t nparticles, int32_t nbody, const gx_body* bodies,
                     const double* w0, const double* t, int64_t ntimes, double atol,
@@ -593,6 +593,22 @@ int gx_mockstream_dop853_wide(const gx_potential* pot, const gx_frame* frame, in
                               int64_t n_systems, int32_t max_members, double* scratch,
                               int64_t scratch_bytes, double* stream_w_out, double* nbody_w_out,
                               int32_t* status, int64_t* stats, void* stream);
+
+/* DirectNBody systems of any size: the same call as gx_nbody_dop853
+ * (direct_nbody_dop853, nbody.pyx:30-115 -> dop853_helper, dop853.pyx:90-193)
+ * for systems too wide for a warp, one CTA per system, its state and
+ * dense-output coefficients in caller-provided device scratch of
+ * gx_nbody_wide_scratch_bytes(n_systems, nparticles) bytes.  Arguments and
+ * outputs as gx_nbody_dop853 without the queue counter.  The error and
+ * stiffness sums are fixed-order CTA sums (gala sums sequentially): results
+ * agree with gala to rounding. */
+int64_t gx_nbody_wide_scratch_bytes(int64_t n_systems, int32_t nparticles);
+int gx_nbody_dop853_wide(const gx_potential* pot, const gx_frame* frame, int64_t n_systems,
+                         int32_t nparticles, int32_t nbody, const gx_body* bodies, const double* w0,
+                         const double* t, int64_t ntimes, double atol, double rtol, int64_t nmax,
+                         double dt_max, int64_t nstiff, int32_t save_all, int64_t out_stride,
+                         double* scratch, int64_t scratch_bytes, double* w_out, int32_t* status,
+                         int64_t* stats, void* stream);
 
 /* MockStreamGenerator.run with output_every: mockstream_dop853_animate
  * (src/gala/dynamics/mockstream/mockstream.pyx:306-440) for n_streams

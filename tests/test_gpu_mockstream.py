@@ -893,3 +893,72 @@ def test_rotating_frame_stream_matches_oracle(oracle, mode):
     assert got.shape == ref.shape
     assert _scale_err(got, ref) < 1e-9
     assert _scale_err(got_nb, ref_nb) < 1e-10
+
+
+def _wide_system(n_massive, n_test, seed):
+    """A cluster of Plummer bodies plus test particles in the MW composite, far
+    enough apart that the orbits are regular over the test's span."""
+    rng = np.random.default_rng(seed)
+    pots = [g.PlummerPotential(m=float(m), b=0.05) for m in rng.uniform(1e5, 1e6, n_massive)] + [None] * n_test
+    w0 = np.ascontiguousarray(W.mw_ics(1, seed=seed).T).repeat(n_massive + n_test, axis=0)
+    w0[:, :3] += rng.normal(0, 0.5, size=(n_massive + n_test, 3))
+    w0[:, 3:] += rng.normal(0, 0.005, size=(n_massive + n_test, 3))
+    return pots, w0
+
+
+@pytest.mark.parametrize("save_all", [True, False])
+def test_nbody_systems_wider_than_a_warp_match_oracle(oracle, save_all):
+    """Systems of 48 particles (24 massive): one CTA per system
+    (gx_nbody_dop853_wide, dop853_helper's arguments, dense output onto the
+    grid), against the oracle's direct_nbody_dop853 on each system."""
+    pot = W.mw_composite()
+    t = g.parse_time_specification(dt=1.0, n_steps=80)
+    systems = [_wide_system(24, 24, 80 + s) for s in range(3)]
+    bodies = pack_bodies([p[:24] for p, _ in systems])
+    w0 = np.stack([w for _, w in systems])
+    out, status = integrate_systems(pot, bodies, w0, t, save_all=save_all, nstiff=-1)
+    out = out.cpu().numpy()
+    assert np.all(status.cpu().numpy() == 1)
+    for s, (pots, w) in enumerate(systems):
+        ref, res = oracle.nbody_dop853(pot, pack_bodies(pots), 24, w, t, save_all=save_all)
+        assert res == 1
+        assert _scale_err(out[s], ref) < 1e-10
+
+
+def test_directnbody_of_forty_bodies_and_a_stream_with_many_perturbers(oracle):
+    """DirectNBody.integrate_orbit with 40 bodies (beyond one warp), and a mock
+    stream whose progenitor has 32 perturbers (every release system wider than a
+    warp), against the oracle."""
+    from gala_gb300.nbody import DirectNBody
+
+    pot = W.mw_composite()
+    pots, w = _wide_system(20, 20, 90)
+    psp = g.PhaseSpacePosition(pos=w[:, :3].T, vel=w[:, 3:].T)
+    orb = DirectNBody(psp, pots, external_potential=pot).integrate_orbit(dt=1.0, n_steps=100)
+    t = g.parse_time_specification(dt=1.0, n_steps=100)
+    ref, res = oracle.nbody_dop853(pot, pack_bodies(pots), 20, w, t)
+    assert res == 1
+    got = np.concatenate([orb.xyz, orb.v_xyz]).transpose(1, 2, 0)
+    assert _scale_err(got, ref) < 1e-10
+
+    prog_pot = g.PlummerPotential(m=2e5, b=0.01)
+    ppots, pw = _wide_system(32, 0, 91)
+    nb = DirectNBody(g.PhaseSpacePosition(pos=pw[1:, :3].T, vel=pw[1:, 3:].T), ppots[1:], external_potential=pot)
+    gen = MockStreamGenerator(FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(4)),
+                              g.Hamiltonian(pot), progenitor_potential=prog_pot)
+    stream, nbody_w = gen.run(g.PhaseSpacePosition.from_w(pw[0]), 2e5, nbody=nb, dt=1.0, n_steps=20)
+    # the oracle's pipeline: the bodies, Fardal releases around body 0, the release systems
+    bodies = pack_bodies([prog_pot] + ppots[1:])
+    t = g.parse_time_specification(dt=1.0, n_steps=20)
+    orbw, res = oracle.nbody_dop853(pot, bodies, 32, pw, t)
+    assert res == 1
+    df = FardalStreamDF(gala_modified=True, random_state=np.random.RandomState(4))
+    counts = df.release_counts(len(t))
+    offset = np.concatenate([[0], np.cumsum(2 * counts)]).astype(np.int64)
+    sw0 = oracle.fardal_sample(pot, orbw[:, 0], np.full(len(t), 2e5), t, offset, df._draws(int(offset[-1])),
+                               g.units.G)
+    rel = np.nonzero(counts > 0)[0]
+    ref_nb, ref_st, st = oracle.mockstream_dop853(pot, bodies, pw, t[rel], sw0, t[rel], t[-1], 2 * counts[rel])
+    assert np.all(st == 1)
+    got = np.vstack([stream.xyz, stream.v_xyz]).T
+    assert _scale_err(got, ref_st) < 1e-9

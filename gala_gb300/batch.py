@@ -42,9 +42,9 @@ def schedule(n_steps, method, chunk):
     """The processing order with an exact sort, in torch: per integrator, orbits
     sorted by cost (longest first) and cut into chunks; chunks of both
     integrators merged by cost, longest first; the tail of each integrator's
-    list padded with -1.  BatchIntegrator builds the same order on the device
-    with costs binned at 4.4 % (gx_batch_schedule); this form is the test's
-    reference for it."""
+    list padded with -1.  BatchIntegrator.capture uses it; one-shot runs build
+    the same order on the device with costs binned at 0.54 %
+    (gx_batch_schedule)."""
     import torch
 
     dev = n_steps.device
@@ -163,19 +163,28 @@ class BatchIntegrator:
         self.state = torch.empty((12, self.n), dtype=torch.float32, device=self.dev) if checkpoint else None
 
     # ------------------------------------------------------------------ run
-    def _prepare(self, stream_handle=None):
-        """The processing order for the current launch shape, built on the
-        device on the launching stream (gx_batch_schedule, no host sync)."""
+    def _prepare(self, stream_handle=None, exact=False):
+        """The processing order for the current launch shape: built on the
+        device on the launching stream (gx_batch_schedule, no host sync, costs
+        binned at 0.54 %), or with exact=True by an exact sort in torch (two
+        host syncs, about 0.7 ms for 262,144 orbits; the binned order measured
+        1.5-2.5 % slower on the uneven MW workload, so a captured graph, which
+        replays one order many times, takes the exact one)."""
         import torch
 
         from ._device import ptr
 
-        lib = _abi.load()
         chunk = self.config["chunk"]
+        if exact:
+            self.order = schedule(self.n_steps, self.method, chunk)
+            self._order_chunk = chunk
+            return
+        lib = _abi.load()
         slots = int(lib.gx_batch_schedule_slots(self.n, chunk))
         words = int(lib.gx_batch_schedule_work_words(self.n, chunk))
         if getattr(self, "order", None) is None or self.order.numel() != slots:
             self.order = torch.empty(slots, dtype=torch.int32, device=self.dev)
+        if getattr(self, "_sched_work", None) is None or self._sched_work.numel() < words:
             self._sched_work = torch.empty(words, dtype=torch.int32, device=self.dev)
         _abi.call("gx_batch_schedule", ptr(self.n_steps), ptr(self.method), self.n, chunk, ptr(self.order), slots,
                   ptr(self._sched_work), words, stream_handle)
@@ -232,7 +241,7 @@ class BatchIntegrator:
 
         if self.n == 0:
             return self
-        self._prepare(stream_handle())
+        self._prepare(stream_handle(), exact=True)
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(s):

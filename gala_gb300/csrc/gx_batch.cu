@@ -438,7 +438,7 @@ extern "C" int gx_fixed_fp32(const gx_potential *pot, int32_t method, const doub
 // ===========================================================================
 // The processing order of a batch, built on the device without a host sync:
 // per integrator the orbits sorted by cost (n_steps x gradient evaluations per
-// step, 1 for Leapfrog and 3 for Ruth4) into 16 bins per octave -- a 4.4 %
+// step, 1 for Leapfrog and 3 for Ruth4) into 128 bins per octave -- a 0.54 %
 // resolution, the most expensive first -- and cut into chunks padded with -1;
 // the chunks of the two integrators merged by the bin of their first orbit
 // (Ruth4 first on ties).  Orbits of one bin keep no particular order; each
@@ -446,10 +446,12 @@ extern "C" int gx_fixed_fp32(const gx_potential *pot, int32_t method, const doub
 // ===========================================================================
 namespace gx {
 
-constexpr int SB_PER_OCT = 16;
+constexpr int SB_PER_OCT = 128;
 constexpr int SB_BINS = 64 * SB_PER_OCT;    // bins per integrator (cost below 2^64)
 constexpr int SB_HIST = 2 * SB_BINS;        // Ruth4 bins, then Leapfrog bins
 constexpr int SB_INFO = 4;                  // chunks of each integrator
+constexpr int SB_SCAN_T = 1024;             // threads of the scan
+constexpr int SB_PER_T = SB_BINS / SB_SCAN_T;  // bins of each half per scan thread
 
 __device__ __forceinline__ int sched_bin(int64_t nsteps, int32_t method) {
     const double cost = (double)(nsteps > 0 ? nsteps : 0) * (method == 0 ? 1.0 : 3.0);
@@ -466,27 +468,41 @@ __global__ void sched_histogram(int32_t *hist, const int64_t *__restrict__ nstep
     if (i < n) atomicAdd(&hist[sched_key(nsteps[i], method[i])], 1);
 }
 
-// Exclusive prefix sums of both halves of the histogram (one CTA of SB_BINS
-// threads, thread t owning bin t of each half); the Leapfrog list starts after
-// the Ruth4 list padded to whole chunks.  info = {Ruth4 chunks, Leapfrog chunks}.
-__global__ void __launch_bounds__(SB_BINS) sched_scan(int32_t *hist, int32_t *info, int chunk) {
-    __shared__ int32_t sr[SB_BINS], sl[SB_BINS];
+// Exclusive prefix sums of both halves of the histogram (one CTA of SB_SCAN_T
+// threads, thread t owning SB_PER_T consecutive bins of each half); the Leapfrog
+// list starts after the Ruth4 list padded to whole chunks.
+// info = {Ruth4 chunks, Leapfrog chunks}.
+__global__ void __launch_bounds__(SB_SCAN_T) sched_scan(int32_t *hist, int32_t *info, int chunk) {
+    __shared__ int32_t sr[SB_SCAN_T], sl[SB_SCAN_T];
     const int t = threadIdx.x;
-    const int32_t cr = hist[t], cl = hist[SB_BINS + t];
-    sr[t] = cr;
-    sl[t] = cl;
+    int32_t cr[SB_PER_T], cl[SB_PER_T], tr = 0, tl = 0;
+#pragma unroll
+    for (int k = 0; k < SB_PER_T; k++) {
+        cr[k] = hist[t * SB_PER_T + k];
+        cl[k] = hist[SB_BINS + t * SB_PER_T + k];
+        tr += cr[k];
+        tl += cl[k];
+    }
+    sr[t] = tr;
+    sl[t] = tl;
     __syncthreads();
-    for (int o = 1; o < SB_BINS; o <<= 1) {  // inclusive Hillis-Steele scans
+    for (int o = 1; o < SB_SCAN_T; o <<= 1) {  // inclusive Hillis-Steele scans of the threads' totals
         const int32_t ar = t >= o ? sr[t - o] : 0, al = t >= o ? sl[t - o] : 0;
         __syncthreads();
         sr[t] += ar;
         sl[t] += al;
         __syncthreads();
     }
-    const int32_t nr = sr[SB_BINS - 1], nl = sl[SB_BINS - 1];
+    const int32_t nr = sr[SB_SCAN_T - 1], nl = sl[SB_SCAN_T - 1];
     const int32_t ncr = (nr + chunk - 1) / chunk, ncl = (nl + chunk - 1) / chunk;
-    hist[t] = sr[t] - cr;
-    hist[SB_BINS + t] = ncr * chunk + sl[t] - cl;
+    int32_t orr = sr[t] - tr, ol = ncr * chunk + sl[t] - tl;
+#pragma unroll
+    for (int k = 0; k < SB_PER_T; k++) {
+        hist[t * SB_PER_T + k] = orr;
+        hist[SB_BINS + t * SB_PER_T + k] = ol;
+        orr += cr[k];
+        ol += cl[k];
+    }
     if (t == 0) {
         info[0] = ncr;
         info[1] = ncl;
@@ -550,7 +566,7 @@ static int launch_schedule(const int64_t *n_steps, const int32_t *method, int64_
     const unsigned gn = (unsigned)((n + tb - 1) / tb);
     const int64_t max_chunks = slots / chunk;
     sched_histogram<<<gn, tb, 0, st>>>(hist, n_steps, method, n);
-    sched_scan<<<1, SB_BINS, 0, st>>>(hist, info, chunk);
+    sched_scan<<<1, SB_SCAN_T, 0, st>>>(hist, info, chunk);
     sched_scatter<<<gn, tb, 0, st>>>(hist, tmp, n_steps, method, n);
     sched_heads<<<(unsigned)((max_chunks + tb - 1) / tb), tb, 0, st>>>(info, tmp, heads, n_steps, method, chunk);
     sched_merge<<<(unsigned)((max_chunks * 32 + tb - 1) / tb), tb, 0, st>>>(info, tmp, heads, order, chunk);

@@ -316,7 +316,7 @@ int gx_dop853_fp32(const gx_potential* pot, const gx_frame* frame, const double*
 
 /* The processing order of a batch for gx_batch_integrate_fp32 / _fp64, built
  * on the device with no host synchronisation: per integrator the orbits by
- * cost (n_steps x 1 for Leapfrog, x 3 for Ruth4) in 16 bins per octave, the
+ * cost (n_steps x 1 for Leapfrog, x 3 for Ruth4) in 128 bins per octave, the
  * most expensive first, cut into chunks of `chunk` padded with -1; the chunks
  * of both integrators merged by the bin of their first orbit.
  *   n_steps, method  DEVICE (N,) as for gx_batch_integrate_fp32
@@ -394,7 +394,7 @@ int gx_batch_integrate_fp64(const gx_potential* pot, const double* w0, int64_t n
  *   address up again.
  *   Every call on a device shares the one array: calls that overlap on the GPU
  *   (different streams, no ordering) race and must not be issued.
- * The library holds the array (about 2.1 MB) on every GPU it is loaded on until
+ * The library holds the array (about 2.2 MB) on every GPU it is loaded on until
  * the process exits. */
 #define GX_NOALLOC_MAX_ORBITS 262144
 int gx_batch_integrate_fp32_noalloc(const gx_potential* pot, const double* w0, int64_t n,

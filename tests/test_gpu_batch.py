@@ -123,7 +123,7 @@ def test_invalid_batch_arguments():
 def test_device_schedule_is_a_cost_ordered_chunking(chunk):
     """gx_batch_schedule: every orbit exactly once; every chunk holds one
     integrator; within each integrator the lists run from the most expensive
-    orbit down (to the 4.4 % bins); chunk heads of the merged order do not
+    orbit down (to the 0.54 % bins); chunk heads of the merged order do not
     increase in cost by more than a bin; the same chunk-head costs as the
     exact torch order to within a bin."""
     import torch
@@ -143,7 +143,7 @@ def test_device_schedule_is_a_cost_ordered_chunking(chunk):
     assert np.array_equal(np.sort(real), np.arange(n))
     ns, me = nsteps.cpu().numpy(), method.cpu().numpy()
     cost = ns * np.where(me == 1, COST[1], COST[0])
-    bin_ratio = 2.0 ** (1 / 16)
+    bin_ratio = 2.0 ** (1 / 128)
     heads = []
     for c in order.reshape(-1, chunk):
         ids = c[c >= 0]

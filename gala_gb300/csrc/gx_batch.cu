@@ -14,7 +14,9 @@
 // does not accumulate over tens of thousands of steps.
 //   leapfrog  kick-drift-kick as c_leapfrog_step (leapfrog.pyx:35-51)
 //   ruth4     c_ruth4_step (ruth4.pyx:24-35); the d = 0 sub-step's gradient is
-//             skipped here (FP32 form, no bit-parity claim)
+//             skipped here (FP32 form, no bit-parity claim); each later sub-step's
+//             kick and drift are fused (kick_drift), the step ending on a drift
+//             so that a resumed run repeats the bits of an uninterrupted one
 #include <mutex>
 
 #include <cuda.h>
@@ -78,7 +80,7 @@ __device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const Bat
         for (int64_t j = 0; j < nsteps; j++) {
             for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], h, vl[k] * h));
             potential_gradient_f<S>(pot, xh, g);
-            for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h);
+            for (int k = 0; k < 3; k++) kick(vh[k], vl[k], -h, g[k]);
         }
         if constexpr (STATE) {
             if (A.state_out)
@@ -109,8 +111,7 @@ __device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const Bat
 #pragma unroll
             for (int s = 1; s < 4; s++) {
                 potential_gradient_f<S>(pot, xh, g);
-                for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], dh[s] * g[k]);
-                for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], ch[s], vl[k] * ch[s]));
+                for (int k = 0; k < 3; k++) kick_drift(xh[k], xl[k], vh[k], vl[k], dh[s], g[k], ch[s]);
             }
         }
         if constexpr (STATE) {
@@ -357,7 +358,7 @@ __global__ void __launch_bounds__(128) fixed_fp32_kernel(const __grid_constant__
         for (int64_t j = 1; j <= A.nsteps; j++) {
             for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], h, vl[k] * h));
             potential_gradient_f<S>(pot, xh, g);
-            for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h);
+            for (int k = 0; k < 3; k++) kick(vh[k], vl[k], -h, g[k]);
             if (A.save_all && j % A.out_stride == 0) {
                 // output velocity of c_leapfrog_step: v_{j+1/2} + g h / 2
                 for (int k = 0; k < 3; k++) v[k] = (double)vh[k] + ((double)vl[k] + (double)(g[k] * h * 0.5f));
@@ -371,8 +372,7 @@ __global__ void __launch_bounds__(128) fixed_fp32_kernel(const __grid_constant__
 #pragma unroll
             for (int s = 1; s < 4; s++) {
                 potential_gradient_f<S>(pot, xh, g);
-                for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -A.d[s] * g[k] * h);
-                for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], A.c[s] * fmaf(vh[k], h, vl[k] * h));
+                for (int k = 0; k < 3; k++) kick_drift(xh[k], xl[k], vh[k], vl[k], -A.d[s] * h, g[k], A.c[s] * h);
             }
             if (A.save_all && j % A.out_stride == 0) {
                 for (int k = 0; k < 3; k++) v[k] = (double)vh[k] + (double)vl[k];

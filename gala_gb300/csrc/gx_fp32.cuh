@@ -53,79 +53,97 @@ __device__ __forceinline__ float lg2_approx(float x) {
     return r;
 }
 
-// f(u)/u^3 for the NFW force, u = r / r_s.  For u < 1, with s = u / (2 + u)
-// (so ln(1 + u) = 2 atanh(s), u / (1 + u) = 2 s / (1 + s), 1 - s = 2 / (2 + u)):
+// f(u)/u^3 for the NFW force, u = r / r_s, without a branch: both forms below
+// are computed and the right one selected, so lanes on either side of u = 1 do
+// not run the two forms one after the other, and the dependent chain of one lane
+// holds no branch.  For u < 1, with s = u / (2 + u) (so ln(1 + u) = 2 atanh(s),
+// u / (1 + u) = 2 s / (1 + s), 1 - s = 2 / (2 + u)):
 //   f(u) / u^3 = (1 - s)^3 / 4 * [1 / (s (1 + s)) + P(s^2)],
 //   P(t) = sum_{k>=0} t^k / (2k + 3),
 // every term positive (no cancellation); s < 1/3, so six terms of P leave a
-// truncation below 2^-24 of the bracket.  For u >= 1 the direct form has no
-// harmful cancellation.
-// The two reciprocals both depend on u alone and run side by side:
-// 1 / (s (1 + s)) = (2 + u)^2 / (2 u (1 + u)), (1 - s)^3 / 4 = 2 r^3, r = 1 / (2 + u).
+// truncation below 2^-24 of the bracket.  For u >= 1 the direct form
+// (ln(1 + u) - u / (1 + u)) / u^3 has no harmful cancellation.  Both forms take
+// their reciprocals from two MUFU reciprocals that depend on u alone:
+// r = 1 / (2 + u), q = 1 / (u (1 + u)), with 1 / (s (1 + s)) = (2 + u)^2 q / 2,
+// (1 - s)^3 / 4 = 2 r^3, 1 / (1 + u) = u q and 1 / u = (1 + u) q.
 __device__ __forceinline__ float nfw_f_over_u3(float u) {
-    if (u < 1.0f) {
-        const float tu = 2.0f + u;
-        const float r = rcp_approx(tu);
-        const float q = rcp_approx(fmaf(u, u, u));
-        const float s = u * r;
-        const float t = s * s;
-        // P(t) in the form a + t^2 (b + t^2 c) (three dependent steps instead of five)
-        const float t2 = t * t;
-        const float pa = fmaf(1.0f / 5.0f, t, 1.0f / 3.0f);
-        const float pb = fmaf(1.0f / 9.0f, t, 1.0f / 7.0f);
-        const float pc = fmaf(1.0f / 13.0f, t, 1.0f / 11.0f);
-        const float P = fmaf(fmaf(pc, t2, pb), t2, pa);
-        const float br = fmaf(0.5f * tu * tu, q, P);
-        return 2.0f * r * r * r * br;
-    }
+    const float tu = 2.0f + u;
+    const float r = rcp_approx(tu);
+    const float q = rcp_approx(fmaf(u, u, u));
+    const float s = u * r;
+    const float t = s * s;
+    // P(t) in the form a + t^2 (b + t^2 c) (three dependent steps instead of five)
+    const float t2 = t * t;
+    const float pa = fmaf(1.0f / 5.0f, t, 1.0f / 3.0f);
+    const float pb = fmaf(1.0f / 9.0f, t, 1.0f / 7.0f);
+    const float pc = fmaf(1.0f / 13.0f, t, 1.0f / 11.0f);
+    const float P = fmaf(fmaf(pc, t2, pb), t2, pa);
+    const float br = fmaf(0.5f * tu * tu, q, P);
+    const float inner = 2.0f * r * r * r * br;
     const float opu = 1.0f + u;
-    const float iopu = rcp_approx(opu);
-    const float f = lg2_approx(opu) * 0.69314718055994531f - u * iopu;
-    const float iu = rcp_approx(u);
-    return f * iu * iu * iu;
+    const float iu = opu * q;
+    const float f = fmaf(lg2_approx(opu), 0.69314718055994531f, -u * u * q);
+    const float outer = f * (iu * iu * iu);
+    return u < 1.0f ? inner : outer;
+}
+
+// Components whose force is fac(r) q (centred, spherical): Kepler, Hernquist,
+// Plummer, spherical NFW.
+template <int T>
+inline constexpr bool spherical_t =
+    T == GX_POT_KEPLER || T == GX_POT_HERNQUIST || T == GX_POT_PLUMMER || T == GX_POT_SPHERICALNFW;
+
+// fac(r) of a spherical component of compile-time type T, from r^2 and 1/r.
+template <int T>
+__device__ __forceinline__ float comp_fac_t(const float *p, float r2, float ri) {
+    if constexpr (T == GX_POT_KEPLER) {  // p = {G m}
+        return (p[0] * ri) * (ri * ri);
+    } else if constexpr (T == GX_POT_HERNQUIST) {  // p = {G m, c}
+        const float irc = rcp_approx(fmaf(r2, ri, p[1]));
+        return (p[0] * ri) * (irc * irc);
+    } else if constexpr (T == GX_POT_PLUMMER) {  // p = {G m, b^2}
+        const float rb = rsqrt_approx(r2 + p[1]);
+        return (p[0] * rb) * (rb * rb);
+    } else {  // spherical NFW, p = {G m / r_s^3, 1 / r_s}
+        return p[0] * nfw_f_over_u3(r2 * ri * p[1]);
+    }
+}
+
+// Gradient of one component of compile-time type T, written to v.
+template <int T>
+__device__ __forceinline__ void comp_vec_t(const float *p, const float *q, float *v) {
+    if constexpr (spherical_t<T>) {
+        const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+        const float fac = comp_fac_t<T>(p, r2, rsqrt_approx(r2));
+        v[0] = fac * q[0]; v[1] = fac * q[1]; v[2] = fac * q[2];
+    } else if constexpr (T == GX_POT_MIYAMOTONAGAI) {  // p = {G m, a, b^2}
+        const float z2b = fmaf(q[2], q[2], p[2]);
+        const float szi = rsqrt_approx(z2b);
+        const float zd = fmaf(z2b, szi, p[1]);
+        const float ti = rsqrt_approx(fmaf(zd, zd, q[0] * q[0] + q[1] * q[1]));
+        const float fac = (p[0] * ti) * (ti * ti);
+        v[0] = fac * q[0]; v[1] = fac * q[1]; v[2] = fac * q[2] * fmaf(p[1], szi, 1.0f);
+    } else if constexpr (T == GX_POT_FLATTENEDNFW) {  // p = {G m / r_s^3, 1 / r_s, 1 / c^2}
+        const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] * p[2];
+        const float u = r2 * rsqrt_approx(r2) * p[1];
+        const float fac = p[0] * nfw_f_over_u3(u);
+        v[0] = fac * q[0]; v[1] = fac * q[1]; v[2] = fac * q[2] * p[2];
+    } else if constexpr (T == GX_POT_TRIAXIALNFW) {  // p = {G m / r_s^3, 1 / r_s, 1/a^2, 1/b^2, 1/c^2}
+        const float r2 = q[0] * q[0] * p[2] + q[1] * q[1] * p[3] + q[2] * q[2] * p[4];
+        const float u = r2 * rsqrt_approx(r2) * p[1];
+        const float fac = p[0] * nfw_f_over_u3(u);
+        v[0] = fac * q[0] * p[2]; v[1] = fac * q[1] * p[3]; v[2] = fac * q[2] * p[4];
+    } else {  // GX_POT_NULL
+        v[0] = 0.f; v[1] = 0.f; v[2] = 0.f;
+    }
 }
 
 // Gradient of one component of compile-time type T, accumulated into g.
 template <int T>
 __device__ __forceinline__ void comp_grad_t(const float *p, const float *q, float *g) {
-    if constexpr (T == GX_POT_KEPLER) {  // p = {G m}
-        const float ri = rsqrt_approx(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
-        const float fac = p[0] * ri * ri * ri;
-        g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2];
-    } else if constexpr (T == GX_POT_HERNQUIST) {  // p = {G m, c}
-        const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-        const float ri = rsqrt_approx(r2);
-        const float rc = fmaf(r2, ri, p[1]);
-        const float irc = rcp_approx(rc);
-        const float fac = p[0] * ri * irc * irc;
-        g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2];
-    } else if constexpr (T == GX_POT_PLUMMER) {  // p = {G m, b^2}
-        const float ri = rsqrt_approx(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + p[1]);
-        const float fac = p[0] * ri * ri * ri;
-        g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2];
-    } else if constexpr (T == GX_POT_MIYAMOTONAGAI) {  // p = {G m, a, b^2}
-        const float z2b = fmaf(q[2], q[2], p[2]);
-        const float szi = rsqrt_approx(z2b);
-        const float zd = fmaf(z2b, szi, p[1]);
-        const float ti = rsqrt_approx(q[0] * q[0] + q[1] * q[1] + zd * zd);
-        const float fac = p[0] * ti * ti * ti;
-        g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2] * fmaf(p[1], szi, 1.0f);
-    } else if constexpr (T == GX_POT_SPHERICALNFW) {  // p = {G m / r_s^3, 1 / r_s}
-        const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-        const float u = r2 * rsqrt_approx(r2) * p[1];
-        const float fac = p[0] * nfw_f_over_u3(u);
-        g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2];
-    } else if constexpr (T == GX_POT_FLATTENEDNFW) {  // p = {G m / r_s^3, 1 / r_s, 1 / c^2}
-        const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] * p[2];
-        const float u = r2 * rsqrt_approx(r2) * p[1];
-        const float fac = p[0] * nfw_f_over_u3(u);
-        g[0] += fac * q[0]; g[1] += fac * q[1]; g[2] += fac * q[2] * p[2];
-    } else if constexpr (T == GX_POT_TRIAXIALNFW) {  // p = {G m / r_s^3, 1 / r_s, 1/a^2, 1/b^2, 1/c^2}
-        const float r2 = q[0] * q[0] * p[2] + q[1] * q[1] * p[3] + q[2] * q[2] * p[4];
-        const float u = r2 * rsqrt_approx(r2) * p[1];
-        const float fac = p[0] * nfw_f_over_u3(u);
-        g[0] += fac * q[0] * p[2]; g[1] += fac * q[1] * p[3]; g[2] += fac * q[2] * p[4];
-    }
+    float v[3];
+    comp_vec_t<T>(p, q, v);
+    g[0] += v[0]; g[1] += v[1]; g[2] += v[2];
 }
 
 // Run-time dispatch on the component type.
@@ -172,26 +190,80 @@ struct SigTypes<PotSig<T0, T1, T2, T3>> {
     static constexpr int t0 = T0, t1 = T1, t2 = T2, t3 = T3;
 };
 
-template <typename S>
-__device__ __forceinline__ void potential_gradient_f(const DevPotF &pot, const float *q, float *g) {
-    g[0] = 0.f; g[1] = 0.f; g[2] = 0.f;
-    if constexpr (S::generic) {
-        for (int i = 0; i < pot.ncomp; i++) comp_gradient_sr(pot.c[i], q, g);
+// One component of a compile-time list: a spherical one adds its factor to fs,
+// any other its gradient to gm (the flags say whether fs / gm hold a term yet;
+// they are compile-time constants after inlining, so no 0 + x is issued).
+template <int T>
+__device__ __forceinline__ void sig_term(const float *p, const float *q, float r2, float ri, float &fs, bool &has_fs,
+                                         float *gm, bool &has_gm) {
+    if constexpr (T < 0) {
+        return;
+    } else if constexpr (spherical_t<T>) {
+        const float f = comp_fac_t<T>(p, r2, ri);
+        fs = has_fs ? fs + f : f;
+        has_fs = true;
     } else {
-        using T = SigTypes<S>;
-        if constexpr (T::t0 >= 0) comp_grad_t<T::t0>(pot.c[0].p, q, g);
-        if constexpr (T::t1 >= 0) comp_grad_t<T::t1>(pot.c[1].p, q, g);
-        if constexpr (T::t2 >= 0) comp_grad_t<T::t2>(pot.c[2].p, q, g);
-        if constexpr (T::t3 >= 0) comp_grad_t<T::t3>(pot.c[3].p, q, g);
+        float v[3];
+        comp_vec_t<T>(p, q, v);
+        for (int k = 0; k < 3; k++) gm[k] = has_gm ? gm[k] + v[k] : v[k];
+        has_gm = true;
     }
 }
 
-// Compensated (Kahan) accumulation s += d with running compensation c.
+// Gradient of the whole potential at q.  A compile-time list shares r^2 and
+// 1/r among its spherical components and multiplies the sum of their factors
+// by q once: g = (sum fac) q + (the other components' gradients).
+template <typename S>
+__device__ __forceinline__ void potential_gradient_f(const DevPotF &pot, const float *q, float *g) {
+    if constexpr (S::generic) {
+        g[0] = 0.f; g[1] = 0.f; g[2] = 0.f;
+        for (int i = 0; i < pot.ncomp; i++) comp_gradient_sr(pot.c[i], q, g);
+    } else {
+        using T = SigTypes<S>;
+        const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+        const float ri = rsqrt_approx(r2);
+        float fs = 0.f, gm[3] = {0.f, 0.f, 0.f};
+        bool has_fs = false, has_gm = false;
+        sig_term<T::t0>(pot.c[0].p, q, r2, ri, fs, has_fs, gm, has_gm);
+        sig_term<T::t1>(pot.c[1].p, q, r2, ri, fs, has_fs, gm, has_gm);
+        sig_term<T::t2>(pot.c[2].p, q, r2, ri, fs, has_fs, gm, has_gm);
+        sig_term<T::t3>(pot.c[3].p, q, r2, ri, fs, has_fs, gm, has_gm);
+        for (int k = 0; k < 3; k++) g[k] = has_fs ? (has_gm ? fmaf(fs, q[k], gm[k]) : fs * q[k]) : gm[k];
+    }
+}
+
+// Compensated accumulation into the pair (s, c), whose value is s + c (the
+// convention of the FP64 split hi = (float)x, lo = (float)(x - hi), of the
+// drift increments h (vh + vl) and of the output hi + lo): the increment d and
+// the carried low part are added to s, and the rounding error of that addition
+// (Fast2Sum, exact while |s| >= |d + c|) becomes the new low part.
 __device__ __forceinline__ void kahan_add(float &s, float &c, float d) {
-    const float y = __fsub_rn(d, c);
+    const float y = __fadd_rn(d, c);
     const float t = __fadd_rn(s, y);
-    c = __fsub_rn(__fsub_rn(t, s), y);
+    c = __fsub_rn(y, __fsub_rn(t, s));
     s = t;
+}
+
+// Kick (vh, vl) += dh g, compensated, with the product fused into the addition
+// of the carried low part.
+__device__ __forceinline__ void kick(float &vh, float &vl, float dh, float g) {
+    const float a = fmaf(dh, g, vl);
+    const float t = __fadd_rn(vh, a);
+    vl = __fsub_rn(a, __fsub_rn(t, vh));
+    vh = t;
+}
+
+// The kick above followed by the drift (xh, xl) += ch v: the drift increment
+// ch (vh + (vl + dh g)) is formed from the velocity before its compensated
+// addition, so the drift does not wait for it (a shorter dependent chain per
+// sub-step than kick, then drift from the new pair).
+__device__ __forceinline__ void kick_drift(float &xh, float &xl, float &vh, float &vl, float dh, float g, float ch) {
+    const float a = fmaf(dh, g, vl);
+    const float d = fmaf(ch, vh, ch * a);
+    const float t = __fadd_rn(vh, a);
+    vl = __fsub_rn(a, __fsub_rn(t, vh));
+    vh = t;
+    kahan_add(xh, xl, d);
 }
 
 }  // namespace gx

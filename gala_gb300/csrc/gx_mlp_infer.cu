@@ -396,10 +396,11 @@ __device__ __forceinline__ void split(double x, float &hi, float &lo) {
     hi = (float)x;
     lo = (float)(x - (double)hi);
 }
+// compensated accumulation into (s, c), value s + c (the split's convention)
 __device__ __forceinline__ void kahan(float &s, float &c, float d) {
-    const float y = __fsub_rn(d, c);
+    const float y = __fadd_rn(d, c);
     const float t = __fadd_rn(s, y);
-    c = __fsub_rn(__fsub_rn(t, s), y);
+    c = __fsub_rn(y, __fsub_rn(t, s));
     s = t;
 }
 

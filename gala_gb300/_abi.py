@@ -15,6 +15,7 @@ from . import _build
 GX_MAX_COMPONENTS = 16
 GX_MAX_INLINE_PARAMS = 128
 GX_NOALLOC_MAX_ORBITS = 262144
+GX_BATCH_QUEUE_WORDS = 1026
 
 GX_OK = 0
 GX_ERR_INVALID_ARGUMENT = -1
@@ -183,7 +184,7 @@ def _bind(path: Path, debug: bool, build_if_missing: bool):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.gx_abi_version() != 2:
+    if lib.gx_abi_version() != 3:
         raise RuntimeError("gala_gb300 library ABI version mismatch")
     return lib
 

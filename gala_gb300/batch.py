@@ -19,6 +19,7 @@ from pathlib import Path
 import numpy as np
 
 from . import _abi
+from ._abi import GX_BATCH_QUEUE_WORDS
 from ._trace import traced
 
 LEAPFROG, RUTH4 = 0, 1
@@ -151,7 +152,8 @@ class BatchIntegrator:
         self.w_out = torch.empty((6, self.n), dtype=torch.float64, device=self.dev)
         self.E0 = torch.empty(self.n, dtype=torch.float64, device=self.dev)
         self.E1 = torch.empty(self.n, dtype=torch.float64, device=self.dev)
-        self.counter = torch.zeros(1, dtype=torch.int32, device=self.dev)
+        # work-queue scratch: [0] main-region claims, [1] lead-region claims, flags
+        self.counter = torch.zeros(GX_BATCH_QUEUE_WORDS, dtype=torch.int32, device=self.dev)
         self.graph = None
         if (checkpoint or state is not None) and precision != "fp32c":
             raise NotImplementedError("integrator checkpoints are kept by the fp32c form")
@@ -258,20 +260,37 @@ class BatchIntegrator:
         """|E(t_end) - E(0)| / |E(0)| per orbit (FP64 diagnostic)."""
         return ((self.E1 - self.E0) / self.E0).abs()
 
+    def _taken_slots(self):
+        """(start, stop) ranges of the order's slots that the last run took:
+        the first min(q[1], n_lead x chunk / 32) blocks of 32 slots of the lead
+        region and the first min(q[0], n_chunks - n_lead) chunks after it,
+        n_lead = min(n_chunks, 4 x multiprocessors / (chunk / 32)) (the queue of
+        the batched kernels)."""
+        chunk = self.config["chunk"]
+        subs = chunk // 32
+        n_chunks = self.order.numel() // chunk
+        n_lead = min(n_chunks, 4 * self.sms // subs)
+        q_main, q_lead = (int(v) for v in self.counter[:2].tolist())
+        lead = min(q_lead, n_lead * subs)
+        main = min(q_main, n_chunks - n_lead)
+        return [(0, 32 * lead), (n_lead * chunk, (n_lead + main) * chunk)]
+
+    def chunks_taken(self):
+        """How many chunks' worth of the order the last run took (all of them
+        unless it was cancelled)."""
+        return sum(b - a for a, b in self._taken_slots()) // self.config["chunk"]
+
     def completed(self):
         """(N,) bool CUDA tensor: the orbits the last run integrated.  All of
         them unless the run was cancelled (``gala_gb300.cancel``): a cancelled
-        launch takes no further queue chunk, so the orbits of the first
-        min(counter, chunks) chunks of the order are done and the others' rows
-        of the output are untouched."""
+        launch takes no further queue chunk, so the orbits of the chunks it
+        took are done and the others' rows of the output are untouched."""
         import torch
 
-        chunk = self.config["chunk"]
-        n_chunks = self.order.numel() // chunk
-        taken = min(int(self.counter.item()), n_chunks)
         done = torch.zeros(self.n, dtype=torch.bool, device=self.dev)
-        ids = self.order[:taken * chunk].long()
-        done[ids[ids >= 0]] = True
+        for a, b in self._taken_slots():
+            ids = self.order[a:b].long()
+            done[ids[ids >= 0]] = True
         return done
 
     # ------------------------------------------------------------- autotune

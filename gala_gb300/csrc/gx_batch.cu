@@ -4,9 +4,10 @@
 // Work queue: the caller supplies a processing order (a permutation of the
 // orbits, padded with -1 to whole chunks) in which each chunk holds orbits of
 // one integrator and similar cost, chunks sorted longest first.  A persistent
-// grid (a few CTAs per SM) pulls chunks from a single atomic counter; every
-// warp integrates `chunk` orbits, one per lane, 32 at a time.  Longest-first
-// order plus dynamic pulling keeps the SMs busy until the very end.
+// grid (a few CTAs per SM) pulls chunks from the counters of gx_queue.cuh (the
+// longest chunks one per SM sub-partition, then the rest in order); every warp
+// integrates `chunk` orbits, one per lane, 32 at a time.  Longest-first order
+// plus dynamic pulling keeps the SMs busy until the very end.
 //
 // Per orbit: positions and velocities are carried as FP32 (hi, lo) pairs with
 // Kahan-compensated updates; forces are evaluated in FP32 at hi (gx_fp32.cuh).
@@ -23,6 +24,7 @@
 
 #include "gx_host.h"
 #include "gx_fp32.cuh"
+#include "gx_queue.cuh"
 #include "gx_scf.cuh"
 
 namespace gx {
@@ -30,6 +32,7 @@ namespace gx {
 struct BatchArgs {
     int64_t n;        // number of orbits
     int64_t slots;    // length of the order array (multiple of chunk)
+    int64_t n_lead;   // chunks in the lead region (gx_queue.cuh)
     int32_t chunk;    // orbits per queue item (multiple of 32)
     int32_t pad;
     float c[4], d[4];  // Ruth4 coefficients
@@ -45,95 +48,169 @@ __device__ __forceinline__ void split(double x, float &hi, float &lo) {
     lo = (float)(x - (double)hi);
 }
 
-// One orbit.  With STATE, the integrator state is read from A.state_in when
-// given (a resumed run: the Leapfrog half-step velocity is not formed again)
-// and written to A.state_out when given, so that a run of k steps followed by a
-// resumed run of n - k steps gives the bits of one run of n steps.
-template <typename S, bool STATE>
-__device__ __forceinline__ void integrate_one_fp32(const DevPotF &pot, const BatchArgs &A, const double *w0,
-                                                   int64_t n, int64_t i, int64_t nsteps, float h, int meth,
-                                                   double *w_out) {
-    const bool resume = STATE && A.state_in != nullptr;
-    if (nsteps == 0 && !(STATE && (resume || A.state_out))) {
-        for (int k = 0; k < 6; k++) w_out[k * n + i] = w0[k * n + i];
-        return;
-    }
+// One orbit's integrator state in registers: position and velocity as FP32
+// (hi, lo) pairs (for Leapfrog the velocity is the half-step v_{n+1/2}), the
+// last gradient, the step and the Ruth4 coefficients times the step.
+struct OrbitF {
     float xh[3], xl[3], vh[3], vl[3], g[3];
+    float h, ch[4], dh[4];
+};
+
+// Load an orbit: from A.state_in in a resumed run, else split from the FP64
+// initial conditions; then the Leapfrog start (c_init_velocity,
+// v_{1/2} = v - g h / 2, which a resumed run already holds; the gradient at the
+// start also serves the output velocity when no step follows) or the Ruth4
+// coefficients times the step (shorter dependent chains per sub-step).
+template <typename S, bool STATE>
+__device__ __forceinline__ void orbit_begin(const DevPotF &pot, const BatchArgs &A, const double *w0, int64_t n,
+                                            int64_t i, int64_t nsteps, float h, int meth, OrbitF &o) {
+    const bool resume = STATE && A.state_in != nullptr;
     if (resume) {
         for (int k = 0; k < 3; k++) {
-            xh[k] = A.state_in[k * n + i];
-            xl[k] = A.state_in[(3 + k) * n + i];
-            vh[k] = A.state_in[(6 + k) * n + i];
-            vl[k] = A.state_in[(9 + k) * n + i];
+            o.xh[k] = A.state_in[k * n + i];
+            o.xl[k] = A.state_in[(3 + k) * n + i];
+            o.vh[k] = A.state_in[(6 + k) * n + i];
+            o.vl[k] = A.state_in[(9 + k) * n + i];
         }
     } else {
         for (int k = 0; k < 3; k++) {
-            split(w0[k * n + i], xh[k], xl[k]);
-            split(w0[(3 + k) * n + i], vh[k], vl[k]);
+            split(w0[k * n + i], o.xh[k], o.xl[k]);
+            split(w0[(3 + k) * n + i], o.vh[k], o.vl[k]);
         }
     }
+    o.h = h;
     if (meth == 0) {
-        // c_init_velocity: v_{1/2} = v - g h / 2 (a resumed run already holds v_{1/2})
-        if (!resume || nsteps == 0) potential_gradient_f<S>(pot, xh, g);
+        if (!resume || nsteps == 0) potential_gradient_f<S>(pot, o.xh, o.g);
         if (!resume)
-            for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], -g[k] * h * 0.5f);
-        for (int64_t j = 0; j < nsteps; j++) {
-            for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], h, vl[k] * h));
-            potential_gradient_f<S>(pot, xh, g);
-            for (int k = 0; k < 3; k++) kick(vh[k], vl[k], -h, g[k]);
-        }
-        if constexpr (STATE) {
-            if (A.state_out)
-                for (int k = 0; k < 3; k++) {
-                    A.state_out[k * n + i] = xh[k];
-                    A.state_out[(3 + k) * n + i] = xl[k];
-                    A.state_out[(6 + k) * n + i] = vh[k];
-                    A.state_out[(9 + k) * n + i] = vl[k];
-                }
-            if (nsteps == 0 && !resume) {  // no step taken: the initial conditions as given
-                for (int k = 0; k < 6; k++) w_out[k * n + i] = w0[k * n + i];
-                return;
-            }
-        }
-        // output velocity at the last step: v_{n+1/2} + g h / 2
-        for (int k = 0; k < 3; k++) kahan_add(vh[k], vl[k], g[k] * h * 0.5f);
+            for (int k = 0; k < 3; k++) kahan_add(o.vh[k], o.vl[k], -o.g[k] * h * 0.5f);
     } else {
-        // the coefficients times the step, once (shorter dependent chains per sub-step)
-        float ch[4], dh[4];
 #pragma unroll
         for (int s = 0; s < 4; s++) {
-            ch[s] = A.c[s] * h;
-            dh[s] = -A.d[s] * h;
+            o.ch[s] = A.c[s] * h;
+            o.dh[s] = -A.d[s] * h;
         }
-        for (int64_t j = 0; j < nsteps; j++) {
-            // sub-step 0 has d = 0: drift only
-            for (int k = 0; k < 3; k++) kahan_add(xh[k], xl[k], fmaf(vh[k], ch[0], vl[k] * ch[0]));
-#pragma unroll
-            for (int s = 1; s < 4; s++) {
-                potential_gradient_f<S>(pot, xh, g);
-                for (int k = 0; k < 3; k++) kick_drift(xh[k], xl[k], vh[k], vl[k], dh[s], g[k], ch[s]);
-            }
-        }
-        if constexpr (STATE) {
-            if (A.state_out)
-                for (int k = 0; k < 3; k++) {
-                    A.state_out[k * n + i] = xh[k];
-                    A.state_out[(3 + k) * n + i] = xl[k];
-                    A.state_out[(6 + k) * n + i] = vh[k];
-                    A.state_out[(9 + k) * n + i] = vl[k];
-                }
-            if (nsteps == 0 && !resume) {
-                for (int k = 0; k < 6; k++) w_out[k * n + i] = w0[k * n + i];
-                return;
-            }
-        }
-    }
-    for (int k = 0; k < 3; k++) {
-        w_out[k * n + i] = (double)xh[k] + (double)xl[k];
-        w_out[(3 + k) * n + i] = (double)vh[k] + (double)vl[k];
     }
 }
 
+// One Leapfrog step (c_leapfrog_step: drift, gradient, kick).
+template <typename S>
+__device__ __forceinline__ void lf_step(const DevPotF &pot, OrbitF &o) {
+    for (int k = 0; k < 3; k++) kahan_add(o.xh[k], o.xl[k], fmaf(o.vh[k], o.h, o.vl[k] * o.h));
+    potential_gradient_f<S>(pot, o.xh, o.g);
+    for (int k = 0; k < 3; k++) kick(o.vh[k], o.vl[k], -o.h, o.g[k]);
+}
+
+// One Ruth4 step: sub-step 0 has d = 0 (drift only); each later sub-step's kick
+// and drift are fused (kick_drift).  The step ends on a drift, so a resumed run
+// repeats the bits of an uninterrupted one.
+template <typename S>
+__device__ __forceinline__ void r4_step(const DevPotF &pot, OrbitF &o) {
+    for (int k = 0; k < 3; k++) kahan_add(o.xh[k], o.xl[k], fmaf(o.vh[k], o.ch[0], o.vl[k] * o.ch[0]));
+#pragma unroll
+    for (int s = 1; s < 4; s++) {
+        potential_gradient_f<S>(pot, o.xh, o.g);
+        for (int k = 0; k < 3; k++) kick_drift(o.xh[k], o.xl[k], o.vh[k], o.vl[k], o.dh[s], o.g[k], o.ch[s]);
+    }
+}
+
+// Finish an orbit: the state for a checkpoint (A.state_out, before the output
+// velocity is formed), the Leapfrog output velocity v_{n+1/2} + g h / 2 and the
+// FP64 final state hi + lo.
+template <bool STATE>
+__device__ __forceinline__ void orbit_end(const BatchArgs &A, const double *w0, int64_t n, int64_t i,
+                                          int64_t nsteps, int meth, OrbitF &o, double *w_out) {
+    if constexpr (STATE) {
+        if (A.state_out)
+            for (int k = 0; k < 3; k++) {
+                A.state_out[k * n + i] = o.xh[k];
+                A.state_out[(3 + k) * n + i] = o.xl[k];
+                A.state_out[(6 + k) * n + i] = o.vh[k];
+                A.state_out[(9 + k) * n + i] = o.vl[k];
+            }
+    }
+    if (nsteps == 0 && !(STATE && A.state_in != nullptr)) {  // no step taken: the initial conditions as given
+        for (int k = 0; k < 6; k++) w_out[k * n + i] = w0[k * n + i];
+        return;
+    }
+    if (meth == 0)
+        for (int k = 0; k < 3; k++) kahan_add(o.vh[k], o.vl[k], o.g[k] * o.h * 0.5f);
+    for (int k = 0; k < 3; k++) {
+        w_out[k * n + i] = (double)o.xh[k] + (double)o.xl[k];
+        w_out[(3 + k) * n + i] = (double)o.vh[k] + (double)o.vl[k];
+    }
+}
+
+__device__ __forceinline__ void swap_orbits(OrbitF &a, OrbitF &b, bool doit) {
+    float *pa = reinterpret_cast<float *>(&a), *pb = reinterpret_cast<float *>(&b);
+#pragma unroll
+    for (int k = 0; k < (int)(sizeof(OrbitF) / sizeof(float)); k++) {
+        const float x = pa[k], y = pb[k];
+        pa[k] = doit ? y : x;
+        pb[k] = doit ? x : y;
+    }
+}
+
+// Orbit ia, and orbit ib (>= 0, same integrator) in the same lane: both step
+// together, two independent dependent chains the scheduler interleaves, while
+// both have steps left; the longer one then finishes alone.  ib = -1 runs ia
+// alone.  Each orbit's arithmetic is the same either way (its result does not
+// depend on its partner).  With STATE, the integrator state is read from
+// A.state_in when given and written to A.state_out when given, so that a run
+// of k steps followed by a resumed run of n - k steps gives the bits of one run
+// of n steps.
+template <typename S, bool STATE>
+__device__ __forceinline__ void integrate_fp32(const DevPotF &pot, const BatchArgs &A, const double *w0,
+                                               const int64_t *nsteps, const double *dt, const int32_t *method,
+                                               int32_t ia, int32_t ib, double *w_out) {
+    const int64_t n = A.n;
+    const bool keep = STATE && (A.state_in != nullptr || A.state_out != nullptr);
+    int64_t na = nsteps[ia];
+    const int meth = method[ia];
+    if (ib < 0 && na == 0 && !keep) {
+        for (int k = 0; k < 6; k++) w_out[k * n + ia] = w0[k * n + ia];
+        return;
+    }
+    const int64_t nb = ib >= 0 ? nsteps[ib] : 0;
+    OrbitF a, b;
+    orbit_begin<S, STATE>(pot, A, w0, n, ia, na, (float)dt[ia], meth, a);
+    if (ib >= 0) orbit_begin<S, STATE>(pot, A, w0, n, ib, nb, (float)dt[ib], meth, b);
+    const int64_t common = ib >= 0 ? (na < nb ? na : nb) : 0;
+    if (meth == 0) {
+        for (int64_t j = 0; j < common; j++) {
+            lf_step<S>(pot, a);
+            lf_step<S>(pot, b);
+        }
+    } else {
+        for (int64_t j = 0; j < common; j++) {
+            r4_step<S>(pot, a);
+            r4_step<S>(pot, b);
+        }
+    }
+    // the remaining steps of the longer orbit, in a
+    int32_t ja = ia, jb = ib;
+    int64_t ma = na, mb = nb;
+    if (ib >= 0) {
+        const bool sw = nb > na;
+        swap_orbits(a, b, sw);
+        ja = sw ? ib : ia;
+        jb = sw ? ia : ib;
+        ma = sw ? nb : na;
+        mb = sw ? na : nb;
+    }
+    if (meth == 0)
+        for (int64_t j = common; j < ma; j++) lf_step<S>(pot, a);
+    else
+        for (int64_t j = common; j < ma; j++) r4_step<S>(pot, a);
+    orbit_end<STATE>(A, w0, n, ja, ma, meth, a, w_out);
+    if (ib >= 0) orbit_end<STATE>(A, w0, n, jb, mb, meth, b, w_out);
+}
+
+// Persistent grid over the queue of gx_queue.cuh: a lead block (32 of the
+// longest orbits, at most one per SM sub-partition) runs one orbit per lane, so
+// its dependent chains keep their latency; a main-region chunk runs its 32-orbit
+// blocks two at a time, lane l pairing orbit l of one block with orbit l of the
+// next (one integrator, similar cost), which doubles the independent work per
+// warp where throughput, not latency, decides.
 template <typename S, bool STATE>
 __global__ void __launch_bounds__(256) batch_fp32_kernel(const __grid_constant__ DevPotF pot, BatchArgs A,
                                                          const double *__restrict__ w0,
@@ -144,19 +221,38 @@ __global__ void __launch_bounds__(256) batch_fp32_kernel(const __grid_constant__
                                                          int32_t *__restrict__ counter, double *__restrict__ w_out) {
     const int lane = threadIdx.x & 31;
     const int64_t nchunks = A.slots / A.chunk;
+    const int subs = A.chunk / 32;
+    int phase = 0;
     for (;;) {
-        // a cancelled launch takes no further chunk (lane 0 decides for the warp)
-        int c = INT_MAX;
-        if (lane == 0 && !cancel_requested(A.cancel)) c = atomicAdd(counter, 1);
+        // a cancelled launch takes no further work (lane 0 decides for the warp)
+        int64_t c = -1;
+        int sub = -1;
+        if (lane == 0 && !cancel_requested(A.cancel)) c = queue_next(counter, nchunks, A.n_lead, subs, phase, sub);
         c = __shfl_sync(0xffffffffu, c, 0);
-        if (c >= nchunks) break;
-        for (int r = 0; r < A.chunk; r += 32) {
-            const int64_t slot = (int64_t)c * A.chunk + r + lane;
-            const int32_t i = order[slot];
+        sub = __shfl_sync(0xffffffffu, sub, 0);
+        if (c < 0) break;
+        // blocks [b0, b1) of chunk c, paired (b, b + 1) in the main region
+        const int b0 = sub >= 0 ? sub : 0, b1 = sub >= 0 ? sub + 1 : subs;
+        for (int b = b0; b < b1; b += 2) {
             // -1 pads the order; any other id outside [0, n) is skipped (and recorded in the debug build)
-            if (i != -1 && GX_DBG_CHECK(i >= 0 && i < A.n, DBG_ORDER, i, A.n)) {
-                integrate_one_fp32<S, STATE>(pot, A, w0, A.n, i, nsteps[i], (float)dt[i], method[i], w_out);
-                GX_DBG_DONE(i, nsteps[i]);
+            int32_t ia = order[c * A.chunk + 32 * b + lane];
+            int32_t ib = b + 1 < b1 ? order[c * A.chunk + 32 * (b + 1) + lane] : -1;
+            if (ia != -1 && !GX_DBG_CHECK(ia >= 0 && ia < A.n, DBG_ORDER, ia, A.n)) ia = -1;
+            if (ib != -1 && !GX_DBG_CHECK(ib >= 0 && ib < A.n, DBG_ORDER, ib, A.n)) ib = -1;
+            if (ia < 0) {
+                ia = ib;
+                ib = -1;
+            }
+            const bool pair = ib >= 0 && method[ia] == method[ib];
+            // at most two calls: (ia, ib) as a pair, or ia and then ib alone
+#pragma unroll 1
+            for (int pass = 0; pass < 2; pass++) {
+                const int32_t x = pass == 0 ? ia : (pair ? -1 : ib);
+                const int32_t y = pass == 0 && pair ? ib : -1;
+                if (x < 0) continue;
+                integrate_fp32<S, STATE>(pot, A, w0, nsteps, dt, method, x, y, w_out);
+                GX_DBG_DONE(x, nsteps[x]);
+                if (y >= 0) GX_DBG_DONE(y, nsteps[y]);
             }
         }
     }
@@ -200,11 +296,12 @@ int pack_potential_f32(const gx_potential *pot, DevPotF *out) {
         case GX_POT_TRIAXIALNFW:
             f.p[0] = (float)(p[0] * p[1] / (p[2] * p[2] * p[2]));
             f.p[1] = (float)(1.0 / p[2]);
-            if (c.type == GX_POT_FLATTENEDNFW) f.p[2] = (float)(1.0 / (p[5] * p[5]));
+            f.p[2] = (float)p[2];
+            if (c.type == GX_POT_FLATTENEDNFW) f.p[3] = (float)(1.0 / (p[5] * p[5]));
             if (c.type == GX_POT_TRIAXIALNFW) {
-                f.p[2] = (float)(1.0 / (p[3] * p[3]));
-                f.p[3] = (float)(1.0 / (p[4] * p[4]));
-                f.p[4] = (float)(1.0 / (p[5] * p[5]));
+                f.p[3] = (float)(1.0 / (p[3] * p[3]));
+                f.p[4] = (float)(1.0 / (p[4] * p[4]));
+                f.p[5] = (float)(1.0 / (p[5] * p[5]));
             }
             break;
         default:
@@ -268,6 +365,7 @@ static int batch_fp32_entry(const gx_potential *pot, const double *w0, int64_t n
     GX_CHECK_ARG(block >= 32 && block <= 256 && block % 32 == 0, "block must be a multiple of 32 in [32, 256]");
     GX_CHECK_ARG(grid >= 1, "grid must be >= 1");
     gx::BatchArgs A;
+    memset(&A, 0, sizeof(A));
     A.n = n;
     A.slots = n_slots;
     A.chunk = chunk;
@@ -283,8 +381,9 @@ static int batch_fp32_entry(const gx_potential *pot, const double *w0, int64_t n
         A.c[k] = (float)c[k];
         A.d[k] = (float)d[k];
     }
+    A.n_lead = gx::queue_lead_chunks(n_slots / chunk, chunk);
     cudaStream_t st = gx::as_stream(stream);
-    GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, sizeof(int32_t), st));
+    GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, GX_BATCH_QUEUE_WORDS * sizeof(int32_t), st));
     gx::launch_batch_fp32(dp, A, w0, n_steps, dt, method, order, queue_counter, w_out, grid, block, st);
     return gx::check_launch("batch_fp32");
 }
@@ -623,8 +722,8 @@ namespace gx {
 constexpr int NA_CHUNK = 32;
 constexpr int64_t NA_SLOTS = GX_NOALLOC_MAX_ORBITS + 2 * NA_CHUNK;   // >= gx_batch_schedule_slots(max, 32)
 constexpr int64_t NA_WORK = SB_HIST + SB_INFO + NA_SLOTS / NA_CHUNK + NA_SLOTS;
-// int32 layout: [0] queue counter | [64 .. 64 + NA_WORK) schedule work | order
-constexpr int64_t NA_WORK_OFF = 64;
+// int32 layout: [0, GX_BATCH_QUEUE_WORDS) queue | [NA_WORK_OFF, + NA_WORK) schedule work | order
+constexpr int64_t NA_WORK_OFF = ((GX_BATCH_QUEUE_WORDS + 63) / 64) * 64;
 constexpr int64_t NA_ORDER_OFF = ((NA_WORK_OFF + NA_WORK + 63) / 64) * 64;
 constexpr int64_t NA_WORDS = NA_ORDER_OFF + NA_SLOTS;
 
@@ -712,13 +811,15 @@ extern "C" int gx_batch_integrate_fp32_noalloc(const gx_potential *pot, const do
     const int64_t slots = gx_batch_schedule_slots(n, gx::NA_CHUNK);
     static_assert(gx::NA_SLOTS >= GX_NOALLOC_MAX_ORBITS + gx::NA_CHUNK, "order capacity");
     cudaStream_t st = gx::as_stream(stream);
-    GX_CUDA_TRY(cudaMemsetAsync(s, 0, sizeof(int32_t), st));  // queue counter
+    GX_CUDA_TRY(cudaMemsetAsync(s, 0, GX_BATCH_QUEUE_WORDS * sizeof(int32_t), st));  // queue
     rc = gx::launch_schedule(n_steps, method, n, gx::NA_CHUNK, s + gx::NA_ORDER_OFF, slots, slots,
                              s + gx::NA_WORK_OFF, st);
     if (rc) return rc;
     gx::BatchArgs A;
+    memset(&A, 0, sizeof(A));
     A.n = n;
     A.slots = slots;
+    A.n_lead = gx::queue_lead_chunks(slots / gx::NA_CHUNK, gx::NA_CHUNK);
     A.chunk = gx::NA_CHUNK;
     A.pad = 0;
     A.cancel = gx::cancel_flag();

@@ -25,7 +25,7 @@ __device__ __forceinline__ void body_consts_f32(const gx_body *b, BodyF &c) {
     case GX_POT_HERNQUIST: c.p[0] = (float)(G * m); c.p[1] = (float)p2; break;
     case GX_POT_PLUMMER: c.p[0] = (float)(G * m); c.p[1] = (float)(p2 * p2); break;
     case GX_POT_MIYAMOTONAGAI: c.p[0] = (float)(G * m); c.p[1] = (float)p2; c.p[2] = (float)(p3 * p3); break;
-    case GX_POT_SPHERICALNFW: c.p[0] = (float)(G * m / (p2 * p2 * p2)); c.p[1] = (float)(1.0 / p2); break;
+    case GX_POT_SPHERICALNFW: c.p[0] = (float)(G * m / (p2 * p2 * p2)); c.p[1] = (float)(1.0 / p2); c.p[2] = (float)p2; break;
     default: c.type = GX_POT_NULL; break;
     }
 }

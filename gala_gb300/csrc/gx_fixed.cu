@@ -8,6 +8,7 @@
 //   leapfrog  c_init_velocity / c_leapfrog_step (leapfrog.pyx:24-51,99-116)
 //   ruth4     c_ruth4_step with gala's coefficients (ruth4.pyx:24-35,65-78,98-108)
 #include "gx_host.h"
+#include "gx_queue.cuh"
 #include "gx_scf.cuh"
 
 namespace gx {
@@ -104,12 +105,12 @@ __global__ void __launch_bounds__(128, 1) ruth4_kernel(const __grid_constant__ D
 // Batched FP64 form of the same two integrators (the plain form of the batched
 // workload): per orbit its own n_steps, dt and integrator, final state only,
 // gala's arithmetic exactly as in the kernels above.  Same work queue as the
-// FP32 batch kernel (gx_batch.cu): chunks of the caller's order pulled from
-// one atomic counter by a persistent grid.
+// FP32 batch kernel (gx_batch.cu, gx_queue.cuh): chunks of the caller's order
+// pulled by a persistent grid.
 // ---------------------------------------------------------------------------
 template <bool SCF>
 __global__ void __launch_bounds__(128, 1) batch_fp64_kernel(const __grid_constant__ DevPot pot, Ruth4Coef co,
-                                                            int64_t n, int64_t slots, int32_t chunk,
+                                                            int64_t n, int64_t slots, int32_t chunk, int64_t n_lead,
                                                             const double *__restrict__ w0,
                                                             const int64_t *__restrict__ nsteps,
                                                             const double *__restrict__ dtv,
@@ -120,14 +121,20 @@ __global__ void __launch_bounds__(128, 1) batch_fp64_kernel(const __grid_constan
                                                             const int32_t *__restrict__ cancel) {
     const int lane = threadIdx.x & 31;
     const int64_t nchunks = slots / chunk;
+    const int subs = chunk / 32;
+    int phase = 0;
     for (;;) {
-        // a cancelled launch takes no further chunk (lane 0 decides for the warp)
-        int c = INT_MAX;
-        if (lane == 0 && !cancel_requested(cancel)) c = atomicAdd(counter, 1);
+        // a cancelled launch takes no further work (lane 0 decides for the warp)
+        int64_t c = -1;
+        int sub = -1;
+        if (lane == 0 && !cancel_requested(cancel)) c = queue_next(counter, nchunks, n_lead, subs, phase, sub);
         c = __shfl_sync(0xffffffffu, c, 0);
-        if (c >= nchunks) break;
-        for (int r = 0; r < chunk; r += 32) {
-            const int32_t i = order[(int64_t)c * chunk + r + lane];
+        sub = __shfl_sync(0xffffffffu, sub, 0);
+        if (c < 0) break;
+        // one lead block, or every block of a main-region chunk
+        const int b0 = sub >= 0 ? sub : 0, b1 = sub >= 0 ? sub + 1 : subs;
+        for (int b = b0; b < b1; b++) {
+            const int32_t i = order[c * chunk + 32 * b + lane];
             // -1 pads the order; any other id outside [0, n) is skipped (and recorded in the debug build)
             if (i == -1 || !GX_DBG_CHECK(i >= 0 && i < n, DBG_ORDER, i, n)) continue;
             GX_DBG_DONE(i, nsteps[i]);
@@ -226,13 +233,14 @@ int gx_batch_integrate_fp64(const gx_potential *pot, const double *w0, int64_t n
     co.d[2] = -two_13 / (2. - two_13);
     co.d[3] = 1. / (2. - two_13);
     cudaStream_t st = gx::as_stream(stream);
-    GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, sizeof(int32_t), st));
+    GX_CUDA_TRY(cudaMemsetAsync(queue_counter, 0, GX_BATCH_QUEUE_WORDS * sizeof(int32_t), st));
+    const int64_t n_lead = gx::queue_lead_chunks(n_slots / chunk, chunk);
     if (dp.has_scf)
-        gx::batch_fp64_kernel<true><<<grid, block, 0, st>>>(dp, co, n, n_slots, chunk, w0, n_steps, dt, method,
-                                                            order, queue_counter, w_out, gx::cancel_flag());
+        gx::batch_fp64_kernel<true><<<grid, block, 0, st>>>(dp, co, n, n_slots, chunk, n_lead, w0, n_steps, dt,
+                                                            method, order, queue_counter, w_out, gx::cancel_flag());
     else
-        gx::batch_fp64_kernel<false><<<grid, block, 0, st>>>(dp, co, n, n_slots, chunk, w0, n_steps, dt, method,
-                                                             order, queue_counter, w_out, gx::cancel_flag());
+        gx::batch_fp64_kernel<false><<<grid, block, 0, st>>>(dp, co, n, n_slots, chunk, n_lead, w0, n_steps, dt,
+                                                             method, order, queue_counter, w_out, gx::cancel_flag());
     return gx::check_launch("batch_fp64");
 }
 

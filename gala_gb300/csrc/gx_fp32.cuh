@@ -3,8 +3,8 @@
 // The closed-form potentials of gx_device.cuh, evaluated in FP32 on the
 // special-function unit: 1/sqrt, reciprocal and log2 are single approximate
 // MUFU instructions (relative error a few 1e-8), and the NFW radial factor
-// f(u) = ln(1+u) - u/(1+u) is computed without cancellation (for u < 1 as a
-// positive series in s = u/(2+u), see nfw_f_over_u3; for u >= 1 directly).
+// f(u)/u^3, f(u) = ln(1+u) - u/(1+u), is a polynomial on either side of u = 1
+// (nfw_fac) with no cancellation.
 // The integrators accumulate positions and velocities in compensated (Kahan)
 // form, so FP32 rounding of the state does not build up; the force error (a
 // few FP32 ulps) acts like a slightly perturbed potential.
@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/gala_gb300.h"
+#include "gx_nfw_poly.cuh"
 
 namespace gx {
 
@@ -53,38 +54,24 @@ __device__ __forceinline__ float lg2_approx(float x) {
     return r;
 }
 
-// f(u)/u^3 for the NFW force, u = r / r_s, without a branch: both forms below
-// are computed and the right one selected, so lanes on either side of u = 1 do
-// not run the two forms one after the other, and the dependent chain of one lane
-// holds no branch.  For u < 1, with s = u / (2 + u) (so ln(1 + u) = 2 atanh(s),
-// u / (1 + u) = 2 s / (1 + s), 1 - s = 2 / (2 + u)):
-//   f(u) / u^3 = (1 - s)^3 / 4 * [1 / (s (1 + s)) + P(s^2)],
-//   P(t) = sum_{k>=0} t^k / (2k + 3),
-// every term positive (no cancellation); s < 1/3, so six terms of P leave a
-// truncation below 2^-24 of the bracket.  For u >= 1 the direct form
-// (ln(1 + u) - u / (1 + u)) / u^3 has no harmful cancellation.  Both forms take
-// their reciprocals from two MUFU reciprocals that depend on u alone:
-// r = 1 / (2 + u), q = 1 / (u (1 + u)), with 1 / (s (1 + s)) = (2 + u)^2 q / 2,
-// (1 - s)^3 / 4 = 2 r^3, 1 / (1 + u) = u q and 1 / u = (1 + u) q.
-__device__ __forceinline__ float nfw_f_over_u3(float u) {
-    const float tu = 2.0f + u;
-    const float r = rcp_approx(tu);
-    const float q = rcp_approx(fmaf(u, u, u));
-    const float s = u * r;
-    const float t = s * s;
-    // P(t) in the form a + t^2 (b + t^2 c) (three dependent steps instead of five)
-    const float t2 = t * t;
-    const float pa = fmaf(1.0f / 5.0f, t, 1.0f / 3.0f);
-    const float pb = fmaf(1.0f / 9.0f, t, 1.0f / 7.0f);
-    const float pc = fmaf(1.0f / 13.0f, t, 1.0f / 11.0f);
-    const float P = fmaf(fmaf(pc, t2, pb), t2, pa);
-    const float br = fmaf(0.5f * tu * tu, q, P);
-    const float inner = 2.0f * r * r * r * br;
-    const float opu = 1.0f + u;
-    const float iu = opu * q;
-    const float f = fmaf(lg2_approx(opu), 0.69314718055994531f, -u * u * q);
-    const float outer = f * (iu * iu * iu);
-    return u < 1.0f ? inner : outer;
+// p0 f(u) / u^3 for the NFW force, f(u) = ln(1 + u) - u / (1 + u), u = s / r_s
+// for the (scaled) radius s, from s^2, 1/s, p0, 1/r_s and r_s.  Both forms below
+// are computed and the right one selected (lanes on either side of u = 1 do not
+// run two branches one after the other), and no special-function instruction
+// waits on another: log2(u^2) issues beside rsqrt(s^2), so the factor is one
+// MUFU latency and a depth-4 polynomial away from s^2.
+//   inside  (u < 1):  f / u^3 = H(u) / (2 u),       H(u) = 2 f(u) / u^2
+//   outside (u >= 1): f / u^3 = (ln u + K(w)) w^3,  K(w) = ln(1 + w) - 1 / (1 + w), w = 1 / u
+// H and K are degree-10 polynomials in 2u - 1 and 2w - 1 (gx_nfw_poly.cuh); the
+// only subtraction that cancels, ln u + K(w) at u ~ 1.3, loses under one bit.
+__device__ __forceinline__ float nfw_fac(float p0, float irs, float rs, float s2, float si) {
+    const float x = fmaf(s2, si * (2.0f * irs), -1.0f);   // 2u - 1
+    const float y = fmaf(si, 2.0f * rs, -1.0f);           // 2w - 1
+    const float lg = lg2_approx(s2 * (irs * irs));        // log2(u^2)
+    const float w = si * rs;
+    const float inner = nfw_poly_h(x) * (si * (0.5f * rs * p0));
+    const float outer = fmaf(lg, 0.34657359027997264f, nfw_poly_k(y)) * ((p0 * w) * (w * w));  // ln u = log2(u^2) ln2 / 2
+    return x < 1.0f ? inner : outer;
 }
 
 // Components whose force is fac(r) q (centred, spherical): Kepler, Hernquist,
@@ -104,8 +91,8 @@ __device__ __forceinline__ float comp_fac_t(const float *p, float r2, float ri) 
     } else if constexpr (T == GX_POT_PLUMMER) {  // p = {G m, b^2}
         const float rb = rsqrt_approx(r2 + p[1]);
         return (p[0] * rb) * (rb * rb);
-    } else {  // spherical NFW, p = {G m / r_s^3, 1 / r_s}
-        return p[0] * nfw_f_over_u3(r2 * ri * p[1]);
+    } else {  // spherical NFW, p = {G m / r_s^3, 1 / r_s, r_s}
+        return nfw_fac(p[0], p[1], p[2], r2, ri);
     }
 }
 
@@ -123,16 +110,14 @@ __device__ __forceinline__ void comp_vec_t(const float *p, const float *q, float
         const float ti = rsqrt_approx(fmaf(zd, zd, q[0] * q[0] + q[1] * q[1]));
         const float fac = (p[0] * ti) * (ti * ti);
         v[0] = fac * q[0]; v[1] = fac * q[1]; v[2] = fac * q[2] * fmaf(p[1], szi, 1.0f);
-    } else if constexpr (T == GX_POT_FLATTENEDNFW) {  // p = {G m / r_s^3, 1 / r_s, 1 / c^2}
-        const float r2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] * p[2];
-        const float u = r2 * rsqrt_approx(r2) * p[1];
-        const float fac = p[0] * nfw_f_over_u3(u);
-        v[0] = fac * q[0]; v[1] = fac * q[1]; v[2] = fac * q[2] * p[2];
-    } else if constexpr (T == GX_POT_TRIAXIALNFW) {  // p = {G m / r_s^3, 1 / r_s, 1/a^2, 1/b^2, 1/c^2}
-        const float r2 = q[0] * q[0] * p[2] + q[1] * q[1] * p[3] + q[2] * q[2] * p[4];
-        const float u = r2 * rsqrt_approx(r2) * p[1];
-        const float fac = p[0] * nfw_f_over_u3(u);
-        v[0] = fac * q[0] * p[2]; v[1] = fac * q[1] * p[3]; v[2] = fac * q[2] * p[4];
+    } else if constexpr (T == GX_POT_FLATTENEDNFW) {  // p = {G m / r_s^3, 1 / r_s, r_s, 1 / c^2}
+        const float s2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] * p[3];
+        const float fac = nfw_fac(p[0], p[1], p[2], s2, rsqrt_approx(s2));
+        v[0] = fac * q[0]; v[1] = fac * q[1]; v[2] = fac * q[2] * p[3];
+    } else if constexpr (T == GX_POT_TRIAXIALNFW) {  // p = {G m / r_s^3, 1 / r_s, r_s, 1/a^2, 1/b^2, 1/c^2}
+        const float s2 = q[0] * q[0] * p[3] + q[1] * q[1] * p[4] + q[2] * q[2] * p[5];
+        const float fac = nfw_fac(p[0], p[1], p[2], s2, rsqrt_approx(s2));
+        v[0] = fac * q[0] * p[3]; v[1] = fac * q[1] * p[4]; v[2] = fac * q[2] * p[5];
     } else {  // GX_POT_NULL
         v[0] = 0.f; v[1] = 0.f; v[2] = 0.f;
     }

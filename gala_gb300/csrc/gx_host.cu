@@ -5,6 +5,7 @@
 #include <vector>
 
 #include "gx_host.h"
+#include "gx_queue.cuh"
 #include "gx_scf.cuh"
 
 namespace gx {
@@ -234,6 +235,17 @@ static std::vector<DbgReader> &dbg_readers() {
     return r;
 }
 void dbg_register(DbgReader r) { dbg_readers().push_back(r); }
+
+// The lead region of the batched integrators' queue: at most one 32-orbit
+// block per SM sub-partition of the current device (four per multiprocessor),
+// in whole chunks.
+int64_t queue_lead_chunks(int64_t n_chunks, int32_t chunk) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        sms = 0;
+    const int64_t lead = 4 * (int64_t)sms / (chunk / 32);
+    return n_chunks < lead ? n_chunks : lead;
+}
 
 }  // namespace gx
 

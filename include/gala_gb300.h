@@ -30,13 +30,22 @@
 extern "C" {
 #endif
 
-#define GX_ABI_VERSION 2
+#define GX_ABI_VERSION 3
 
 /* Capacity of the by-value potential descriptor handed to every kernel.  A
  * potential with more components (gala's composites have no limit) is read by
  * the FP64 kernels from a component table in device memory instead
  * (gx_potential.table_device); the FP32 forms take at most GX_MAX_COMPONENTS. */
 #define GX_MAX_COMPONENTS 16
+/* Scratch of the batched integrators' work queue (gx_batch_integrate_fp32,
+ * _fp32_state, _fp64), in int32: two counters and one flag per SM
+ * sub-partition for up to 256 multiprocessors.  The order's first n_lead =
+ * min(n_chunks, 4 x multiprocessors / (chunk / 32)) chunks (the longest) go
+ * out in blocks of 32 orbits, at most one per sub-partition, before the rest in
+ * whole chunks.  After a run (also a cancelled one) the integrated orbits are
+ * the first min(q[1], n_lead x chunk / 32) blocks of 32 slots and the first
+ * min(q[0], n_chunks - n_lead) chunks after the lead region. */
+#define GX_BATCH_QUEUE_WORDS 1026
 #define GX_MAX_INLINE_PARAMS 128
 
 /* ------------------------------------------------------------------------- */
@@ -339,7 +348,8 @@ int gx_batch_schedule(const int64_t* n_steps, const int32_t* method, int64_t n, 
 /*   method   (N,) int32: 0 leapfrog, 1 ruth4                                 */
 /*   order    (n_slots,) int32 processing order: orbit indices, -1 = padding; */
 /*            n_slots is a multiple of `chunk`; each chunk is one queue item  */
-/*   queue_counter  DEVICE int32 scratch (zeroed by the call)                 */
+/*   queue_counter  DEVICE int32[GX_BATCH_QUEUE_WORDS] scratch (zeroed by    */
+/*                  the call)                                                 */
 /*   block, grid    launch shape of the persistent grid                       */
 /*   w_out    (6, N) float64 final states (t = n_steps * dt after the start)  */
 /* Closed-form components only (SCF -> GX_ERR_UNSUPPORTED).                   */

@@ -31,7 +31,7 @@ def test_library_loads_and_exports_every_declared_symbol():
     missing = [n for n in declared if not hasattr(lib, n)]
     assert not missing, missing
     assert set(_abi.SIGNATURES) >= declared, declared - set(_abi.SIGNATURES)
-    assert lib.gx_abi_version() == 2
+    assert lib.gx_abi_version() == 3
 
 
 def test_struct_layout_matches_header():

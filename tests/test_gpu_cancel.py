@@ -34,7 +34,7 @@ def test_flag_set_before_the_launch_takes_no_chunk(precision):
     with flag.installed():
         b.run()
     torch.cuda.synchronize()
-    assert int(b.counter.item()) == 0
+    assert b.chunks_taken() == 0
     assert not bool(b.completed().any())
     flag.clear()
     with flag.installed():  # a cleared flag changes nothing
@@ -77,7 +77,7 @@ def test_cancel_during_a_batch_run_stops_taking_chunks():
     torch.cuda.synchronize()
     t_part = e0.elapsed_time(e1)
     done = part.completed()
-    taken = int(part.counter.item())
+    taken = part.chunks_taken()
     n_chunks = n // cfg["chunk"]
     assert 0 < taken < n_chunks, (taken, n_chunks)
     assert t_part < 0.8 * t_full, (t_part, t_full)

@@ -74,7 +74,7 @@ F_HERNQUIST = 17
 # read once; the outputs are still in the 129 MB L2 when a launch ends):
 #   batch_fp32c  18,895,872 B for 262,144 orbits (full size)  profiles/batch_fp32_kernel_uneven.md
 #   dop853       1,700,864 B for 30,000 orbits                profiles/dop853_fp64_mw_composite.md
-TRAFFIC_PER_ORBIT = {"batch_fp32c": 18_895_872 / 262_144, "dop853": 1_700_864 / 30_000}
+TRAFFIC_PER_ORBIT = {"batch_fp32c": (18_925_568 + 256) / 262_144, "dop853": 1_700_864 / 30_000}
 
 
 def sig(x, n=4):
@@ -1240,7 +1240,7 @@ def run_gx(args):
         "roofline": {**{k: sig(v, 4) for k, v in f32["roofline"].items()},
                      "kernel": "batch_fp32_kernel, CUDA events",
                      "peak_source": "FP32 FMA-chain probe, same run",
-                     "work": "flops/step: Leapfrog 102, Ruth4 396"},
+                     "work": "flops/step: Leapfrog 102, Ruth4 306 (3 gradients)"},
         "clocks": clocks.summary(),
         "wall_s_timed_region": sig(head.get("wall_s_timed_region")),
         "variants": variants,

@@ -444,3 +444,30 @@ def test_rotating_frame_transform_matches_galas_rotation():
         psp.to_frame(fr)
     with pytest.raises(ValueError, match="current_frame"):
         g.PhaseSpacePosition(pos=[1.0, 2.0, 3.0], vel=[0.1, 0.2, 0.3]).to_frame(fr)
+
+
+def test_batch_queue_regions_taken():
+    """BatchIntegrator._taken_slots: the orbits a (possibly cancelled) run took
+    are the first q[1] 32-orbit blocks of the lead region (at most one block per
+    SM sub-partition, whole chunks) and the first q[0] chunks after it."""
+    import torch
+
+    from gala_gb300.batch import BatchIntegrator
+
+    b = object.__new__(BatchIntegrator)
+    b.sms = 152
+    b.config = {"chunk": 64}
+    b.order = torch.arange(64 * 1000, dtype=torch.int32)
+    b.counter = torch.zeros(1026, dtype=torch.int32)
+    n_lead = 4 * 152 // 2                      # 304 chunks = 608 blocks
+    b.counter[1] = 5                           # five lead blocks
+    b.counter[0] = 3                           # three main chunks
+    assert b._taken_slots() == [(0, 160), (n_lead * 64, (n_lead + 3) * 64)]
+    b.counter[1] = 10_000                      # every lead block (and the probes beyond)
+    b.counter[0] = 10_000
+    assert b._taken_slots() == [(0, n_lead * 64), (n_lead * 64, 1000 * 64)]
+    assert b.chunks_taken() == 1000
+    b.config = {"chunk": 32}
+    b.order = torch.arange(32 * 100, dtype=torch.int32)   # fewer chunks than the lead region
+    b.counter[1], b.counter[0] = 100, 1
+    assert b._taken_slots() == [(0, 3200), (3200, 3200)]

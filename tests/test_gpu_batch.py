@@ -191,6 +191,31 @@ def test_checkpoint_resume_is_bit_identical():
     assert torch.equal(c.energy_drift(), ref.energy_drift())
 
 
+def test_orbit_pairs_give_the_bits_of_single_orbits():
+    """Main-region chunks of 64 orbits run two orbits per lane; lead blocks and
+    32-orbit chunks run one.  Every orbit's bits are the same either way, also
+    with zero-step orbits among them and through a checkpoint and resume."""
+    import torch
+
+    n = 40_000  # more than the lead region (4 x SMs blocks of 32), so both regions run
+    pot = W.mw_composite()
+    w0 = W.mw_ics(n, seed=95)
+    nsteps, dt, method = _workload(n, 96, 300)
+    nsteps[::97] = 0
+    one = dict(block=128, ctas_per_sm=2, chunk=32)
+    two = dict(block=128, ctas_per_sm=2, chunk=64)
+    single = BatchIntegrator(pot, w0, nsteps, dt, method, config=one).run().clone()
+    paired = BatchIntegrator(pot, w0, nsteps, dt, method, config=two)
+    assert torch.equal(paired.run(), single)
+    assert bool(paired.completed().all())
+    k1 = nsteps // 2
+    a = BatchIntegrator(pot, w0, k1, dt, method, config=two, checkpoint=True)
+    a.run()
+    b = BatchIntegrator(pot, w0, nsteps - k1, dt, method, config=two, state=a.state)
+    torch.cuda.synchronize()
+    assert torch.equal(b.run(), single)
+
+
 def test_checkpoint_arguments():
     pot = W.mw_composite()
     w0 = W.mw_ics(64, seed=93)

@@ -362,7 +362,9 @@ int gx_batch_integrate_fp32(const gx_potential* pot, const double* w0, int64_t n
 
 /* The same with the integrator state in device memory, for checkpoints: a run
  * of k steps that writes its state, then a run of n - k steps that resumes from
- * it, gives the bits of one run of n steps (orbit by orbit).
+ * it, gives the bits of one run of n steps (orbit by orbit; for n = 0 the
+ * resumed run returns the state's value, hi + lo, where one run of no steps
+ * returns w0 itself).
  *   state_in   DEVICE float[12][N] or NULL: position hi (3), lo (3), velocity
  *              hi (3), lo (3) -- for Leapfrog the half-step velocity v_{1/2},
  *              which the resumed run uses as is (no second c_init_velocity);

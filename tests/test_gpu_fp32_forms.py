@@ -169,3 +169,22 @@ def test_fp32_dop853_result_independent_of_processing_order():
         assert torch.all(st == 1)
         outs.append(out.cpu().numpy())
     assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("name", ["kepler", "hernquist", "plummer", "miyamotonagai", "sphericalnfw",
+                                  "flattenednfw", "triaxialnfw", "shifted_rotated"])
+def test_fp32c_every_component_type(oracle, name):
+    """The FP32 force of every closed-form component type (the run-time
+    component loop, with the shift / rotation path): Ruth4 with FP32 forces
+    and compensated state against the FP64 oracle on near-circular orbits."""
+    from ._cases import potentials
+    from .test_gpu_parity import _near_circular_ics
+
+    pot = potentials()[name]
+    w0 = _near_circular_ics(oracle, pot, 64, seed=67)
+    t = g.parse_time_specification(dt=0.5, n_steps=500)
+    w = pot.integrate_orbit(w0, t=t, Integrator="ruth4",
+                            Integrator_kwargs=dict(precision="fp32c", out_stride=50)).w()
+    ref = oracle.fixed(pot, w0, t, "ruth4")[:, ::50]
+    err = rel_err(w[:3], ref[:3])
+    assert np.median(err) <= 1e-5 and np.max(err) <= 1e-4, (name, np.median(err), np.max(err))

@@ -4,10 +4,11 @@
 // Work queue: the caller supplies a processing order (a permutation of the
 // orbits, padded with -1 to whole chunks) in which each chunk holds orbits of
 // one integrator and similar cost, chunks sorted longest first.  A persistent
-// grid (a few CTAs per SM) pulls chunks from the counters of gx_queue.cuh (the
-// longest chunks one per SM sub-partition, then the rest in order); every warp
-// integrates `chunk` orbits, one per lane, 32 at a time.  Longest-first order
-// plus dynamic pulling keeps the SMs busy until the very end.
+// grid (a few CTAs per SM) pulls work from the counters of gx_queue.cuh: the
+// longest 32-orbit blocks one per SM sub-partition (one orbit per lane), then
+// the other chunks in order (two orbits per lane where a chunk holds 64 or
+// more).  Longest-first order plus dynamic pulling keeps the SMs busy until
+// the very end.
 //
 // Per orbit: positions and velocities are carried as FP32 (hi, lo) pairs with
 // Kahan-compensated updates; forces are evaluated in FP32 at hi (gx_fp32.cuh).
